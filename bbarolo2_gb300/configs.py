@@ -1,0 +1,61 @@
+"""Synthetic workloads of the model-evaluation path, with the shapes of the benchmark problems.
+
+There is no public dataset for these problems: each is a mock cube on a header of the stated size, with
+rings of the stated shape. Choices not fixed by the problem statements are made here once and documented:
+
+* ``classic64``  - 64x64 px x 64 channels, 10" pixels, 5 km/s channels centred on 1000 km/s (channel 32),
+  8 rings at 10-150" (step 20"), centre (32, 32), vrot 150 (1 - exp(-r/40")), vdisp 10, inc 55, pa 45, z0 0,
+  dens exp(-r/60"), CDENS 10, 30" circular beam.
+* ``global160``  - 160x160 px x 128 channels, 8" pixels, 4 km/s channels centred on 1000 km/s (channel 64),
+  40 rings at 8 + 16k" (k = 0..39), centre (79.5, 79.5), vrot 200 (2/pi) atan(r/60"), vdisp 12 -> 6 km/s
+  linearly, inc 65, pa 120, z0 10" with a sech2 layer (LTYPE 2), dens 0.8 exp(-r/160"), 30"x20" beam at
+  BPA 30.  The density peak below 0.95 keeps CDENS * DENS under 10 clouds per pixel, where the cloud count of
+  every sub-ring is the floor of 10 per pixel of ring area (``bbarolo/galmod.py:112-114``).
+* ``bayes256``   - 256x256 px x 192 channels, 4" pixels, 6 km/s channels, 20 rings at 8 + 16k", beam 4 px FWHM
+  (16"), truth drawn from the priors (vrot U(0,350), vdisp U(1,40), inc U(30,80), pa U(0,360)) with seed 7.
+"""
+
+import math
+
+import numpy as np
+
+from .cube import Cube, Params
+from .rings import Rings
+
+
+def classic64(galmodtype="MC", iseed=1):
+    par = Params(CDENS=10, ISEED=iseed, LTYPE=1, galmodtype=galmodtype)
+    cube = Cube.empty(64, 64, 64, [-10. / 3600., 10. / 3600., 5.], beam=30. / 3600., par=par,
+                      crpix=[33., 33., 33.], crval=[60., 0., 1000.], cunit=("deg", "deg", "km/s"))
+    r = np.arange(10., 151., 20.)
+    rings = Rings().setRings(radii=r, xpos=32., ypos=32., vsys=1000., vrot=150. * (1 - np.exp(-r / 40.)),
+                             vdisp=10., inc=55., phi=45., z0=0., dens=np.exp(-r / 60.))
+    return cube, rings
+
+
+def global160(galmodtype="MC", iseed=1):
+    par = Params(CDENS=10, ISEED=iseed, LTYPE=2, galmodtype=galmodtype)
+    cube = Cube.empty(160, 160, 128, [-8. / 3600., 8. / 3600., 4.], beam=[30. / 3600., 20. / 3600., 30.],
+                      par=par, crpix=[80.5, 80.5, 65.], crval=[60., 0., 1000.], cunit=("deg", "deg", "km/s"))
+    r = 8. + 16. * np.arange(40)
+    rings = Rings().setRings(radii=r, xpos=79.5, ypos=79.5, vsys=1000.,
+                             vrot=200. * (2 / math.pi) * np.arctan(r / 60.),
+                             vdisp=np.linspace(12., 6., r.size), inc=65., phi=120., z0=10.,
+                             dens=0.8 * np.exp(-r / 160.))
+    return cube, rings
+
+
+def bayes256(galmodtype="ANALYTIC", iseed=1, seed=7):
+    par = Params(CDENS=10, ISEED=iseed, LTYPE=1, galmodtype=galmodtype)
+    cube = Cube.empty(256, 256, 192, [-4. / 3600., 4. / 3600., 6.], beam=16. / 3600., par=par,
+                      crpix=[128.5, 128.5, 97.], crval=[60., 0., 1000.], cunit=("deg", "deg", "km/s"))
+    r = 8. + 16. * np.arange(20)
+    g = np.random.default_rng(seed)
+    rings = Rings().setRings(radii=r, xpos=127.5, ypos=127.5, vsys=1000.,
+                             vrot=g.uniform(0., 350., r.size), vdisp=g.uniform(1., 40., r.size),
+                             inc=g.uniform(30., 80.), phi=g.uniform(0., 360.), z0=0.,
+                             dens=np.exp(-r / 100.))
+    return cube, rings
+
+
+WORKLOADS = {"classic64": classic64, "global160": global160, "bayes256": bayes256}

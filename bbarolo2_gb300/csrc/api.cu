@@ -1,0 +1,817 @@
+// The C ABI of bbgpu (include/bbgpu.h): contexts, device memory, the cache of MC stream layouts, and the
+// batched likelihood pipeline.
+//
+// One context = one device, one CUDA stream, the constants of one cube (grid, beam kernel, data). Device
+// buffers grow with the largest batch seen and are reused. Errors are returned as status codes with a
+// message (bbgpu_last_error); nothing throws across the ABI.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/bbgpu.h"
+#include "kernels.h"
+
+#define BBGPU_VERSION 1
+#define NLAYOUT 4
+#define NTIMER 6
+
+static const char *KNAMES[NTIMER] = {"mc_bin", "scan_tiles", "mc_scatter", "mc_deposit", "conv_resid",
+                                     "reduce_partials"};
+
+struct LayoutEntry {
+    LayoutHost host;
+    LayoutDev dev;
+    bool valid = false;
+    long long last_use = 0;
+};
+
+struct bbgpu_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    bool grid_set = false, kernel_set = false, cube_set = false;
+    GridDev g{};
+    // constants
+    double *d_cd2i = nullptr;
+    float *d_cd2if = nullptr;
+    ZigDev *d_zig = nullptr;
+    float *d_taps = nullptr;
+    int ky = 0, kx = 0, kxw = 0;
+    // cube
+    float *d_data = nullptr;
+    uint8_t *d_mask = nullptr, *d_region = nullptr;
+    float *d_deff[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
+    // layouts
+    LayoutEntry layouts[NLAYOUT];
+    long long use_clock = 0;
+    LayoutEntry *cur = nullptr;
+    // batch
+    int nb = 0, nsub = 0, galmodtype = 0, tx = 8, ty = 8, ntile_total = 0, npart = 0;
+    bool uploaded = false, ran = false;
+    std::vector<MemberDev> mem_host;
+    SubMC *h_sub = nullptr;
+    size_t h_sub_cap = 0;
+    MemberDev *h_mem = nullptr;
+    size_t h_mem_cap = 0;
+    double *h_out2 = nullptr;
+    size_t h_out2_cap = 0;
+    int *h_err = nullptr;
+    SubMC *d_sub = nullptr;
+    size_t d_sub_cap = 0;
+    MemberDev *d_mem = nullptr;
+    size_t d_mem_cap = 0;
+    int *d_pix = nullptr;
+    size_t d_pix_cap = 0;
+    int *d_bucket = nullptr;
+    size_t d_bucket_cap = 0;
+    int *d_tcount = nullptr, *d_toff = nullptr, *d_tcur = nullptr;
+    size_t d_tcount_cap = 0, d_toff_cap = 0, d_tcur_cap = 0;
+    float *d_model = nullptr;
+    size_t d_model_cap = 0;
+    float *d_smooth = nullptr;
+    size_t d_smooth_cap = 0;
+    double *d_model64 = nullptr;
+    size_t d_model64_cap = 0;
+    double *d_partial = nullptr;
+    size_t d_partial_cap = 0;
+    double *d_out2 = nullptr;
+    size_t d_out2_cap = 0;
+    int *d_err = nullptr;
+    long long mstride = 0;
+    // options
+    bool keep_smoothed = false, timing = false, want64 = false;
+    long long launches = 0;
+    long long h2d = 0, d2h = 0;
+    cudaEvent_t ev[NTIMER + 1] = {};
+    double times[NTIMER] = {};
+};
+
+// ------------------------------------------------------------------------------------------- helpers
+static int fail(bbgpu_ctx *c, int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+
+#define CK(call)                                                                                           \
+    do {                                                                                                   \
+        cudaError_t e_ = (call);                                                                           \
+        if (e_ != cudaSuccess) return fail(ctx, BBGPU_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+#define CKL()                                                                                               \
+    do {                                                                                                    \
+        cudaError_t e_ = cudaGetLastError();                                                                \
+        if (e_ != cudaSuccess) return fail(ctx, BBGPU_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(e_)); \
+        ctx->launches++;                                                                                    \
+    } while (0)
+
+template <class T>
+static int dgrow(bbgpu_ctx *ctx, T **p, size_t *cap, size_t n) {
+    if (n <= *cap && *p) return 0;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    size_t m = n + n / 4 + 16;
+    if (cudaMalloc((void **)p, m * sizeof(T)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, BBGPU_ERR_NOMEM, "device allocation of %zu bytes failed", m * sizeof(T));
+    }
+    *cap = m;
+    return 0;
+}
+
+template <class T>
+static int hgrow(bbgpu_ctx *ctx, T **p, size_t *cap, size_t n) {
+    if (n <= *cap && *p) return 0;
+    if (*p) cudaFreeHost(*p);
+    *p = nullptr;
+    *cap = 0;
+    size_t m = n + n / 4 + 16;
+    if (cudaMallocHost((void **)p, m * sizeof(T)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, BBGPU_ERR_NOMEM, "pinned allocation of %zu bytes failed", m * sizeof(T));
+    }
+    *cap = m;
+    return 0;
+}
+
+static void layout_dev_free(LayoutDev &d) {
+    cudaFree(d.cf); cudaFree(d.cd); cudaFree(d.sub); cudaFree(d.slow_base); cudaFree(d.hz); cudaFree(d.slow_val);
+    cudaFree(d.sub_base); cudaFree(d.cloud_base);
+    memset(&d, 0, sizeof d);
+}
+
+static int upload_layout(bbgpu_ctx *ctx, LayoutEntry &E) {
+    LayoutHost &H = E.host;
+    LayoutDev &D = E.dev;
+    memset(&D, 0, sizeof D);
+    D.ncloud = H.ncloud;
+    D.nsub = H.nsub;
+    D.nsubcloud = H.nsubcloud;
+    D.nslow = H.nslow;
+    size_t nc = (size_t)(H.ncloud ? H.ncloud : 1);
+    std::vector<float4> cf(nc);
+    std::vector<double> cd(4 * nc);
+    for (int c = 0; c < H.ncloud; c++) {
+        cf[c] = make_float4((float)H.R[c], (float)H.caz[c], (float)H.saz[c], (float)H.fdev[c]);
+        cd[4 * c] = H.R[c];
+        cd[4 * c + 1] = H.caz[c];
+        cd[4 * c + 2] = H.saz[c];
+        cd[4 * c + 3] = H.fdev[c];
+    }
+    CK(cudaMalloc(&D.cf, nc * sizeof(float4)));
+    CK(cudaMalloc(&D.cd, 4 * nc * sizeof(double)));
+    CK(cudaMalloc(&D.sub, nc * sizeof(int)));
+    CK(cudaMalloc(&D.slow_base, nc * sizeof(int)));
+    CK(cudaMalloc(&D.hz, (size_t)(H.nsubcloud ? H.nsubcloud : 1) * sizeof(int32_t)));
+    CK(cudaMalloc(&D.slow_val, (size_t)(H.nslow ? H.nslow : 1) * sizeof(double)));
+    CK(cudaMalloc(&D.sub_base, (size_t)(H.nsub ? H.nsub : 1) * sizeof(long long)));
+    CK(cudaMalloc(&D.cloud_base, (size_t)(H.nsub ? H.nsub : 1) * sizeof(int)));
+    CK(cudaMemcpy(D.cf, cf.data(), nc * sizeof(float4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(D.cd, cd.data(), 4 * nc * sizeof(double), cudaMemcpyHostToDevice));
+    if (H.ncloud) {
+        CK(cudaMemcpy(D.sub, H.sub, (size_t)H.ncloud * sizeof(int), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(D.slow_base, H.slow_base, (size_t)H.ncloud * sizeof(int), cudaMemcpyHostToDevice));
+    }
+    if (H.nsubcloud) CK(cudaMemcpy(D.hz, H.hz, (size_t)H.nsubcloud * sizeof(int32_t), cudaMemcpyHostToDevice));
+    if (H.nslow) CK(cudaMemcpy(D.slow_val, H.slow_val, (size_t)H.nslow * sizeof(double), cudaMemcpyHostToDevice));
+    if (H.nsub) {
+        CK(cudaMemcpy(D.sub_base, H.sub_base, (size_t)H.nsub * sizeof(long long), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(D.cloud_base, H.cloud_base, (size_t)H.nsub * sizeof(int), cudaMemcpyHostToDevice));
+    }
+    return 0;
+}
+
+// The layout of (seed, ltype, nc, nv, R0): cached (NLAYOUT most recent), parsed on the host on a miss.
+static int get_layout(bbgpu_ctx *ctx, uint64_t seed, int nsub, const int *nc, const int *nv, const double *R0,
+                      LayoutEntry **out) {
+    uint64_t key = bbh_layout_key(seed, ctx->g.ltype, nsub, nc, nv, R0, ctx->g.radsep);
+    LayoutEntry *victim = &ctx->layouts[0];
+    for (auto &E : ctx->layouts) {
+        if (E.valid && E.host.key == key && E.host.nsub == nsub && memcmp(E.host.nc, nc, sizeof(int) * nsub) == 0 &&
+            memcmp(E.host.nv, nv, sizeof(int) * nsub) == 0) {
+            E.last_use = ++ctx->use_clock;
+            *out = &E;
+            return 0;
+        }
+        if (!E.valid || E.last_use < victim->last_use) victim = &E;
+    }
+    if (victim->valid) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        layout_dev_free(victim->dev);
+        bbh_layout_free(&victim->host);
+        victim->valid = false;
+    }
+    if (bbh_layout_build(&victim->host, seed, ctx->g.ltype, nsub, nc, nv, R0, ctx->g.radsep) != 0)
+        return fail(ctx, BBGPU_ERR_NOMEM, "MC layout: too many clouds or host allocation failed");
+    int rc = upload_layout(ctx, *victim);
+    if (rc) return rc;
+    victim->valid = true;
+    victim->last_use = ++ctx->use_clock;
+    *out = victim;
+    return 0;
+}
+
+static int ensure_deff(bbgpu_ctx *ctx, int maskmode, int use_region) {
+    if (maskmode < 0 || maskmode > 2) return fail(ctx, BBGPU_ERR_ARG, "maskmode must be 0, 1 or 2");
+    if (use_region && !ctx->d_region) return fail(ctx, BBGPU_ERR_ARG, "use_region without a region");
+    float *&d = ctx->d_deff[maskmode][use_region ? 1 : 0];
+    if (d) return 0;
+    size_t n = (size_t)ctx->g.nx * ctx->g.ny * ctx->g.nz;
+    CK(cudaMalloc(&d, n * sizeof(float)));
+    launch_prep_deff(ctx->stream, ctx->d_data, ctx->d_mask, use_region ? ctx->d_region : nullptr, maskmode, ctx->g.nz,
+                     ctx->g.ny, ctx->g.nx, d);
+    CKL();
+    return 0;
+}
+
+// ------------------------------------------------------------------------------------------- context
+extern "C" int bbgpu_version(void) { return BBGPU_VERSION; }
+
+extern "C" int bbgpu_ctx_create(bbgpu_ctx **out, int device) {
+    bbgpu_ctx *ctx = nullptr;
+    if (!out) return BBGPU_ERR_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return BBGPU_ERR_CUDA;
+    }
+    if (device < 0 || device >= n) return BBGPU_ERR_ARG;
+    ctx = new (std::nothrow) bbgpu_ctx();
+    if (!ctx) return BBGPU_ERR_NOMEM;
+    ctx->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete ctx;
+        return BBGPU_ERR_CUDA;
+    }
+    // ziggurat tables (fast-path bound kn fits 32 bits)
+    ZigDev z;
+    int64_t kn[128];
+    double wn[128], fn[128];
+    bbh_zig_tables(kn, wn, fn);
+    for (int i = 0; i < 128; i++) {
+        z.kn[i] = (unsigned)kn[i];
+        z.wnf[i] = (float)wn[i];
+        z.wn[i] = wn[i];
+    }
+    if (cudaMalloc(&ctx->d_zig, sizeof z) != cudaSuccess || cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess ||
+        cudaMemcpy(ctx->d_zig, &z, sizeof z, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(ctx->d_err, 0, sizeof(int)) != cudaSuccess ||
+        cudaMallocHost(&ctx->h_err, sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        bbgpu_ctx_destroy(ctx);
+        return BBGPU_ERR_CUDA;
+    }
+    for (int i = 0; i <= NTIMER; i++) cudaEventCreate(&ctx->ev[i]);
+    *out = ctx;
+    return BBGPU_OK;
+}
+
+extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
+    if (!ctx) return BBGPU_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (auto &E : ctx->layouts)
+        if (E.valid) {
+            layout_dev_free(E.dev);
+            bbh_layout_free(&E.host);
+        }
+    cudaFree(ctx->d_cd2i); cudaFree(ctx->d_cd2if); cudaFree(ctx->d_zig); cudaFree(ctx->d_taps);
+    cudaFree(ctx->d_data); cudaFree(ctx->d_mask); cudaFree(ctx->d_region);
+    for (auto &a : ctx->d_deff)
+        for (auto &b : a) cudaFree(b);
+    cudaFree(ctx->d_sub); cudaFree(ctx->d_mem); cudaFree(ctx->d_pix); cudaFree(ctx->d_bucket);
+    cudaFree(ctx->d_tcount); cudaFree(ctx->d_toff); cudaFree(ctx->d_tcur); cudaFree(ctx->d_model);
+    cudaFree(ctx->d_smooth); cudaFree(ctx->d_model64); cudaFree(ctx->d_partial); cudaFree(ctx->d_out2);
+    cudaFree(ctx->d_err);
+    cudaFreeHost(ctx->h_sub); cudaFreeHost(ctx->h_mem); cudaFreeHost(ctx->h_out2); cudaFreeHost(ctx->h_err);
+    for (int i = 0; i <= NTIMER; i++)
+        if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    cudaGetLastError();
+    delete ctx;
+    return BBGPU_OK;
+}
+
+extern "C" const char *bbgpu_last_error(const bbgpu_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+extern "C" int bbgpu_sync(bbgpu_ctx *ctx) {
+    if (!ctx) return BBGPU_ERR_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return BBGPU_OK;
+}
+
+extern "C" int64_t bbgpu_launch_count(const bbgpu_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+extern "C" int bbgpu_last_run_times(const bbgpu_ctx *ctx, double *times, int n) {
+    if (!ctx || !times) return BBGPU_ERR_ARG;
+    for (int i = 0; i < n && i < NTIMER; i++) times[i] = ctx->times[i];
+    return NTIMER;
+}
+
+extern "C" const char *bbgpu_kernel_name(int i) { return (i >= 0 && i < NTIMER) ? KNAMES[i] : ""; }
+
+extern "C" int bbgpu_transfer_bytes(const bbgpu_ctx *ctx, int64_t *h2d, int64_t *d2h) {
+    if (!ctx) return BBGPU_ERR_ARG;
+    if (h2d) *h2d = ctx->h2d;
+    if (d2h) *d2h = ctx->d2h;
+    return BBGPU_OK;
+}
+
+extern "C" int bbgpu_set_option(bbgpu_ctx *ctx, int opt, int value) {
+    if (!ctx) return BBGPU_ERR_ARG;
+    switch (opt) {
+        case 1: ctx->keep_smoothed = value != 0; break;
+        case 2: ctx->timing = value != 0; break;
+        default: return fail(ctx, BBGPU_ERR_ARG, "unknown option %d", opt);
+    }
+    return BBGPU_OK;
+}
+
+// ------------------------------------------------------------------------------------------- set-up
+extern "C" int bbgpu_set_grid(bbgpu_ctx *ctx, const bbgpu_grid *gr, const double *cd2i, const double *lfreq0,
+                              const double *relint, const double *vedges) {
+    (void)vedges;
+    if (!ctx || !gr || !cd2i || !lfreq0 || !relint) return fail(ctx, BBGPU_ERR_ARG, "set_grid: null argument");
+    if (gr->nx <= 0 || gr->ny <= 0 || gr->nz <= 0) return fail(ctx, BBGPU_ERR_ARG, "set_grid: empty cube");
+    if (gr->nlines < 1 || gr->nlines > BBGPU_MAXL)
+        return fail(ctx, BBGPU_ERR_ARG, "set_grid: %d lines (1 to %d supported)", gr->nlines, BBGPU_MAXL);
+    if (!(gr->cdelt3 != 0) || !(gr->pixarea > 0) || !(gr->radsep > 0))
+        return fail(ctx, BBGPU_ERR_ARG, "set_grid: invalid cdelt3, pixarea or radsep");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    GridDev &g = ctx->g;
+    memset(&g, 0, sizeof g);
+    g.nx = gr->nx; g.ny = gr->ny; g.nz = gr->nz; g.nlines = gr->nlines;
+    g.axtyp = gr->axtyp; g.velsys = gr->velsys; g.ltype = gr->ltype; g.cmode = gr->cmode;
+    g.radsep = gr->radsep; g.cdens = gr->cdens; g.pixarea = gr->pixarea; g.cdelt0 = gr->cdelt0; g.cdelt1 = gr->cdelt1;
+    g.crota2 = gr->crota2; g.sig_instr = gr->sig_instr; g.crval3 = gr->crval3; g.cdelt3 = gr->cdelt3;
+    g.crpix3 = gr->crpix3; g.chwidth = gr->chwidth; g.zstep = gr->zstep; g.scalefactor = gr->scalefactor;
+    // bbarolo/galmod.py:103-105: the linear channel map of a velocity axis
+    g.ia = 1.0 / g.cdelt3;
+    g.ib = -g.crval3 / g.cdelt3 + g.crpix3 - 1;
+    for (int nl = 0; nl < g.nlines; nl++) {
+        g.lfreq0[nl] = lfreq0[nl];
+        g.relint[nl] = relint[nl];
+        if (g.axtyp == 4) {
+            g.lia[nl] = (float)g.ia;
+            g.lib[nl] = (float)g.ib;
+        } else {
+            // radio velocities on a frequency axis: channel = v (-f0 / (c cdelt3)) + (f0 - crval3) / cdelt3 + crpix3 - 1
+            g.lia[nl] = (float)(-lfreq0[nl] / (2.99792458e08 * g.cdelt3));
+            g.lib[nl] = (float)((lfreq0[nl] - g.crval3) / g.cdelt3 + g.crpix3 - 1);
+        }
+    }
+    g.fast_ok = (g.axtyp == 4 && g.nlines == 1) || (g.axtyp == 3 && g.velsys == 1);
+    std::vector<float> cf(g.nz);
+    for (int i = 0; i < g.nz; i++) cf[i] = (float)cd2i[i];
+    cudaFree(ctx->d_cd2i);
+    cudaFree(ctx->d_cd2if);
+    ctx->d_cd2i = nullptr;
+    ctx->d_cd2if = nullptr;
+    CK(cudaMalloc(&ctx->d_cd2i, g.nz * sizeof(double)));
+    CK(cudaMalloc(&ctx->d_cd2if, g.nz * sizeof(float)));
+    CK(cudaMemcpy(ctx->d_cd2i, cd2i, g.nz * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_cd2if, cf.data(), g.nz * sizeof(float), cudaMemcpyHostToDevice));
+    // deposit tile: pixels x channels of 8-byte sums within 64 KB
+    int tp = 65536 / (8 * g.nz);
+    if (tp >= 64) { ctx->tx = 8; ctx->ty = 8; }
+    else if (tp >= 32) { ctx->tx = 8; ctx->ty = 4; }
+    else if (tp >= 16) { ctx->tx = 4; ctx->ty = 4; }
+    else if (tp >= 8) { ctx->tx = 4; ctx->ty = 2; }
+    else if (tp >= 2) { ctx->tx = 2; ctx->ty = 1; }
+    else { ctx->tx = 1; ctx->ty = 1; }
+    for (auto &E : ctx->layouts)
+        if (E.valid) {
+            layout_dev_free(E.dev);
+            bbh_layout_free(&E.host);
+            E.valid = false;
+        }
+    ctx->grid_set = true;
+    ctx->uploaded = ctx->ran = false;
+    return BBGPU_OK;
+}
+
+extern "C" int bbgpu_set_kernel(bbgpu_ctx *ctx, const double *kernel, int ky, int kx) {
+    if (!ctx) return BBGPU_ERR_ARG;
+    if (!kernel || ky < 1 || kx < 1 || !(ky & 1) || !(kx & 1) || ky > BBGPU_MAXK || kx > BBGPU_MAXK)
+        return fail(ctx, BBGPU_ERR_ARG, "set_kernel: kernel sides must be odd, 1 to %d", BBGPU_MAXK);
+    std::vector<float> taps((size_t)ky * 31);
+    int kxw = conv_taps(kernel, ky, kx, taps.data());
+    if (!kxw) return fail(ctx, BBGPU_ERR_ARG, "set_kernel: kernel width %d above 31", kx);
+    size_t smem = (size_t)(16 + ky - 1) * (16 + kxw - 1) * 32 * 4 + (size_t)ky * kxw * 4;
+    if (smem > 220 * 1024) return fail(ctx, BBGPU_ERR_ARG, "set_kernel: kernel %dx%d too large", ky, kx);
+    CK(cudaSetDevice(ctx->device));
+    cudaFree(ctx->d_taps);
+    ctx->d_taps = nullptr;
+    CK(cudaMalloc(&ctx->d_taps, (size_t)ky * kxw * sizeof(float)));
+    CK(cudaMemcpy(ctx->d_taps, taps.data(), (size_t)ky * kxw * sizeof(float), cudaMemcpyHostToDevice));
+    ctx->ky = ky;
+    ctx->kx = kx;
+    ctx->kxw = kxw;
+    ctx->kernel_set = true;
+    return BBGPU_OK;
+}
+
+extern "C" int bbgpu_set_cube(bbgpu_ctx *ctx, const float *data, const uint8_t *mask, const uint8_t *region) {
+    if (!ctx) return BBGPU_ERR_ARG;
+    if (!ctx->grid_set) return fail(ctx, BBGPU_ERR_STATE, "set_cube before set_grid");
+    if (!data) return fail(ctx, BBGPU_ERR_ARG, "set_cube: null data");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    size_t n = (size_t)ctx->g.nx * ctx->g.ny * ctx->g.nz;
+    cudaFree(ctx->d_data); cudaFree(ctx->d_mask); cudaFree(ctx->d_region);
+    ctx->d_data = nullptr; ctx->d_mask = nullptr; ctx->d_region = nullptr;
+    for (auto &a : ctx->d_deff)
+        for (auto &b : a) { cudaFree(b); b = nullptr; }
+    CK(cudaMalloc(&ctx->d_data, n * sizeof(float)));
+    CK(cudaMemcpy(ctx->d_data, data, n * sizeof(float), cudaMemcpyHostToDevice));
+    if (mask) {
+        CK(cudaMalloc(&ctx->d_mask, n));
+        CK(cudaMemcpy(ctx->d_mask, mask, n, cudaMemcpyHostToDevice));
+    }
+    if (region) {
+        CK(cudaMalloc(&ctx->d_region, (size_t)ctx->g.nx * ctx->g.ny));
+        CK(cudaMemcpy(ctx->d_region, region, (size_t)ctx->g.nx * ctx->g.ny, cudaMemcpyHostToDevice));
+    }
+    ctx->cube_set = true;
+    return BBGPU_OK;
+}
+
+// ------------------------------------------------------------------------------------------- batches
+static int batch_prepare(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const double *sr, const int64_t *nv,
+                         const bbgpu_eval_desc *descs, bool need_cube) {
+    if (!ctx->grid_set) return fail(ctx, BBGPU_ERR_STATE, "evaluation before set_grid");
+    if (need_cube && !ctx->cube_set) return fail(ctx, BBGPU_ERR_STATE, "evaluation before set_cube");
+    if (galmodtype != BBGPU_MC) return fail(ctx, BBGPU_ERR_ARG, "galmodtype %d not supported by the batch path", galmodtype);
+    if (nb < 1 || nsub < 0 || !sr || !nv || !descs) return fail(ctx, BBGPU_ERR_ARG, "eval: invalid batch");
+    const GridDev &g = ctx->g;
+    std::vector<int> nc0(nsub), nv0(nsub), nc(nsub), nvv(nsub);
+    std::vector<double> R0(nsub);
+    for (int i = 0; i < nsub; i++) R0[i] = sr[i];
+    bbh_cloud_counts(sr, nsub, nv, &g, nc0.data(), nv0.data());
+    uint64_t seed = descs[0].seed;
+    for (int k = 1; k < nb; k++) {
+        const double *s = sr + (size_t)k * BBGPU_NSR * nsub;
+        bbh_cloud_counts(s, nsub, nv + (size_t)k * nsub, &g, nc.data(), nvv.data());
+        if (descs[k].seed != seed || memcmp(nc.data(), nc0.data(), sizeof(int) * nsub) ||
+            memcmp(nvv.data(), nv0.data(), sizeof(int) * nsub) || memcmp(s, sr, sizeof(double) * nsub))
+            return fail(ctx, BBGPU_ERR_ARG,
+                        "eval: member %d has another cloud layout (seed, radii, cloud or velocity counts): "
+                        "evaluate it in another batch", k);
+    }
+    LayoutEntry *E = nullptr;
+    int rc = get_layout(ctx, seed, nsub, nc0.data(), nv0.data(), R0.data(), &E);
+    if (rc) return rc;
+    ctx->cur = E;
+    if ((rc = hgrow(ctx, &ctx->h_sub, &ctx->h_sub_cap, (size_t)nb * (nsub ? nsub : 1)))) return rc;
+    if ((rc = hgrow(ctx, &ctx->h_mem, &ctx->h_mem_cap, (size_t)nb))) return rc;
+    ctx->mem_host.resize(nb);
+    int toff = 0;
+    for (int k = 0; k < nb; k++) {
+        const bbgpu_eval_desc &d = descs[k];
+        if (d.blo0 < 0 || d.blo1 < 0 || d.bhi0 > g.nx || d.bhi1 > g.ny || d.bhi0 < d.blo0 || d.bhi1 < d.blo1)
+            return fail(ctx, BBGPU_ERR_ARG, "eval: member %d: box outside the cube", k);
+        SubMC *S = ctx->h_sub + (size_t)k * nsub;
+        int e = bbh_submc(sr + (size_t)k * BBGPU_NSR * nsub, nsub, nc0.data(), nv0.data(), &g, S);
+        MemberDev &M = ctx->mem_host[k];
+        memset(&M, 0, sizeof M);
+        M.blo0 = d.blo0; M.blo1 = d.blo1; M.bhi0 = d.bhi0; M.bhi1 = d.bhi1;
+        M.bx = d.bhi0 - d.blo0; M.by = d.bhi1 - d.blo1;
+        M.ntx = (M.bx + ctx->tx - 1) / ctx->tx;
+        M.nty = (M.by + ctx->ty - 1) / ctx->ty;
+        M.tile_off = toff;
+        toff += M.ntx * M.nty;
+        M.fix_exp = e;
+        M.maskmode = d.maskmode;
+        M.use_region = d.use_region;
+        M.sigma2 = d.sigma2;
+        M.eps2 = d.eps2;
+        M.sigma2f = (float)d.sigma2;
+        M.eps2f = (float)d.eps2;
+        if (d.eps2 > 0 && !(d.sigma2 > 0)) return fail(ctx, BBGPU_ERR_ARG, "eval: member %d: eps2 > 0 needs sigma2 > 0", k);
+        if (need_cube) {
+            if ((rc = ensure_deff(ctx, d.maskmode, d.use_region))) return rc;
+            M.deff = ctx->d_deff[d.maskmode][d.use_region ? 1 : 0];
+        }
+        ctx->h_mem[k] = M;
+    }
+    ctx->nb = nb;
+    ctx->nsub = nsub;
+    ctx->galmodtype = galmodtype;
+    ctx->ntile_total = toff;
+    ctx->mstride = (long long)g.nx * g.ny * g.nz;
+    ctx->npart = conv_resid_npart(ctx->mem_host.data(), nb, g.nz);
+    size_t ncl = (size_t)nb * (E->host.ncloud ? E->host.ncloud : 1);
+    if ((rc = dgrow(ctx, &ctx->d_sub, &ctx->d_sub_cap, (size_t)nb * (nsub ? nsub : 1)))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_mem, &ctx->d_mem_cap, (size_t)nb))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_pix, &ctx->d_pix_cap, ncl))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_bucket, &ctx->d_bucket_cap, ncl))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_tcount, &ctx->d_tcount_cap, (size_t)toff + 1))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_toff, &ctx->d_toff_cap, (size_t)toff + 1))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_tcur, &ctx->d_tcur_cap, (size_t)toff + 1))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_model, &ctx->d_model_cap, (size_t)nb * ctx->mstride))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_partial, &ctx->d_partial_cap, (size_t)2 * nb * (ctx->npart ? ctx->npart : 1)))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_out2, &ctx->d_out2_cap, (size_t)2 * nb))) return rc;
+    if ((rc = hgrow(ctx, &ctx->h_out2, &ctx->h_out2_cap, (size_t)2 * nb))) return rc;
+    if (ctx->keep_smoothed)
+        if ((rc = dgrow(ctx, &ctx->d_smooth, &ctx->d_smooth_cap, (size_t)nb * ctx->mstride))) return rc;
+    if (ctx->want64)
+        if ((rc = dgrow(ctx, &ctx->d_model64, &ctx->d_model64_cap, (size_t)nb * ctx->mstride))) return rc;
+    CK(cudaMemcpyAsync(ctx->d_sub, ctx->h_sub, sizeof(SubMC) * (size_t)nb * nsub, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_mem, ctx->h_mem, sizeof(MemberDev) * (size_t)nb, cudaMemcpyHostToDevice, ctx->stream));
+    ctx->h2d = (long long)(sizeof(SubMC) * (size_t)nb * nsub + sizeof(MemberDev) * (size_t)nb);
+    ctx->uploaded = true;
+    ctx->ran = false;
+    return 0;
+}
+
+static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
+    if (!ctx->uploaded) return fail(ctx, BBGPU_ERR_STATE, "run before upload");
+    const GridDev &g = ctx->g;
+    const LayoutDev &L = ctx->cur->dev;
+    cudaStream_t s = ctx->stream;
+    const bool tm = ctx->timing;
+    if (tm) CK(cudaEventRecord(ctx->ev[0], s));
+    CK(cudaMemsetAsync(ctx->d_tcount, 0, sizeof(int) * (size_t)(ctx->ntile_total + 1), s));
+    launch_mc_bin(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->nb, ctx->tx, ctx->ty, ctx->d_pix, ctx->d_tcount,
+                  ctx->d_err);
+    CKL();
+    if (tm) CK(cudaEventRecord(ctx->ev[1], s));
+    launch_scan_tiles(s, ctx->d_tcount, ctx->d_toff, ctx->d_tcur, ctx->ntile_total);
+    CKL();
+    if (tm) CK(cudaEventRecord(ctx->ev[2], s));
+    launch_mc_scatter(s, L, ctx->d_mem, ctx->nb, ctx->tx, ctx->ty, ctx->d_pix, ctx->d_tcur, ctx->d_bucket);
+    CKL();
+    if (tm) CK(cudaEventRecord(ctx->ev[3], s));
+    launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->tx, ctx->ty,
+                      ctx->d_pix, ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig, ctx->d_cd2if, ctx->d_cd2i,
+                      ctx->d_model, ctx->mstride, ctx->want64 ? ctx->d_model64 : nullptr, ctx->d_err);
+    CKL();
+    if (tm) CK(cudaEventRecord(ctx->ev[4], s));
+    const bool conv = ctx->kernel_set;
+    if (do_resid || ctx->keep_smoothed) {
+        launch_conv_resid(s, g, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->d_model, ctx->mstride, g.nz,
+                          ctx->d_taps, ctx->ky, ctx->kx, ctx->kxw, ctx->keep_smoothed ? ctx->d_smooth : nullptr,
+                          conv ? 1 : 0, do_resid ? 1 : 0, ctx->d_partial);
+        CKL();
+    }
+    if (tm) CK(cudaEventRecord(ctx->ev[5], s));
+    if (do_resid) {
+        launch_reduce_partials(s, ctx->d_partial, ctx->npart, ctx->nb, ctx->d_out2);
+        CKL();
+    }
+    if (tm) {
+        CK(cudaEventRecord(ctx->ev[6], s));
+        CK(cudaEventSynchronize(ctx->ev[6]));
+        for (int i = 0; i < NTIMER; i++) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ctx->ev[i], ctx->ev[i + 1]);
+            ctx->times[i] = ms;
+        }
+    }
+    ctx->ran = true;
+    return 0;
+}
+
+static int check_err(bbgpu_ctx *ctx) {
+    CK(cudaMemcpyAsync(ctx->h_err, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (*ctx->h_err) {
+        int e = *ctx->h_err;
+        CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+        return fail(ctx, BBGPU_ERR_KERNEL, "kernel error flag 0x%x (cloud layout inconsistent with the sub-rings)", e);
+    }
+    return 0;
+}
+
+extern "C" int bbgpu_eval_upload(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const double *sr,
+                                 const int64_t *nv, const bbgpu_eval_desc *descs) {
+    if (!ctx) return BBGPU_ERR_ARG;
+    CK(cudaSetDevice(ctx->device));
+    ctx->want64 = false;
+    return batch_prepare(ctx, galmodtype, nb, nsub, sr, nv, descs, true);
+}
+
+extern "C" int bbgpu_eval_run(bbgpu_ctx *ctx) {
+    if (!ctx) return BBGPU_ERR_ARG;
+    CK(cudaSetDevice(ctx->device));
+    return batch_run(ctx, true);
+}
+
+extern "C" int bbgpu_eval_download(bbgpu_ctx *ctx, double *ss, double *lg) {
+    if (!ctx || !ss) return BBGPU_ERR_ARG;
+    if (!ctx->ran) return fail(ctx, BBGPU_ERR_STATE, "download before run");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemcpyAsync(ctx->h_out2, ctx->d_out2, sizeof(double) * 2 * ctx->nb, cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->d2h = (long long)(sizeof(double) * 2 * ctx->nb + sizeof(int));
+    int rc = check_err(ctx);
+    if (rc) return rc;
+    for (int k = 0; k < ctx->nb; k++) {
+        ss[k] = ctx->h_out2[2 * k];
+        if (lg) lg[k] = ctx->h_out2[2 * k + 1];
+    }
+    return BBGPU_OK;
+}
+
+extern "C" int bbgpu_eval_batch(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const double *sr, const int64_t *nv,
+                                const bbgpu_eval_desc *descs, double *ss, double *lg) {
+    int rc = bbgpu_eval_upload(ctx, galmodtype, nb, nsub, sr, nv, descs);
+    if (rc) return rc;
+    rc = bbgpu_eval_run(ctx);
+    if (rc) return rc;
+    return bbgpu_eval_download(ctx, ss, lg);
+}
+
+extern "C" int bbgpu_eval_model(bbgpu_ctx *ctx, int k, int smoothed, float *out, int by, int bx, int nz) {
+    if (!ctx || !out) return BBGPU_ERR_ARG;
+    if (!ctx->ran || k < 0 || k >= ctx->nb) return fail(ctx, BBGPU_ERR_STATE, "eval_model: no such member");
+    const MemberDev &M = ctx->mem_host[k];
+    if (by != M.by || bx != M.bx || nz != ctx->g.nz) return fail(ctx, BBGPU_ERR_ARG, "eval_model: shape mismatch");
+    if (smoothed && !ctx->keep_smoothed) return fail(ctx, BBGPU_ERR_STATE, "eval_model: smoothed models not kept");
+    const float *src = (smoothed ? ctx->d_smooth : ctx->d_model) + (size_t)k * ctx->mstride;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemcpyAsync(out, src, sizeof(float) * (size_t)by * bx * nz, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return BBGPU_OK;
+}
+
+// ------------------------------------------------------------------------------------------- reference kernels
+extern "C" int bbgpu_galmod_mc(bbgpu_ctx *ctx, double *out, const double *sr, int nsub, int ring_lo, int ring_hi,
+                               uint64_t seed, const int64_t *nv, int blo0, int blo1, int bhi0, int bhi1) {
+    if (!ctx) return BBGPU_ERR_ARG;
+    if (!out || !sr || !nv || ring_lo < 0 || ring_hi > nsub || ring_lo > ring_hi)
+        return fail(ctx, BBGPU_ERR_ARG, "galmod_mc: invalid arguments");
+    CK(cudaSetDevice(ctx->device));
+    // sub-rings [ring_lo, ring_hi) with a stream seeded by seed: the table restricted to them
+    int ns = ring_hi - ring_lo;
+    std::vector<double> s2((size_t)BBGPU_NSR * (ns ? ns : 1));
+    std::vector<int64_t> nv2(ns ? ns : 1);
+    for (int r = 0; r < BBGPU_NSR; r++)
+        for (int i = 0; i < ns; i++) s2[(size_t)r * ns + i] = sr[(size_t)r * nsub + ring_lo + i];
+    for (int i = 0; i < ns; i++) nv2[i] = nv[ring_lo + i];
+    int by = bhi1 - blo1, bx = bhi0 - blo0;
+    if (ns == 0 || by <= 0 || bx <= 0) return BBGPU_OK;
+    bbgpu_eval_desc d{};
+    d.blo0 = blo0; d.blo1 = blo1; d.bhi0 = bhi0; d.bhi1 = bhi1; d.seed = seed;
+    ctx->want64 = true;
+    int rc = batch_prepare(ctx, BBGPU_MC, 1, ns, s2.data(), nv2.data(), &d, false);
+    if (rc) return rc;
+    rc = batch_run(ctx, false);
+    ctx->want64 = false;
+    if (rc) return rc;
+    rc = check_err(ctx);
+    if (rc) return rc;
+    size_t n = (size_t)by * bx * ctx->g.nz;
+    std::vector<double> tmp(n);
+    CK(cudaMemcpy(tmp.data(), ctx->d_model64, n * sizeof(double), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; i++) out[i] += tmp[i];
+    ctx->uploaded = ctx->ran = false;
+    return BBGPU_OK;
+}
+
+extern "C" int bbgpu_convolve(bbgpu_ctx *ctx, const double *in, double *out, int nz, int ny, int nx, double scale,
+                              int threshold) {
+    if (!ctx) return BBGPU_ERR_ARG;
+    if (!in || !out || nz < 1 || ny < 1 || nx < 1) return fail(ctx, BBGPU_ERR_ARG, "convolve: invalid arguments");
+    if (!ctx->kernel_set) return fail(ctx, BBGPU_ERR_STATE, "convolve before set_kernel");
+    CK(cudaSetDevice(ctx->device));
+    size_t n = (size_t)nz * ny * nx;
+    double *d64 = nullptr;
+    float *a = nullptr, *b = nullptr;
+    MemberDev *dm = nullptr;
+    int rc = 0;
+    GridDev g = ctx->g;
+    g.scalefactor = threshold ? scale : 1.0;
+    MemberDev M{};
+    M.blo0 = 0; M.blo1 = 0; M.bhi0 = nx; M.bhi1 = ny; M.bx = nx; M.by = ny;
+    cudaStream_t s = ctx->stream;
+    if (cudaMalloc(&d64, n * sizeof(double)) != cudaSuccess || cudaMalloc(&a, n * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&b, n * sizeof(float)) != cudaSuccess || cudaMalloc(&dm, sizeof M) != cudaSuccess) {
+        cudaGetLastError();
+        rc = fail(ctx, BBGPU_ERR_NOMEM, "convolve: allocation failed");
+    }
+    int npart = conv_resid_npart(&M, 1, nz);
+    double *dp = nullptr;
+    if (!rc && cudaMalloc(&dp, 2 * sizeof(double) * (npart ? npart : 1)) != cudaSuccess) {
+        cudaGetLastError();
+        rc = fail(ctx, BBGPU_ERR_NOMEM, "convolve: allocation failed");
+    }
+    if (!rc) {
+        cudaMemcpyAsync(d64, in, n * sizeof(double), cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(dm, &M, sizeof M, cudaMemcpyHostToDevice, s);
+        launch_zyx64_to_yxz32(s, d64, a, nz, ny, nx);
+        launch_conv_resid(s, g, dm, &M, 1, a, (long long)n, nz, ctx->d_taps, ctx->ky, ctx->kx, ctx->kxw, b,
+                          threshold ? 1 : 2, 0, dp);
+        launch_yxz32_to_zyx64(s, b, d64, nz, ny, nx);
+        ctx->launches += 3;
+        cudaMemcpyAsync(out, d64, n * sizeof(double), cudaMemcpyDeviceToHost, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = fail(ctx, BBGPU_ERR_CUDA, "convolve: %s", cudaGetErrorString(e));
+    }
+    cudaFree(d64); cudaFree(a); cudaFree(b); cudaFree(dm); cudaFree(dp);
+    return rc;
+}
+
+static int sumsq_common(bbgpu_ctx *ctx, const double *model, const float *data, const uint8_t *mask, int maskmode,
+                        const uint8_t *region, int nz, int ny, int nx, double sigma2, double eps2, double *out2) {
+    if (!ctx) return BBGPU_ERR_ARG;
+    if (!model || !data || !out2 || nz < 0 || ny < 0 || nx < 0) return fail(ctx, BBGPU_ERR_ARG, "residuals: invalid arguments");
+    if (maskmode != 0 && !mask) return fail(ctx, BBGPU_ERR_ARG, "residuals: maskmode %d without a mask", maskmode);
+    CK(cudaSetDevice(ctx->device));
+    size_t n = (size_t)nz * ny * nx;
+    out2[0] = out2[1] = 0.0;
+    if (n == 0) return BBGPU_OK;
+    double *dm = nullptr, *dp = nullptr;
+    float *dd = nullptr;
+    uint8_t *dk = nullptr, *dr = nullptr;
+    const int maxb = 1024;
+    int rc = 0;
+    if (cudaMalloc(&dm, n * 8) != cudaSuccess || cudaMalloc(&dd, n * 4) != cudaSuccess ||
+        cudaMalloc(&dp, 2 * 8 * maxb) != cudaSuccess || (mask && cudaMalloc(&dk, n) != cudaSuccess) ||
+        (region && cudaMalloc(&dr, (size_t)ny * nx) != cudaSuccess)) {
+        cudaGetLastError();
+        rc = fail(ctx, BBGPU_ERR_NOMEM, "residuals: allocation failed");
+    }
+    if (!rc) {
+        cudaStream_t s = ctx->stream;
+        cudaMemcpyAsync(dm, model, n * 8, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(dd, data, n * 4, cudaMemcpyHostToDevice, s);
+        if (mask) cudaMemcpyAsync(dk, mask, n, cudaMemcpyHostToDevice, s);
+        if (region) cudaMemcpyAsync(dr, region, (size_t)ny * nx, cudaMemcpyHostToDevice, s);
+        int nbk = launch_sumsq64(s, dm, dd, dk, maskmode, dr, nz, ny, nx, sigma2, eps2, dp, maxb);
+        ctx->launches++;
+        std::vector<double> hp(2 * (size_t)nbk);
+        cudaMemcpyAsync(hp.data(), dp, 2 * 8 * (size_t)nbk, cudaMemcpyDeviceToHost, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = fail(ctx, BBGPU_ERR_CUDA, "residuals: %s", cudaGetErrorString(e));
+        for (int i = 0; i < nbk; i++) {
+            out2[0] += hp[2 * i];
+            out2[1] += hp[2 * i + 1];
+        }
+    }
+    cudaFree(dm); cudaFree(dd); cudaFree(dp); cudaFree(dk); cudaFree(dr);
+    return rc;
+}
+
+extern "C" int bbgpu_sumsq_residuals(bbgpu_ctx *ctx, const double *model, const float *data, const uint8_t *mask,
+                                     int maskmode, const uint8_t *region, int nz, int ny, int nx, double *out) {
+    double o2[2];
+    int rc = sumsq_common(ctx, model, data, mask, maskmode, region, nz, ny, nx, 1.0, 0.0, o2);
+    if (!rc && out) *out = o2[0];
+    return rc;
+}
+
+extern "C" int bbgpu_residuals_fracerr(bbgpu_ctx *ctx, const double *model, const float *data, const uint8_t *mask,
+                                       int maskmode, const uint8_t *region, int nz, int ny, int nx, double sigma2,
+                                       double eps2, double *out2) {
+    if (ctx && !(sigma2 > 0)) return fail(ctx, BBGPU_ERR_ARG, "residuals_fracerr: sigma2 must be > 0");
+    if (ctx && !(eps2 > 0)) return fail(ctx, BBGPU_ERR_ARG, "residuals_fracerr: eps2 must be > 0");
+    return sumsq_common(ctx, model, data, mask, maskmode, region, nz, ny, nx, sigma2, eps2, out2);
+}
+
+// ------------------------------------------------------------------------------------------- not yet on the device
+extern "C" int bbgpu_galmod_analytic(bbgpu_ctx *ctx, double *out, const double *sr, int nsub, int ring_lo, int ring_hi,
+                                     int nzq, int blo0, int blo1, int bhi0, int bhi1) {
+    (void)out; (void)sr; (void)nsub; (void)ring_lo; (void)ring_hi; (void)nzq; (void)blo0; (void)blo1; (void)bhi0; (void)bhi1;
+    return fail(ctx, BBGPU_ERR_ARG, "galmod_analytic: not available in this build");
+}
+
+extern "C" int bbgpu_ring_maps_analytic(bbgpu_ctx *ctx, double *out, int nr, const double *sr, int nsub,
+                                        const int64_t *widx, const double *wval, int nzq, int blo0, int blo1, int bhi0,
+                                        int bhi1) {
+    (void)out; (void)nr; (void)sr; (void)nsub; (void)widx; (void)wval; (void)nzq; (void)blo0; (void)blo1; (void)bhi0; (void)bhi1;
+    return fail(ctx, BBGPU_ERR_ARG, "ring_maps_analytic: not available in this build");
+}
+
+extern "C" int bbgpu_conv_sparse(bbgpu_ctx *ctx, const double *model, double *out, int ny, int nx, int nz,
+                                 const double *kernel, int ky, int kx, double scale) {
+    (void)model; (void)out; (void)ny; (void)nx; (void)nz; (void)kernel; (void)ky; (void)kx; (void)scale;
+    return fail(ctx, BBGPU_ERR_ARG, "conv_sparse: not available in this build");
+}
+
+extern "C" int bbgpu_norm(bbgpu_ctx *ctx, double *model, int bsy, int bsx, int nz, const float *data, const uint8_t *mask,
+                          int dny, int dnx, int64_t blo0, int64_t blo1, double x0, double y0, double phi, double inc,
+                          double r1, double r2, double wpow, int side, int ftype, const double *chan_noise,
+                          double data_noise, double bweight, int normtype, const double *pre, const int64_t *ilo,
+                          const int64_t *ihi, int ky, const double *thr, int foot, double hmax, double *out) {
+    (void)model; (void)bsy; (void)bsx; (void)nz; (void)data; (void)mask; (void)dny; (void)dnx; (void)blo0; (void)blo1;
+    (void)x0; (void)y0; (void)phi; (void)inc; (void)r1; (void)r2; (void)wpow; (void)side; (void)ftype; (void)chan_noise;
+    (void)data_noise; (void)bweight; (void)normtype; (void)pre; (void)ilo; (void)ihi; (void)ky; (void)thr; (void)foot;
+    (void)hmax; (void)out;
+    return fail(ctx, BBGPU_ERR_ARG, "norm: not available in this build");
+}

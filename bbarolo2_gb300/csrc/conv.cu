@@ -1,0 +1,225 @@
+// Beam convolution of the model and the masked residual, fused (bbarolo/smooth.py:145-165,
+// bbarolo/galmod.py:1273-1283, bbarolo/bayesian/likelihood.py:22-77).
+//
+// The model of a member is (by, bx, nz) float32: channels fastest, so that a warp holds 32 channels of one
+// pixel and every load and store is a 128-byte line. One CTA computes a 16 x 16 pixel tile of 32 channels:
+// the input tile with its halo (zero outside the box: the reference convolves the box with zero padding) is
+// staged in shared memory, each thread accumulates two output rows of 16 pixels for its channel over the
+// kernel rows, from a register window of the input row (float32 FMAs; the taps are broadcast from shared
+// memory). The epilogue applies the reference's threshold (values below 1e-12 set to zero) and flux scale,
+// and, instead of writing the smoothed cube, compares it with the data: each CTA leaves the sum of squared
+// residuals of its voxels (and the sum of log-variances for a fractional model error), reduced in float64.
+// Tiles whose input is all zero skip the convolution (empty channels and the corners of the box).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "kernels.h"
+
+namespace {
+
+constexpr int TO = 16;        // output tile side (pixels)
+constexpr int ZB = 32;        // channels per CTA (one per lane)
+constexpr int NW = 8;         // warps per CTA: two output rows each
+
+template <int KXW>
+__global__ void __launch_bounds__(256) k_conv_resid(GridDev g, const MemberDev *__restrict__ mem,
+                                                    const float *__restrict__ model, long long mstride, int nz,
+                                                    const float *__restrict__ taps, int ky, int kx,
+                                                    float *__restrict__ smoothed, int do_conv, int do_resid,
+                                                    double *__restrict__ partial, int npart) {
+    extern __shared__ float sm[];
+    constexpr int W = TO + KXW - 1;
+    const int k = blockIdx.x;
+    const MemberDev &M = mem[k];
+    const int ntx = (M.bx + TO - 1) / TO, nty = (M.by + TO - 1) / TO;
+    const int t = blockIdx.y, zb = blockIdx.z;
+    const int nzb = gridDim.z;
+    double *pout = partial + 2 * ((size_t)k * npart + (size_t)t * nzb + zb);
+    if (t >= ntx * nty) {
+        if (threadIdx.x == 0) { pout[0] = 0.0; pout[1] = 0.0; }
+        return;
+    }
+    const int ky_eff = do_conv ? ky : 1, kx_eff = do_conv ? kx : 1;
+    const int hy = ky_eff / 2, hx = kx_eff / 2;
+    const int H = TO + ky_eff - 1;
+    float *S = sm;                          // H x W x ZB
+    float *sk = sm + (size_t)H * W * ZB;    // ky x KXW taps
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int y0 = (t / ntx) * TO, x0 = (t % ntx) * TO;
+    const int z = zb * ZB + lane;
+    const bool zok = z < nz;
+    if (do_conv)
+        for (int i = threadIdx.x; i < ky * KXW; i += blockDim.x) sk[i] = taps[i];
+    const float *mk = model + (size_t)k * mstride;
+    int any = 0;
+    for (int q = warp; q < H * W; q += NW) {
+        const int r = q / W, col = q - r * W;
+        const int yy = y0 - hy + r, xx = x0 - hx + col;
+        float v = 0.0f;
+        if (zok && col < TO + kx_eff - 1 && yy >= 0 && yy < M.by && xx >= 0 && xx < M.bx)
+            v = mk[((size_t)yy * M.bx + xx) * nz + z];
+        S[(size_t)q * ZB + lane] = v;
+        any |= v != 0.0f;
+    }
+    const int nonempty = __syncthreads_or(any);
+    float acc[2][TO];
+#pragma unroll
+    for (int rr = 0; rr < 2; rr++)
+#pragma unroll
+        for (int x = 0; x < TO; x++) acc[rr][x] = 0.0f;
+    if (nonempty) {
+        if (do_conv) {
+            for (int a = 0; a < ky; a++) {
+#pragma unroll
+                for (int rr = 0; rr < 2; rr++) {
+                    const int ty = warp * 2 + rr;
+                    const float *row = S + (size_t)((ty + a) * W) * ZB + lane;
+                    float win[W];
+#pragma unroll
+                    for (int j = 0; j < W; j++) win[j] = row[j * ZB];
+#pragma unroll
+                    for (int b = 0; b < KXW; b++) {
+                        const float kv = sk[a * KXW + b];
+#pragma unroll
+                        for (int x = 0; x < TO; x++) acc[rr][x] = fmaf(kv, win[x + b], acc[rr][x]);
+                    }
+                }
+            }
+        } else {
+#pragma unroll
+            for (int rr = 0; rr < 2; rr++) {
+                const int ty = warp * 2 + rr;
+#pragma unroll
+                for (int x = 0; x < TO; x++) acc[rr][x] = S[(size_t)(ty * W + x) * ZB + lane];
+            }
+        }
+    }
+    // epilogue: threshold + scale (smoothed models only), residual
+    const float scale = (float)g.scalefactor;
+    float ss = 0.0f, lg = 0.0f;
+    const bool fr = M.eps2 > 0.0;
+#pragma unroll
+    for (int rr = 0; rr < 2; rr++) {
+        const int y = y0 + warp * 2 + rr;
+        if (y >= M.by || !zok) continue;
+#pragma unroll
+        for (int x = 0; x < TO; x++) {
+            const int xx = x0 + x;
+            if (xx >= M.bx) continue;
+            float m = acc[rr][x];
+            if (do_conv == 1) m = m < 1.0e-12f ? 0.0f : m * scale;
+            if (smoothed) smoothed[(size_t)k * mstride + ((size_t)y * M.bx + xx) * nz + z] = m;
+            if (do_resid) {
+                const float d = M.deff[((size_t)(y + M.blo1) * g.nx + (xx + M.blo0)) * g.nz + z];
+                if (d == d) {
+                    const float r = d - m;
+                    if (fr && m != 0.0f) {
+                        const float v = M.sigma2f + M.eps2f * m * m;
+                        ss += r * r / v;
+                        lg += logf(v / M.sigma2f);
+                    } else if (fr) {
+                        ss += r * r / M.sigma2f;
+                    } else {
+                        ss += r * r;
+                    }
+                }
+            }
+        }
+    }
+    // float64 reduction of the CTA's sums
+    double ds = (double)ss, dl = (double)lg;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ds += __shfl_down_sync(0xffffffffu, ds, o);
+        dl += __shfl_down_sync(0xffffffffu, dl, o);
+    }
+    __shared__ double red[2][NW];
+    if (lane == 0) { red[0][warp] = ds; red[1][warp] = dl; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int w = 0; w < NW; w++) { a += red[0][w]; b += red[1][w]; }
+        pout[0] = a;
+        pout[1] = b;
+    }
+}
+
+__global__ void k_reduce_partials(const double *__restrict__ partial, int npart, double *__restrict__ out2) {
+    // one CTA per member; fixed summation order (deterministic)
+    __shared__ double sa[256], sb[256];
+    const int k = blockIdx.x;
+    const double *p = partial + 2 * (size_t)k * npart;
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < npart; i += 256) { a += p[2 * i]; b += p[2 * i + 1]; }
+    sa[threadIdx.x] = a;
+    sb[threadIdx.x] = b;
+    __syncthreads();
+    for (int d = 128; d > 0; d >>= 1) {
+        if (threadIdx.x < d) { sa[threadIdx.x] += sa[threadIdx.x + d]; sb[threadIdx.x] += sb[threadIdx.x + d]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { out2[2 * k] = sa[0]; out2[2 * k + 1] = sb[0]; }
+}
+
+template <int KXW>
+void launch_t(cudaStream_t s, const GridDev &g, const MemberDev *mem, int nb, int maxt, int nzb, const float *model,
+              long long mstride, int nz, const float *taps, int ky, int kx, float *smoothed, int do_conv,
+              int do_resid, double *partial, int npart) {
+    const int kye = do_conv ? ky : 1;
+    size_t smem = (size_t)(TO + kye - 1) * (TO + KXW - 1) * ZB * sizeof(float) + (size_t)ky * KXW * sizeof(float);
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        cudaFuncSetAttribute(k_conv_resid<KXW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        configured = smem;
+    }
+    dim3 grid(nb, maxt, nzb);
+    k_conv_resid<KXW><<<grid, 256, smem, s>>>(g, mem, model, mstride, nz, taps, ky, kx, smoothed, do_conv, do_resid,
+                                             partial, npart);
+}
+
+}  // namespace
+
+static const int KXWS[] = {1, 3, 5, 7, 9, 11, 13, 15, 17, 21, 25, 31};
+
+int conv_taps(const double *k, int ky, int kx, float *taps) {
+    int kxw = 0;
+    for (int w : KXWS)
+        if (w >= kx) { kxw = w; break; }
+    if (!kxw) return 0;
+    // flipped: out[y, x] = sum_{a, b} kf[a, b] in[y - hy + a, x - hx + b], kf[a, b] = k[ky-1-a, kx-1-b]
+    for (int a = 0; a < ky; a++)
+        for (int b = 0; b < kxw; b++)
+            taps[a * kxw + b] = b < kx ? (float)k[(ky - 1 - a) * kx + (kx - 1 - b)] : 0.0f;
+    return kxw;
+}
+
+int conv_resid_npart(const MemberDev *mem_host, int nb, int nz) {
+    int maxt = 0;
+    for (int k = 0; k < nb; k++)
+        maxt = max(maxt, ((mem_host[k].bx + TO - 1) / TO) * ((mem_host[k].by + TO - 1) / TO));
+    return maxt * ((nz + ZB - 1) / ZB);
+}
+
+void launch_conv_resid(cudaStream_t s, const GridDev &g, const MemberDev *mem, const MemberDev *mem_host, int nb,
+                       const float *model, long long mstride, int nz, const float *taps, int ky, int kx, int kxw,
+                       float *smoothed, int do_conv, int do_resid, double *partial) {
+    int maxt = 0;
+    for (int k = 0; k < nb; k++)
+        maxt = max(maxt, ((mem_host[k].bx + TO - 1) / TO) * ((mem_host[k].by + TO - 1) / TO));
+    if (nb == 0 || maxt == 0) return;
+    const int nzb = (nz + ZB - 1) / ZB;
+    const int npart = maxt * nzb;
+    if (!do_conv) kxw = 1;
+#define CASE(W) case W: launch_t<W>(s, g, mem, nb, maxt, nzb, model, mstride, nz, taps, ky, kx, smoothed, do_conv, do_resid, partial, npart); break;
+    switch (kxw) {
+        CASE(1) CASE(3) CASE(5) CASE(7) CASE(9) CASE(11) CASE(13) CASE(15) CASE(17) CASE(21) CASE(25) CASE(31)
+        default: break;
+    }
+#undef CASE
+}
+
+void launch_reduce_partials(cudaStream_t s, const double *partial, int npart, int nb, double *out2) {
+    if (nb == 0) return;
+    k_reduce_partials<<<nb, 256, 0, s>>>(partial, npart, out2);
+}

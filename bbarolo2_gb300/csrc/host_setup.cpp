@@ -1,0 +1,310 @@
+// Host set-up of the bbgpu runtime: random-stream layouts of the MC model and the per-sub-ring constants.
+//
+// Compiled with -ffp-contract=off: the float64 expressions below round exactly as the reference's
+// (bbarolo/galmod.py), and its transcendental functions are the C library's, as numba's.
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "internal.h"
+
+namespace {
+
+// ---------------------------------------------------------------- ziggurat tables (bbarolo/_rng.py:17-38)
+struct Zig {
+    int64_t kn[128];
+    double wn[128], fn[128];
+    Zig() {
+        double dn = 3.442619855899, tn = dn;
+        const double vn = 9.91256303526217e-3, m1 = 2147483648.0;
+        const double q = vn / exp(-.5 * dn * dn);
+        kn[0] = (int64_t)((dn / q) * m1);
+        kn[1] = 0;
+        wn[0] = q / m1;
+        wn[127] = dn / m1;
+        fn[0] = 1.;
+        fn[127] = exp(-.5 * dn * dn);
+        for (int i = 126; i >= 1; i--) {
+            dn = sqrt(-2. * log(vn / dn + exp(-.5 * dn * dn)));
+            kn[i + 1] = (int64_t)((dn / tn) * m1);
+            tn = dn;
+            fn[i] = exp(-.5 * dn * dn);
+            wn[i] = dn / m1;
+        }
+    }
+};
+const Zig &zig() {
+    static Zig z;
+    return z;
+}
+
+// ---------------------------------------------------------------- the stream (bbarolo/_rng.py:49-100)
+struct Stream {
+    uint64_t s0, s1;
+    explicit Stream(uint64_t seed) {
+        // splitmix64 seeding: two outputs of the splitmix sequence started at seed + golden gamma
+        uint64_t z = seed + 0x9E3779B97F4A7C15ULL;
+        uint64_t out[2];
+        for (int i = 0; i < 2; i++) {
+            z += 0x9E3779B97F4A7C15ULL;
+            uint64_t x = z;
+            x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+            x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+            out[i] = x ^ (x >> 31);
+        }
+        s0 = out[0];
+        s1 = out[1];
+        if (s0 == 0 && s1 == 0) s0 = 1;
+    }
+    inline uint64_t next() {   // xoroshiro128+
+        uint64_t a = s0, b = s1, r = a + b;
+        b ^= a;
+        s0 = ((a << 24) | (a >> 40)) ^ b ^ (b << 16);
+        s1 = (b << 37) | (b >> 27);
+        return r;
+    }
+    inline double uniform() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
+    // Ziggurat normal. first_hz: the high word (minus 2^31) of its first draw; slow: it did not take the
+    // one-draw path (its value must then be recorded).
+    inline double normal(int32_t *first_hz, bool *slow) {
+        const Zig &Z = zig();
+        bool first = true;
+        *slow = false;
+        for (;;) {
+            int64_t hz = (int64_t)(next() >> 32) - 2147483648LL;
+            if (first) { *first_hz = (int32_t)hz; first = false; }
+            int64_t iz = hz & 127;
+            int64_t ahz = hz < 0 ? -hz : hz;
+            if (ahz < Z.kn[iz]) return (double)hz * Z.wn[iz];
+            *slow = true;
+            double x = (double)hz * Z.wn[iz];
+            if (iz == 0) {
+                double xx, yy;
+                for (;;) {
+                    xx = -log(1.0 - uniform()) * 0.2904764;
+                    yy = -log(1.0 - uniform());
+                    if (yy + yy >= xx * xx) break;
+                }
+                return hz > 0 ? 3.442620 + xx : -3.442620 - xx;
+            }
+            if (Z.fn[iz] + uniform() * (Z.fn[iz - 1] - Z.fn[iz]) < exp(-.5 * x * x)) return x;
+        }
+    }
+    inline double normal() {
+        int32_t h;
+        bool s;
+        return normal(&h, &s);
+    }
+};
+
+inline int64_t lround_ref(double x) {   // bbarolo/galmod.py:38-46
+    if (!(fabs(x) < 1e18)) return -((int64_t)1 << 62);
+    if (x >= 0) return (int64_t)(x + 0.5);
+    return -(int64_t)(-x + 0.5);
+}
+
+// layer deviate (bbarolo/galmod.py:76-89)
+inline double layer_deviate(int ltype, Stream &st) {
+    if (ltype == 1) return st.normal();
+    double x = 2.0 * st.uniform() - 1.0;
+    if (ltype == 2) return atanh(x);
+    if (ltype == 3) return x >= 0.0 ? -log(x) : log(-x);
+    if (ltype == 4) return tan(0.5 * M_PI * x);
+    return x;
+}
+
+template <class T>
+T *dup(const std::vector<T> &v) {
+    T *p = (T *)malloc(sizeof(T) * (v.size() ? v.size() : 1));
+    if (p && !v.empty()) memcpy(p, v.data(), sizeof(T) * v.size());
+    return p;
+}
+
+}  // namespace
+
+void bbh_zig_tables(int64_t *kn, double *wn, double *fn) {
+    const Zig &Z = zig();
+    memcpy(kn, Z.kn, sizeof Z.kn);
+    memcpy(wn, Z.wn, sizeof Z.wn);
+    memcpy(fn, Z.fn, sizeof Z.fn);
+}
+
+// Phi(t) on the 1/512 grid of bbarolo/galmod.py:176-180
+void bbh_phi_table(double *tab) {
+    for (int k = 0; k < 6146; k++) tab[k] = 0.5 * erfc(-(-6.0 + k / 512.0) / sqrt(2.0));
+}
+
+uint64_t bbh_layout_key(uint64_t seed, int ltype, int nsub, const int *nc, const int *nv, const double *R0,
+                        double radsep) {
+    uint64_t h = 1469598103934665603ULL;
+    auto mix = [&h](const void *p, size_t n) {
+        const unsigned char *c = (const unsigned char *)p;
+        for (size_t i = 0; i < n; i++) { h ^= c[i]; h *= 1099511628211ULL; }
+    };
+    mix(&seed, sizeof seed);
+    mix(&ltype, sizeof ltype);
+    mix(&nsub, sizeof nsub);
+    mix(nc, sizeof(int) * nsub);
+    mix(nv, sizeof(int) * nsub);
+    mix(R0, sizeof(double) * nsub);
+    mix(&radsep, sizeof radsep);
+    return h;
+}
+
+// Parses the stream of _galmod_mc (bbarolo/galmod.py:100-144) for clouds counts nc and velocity samples nv
+// per sub-ring: the draws are the same whatever the ring velocities, geometry and box, so each cloud's
+// radius, azimuth, layer deviate and the first word of each of its normals are recorded once.
+int bbh_layout_build(LayoutHost *L, uint64_t seed, int ltype, int nsub, const int *nc, const int *nv,
+                     const double *R0, double radsep) {
+    memset(L, 0, sizeof *L);
+    L->key = bbh_layout_key(seed, ltype, nsub, nc, nv, R0, radsep);
+    L->nsub = nsub;
+    long long ncl = 0, nsc = 0;
+    std::vector<int> vnc(nsub), vnv(nsub), vcb(nsub);
+    std::vector<long long> vsb(nsub);
+    for (int i = 0; i < nsub; i++) {
+        vnc[i] = nc[i];
+        vnv[i] = nv[i];
+        vcb[i] = (int)ncl;
+        vsb[i] = nsc;
+        ncl += nc[i];
+        nsc += (long long)nc[i] * nv[i];
+    }
+    if (ncl > 0x7fffffffLL) return -1;
+    L->ncloud = (int)ncl;
+    L->nsubcloud = nsc;
+    std::vector<double> R(ncl), caz(ncl), saz(ncl), fd(ncl);
+    std::vector<int> sub(ncl), slow_base(ncl);
+    int32_t *hz = (int32_t *)malloc(sizeof(int32_t) * (nsc ? nsc : 1));
+    if (!hz) return -1;
+    std::vector<double> slow;
+    slow.reserve((size_t)(nsc / 20 + 16));
+    Stream st(seed);
+    long long c = 0, q = 0;
+    for (int ir = 0; ir < nsub; ir++) {
+        if (nc[ir] <= 0) continue;
+        double r_inner = R0[ir] - 0.5 * radsep;
+        double r_inner_sq = r_inner * r_inner;
+        double r_cross = 2.0 * radsep * R0[ir];
+        for (int ic = 0; ic < nc[ir]; ic++, c++) {
+            R[c] = sqrt(r_inner_sq + r_cross * fabs(2.0 * st.uniform() - 1.0));
+            double az = 2 * M_PI * fabs(2.0 * st.uniform() - 1.0);
+            saz[c] = sin(az);
+            caz[c] = cos(az);
+            fd[c] = layer_deviate(ltype, st);
+            sub[c] = ir;
+            slow_base[c] = (int)slow.size();
+            for (int iv = 0; iv < nv[ir]; iv++, q++) {
+                bool s;
+                double v = st.normal(&hz[q], &s);
+                if (s) slow.push_back(v);
+            }
+        }
+    }
+    L->nc = dup(vnc);
+    L->nv = dup(vnv);
+    L->cloud_base = dup(vcb);
+    L->sub_base = dup(vsb);
+    L->R = dup(R);
+    L->caz = dup(caz);
+    L->saz = dup(saz);
+    L->fdev = dup(fd);
+    L->sub = dup(sub);
+    L->slow_base = dup(slow_base);
+    L->hz = hz;
+    L->slow_val = dup(slow);
+    L->nslow = (long long)slow.size();
+    return 0;
+}
+
+void bbh_layout_free(LayoutHost *L) {
+    free(L->nc); free(L->nv); free(L->cloud_base); free(L->sub_base);
+    free(L->R); free(L->caz); free(L->saz); free(L->fdev); free(L->sub); free(L->slow_base);
+    free(L->hz); free(L->slow_val);
+    memset(L, 0, sizeof *L);
+}
+
+// Cloud counts of _galmod_mc (bbarolo/galmod.py:107-114): 0 for the sub-rings without density.
+void bbh_cloud_counts(const double *sr, int nsub, const int64_t *nv_in, const GridDev *g, int *nc, int *nv) {
+    for (int ir = 0; ir < nsub; ir++) {
+        double R0 = sr[0 * nsub + ir], dens = sr[5 * nsub + ir];
+        nv[ir] = (int)nv_in[ir];
+        if (dens == 0) { nc[ir] = 0; continue; }
+        double ring_area_pix = 2 * M_PI * R0 * g->radsep / g->pixarea;
+        double dp = g->cmode == 1 ? pow(dens, 1.0) : pow(dens, (double)g->cmode);
+        int64_t n = lround_ref(g->cdens * dp * ring_area_pix);
+        if ((double)lround_ref((double)n / ring_area_pix) < 10.) n = lround_ref(10 * ring_area_pix);
+        nc[ir] = n > 0x3fffffff ? 0x3fffffff : (n < 0 ? 0 : (int)n);
+    }
+}
+
+// The per-sub-ring constants of one member (bbarolo/galmod.py:111-127 and the cloud loop's invariants).
+// Returns e: the deposits are fixed-point numbers in units of 2^-e.
+int bbh_submc(const double *sr, int nsub, const int *nc, const int *nv, const GridDev *g, SubMC *out) {
+    double bound = 0.;
+    for (int ir = 0; ir < nsub; ir++) {
+        SubMC &S = out[ir];
+        memset(&S, 0, sizeof S);
+#define R_(row) sr[(size_t)(row) * nsub + ir]
+        double R0 = R_(0), dens = R_(5);
+        S.nc = nc[ir];
+        S.nv = nv[ir];
+        S.active = dens != 0 && nc[ir] > 0;
+        if (!S.active) continue;
+        double ring_area_pix = 2 * M_PI * R0 * g->radsep / g->pixarea;
+        double fluxsc = (double)(float)(dens * ring_area_pix * g->pixarea / (double)((int64_t)nc[ir] * nv[ir]));
+        S.vdisptmp = sqrt(R_(4) * R_(4) + g->sig_instr * g->sig_instr);
+        S.vrot = R_(1); S.vrad = R_(2); S.vvert = R_(3);
+        S.z0 = R_(6); S.dvdz = R_(7); S.zcyl = R_(8);
+        S.sinc = sin(R_(9)); S.cinc = cos(R_(9));
+        double phi = R_(10);
+        S.spa = sin(phi) * cos(g->crota2) + cos(phi) * sin(g->crota2);
+        S.cpa = cos(phi) * cos(g->crota2) - sin(phi) * sin(g->crota2);
+        S.xpos = R_(11); S.ypos = R_(12); S.vsys = R_(13);
+        S.wrec = R_(14); S.wapp = R_(15);
+#undef R_
+        double wmax = fmax(fabs(S.wrec), fabs(S.wapp));
+        for (int nl = 0; nl < g->nlines && nl < BBGPU_MAXL; nl++) {
+            S.valrel[nl] = g->relint[nl] * fluxsc;
+            bound += (double)nc[ir] * (double)nv[ir] * fabs(S.valrel[nl]) * wmax;
+        }
+        // fast-path coefficients (any rounding: the error is bounded in the kernel)
+        S.P1 = (float)(S.spa / g->cdelt0);
+        S.P2 = (float)(S.cinc * S.cpa / g->cdelt0);
+        S.P3 = (float)(S.sinc * S.cpa / g->cdelt0);
+        S.Q1 = (float)(S.cpa / g->cdelt1);
+        S.Q2 = (float)(S.cinc * S.spa / g->cdelt1);
+        S.Q3 = (float)(-S.sinc * S.spa / g->cdelt1);
+        S.xposf = (float)S.xpos;
+        S.yposf = (float)S.ypos;
+        for (int nl = 0; nl < g->nlines && nl < BBGPU_MAXL; nl++) {
+            double ia = g->axtyp == 4 ? g->ia : (double)g->lia[nl];
+            double ib = g->axtyp == 4 ? g->ib : (double)g->lib[nl];
+            S.c0[nl] = (float)((S.vsys + S.vvert * S.cinc) * ia + ib);
+            S.sia[nl] = (float)(S.sinc * ia);
+            S.sg[nl] = (float)(S.vdisptmp * ia);
+        }
+        S.z0f = (float)S.z0;
+        S.zcylf = (float)S.zcyl;
+        S.dvdzf = (float)S.dvdz;
+        S.vrotf = (float)S.vrot;
+        S.vradf = (float)S.vrad;
+    }
+    // fixed point: every voxel sum stays below 2^62
+    double Q = bound > 0 ? ldexp(1.0, (int)floor(62.0 - log2(bound))) : 1.0;
+    int cb = 0;
+    for (int ir = 0; ir < nsub; ir++) {
+        SubMC &S = out[ir];
+        S.cloud_base = cb;
+        cb += S.active ? S.nc : 0;
+        if (!S.active) continue;
+        for (int nl = 0; nl < g->nlines && nl < BBGPU_MAXL; nl++) {
+            S.fix[0][nl] = llrint(S.valrel[nl] * S.wrec * Q);
+            S.fix[1][nl] = llrint(S.valrel[nl] * S.wapp * Q);
+        }
+    }
+    return bound > 0 ? (int)floor(62.0 - log2(bound)) : 0;
+}

@@ -1,0 +1,80 @@
+// Launch wrappers of the bbgpu kernels (defined in mc.cu, conv.cu, analytic.cu, resid.cu), called by api.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "internal.h"
+
+// The device copy of a parsed MC stream (LayoutHost).
+struct LayoutDev {
+    int ncloud, nsub;
+    long long nsubcloud, nslow;
+    float4 *cf;          // per cloud: R, cos az, sin az, layer deviate (float32)
+    double *cd;          // per cloud: the same in float64, 4 values per cloud
+    int *sub;            // per cloud: sub-ring
+    int *slow_base;      // per cloud: slow normals before it
+    int32_t *hz;         // per sub-cloud
+    double *slow_val;    // slow normal values
+    long long *sub_base; // per sub-ring: first sub-cloud
+    int *cloud_base;     // per sub-ring: first cloud
+};
+
+// Per member of a batch (device array).
+struct MemberDev {
+    int blo0, blo1, bhi0, bhi1;   // box
+    int bx, by;                   // box size
+    int ntx, nty;                 // tiles of the deposit
+    int tile_off;                 // first tile of the member in the tile arrays
+    int fix_exp;                  // fixed-point exponent e (unit 2^-e)
+    int maskmode, use_region;
+    float sigma2f, eps2f;
+    double sigma2, eps2;
+    const float *deff;            // data used by the residual, (ny, nx, nz) float32, NaN where not used
+};
+
+struct ZigDev {
+    unsigned kn[128];
+    float wnf[128];
+    double wn[128];
+};
+
+// ---- MC (mc.cu)
+// For every (member, cloud): its pixel in the member's box (or -1) and the count of clouds per tile.
+void launch_mc_bin(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
+                   const MemberDev *mem, int nb, int tx, int ty, int *pix, int *tile_count, int *err);
+// Exclusive scan of tile counts into offsets (and cursors), for ntile_total tiles.
+void launch_scan_tiles(cudaStream_t s, const int *count, int *offset, int *cursor, int ntile_total);
+void launch_mc_scatter(cudaStream_t s, const LayoutDev &L, const MemberDev *mem, int nb, int tx, int ty,
+                       const int *pix, int *cursor, int *bucket);
+// Deposits the clouds of every tile into a shared-memory fixed-point tile and writes the model
+// (by, bx, nz) float32 of each member at model + k * mstride (and, if model64, float64 sums).
+void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
+                       const MemberDev *mem, const MemberDev *mem_host, int nb, int tx, int ty, const int *pix,
+                       const int *offset, const int *count, const int *bucket, const ZigDev *zig,
+                       const float *cd2if, const double *cd2i, float *model, long long mstride, double *model64,
+                       int *err);
+
+// ---- convolution + residual (conv.cu)
+// The taps of a beam kernel (ky, kx) as the conv kernels read them: flipped, float32, rows padded to the
+// compile-time window width kxw >= kx (returned; 0 if kx is too large). taps must hold ky * kxw floats.
+int conv_taps(const double *k, int ky, int kx, float *taps);
+// model (by, bx, nz) float32 per member -> the "same" convolution, threshold and scale, then the residual
+// against deff (ny, nx, nz) float32 (NaN: voxel not used) over the box; per-CTA partial sums (ss, lg).
+// If smoothed is not NULL the convolved model is written there (same layout).
+// partial: (nb, npart) pairs (ss, lg), npart = tiles of the largest box x channel blocks (returned).
+int conv_resid_npart(const MemberDev *mem_host, int nb, int nz);
+void launch_conv_resid(cudaStream_t s, const GridDev &g, const MemberDev *mem, const MemberDev *mem_host, int nb,
+                       const float *model, long long mstride, int nz, const float *taps, int ky, int kx, int kxw,
+                       float *smoothed, int do_conv, int do_resid, double *partial);
+void launch_reduce_partials(cudaStream_t s, const double *partial, int npart, int nb, double *out2);
+
+// ---- layouts and stand-alone residuals (resid.cu)
+void launch_prep_deff(cudaStream_t s, const float *data, const uint8_t *mask, const uint8_t *region, int maskmode,
+                      int nz, int ny, int nx, float *deff);
+// returns the number of partial pairs written
+int launch_sumsq64(cudaStream_t s, const double *model, const float *data, const uint8_t *mask, int maskmode,
+                   const uint8_t *region, int nz, int ny, int nx, double sigma2, double eps2, double *partial,
+                   int maxblocks);
+void launch_zyx64_to_yxz32(cudaStream_t s, const double *in, float *out, int nz, int ny, int nx);
+void launch_yxz32_to_zyx64(cudaStream_t s, const float *in, double *out, int nz, int ny, int nx);

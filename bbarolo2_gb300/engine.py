@@ -1,0 +1,301 @@
+"""The device model engine: ``DiskModel`` (``bbarolo/galmod.py:1147-1377``) with its models built, convolved and
+compared with the data on the GPU.
+
+``DiskModel(cube, par=None, ringmode=None, densflux=None, galmodtype=None, smooth=None)`` has the reference's
+constructor and methods (``box``, ``array``, ``convolve``, ``ring_maps``), with the header-derived constants
+(``GalmodSetup``) and the beam kernel computed on the host as the reference, and every model evaluation on the
+device through ``libbbgpu.so``. ``BatchLikelihood`` evaluates the Gaussian log-likelihood of
+``LikelihoodMixin._log_likelihood`` (``bbarolo/bayesian/likelihood.py:567-619``) for a batch of ring sets in
+one device pass.
+"""
+
+import math
+
+import numpy as np
+
+from . import _lib
+from .beam import BeamKernel
+from .galmod import (GalmodSetup, ZSTEP_BEAM, ZSTEP_COARSE, ZSTEP_FINE, ZSAMPLES_MAX, arcsconv, model_rings,
+                     outer_edge, ringmode_name, seed32, subrings_batch)
+from .rings import RING_KEYS
+
+
+def grid_struct(st, scalefactor):
+    """The ``bbgpu_grid`` of a GalmodSetup."""
+    g = _lib.Grid()
+    g.nx, g.ny, g.nz = st.dimx, st.dimy, st.nsubs
+    g.nlines = int(st.lfreq0.size)
+    g.axtyp, g.velsys, g.ltype, g.cmode = int(st.axtyp), int(st.velsys), int(st.ltype), int(st.cmode)
+    g.radsep, g.cdens, g.pixarea = st.radsep, st.cdens, st.pixarea
+    g.cdelt0, g.cdelt1, g.crota2 = st.cdelt[0], st.cdelt[1], st.crota2
+    g.sig_instr, g.crval3, g.cdelt3, g.crpix3 = st.sig_instr, st.crval3, st.cdelt3, st.crpix3
+    g.chwidth, g.zstep, g.scalefactor = st._chmin, st.zstep, float(scalefactor)
+    return g
+
+
+class DiskModel:
+    """Models of a rotating disk on the grid of a cube, built on the GPU (see the module docstring)."""
+
+    def __init__(self, cube, par=None, ringmode=None, densflux=None, galmodtype=None, smooth=None, device=0):
+        p = cube.pars()
+        self.cin = cube
+        self.par = p.gf if par is None else par
+        self.setup = GalmodSetup(cube, gmpar=self.par, galmodtype=galmodtype,
+                                 densflux=self.par.DENSFLUX if densflux is None else densflux)
+        self.ringmode = ringmode_name(getattr(p, "ringmode", "CENTRED") if ringmode is None else ringmode)
+        self.arcconv = arcsconv(cube.Head().Cunit(0))
+        self.cfield = None
+        self.scalefactor = 1.
+        self.smooth = bool(self.par.SM if smooth is None else smooth)
+        if self.smooth:
+            bk = BeamKernel.from_cube(cube)
+            if bk.kernel is None:
+                self.smooth = False
+            else:
+                self.cfield = bk.kernel
+                self.scalefactor = 1.0 if self.setup.densIsFlux else bk.scalefac
+        self.setup.zstep = self.zstep
+        self.ctx = _lib.Context(device)
+        st = self.setup
+        self.ctx.check(self.ctx.L.bbgpu_set_grid(self.ctx.h, self._grid(), _lib.ptr(st.cd2i), _lib.ptr(st.lfreq0),
+                                                 _lib.ptr(st.relint), _lib.ptr(st._vedges_lines)))
+        if self.cfield is not None:
+            k = np.ascontiguousarray(self.cfield, np.float64)
+            self.ctx.check(self.ctx.L.bbgpu_set_kernel(self.ctx.h, _lib.ptr(k), k.shape[0], k.shape[1]))
+        self._data_set = False
+
+    def _grid(self):
+        return grid_struct(self.setup, self.scalefactor)
+
+    @property
+    def conv(self):
+        return self.cfield
+
+    @property
+    def zstep(self):
+        """ZSTEP_COARSE for a beam whose minor axis is at least ZSTEP_BEAM pixels (``galmod.py:1193-1203``)."""
+        if self.cfield is None:
+            return ZSTEP_FINE
+        h = self.cin.Head()
+        pix = max(self.setup.pixsize) / 60.
+        bmin = min(abs(h.Bmaj()), abs(h.Bmin()))
+        return ZSTEP_COARSE if pix > 0 and bmin / pix >= ZSTEP_BEAM else ZSTEP_FINE
+
+    # ------------------------------------------------------------------------------------------ geometry
+    def box(self, rings, final=False):
+        """Box [blo, bhi) of the cube containing the model (``bbarolo/galmod.py:1224-1240``)."""
+        h = self.cin.Head()
+        ext = rings.radii[-1] + rings.radsep / 2.
+        if final:
+            ext = max(ext, outer_edge(rings, self.ringmode))
+        ext = ext + 3 * float(rings.layer_height()[-1])
+        xdis = int(math.ceil(ext / (abs(h.Cdelt(0)) * self.arcconv)))
+        ydis = int(math.ceil(ext / (abs(h.Cdelt(1)) * self.arcconv)))
+        xpos = int(math.ceil(rings.xpos[-1]))
+        ypos = int(math.ceil(rings.ypos[-1]))
+        blo = [max(xpos - xdis, 0), max(ypos - ydis, 0)]
+        bhi = [min(xpos + xdis + 1, self.cin.DimX()), min(ypos + ydis + 1, self.cin.DimY())]
+        return blo, bhi
+
+    # ------------------------------------------------------------------------------------------ models
+    def galmod_mc(self, out, sr, ring_lo, ring_hi, seed, nv, blo, bhi):
+        """``_galmod_mc`` on the device: out (by, bx, nz) float64 accumulated (``bbarolo/galmod.py:92-171``)."""
+        sr = np.ascontiguousarray(sr, np.float64)
+        nv = np.ascontiguousarray(nv, np.int64)
+        assert out.dtype == np.float64 and out.flags.c_contiguous
+        self.ctx.check(self.ctx.L.bbgpu_galmod_mc(self.ctx.h, _lib.ptr(out), _lib.ptr(sr), sr.shape[1],
+                                                  int(ring_lo), int(ring_hi), int(seed) & 0xFFFFFFFFFFFFFFFF,
+                                                  _lib.ptr(nv), int(blo[0]), int(blo[1]), int(bhi[0]), int(bhi[1])))
+        return out
+
+    def build(self, rings, blo=(0, 0), bhi=None, seed=None, galmodtype=None, layout="zyx"):
+        """The non-convolved model of rings (used as nodes) in [blo, bhi) (``GalmodSetup.build``)."""
+        st = self.setup
+        if bhi is None:
+            bhi = (st.dimx, st.dimy)
+        gtype = (galmodtype or st.galmodtype).upper()
+        sr, nv = st.subrings(rings)
+        out = np.zeros((bhi[1] - blo[1], bhi[0] - blo[0], st.nsubs))
+        if sr.shape[1]:
+            if gtype == "ANALYTIC":
+                nzq = 1 if not np.any(sr[6] > 0) else ZSAMPLES_MAX
+                self.ctx.check(self.ctx.L.bbgpu_galmod_analytic(self.ctx.h, _lib.ptr(out), _lib.ptr(sr), sr.shape[1],
+                                                                0, sr.shape[1], nzq, int(blo[0]), int(blo[1]),
+                                                                int(bhi[0]), int(bhi[1])))
+            else:
+                s = seed32(st.iseed if seed is None else seed)
+                self.galmod_mc(out, sr, 0, sr.shape[1], s, nv, blo, bhi)
+        if layout == "zyx":
+            return np.ascontiguousarray(out.transpose(2, 0, 1))
+        return out
+
+    def array(self, rings, blo=None, bhi=None, final=True, ringmode=None, seed=None, galmodtype=None,
+              layout="zyx", support=None, threads=None):
+        """The model of the rings, convolved with the beam if smoothing is on (``bbarolo/galmod.py:1242-1271``).
+        The device builds one model per call, so ``threads`` has no effect (the reference's THREADS>1 final
+        models use one stream per thread chunk; this path reproduces THREADS=1)."""
+        if blo is None or bhi is None:
+            blo, bhi = (0, 0), (self.cin.DimX(), self.cin.DimY())
+        if final:
+            rings = model_rings(rings, self.ringmode if ringmode is None else ringmode, self.setup.radsep)
+        mod = self.build(rings, blo, bhi, seed=seed, galmodtype=galmodtype, layout="yxz")
+        if self.cfield is not None:
+            if final:
+                return self.convolve(mod, layout)
+            out = np.zeros_like(mod)
+            k = np.ascontiguousarray(self.cfield, np.float64)
+            self.ctx.check(self.ctx.L.bbgpu_conv_sparse(self.ctx.h, _lib.ptr(mod), _lib.ptr(out), *mod.shape,
+                                                        _lib.ptr(k), k.shape[0], k.shape[1], float(self.scalefactor)))
+            mod = out
+        if layout == "zyx":
+            return np.ascontiguousarray(mod.transpose(2, 0, 1))
+        return mod
+
+    def convolve(self, mod, layout="zyx", workers=1):
+        """A dense model (ny, nx, nz) convolved with the beam, values below 1e-12 set to zero, times the scale
+        factor (``bbarolo/galmod.py:1273-1283``), as (nz, ny, nx) or (ny, nx, nz) with layout='yxz'."""
+        if self.cfield is None:
+            return np.ascontiguousarray(mod.transpose(2, 0, 1) if layout == "zyx" else mod.copy())
+        a = np.ascontiguousarray(np.asarray(mod, np.float64).transpose(2, 0, 1))
+        out = np.empty_like(a)
+        self.ctx.check(self.ctx.L.bbgpu_convolve(self.ctx.h, _lib.ptr(a), _lib.ptr(out), *a.shape,
+                                                 float(self.scalefactor), 1))
+        return out if layout == "zyx" else np.ascontiguousarray(out.transpose(1, 2, 0))
+
+    def convolve_planes(self, planes, threshold=False, scale=1.0):
+        """The "same" convolution of a stack (n, ny, nx) (``FFTConvolver.__call__``, bbarolo/smooth.py:145)."""
+        a = np.ascontiguousarray(planes, np.float64)
+        if a.ndim == 2:
+            return self.convolve_planes(a[None], threshold, scale)[0]
+        out = np.empty_like(a)
+        self.ctx.check(self.ctx.L.bbgpu_convolve(self.ctx.h, _lib.ptr(a), _lib.ptr(out), *a.shape, float(scale),
+                                                 1 if threshold else 0))
+        return out
+
+    def model_rows(self, rows, proto, ringmode=None):
+        """Ring-value rows (B, 17, nr) of ring sets like ``proto`` -> the rows of their model rings (with the
+        ring convention) and the model-ring prototype."""
+        mode = self.ringmode if ringmode is None else ringmode_name(ringmode)
+        probe = proto.copy()
+        probe.radii = np.asarray(proto.radii, float)
+        mr = model_rings(probe, mode, self.setup.radsep)
+        if mr is probe:
+            return np.asarray(rows, float), probe
+        # the model rings repeat the first/last ring (CENTRED) or shift the end radii (SHIFTED)
+        idx = []
+        for r in mr.radii:
+            j = np.flatnonzero(np.asarray(proto.radii) == r)
+            idx.append(int(j[0]) if j.size else -1)
+        nr = proto.nr
+        if idx and idx[0] == -1:
+            idx[0] = 0
+        if idx and idx[-1] == -1:
+            idx[-1] = nr - 1
+        if any(i < 0 for i in idx):
+            raise ValueError("model_rows: ring convention not representable")
+        out = np.asarray(rows, float)[:, :, idx].copy()
+        out[:, 0, :] = mr.radii
+        return out, mr
+
+
+class BatchLikelihood:
+    """The Gaussian log-likelihood of ``LikelihoodMixin._log_likelihood`` for batches of ring sets.
+
+    data (nz, ny, nx) float32, likemask (nz, ny, nx) bool (the voxels of the likelihood), maskmode 2 (only the
+    voxels in the mask, the default of Bayesian3DFIT) or 1 (data * mask) or 0; region (ny, nx) bool or None;
+    sigma (noise per voxel); likefactor (the noise-correlation factor); likebox ([blo], [bhi]) the likelihood
+    region's box (default the cube). For each ring set: -likefactor * (0.5 (ss + ss_out) / sigma^2 +
+    0.5 nvox log(2 pi sigma^2)), ss over the model box on the device, ss_out (the data outside the box) from a
+    summed-area table (``likelihood.py:437-440``), fracerr eps optional (``likelihood.py:512-531``)."""
+
+    def __init__(self, model, data, likemask=None, maskmode=2, region=None, sigma=1.0, likefactor=1.0,
+                 likebox=None, fracerr=None, nvox=None):
+        self.model = model
+        d = np.ascontiguousarray(data, np.float32)
+        nz, ny, nx = d.shape
+        self.shape = d.shape
+        self.maskmode = int(maskmode) if likemask is not None else 0
+        self.mask = None if likemask is None else np.ascontiguousarray(likemask, dtype=bool)
+        self.region = None if region is None else np.ascontiguousarray(region, dtype=bool)
+        self.sigma = float(sigma)
+        self.likefactor = float(likefactor)
+        self.eps = None if fracerr is None else float(fracerr)
+        self.likebox = likebox if likebox is not None else ([0, 0], [nx, ny])
+        ctx = model.ctx
+        mk = None if self.mask is None else self.mask.view(np.uint8)
+        rg = None if self.region is None else self.region.view(np.uint8)
+        ctx.check(ctx.L.bbgpu_set_cube(ctx.h, _lib.ptr(d), _lib.ptr(mk), _lib.ptr(rg)))
+        # the data of the likelihood (the rule of _sumsq_residuals), its squares per pixel and their count
+        valid = np.isfinite(d) & (d != 0)
+        dd = np.where(valid, d, 0.).astype(np.float64)
+        if self.maskmode == 2:
+            valid &= self.mask
+        elif self.maskmode == 1:
+            dd = np.where(self.mask, dd, 0.)
+        if self.region is not None:
+            valid &= self.region[None]
+        dm2 = np.where(valid, dd * dd, 0.).sum(axis=0)
+        self._dm2_sat = np.zeros((ny + 1, nx + 1))
+        self._dm2_sat[1:, 1:] = dm2.cumsum(0).cumsum(1)
+        Lb, Hb = self.likebox
+        self._dm2_box = self._boxsum(Lb, Hb)
+        self.nvox = int(valid[:, Lb[1]:Hb[1], Lb[0]:Hb[0]].sum()) if nvox is None else int(nvox)
+
+    def _boxsum(self, blo, bhi):
+        S = self._dm2_sat
+        return float(S[bhi[1], bhi[0]] - S[blo[1], bhi[0]] - S[bhi[1], blo[0]] + S[blo[1], blo[0]])
+
+    def model_box(self, rings):
+        blo, bhi = self.model.box(rings, final=True)
+        Lb, Hb = self.likebox
+        blo = [max(blo[0], Lb[0]), max(blo[1], Lb[1])]
+        bhi = [max(min(bhi[0], Hb[0]), blo[0]), max(min(bhi[1], Hb[1]), blo[1])]
+        return blo, bhi
+
+    def prepare(self, rows, proto, seed=None):
+        """Host side of a batch: sub-ring tables, boxes and descriptors of the ring-value rows (B, 17, nr)."""
+        dm = self.model
+        mrows, mr = dm.model_rows(rows, proto)
+        sr, nv = subrings_batch(dm.setup, mr, mrows)
+        B = sr.shape[0]
+        descs = np.zeros(B, _lib.EVAL_DTYPE)
+        s = seed32(dm.setup.iseed if seed is None else seed)
+        boxes = []
+        r = proto.copy()
+        for k in range(B):
+            for j, key in enumerate(RING_KEYS):
+                setattr(r, key, rows[k, j])
+            blo, bhi = self.model_box(r)
+            boxes.append((blo, bhi))
+            descs[k] = (blo[0], blo[1], bhi[0], bhi[1], s, self.maskmode, 1 if self.region is not None else 0,
+                        self.sigma ** 2, (self.eps or 0.) ** 2)
+        return sr, nv, descs, boxes
+
+    def evaluate(self, rows, proto, seed=None, galmodtype=None):
+        """log L of each ring set (rows (B, 17, nr) in RING_KEYS order, radii and options as proto)."""
+        sr, nv, descs, boxes = self.prepare(rows, proto, seed)
+        ss, lg = self.run(sr, nv, descs, galmodtype)
+        return self.finish(ss, lg, boxes)
+
+    def run(self, sr, nv, descs, galmodtype=None):
+        dm = self.model
+        gt = (galmodtype or dm.setup.galmodtype).upper()
+        B, _, nsub = sr.shape
+        ss = np.zeros(B)
+        lg = np.zeros(B)
+        ctx = dm.ctx
+        ctx.check(ctx.L.bbgpu_eval_batch(ctx.h, _lib.ANALYTIC if gt == "ANALYTIC" else _lib.MC, B, nsub,
+                                         _lib.ptr(sr), _lib.ptr(nv), _lib.ptr(descs), _lib.ptr(ss), _lib.ptr(lg)))
+        return ss, lg
+
+    def finish(self, ss, lg, boxes):
+        s2 = self.sigma ** 2
+        out = np.empty(len(ss))
+        for k, (blo, bhi) in enumerate(boxes):
+            ss_out = max(self._dm2_box - self._boxsum(blo, bhi), 0.)
+            if self.eps is not None and self.eps > 0:
+                res = 0.5 * (ss[k] + ss_out / s2) + 0.5 * self.nvox * math.log(2. * math.pi * s2) + 0.5 * lg[k]
+            else:
+                res = 0.5 * (ss[k] + ss_out) / s2 + 0.5 * self.nvox * math.log(2. * math.pi * s2)
+            out[k] = -self.likefactor * res
+        return out

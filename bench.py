@@ -1,0 +1,290 @@
+"""Benchmark: GALMOD + beam + log L evaluations per second on the 160x160x128 GLOBAL workload.
+
+One step = one batch of likelihood evaluations of the GLOBAL 3DFIT problem (40 rings, VROT VDISP INC PA free
+per ring: the base parameters and one step of each of the 160 free parameters, 161 evaluations), each a full
+Monte-Carlo GALMOD model in its box, its beam convolution (30"x20" beam, 13x9 kernel) and the masked residual
+reduced to log L. Synthetic mock data (no public dataset): the model of the rings plus beam-correlated noise
+(sigma 0.5% of the peak), likelihood voxels the 3-sigma mask of the noise-free model dilated by one beam and
++-3 channels.
+
+  value  device throughput with the batch resident in HBM (bbgpu_eval_run), evaluations / s;
+  e2e    the same through the C ABI from host arrays: ring values -> sub-ring tables (host) -> upload ->
+         device -> download of the sums -> log L, evaluations / s.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--batch B] [--impl reference]
+Under torchrun (N > 1) each rank evaluates its own batch on its GPU (replicas: the evaluations are independent),
+the time is the max over ranks and value the evaluations of all ranks / that time.
+"""
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "GALMOD+beam+logL evals/s (160x160x128 f32)"
+UNIT = "evals/s"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), float(p["bf16_tflops"]), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.p = None
+        self.path = os.path.join("/tmp", f"bb_clocks_{os.getpid()}.csv")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(5)
+        except Exception:
+            self.p.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def workload(batch):
+    """The device model, likelihood and one batch of ring-value rows (base + one step per free parameter)."""
+    from bbarolo2_gb300 import configs, engine
+    from bbarolo2_gb300.galmod import ring_rows_batch
+    from scipy import ndimage
+    cube, rings = configs.global160(galmodtype="MC")
+    dm = engine.DiskModel(cube)
+    truth = dm.array(rings, seed=1)
+    rms = 0.005 * float(truth.max())
+    g = np.random.default_rng(1)
+    noise = dm.convolve_planes(g.normal(0., rms, truth.shape))
+    noise *= rms / np.std(noise)
+    data = (truth + noise).astype(np.float32)
+    h = cube.Head()
+    rad = abs(h.Bmaj() / h.Cdelt(1))
+    yy, xx = np.mgrid[-int(rad) - 1:int(rad) + 2, -int(rad) - 1:int(rad) + 2]
+    disk = (xx * xx + yy * yy) <= rad * rad
+    mask = ndimage.binary_dilation(truth > 3 * rms, structure=disk[None])
+    mask = ndimage.binary_dilation(mask, structure=np.ones((7, 1, 1), bool))
+    L = engine.BatchLikelihood(dm, data, mask, maskmode=2, sigma=rms)
+    base = ring_rows_batch([rings])[0]
+    rows = np.repeat(base[None], batch, axis=0)
+    free = [(4, 2.0), (5, 0.5), (12, 0.5), (13, 0.5)]       # vrot, vdisp, inc, phi steps
+    k = 1
+    for j in range(rings.nr):
+        for row, step in free:
+            if k < batch:
+                rows[k, row, j] += step
+                k += 1
+    return dm, L, rings, rows, data, mask
+
+
+def algorithmic(dm, L, sr, nv, descs):
+    """Algorithmic bytes / flops per launch of the kernels (summed over the batch)."""
+    st = dm.setup
+    nz = st.nsubs
+    ky, kx = dm.cfield.shape
+    taps = int(np.count_nonzero(dm.cfield))
+    vox = sum((int(d["bhi0"]) - int(d["blo0"])) * (int(d["bhi1"]) - int(d["blo1"])) * nz for d in descs)
+    # MC: per member, the velocity samples read (4 B each), the clouds (16 B), the model written (4 B/voxel)
+    from bbarolo2_gb300.galmod import cloud_counts
+    ncl, nsubcl = cloud_counts(st, sr[0], nv[0])
+    B = len(descs)
+    mc_bytes = B * (4 * nsubcl + 16 * ncl) + 4 * vox
+    conv_flops = 2.0 * taps * vox
+    conv_bytes = 4 * vox * 2 + vox // 1        # model read + data read (+ mask folded in the data)
+    return dict(mc_deposit=("hbm", mc_bytes), conv_resid=("tensor", conv_flops), conv_bytes=conv_bytes,
+                deposits=B * nsubcl, voxels=vox, taps=taps, kernel=[ky, kx])
+
+
+def cpu_leg(dm, L, rows, rings, data, mask, cores=None, sample=None, steps=1):
+    """The reference algorithm on the host cores (oracle C kernels + scipy FFT), bounded sample."""
+    from oracle import cpu_baseline
+    sr, nv, descs, boxes = L.prepare(rows, rings, seed=1)
+    payload = cpu_baseline.setup_payload(dm, sr, nv, boxes, 1, data, L.mask, L.maskmode)
+    pool = cpu_baseline.Pool(payload, cores)
+    n = sample or min(len(rows), 2 * pool.cores)
+    pool.run(range(min(pool.cores, len(rows))))              # warm-up (FFT plans, caches)
+    vals = []
+    for _ in range(steps):
+        _, wall = pool.run(range(n))
+        vals.append(n / wall)
+    pool.close()
+    return vals, pool.cores, n
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=161)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        return reference_arm(args, world)
+    from bbarolo2_gb300 import _lib, build
+    build.build()
+    dm, L, rings, rows, data, mask = workload(args.batch)
+    ctx = dm.ctx
+    B = rows.shape[0]
+    sr, nv, descs, boxes = L.prepare(rows, rings, seed=1)
+    # ---- device-resident throughput
+    ctx.check(ctx.L.bbgpu_eval_upload(ctx.h, _lib.MC, B, sr.shape[2], _lib.ptr(sr), _lib.ptr(nv), _lib.ptr(descs)))
+    for _ in range(args.warmup):
+        ctx.check(ctx.L.bbgpu_eval_run(ctx.h))
+    ctx.check(ctx.L.bbgpu_sync(ctx.h))
+    clk = Clocks(local)
+    if dist:
+        dist.barrier()
+    l0 = ctx.launches
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.check(ctx.L.bbgpu_eval_run(ctx.h))
+    ctx.check(ctx.L.bbgpu_sync(ctx.h))
+    dt = time.perf_counter() - t0
+    launches = ctx.launches - l0
+    if dist:
+        import torch
+        t = torch.tensor([dt], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dt = float(t.item())
+        dist.barrier()
+    ss = np.zeros(B)
+    lg = np.zeros(B)
+    ctx.check(ctx.L.bbgpu_eval_download(ctx.h, _lib.ptr(ss), _lib.ptr(lg)))
+    value = B * args.steps * world / dt
+    # ---- per-kernel device times (CUDA events on the context's stream)
+    ctx.set_option(_lib.OPT_TIMING, 1)
+    ktimes = {}
+    for _ in range(3):
+        ctx.check(ctx.L.bbgpu_eval_run(ctx.h))
+        for kname, v in ctx.run_times().items():
+            ktimes.setdefault(kname, []).append(v)
+    ctx.set_option(_lib.OPT_TIMING, 0)
+    kt = {k: float(np.median(v)) for k, v in ktimes.items()}
+    # ---- end to end through the C ABI from host arrays
+    for _ in range(max(1, args.warmup // 2)):
+        L.evaluate(rows, rings, seed=1)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        out = L.evaluate(rows, rings, seed=1)
+    te = time.perf_counter() - t0
+    if dist:
+        import torch
+        t = torch.tensor([te], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        te = float(t.item())
+    h2d, d2h = ctx.transfer_bytes()
+    clocks = clk.stop()
+    e2e = B * args.steps * world / te
+    # ---- roofline of the dominant kernel
+    hbm, bf16, src = peaks()
+    alg = algorithmic(dm, L, sr, nv, descs)
+    dom = max(kt, key=kt.get)
+    if dom == "conv_resid":
+        achieved = alg["conv_resid"][1] / (kt[dom] * 1e-3) / 1e12
+        roof = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16,
+                "traffic": None, "kernel": dom, "peak_source": src}
+    else:
+        nbytes = alg["mc_deposit"][1] if dom == "mc_deposit" else alg["conv_bytes"]
+        achieved = nbytes / (kt[dom] * 1e-3) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                "traffic": None, "kernel": dom, "peak_source": src}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (f64 reduction; bit-exact int cloud indices)", "data": "synthetic",
+            "config": {"workload": "global160: GLOBAL 3DFIT 160x160x128, 40 rings, MC GALMOD, 13x9 beam, batch of "
+                                   f"{B} (base + 160 parameter steps)", "batch": B, "galmodtype": "MC",
+                       "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (per-batch models 2 GB)",
+                       "flux_normalisation": "fixed density profile (not re-deconvolved per evaluation)"},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches, "kernel_ms": kt, "roofline": roof, "clocks": clocks,
+            "logL_sample": [float(out[0]), float(out[1])]}
+    if rank == 0 and not args.no_cpu:
+        vals, cores, n = cpu_leg(dm, L, rows, rings, data, mask)
+        line["cpu_baseline"] = {"value": float(np.median(vals)), "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": f"{n} evaluations of the batch, one per process (C restatement of the "
+                                          "numba kernels + scipy FFT convolution)"}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def reference_arm(args, world):
+    """The reference's CPU evaluation (its kernels restated in C + its FFT convolution) on the host cores."""
+    from bbarolo2_gb300 import build
+    build.build()
+    dm, L, rings, rows, data, mask = workload(args.batch)
+    vals, cores, n = cpu_leg(dm, L, rows, rings, data, mask, steps=max(1, args.steps // 10))
+    v = float(np.median(vals))
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": len(vals), "warmup": 1,
+            "ms_per_step": 1e3 * n / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": "global160: GLOBAL 3DFIT 160x160x128, 40 rings, MC GALMOD, 13x9 beam",
+                       "batch": n, "galmodtype": "MC"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{n} evaluations per step, one per process"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,149 @@
+/*
+ * bbgpu: the C ABI of the GB300 (sm_103a) model-evaluation path of BBarolo 2's 3DFIT.
+ *
+ * Plain C types only (pointers, sizes, doubles). Every function returns an int status (BBGPU_OK = 0, or a
+ * negative code; bbgpu_last_error() gives the message of the last failure of the context) and never throws
+ * or aborts. Host arrays are caller-owned and C-contiguous; device buffers are owned by the context.
+ *
+ * Reference interfaces replaced (paths within the reference project):
+ *   bbgpu_galmod_mc           <- _galmod_mc(out, sr, ring_lo, ring_hi, seed, radsep, nv, ...)   bbarolo/galmod.py:92-95
+ *   bbgpu_galmod_analytic     <- _galmod_analytic(out, sr, ring_lo, ring_hi, ...)                bbarolo/galmod.py:326-329
+ *   bbgpu_ring_maps_analytic  <- _ring_maps_analytic(out, sr, widx, wval, ...)                   bbarolo/galmod.py:468-470
+ *   bbgpu_convolve            <- FFTConvolver.__call__(data, workers) + the threshold and scale of
+ *                                DiskModel.convolve(mod, layout, workers)                          bbarolo/smooth.py:145, bbarolo/galmod.py:1273
+ *   bbgpu_conv_sparse         <- _conv_sparse(model, kern, scale)                                 bbarolo/galmod.py:974-975
+ *   bbgpu_sumsq_residuals     <- _sumsq_residuals(model, data, mask, maskmode, region)            bbarolo/bayesian/likelihood.py:22-23
+ *   bbgpu_residuals_fracerr   <- _residuals_fracerr(model, data, mask, maskmode, region, s2, e2)  bbarolo/bayesian/likelihood.py:48-49
+ *   bbgpu_norm                <- _norm(model, data, mask, blo0, blo1, x0, y0, phi, inc, ...)      bbarolo/galfit.py:39-41
+ *   bbgpu_eval_*              <- LikelihoodMixin._log_likelihood(theta) for a batch of theta:
+ *                                DiskModel.array -> convolve -> _calculate_residuals             bbarolo/bayesian/likelihood.py:567-619
+ *
+ * Layouts follow the reference: sub-ring tables sr (16, nsub) float64 in internal units (row order of
+ * GalmodSetup.subrings, bbarolo/galmod.py:761-851); models (ny, nx, nz) float64 ("yxz"); cubes (nz, ny, nx).
+ */
+#ifndef BBGPU_H
+#define BBGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    BBGPU_OK = 0,
+    BBGPU_ERR_ARG = -1,       /* invalid argument (shape, size, null pointer, unsupported option) */
+    BBGPU_ERR_CUDA = -2,      /* a CUDA runtime call failed */
+    BBGPU_ERR_NOMEM = -3,     /* device or host allocation failed */
+    BBGPU_ERR_STATE = -4,     /* call out of order (e.g. evaluation before bbgpu_set_grid) */
+    BBGPU_ERR_KERNEL = -5     /* a kernel reported an inconsistency (its error flag) */
+};
+
+enum { BBGPU_MC = 0, BBGPU_ANALYTIC = 1 };
+
+typedef struct bbgpu_ctx bbgpu_ctx;
+
+/* The header-derived constants of a cube (GalmodSetup, bbarolo/galmod.py:613-725). */
+typedef struct {
+    int nx, ny, nz;           /* cube dimensions */
+    int nlines;               /* number of emission lines (lfreq0, relint) */
+    int axtyp, velsys;        /* spectral axis: 2 wave, 3 freq, 4 velocity; 1 radio, 2 optical, 3 relativistic */
+    int ltype, cmode;         /* vertical layer (1..5), cloud-number mode (0..2) */
+    double radsep, cdens, pixarea, cdelt0, cdelt1, crota2, sig_instr;
+    double crval3, cdelt3, crpix3;
+    double chwidth;           /* narrowest channel in velocity (GalmodSetup._chmin): ANALYTIC line windows */
+    double zstep;             /* vertical sample spacing of the ANALYTIC models (pixels) */
+    double scalefactor;       /* flux scale of the convolution (1 for DENSFLUX) */
+} bbgpu_grid;
+
+/* One evaluation of a batch: the model of one sub-ring table in a box, convolved, compared with the cube. */
+typedef struct {
+    int32_t blo0, blo1, bhi0, bhi1;   /* model box [blo, bhi) in pixels (x, y) */
+    uint64_t seed;            /* MC stream seed (ISEED & 0xFFFFFFFF) */
+    int32_t maskmode;         /* residual mode: 0 all voxels, 1 data*mask, 2 voxels in the mask only */
+    int32_t use_region;       /* 1: skip the pixels outside the region set with bbgpu_set_cube */
+    double sigma2;            /* noise variance (fracerr mode) */
+    double eps2;              /* fractional model error squared; 0: plain sum of squares */
+} bbgpu_eval_desc;
+
+/* ---- context ---------------------------------------------------------------------------------------- */
+int bbgpu_ctx_create(bbgpu_ctx **out, int device);
+int bbgpu_ctx_destroy(bbgpu_ctx *ctx);
+const char *bbgpu_last_error(const bbgpu_ctx *ctx);
+int bbgpu_version(void);
+
+/* ---- set-up (once per cube / kernel) ------------------------------------------------------------------ */
+/* cd2i (nz), lfreq0 (nlines), relint (nlines), vedges (nlines, nz+1) velocity channel edges per line. */
+int bbgpu_set_grid(bbgpu_ctx *ctx, const bbgpu_grid *g, const double *cd2i, const double *lfreq0,
+                   const double *relint, const double *vedges);
+/* Beam kernel (ky, kx) float64 (bbarolo/smooth.py:62-88); ky, kx odd, at most 63 x 63. */
+int bbgpu_set_kernel(bbgpu_ctx *ctx, const double *kernel, int ky, int kx);
+/* Cube data (nz, ny, nx) float32, mask (nz, ny, nx) uint8 or NULL, region (ny, nx) uint8 or NULL. */
+int bbgpu_set_cube(bbgpu_ctx *ctx, const float *data, const uint8_t *mask, const uint8_t *region);
+
+/* ---- reference-kernel entry points (one model per call; host arrays in and out) ------------------------ */
+/* out (bhi1-blo1, bhi0-blo0, nz) float64 is ACCUMULATED (out +=), as the reference kernels. */
+int bbgpu_galmod_mc(bbgpu_ctx *ctx, double *out, const double *sr, int nsub, int ring_lo, int ring_hi,
+                    uint64_t seed, const int64_t *nv, int blo0, int blo1, int bhi0, int bhi1);
+int bbgpu_galmod_analytic(bbgpu_ctx *ctx, double *out, const double *sr, int nsub, int ring_lo, int ring_hi,
+                          int nzq, int blo0, int blo1, int bhi0, int bhi1);
+/* out (nr, bhi1-blo1, bhi0-blo0) float64 accumulated; widx (nsub, 2) int64 (-1: none), wval (nsub, 2). */
+int bbgpu_ring_maps_analytic(bbgpu_ctx *ctx, double *out, int nr, const double *sr, int nsub,
+                             const int64_t *widx, const double *wval, int nzq, int blo0, int blo1, int bhi0,
+                             int bhi1);
+/* "same" convolution of each plane of in (nz, ny, nx) float64 with the kernel; threshold != 0: values
+ * below 1e-12 set to zero, then x scale (DiskModel.convolve); out (nz, ny, nx) float64. */
+int bbgpu_convolve(bbgpu_ctx *ctx, const double *in, double *out, int nz, int ny, int nx, double scale,
+                   int threshold);
+/* model (ny, nx, nz) float64 -> out (ny, nx, nz) float64 (bbarolo/galmod.py:974-1037). */
+int bbgpu_conv_sparse(bbgpu_ctx *ctx, const double *model, double *out, int ny, int nx, int nz,
+                      const double *kernel, int ky, int kx, double scale);
+/* model (nz, ny, nx) float64, data float32 and mask uint8 of the same shape, region (ny, nx) or NULL. */
+int bbgpu_sumsq_residuals(bbgpu_ctx *ctx, const double *model, const float *data, const uint8_t *mask,
+                          int maskmode, const uint8_t *region, int nz, int ny, int nx, double *out);
+int bbgpu_residuals_fracerr(bbgpu_ctx *ctx, const double *model, const float *data, const uint8_t *mask,
+                            int maskmode, const uint8_t *region, int nz, int ny, int nx, double sigma2,
+                            double eps2, double *out2);
+/* CLASSIC normalisation + residual; model (bsy, bsx, nz) float64 is multiplied by the factor in place;
+ * data float32 and mask uint8 (dny, dnx, nz) ("yxz"); pre (bsy, bsx, nz) or NULL (MC support emulation);
+ * ilo, ihi (ky) int64; thr (nz). Result in *out. */
+int bbgpu_norm(bbgpu_ctx *ctx, double *model, int bsy, int bsx, int nz, const float *data, const uint8_t *mask,
+               int dny, int dnx, int64_t blo0, int64_t blo1, double x0, double y0, double phi, double inc,
+               double r1, double r2, double wpow, int side, int ftype, const double *chan_noise,
+               double data_noise, double bweight, int normtype, const double *pre, const int64_t *ilo,
+               const int64_t *ihi, int ky, const double *thr, int foot, double hmax, double *out);
+
+/* ---- batched likelihood path ------------------------------------------------------------------------- */
+/* A batch of nb evaluations of the same sub-ring count nsub: sr (nb, 16, nsub) float64, nv (nb, nsub) int64,
+ * descs (nb). The GALMOD model (galmodtype), the beam convolution (if a kernel is set), the threshold and
+ * scale, and the residual over the box are computed on the device; ss (nb) receives the sum of squares
+ * (fracerr: the variance-weighted sum) and lg (nb, may be NULL) the sum of log(v / sigma2).
+ * bbgpu_eval_upload copies the batch to the device, bbgpu_eval_run computes it on the device (inputs
+ * resident), bbgpu_eval_download copies the results; bbgpu_eval_batch does the three. */
+int bbgpu_eval_upload(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const double *sr, const int64_t *nv,
+                      const bbgpu_eval_desc *descs);
+int bbgpu_eval_run(bbgpu_ctx *ctx);
+int bbgpu_eval_download(bbgpu_ctx *ctx, double *ss, double *lg);
+int bbgpu_eval_batch(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const double *sr, const int64_t *nv,
+                     const bbgpu_eval_desc *descs, double *ss, double *lg);
+/* The smoothed (or unsmoothed, smoothed = 0) model of member k of the last batch run: (by, bx, nz) float32. */
+int bbgpu_eval_model(bbgpu_ctx *ctx, int k, int smoothed, float *out, int by, int bx, int nz);
+/* Synchronise the context's stream. */
+int bbgpu_sync(bbgpu_ctx *ctx);
+/* Options: 1 keep the smoothed models of a batch (for bbgpu_eval_model), 2 time the kernels of each run. */
+int bbgpu_set_option(bbgpu_ctx *ctx, int option, int value);
+
+/* ---- counters --------------------------------------------------------------------------------------- */
+/* Kernel launches issued by the context so far, and the device time (ms) of the last bbgpu_eval_run split
+ * into its kernels: times[0..n) in the order of bbgpu_kernel_name(i). */
+int64_t bbgpu_launch_count(const bbgpu_ctx *ctx);
+int bbgpu_last_run_times(const bbgpu_ctx *ctx, double *times, int n);
+const char *bbgpu_kernel_name(int i);
+/* Bytes copied host -> device and device -> host by the last bbgpu_eval_upload / bbgpu_eval_download. */
+int bbgpu_transfer_bytes(const bbgpu_ctx *ctx, int64_t *h2d, int64_t *d2h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BBGPU_H */

@@ -1,0 +1,762 @@
+/*
+ * CPU restatement of BBarolo 2's model-evaluation kernels: the ORACLE of the GPU path.
+ *
+ * This file is test infrastructure. Only the tests, the smoke check and the CPU-baseline leg of the
+ * benchmark load it, as the checker; the product never links or calls it.
+ *
+ * Each function restates, in plain C with the reference's operation order (compile with
+ * -ffp-contract=off: no fused multiply-adds, so every operation rounds as in the reference's float64),
+ * the numba kernel cited beside it. The reference runs these kernels through numba, whose math
+ * functions are the C library's (exp, log, sin, cos, sqrt, atanh, tan, erf, erfc, tanh, atan): the same
+ * functions are called here.
+ *
+ * Pinned against the reference itself: the golden fixtures under tests/golden/ were produced by running
+ * the reference's Python kernels (bbarolo/_rng.py, bbarolo/galmod.py, bbarolo/smooth.py,
+ * bbarolo/galfit.py, bbarolo/bayesian/likelihood.py) and the CPU tests check this file against them.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define C_MS 2.99792458e08
+
+/* ------------------------------------------------------------------ RNG (bbarolo/_rng.py) */
+static int64_t KN[128];
+static double WN[128], FN[128];
+static int zig_ready = 0;
+
+/* bbarolo/_rng.py:17-38 */
+static void zig_tables(void) {
+    double dn = 3.442619855899, tn = dn, vn = 9.91256303526217e-3, m1 = 2147483648.0;
+    double q = vn / exp(-.5 * dn * dn);
+    KN[0] = (int64_t)((dn / q) * m1);
+    KN[1] = 0;
+    WN[0] = q / m1;
+    WN[127] = dn / m1;
+    FN[0] = 1.;
+    FN[127] = exp(-.5 * dn * dn);
+    for (int i = 126; i >= 1; i--) {
+        dn = sqrt(-2. * log(vn / dn + exp(-.5 * dn * dn)));
+        KN[i + 1] = (int64_t)((dn / tn) * m1);
+        tn = dn;
+        FN[i] = exp(-.5 * dn * dn);
+        WN[i] = dn / m1;
+    }
+    zig_ready = 1;
+}
+
+void ref_zig_tables(int64_t *kn, double *wn, double *fn) {
+    if (!zig_ready) zig_tables();
+    memcpy(kn, KN, sizeof KN); memcpy(wn, WN, sizeof WN); memcpy(fn, FN, sizeof FN);
+}
+
+static inline uint64_t rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+/* bbarolo/_rng.py:49-63 (splitmix64) */
+void ref_rng_init(uint64_t seed, uint64_t *s) {
+    uint64_t z = seed + 0x9E3779B97F4A7C15ULL;
+    for (int i = 0; i < 2; i++) {
+        z = z + 0x9E3779B97F4A7C15ULL;
+        uint64_t x = z;
+        x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+        x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+        x = x ^ (x >> 31);
+        s[i] = x;
+    }
+    if (s[0] == 0 && s[1] == 0) s[0] = 1;
+}
+
+/* bbarolo/_rng.py:66-74 (xoroshiro128+) */
+uint64_t ref_rng_next(uint64_t *s) {
+    uint64_t s0 = s[0], s1 = s[1], r = s0 + s1;
+    s1 ^= s0;
+    s[0] = rotl(s0, 24) ^ s1 ^ (s1 << 16);
+    s[1] = rotl(s1, 37);
+    return r;
+}
+
+/* bbarolo/_rng.py:77-80 */
+double ref_rng_uniform(uint64_t *s) { return (double)(ref_rng_next(s) >> 11) * (1.0 / 9007199254740992.0); }
+
+/* bbarolo/_rng.py:83-100 (Marsaglia & Tsang ziggurat) */
+double ref_rng_normal(uint64_t *s) {
+    if (!zig_ready) zig_tables();
+    for (;;) {
+        int64_t hz = (int64_t)(ref_rng_next(s) >> 32) - 2147483648LL;
+        int64_t iz = hz & 127;
+        int64_t ahz = hz < 0 ? -hz : hz;
+        if (ahz < KN[iz]) return (double)hz * WN[iz];
+        double x = (double)hz * WN[iz];
+        if (iz == 0) {
+            double xx, yy;
+            for (;;) {
+                xx = -log(1.0 - ref_rng_uniform(s)) * 0.2904764;
+                yy = -log(1.0 - ref_rng_uniform(s));
+                if (yy + yy >= xx * xx) break;
+            }
+            return hz > 0 ? 3.442620 + xx : -3.442620 - xx;
+        }
+        if (FN[iz] + ref_rng_uniform(s) * (FN[iz - 1] - FN[iz]) < exp(-.5 * x * x)) return x;
+    }
+}
+
+/* ------------------------------------------------------------------ helpers (bbarolo/galmod.py:38-89) */
+static inline int64_t lround_ref(double x) {
+    if (!(fabs(x) < 1e18)) return -((int64_t)1 << 62);
+    if (x >= 0) return (int64_t)(x + 0.5);
+    return -(int64_t)(-x + 0.5);
+}
+
+static inline double velgrid(double v, int axtyp, int velsys, double freq0, double crval3, double cdelt3,
+                             double crpix3) {
+    double w;
+    if (axtyp == 4) w = v;
+    else {
+        if (velsys == 1) w = freq0 * (1 - v / C_MS);
+        else if (velsys == 2) w = freq0 * (C_MS / (C_MS + v));
+        else w = freq0 * sqrt((C_MS - v) / (C_MS + v));
+        if (axtyp == 2) w = C_MS / w;
+    }
+    return (w - crval3) / cdelt3 + crpix3 - 1;
+}
+
+static inline double lagged(double vrot, double dvdz, double dz) {
+    double v = vrot - dvdz * dz;
+    if (vrot >= 0.0) return (0.0 > v) ? 0.0 : v;
+    return (0.0 < v) ? 0.0 : v;
+}
+
+static inline double fdev(int ltype, uint64_t *st) {
+    if (ltype == 1) return ref_rng_normal(st);
+    double x = 2.0 * ref_rng_uniform(st) - 1.0;
+    if (ltype == 2) return atanh(x);
+    if (ltype == 3) return x >= 0.0 ? -log(x) : log(-x);
+    if (ltype == 4) return tan(0.5 * M_PI * x);
+    return x;
+}
+
+#define SR(row, ir) sr[(size_t)(row) * nsub + (ir)]
+
+/* ------------------------------------------------------------------ _galmod_mc (bbarolo/galmod.py:92-171)
+ * out: (ny, nx, nz) float64, accumulated. sr: (16, nsub). */
+void ref_galmod_mc(double *out, int ny, int nx, int nz, const double *sr, int nsub, int ring_lo, int ring_hi,
+                   uint64_t seed, double radsep, const int64_t *nv, double cdens, int cmode, double pixarea,
+                   double cdelt0, double cdelt1, double crota2, int64_t blo0, int64_t blo1, int64_t bhi0,
+                   int64_t bhi1, int ltype, double sig_instr, int axtyp, int velsys, int nlines,
+                   const double *lfreq0, double crval3, double cdelt3, double crpix3, const double *relint,
+                   const double *cd2i) {
+    (void)ny;
+    uint64_t st[2];
+    ref_rng_init(seed, st);
+    int linear = axtyp == 4 && nlines == 1;
+    double ia = 1.0 / cdelt3;
+    double ib = -crval3 / cdelt3 + crpix3 - 1;
+    for (int ir = ring_lo; ir < ring_hi; ir++) {
+        double R0 = SR(0, ir), dens = SR(5, ir);
+        if (dens == 0) continue;
+        double ring_area_pix = 2 * M_PI * R0 * radsep / pixarea;
+        double dpow = cmode == 1 ? pow(dens, 1.0) : pow(dens, (double)cmode);
+        int64_t nc = lround_ref(cdens * dpow * ring_area_pix);
+        if ((double)lround_ref((double)nc / ring_area_pix) < 10.) nc = lround_ref(10 * ring_area_pix);
+        double vrot = SR(1, ir), vrad = SR(2, ir), vvert = SR(3, ir);
+        double vdisptmp = sqrt(SR(4, ir) * SR(4, ir) + sig_instr * sig_instr);
+        double z0 = SR(6, ir), dvdz = SR(7, ir), zcyl = SR(8, ir);
+        double sinc = sin(SR(9, ir)), cinc = cos(SR(9, ir));
+        double phi = SR(10, ir);
+        double spa = sin(phi) * cos(crota2) + cos(phi) * sin(crota2);
+        double cpa = cos(phi) * cos(crota2) - sin(phi) * sin(crota2);
+        double xpos = SR(11, ir), ypos = SR(12, ir), vsys0 = SR(13, ir);
+        int64_t nvr = nv[ir];
+        double fluxsc = (double)(float)(dens * ring_area_pix * pixarea / (double)(nc * nvr));
+        double r_inner = R0 - 0.5 * radsep;
+        double r_inner_sq = r_inner * r_inner;
+        double r_cross = 2.0 * radsep * R0;
+        for (int64_t ic = 0; ic < nc; ic++) {
+            double R = sqrt(r_inner_sq + r_cross * fabs(2.0 * ref_rng_uniform(st) - 1.0));
+            double az = 2 * M_PI * fabs(2.0 * ref_rng_uniform(st) - 1.0);
+            double saz = sin(az), caz = cos(az);
+            double z = fdev(ltype, st) * z0;
+            double x = R * caz;
+            double y = R * saz * cinc - z * sinc;
+            int64_t g0 = lround_ref(xpos + (x * spa - y * cpa) / cdelt0);
+            int64_t g1 = lround_ref(ypos + (x * cpa + y * spa) / cdelt1);
+            double wside = caz >= 0.0 ? SR(14, ir) : SR(15, ir);
+            if (wside == 0.0 || g0 < blo0 || g0 >= bhi0 || g1 < blo1 || g1 >= bhi1) {
+                for (int64_t iv = 0; iv < nvr; iv++) ref_rng_normal(st);
+                continue;
+            }
+            int64_t px = g0 - blo0, py = g1 - blo1;
+            double az_ = fabs(z), vs;
+            if (az_ > zcyl) vs = vsys0 + (lagged(vrot, dvdz, az_ - zcyl) * caz + vrad * saz) * sinc;
+            else vs = vsys0 + (vrot * caz + vrad * saz) * sinc;
+            vs += vvert * cinc;
+            double *o = out + ((size_t)py * nx + (size_t)px) * nz;
+            if (linear) {
+                double gz = vs * ia + ib, sg = vdisptmp * ia;
+                double val = relint[0] * fluxsc * wside;
+                for (int64_t iv = 0; iv < nvr; iv++) {
+                    int64_t isubs = lround_ref(gz + ref_rng_normal(st) * sg);
+                    if (isubs < 0 || isubs >= nz) continue;
+                    o[isubs] += val * cd2i[isubs];
+                }
+            } else {
+                for (int64_t iv = 0; iv < nvr; iv++) {
+                    double v = vs + ref_rng_normal(st) * vdisptmp;
+                    for (int nl = 0; nl < nlines; nl++) {
+                        int64_t isubs = lround_ref(velgrid(v, axtyp, velsys, lfreq0[nl], crval3, cdelt3, crpix3));
+                        if (isubs < 0 || isubs >= nz) continue;
+                        o[isubs] += relint[nl] * fluxsc * wside * cd2i[isubs];
+                    }
+                }
+            }
+        }
+    }
+}
+
+/* ------------------------------------------------------------------ ANALYTIC (bbarolo/galmod.py:174-465) */
+#define PHI_N 6146
+static double PHI_TAB[PHI_N];
+static int phi_ready = 0;
+
+/* bbarolo/galmod.py:176-180 */
+static void phi_table(void) {
+    for (int k = 0; k < PHI_N; k++) PHI_TAB[k] = 0.5 * erfc(-(-6.0 + k / 512.0) / sqrt(2.0));
+    phi_ready = 1;
+}
+
+void ref_phi_table(double *out) {
+    if (!phi_ready) phi_table();
+    memcpy(out, PHI_TAB, sizeof PHI_TAB);
+}
+
+/* bbarolo/galmod.py:183-191 */
+static inline double phi_interp(double t) {
+    double x = (t + 6.0) * 512.0;
+    if (x <= 0.0) return 0.0;
+    int64_t k = (int64_t)x;
+    if (k >= PHI_N - 1) return 1.0;
+    return PHI_TAB[k] + (x - (double)k) * (PHI_TAB[k + 1] - PHI_TAB[k]);
+}
+
+/* bbarolo/galmod.py:194-214 */
+static inline int line_profile(double *prof, double v, double sig, const double *vedges, const double *cd2i,
+                               int64_t kc, int64_t K, int64_t nz, int64_t *k0out) {
+    int64_t k0 = kc - K;
+    if (k0 < 0) k0 = 0;
+    int64_t k1 = kc + K + 1;
+    if (k1 > nz) k1 = nz;
+    if (k1 <= k0) { *k0out = 0; return 0; }
+    double inv = 1.0 / sig;
+    double pp = phi_interp((vedges[k0] - v) * inv);
+    for (int64_t k = k0; k < k1; k++) {
+        double pn = phi_interp((vedges[k + 1] - v) * inv);
+        double f = pn - pp;
+        prof[k - k0] = (f >= 0 ? f : -f) * cd2i[k];
+        pp = pn;
+    }
+    *k0out = k0;
+    return (int)(k1 - k0);
+}
+
+/* bbarolo/galmod.py:217-259 */
+static inline double layer_cdf(int ltype, double x) {
+    if (ltype == 1) return 0.5 * (1.0 + erf(x / sqrt(2.0)));
+    if (ltype == 2) return 0.5 * (1.0 + tanh(x));
+    if (ltype == 3) return x >= 0 ? 1.0 - 0.5 * exp(-x) : 0.5 * exp(x);
+    if (ltype == 4) return 0.5 + atan(x) / M_PI;
+    double c = x < -1.0 ? -1.0 : x;
+    c = c > 1.0 ? 1.0 : c;
+    return 0.5 * (c + 1.0);
+}
+
+static inline double layer_extent(int ltype) {
+    return ltype == 1 ? 5.0 : ltype == 2 ? 7.6 : ltype == 3 ? 14.0 : ltype == 4 ? 1e30 : 1.0;
+}
+
+static inline double layer_core(int ltype) {
+    return ltype == 1 ? 3.717 : ltype == 2 ? 4.147 : ltype == 3 ? 6.908 : ltype == 4 ? 31.61 : 1e30;
+}
+
+static inline double dmax(double a, double b) { return a > b ? a : b; }
+static inline double dmin(double a, double b) { return a < b ? a : b; }
+
+/* bbarolo/galmod.py:276-323 */
+int ref_zgrid(double *zq, double *wq, int nmax, int ltype, double z0, double sinc, double pixsize, double dvdz,
+              double sig, double R0, double radsep, double xpos, double ypos, double cdelt0, double cdelt1,
+              int64_t blo0, int64_t blo1, int64_t bhi0, int64_t bhi1, double zstep) {
+    double s = fabs(sinc);
+    if (z0 <= 0 || nmax < 2 || s < 1e-6) { zq[0] = 0.0; wq[0] = 1.0; return 1; }
+    double dx = dmax(fabs((double)blo0 - 0.5 - xpos), fabs((double)bhi0 - 0.5 - xpos)) * fabs(cdelt0);
+    double dy = dmax(fabs((double)blo1 - 0.5 - ypos), fabs((double)bhi1 - 0.5 - ypos)) * fabs(cdelt1);
+    double zlim = dmin(layer_extent(ltype), (R0 + radsep + sqrt(dx * dx + dy * dy)) / (s * z0));
+    double step = zstep * pixsize / (z0 * s);
+    if (dvdz != 0) step = dmin(step, 0.5 * sig / (fabs(dvdz) * z0 * s));
+    double zc = layer_core(ltype);
+    int64_t nin, nout;
+    for (;;) {
+        nin = (int64_t)ceil(dmin(zc, zlim) / step);
+        if (nin < 1) nin = 1;
+        nout = (int64_t)ceil((zlim - (double)nin * step) / (4.0 * step));
+        if (nout < 0) nout = 0;
+        if (2 * (nin + nout) <= nmax) break;
+        step *= 1.01 * (double)(nin + nout) / (double)(nmax / 2);
+    }
+    int64_t half = nin + nout;
+    for (int64_t j = 0; j < half; j++) {
+        double lo = j < nin ? (double)j * step : (double)(nin + 4 * (j - nin)) * step;
+        double hi = dmin(lo + (j < nin ? step : 4.0 * step), zlim);
+        double w = layer_cdf(ltype, hi) - layer_cdf(ltype, lo);
+        zq[half + j] = 0.5 * (lo + hi); wq[half + j] = w;
+        zq[half - 1 - j] = -0.5 * (lo + hi); wq[half - 1 - j] = w;
+    }
+    return (int)(2 * half);
+}
+
+/* bbarolo/galmod.py:326-465. vedges: (nlines, nz+1). */
+void ref_galmod_analytic(double *out, int ny, int nx, int nz, const double *sr, int nsub, int ring_lo,
+                         int ring_hi, double radsep, double cdens, double pixarea, double cdelt0, double cdelt1,
+                         double crota2, int64_t blo0, int64_t blo1, int64_t bhi0, int64_t bhi1, int ltype,
+                         double sig_instr, const double *vedges, const double *relint, const double *cd2i,
+                         int nzq, int axtyp, int velsys, int nlines, const double *lfreq0, double crval3,
+                         double cdelt3, double crpix3, double chwidth, double zstep) {
+    (void)cdens; (void)ny;
+    if (!phi_ready) phi_table();
+    int nb = nzq > 1 ? nzq : 1;
+    double pixsize = sqrt(pixarea);
+    double *zq = malloc(sizeof(double) * nb), *wq = malloc(sizeof(double) * nb);
+    double *prof = malloc(sizeof(double) * (nz + 1));
+    int64_t *gx = malloc(sizeof(int64_t) * nb), *gy = malloc(sizeof(int64_t) * nb);
+    for (int ir = ring_lo; ir < ring_hi; ir++) {
+        double R0 = SR(0, ir), dens = SR(5, ir);
+        if (dens == 0) continue;
+        double ring_area_pix = 2 * M_PI * R0 * radsep / pixarea;
+        double circ_pix = 2 * M_PI * R0 / sqrt(pixarea);
+        int64_t naz = (int64_t)(3 * circ_pix + 0.5);
+        if (naz < 16) naz = 16;
+        int nrad = 2;
+        double vrot = SR(1, ir), vrad = SR(2, ir), vvert = SR(3, ir);
+        double sig = dmax(sqrt(SR(4, ir) * SR(4, ir) + sig_instr * sig_instr), 1e-6 * fabs(chwidth));
+        int64_t K = (int64_t)(5.0 * sig / chwidth) + 2;
+        double z0 = SR(6, ir), dvdz = SR(7, ir), zcyl = SR(8, ir);
+        double sinc = sin(SR(9, ir)), cinc = cos(SR(9, ir));
+        double phi = SR(10, ir);
+        double spa = sin(phi) * cos(crota2) + cos(phi) * sin(crota2);
+        double cpa = cos(phi) * cos(crota2) - sin(phi) * sin(crota2);
+        double xpos = SR(11, ir), ypos = SR(12, ir), vsys0 = SR(13, ir);
+        int nzz = ref_zgrid(zq, wq, nzq, ltype, z0, sinc, pixsize, dvdz, sig, R0, radsep, xpos, ypos, cdelt0,
+                            cdelt1, blo0, blo1, bhi0, bhi1, zstep);
+        double fluxsc = dens * ring_area_pix * pixarea / (double)(naz * nrad);
+        int zdep = 0;
+        if (dvdz != 0 && nzz > 1)
+            for (int kz = 0; kz < nzz; kz++)
+                if (fabs(zq[kz] * z0) > zcyl) { zdep = 1; break; }
+        double r_inner = R0 - 0.5 * radsep;
+        double daz = 2 * M_PI / (double)naz;
+        double cd = cos(daz), sd = sin(daz);
+        for (int kr = 0; kr < nrad; kr++) {
+            double u = (kr + 0.5) / nrad;
+            double R = sqrt(r_inner * r_inner + 2.0 * radsep * R0 * u);
+            double az0 = 2 * M_PI * (0.5 * ((kr + 1) % 2) + 0.25) / (double)naz;
+            double caz = cos(az0), saz = sin(az0);
+            for (int64_t ka = 0; ka < naz; ka++) {
+                if (ka > 0) {
+                    double c2 = caz * cd - saz * sd, s2 = saz * cd + caz * sd;
+                    caz = c2; saz = s2;
+                }
+                double wside = caz >= 0.0 ? SR(14, ir) : SR(15, ir);
+                if (wside == 0.0) continue;
+                double x = R * caz, yb = R * saz * cinc, xs = x * spa, xc = x * cpa;
+                for (int kz = 0; kz < nzz; kz++) {
+                    double z = nzz > 1 ? zq[kz] * z0 : 0.0;
+                    double y = yb - z * sinc;
+                    gx[kz] = lround_ref(xpos + (xs - y * cpa) / cdelt0);
+                    gy[kz] = lround_ref(ypos + (xc + y * spa) / cdelt1);
+                }
+                double vplane = vsys0 + (vrot * caz + vrad * saz) * sinc + vvert * cinc;
+                int inbox = 0;
+                for (int kz = 0; kz < nzz; kz++)
+                    if (blo0 <= gx[kz] && gx[kz] < bhi0 && blo1 <= gy[kz] && gy[kz] < bhi1) { inbox = 1; break; }
+                if (!inbox) continue;
+                for (int nl = 0; nl < nlines; nl++) {
+                    double a = relint[nl] * fluxsc * wside;
+                    const double *ve = vedges + (size_t)nl * (nz + 1);
+                    int64_t k0;
+                    if (!zdep) {
+                        double v = vplane;
+                        int64_t kc = lround_ref(velgrid(v, axtyp, velsys, lfreq0[nl], crval3, cdelt3, crpix3));
+                        int nk = line_profile(prof, v, sig, ve, cd2i, kc, K, nz, &k0);
+                        if (nk == 0) continue;
+                        int kz = 0;
+                        while (kz < nzz) {
+                            int64_t g0 = gx[kz], g1 = gy[kz];
+                            double ws = wq[kz];
+                            int w = 1;
+                            while (kz + w < nzz && gx[kz + w] == g0 && gy[kz + w] == g1) { ws += wq[kz + w]; w++; }
+                            kz += w;
+                            if (g0 < blo0 || g0 >= bhi0 || g1 < blo1 || g1 >= bhi1) continue;
+                            double aw = a * ws;
+                            double *o = out + ((size_t)(g1 - blo1) * nx + (size_t)(g0 - blo0)) * nz;
+                            for (int j = 0; j < nk; j++) o[k0 + j] += aw * prof[j];
+                        }
+                    } else {
+                        for (int kz = 0; kz < (nzz + 1) / 2; kz++) {
+                            int kz2 = nzz - 1 - kz;
+                            int in1 = !(gx[kz] < blo0 || gx[kz] >= bhi0 || gy[kz] < blo1 || gy[kz] >= bhi1);
+                            int in2 = kz2 != kz && !(gx[kz2] < blo0 || gx[kz2] >= bhi0 || gy[kz2] < blo1 ||
+                                                     gy[kz2] >= bhi1);
+                            if (!(in1 || in2)) continue;
+                            double az_ = fabs(zq[kz] * z0), v;
+                            if (az_ > zcyl) v = vsys0 + (lagged(vrot, dvdz, az_ - zcyl) * caz + vrad * saz) * sinc +
+                                                vvert * cinc;
+                            else v = vplane;
+                            int64_t kc = lround_ref(velgrid(v, axtyp, velsys, lfreq0[nl], crval3, cdelt3, crpix3));
+                            int nk = line_profile(prof, v, sig, ve, cd2i, kc, K, nz, &k0);
+                            if (nk == 0) continue;
+                            if (in1 && in2 && gx[kz] == gx[kz2] && gy[kz] == gy[kz2]) {
+                                double *o = out + ((size_t)(gy[kz] - blo1) * nx + (size_t)(gx[kz] - blo0)) * nz;
+                                double aw = a * (wq[kz] + wq[kz2]);
+                                for (int j = 0; j < nk; j++) o[k0 + j] += aw * prof[j];
+                                continue;
+                            }
+                            if (in1) {
+                                double *o = out + ((size_t)(gy[kz] - blo1) * nx + (size_t)(gx[kz] - blo0)) * nz;
+                                double aw = a * wq[kz];
+                                for (int j = 0; j < nk; j++) o[k0 + j] += aw * prof[j];
+                            }
+                            if (in2) {
+                                double *o = out + ((size_t)(gy[kz2] - blo1) * nx + (size_t)(gx[kz2] - blo0)) * nz;
+                                double aw = a * wq[kz2];
+                                for (int j = 0; j < nk; j++) o[k0 + j] += aw * prof[j];
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+    free(zq); free(wq); free(prof); free(gx); free(gy);
+}
+
+/* bbarolo/galmod.py:468-536. out: (nr, ny, nx); widx, wval: (nsub, 2). */
+void ref_ring_maps_analytic(double *out, int nr, int ny, int nx, const double *sr, int nsub, const int64_t *widx,
+                            const double *wval, double radsep, double pixarea, double cdelt0, double cdelt1,
+                            double crota2, int64_t blo0, int64_t blo1, int64_t bhi0, int64_t bhi1, int ltype,
+                            int nzq, double sig_instr, double chwidth, double zstep) {
+    (void)nr;
+    int nb = nzq > 1 ? nzq : 1;
+    double pixsize = sqrt(pixarea);
+    double *zq = malloc(sizeof(double) * nb), *wq = malloc(sizeof(double) * nb);
+    int64_t *gx = malloc(sizeof(int64_t) * nb), *gy = malloc(sizeof(int64_t) * nb);
+    for (int ir = 0; ir < nsub; ir++) {
+        if (widx[2 * ir] < 0 && widx[2 * ir + 1] < 0) continue;
+        double R0 = SR(0, ir);
+        double ring_area_pix = 2 * M_PI * R0 * radsep / pixarea;
+        double circ_pix = 2 * M_PI * R0 / sqrt(pixarea);
+        int64_t naz = (int64_t)(3 * circ_pix + 0.5);
+        if (naz < 16) naz = 16;
+        int nrad = 2;
+        double z0 = SR(6, ir);
+        double sinc = sin(SR(9, ir));
+        double phi = SR(10, ir);
+        double spa = sin(phi) * cos(crota2) + cos(phi) * sin(crota2);
+        double cpa = cos(phi) * cos(crota2) - sin(phi) * sin(crota2);
+        double xpos = SR(11, ir), ypos = SR(12, ir);
+        double sig = dmax(sqrt(SR(4, ir) * SR(4, ir) + sig_instr * sig_instr), 1e-6 * fabs(chwidth));
+        int nzz = ref_zgrid(zq, wq, nzq, ltype, z0, sinc, pixsize, SR(7, ir), sig, R0, radsep, xpos, ypos,
+                            cdelt0, cdelt1, blo0, blo1, bhi0, bhi1, zstep);
+        double cinc = cos(SR(9, ir));
+        double fluxsc = ring_area_pix * pixarea / (double)(naz * nrad);
+        double r_inner = R0 - 0.5 * radsep;
+        double daz = 2 * M_PI / (double)naz;
+        double cd = cos(daz), sd = sin(daz);
+        for (int kr = 0; kr < nrad; kr++) {
+            double u = (kr + 0.5) / nrad;
+            double R = sqrt(r_inner * r_inner + 2.0 * radsep * R0 * u);
+            double az0 = 2 * M_PI * (0.5 * ((kr + 1) % 2) + 0.25) / (double)naz;
+            double caz = cos(az0), saz = sin(az0);
+            for (int64_t ka = 0; ka < naz; ka++) {
+                if (ka > 0) {
+                    double c2 = caz * cd - saz * sd, s2 = saz * cd + caz * sd;
+                    caz = c2; saz = s2;
+                }
+                double wside = caz >= 0.0 ? SR(14, ir) : SR(15, ir);
+                if (wside == 0.0) continue;
+                double x = R * caz, yb = R * saz * cinc, xs = x * spa, xc = x * cpa;
+                for (int kz = 0; kz < nzz; kz++) {
+                    double z = nzz > 1 ? zq[kz] * z0 : 0.0;
+                    double y = yb - z * sinc;
+                    gx[kz] = lround_ref(xpos + (xs - y * cpa) / cdelt0);
+                    gy[kz] = lround_ref(ypos + (xc + y * spa) / cdelt1);
+                }
+                int kz = 0;
+                while (kz < nzz) {
+                    int64_t g0 = gx[kz], g1 = gy[kz];
+                    double ws = wq[kz];
+                    kz++;
+                    while (kz < nzz && gx[kz] == g0 && gy[kz] == g1) { ws += wq[kz]; kz++; }
+                    if (g0 < blo0 || g0 >= bhi0 || g1 < blo1 || g1 >= bhi1) continue;
+                    for (int m = 0; m < 2; m++) {
+                        int64_t r = widx[2 * ir + m];
+                        if (r >= 0)
+                            out[((size_t)r * ny + (size_t)(g1 - blo1)) * nx + (size_t)(g0 - blo0)] +=
+                                fluxsc * ws * wval[2 * ir + m] * wside;
+                    }
+                }
+            }
+        }
+    }
+    free(zq); free(wq); free(gx); free(gy);
+}
+
+/* ------------------------------------------------------------------ beam convolution
+ * Direct "same" linear convolution of each plane of a (nz, ny, nx) float64 array with the kernel (ky, kx):
+ * out[y, x] = sum_{j,i} k[j, i] in[y + ky/2 - j, x + kx/2 - i] (zero outside), the crop of the full linear
+ * convolution taken by FFTConvolver (bbarolo/smooth.py:145-165); then, as DiskModel.convolve
+ * (bbarolo/galmod.py:1273-1283), values below 1e-12 set to zero and the flux scale applied. This is the
+ * FP64 oracle of the smoothed cube: it agrees with the FFT of the reference to ~1e-16 of the peak. */
+void ref_conv_same(const double *in, double *out, int nz, int ny, int nx, const double *k, int ky, int kx,
+                   double scale, int threshold) {
+    int hy = ky / 2, hx = kx / 2;
+    for (int z = 0; z < nz; z++) {
+        const double *p = in + (size_t)z * ny * nx;
+        double *o = out + (size_t)z * ny * nx;
+        for (int y = 0; y < ny; y++)
+            for (int x = 0; x < nx; x++) {
+                double s = 0.;
+                for (int j = 0; j < ky; j++) {
+                    int yy = y + hy - j;
+                    if (yy < 0 || yy >= ny) continue;
+                    for (int i = 0; i < kx; i++) {
+                        int xx = x + hx - i;
+                        if (xx < 0 || xx >= nx) continue;
+                        s += k[j * kx + i] * p[(size_t)yy * nx + xx];
+                    }
+                }
+                if (threshold && s < 1.E-12) s = 0.;
+                else if (scale != 1.0) s *= scale;
+                o[(size_t)y * nx + x] = s;
+            }
+    }
+}
+
+/* bbarolo/galmod.py:974-1037: model (ny, nx, nz) -> out (ny, nx, nz), out zeroed by the caller. */
+void ref_conv_sparse(const double *model, double *out, int ny, int nx, int nz, const double *kern, int ky, int kx,
+                     double scale) {
+    int hy = ky / 2, hx = kx / 2;
+    int nk = 0;
+    for (int j = 0; j < ky * kx; j++) nk += kern[j] != 0;
+    int64_t *kj = malloc(sizeof(int64_t) * (nk + 1)), *ki = malloc(sizeof(int64_t) * (nk + 1));
+    double *kv = malloc(sizeof(double) * (nk + 1));
+    nk = 0;
+    for (int j = 0; j < ky; j++)
+        for (int i = 0; i < kx; i++)
+            if (kern[j * kx + i] != 0) { kj[nk] = j - hy; ki[nk] = i - hx; kv[nk] = kern[j * kx + i]; nk++; }
+    int64_t *zl = malloc(sizeof(int64_t) * ny * nx), *zh = malloc(sizeof(int64_t) * ny * nx);
+    for (int q = 0; q < ny * nx; q++) { zl[q] = nz; zh[q] = -1; }
+    for (int y = 0; y < ny; y++)
+        for (int x = 0; x < nx; x++) {
+            const double *m = model + ((size_t)y * nx + x) * nz;
+            int64_t zlo = -1, zhi = -1;
+            for (int z = 0; z < nz; z++)
+                if (m[z] != 0) { if (zlo < 0) zlo = z; zhi = z; }
+            if (zlo < 0) continue;
+            for (int n = 0; n < nk; n++) {
+                int64_t yy = y + kj[n], xx = x + ki[n];
+                if (yy < 0 || yy >= ny || xx < 0 || xx >= nx) continue;
+                size_t q = (size_t)yy * nx + xx;
+                if (zlo < zl[q]) zl[q] = zlo;
+                if (zhi > zh[q]) zh[q] = zhi;
+                double kk = kv[n];
+                double *o = out + q * nz;
+                for (int64_t z = zlo; z <= zhi; z++) o[z] += kk * m[z];
+            }
+        }
+    for (int q = 0; q < ny * nx; q++) {
+        double *o = out + (size_t)q * nz;
+        for (int64_t z = zl[q]; z <= zh[q]; z++) {
+            double v = o[z];
+            if (v < 1.E-12) o[z] = 0.;
+            else if (scale != 1.0) o[z] = v * scale;
+        }
+    }
+    free(kj); free(ki); free(kv); free(zl); free(zh);
+}
+
+/* ------------------------------------------------------------------ residuals (bbarolo/bayesian/likelihood.py:22-77)
+ * model f64 (nz, ny, nx), data f32 and mask u8 with the same shape (views of the box), region u8 (ny, nx)
+ * or NULL. */
+double ref_sumsq_residuals(const double *model, const float *data, const uint8_t *mask, int maskmode,
+                           const uint8_t *region, int nz, int ny, int nx) {
+    double s = 0.;
+    for (int k = 0; k < nz; k++)
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < nx; i++) {
+                if (region && !region[j * nx + i]) continue;
+                size_t q = ((size_t)k * ny + j) * nx + i;
+                double d = data[q];
+                if (d != d || d == 0.) continue;
+                if (maskmode != 0 && !mask[q]) {
+                    if (maskmode == 2) continue;
+                    d = 0.;
+                }
+                double r = d - model[q];
+                s += r * r;
+            }
+    return s;
+}
+
+void ref_residuals_fracerr(const double *model, const float *data, const uint8_t *mask, int maskmode,
+                           const uint8_t *region, int nz, int ny, int nx, double sigma2, double eps2, double *out) {
+    double s = 0., lg = 0.;
+    for (int k = 0; k < nz; k++)
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < nx; i++) {
+                if (region && !region[j * nx + i]) continue;
+                size_t q = ((size_t)k * ny + j) * nx + i;
+                double d = data[q];
+                if (d != d || d == 0.) continue;
+                if (maskmode != 0 && !mask[q]) {
+                    if (maskmode == 2) continue;
+                    d = 0.;
+                }
+                double m = model[q], r = d - m;
+                if (m != 0.) {
+                    double v = sigma2 + eps2 * m * m;
+                    s += r * r / v;
+                    lg += log(v / sigma2);
+                } else s += r * r / sigma2;
+            }
+    out[0] = s;
+    out[1] = lg;
+}
+
+/* ------------------------------------------------------------------ CLASSIC normalisation + residual
+ * bbarolo/galfit.py:39-188. model (bsy, bsx, nz) f64 is MODIFIED (x factor) as in the reference; data f32
+ * and mask u8 are (ny, nx, nz) full arrays ("yxz"); chan_noise (nz); pre (bsy, bsx, nz) or NULL; ilo/ihi (ky);
+ * thr (nz); P work (ky, bsx+1, nz). */
+double ref_norm(double *model, int bsy, int bsx, int nz, const float *data, const uint8_t *mask, int dny, int dnx,
+                int64_t blo0, int64_t blo1, double x0, double y0, double phi, double inc, double r1, double r2,
+                double wpow, int side, int ftype, const double *chan_noise, double data_noise, double bweight,
+                int normtype, const double *pre, const int64_t *ilo, const int64_t *ihi, int ky, const double *thr,
+                int foot, double hmax) {
+    (void)dny;
+    int trunc = pre != NULL;
+    int hy = ky / 2;
+    double *lam = calloc(nz, sizeof(double));
+    double *P = trunc ? calloc((size_t)ky * (bsx + 1) * nz, sizeof(double)) : NULL;
+    int64_t nextrow = 0;
+    double F = M_PI / 180.;
+    double sphi = sin(F * phi), cphi = cos(F * phi), cinc = cos(F * inc);
+    int64_t numBlanks = 0, numPix_tot = 0;
+    double minfunc = 0.0;
+    int usesin = wpow < 0;
+    double apow = fabs(wpow);
+    uint8_t *inside = calloc((size_t)bsy * bsx, 1);
+    double *wmap = calloc((size_t)bsy * bsx, sizeof(double));
+#define DAT(y, x, z) data[(((size_t)(y) + blo1) * dnx + ((size_t)(x) + blo0)) * nz + (z)]
+#define MSK(y, x, z) mask[(((size_t)(y) + blo1) * dnx + ((size_t)(x) + blo0)) * nz + (z)]
+#define MOD(y, x, z) model[(((size_t)(y)) * bsx + (size_t)(x)) * nz + (z)]
+    for (int y = 0; y < bsy; y++)
+        for (int x = 0; x < bsx; x++) {
+            double xr = -(x - x0) * sphi + (y - y0) * cphi;
+            double ys = -(x - x0) * cphi - (y - y0) * sphi;
+            double yr = ys / cinc;
+            double r = sqrt(xr * xr + yr * yr);
+            double th = r < 0.1 ? 0.0 : atan2(yr, xr) / F;
+            if (foot == 1) {
+                if (!(fabs(xr) >= r1 && fabs(xr) <= r2 && fabs(ys) <= hmax)) continue;
+                th = xr >= 0 ? 0.0 : 180.0;
+            } else if (!(r >= r1 && r <= r2)) continue;
+            if (side == 1 && !(fabs(th) <= 90.0)) continue;
+            if (side == 2 && !(fabs(th) >= 90.0)) continue;
+            inside[y * bsx + x] = 1;
+            if (foot == 1) { wmap[y * bsx + x] = 1.0; continue; }
+            double wf = usesin ? fabs(sin(th * F)) : fabs(cos(th * F));
+            wmap[y * bsx + x] = pow(wf, apow);
+        }
+    double factor = 1.0;
+    if (normtype == 1) {
+        double modSum = 0.0, obsSum = 0.0;
+        for (int y = 0; y < bsy; y++)
+            for (int x = 0; x < bsx; x++) {
+                if (!inside[y * bsx + x]) continue;
+                for (int z = 0; z < nz; z++) {
+                    modSum += MOD(y, x, z);
+                    if (MSK(y, x, z)) obsSum += DAT(y, x, z);
+                }
+            }
+        factor = modSum != 0 ? obsSum / modSum : 0.0;
+    }
+    for (int y = 0; y < bsy; y++) {
+        if (trunc) {
+            int anyin = 0;
+            for (int x = 0; x < bsx; x++) if (inside[y * bsx + x]) { anyin = 1; break; }
+            if (anyin) {
+                if (nextrow < y - hy) nextrow = y - hy;
+                while (nextrow <= (y + hy < bsy - 1 ? y + hy : bsy - 1)) {
+                    double *Pr = P + (size_t)(nextrow % ky) * (bsx + 1) * nz;
+                    const double *pr = pre + (size_t)nextrow * bsx * nz;
+                    for (int z = 0; z < nz; z++) Pr[z] = 0.;
+                    for (int x = 0; x < bsx; x++)
+                        for (int z = 0; z < nz; z++)
+                            Pr[(size_t)(x + 1) * nz + z] = Pr[(size_t)x * nz + z] + pr[(size_t)x * nz + z];
+                    nextrow++;
+                }
+            }
+        }
+        for (int x = 0; x < bsx; x++) {
+            if (!inside[y * bsx + x]) continue;
+            if (normtype == 0) {
+                double modSum = 0.0, obsSum = 0.0;
+                for (int z = 0; z < nz; z++) {
+                    modSum += MOD(y, x, z);
+                    double o = DAT(y, x, z);
+                    if (o > 0 && MSK(y, x, z)) obsSum += o;
+                }
+                factor = modSum != 0 ? obsSum / modSum : 0.0;
+            }
+            double wi = wmap[y * bsx + x];
+            if (trunc) {
+                int ca = nz, cb = -1;
+                for (int z = 0; z < nz; z++)
+                    if (MOD(y, x, z) != 0 && !MSK(y, x, z)) { if (ca == nz) ca = z; cb = z; }
+                for (int z = ca; z <= cb; z++) lam[z] = 0.;
+                if (cb >= ca)
+                    for (int j = 0; j < ky; j++) {
+                        int yy = y + hy - j;
+                        if (yy < 0 || yy >= bsy) continue;
+                        int64_t xa = x + ilo[j] > 0 ? x + ilo[j] : 0;
+                        int64_t xb = x + ihi[j] + 1 < bsx ? x + ihi[j] + 1 : bsx;
+                        if (xb <= xa) continue;
+                        const double *p1 = P + ((size_t)(yy % ky) * (bsx + 1) + xb) * nz;
+                        const double *p0 = P + ((size_t)(yy % ky) * (bsx + 1) + xa) * nz;
+                        for (int z = ca; z <= cb; z++) lam[z] += p1[z] - p0[z];
+                    }
+            }
+            for (int z = 0; z < nz; z++) {
+                if (normtype != 2) MOD(y, x, z) *= factor;
+                double o = DAT(y, x, z);
+                double obs = o > 0 ? o : data_noise;
+                double mod = MOD(y, x, z);
+                if (!MSK(y, x, z)) {
+                    if (mod == 0) continue;
+                    if (trunc && lam[z] < thr[z]) continue;
+                    numBlanks++;
+                }
+                numPix_tot++;
+                double nw = chan_noise[z];
+                if (ftype == 1) minfunc += wi * ((mod - obs) * (mod - obs)) / sqrt(obs) / nw;
+                else if (ftype == 2) minfunc += wi * fabs(mod - obs) / nw;
+                else if (ftype == 3) minfunc += wi * fabs(mod - obs) / (mod + obs) / nw;
+                else if (ftype == 4) minfunc += wi * ((mod - obs) * (mod - obs)) / nw;
+            }
+        }
+    }
+#undef DAT
+#undef MSK
+#undef MOD
+    free(lam); free(P); free(inside); free(wmap);
+    if (numPix_tot - numBlanks == 0) return INFINITY;
+    return pow(1 + (double)numBlanks / (double)numPix_tot, bweight) * minfunc / (double)(numPix_tot - numBlanks);
+}

@@ -1,0 +1,102 @@
+"""The reference's CPU likelihood evaluation, timed on the host cores (the CPU baseline of the benchmark).
+
+TEST INFRASTRUCTURE: used only by the CPU-baseline leg of ``bench.py`` (and its ``--impl reference`` arm).
+
+numba is not available where the benchmark runs, so the reference's numba kernels are timed through their C
+restatement (``oracle/bbref.c``, bit-exact with the reference): the MC model (``_galmod_mc``) and the residual
+(``_sumsq_residuals``). The beam convolution is the reference's own algorithm with the same library:
+``FFTConvolver.__call__`` (``bbarolo/smooth.py:145-165``) restated here with scipy.fft (real FFTs padded to
+``next_fast_len(n + k // 2)``, empty planes skipped), followed by the threshold of ``DiskModel.convolve``.
+One evaluation per process, as the reference's fork pool (``bbarolo/bayesian/sampling.py:184-193``), with the
+FFT on one worker thread; throughput = evaluations / wall time over all processes.
+"""
+
+import multiprocessing as mp
+import os
+import time
+
+import numpy as np
+
+_W = {}
+
+
+def fft_convolve(data, kernel):
+    """"Same" convolution of the planes (nz, ny, nx) by the FFT, as FFTConvolver (empty planes skipped)."""
+    import scipy.fft as sfft
+    nz = data.shape[0]
+    full = data.reshape(nz, -1).any(axis=1)
+    out = np.zeros(data.shape, np.float64)
+    if not full.any():
+        return out
+    d = data[full]
+    ny, nx = d.shape[-2:]
+    ky, kx = kernel.shape
+    Ny = sfft.next_fast_len(ny + ky // 2, real=True)
+    Nx = sfft.next_fast_len(nx + kx // 2, real=True)
+    kf = _W.get(("kf", Ny, Nx))
+    if kf is None:
+        kf = sfft.rfft2(kernel, s=(Ny, Nx))
+        _W[("kf", Ny, Nx)] = kf
+    f = sfft.rfft2(d, s=(Ny, Nx), workers=1)
+    f *= kf
+    r = sfft.irfft2(f, s=(Ny, Nx), workers=1)
+    out[full] = r[..., ky // 2:ky // 2 + ny, kx // 2:kx // 2 + nx]
+    return out
+
+
+def _init(payload):
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    _W.update(payload)
+    from oracle import oracle
+    oracle.lib()
+
+
+def evaluate(k):
+    """log-likelihood sum of squares of member k of the batch in the worker's payload."""
+    from oracle import oracle as O
+    P = _W
+    st = P["setup"]
+    blo, bhi = P["boxes"][k]
+    m = np.zeros((bhi[1] - blo[1], bhi[0] - blo[0], st["nz"]))
+    O.galmod_mc(m, P["sr"][k], 0, P["sr"].shape[2], P["seed"], st["radsep"], P["nv"][k], st["cdens"], st["cmode"],
+                st["pixarea"], st["cdelt0"], st["cdelt1"], st["crota2"], blo[0], blo[1], bhi[0], bhi[1], st["ltype"],
+                st["sig_instr"], st["axtyp"], st["velsys"], P["lfreq0"], st["crval3"], st["cdelt3"], st["crpix3"],
+                P["relint"], P["cd2i"])
+    sm = fft_convolve(np.ascontiguousarray(m.transpose(2, 0, 1)), P["kernel"])
+    sm[sm < 1e-12] = 0.
+    sl = (slice(None), slice(blo[1], bhi[1]), slice(blo[0], bhi[0]))
+    return O.sumsq_residuals(sm, P["data"][sl], P["mask"][sl], P["maskmode"], None)
+
+
+def setup_payload(dm, sr, nv, boxes, seed, data, mask, maskmode):
+    st = dm.setup
+    return dict(setup=dict(nz=st.nsubs, radsep=st.radsep, cdens=st.cdens, cmode=st.cmode, pixarea=st.pixarea,
+                           cdelt0=st.cdelt[0], cdelt1=st.cdelt[1], crota2=st.crota2, ltype=st.ltype,
+                           sig_instr=st.sig_instr, axtyp=st.axtyp, velsys=st.velsys, crval3=st.crval3,
+                           cdelt3=st.cdelt3, crpix3=st.crpix3),
+                sr=sr, nv=nv, boxes=boxes, seed=seed, lfreq0=st.lfreq0, relint=st.relint, cd2i=st.cd2i,
+                kernel=dm.cfield, data=data, mask=mask, maskmode=maskmode)
+
+
+class Pool:
+    """A spawn pool of `cores` processes holding the payload (started before any GPU work of the caller)."""
+
+    def __init__(self, payload, cores=None):
+        self.cores = int(cores or os.cpu_count() or 1)
+        ctx = mp.get_context("spawn")
+        self.pool = ctx.Pool(self.cores, initializer=_init, initargs=(payload,))
+        self.pool.map(_noop, range(self.cores))
+
+    def run(self, members):
+        """Evaluates the members (indices); returns (sums of squares, wall seconds)."""
+        t0 = time.perf_counter()
+        out = self.pool.map(evaluate, list(members), chunksize=1)
+        return np.array(out), time.perf_counter() - t0
+
+    def close(self):
+        self.pool.terminate()
+        self.pool.join()
+
+
+def _noop(_):
+    return 0

@@ -1,0 +1,87 @@
+"""Host-side mirror of the reference interface: sub-ring tables, model rings, beam kernels (no GPU)."""
+import json
+
+import numpy as np
+import pytest
+
+import golden_io as G
+from bbarolo2_gb300 import configs, galmod
+from bbarolo2_gb300.beam import BeamKernel
+
+
+def _cases():
+    z = G.load("subrings.npz")
+    return [(z, m) for m in json.loads(str(z["index"]))]
+
+
+def _rebuild(name):
+    """The (cube, rings, ringmode) of a named fixture case (same constructions as make_golden.py)."""
+    import importlib.util
+    import os
+    import sys
+    spec = importlib.util.spec_from_file_location("mg_cases", os.path.join(G.GOLDEN, "cases.py"))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["mg_cases"] = mod
+    spec.loader.exec_module(mod)
+    return mod.case(name)
+
+
+@pytest.mark.parametrize("case", _cases(), ids=lambda c: c[1]["name"])
+def test_subrings_bit_equal(case):
+    z, m = case
+    cube, rings, mode = _rebuild(m["name"])
+    st = galmod.GalmodSetup(cube, densflux=True)
+    mr = galmod.model_rings(rings, mode, st.radsep)
+    assert np.array_equal(np.asarray(mr.radii, float), z[m["name"] + "/model_radii"])
+    sr, nv = st.subrings(mr)
+    assert np.array_equal(sr, z[m["name"] + "/sr"])
+    assert np.array_equal(nv, z[m["name"] + "/nv"])
+
+
+@pytest.mark.parametrize("case", _cases(), ids=lambda c: c[1]["name"])
+def test_subrings_batch_equal_single(case):
+    """The vectorised batch tables equal the per-set tables."""
+    z, m = case
+    cube, rings, mode = _rebuild(m["name"])
+    st = galmod.GalmodSetup(cube, densflux=True)
+    mr = galmod.model_rings(rings, mode, st.radsep)
+    rows = galmod.ring_rows_batch([mr, mr])
+    rows[1, 4] *= 1.1          # vrot
+    sr, nv = galmod.subrings_batch(st, mr, rows)
+    assert np.array_equal(sr[0], z[m["name"] + "/sr"])
+    r2 = mr.copy()
+    r2.vrot = rows[1, 4].copy()
+    s2, n2 = st.subrings(r2)
+    assert np.array_equal(sr[1], s2) and np.array_equal(nv[1], n2)
+
+
+@pytest.mark.parametrize("wl", ["classic64", "global160", "bayes256"])
+def test_beam_kernel(wl):
+    z = G.load("beam_conv.npz")
+    cube, _ = configs.WORKLOADS[wl]()
+    bk = BeamKernel.from_cube(cube)
+    assert np.array_equal(bk.kernel, z[wl + "/kernel"])
+    assert bk.scalefac == float(z[wl + "/scalefac_coldens"])
+
+
+def test_beam_kernel_swapped_axes():
+    from bbarolo2_gb300.cube import Cube
+    z = G.load("beam_conv.npz")
+    cube = Cube.empty(64, 64, 64, [-10. / 3600., 10. / 3600., 5.], beam=[20. / 3600., 40. / 3600., 10.], crota=15.,
+                      cunit=("deg", "deg", "km/s"))
+    assert np.array_equal(BeamKernel.from_cube(cube).kernel, z["swapped/kernel"])
+
+
+def test_subring_errors():
+    cube, rings = configs.classic64()
+    st = galmod.GalmodSetup(cube)
+    r = rings.copy()
+    r.vdisp[2] = -1
+    with pytest.raises(ValueError):
+        st.subrings(r)
+    r = rings.copy()
+    r.radii[3] = r.radii[2]
+    with pytest.raises(galmod.BBaroloError):
+        st.subrings(r)
+    with pytest.raises(galmod.BBaroloError):
+        galmod.model_rings(rings.subset(np.array([0])), "NODES")
