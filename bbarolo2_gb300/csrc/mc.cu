@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(256) k_mc_deposit(GridDev g, LayoutDev L, cons
                                                     const int *__restrict__ count, const int *__restrict__ bucket,
                                                     const ZigDev *__restrict__ zig, const float *__restrict__ cd2if,
                                                     const double *__restrict__ cd2i, float *__restrict__ model,
-                                                    long long mstride, double *__restrict__ model64) {
+                                                    long long mstride, double *__restrict__ model64, int *err) {
     extern __shared__ unsigned long long tile[];
     __shared__ unsigned s_kn[128];
     __shared__ float s_wnf[128];
@@ -244,7 +244,13 @@ __global__ void __launch_bounds__(256) k_mc_deposit(GridDev g, LayoutDev L, cons
             double nex = 0.0;
             float nf;
             if (slow) {
-                nex = L.slow_val[slow_ord + __popc(bal & ltmask)];
+                const long long o = (long long)slow_ord + __popc(bal & ltmask);
+                if (o < L.nslow) {
+                    nex = L.slow_val[o];
+                } else {
+                    atomicOr(err, ERR_LAYOUT);
+                    nex = 0.0;
+                }
                 nf = (float)nex;
             } else {
                 nf = __int2float_rn(h) * s_wnf[iz];
@@ -319,7 +325,6 @@ void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, con
                        const int *offset, const int *count, const int *bucket, const ZigDev *zig,
                        const float *cd2if, const double *cd2i, float *model, long long mstride, double *model64,
                        int *err) {
-    (void)err;
     int maxt = 0;
     for (int k = 0; k < nb; k++) maxt = max(maxt, mem_host[k].ntx * mem_host[k].nty);
     if (maxt == 0 || nb == 0) return;
@@ -331,5 +336,5 @@ void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, con
     }
     dim3 grid(nb, maxt);
     k_mc_deposit<<<grid, 256, smem, s>>>(g, L, sub, nsub, mem, tx, ty, pix, offset, count, bucket, zig, cd2if, cd2i,
-                                        model, mstride, model64);
+                                        model, mstride, model64, err);
 }
