@@ -12,6 +12,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -69,10 +70,12 @@ struct bbgpu_ctx {
     size_t d_mem_cap = 0;
     int *d_pix = nullptr;
     size_t d_pix_cap = 0;
-    int *d_bucket = nullptr;
+    int4 *d_bucket = nullptr;     // (2 int4 per entry)
     size_t d_bucket_cap = 0;
     int *d_tcount = nullptr, *d_toff = nullptr, *d_tcur = nullptr;
     size_t d_tcount_cap = 0, d_toff_cap = 0, d_tcur_cap = 0;
+    int *d_scan = nullptr;
+    size_t d_scan_cap = 0;
     float *d_model = nullptr;
     size_t d_model_cap = 0;
     float *d_smooth = nullptr;
@@ -149,6 +152,7 @@ static int hgrow(bbgpu_ctx *ctx, T **p, size_t *cap, size_t n) {
 
 static void layout_dev_free(LayoutDev &d) {
     cudaFree(d.cf); cudaFree(d.cd); cudaFree(d.sub); cudaFree(d.slow_base); cudaFree(d.hz); cudaFree(d.slow_val);
+    cudaFree(d.nf); cudaFree(d.nvs); cudaFree(d.ord); cudaFree(d.pbase);
     cudaFree(d.sub_base); cudaFree(d.cloud_base);
     memset(&d, 0, sizeof d);
 }
@@ -179,6 +183,7 @@ static int upload_layout(bbgpu_ctx *ctx, LayoutEntry &E) {
     CK(cudaMalloc(&D.slow_val, (size_t)(H.nslow ? H.nslow : 1) * sizeof(double)));
     CK(cudaMalloc(&D.sub_base, (size_t)(H.nsub ? H.nsub : 1) * sizeof(long long)));
     CK(cudaMalloc(&D.cloud_base, (size_t)(H.nsub ? H.nsub : 1) * sizeof(int)));
+    CK(cudaMalloc(&D.nvs, (size_t)(H.nsub ? H.nsub : 1) * sizeof(int)));
     CK(cudaMemcpy(D.cf, cf.data(), nc * sizeof(float4), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(D.cd, cd.data(), 4 * nc * sizeof(double), cudaMemcpyHostToDevice));
     if (H.ncloud) {
@@ -186,10 +191,58 @@ static int upload_layout(bbgpu_ctx *ctx, LayoutEntry &E) {
         CK(cudaMemcpy(D.slow_base, H.slow_base, (size_t)H.ncloud * sizeof(int), cudaMemcpyHostToDevice));
     }
     if (H.nsubcloud) CK(cudaMemcpy(D.hz, H.hz, (size_t)H.nsubcloud * sizeof(int32_t), cudaMemcpyHostToDevice));
+    {
+        // the normal deviates of each cloud, sorted by value (descending when the channel decreases with the
+        // velocity): the channels of a cloud's samples are then non-decreasing along the sorted order
+        int64_t kn[128];
+        double wn[128], fn[128];
+        bbh_zig_tables(kn, wn, fn);
+        const GridDev &g = ctx->g;
+        const bool desc = g.axtyp == 4 ? g.cdelt3 < 0 : g.cdelt3 > 0;
+        std::vector<long long> pbase(H.nsub ? H.nsub : 1);
+        long long np = 0;
+        for (int ir = 0; ir < H.nsub; ir++) {
+            pbase[ir] = np;
+            np += (long long)H.nc[ir] * ((H.nv[ir] + 3) & ~3);
+        }
+        size_t nsc = (size_t)(np ? np : 1);
+        std::vector<float> nf(nsc, 0.0f);
+        std::vector<uint16_t> ord(nsc, 0);
+        std::vector<double> val;
+        std::vector<int> idx;
+        long long so = 0, q = 0;
+        for (int c = 0; c < H.ncloud; c++) {
+            const int ir = H.sub[c];
+            const int nv = H.nv[ir];
+            val.resize(nv);
+            idx.resize(nv);
+            for (int i = 0; i < nv; i++, q++) {
+                int32_t h = H.hz[q];
+                int iz = h & 127;
+                long long ah = h < 0 ? -(long long)h : (long long)h;
+                val[i] = ah < kn[iz] ? (double)h * wn[iz] : H.slow_val[so++];
+                idx[i] = i;
+            }
+            std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return desc ? val[a] > val[b] : val[a] < val[b]; });
+            long long b0 = pbase[ir] + (long long)(c - H.cloud_base[ir]) * ((nv + 3) & ~3);
+            for (int i = 0; i < nv; i++) {
+                nf[b0 + i] = (float)val[idx[i]];
+                ord[b0 + i] = (uint16_t)idx[i];
+            }
+        }
+        D.npad = np;
+        CK(cudaMalloc(&D.pbase, pbase.size() * sizeof(long long)));
+        CK(cudaMemcpy(D.pbase, pbase.data(), pbase.size() * sizeof(long long), cudaMemcpyHostToDevice));
+        CK(cudaMalloc(&D.nf, nsc * sizeof(float)));
+        CK(cudaMalloc(&D.ord, nsc * sizeof(uint16_t)));
+        CK(cudaMemcpy(D.nf, nf.data(), nsc * sizeof(float), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(D.ord, ord.data(), nsc * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    }
     if (H.nslow) CK(cudaMemcpy(D.slow_val, H.slow_val, (size_t)H.nslow * sizeof(double), cudaMemcpyHostToDevice));
     if (H.nsub) {
         CK(cudaMemcpy(D.sub_base, H.sub_base, (size_t)H.nsub * sizeof(long long), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(D.cloud_base, H.cloud_base, (size_t)H.nsub * sizeof(int), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(D.nvs, H.nv, (size_t)H.nsub * sizeof(int), cudaMemcpyHostToDevice));
     }
     return 0;
 }
@@ -295,7 +348,7 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
     for (auto &a : ctx->d_deff)
         for (auto &b : a) cudaFree(b);
     cudaFree(ctx->d_sub); cudaFree(ctx->d_mem); cudaFree(ctx->d_pix); cudaFree(ctx->d_bucket);
-    cudaFree(ctx->d_tcount); cudaFree(ctx->d_toff); cudaFree(ctx->d_tcur); cudaFree(ctx->d_model);
+    cudaFree(ctx->d_tcount); cudaFree(ctx->d_toff); cudaFree(ctx->d_tcur); cudaFree(ctx->d_model); cudaFree(ctx->d_scan);
     cudaFree(ctx->d_smooth); cudaFree(ctx->d_model64); cudaFree(ctx->d_partial); cudaFree(ctx->d_out2);
     cudaFree(ctx->d_err);
     cudaFreeHost(ctx->h_sub); cudaFreeHost(ctx->h_mem); cudaFreeHost(ctx->h_out2); cudaFreeHost(ctx->h_err);
@@ -387,8 +440,8 @@ extern "C" int bbgpu_set_grid(bbgpu_ctx *ctx, const bbgpu_grid *gr, const double
     CK(cudaMalloc(&ctx->d_cd2if, g.nz * sizeof(float)));
     CK(cudaMemcpy(ctx->d_cd2i, cd2i, g.nz * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->d_cd2if, cf.data(), g.nz * sizeof(float), cudaMemcpyHostToDevice));
-    // deposit tile: pixels x channels of 8-byte sums within 64 KB
-    int tp = 65536 / (8 * g.nz);
+    // deposit tile: pixels x channels of 8-byte sums within 56 KB (3 CTAs per SM with the staging buffers)
+    int tp = 57344 / (8 * g.nz);
     if (tp >= 64) { ctx->tx = 8; ctx->ty = 8; }
     else if (tp >= 32) { ctx->tx = 8; ctx->ty = 4; }
     else if (tp >= 16) { ctx->tx = 4; ctx->ty = 4; }
@@ -474,6 +527,8 @@ static int batch_prepare(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const
                         "eval: member %d has another cloud layout (seed, radii, cloud or velocity counts): "
                         "evaluate it in another batch", k);
     }
+    for (int i = 0; i < nsub; i++)
+        if (nv0[i] > 65535) return fail(ctx, BBGPU_ERR_ARG, "eval: NV above 65535 velocity samples per cloud");
     LayoutEntry *E = nullptr;
     int rc = get_layout(ctx, seed, nsub, nc0.data(), nv0.data(), R0.data(), &E);
     if (rc) return rc;
@@ -520,10 +575,11 @@ static int batch_prepare(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const
     if ((rc = dgrow(ctx, &ctx->d_sub, &ctx->d_sub_cap, (size_t)nb * (nsub ? nsub : 1)))) return rc;
     if ((rc = dgrow(ctx, &ctx->d_mem, &ctx->d_mem_cap, (size_t)nb))) return rc;
     if ((rc = dgrow(ctx, &ctx->d_pix, &ctx->d_pix_cap, ncl))) return rc;
-    if ((rc = dgrow(ctx, &ctx->d_bucket, &ctx->d_bucket_cap, ncl))) return rc;
-    if ((rc = dgrow(ctx, &ctx->d_tcount, &ctx->d_tcount_cap, (size_t)toff + 1))) return rc;
-    if ((rc = dgrow(ctx, &ctx->d_toff, &ctx->d_toff_cap, (size_t)toff + 1))) return rc;
-    if ((rc = dgrow(ctx, &ctx->d_tcur, &ctx->d_tcur_cap, (size_t)toff + 1))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_bucket, &ctx->d_bucket_cap, ncl * (ENTRY_BYTES / 16)))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_tcount, &ctx->d_tcount_cap, (size_t)toff * NOWN + 1))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_toff, &ctx->d_toff_cap, (size_t)toff * NOWN + 1))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_tcur, &ctx->d_tcur_cap, (size_t)toff * NOWN + 1))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_scan, &ctx->d_scan_cap, (size_t)toff * NOWN / 1024 + 2))) return rc;
     if ((rc = dgrow(ctx, &ctx->d_model, &ctx->d_model_cap, (size_t)nb * ctx->mstride))) return rc;
     if ((rc = dgrow(ctx, &ctx->d_partial, &ctx->d_partial_cap, (size_t)2 * nb * (ctx->npart ? ctx->npart : 1)))) return rc;
     if ((rc = dgrow(ctx, &ctx->d_out2, &ctx->d_out2_cap, (size_t)2 * nb))) return rc;
@@ -547,19 +603,20 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
     cudaStream_t s = ctx->stream;
     const bool tm = ctx->timing;
     if (tm) CK(cudaEventRecord(ctx->ev[0], s));
-    CK(cudaMemsetAsync(ctx->d_tcount, 0, sizeof(int) * (size_t)(ctx->ntile_total + 1), s));
+    CK(cudaMemsetAsync(ctx->d_tcount, 0, sizeof(int) * (size_t)(ctx->ntile_total * NOWN + 1), s));
     launch_mc_bin(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->nb, ctx->tx, ctx->ty, ctx->d_pix, ctx->d_tcount,
                   ctx->d_err);
     CKL();
     if (tm) CK(cudaEventRecord(ctx->ev[1], s));
-    launch_scan_tiles(s, ctx->d_tcount, ctx->d_toff, ctx->d_tcur, ctx->ntile_total);
+    launch_scan_tiles(s, ctx->d_tcount, ctx->d_toff, ctx->d_tcur, ctx->ntile_total * NOWN, ctx->d_scan);
     CKL();
     if (tm) CK(cudaEventRecord(ctx->ev[2], s));
-    launch_mc_scatter(s, L, ctx->d_mem, ctx->nb, ctx->tx, ctx->ty, ctx->d_pix, ctx->d_tcur, ctx->d_bucket);
+    launch_mc_scatter(s, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->nb, ctx->tx, ctx->ty, ctx->d_pix, ctx->d_tcur,
+                      ctx->d_bucket);
     CKL();
     if (tm) CK(cudaEventRecord(ctx->ev[3], s));
     launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->tx, ctx->ty,
-                      ctx->d_pix, ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig, ctx->d_cd2if, ctx->d_cd2i,
+                      ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig, ctx->d_cd2if, ctx->d_cd2i,
                       ctx->d_model, ctx->mstride, ctx->want64 ? ctx->d_model64 : nullptr, ctx->d_err);
     CKL();
     if (tm) CK(cudaEventRecord(ctx->ev[4], s));

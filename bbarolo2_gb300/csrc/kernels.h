@@ -14,9 +14,15 @@ struct LayoutDev {
     double *cd;          // per cloud: the same in float64, 4 values per cloud
     int *sub;            // per cloud: sub-ring
     int *slow_base;      // per cloud: slow normals before it
-    int32_t *hz;         // per sub-cloud
+    int32_t *hz;         // per sub-cloud: the first word of its normal (exact path)
+    float *nf;           // per cloud: its normal deviates in float32, sorted (ascending channel order); each
+                         // cloud's run starts at a multiple of 4 floats (16 bytes): pbase[ir] + (c - cloud_base) nvp
+    uint16_t *ord;       // same layout: the index in the stream of the sorted normal at that position
+    long long *pbase;    // per sub-ring: first padded position
+    long long npad;      // padded length
     double *slow_val;    // slow normal values
     long long *sub_base; // per sub-ring: first sub-cloud
+    int *nvs;            // per sub-ring: velocity samples per cloud
     int *cloud_base;     // per sub-ring: first cloud
 };
 
@@ -41,17 +47,21 @@ struct ZigDev {
 
 // ---- MC (mc.cu)
 // For every (member, cloud): its pixel in the member's box (or -1) and the count of clouds per tile.
+// Tile lists are split by owner warp (NOWN per tile): list index = (tile_off + tile) * NOWN + owner.
+#define NOWN 8
 void launch_mc_bin(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
                    const MemberDev *mem, int nb, int tx, int ty, int *pix, int *tile_count, int *err);
-// Exclusive scan of tile counts into offsets (and cursors), for ntile_total tiles.
-void launch_scan_tiles(cudaStream_t s, const int *count, int *offset, int *cursor, int ntile_total);
-void launch_mc_scatter(cudaStream_t s, const LayoutDev &L, const MemberDev *mem, int nb, int tx, int ty,
-                       const int *pix, int *cursor, int *bucket);
+// Exclusive scan of n list counts into offsets (and cursors); scratch holds (n + 1023) / 1024 ints.
+void launch_scan_tiles(cudaStream_t s, const int *count, int *offset, int *cursor, int n, int *scratch);
+// bucket: 32-byte entries (Entry in mc.cu), one per in-box (member, cloud)
+#define ENTRY_BYTES 32
+void launch_mc_scatter(cudaStream_t s, const LayoutDev &L, const SubMC *sub, int nsub, const MemberDev *mem, int nb,
+                       int tx, int ty, const int *pix, int *cursor, void *bucket);
 // Deposits the clouds of every tile into a shared-memory fixed-point tile and writes the model
 // (by, bx, nz) float32 of each member at model + k * mstride (and, if model64, float64 sums).
 void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
-                       const MemberDev *mem, const MemberDev *mem_host, int nb, int tx, int ty, const int *pix,
-                       const int *offset, const int *count, const int *bucket, const ZigDev *zig,
+                       const MemberDev *mem, const MemberDev *mem_host, int nb, int tx, int ty,
+                       const int *offset, const int *count, const void *bucket, const ZigDev *zig,
                        const float *cd2if, const double *cd2i, float *model, long long mstride, double *model64,
                        int *err);
 

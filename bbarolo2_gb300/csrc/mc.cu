@@ -136,18 +136,440 @@ __global__ void k_mc_bin(GridDev g, LayoutDev L, const SubMC *__restrict__ sub, 
     }
     int px = ix - M.blo0, py = iy - M.blo1;
     pix[idx] = py * M.bx + px;
-    atomicAdd(&tile_count[M.tile_off + (py / ty) * M.ntx + px / tx], 1);
+    const int owner = ((py % ty) * tx + (px % tx)) % NOWN;
+    atomicAdd(&tile_count[(M.tile_off + (py / ty) * M.ntx + px / tx) * NOWN + owner], 1);
 }
 
-__global__ void k_scan_tiles(const int *__restrict__ count, int *__restrict__ offset, int *__restrict__ cursor,
-                             int n) {
-    // one CTA of 1024 threads: each scans a contiguous chunk, then the chunk totals are scanned
+// The deposit entry of a (member, cloud) in its tile's list: computed here, one thread per entry.
+struct __align__(16) Entry {
+    int c;          // cloud
+    int pb;         // first of the cloud's sorted normals (padded layout)
+    int meta;       // nv | pixel in the tile << 16 | half << 24
+    float tc;       // channel of the cloud's velocity (line 0, float32 with the bound epsc)
+    long long fix;  // fixed-point flux of one sample (line 0)
+    float epsc;     // rounding bound of tc
+    float sg;       // channels per unit normal deviate
+};
+
+// channel centre of a cloud and its rounding bound (float32), for line nl (see the fast path of k_mc_deposit)
+__device__ __forceinline__ void cloud_centre(const SubMC &S, float4 cf, int nl, float &tc, float &epsc) {
+    const float zf = cf.w * S.z0f;
+    const float azf = fabsf(zf);
+    float vr = S.vrotf;
+    if (azf > S.zcylf) {
+        float v = S.vrotf - S.dvdzf * (azf - S.zcylf);
+        vr = S.vrotf >= 0.0f ? fmaxf(v, 0.0f) : fminf(v, 0.0f);
+    }
+    const float base = vr * cf.y + S.vradf * cf.z;
+    const float mbase = fabsf(vr * cf.y) + fabsf(S.vradf * cf.z) + fabsf(S.dvdzf) * (azf + fabsf(S.zcylf));
+    tc = S.c0[nl] + base * S.sia[nl];
+    epsc = (fabsf(S.c0[nl]) + mbase * fabsf(S.sia[nl]) + 1.0f) * EPS_REL;
+}
+
+__global__ void k_mc_scatter(LayoutDev L, const SubMC *__restrict__ sub, int nsub, const MemberDev *__restrict__ mem,
+                             int nb, int tx, int ty, const int *__restrict__ pix, int *__restrict__ cursor,
+                             Entry *__restrict__ bucket) {
+    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)nb * L.ncloud) return;
+    int p = pix[idx];
+    if (p < 0) return;
+    int k = (int)(idx / L.ncloud);
+    int c = (int)(idx - (long long)k * L.ncloud);
+    const MemberDev &M = mem[k];
+    int py = p / M.bx, px = p - py * M.bx;
+    const int lp = (py % ty) * tx + (px % tx);
+    int slot = atomicAdd(&cursor[(M.tile_off + (py / ty) * M.ntx + px / tx) * NOWN + lp % NOWN], 1);
+    const float4 cf = L.cf[c];
+    const int half = cf.y >= 0.0f ? 0 : 1;
+    const int ir = L.sub[c];
+    const int nv = L.nvs[ir];
+    const SubMC &S = sub[(size_t)k * nsub + ir];
+    Entry e;
+    e.c = c;
+    e.pb = (int)(L.pbase[ir] + (long long)(c - L.cloud_base[ir]) * ((nv + 3) & ~3));
+    e.meta = (nv & 0xffff) | (lp << 16) | (half << 24);
+    cloud_centre(S, cf, 0, e.tc, e.epsc);
+    e.fix = S.fix[half][0];
+    e.sg = S.sg[0];
+    bucket[slot] = e;
+}
+
+// the exact channel of a sub-cloud (bbarolo/galmod.py:153-170), not clipped to the cube
+__device__ __noinline__ long long channel_exact_raw(const SubMC &S, const GridDev &g, const double *cd, double nx,
+                                                    int nl) {
+    const double vs = vlos_exact(S, cd);
+    if (g.axtyp == 4 && g.nlines == 1) {
+        double gz = __dadd_rn(__dmul_rn(vs, g.ia), g.ib);
+        double sg = __dmul_rn(S.vdisptmp, g.ia);
+        return lround_ref(__dadd_rn(gz, __dmul_rn(nx, sg)));
+    }
+    double v = __dadd_rn(vs, __dmul_rn(nx, S.vdisptmp));
+    return lround_ref(velgrid_exact(v, g, nl));
+}
+
+// the exact channel in the cube, or -1 outside it
+__device__ __forceinline__ int channel_exact(const SubMC &S, const GridDev &g, const double *cd, double nx, int nl) {
+    const long long is = channel_exact_raw(S, g, cd, nx, nl);
+    return (is < 0 || is >= g.nz) ? -1 : (int)is;
+}
+
+#define XQ 64         // capacity of a warp's queue of sub-clouds deferred to the exact path
+
+// The exact normal deviate of sub-cloud iv of a cloud: from its first word, or from the list of slow ones
+// (its ordinal among the cloud's slow normals counted from the words before it: a rare path).
+__device__ __noinline__ double normal_exact(const LayoutDev &L, const ZigDev *zig, long long sb, int iv, int slow_base,
+                                            int *err) {
+    const int h = L.hz[sb + iv];
+    const int iz = h & 127;
+    const unsigned ah = h < 0 ? 0u - (unsigned)h : (unsigned)h;
+    if (ah < zig->kn[iz]) return __dmul_rn((double)h, zig->wn[iz]);
+    int o = slow_base;
+    for (int j = 0; j < iv; j++) {
+        const int hj = L.hz[sb + j];
+        const unsigned aj = hj < 0 ? 0u - (unsigned)hj : (unsigned)hj;
+        o += !(aj < zig->kn[hj & 127]);
+    }
+    if (o >= L.nslow) {
+        atomicOr(err, ERR_LAYOUT);
+        return 0.0;
+    }
+    return L.slow_val[o];
+}
+
+// Adds v to row[ch] for the lanes with a pending deposit, one lane at a time: the warp owns its pixels, so the
+// plain read-modify-write is race-free once same-channel lanes are serialised (a rare path).
+__device__ __forceinline__ void warp_serial_add(unsigned long long *row, bool pending, int ch, long long v, int lane) {
+    unsigned mask = __ballot_sync(0xffffffffu, pending);
+    while (mask) {
+        const int src = __ffs(mask) - 1;
+        const int c = __shfl_sync(0xffffffffu, ch, src);
+        const long long w = __shfl_sync(0xffffffffu, v, src);
+        if (lane == 0) row[c] += (unsigned long long)w;
+        __syncwarp();
+        mask &= mask - 1;
+    }
+}
+
+__device__ __forceinline__ long long stream_base(const LayoutDev &L, int c, int ir, int nv) {
+    return L.sub_base[ir] + (long long)(c - L.cloud_base[ir]) * nv;
+}
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+#define WB 256        // sorted normals of a cloud staged per warp (clouds with more samples: per-sample path)
+#define DEPTH 3       // clouds in flight per warp (cp.async pipeline)
+#define EMAX 8        // sorted samples per lane (WB / 32)
+
+// The channels of one cloud's samples counted one by one (float32 with the exact fallback) into the warp's bins
+// [ws, ws + 32 m) and added to the pixel's row; samples beyond the bins are added individually. Used when the
+// binary search does not apply: non-linear spectral axes, more than WB samples, a centre out of range.
+__device__ __noinline__ void deposit_per_sample(const GridDev &g, const LayoutDev &L, const ZigDev *zig,
+                                                const SubMC &S, int c, long long pb, long long sb, int nv, float tc,
+                                                float sg, float epsc, float epsn, long long fix, int nl, bool fast,
+                                                unsigned long long *row, int *myh, int *myq, int lane, int *err) {
+    const unsigned ltmask = (1u << lane) - 1u;
+    const int nz = g.nz;
+    const float span = 10.0f * fabsf(sg) + 2.0f;
+    const int m = span <= 32.0f ? 1 : (span <= 64.0f ? 2 : 4);
+    const int ws = fabsf(tc) < 1.0e6f ? (int)floorf(tc + 0.5f) - 16 * m : 0;
+    int nq = 0;
+    for (int j0 = 0; j0 < nv; j0 += 32) {
+        const int i = j0 + lane;
+        const bool act = i < nv;
+        const float nf = act ? __ldg(&L.nf[pb + i]) : 0.0f;
+        const float tt = fmaf(nf, sg, tc);
+        const float eps = fmaf(fabsf(nf), epsn, epsc);
+        const float f = tt + 0.5f;
+        const float fl = floorf(f);
+        const float dd = f - fl;
+        const bool ok = fast && fabsf(tt) < 1.0e6f && dd >= eps && dd <= 1.0f - eps;
+        const bool ex = act && !ok;
+        if (__any_sync(0xffffffffu, ex)) {
+            const unsigned eb = __ballot_sync(0xffffffffu, ex);
+            if (ex) myq[nq + __popc(eb & ltmask)] = i;
+            nq += __popc(eb);
+        }
+        const int isub = (int)fl;
+        const bool dep = act && ok && isub >= 0 && isub < nz;
+        const int d = isub - ws;
+        const bool inw = dep && d >= 0 && d < 32 * m;
+        if (inw) atomicAdd(&myh[d], 1);
+        if (__any_sync(0xffffffffu, dep && !inw)) warp_serial_add(row, dep && !inw, isub, fix, lane);
+        if (nq > XQ - 32 || (j0 + 32 >= nv && nq > 0)) {             // (warp-uniform)
+            __syncwarp();
+            for (int q0 = 0; q0 < nq; q0 += 32) {
+                const int q = q0 + lane;
+                int is = -1;
+                if (q < nq) {
+                    const double nx = normal_exact(L, zig, sb, L.ord[pb + myq[q]], __ldg(&L.slow_base[c]), err);
+                    is = channel_exact(S, g, L.cd + 4 * (size_t)c, nx, nl);
+                }
+                warp_serial_add(row, is >= 0, is, fix, lane);
+            }
+            __syncwarp();
+            nq = 0;
+        }
+    }
+    __syncwarp();
+    for (int q = 0; q < m; q++) {
+        const int bb = lane + 32 * q;
+        const int cnt = myh[bb];
+        if (cnt) {
+            row[ws + bb] += (unsigned long long)(fix * (long long)cnt);
+            myh[bb] = 0;
+        }
+    }
+    __syncwarp();
+}
+
+// The run-length deposit of one cloud whose E samples per lane are staged (sorted) in w: lane l takes samples
+// l E .. l E + E - 1, computes their channels (float32 within one rounding bound for the cloud; the exact
+// float64 channel near a half-integer), and every run of equal channels is added once to the pixel row:
+// count = index of the next run's first sample - index of its first sample (channels are non-decreasing).
+template <int E>
+__device__ __forceinline__ void deposit_runs(const GridDev &g, const LayoutDev &L, const ZigDev *zig,
+                                             const SubMC *__restrict__ subk, const float *w, int c, long long pb,
+                                             int nv, float tc, float sg, float eps, long long fix,
+                                             unsigned long long *row, int lane, int *err) {
+    const int nz = g.nz;
+    const int i0 = lane * E;
+    int ch[E];
+    unsigned need = 0;
+#pragma unroll
+    for (int j = 0; j < E; j++) {
+        ch[j] = 0x7fffffff;                                   // (past the last sample: the terminator)
+        const bool in = i0 + j < nv;
+        const float f = fmaf(in ? w[i0 + j] : 0.0f, sg, tc) + 0.5f;
+        const float fl = floorf(f);
+        const float dd = f - fl;
+        if (in) {
+            if (dd >= eps && dd <= 1.0f - eps) ch[j] = (int)fl;
+            else need |= 1u << j;
+        }
+    }
+    if (__any_sync(0xffffffffu, need != 0)) {                 // rare: exact channels
+        const int ir = __ldg(&L.sub[c]);
+        const SubMC &S = subk[ir];
+        const long long sb = stream_base(L, c, ir, nv);
+        const int sbase = __ldg(&L.slow_base[c]);
+#pragma unroll
+        for (int j = 0; j < E; j++)
+            if (need & (1u << j)) {
+                const double nx = normal_exact(L, zig, sb, L.ord[pb + i0 + j], sbase, err);
+                const long long is = channel_exact_raw(S, g, L.cd + 4 * (size_t)c, nx, 0);
+                ch[j] = is < -0x3fffffffLL ? -0x3fffffff : (is > 0x3fffffffLL ? 0x3fffffff : (int)is);
+            }
+    }
+    // run starts: a sample whose channel differs from the previous sample's (lane 0's first always starts)
+    const int prev0 = __shfl_up_sync(0xffffffffu, ch[E - 1], 1);
+    unsigned starts = 0;
+#pragma unroll
+    for (int j = 0; j < E; j++) {
+        const int pv = j == 0 ? (lane == 0 ? (int)0x80000000 : prev0) : ch[j - 1];
+        if (ch[j] != pv && i0 + j < nv) starts |= 1u << j;
+    }
+    // the first start after this lane's samples (or the end)
+    const unsigned B = __ballot_sync(0xffffffffu, starts != 0);
+    const unsigned after = lane < 31 ? (B & (0xffffffffu << (lane + 1))) : 0u;
+    const int l2 = after ? __ffs(after) - 1 : lane;
+    const unsigned s2 = __shfl_sync(0xffffffffu, starts, l2);
+    const int nextl = after ? l2 * E + __ffs(s2) - 1 : nv;
+    while (starts) {
+        const int j = __ffs(starts) - 1;
+        starts &= starts - 1;
+        const int nxt = starts ? i0 + __ffs(starts) - 1 : nextl;
+        int chj = ch[0];
+#pragma unroll
+        for (int q = 1; q < E; q++)
+            if (q == j) chj = ch[q];
+        const int cnt = nxt - (i0 + j);
+        if (chj >= 0 && chj < nz) row[chj] += (unsigned long long)(fix * (long long)cnt);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_mc_deposit(GridDev g, LayoutDev L, const SubMC *__restrict__ sub, int nsub,
+                                                    const MemberDev *__restrict__ mem, int tx, int ty,
+                                                    const int *__restrict__ offset, const int *__restrict__ count,
+                                                    const Entry *__restrict__ bucket, const ZigDev *__restrict__ zig,
+                                                    const float *__restrict__ cd2if, const double *__restrict__ cd2i,
+                                                    float *__restrict__ model, long long mstride,
+                                                    double *__restrict__ model64, int *err) {
+    extern __shared__ unsigned long long tile[];   // TP x nz sums, then the warps' staging slots, then nz scales
+    __shared__ int bins[8][128 + XQ];
+    __shared__ Entry ents[8][DEPTH];
+    const int k = blockIdx.x;
+    const MemberDev &M = mem[k];
+    const int t = blockIdx.y;
+    if (t >= M.ntx * M.nty) return;
+    const int nz = g.nz;
+    const int TP = tx * ty;
+    const int tyi = t / M.ntx, txi = t - tyi * M.ntx;
+    const int x0 = txi * tx, y0 = tyi * ty;
+    float *mout = model + (size_t)k * mstride;
+    // a tile without clouds (outside the disk): zeros, without the shared-memory tile
+    {
+        int any = 0;
+        if (threadIdx.x < NOWN) any = count[(M.tile_off + t) * NOWN + threadIdx.x] != 0;
+        if (!__syncthreads_or(any)) {
+            const int wid = threadIdx.x >> 5, ln = threadIdx.x & 31;
+            for (int lp = wid; lp < TP; lp += 8) {
+                const int py = y0 + lp / tx, px = x0 + lp % tx;
+                if (py >= M.by || px >= M.bx) continue;
+                float *o = mout + ((size_t)py * M.bx + px) * nz;
+                for (int z = ln; z < nz; z += 32) o[z] = 0.0f;
+                if (model64) {
+                    double *o64 = model64 + (size_t)k * mstride + ((size_t)py * M.bx + px) * nz;
+                    for (int z = ln; z < nz; z += 32) o64[z] = 0.0;
+                }
+            }
+            return;
+        }
+    }
+    // (the staging slots start at a 16-byte boundary: cp.async copies 16-byte chunks)
+    float *stg = (float *)(((uintptr_t)(tile + (size_t)TP * nz) + 15) & ~(uintptr_t)15);
+    float *chs = stg + 8 * DEPTH * WB;
+    {
+        ulonglong2 *t2 = (ulonglong2 *)tile;
+        for (int i = threadIdx.x; i < TP * nz / 2; i += blockDim.x) t2[i] = make_ulonglong2(0ULL, 0ULL);
+        if (((TP * nz) & 1) && threadIdx.x == 0) tile[TP * nz - 1] = 0ULL;
+        for (int i = threadIdx.x; i < 8 * (128 + XQ); i += blockDim.x) (&bins[0][0])[i] = 0;
+        for (int z = threadIdx.x; z < nz; z += blockDim.x) chs[z] = ldexpf(cd2if[z], -M.fix_exp);
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lst = (M.tile_off + t) * NOWN + warp;              // this warp's list: the clouds of its pixels
+    const int beg = offset[lst], n = count[lst];
+    const bool fast_ok = g.fast_ok;
+    const SubMC *__restrict__ subk = sub + (size_t)k * nsub;
+    float *slots = stg + warp * DEPTH * WB;
+    int *myh = bins[warp];
+    int *myq = myh + 128;
+    // the (pb, meta) of the list's entries, 32 per register chunk: chunk of the current entry and the next one
+    int pa = lane < n ? __ldg(&bucket[beg + lane].pb) : 0, ma = lane < n ? __ldg(&bucket[beg + lane].meta) : 0;
+    int pn = 32 + lane < n ? __ldg(&bucket[beg + 32 + lane].pb) : 0;
+    int mn = 32 + lane < n ? __ldg(&bucket[beg + 32 + lane].meta) : 0;
+    // prefetch of entry j and its normals into slot j % DEPTH (one commit group per entry); i: the entry in use
+    auto issue = [&](int j, int i) {
+        if (j < n) {
+            const bool same = (j >> 5) == (i >> 5);
+            const int pbj = __shfl_sync(0xffffffffu, same ? pa : pn, j & 31);
+            const int mj = __shfl_sync(0xffffffffu, same ? ma : mn, j & 31);
+            const Entry *src = bucket + beg + j;
+            Entry *dst = &ents[warp][j % DEPTH];
+            if (lane < 2) cp_async16((char *)dst + 16 * lane, (const char *)src + 16 * lane);
+            const int nv = mj & 0xffff;
+            if (nv <= WB) {
+                const float *nsrc = L.nf + (unsigned)pbj;
+                float *ndst = slots + (j % DEPTH) * WB;
+                for (int q = lane; q < (nv + 3) >> 2; q += 32) cp_async16(ndst + 4 * q, nsrc + 4 * q);
+            }
+        }
+        cp_async_commit();
+    };
+#pragma unroll
+    for (int d = 0; d < DEPTH - 1; d++) issue(d, 0);
+    for (int i = 0; i < n; i++) {
+        issue(i + DEPTH - 1, i);
+        cp_async_wait<DEPTH - 1>();
+        __syncwarp();
+        const Entry en = ents[warp][i % DEPTH];
+        const float *w = slots + (i % DEPTH) * WB;
+        const int c = en.c;
+        const int nv = en.meta & 0xffff, lp = (en.meta >> 16) & 255, half = en.meta >> 24;
+        unsigned long long *row = tile + (size_t)lp * nz;
+        const float tc = en.tc, sg = en.sg, epsc = en.epsc;
+        const long long fix = en.fix;
+        const float epsn = fabsf(sg) * EPS_REL;
+        const float span = 10.0f * fabsf(sg) + 2.0f;
+        const int m = span <= 32.0f ? 1 : (span <= 64.0f ? 2 : 4);
+        const bool fast = fast_ok && nv <= WB && fabsf(tc) < 1.0e5f;
+        const int ws = fast ? (int)floorf(tc + 0.5f) - 16 * m : 0;
+        if (fast) {
+            // one rounding bound for the cloud: its largest |normal| is at an end of the sorted run
+            const float nmax = fmaxf(fabsf(w[0]), fabsf(w[nv - 1]));
+            const float eps = fmaf(nmax, epsn, epsc);
+            const int E = (nv + 31) >> 5;
+            if (E <= 1) deposit_runs<1>(g, L, zig, subk, w, c, (unsigned)en.pb, nv, tc, sg, eps, fix, row, lane, err);
+            else if (E <= 2) deposit_runs<2>(g, L, zig, subk, w, c, (unsigned)en.pb, nv, tc, sg, eps, fix, row, lane, err);
+            else if (E <= 4) deposit_runs<4>(g, L, zig, subk, w, c, (unsigned)en.pb, nv, tc, sg, eps, fix, row, lane, err);
+            else deposit_runs<8>(g, L, zig, subk, w, c, (unsigned)en.pb, nv, tc, sg, eps, fix, row, lane, err);
+        }
+        if (!fast || g.nlines > 1) {
+            // the general path: every line with the per-sample kernel (lines after the first, non-linear axes,
+            // many samples, a centre out of range)
+            const int ir = __ldg(&L.sub[c]);
+            const SubMC &S = sub[(size_t)k * nsub + ir];
+            const float4 cf = __ldg(&L.cf[c]);
+            for (int nl = fast ? 1 : 0; nl < g.nlines; nl++) {
+                float tcl, epscl;
+                cloud_centre(S, cf, nl, tcl, epscl);
+                deposit_per_sample(g, L, zig, S, c, (unsigned)en.pb, stream_base(L, c, ir, nv), nv, tcl, S.sg[nl],
+                                   epscl, fabsf(S.sg[nl]) * EPS_REL, S.fix[half][nl], nl, fast_ok, row, myh, myq, lane,
+                                   err);
+            }
+        }
+        __syncwarp();
+        if (((i + 1) & 31) == 0) {                            // next chunk of entries
+            pa = pn;
+            ma = mn;
+            const int j = i + 1 + 32 + lane;
+            pn = j < n ? __ldg(&bucket[beg + j].pb) : 0;
+            mn = j < n ? __ldg(&bucket[beg + j].meta) : 0;
+        }
+    }
+    cp_async_wait<0>();
+    __syncthreads();
+    // write-out: a warp per pixel, lanes along the channels (the sums times cd2i 2^-e, as float32)
+    for (int lp = warp; lp < TP; lp += 8) {
+        const int py = y0 + lp / tx, px = x0 + lp % tx;
+        if (py >= M.by || px >= M.bx) continue;
+        const unsigned long long *src = tile + (size_t)lp * nz;
+        float *o = mout + ((size_t)py * M.bx + px) * nz;
+        for (int z = lane; z < nz; z += 32) {
+            // (int64 -> float32 through two exact 32-bit halves: one rounding in the final add)
+            const long long v = (long long)src[z];
+            const float hi = (float)(int)(v >> 32) * 4294967296.0f;
+            const float lo = (float)(unsigned)(v & 0xffffffffLL);
+            o[z] = (hi + lo) * chs[z];
+        }
+        if (model64) {
+            double *o64 = model64 + (size_t)k * mstride + ((size_t)py * M.bx + px) * nz;
+            for (int z = lane; z < nz; z += 32) o64[z] = ldexp((double)(long long)src[z] * cd2i[z], -M.fix_exp);
+        }
+    }
+}
+
+// exclusive scan of n counts in three passes: block sums, scan of the sums, block scans
+__global__ void k_scan_a(const int *__restrict__ count, int n, int *__restrict__ bsum) {
+    __shared__ int r[32];
+    const int i = blockIdx.x * 1024 + threadIdx.x;
+    int v = i < n ? count[i] : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) r[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        v = r[threadIdx.x];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) bsum[blockIdx.x] = v;
+    }
+}
+
+__global__ void k_scan_b(int *__restrict__ bsum, int nb) {
+    // one CTA of 1024 threads over nb block sums (chunks per thread), in place, exclusive
     __shared__ int part[1024];
-    int t = threadIdx.x;
-    int chunk = (n + 1023) / 1024;
-    int b = t * chunk, e = min(n, b + chunk);
+    const int t = threadIdx.x;
+    const int chunk = (nb + 1023) / 1024;
+    const int b = t * chunk, e = min(nb, b + chunk);
     int s = 0;
-    for (int i = b; i < e; i++) s += count[i];
+    for (int i = b; i < e; i++) s += bsum[i];
     part[t] = s;
     __syncthreads();
     for (int d = 1; d < 1024; d <<= 1) {
@@ -158,145 +580,40 @@ __global__ void k_scan_tiles(const int *__restrict__ count, int *__restrict__ of
     }
     int run = part[t] - s;
     for (int i = b; i < e; i++) {
-        offset[i] = run;
-        cursor[i] = run;
-        run += count[i];
+        const int c = bsum[i];
+        bsum[i] = run;
+        run += c;
     }
 }
 
-__global__ void k_mc_scatter(LayoutDev L, const MemberDev *__restrict__ mem, int nb, int tx, int ty,
-                             const int *__restrict__ pix, int *__restrict__ cursor, int *__restrict__ bucket) {
-    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long long)nb * L.ncloud) return;
-    int p = pix[idx];
-    if (p < 0) return;
-    int k = (int)(idx / L.ncloud);
-    int c = (int)(idx - (long long)k * L.ncloud);
-    const MemberDev &M = mem[k];
-    int py = p / M.bx, px = p - py * M.bx;
-    int slot = atomicAdd(&cursor[M.tile_off + (py / ty) * M.ntx + px / tx], 1);
-    bucket[slot] = c;
-}
-
-__global__ void __launch_bounds__(256) k_mc_deposit(GridDev g, LayoutDev L, const SubMC *__restrict__ sub, int nsub,
-                                                    const MemberDev *__restrict__ mem, int tx, int ty,
-                                                    const int *__restrict__ pix, const int *__restrict__ offset,
-                                                    const int *__restrict__ count, const int *__restrict__ bucket,
-                                                    const ZigDev *__restrict__ zig, const float *__restrict__ cd2if,
-                                                    const double *__restrict__ cd2i, float *__restrict__ model,
-                                                    long long mstride, double *__restrict__ model64, int *err) {
-    extern __shared__ unsigned long long tile[];
-    __shared__ unsigned s_kn[128];
-    __shared__ float s_wnf[128];
-    __shared__ double s_wn[128];
-    const int k = blockIdx.x;
-    const MemberDev &M = mem[k];
-    const int t = blockIdx.y;
-    if (t >= M.ntx * M.nty) return;
-    const int nz = g.nz;
-    const int TP = tx * ty;
-    for (int i = threadIdx.x; i < TP * nz; i += blockDim.x) tile[i] = 0ULL;
-    for (int i = threadIdx.x; i < 128; i += blockDim.x) {
-        s_kn[i] = zig->kn[i];
-        s_wnf[i] = zig->wnf[i];
-        s_wn[i] = zig->wn[i];
+__global__ void k_scan_c(const int *__restrict__ count, int n, const int *__restrict__ bsum, int *__restrict__ offset,
+                         int *__restrict__ cursor) {
+    __shared__ int r[32];
+    const int i = blockIdx.x * 1024 + threadIdx.x;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int v = i < n ? count[i] : 0;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) r[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int w = r[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        r[lane] = w;
     }
     __syncthreads();
-    const int tyi = t / M.ntx, txi = t - tyi * M.ntx;
-    const int x0 = txi * tx, y0 = tyi * ty;
-    const int beg = offset[M.tile_off + t], n = count[M.tile_off + t];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const unsigned ltmask = (1u << lane) - 1u;
-    const int nlines = g.nlines;
-    for (int e = warp; e < n; e += nw) {
-        const int c = bucket[beg + e];
-        const int p = pix[(size_t)k * L.ncloud + c];
-        const int py = p / M.bx, px = p - py * M.bx;
-        const int lp = (py - y0) * tx + (px - x0);
-        const int ir = L.sub[c];
-        const SubMC &S = sub[(size_t)k * nsub + ir];
-        const float4 cf = L.cf[c];
-        const double *cd = L.cd + 4 * (size_t)c;
-        const int half = cf.y >= 0.0f ? 0 : 1;
-        // channel centre of the cloud (fast path): c0 + (vr caz + vrad saz) sin(i) ia, vr lagged above zcyl
-        const float zf = cf.w * S.z0f;
-        const float azf = fabsf(zf);
-        float vr = S.vrotf;
-        if (azf > S.zcylf) {
-            float v = S.vrotf - S.dvdzf * (azf - S.zcylf);
-            vr = S.vrotf >= 0.0f ? fmaxf(v, 0.0f) : fminf(v, 0.0f);
-        }
-        const float base = vr * cf.y + S.vradf * cf.z;
-        const float mbase = fabsf(vr * cf.y) + fabsf(S.vradf * cf.z) + fabsf(S.dvdzf) * (azf + fabsf(S.zcylf));
-        const long long sb = L.sub_base[ir] + (long long)(c - L.cloud_base[ir]) * S.nv;
-        int slow_ord = L.slow_base[c];
-        bool have_vs = false;
-        double vs = 0.0;
-        unsigned long long *row = tile + (size_t)lp * nz;
-        for (int it = 0; it < S.nv; it += 32) {
-            const int iv = it + lane;
-            const bool act = iv < S.nv;
-            const int h = act ? L.hz[sb + iv] : 0;
-            const int iz = h & 127;
-            const unsigned ah = h < 0 ? (unsigned)(-(long long)h) : (unsigned)h;
-            const bool slow = act && !(ah < s_kn[iz]);
-            const unsigned bal = __ballot_sync(0xffffffffu, slow);
-            double nex = 0.0;
-            float nf;
-            if (slow) {
-                const long long o = (long long)slow_ord + __popc(bal & ltmask);
-                if (o < L.nslow) {
-                    nex = L.slow_val[o];
-                } else {
-                    atomicOr(err, ERR_LAYOUT);
-                    nex = 0.0;
-                }
-                nf = (float)nex;
-            } else {
-                nf = __int2float_rn(h) * s_wnf[iz];
-            }
-            slow_ord += __popc(bal);
-            if (!act) continue;
-            for (int nl = 0; nl < nlines; nl++) {
-                int isub;
-                bool ok = false;
-                if (g.fast_ok) {
-                    const float tc = S.c0[nl] + base * S.sia[nl];
-                    const float ns = nf * S.sg[nl];
-                    const float eps = (fabsf(S.c0[nl]) + mbase * fabsf(S.sia[nl]) + fabsf(ns) + 1.0f) * EPS_REL;
-                    ok = round_fast(tc + ns, eps, isub);
-                }
-                if (!ok) {
-                    if (!have_vs) {
-                        vs = vlos_exact(S, cd);
-                        have_vs = true;
-                    }
-                    const double nx = slow ? nex : __dmul_rn((double)h, s_wn[iz]);
-                    long long is;
-                    if (g.axtyp == 4 && nlines == 1) {
-                        double gz = __dadd_rn(__dmul_rn(vs, g.ia), g.ib);
-                        double sg = __dmul_rn(S.vdisptmp, g.ia);
-                        is = lround_ref(__dadd_rn(gz, __dmul_rn(nx, sg)));
-                    } else {
-                        double v = __dadd_rn(vs, __dmul_rn(nx, S.vdisptmp));
-                        is = lround_ref(velgrid_exact(v, g, nl));
-                    }
-                    isub = (is < 0 || is >= nz) ? -1 : (int)is;
-                }
-                if (isub >= 0 && isub < nz) atomicAdd(&row[isub], (unsigned long long)S.fix[half][nl]);
-            }
-        }
-    }
-    __syncthreads();
-    float *mout = model + (size_t)k * mstride;
-    for (int i = threadIdx.x; i < TP * nz; i += blockDim.x) {
-        const int lp = i / nz, z = i - lp * nz;
-        const int py = y0 + lp / tx, px = x0 + lp % tx;
-        if (py >= M.by || px >= M.bx) continue;
-        const long long v = (long long)tile[i];
-        const size_t o = ((size_t)py * M.bx + px) * nz + z;
-        mout[o] = ldexpf(__ll2float_rn(v) * cd2if[z], -M.fix_exp);
-        if (model64) model64[(size_t)k * mstride + o] = ldexp((double)v * cd2i[z], -M.fix_exp);
+    const int ex = x - v + (wid > 0 ? r[wid - 1] : 0) + bsum[blockIdx.x];
+    if (i < n) {
+        offset[i] = ex;
+        cursor[i] = ex;
     }
 }
 
@@ -309,32 +626,38 @@ void launch_mc_bin(cudaStream_t s, const GridDev &g, const LayoutDev &L, const S
     k_mc_bin<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g, L, sub, nsub, mem, nb, tx, ty, pix, tile_count, err);
 }
 
-void launch_scan_tiles(cudaStream_t s, const int *count, int *offset, int *cursor, int n) {
-    k_scan_tiles<<<1, 1024, 0, s>>>(count, offset, cursor, n);
+void launch_scan_tiles(cudaStream_t s, const int *count, int *offset, int *cursor, int n, int *scratch) {
+    const int nb = (n + 1023) / 1024;
+    if (nb == 0) return;
+    k_scan_a<<<nb, 1024, 0, s>>>(count, n, scratch);
+    k_scan_b<<<1, 1024, 0, s>>>(scratch, nb);
+    k_scan_c<<<nb, 1024, 0, s>>>(count, n, scratch, offset, cursor);
 }
 
-void launch_mc_scatter(cudaStream_t s, const LayoutDev &L, const MemberDev *mem, int nb, int tx, int ty,
-                       const int *pix, int *cursor, int *bucket) {
+void launch_mc_scatter(cudaStream_t s, const LayoutDev &L, const SubMC *sub, int nsub, const MemberDev *mem, int nb,
+                       int tx, int ty, const int *pix, int *cursor, void *bucket) {
     long long n = (long long)nb * L.ncloud;
     if (n == 0) return;
-    k_mc_scatter<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(L, mem, nb, tx, ty, pix, cursor, bucket);
+    k_mc_scatter<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(L, sub, nsub, mem, nb, tx, ty, pix, cursor,
+                                                             (Entry *)bucket);
 }
 
 void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
-                       const MemberDev *mem, const MemberDev *mem_host, int nb, int tx, int ty, const int *pix,
-                       const int *offset, const int *count, const int *bucket, const ZigDev *zig,
+                       const MemberDev *mem, const MemberDev *mem_host, int nb, int tx, int ty,
+                       const int *offset, const int *count, const void *bucket, const ZigDev *zig,
                        const float *cd2if, const double *cd2i, float *model, long long mstride, double *model64,
                        int *err) {
     int maxt = 0;
     for (int k = 0; k < nb; k++) maxt = max(maxt, mem_host[k].ntx * mem_host[k].nty);
     if (maxt == 0 || nb == 0) return;
-    size_t smem = (size_t)tx * ty * g.nz * sizeof(unsigned long long);
+    size_t smem = (size_t)tx * ty * g.nz * sizeof(unsigned long long) + 16 + (size_t)8 * DEPTH * WB * sizeof(float) +
+                  (size_t)g.nz * sizeof(float);
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {
         cudaFuncSetAttribute(k_mc_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         configured = smem;
     }
     dim3 grid(nb, maxt);
-    k_mc_deposit<<<grid, 256, smem, s>>>(g, L, sub, nsub, mem, tx, ty, pix, offset, count, bucket, zig, cd2if, cd2i,
-                                        model, mstride, model64, err);
+    k_mc_deposit<<<grid, 256, smem, s>>>(g, L, sub, nsub, mem, tx, ty, offset, count, (const Entry *)bucket, zig, cd2if,
+                                        cd2i, model, mstride, model64, err);
 }
