@@ -133,6 +133,20 @@ int bbgpu_sync(bbgpu_ctx *ctx);
 /* Options: 1 keep the smoothed models of a batch (for bbgpu_eval_model), 2 time the kernels of each run. */
 int bbgpu_set_option(bbgpu_ctx *ctx, int option, int value);
 
+/* ---- without allocation ------------------------------------------------------------------------------- */
+/* bbgpu_sumsq_residuals / bbgpu_residuals_fracerr for callers that may not allocate device memory (their own
+ * memory pool, a stream being captured into a CUDA graph, a fixed footprint after warm-up). No counterpart in
+ * the reference: it exists for such callers. Needs no context. model (nz, ny, nx) float64, data float32, mask
+ * and region uint8 and out2 (double[2]: sum of squares or variance-weighted sum, sum of log-variances) are
+ * DEVICE pointers of the current device; eps2 = 0 gives the plain sum of squares. Kernels run on stream
+ * (cudaStream_t, NULL: the default stream) and out2 is written there. The partial sums use a 64 KB scratch
+ * array held by every GPU that loads the library; at most 16,777,216 voxels (4096 blocks of 4096) per call,
+ * BBGPU_ERR_ARG beyond. The first call on a device looks the array's address up (cudaGetSymbolAddress): make
+ * it before any stream capture. Calls whose kernels overlap on the GPU share the array and race. */
+int bbgpu_sumsq_residuals_noalloc(const double *model, const float *data, const uint8_t *mask, int maskmode,
+                                  const uint8_t *region, int nz, int ny, int nx, double sigma2, double eps2,
+                                  double *out2, void *stream);
+
 /* ---- counters --------------------------------------------------------------------------------------- */
 /* Kernel launches issued by the context so far, and the device time (ms) of the last bbgpu_eval_run split
  * into its kernels: times[0..n) in the order of bbgpu_kernel_name(i). */
