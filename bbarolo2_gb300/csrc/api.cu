@@ -90,6 +90,7 @@ struct bbgpu_ctx {
     long long mstride = 0;
     // options
     bool keep_smoothed = false, timing = false, want64 = false;
+    int lean = 0;                 // the batch qualifies for the lean deposit kernel
     long long launches = 0;
     long long h2d = 0, d2h = 0;
     cudaEvent_t ev[NTIMER + 1] = {};
@@ -568,6 +569,11 @@ static int batch_prepare(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const
     ctx->nb = nb;
     ctx->nsub = nsub;
     ctx->galmodtype = galmodtype;
+    {
+        int maxnv = 0;
+        for (int i = 0; i < nsub; i++) maxnv = nv0[i] > maxnv ? nv0[i] : maxnv;
+        ctx->lean = g.fast_ok && g.nlines == 1 && maxnv <= 128;
+    }
     ctx->ntile_total = toff;
     ctx->mstride = (long long)g.nx * g.ny * g.nz;
     ctx->npart = conv_resid_npart(ctx->mem_host.data(), nb, g.nz);
@@ -617,7 +623,7 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
     if (tm) CK(cudaEventRecord(ctx->ev[3], s));
     launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->tx, ctx->ty,
                       ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig, ctx->d_cd2if, ctx->d_cd2i,
-                      ctx->d_model, ctx->mstride, ctx->want64 ? ctx->d_model64 : nullptr, ctx->d_err);
+                      ctx->d_model, ctx->mstride, ctx->want64 ? ctx->d_model64 : nullptr, ctx->d_err, ctx->lean);
     CKL();
     if (tm) CK(cudaEventRecord(ctx->ev[4], s));
     const bool conv = ctx->kernel_set;

@@ -63,7 +63,7 @@ void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, con
                        const MemberDev *mem, const MemberDev *mem_host, int nb, int tx, int ty,
                        const int *offset, const int *count, const void *bucket, const ZigDev *zig,
                        const float *cd2if, const double *cd2i, float *model, long long mstride, double *model64,
-                       int *err);
+                       int *err, int lean);
 
 // ---- convolution + residual (conv.cu)
 // The taps of a beam kernel (ky, kx) as the conv kernels read them: flipped, float32, rows padded to the

@@ -545,6 +545,166 @@ __global__ void __launch_bounds__(256) k_mc_deposit(GridDev g, LayoutDev L, cons
     }
 }
 
+// The common case in a lean kernel: a linear channel map, one line, at most 128 samples per cloud (4 per
+// lane). Same entries, lists, staging and run-length deposit as k_mc_deposit; the rare clouds outside the
+// fast criteria go through the per-sample path.
+__global__ void __launch_bounds__(256, 2) k_mc_deposit_lean(GridDev g, LayoutDev L, const SubMC *__restrict__ sub,
+                                                           int nsub, const MemberDev *__restrict__ mem, int tx, int ty,
+                                                           const int *__restrict__ offset,
+                                                           const int *__restrict__ count,
+                                                           const Entry *__restrict__ bucket,
+                                                           const ZigDev *__restrict__ zig,
+                                                           const float *__restrict__ cd2if, float *__restrict__ model,
+                                                           long long mstride, int *err) {
+    extern __shared__ unsigned long long tile[];
+    __shared__ int bins[8][128 + XQ];
+    __shared__ Entry ents[8][DEPTH];
+    constexpr int E = 4;
+    const int k = blockIdx.x;
+    const int t = blockIdx.y;
+    const int ntx = mem[k].ntx;
+    if (t >= ntx * mem[k].nty) return;
+    const int nz = g.nz;
+    const int TP = tx * ty;
+    const int tyi = t / ntx, txi = t - tyi * ntx;
+    const int x0 = txi * tx, y0 = tyi * ty;
+    const int bx = mem[k].bx, by = mem[k].by;
+    const int lbase = (mem[k].tile_off + t) * NOWN;
+    float *mout = model + (size_t)k * mstride;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    {
+        int any = 0;
+        if (threadIdx.x < NOWN) any = count[lbase + threadIdx.x] != 0;
+        if (!__syncthreads_or(any)) {
+            for (int lp = warp; lp < TP; lp += 8) {
+                const int py = y0 + lp / tx, px = x0 + lp % tx;
+                if (py >= by || px >= bx) continue;
+                float *o = mout + ((size_t)py * bx + px) * nz;
+                for (int z = lane; z < nz; z += 32) o[z] = 0.0f;
+            }
+            return;
+        }
+    }
+    float *stg = (float *)(((uintptr_t)(tile + (size_t)TP * nz) + 15) & ~(uintptr_t)15);
+    float *chs = stg + 8 * DEPTH * WB;
+    {
+        ulonglong2 *t2 = (ulonglong2 *)tile;
+        for (int i = threadIdx.x; i < TP * nz / 2; i += blockDim.x) t2[i] = make_ulonglong2(0ULL, 0ULL);
+        if (((TP * nz) & 1) && threadIdx.x == 0) tile[TP * nz - 1] = 0ULL;
+        for (int i = threadIdx.x; i < 8 * (128 + XQ); i += blockDim.x) (&bins[0][0])[i] = 0;
+        const int fe = mem[k].fix_exp;
+        for (int z = threadIdx.x; z < nz; z += blockDim.x) chs[z] = ldexpf(cd2if[z], -fe);
+    }
+    __syncthreads();
+    const int beg = offset[lbase + warp], n = count[lbase + warp];
+    float *slots = stg + warp * DEPTH * WB;
+    int pa = lane < n ? __ldg(&bucket[beg + lane].pb) : 0, ma = lane < n ? __ldg(&bucket[beg + lane].meta) : 0;
+    int pn = 32 + lane < n ? __ldg(&bucket[beg + 32 + lane].pb) : 0;
+    int mn = 32 + lane < n ? __ldg(&bucket[beg + 32 + lane].meta) : 0;
+    auto issue = [&](int j, int i) {
+        if (j < n) {
+            const bool same = (j >> 5) == (i >> 5);
+            const int pbj = __shfl_sync(0xffffffffu, same ? pa : pn, j & 31);
+            const int mj = __shfl_sync(0xffffffffu, same ? ma : mn, j & 31);
+            if (lane < 2)
+                cp_async16((char *)&ents[warp][j % DEPTH] + 16 * lane, (const char *)(bucket + beg + j) + 16 * lane);
+            if (lane < ((mj & 0xffff) + 3) >> 2)
+                cp_async16(slots + (j % DEPTH) * WB + 4 * lane, L.nf + (unsigned)pbj + 4 * lane);
+        }
+        cp_async_commit();
+    };
+    issue(0, 0);
+    issue(1, 0);
+    for (int i = 0; i < n; i++) {
+        issue(i + 2, i);
+        cp_async_wait<DEPTH - 1>();
+        __syncwarp();
+        const Entry en = ents[warp][i % DEPTH];
+        const float *w = slots + (i % DEPTH) * WB;
+        const int nv = en.meta & 0xffff;
+        unsigned long long *row = tile + (size_t)((en.meta >> 16) & 255) * nz;
+        const float tc = en.tc, sg = en.sg;
+        const long long fix = en.fix;
+        if (nv <= 32 * E && fabsf(tc) < 1.0e5f) {
+            const float4 nn = *(const float4 *)(w + 4 * lane);     // (zeros past nv: masked below)
+            const float nmax = fmaxf(fabsf(w[0]), fabsf(w[nv - 1]));
+            const float eps = fmaf(nmax, fabsf(sg) * EPS_REL, en.epsc);
+            const float hw = 0.5f - eps;
+            const int i0 = lane * E;
+            const float nv4[4] = {nn.x, nn.y, nn.z, nn.w};
+            int ch[E];
+            unsigned need = 0;
+#pragma unroll
+            for (int j = 0; j < E; j++) {
+                const float f = fmaf(nv4[j], sg, tc) + 0.5f;
+                const float fl = floorf(f);
+                const bool okj = fabsf(f - fl - 0.5f) <= hw;
+                ch[j] = i0 + j < nv ? (int)fl : 0x7fffffff;
+                if (i0 + j < nv && !okj) need |= 1u << j;
+            }
+            if (need) {                                         // rare: exact channels
+                const int ir = __ldg(&L.sub[en.c]);
+                const SubMC &S = sub[(size_t)k * nsub + ir];
+                const long long sb = stream_base(L, en.c, ir, nv);
+                const int sbase = __ldg(&L.slow_base[en.c]);
+#pragma unroll
+                for (int j = 0; j < E; j++)
+                    if (need & (1u << j)) {
+                        const double nx = normal_exact(L, zig, sb, L.ord[(unsigned)en.pb + i0 + j], sbase, err);
+                        const long long is = channel_exact_raw(S, g, L.cd + 4 * (size_t)en.c, nx, 0);
+                        ch[j] = is < -0x3fffffffLL ? -0x3fffffff : (is > 0x3fffffffLL ? 0x3fffffff : (int)is);
+                    }
+            }
+            const int prev0 = __shfl_up_sync(0xffffffffu, ch[E - 1], 1);
+            unsigned starts = 0;
+#pragma unroll
+            for (int j = 0; j < E; j++) {
+                const int pv = j == 0 ? (lane == 0 ? (int)0x80000000 : prev0) : ch[j - 1];
+                if (ch[j] != pv && i0 + j < nv) starts |= 1u << j;
+            }
+            const unsigned B = __ballot_sync(0xffffffffu, starts != 0);
+            const unsigned after = lane < 31 ? (B & (0xffffffffu << (lane + 1))) : 0u;
+            const int l2 = after ? __ffs(after) - 1 : lane;
+            const unsigned s2 = __shfl_sync(0xffffffffu, starts, l2);
+            const int nextl = after ? l2 * E + __ffs(s2) - 1 : nv;
+            while (starts) {
+                const int j = __ffs(starts) - 1;
+                starts &= starts - 1;
+                const int nxt = starts ? i0 + __ffs(starts) - 1 : nextl;
+                const int chj = j == 0 ? ch[0] : (j == 1 ? ch[1] : (j == 2 ? ch[2] : ch[3]));
+                if (chj >= 0 && chj < nz) row[chj] += (unsigned long long)(fix * (long long)(nxt - i0 - j));
+            }
+        } else {
+            const int ir = __ldg(&L.sub[en.c]);
+            const SubMC &S = sub[(size_t)k * nsub + ir];
+            deposit_per_sample(g, L, zig, S, en.c, (unsigned)en.pb, stream_base(L, en.c, ir, nv), nv, tc, sg, en.epsc,
+                               fabsf(sg) * EPS_REL, fix, 0, true, row, bins[warp], bins[warp] + 128, lane, err);
+        }
+        __syncwarp();
+        if (((i + 1) & 31) == 0) {
+            pa = pn;
+            ma = mn;
+            const int j = i + 1 + 32 + lane;
+            pn = j < n ? __ldg(&bucket[beg + j].pb) : 0;
+            mn = j < n ? __ldg(&bucket[beg + j].meta) : 0;
+        }
+    }
+    cp_async_wait<0>();
+    __syncthreads();
+    for (int lp = warp; lp < TP; lp += 8) {
+        const int py = y0 + lp / tx, px = x0 + lp % tx;
+        if (py >= by || px >= bx) continue;
+        const unsigned long long *src = tile + (size_t)lp * nz;
+        float *o = mout + ((size_t)py * bx + px) * nz;
+        for (int z = lane; z < nz; z += 32) {
+            const long long v = (long long)src[z];
+            const float hi = (float)(int)(v >> 32) * 4294967296.0f;
+            const float lo = (float)(unsigned)(v & 0xffffffffLL);
+            o[z] = (hi + lo) * chs[z];
+        }
+    }
+}
+
 // exclusive scan of n counts in three passes: block sums, scan of the sums, block scans
 __global__ void k_scan_a(const int *__restrict__ count, int n, int *__restrict__ bsum) {
     __shared__ int r[32];
@@ -646,7 +806,7 @@ void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, con
                        const MemberDev *mem, const MemberDev *mem_host, int nb, int tx, int ty,
                        const int *offset, const int *count, const void *bucket, const ZigDev *zig,
                        const float *cd2if, const double *cd2i, float *model, long long mstride, double *model64,
-                       int *err) {
+                       int *err, int lean) {
     int maxt = 0;
     for (int k = 0; k < nb; k++) maxt = max(maxt, mem_host[k].ntx * mem_host[k].nty);
     if (maxt == 0 || nb == 0) return;
@@ -658,6 +818,16 @@ void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, con
         configured = smem;
     }
     dim3 grid(nb, maxt);
+    if (lean && !model64) {
+        static size_t cfg_lean = 0;
+        if (smem > 48 * 1024 && smem > cfg_lean) {
+            cudaFuncSetAttribute(k_mc_deposit_lean, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cfg_lean = smem;
+        }
+        k_mc_deposit_lean<<<grid, 256, smem, s>>>(g, L, sub, nsub, mem, tx, ty, offset, count, (const Entry *)bucket,
+                                                 zig, cd2if, model, mstride, err);
+        return;
+    }
     k_mc_deposit<<<grid, 256, smem, s>>>(g, L, sub, nsub, mem, tx, ty, offset, count, (const Entry *)bucket, zig, cd2if,
                                         cd2i, model, mstride, model64, err);
 }

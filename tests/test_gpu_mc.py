@@ -107,3 +107,33 @@ def test_mc_full_workloads_vs_oracle(gpu_lib, oracle_lib, wl):
                          st.crval3, st.cdelt3, st.crpix3, st.relint, st.cd2i)
     assert np.array_equal(out != 0, ref != 0)
     np.testing.assert_allclose(out, ref, rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("wl", ["classic64", "global160"])
+def test_batch_path_models_bit_exact(gpu_lib, oracle_lib, wl):
+    """The unsmoothed float32 models of the batch path (the kernels the likelihood uses) against the oracle:
+    the same voxels, values within float32 rounding (a misplaced sub-cloud moves a whole deposit)."""
+    from bbarolo2_gb300 import _lib, configs, engine
+    from bbarolo2_gb300.galmod import ring_rows_batch
+    cube, rings = configs.WORKLOADS[wl](galmodtype="MC")
+    dm = engine.DiskModel(cube)
+    st = dm.setup
+    data = np.zeros(cube.array.shape, np.float32)
+    L = engine.BatchLikelihood(dm, data + 1.0, None, maskmode=0, sigma=1.0)
+    rows = ring_rows_batch([rings] * 3)
+    rows[1, 4] *= 1.07
+    rows[2, 12] += 3.0
+    sr, nv, descs, boxes = L.prepare(rows, rings, seed=1)
+    L.run(sr, nv, descs)
+    for k in range(3):
+        (blo, bhi) = boxes[k]
+        by, bx = bhi[1] - blo[1], bhi[0] - blo[0]
+        got = np.zeros((by, bx, st.nsubs), np.float32)
+        dm.ctx.check(dm.ctx.L.bbgpu_eval_model(dm.ctx.h, k, 0, _lib.ptr(got), by, bx, st.nsubs))
+        ref = np.zeros((by, bx, st.nsubs))
+        oracle_lib.galmod_mc(ref, sr[k], 0, sr.shape[2], 1, st.radsep, nv[k], st.cdens, st.cmode, st.pixarea,
+                             st.cdelt[0], st.cdelt[1], st.crota2, blo[0], blo[1], bhi[0], bhi[1], st.ltype,
+                             st.sig_instr, st.axtyp, st.velsys, st.lfreq0, st.crval3, st.cdelt3, st.crpix3, st.relint,
+                             st.cd2i)
+        assert np.array_equal(got != 0, ref != 0), k
+        np.testing.assert_allclose(got, ref, rtol=1e-6, atol=0)
