@@ -861,10 +861,45 @@ extern "C" int bbgpu_ring_maps_analytic(bbgpu_ctx *ctx, double *out, int nr, con
     return fail(ctx, BBGPU_ERR_ARG, "ring_maps_analytic: not available in this build");
 }
 
+// A scoped set of device buffers freed at the end of a stand-alone entry point.
+struct DevBufs {
+    std::vector<void *> p;
+    ~DevBufs() {
+        for (void *q : p) cudaFree(q);
+    }
+    template <class T>
+    bool get(T **out, size_t n) {
+        void *q = nullptr;
+        if (cudaMalloc(&q, n ? n : 1) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        p.push_back(q);
+        *out = (T *)q;
+        return true;
+    }
+};
+
 extern "C" int bbgpu_conv_sparse(bbgpu_ctx *ctx, const double *model, double *out, int ny, int nx, int nz,
                                  const double *kernel, int ky, int kx, double scale) {
-    (void)model; (void)out; (void)ny; (void)nx; (void)nz; (void)kernel; (void)ky; (void)kx; (void)scale;
-    return fail(ctx, BBGPU_ERR_ARG, "conv_sparse: not available in this build");
+    if (!ctx) return BBGPU_ERR_ARG;
+    if (!model || !out || !kernel || ny < 0 || nx < 0 || nz < 0 || ky < 1 || kx < 1)
+        return fail(ctx, BBGPU_ERR_ARG, "conv_sparse: invalid arguments");
+    CK(cudaSetDevice(ctx->device));
+    const size_t n = (size_t)ny * nx * nz;
+    if (n == 0) return BBGPU_OK;
+    DevBufs B;
+    double *dm = nullptr, *dout = nullptr, *dk = nullptr;
+    if (!B.get(&dm, n * 8) || !B.get(&dout, n * 8) || !B.get(&dk, (size_t)ky * kx * 8))
+        return fail(ctx, BBGPU_ERR_NOMEM, "conv_sparse: allocation failed");
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(dm, model, n * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dk, kernel, (size_t)ky * kx * 8, cudaMemcpyHostToDevice, s));
+    launch_conv_sparse(s, dm, dout, ny, nx, nz, dk, ky, kx, scale);
+    CKL();
+    CK(cudaMemcpyAsync(out, dout, n * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return BBGPU_OK;
 }
 
 extern "C" int bbgpu_norm(bbgpu_ctx *ctx, double *model, int bsy, int bsx, int nz, const float *data, const uint8_t *mask,
@@ -872,9 +907,87 @@ extern "C" int bbgpu_norm(bbgpu_ctx *ctx, double *model, int bsy, int bsx, int n
                           double r1, double r2, double wpow, int side, int ftype, const double *chan_noise,
                           double data_noise, double bweight, int normtype, const double *pre, const int64_t *ilo,
                           const int64_t *ihi, int ky, const double *thr, int foot, double hmax, double *out) {
-    (void)model; (void)bsy; (void)bsx; (void)nz; (void)data; (void)mask; (void)dny; (void)dnx; (void)blo0; (void)blo1;
-    (void)x0; (void)y0; (void)phi; (void)inc; (void)r1; (void)r2; (void)wpow; (void)side; (void)ftype; (void)chan_noise;
-    (void)data_noise; (void)bweight; (void)normtype; (void)pre; (void)ilo; (void)ihi; (void)ky; (void)thr; (void)foot;
-    (void)hmax; (void)out;
-    return fail(ctx, BBGPU_ERR_ARG, "norm: not available in this build");
+    if (!ctx) return BBGPU_ERR_ARG;
+    if (!model || !data || !mask || !chan_noise || !out || bsy < 0 || bsx < 0 || nz < 1 || blo0 < 0 || blo1 < 0 ||
+        blo1 + bsy > dny || blo0 + bsx > dnx || (pre && (!ilo || !ihi || !thr || ky < 1)))
+        return fail(ctx, BBGPU_ERR_ARG, "norm: invalid arguments");
+    CK(cudaSetDevice(ctx->device));
+    const int np = bsy * bsx;
+    const size_t n = (size_t)np * nz;
+    // the ring's pixels and weights (host: the reference's float64 and C library calls)
+    std::vector<uint8_t> inside(np ? np : 1);
+    std::vector<double> wmap(np ? np : 1);
+    bbh_norm_footprint(bsy, bsx, x0, y0, phi, inc, r1, r2, wpow, side, foot, hmax, inside.data(), wmap.data());
+    // the box of the data and mask ("yxz"), contiguous
+    std::vector<float> dbox(n ? n : 1);
+    std::vector<uint8_t> mbox(n ? n : 1);
+    for (int y = 0; y < bsy; y++)
+        for (int x = 0; x < bsx; x++) {
+            const size_t src = (((size_t)(y + blo1)) * dnx + (size_t)(x + blo0)) * nz;
+            memcpy(&dbox[((size_t)y * bsx + x) * nz], data + src, sizeof(float) * nz);
+            memcpy(&mbox[((size_t)y * bsx + x) * nz], mask + src, nz);
+        }
+    DevBufs B;
+    double *dm = nullptr, *dw = nullptr, *dcn = nullptr, *dpre = nullptr, *dthr = nullptr, *dpart = nullptr,
+           *dP = nullptr;
+    float *dd = nullptr;
+    uint8_t *dk = nullptr, *din = nullptr;
+    long long *dilo = nullptr, *dihi = nullptr;
+    if (!B.get(&dm, n * 8) || !B.get(&dd, n * 4) || !B.get(&dk, n) || !B.get(&din, np) || !B.get(&dw, np * 8) ||
+        !B.get(&dcn, (size_t)nz * 8) || !B.get(&dpart, (size_t)np * 4 * 8) ||
+        (pre && (!B.get(&dpre, n * 8) || !B.get(&dP, (size_t)bsy * (bsx + 1) * nz * 8) ||
+                 !B.get(&dthr, (size_t)nz * 8) || !B.get(&dilo, (size_t)ky * 8) ||
+                 !B.get(&dihi, (size_t)ky * 8))))
+        return fail(ctx, BBGPU_ERR_NOMEM, "norm: allocation failed");
+    cudaStream_t s = ctx->stream;
+    if (n) {
+        CK(cudaMemcpyAsync(dm, model, n * 8, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dd, dbox.data(), n * 4, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dk, mbox.data(), n, cudaMemcpyHostToDevice, s));
+    }
+    if (np) {
+        CK(cudaMemcpyAsync(din, inside.data(), np, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dw, wmap.data(), (size_t)np * 8, cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaMemcpyAsync(dcn, chan_noise, (size_t)nz * 8, cudaMemcpyHostToDevice, s));
+    if (pre) {
+        CK(cudaMemcpyAsync(dpre, pre, n * 8, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dthr, thr, (size_t)nz * 8, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dilo, ilo, (size_t)ky * 8, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dihi, ihi, (size_t)ky * 8, cudaMemcpyHostToDevice, s));
+        launch_norm_prefix(s, dpre, dP, bsy, bsx, nz);
+        CKL();
+    }
+    std::vector<double> part((size_t)np * 4 + 1);
+    double factor = 1.0;
+    if (normtype == 1 && np) {
+        launch_norm_sums(s, dm, dd, dk, din, bsy, bsx, nz, dpart);
+        CKL();
+        CK(cudaMemcpyAsync(part.data(), dpart, (size_t)np * 2 * 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        double ms = 0.0, os = 0.0;
+        for (int p = 0; p < np; p++) {
+            ms += part[2 * p];
+            os += part[2 * p + 1];
+        }
+        factor = ms != 0 ? os / ms : 0.0;
+    }
+    if (np) {
+        launch_norm_pix(s, dm, dd, dk, din, dw, bsy, bsx, nz, ftype, dcn, data_noise, normtype, factor, dP, dilo, dihi,
+                        ky, dthr, dpart);
+        CKL();
+        CK(cudaMemcpyAsync(part.data(), dpart, (size_t)np * 4 * 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(model, dm, n * 8, cudaMemcpyDeviceToHost, s));
+    }
+    CK(cudaStreamSynchronize(s));
+    double minfunc = 0.0;
+    long long nb = 0, nt = 0;
+    for (int p = 0; p < np; p++) {
+        minfunc += part[4 * p];
+        nb += (long long)part[4 * p + 1];
+        nt += (long long)part[4 * p + 2];
+    }
+    if (nt - nb == 0) *out = INFINITY;
+    else *out = pow(1 + (double)nb / (double)nt, bweight) * minfunc / (double)(nt - nb);
+    return BBGPU_OK;
 }

@@ -308,3 +308,38 @@ int bbh_submc(const double *sr, int nsub, const int *nc, const int *nv, const Gr
     }
     return bound > 0 ? (int)floor(62.0 - log2(bound)) : 0;
 }
+
+// The ring footprint of _norm (bbarolo/galfit.py:62-93): the reference's float64 expressions and C library calls.
+void bbh_norm_footprint(int bsy, int bsx, double x0, double y0, double phi, double inc, double r1, double r2,
+                        double wpow, int side, int foot, double hmax, uint8_t *inside, double *wmap) {
+    const double F = M_PI / 180.;
+    const double sphi = sin(F * phi), cphi = cos(F * phi), cinc = cos(F * inc);
+    const int usesin = wpow < 0;
+    const double apow = fabs(wpow);
+    for (int y = 0; y < bsy; y++)
+        for (int x = 0; x < bsx; x++) {
+            const int p = y * bsx + x;
+            inside[p] = 0;
+            wmap[p] = 0.0;
+            const double xr = -(x - x0) * sphi + (y - y0) * cphi;
+            const double ys = -(x - x0) * cphi - (y - y0) * sphi;
+            const double yr = ys / cinc;
+            const double r = sqrt(xr * xr + yr * yr);
+            double th = r < 0.1 ? 0.0 : atan2(yr, xr) / F;
+            if (foot == 1) {
+                if (!(fabs(xr) >= r1 && fabs(xr) <= r2 && fabs(ys) <= hmax)) continue;
+                th = xr >= 0 ? 0.0 : 180.0;
+            } else if (!(r >= r1 && r <= r2)) {
+                continue;
+            }
+            if (side == 1 && !(fabs(th) <= 90.0)) continue;
+            if (side == 2 && !(fabs(th) >= 90.0)) continue;
+            inside[p] = 1;
+            if (foot == 1) {
+                wmap[p] = 1.0;
+                continue;
+            }
+            const double wf = usesin ? fabs(sin(th * F)) : fabs(cos(th * F));
+            wmap[p] = pow(wf, apow);
+        }
+}

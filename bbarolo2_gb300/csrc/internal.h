@@ -76,5 +76,8 @@ uint64_t bbh_layout_key(uint64_t seed, int ltype, int nsub, const int *nc, const
 void bbh_cloud_counts(const double *sr, int nsub, const int64_t *nv_in, const GridDev *g, int *nc, int *nv);
 // SubMC of one table; returns the exponent e of the fixed-point unit 2^-e of its deposits
 int bbh_submc(const double *sr, int nsub, const int *nc, const int *nv, const GridDev *g, SubMC *out);
+// The pixels of a ring for the CLASSIC residual (bbarolo/galfit.py:62-93): inside flags and weights (bsy, bsx)
+void bbh_norm_footprint(int bsy, int bsx, double x0, double y0, double phi, double inc, double r1, double r2,
+                        double wpow, int side, int foot, double hmax, uint8_t *inside, double *wmap);
 }
 #endif

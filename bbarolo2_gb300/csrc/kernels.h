@@ -88,3 +88,14 @@ int launch_sumsq64(cudaStream_t s, const double *model, const float *data, const
                    int maxblocks);
 void launch_zyx64_to_yxz32(cudaStream_t s, const double *in, float *out, int nz, int ny, int nx);
 void launch_yxz32_to_zyx64(cudaStream_t s, const float *in, double *out, int nz, int ny, int nx);
+
+// ---- CLASSIC (classic.cu)
+void launch_conv_sparse(cudaStream_t s, const double *model, double *out, int ny, int nx, int nz, const double *kern,
+                        int ky, int kx, double scale);
+void launch_norm_sums(cudaStream_t s, const double *model, const float *data, const uint8_t *mask,
+                      const uint8_t *inside, int bsy, int bsx, int nz, double *part);
+void launch_norm_prefix(cudaStream_t s, const double *pre, double *P, int bsy, int bsx, int nz);
+void launch_norm_pix(cudaStream_t s, double *model, const float *data, const uint8_t *mask, const uint8_t *inside,
+                     const double *wmap, int bsy, int bsx, int nz, int ftype, const double *chan_noise,
+                     double data_noise, int normtype, double factor_azim, const double *P, const long long *ilo,
+                     const long long *ihi, int ky, const double *thr, double *part);
