@@ -1,0 +1,352 @@
+// The ANALYTIC GALMOD deposit and the ring maps on the device (the reference's _galmod_analytic and
+// _ring_maps_analytic, bbarolo/galmod.py:326-536).
+//
+// One warp per azimuthal sample (sub-ring, radial sample, azimuth). The warp computes the pixels of the
+// sample's vertical samples (lanes over heights), merges consecutive heights that fall in the same pixel
+// (lane 0, in order, as the reference), and deposits each merged run: for a model, the channel-integrated
+// line profile (lanes over channels, computed once per sample and line from the tabulated normal CDF), for
+// ring maps the run's weight. All arithmetic that decides an index or a value is the reference's float64,
+// each operation rounded once in its order (no contraction), so pixels and channels are bit-exact. The sums
+// are in 64-bit fixed point (units 2^-e, e per member from a bound on its total flux): integer atomics, exact
+// and independent of the order of the deposits, so the model is deterministic; it differs from the
+// reference's running float64 sum by rounding only.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "devmath.cuh"
+#include "kernels.h"
+
+#define PHI_N 6146
+#define AN_WPB 8            // warps per CTA
+#define FULL 0xffffffffu
+
+namespace {
+
+// bbarolo/galmod.py:183-191: the normal CDF at t from the table (512 entries per unit from -6)
+__device__ __forceinline__ double phi_interp(double t, const double *__restrict__ tab) {
+    const double x = __dmul_rn(__dadd_rn(t, 6.0), 512.0);
+    if (x <= 0.0) return 0.0;
+    if (!(x < (double)(PHI_N - 1))) return 1.0;
+    const int k = (int)x;
+    const double t0 = tab[k], t1 = tab[k + 1];
+    return __dadd_rn(t0, __dmul_rn(__dsub_rn(x, (double)k), __dsub_rn(t1, t0)));
+}
+
+__device__ __forceinline__ int clamp_pix(long long v) {
+    return v < -(1LL << 30) ? -(1 << 30) : (v > (1LL << 30) ? (1 << 30) : (int)v);
+}
+
+// bbarolo/galmod.py:400-406: the pixel of the vertical sample at height z (z = 0 for a thin layer)
+__device__ __forceinline__ void an_pixel(const AnSub &S, double cdelt0, double cdelt1, double xs, double xc,
+                                         double yb, double z, int &g0, int &g1) {
+    const double y = __dsub_rn(yb, __dmul_rn(z, S.sinc));
+    g0 = clamp_pix(lround_ref(__dadd_rn(S.xpos, __ddiv_rn(__dsub_rn(xs, __dmul_rn(y, S.cpa)), cdelt0))));
+    g1 = clamp_pix(lround_ref(__dadd_rn(S.ypos, __ddiv_rn(__dadd_rn(xc, __dmul_rn(y, S.spa)), cdelt1))));
+}
+
+// bbarolo/galmod.py:194-214: the CDF at the channel edges k0 .. k0 + nk of the line at velocity v (lanes over
+// edges) into pe; the profile of channel k0 + j is |pe[j + 1] - pe[j]| * cd2i[k0 + j].
+__device__ __forceinline__ void an_profile(const GridDev &g, int nl, double v, const AnSub &S,
+                                           const double *__restrict__ vedges, const double *__restrict__ ptab,
+                                           double *pe, int &k0, int &nk) {
+    const int lane = threadIdx.x & 31;
+    const long long kc = lround_ref(velgrid_exact(v, g, nl));
+    long long a0 = kc - S.K, a1 = kc + S.K + 1;
+    if (a0 < 0) a0 = 0;
+    if (a1 > g.nz) a1 = g.nz;
+    if (a1 <= a0) {
+        k0 = 0;
+        nk = 0;
+        return;
+    }
+    k0 = (int)a0;
+    nk = (int)(a1 - a0);
+    const double *ve = vedges + (size_t)nl * (g.nz + 1) + k0;
+    for (int j = lane; j <= nk; j += 32) pe[j] = phi_interp(__dmul_rn(__dsub_rn(ve[j], v), S.inv), ptab);
+    __syncwarp();
+}
+
+// The channels of a profile times aw, added in fixed point to the spectrum o (whole warp).
+__device__ __forceinline__ void an_add(unsigned long long *o, const double *pe, const double *__restrict__ cd2i,
+                                       int k0, int nk, double aw, double fscale) {
+    const int lane = threadIdx.x & 31;
+    for (int j = lane; j < nk; j += 32) {
+        double f = __dsub_rn(pe[j + 1], pe[j]);
+        f = f >= 0 ? f : -f;
+        const double t = __dmul_rn(aw, __dmul_rn(f, cd2i[k0 + j]));
+        const long long q = __double2ll_rn(__dmul_rn(t, fscale));
+        if (q) atomicAdd(o + k0 + j, (unsigned long long)q);
+    }
+}
+
+// The runs of consecutive vertical samples in one pixel (bbarolo/galmod.py:412-421 and :518-524), in order:
+// emit(g0, g1, ws) is called by the whole warp for each run (warp-uniform arguments).
+template <class F>
+__device__ __forceinline__ void an_runs(const AnSub &S, const double *__restrict__ zq, const double *__restrict__ wq,
+                                        double cdelt0, double cdelt1, double xs, double xc, double yb, int *sgx,
+                                        int *sgy, int *rg0, int *rg1, double *rws, F emit) {
+    const int lane = threadIdx.x & 31;
+    const int nzz = S.nzz;
+    int og0 = 0, og1 = 0;
+    double ows = 0.0;
+    bool open = false;
+    for (int base = 0; base < nzz; base += 32) {
+        const int cnt = min(32, nzz - base);
+        if (lane < cnt) {
+            const double z = nzz > 1 ? __dmul_rn(zq[base + lane], S.z0) : 0.0;
+            an_pixel(S, cdelt0, cdelt1, xs, xc, yb, z, sgx[lane], sgy[lane]);
+        }
+        __syncwarp();
+        int nr = 0;
+        if (lane == 0) {
+            for (int t = 0; t < cnt; t++) {
+                const int a = sgx[t], b = sgy[t];
+                const double w = wq[base + t];
+                if (open && a == og0 && b == og1) {
+                    ows = __dadd_rn(ows, w);
+                } else {
+                    if (open) {
+                        rg0[nr] = og0;
+                        rg1[nr] = og1;
+                        rws[nr] = ows;
+                        nr++;
+                    }
+                    og0 = a;
+                    og1 = b;
+                    ows = w;
+                    open = true;
+                }
+            }
+        }
+        nr = __shfl_sync(FULL, nr, 0);
+        __syncwarp();
+        for (int r = 0; r < nr; r++) emit(rg0[r], rg1[r], rws[r]);
+        __syncwarp();
+    }
+    if (lane == 0) {
+        rg0[0] = og0;
+        rg1[0] = og1;
+        rws[0] = ows;
+    }
+    __syncwarp();
+    emit(rg0[0], rg1[0], rws[0]);
+    __syncwarp();
+}
+
+struct AnWarp {
+    int sgx[32], sgy[32], rg0[33], rg1[33];
+    double rws[33];
+    int k0[BBGPU_MAXL], nk[BBGPU_MAXL];
+};
+
+// The sample of this warp: member k, sub-ring S, cos/sin of its azimuth; false if nothing to deposit.
+__device__ __forceinline__ bool an_sample(long long gs, long long nsamp, int nsub, const AnSub *__restrict__ subs,
+                                          const int *__restrict__ sbase, const int *__restrict__ ssub,
+                                          const double2 *__restrict__ cs, int &k, const AnSub *&S, double &caz,
+                                          double &saz, double &R) {
+    k = (int)(gs / nsamp);
+    const long long s = gs - (long long)k * nsamp;
+    const int ir = ssub[s];
+    S = subs + (size_t)k * nsub + ir;
+    if (!S->active) return false;
+    const int local = (int)(s - sbase[ir]);
+    const double2 c = cs[s];
+    caz = c.x;
+    saz = c.y;
+    R = S->R[local >= S->naz ? 1 : 0];
+    return true;
+}
+
+// Models: out64 (per member: box (by, bx, nz), stride mstride) += fixed-point deposits.
+__global__ void __launch_bounds__(AN_WPB * 32) k_an_model(GridDev g, const AnSub *__restrict__ subs, int nsub,
+                                                          const int *__restrict__ sbase, const int *__restrict__ ssub,
+                                                          const double2 *__restrict__ cs, long long nsamp, int nb,
+                                                          const double *__restrict__ zq, const double *__restrict__ wq,
+                                                          const double *__restrict__ vedges,
+                                                          const double *__restrict__ cd2i,
+                                                          const double *__restrict__ ptab,
+                                                          const MemberDev *__restrict__ mem,
+                                                          unsigned long long *__restrict__ out64, long long mstride) {
+    extern __shared__ double an_smem[];
+    __shared__ AnWarp wsm[AN_WPB];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long gs = (long long)blockIdx.x * AN_WPB + w;
+    if (gs >= nsamp * nb) return;
+    int k;
+    const AnSub *Sp;
+    double caz, saz, R;
+    if (!an_sample(gs, nsamp, nsub, subs, sbase, ssub, cs, k, Sp, caz, saz, R)) return;
+    const AnSub &S = *Sp;
+    const double wside = caz >= 0.0 ? S.wrec : S.wapp;
+    if (wside == 0.0) return;
+    const MemberDev &M = mem[k];
+    const int nz = g.nz, nl_n = g.nlines;
+    double *pe = an_smem + (size_t)w * nl_n * (nz + 2);
+    AnWarp &W = wsm[w];
+    const double fscale = ldexp(1.0, M.fix_exp);
+    unsigned long long *o64 = out64 + (size_t)k * mstride;
+    const double x = __dmul_rn(R, caz);
+    const double yb = __dmul_rn(__dmul_rn(R, saz), S.cinc);
+    const double xs = __dmul_rn(x, S.spa), xc = __dmul_rn(x, S.cpa);
+    // bbarolo/galmod.py:407
+    const double vplane = __dadd_rn(__dadd_rn(S.vsys, __dmul_rn(__dadd_rn(__dmul_rn(S.vrot, caz), __dmul_rn(S.vrad, saz)),
+                                                                S.sinc)),
+                                    __dmul_rn(S.vvert, S.cinc));
+    const double *zqs = zq + S.zq_off, *wqs = wq + S.zq_off;
+    if (!S.zdep) {
+        bool ready = false;
+        auto emit = [&](int g0, int g1, double ws) {
+            if (g0 < M.blo0 || g0 >= M.bhi0 || g1 < M.blo1 || g1 >= M.bhi1) return;
+            if (!ready) {
+                for (int nl = 0; nl < nl_n; nl++) {
+                    int k0, nk;
+                    an_profile(g, nl, vplane, S, vedges, ptab, pe + (size_t)nl * (nz + 2), k0, nk);
+                    W.k0[nl] = k0;
+                    W.nk[nl] = nk;
+                }
+                ready = true;
+            }
+            unsigned long long *o = o64 + ((size_t)(g1 - M.blo1) * M.bx + (size_t)(g0 - M.blo0)) * nz;
+            for (int nl = 0; nl < nl_n; nl++) {
+                if (W.nk[nl] == 0) continue;
+                const double aw = __dmul_rn(__dmul_rn(S.a[nl], wside), ws);
+                an_add(o, pe + (size_t)nl * (nz + 2), cd2i, W.k0[nl], W.nk[nl], aw, fscale);
+            }
+            __syncwarp();
+        };
+        an_runs(S, zqs, wqs, g.cdelt0, g.cdelt1, xs, xc, yb, W.sgx, W.sgy, W.rg0, W.rg1, W.rws, emit);
+        return;
+    }
+    // bbarolo/galmod.py:430-463: the velocity depends on |z|; the samples at +z and -z share a profile
+    const int nzz = S.nzz;
+    for (int kz = 0; kz < (nzz + 1) / 2; kz++) {
+        const int kz2 = nzz - 1 - kz;
+        int ga = 0, gb = 0;
+        if (lane < 2) {
+            const double z = __dmul_rn(zqs[lane == 0 ? kz : kz2], S.z0);
+            an_pixel(S, g.cdelt0, g.cdelt1, xs, xc, yb, z, ga, gb);
+        }
+        const int gx1 = __shfl_sync(FULL, ga, 0), gy1 = __shfl_sync(FULL, gb, 0);
+        const int gx2 = __shfl_sync(FULL, ga, 1), gy2 = __shfl_sync(FULL, gb, 1);
+        const bool in1 = !(gx1 < M.blo0 || gx1 >= M.bhi0 || gy1 < M.blo1 || gy1 >= M.bhi1);
+        const bool in2 = kz2 != kz && !(gx2 < M.blo0 || gx2 >= M.bhi0 || gy2 < M.blo1 || gy2 >= M.bhi1);
+        if (!(in1 || in2)) continue;
+        const double az_ = fabs(__dmul_rn(zqs[kz], S.z0));
+        double v = vplane;
+        if (az_ > S.zcyl) {
+            const double lv = __dsub_rn(S.vrot, __dmul_rn(S.dvdz, __dsub_rn(az_, S.zcyl)));
+            const double vr = S.vrot >= 0.0 ? ((0.0 > lv) ? 0.0 : lv) : ((0.0 < lv) ? 0.0 : lv);
+            v = __dadd_rn(__dadd_rn(S.vsys, __dmul_rn(__dadd_rn(__dmul_rn(vr, caz), __dmul_rn(S.vrad, saz)), S.sinc)),
+                          __dmul_rn(S.vvert, S.cinc));
+        }
+        for (int nl = 0; nl < nl_n; nl++) {
+            int k0, nk;
+            an_profile(g, nl, v, S, vedges, ptab, pe, k0, nk);
+            if (nk == 0) continue;
+            const double a = __dmul_rn(S.a[nl], wside);
+            if (in1 && in2 && gx1 == gx2 && gy1 == gy2) {
+                unsigned long long *o = o64 + ((size_t)(gy1 - M.blo1) * M.bx + (size_t)(gx1 - M.blo0)) * nz;
+                an_add(o, pe, cd2i, k0, nk, __dmul_rn(a, __dadd_rn(wqs[kz], wqs[kz2])), fscale);
+            } else {
+                if (in1) {
+                    unsigned long long *o = o64 + ((size_t)(gy1 - M.blo1) * M.bx + (size_t)(gx1 - M.blo0)) * nz;
+                    an_add(o, pe, cd2i, k0, nk, __dmul_rn(a, wqs[kz]), fscale);
+                }
+                if (in2) {
+                    unsigned long long *o = o64 + ((size_t)(gy2 - M.blo1) * M.bx + (size_t)(gx2 - M.blo0)) * nz;
+                    an_add(o, pe, cd2i, k0, nk, __dmul_rn(a, wqs[kz2]), fscale);
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// Ring maps: maps64 (nr, by, bx) += fixed-point weights of the runs (bbarolo/galmod.py:518-529).
+__global__ void __launch_bounds__(AN_WPB * 32) k_an_maps(GridDev g, const AnSub *__restrict__ subs, int nsub,
+                                                         const int *__restrict__ sbase, const int *__restrict__ ssub,
+                                                         const double2 *__restrict__ cs, long long nsamp,
+                                                         const double *__restrict__ zq, const double *__restrict__ wq,
+                                                         const long long *__restrict__ widx,
+                                                         const double *__restrict__ wval, MemberDev M,
+                                                         unsigned long long *__restrict__ maps64) {
+    __shared__ AnWarp wsm[AN_WPB];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long gs = (long long)blockIdx.x * AN_WPB + w;
+    if (gs >= nsamp) return;
+    int k;
+    const AnSub *Sp;
+    double caz, saz, R;
+    if (!an_sample(gs, nsamp, nsub, subs, sbase, ssub, cs, k, Sp, caz, saz, R)) return;
+    const AnSub &S = *Sp;
+    const double wside = caz >= 0.0 ? S.wrec : S.wapp;
+    if (wside == 0.0) return;
+    AnWarp &W = wsm[w];
+    const double fscale = ldexp(1.0, M.fix_exp);
+    const double x = __dmul_rn(R, caz);
+    const double yb = __dmul_rn(__dmul_rn(R, saz), S.cinc);
+    const double xs = __dmul_rn(x, S.spa), xc = __dmul_rn(x, S.cpa);
+    const size_t plane = (size_t)M.by * M.bx;
+    auto emit = [&](int g0, int g1, double ws) {
+        if (g0 < M.blo0 || g0 >= M.bhi0 || g1 < M.blo1 || g1 >= M.bhi1) return;
+        if (lane < 2) {
+            const long long r = widx[2 * S.sub + lane];
+            if (r >= 0) {
+                const double t = __dmul_rn(__dmul_rn(__dmul_rn(S.fluxsc, ws), wval[2 * S.sub + lane]), wside);
+                const long long q = __double2ll_rn(__dmul_rn(t, fscale));
+                if (q)
+                    atomicAdd(maps64 + (size_t)r * plane + (size_t)(g1 - M.blo1) * M.bx + (size_t)(g0 - M.blo0),
+                              (unsigned long long)q);
+            }
+        }
+    };
+    an_runs(S, zq + S.zq_off, wq + S.zq_off, g.cdelt0, g.cdelt1, xs, xc, yb, W.sgx, W.sgy, W.rg0, W.rg1, W.rws,
+            emit);
+}
+
+// fixed point (units 2^-e of member k) -> float32 model and, optionally, float64 copy
+__global__ void k_fix_to_model(const long long *__restrict__ in, const MemberDev *__restrict__ mem, long long mstride,
+                               int nz, float *__restrict__ model, double *__restrict__ model64) {
+    const int k = blockIdx.y;
+    const MemberDev &M = mem[k];
+    const long long n = (long long)M.by * M.bx * nz;
+    const double sc = ldexp(1.0, -M.fix_exp);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double v = __dmul_rn((double)in[(size_t)k * mstride + i], sc);
+        model[(size_t)k * mstride + i] = (float)v;
+        if (model64) model64[(size_t)k * mstride + i] = v;
+    }
+}
+
+}  // namespace
+
+size_t an_smem_bytes(int nz, int nlines) { return (size_t)AN_WPB * nlines * (nz + 2) * sizeof(double); }
+
+void launch_an_model(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase, const int *ssub,
+                     const double *cs, long long nsamp, int nb, const double *zq, const double *wq,
+                     const double *vedges, const double *cd2i, const double *ptab, const MemberDev *mem,
+                     long long *out64, long long mstride) {
+    const long long nw = nsamp * nb;
+    if (nw == 0) return;
+    const size_t smem = an_smem_bytes(g.nz, g.nlines);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_an_model, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_an_model<<<(unsigned)((nw + AN_WPB - 1) / AN_WPB), AN_WPB * 32, smem, s>>>(
+        g, subs, nsub, sbase, ssub, (const double2 *)cs, nsamp, nb, zq, wq, vedges, cd2i, ptab, mem,
+        (unsigned long long *)out64, mstride);
+}
+
+void launch_an_maps(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase, const int *ssub,
+                    const double *cs, long long nsamp, const double *zq, const double *wq, const long long *widx,
+                    const double *wval, const MemberDev &M, long long *maps64) {
+    if (nsamp == 0) return;
+    k_an_maps<<<(unsigned)((nsamp + AN_WPB - 1) / AN_WPB), AN_WPB * 32, 0, s>>>(
+        g, subs, nsub, sbase, ssub, (const double2 *)cs, nsamp, zq, wq, widx, wval, M, (unsigned long long *)maps64);
+}
+
+void launch_fix_to_model(cudaStream_t s, const long long *in, const MemberDev *mem, int nb, long long mstride, int nz,
+                         float *model, double *model64) {
+    if (nb == 0) return;
+    dim3 grid(256, nb);
+    k_fix_to_model<<<grid, 256, 0, s>>>(in, mem, mstride, nz, model, model64);
+}

@@ -42,6 +42,9 @@ struct bbgpu_ctx {
     // constants
     double *d_cd2i = nullptr;
     float *d_cd2if = nullptr;
+    std::vector<double> h_cd2i;
+    double *d_vedges = nullptr;   // channel edges per line (nlines, nz + 1): ANALYTIC models
+    double *d_ptab = nullptr;     // normal CDF table of the ANALYTIC line profiles
     ZigDev *d_zig = nullptr;
     float *d_taps = nullptr;
     int ky = 0, kx = 0, kxw = 0;
@@ -345,6 +348,7 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
             bbh_layout_free(&E.host);
         }
     cudaFree(ctx->d_cd2i); cudaFree(ctx->d_cd2if); cudaFree(ctx->d_zig); cudaFree(ctx->d_taps);
+    cudaFree(ctx->d_vedges); cudaFree(ctx->d_ptab);
     cudaFree(ctx->d_data); cudaFree(ctx->d_mask); cudaFree(ctx->d_region);
     for (auto &a : ctx->d_deff)
         for (auto &b : a) cudaFree(b);
@@ -399,7 +403,6 @@ extern "C" int bbgpu_set_option(bbgpu_ctx *ctx, int opt, int value) {
 // ------------------------------------------------------------------------------------------- set-up
 extern "C" int bbgpu_set_grid(bbgpu_ctx *ctx, const bbgpu_grid *gr, const double *cd2i, const double *lfreq0,
                               const double *relint, const double *vedges) {
-    (void)vedges;
     if (!ctx || !gr || !cd2i || !lfreq0 || !relint) return fail(ctx, BBGPU_ERR_ARG, "set_grid: null argument");
     if (gr->nx <= 0 || gr->ny <= 0 || gr->nz <= 0) return fail(ctx, BBGPU_ERR_ARG, "set_grid: empty cube");
     if (gr->nlines < 1 || gr->nlines > BBGPU_MAXL)
@@ -441,6 +444,20 @@ extern "C" int bbgpu_set_grid(bbgpu_ctx *ctx, const bbgpu_grid *gr, const double
     CK(cudaMalloc(&ctx->d_cd2if, g.nz * sizeof(float)));
     CK(cudaMemcpy(ctx->d_cd2i, cd2i, g.nz * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->d_cd2if, cf.data(), g.nz * sizeof(float), cudaMemcpyHostToDevice));
+    ctx->h_cd2i.assign(cd2i, cd2i + g.nz);
+    cudaFree(ctx->d_vedges);
+    ctx->d_vedges = nullptr;
+    if (vedges) {
+        const size_t ne = (size_t)g.nlines * (g.nz + 1);
+        CK(cudaMalloc(&ctx->d_vedges, ne * sizeof(double)));
+        CK(cudaMemcpy(ctx->d_vedges, vedges, ne * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    if (!ctx->d_ptab) {
+        std::vector<double> tab(6146);
+        bbh_phi_table(tab.data());
+        CK(cudaMalloc(&ctx->d_ptab, tab.size() * sizeof(double)));
+        CK(cudaMemcpy(ctx->d_ptab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
     // deposit tile: pixels x channels of 8-byte sums within 56 KB (3 CTAs per SM with the staging buffers)
     int tp = 57344 / (8 * g.nz);
     if (tp >= 64) { ctx->tx = 8; ctx->ty = 8; }
@@ -847,20 +864,6 @@ extern "C" int bbgpu_residuals_fracerr(bbgpu_ctx *ctx, const double *model, cons
     return sumsq_common(ctx, model, data, mask, maskmode, region, nz, ny, nx, sigma2, eps2, out2);
 }
 
-// ------------------------------------------------------------------------------------------- not yet on the device
-extern "C" int bbgpu_galmod_analytic(bbgpu_ctx *ctx, double *out, const double *sr, int nsub, int ring_lo, int ring_hi,
-                                     int nzq, int blo0, int blo1, int bhi0, int bhi1) {
-    (void)out; (void)sr; (void)nsub; (void)ring_lo; (void)ring_hi; (void)nzq; (void)blo0; (void)blo1; (void)bhi0; (void)bhi1;
-    return fail(ctx, BBGPU_ERR_ARG, "galmod_analytic: not available in this build");
-}
-
-extern "C" int bbgpu_ring_maps_analytic(bbgpu_ctx *ctx, double *out, int nr, const double *sr, int nsub,
-                                        const int64_t *widx, const double *wval, int nzq, int blo0, int blo1, int bhi0,
-                                        int bhi1) {
-    (void)out; (void)nr; (void)sr; (void)nsub; (void)widx; (void)wval; (void)nzq; (void)blo0; (void)blo1; (void)bhi0; (void)bhi1;
-    return fail(ctx, BBGPU_ERR_ARG, "ring_maps_analytic: not available in this build");
-}
-
 // A scoped set of device buffers freed at the end of a stand-alone entry point.
 struct DevBufs {
     std::vector<void *> p;
@@ -879,6 +882,129 @@ struct DevBufs {
         return true;
     }
 };
+
+// The azimuthal samples and sub-ring constants of one ANALYTIC call, on the device.
+struct AnDev {
+    AnSub *subs = nullptr;
+    int *sbase = nullptr, *ssub = nullptr;
+    double *cs = nullptr, *zq = nullptr, *wq = nullptr;
+    long long nsamp = 0;
+};
+
+static int an_upload(bbgpu_ctx *ctx, DevBufs &B, const std::vector<AnSub> &subs, const double *R0, int nsub,
+                     const std::vector<double> &zq, const std::vector<double> &wq, AnDev &D) {
+    std::vector<int> sbase, ssub;
+    std::vector<double> cs;
+    bbh_an_samples(R0, nsub, &ctx->g, sbase, ssub, cs);
+    D.nsamp = sbase[nsub];
+    if (!B.get(&D.subs, sizeof(AnSub) * (subs.size() ? subs.size() : 1)) || !B.get(&D.sbase, sizeof(int) * sbase.size()) ||
+        !B.get(&D.ssub, sizeof(int) * ssub.size()) || !B.get(&D.cs, sizeof(double) * cs.size()) ||
+        !B.get(&D.zq, sizeof(double) * (zq.size() ? zq.size() : 1)) ||
+        !B.get(&D.wq, sizeof(double) * (wq.size() ? wq.size() : 1)))
+        return fail(ctx, BBGPU_ERR_NOMEM, "analytic: allocation failed");
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(D.subs, subs.data(), sizeof(AnSub) * subs.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(D.sbase, sbase.data(), sizeof(int) * sbase.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(D.ssub, ssub.data(), sizeof(int) * ssub.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(D.cs, cs.data(), sizeof(double) * cs.size(), cudaMemcpyHostToDevice, s));
+    if (zq.size()) {
+        CK(cudaMemcpyAsync(D.zq, zq.data(), sizeof(double) * zq.size(), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(D.wq, wq.data(), sizeof(double) * wq.size(), cudaMemcpyHostToDevice, s));
+    }
+    // (the host vectors are freed on return: the copies complete first)
+    CK(cudaStreamSynchronize(s));
+    return 0;
+}
+
+extern "C" int bbgpu_galmod_analytic(bbgpu_ctx *ctx, double *out, const double *sr, int nsub, int ring_lo, int ring_hi,
+                                     int nzq, int blo0, int blo1, int bhi0, int bhi1) {
+    if (!ctx) return BBGPU_ERR_ARG;
+    if (!out || !sr || ring_lo < 0 || ring_hi > nsub || ring_lo > ring_hi || blo0 > bhi0 || blo1 > bhi1)
+        return fail(ctx, BBGPU_ERR_ARG, "galmod_analytic: invalid arguments");
+    if (!ctx->grid_set) return fail(ctx, BBGPU_ERR_STATE, "galmod_analytic before set_grid");
+    if (!ctx->d_vedges) return fail(ctx, BBGPU_ERR_STATE, "galmod_analytic: set_grid was given no channel edges");
+    const GridDev &g = ctx->g;
+    if (an_smem_bytes(g.nz, g.nlines) > AN_SMEM_MAX)
+        return fail(ctx, BBGPU_ERR_ARG, "galmod_analytic: %d channels x %d lines above the device limit", g.nz, g.nlines);
+    CK(cudaSetDevice(ctx->device));
+    const int ns = ring_hi - ring_lo, by = bhi1 - blo1, bx = bhi0 - blo0;
+    if (ns == 0 || by == 0 || bx == 0) return BBGPU_OK;
+    std::vector<double> s2((size_t)BBGPU_NSR * ns);
+    for (int r = 0; r < BBGPU_NSR; r++)
+        for (int i = 0; i < ns; i++) s2[(size_t)r * ns + i] = sr[(size_t)r * nsub + ring_lo + i];
+    std::vector<AnSub> subs(ns);
+    std::vector<double> zq, wq;
+    const int e = bbh_an_subs(s2.data(), ns, &g, nzq, blo0, blo1, bhi0, bhi1, ctx->h_cd2i.data(), 0, nullptr, nullptr,
+                              subs.data(), zq, wq);
+    if (e == -10000) return fail(ctx, BBGPU_ERR_ARG, "galmod_analytic: the total flux is not finite");
+    DevBufs B;
+    AnDev D;
+    int rc = an_upload(ctx, B, subs, s2.data(), ns, zq, wq, D);
+    if (rc) return rc;
+    const size_t n = (size_t)by * bx * g.nz;
+    long long *o64 = nullptr;
+    MemberDev *dm = nullptr;
+    if (!B.get(&o64, n * sizeof(long long)) || !B.get(&dm, sizeof(MemberDev)))
+        return fail(ctx, BBGPU_ERR_NOMEM, "galmod_analytic: allocation failed");
+    MemberDev M{};
+    M.blo0 = blo0; M.blo1 = blo1; M.bhi0 = bhi0; M.bhi1 = bhi1; M.bx = bx; M.by = by; M.fix_exp = e;
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(dm, &M, sizeof M, cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(o64, 0, n * sizeof(long long), s));
+    launch_an_model(s, g, D.subs, ns, D.sbase, D.ssub, D.cs, D.nsamp, 1, D.zq, D.wq, ctx->d_vedges, ctx->d_cd2i,
+                    ctx->d_ptab, dm, o64, (long long)n);
+    CKL();
+    std::vector<long long> h(n);
+    CK(cudaMemcpyAsync(h.data(), o64, n * sizeof(long long), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const double sc = ldexp(1.0, -e);
+    for (size_t i = 0; i < n; i++) out[i] += (double)h[i] * sc;
+    return BBGPU_OK;
+}
+
+extern "C" int bbgpu_ring_maps_analytic(bbgpu_ctx *ctx, double *out, int nr, const double *sr, int nsub,
+                                        const int64_t *widx, const double *wval, int nzq, int blo0, int blo1, int bhi0,
+                                        int bhi1) {
+    if (!ctx) return BBGPU_ERR_ARG;
+    if (!out || !sr || !widx || !wval || nr < 0 || nsub < 0 || blo0 > bhi0 || blo1 > bhi1)
+        return fail(ctx, BBGPU_ERR_ARG, "ring_maps_analytic: invalid arguments");
+    if (!ctx->grid_set) return fail(ctx, BBGPU_ERR_STATE, "ring_maps_analytic before set_grid");
+    for (int i = 0; i < 2 * nsub; i++)
+        if (widx[i] >= nr) return fail(ctx, BBGPU_ERR_ARG, "ring_maps_analytic: ring index %lld >= %d", (long long)widx[i], nr);
+    CK(cudaSetDevice(ctx->device));
+    const int by = bhi1 - blo1, bx = bhi0 - blo0;
+    if (nsub == 0 || nr == 0 || by == 0 || bx == 0) return BBGPU_OK;
+    const GridDev &g = ctx->g;
+    std::vector<AnSub> subs(nsub);
+    std::vector<double> zq, wq;
+    const int e = bbh_an_subs(sr, nsub, &g, nzq, blo0, blo1, bhi0, bhi1, ctx->h_cd2i.data(), 1, widx, wval,
+                              subs.data(), zq, wq);
+    if (e == -10000) return fail(ctx, BBGPU_ERR_ARG, "ring_maps_analytic: the weights are not finite");
+    DevBufs B;
+    AnDev D;
+    int rc = an_upload(ctx, B, subs, sr, nsub, zq, wq, D);
+    if (rc) return rc;
+    const size_t n = (size_t)nr * by * bx;
+    long long *m64 = nullptr, *dwi = nullptr;
+    double *dwv = nullptr;
+    if (!B.get(&m64, n * sizeof(long long)) || !B.get(&dwi, sizeof(long long) * 2 * nsub) ||
+        !B.get(&dwv, sizeof(double) * 2 * nsub))
+        return fail(ctx, BBGPU_ERR_NOMEM, "ring_maps_analytic: allocation failed");
+    MemberDev M{};
+    M.blo0 = blo0; M.blo1 = blo1; M.bhi0 = bhi0; M.bhi1 = bhi1; M.bx = bx; M.by = by; M.fix_exp = e;
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(dwi, widx, sizeof(long long) * 2 * nsub, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dwv, wval, sizeof(double) * 2 * nsub, cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(m64, 0, n * sizeof(long long), s));
+    launch_an_maps(s, g, D.subs, nsub, D.sbase, D.ssub, D.cs, D.nsamp, D.zq, D.wq, dwi, dwv, M, m64);
+    CKL();
+    std::vector<long long> h(n);
+    CK(cudaMemcpyAsync(h.data(), m64, n * sizeof(long long), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const double sc = ldexp(1.0, -e);
+    for (size_t i = 0; i < n; i++) out[i] += (double)h[i] * sc;
+    return BBGPU_OK;
+}
 
 extern "C" int bbgpu_conv_sparse(bbgpu_ctx *ctx, const double *model, double *out, int ny, int nx, int nz,
                                  const double *kernel, int ky, int kx, double scale) {

@@ -7,6 +7,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
+#include <cmath>
 #include <vector>
 
 #include "internal.h"
@@ -342,4 +344,165 @@ void bbh_norm_footprint(int bsy, int bsx, double x0, double y0, double phi, doub
             const double wf = usesin ? fabs(sin(th * F)) : fabs(cos(th * F));
             wmap[p] = pow(wf, apow);
         }
+}
+
+// ------------------------------------------------------------------------------------------- ANALYTIC
+// The vertical layers of the ANALYTIC models (bbarolo/galmod.py:217-259): the cumulative flux below x (units
+// of z0), the height beyond which less than 1e-6 of the flux remains, the height where the density falls
+// below 1e-3 of its peak.
+static double layer_cdf(int ltype, double x) {
+    if (ltype == 1) return 0.5 * (1.0 + erf(x / sqrt(2.0)));
+    if (ltype == 2) return 0.5 * (1.0 + tanh(x));
+    if (ltype == 3) return x >= 0 ? 1.0 - 0.5 * exp(-x) : 0.5 * exp(x);
+    if (ltype == 4) return 0.5 + atan(x) / M_PI;
+    const double c = x < -1.0 ? -1.0 : (x > 1.0 ? 1.0 : x);
+    return 0.5 * (c + 1.0);
+}
+
+static double layer_extent(int ltype) {
+    return ltype == 1 ? 5.0 : ltype == 2 ? 7.6 : ltype == 3 ? 14.0 : ltype == 4 ? 1e30 : 1.0;
+}
+
+static double layer_core(int ltype) {
+    return ltype == 1 ? 3.717 : ltype == 2 ? 4.147 : ltype == 3 ? 6.908 : ltype == 4 ? 31.61 : 1e30;
+}
+
+int bbh_zgrid(double *zq, double *wq, int nmax, int ltype, double z0, double sinc, double pixsize, double dvdz,
+              double sig, double R0, double radsep, double xpos, double ypos, double cdelt0, double cdelt1,
+              long long blo0, long long blo1, long long bhi0, long long bhi1, double zstep) {
+    const double s = fabs(sinc);
+    if (z0 <= 0 || nmax < 2 || s < 1e-6) {
+        zq[0] = 0.0;
+        wq[0] = 1.0;
+        return 1;
+    }
+    const double dx = std::max(fabs((double)blo0 - 0.5 - xpos), fabs((double)bhi0 - 0.5 - xpos)) * fabs(cdelt0);
+    const double dy = std::max(fabs((double)blo1 - 0.5 - ypos), fabs((double)bhi1 - 0.5 - ypos)) * fabs(cdelt1);
+    const double zlim = std::min(layer_extent(ltype), (R0 + radsep + sqrt(dx * dx + dy * dy)) / (s * z0));
+    double step = zstep * pixsize / (z0 * s);
+    if (dvdz != 0) step = std::min(step, 0.5 * sig / (fabs(dvdz) * z0 * s));
+    const double zc = layer_core(ltype);
+    long long nin, nout;
+    for (;;) {
+        nin = std::max((long long)ceil(std::min(zc, zlim) / step), 1LL);
+        nout = std::max((long long)ceil((zlim - (double)nin * step) / (4.0 * step)), 0LL);
+        if (2 * (nin + nout) <= nmax) break;
+        step *= 1.01 * (double)(nin + nout) / (double)(nmax / 2);
+    }
+    const long long half = nin + nout;
+    for (long long j = 0; j < half; j++) {
+        const double lo = j < nin ? (double)j * step : (double)(nin + 4 * (j - nin)) * step;
+        const double hi = std::min(lo + (j < nin ? step : 4.0 * step), zlim);
+        const double w = layer_cdf(ltype, hi) - layer_cdf(ltype, lo);
+        zq[half + j] = 0.5 * (lo + hi);
+        wq[half + j] = w;
+        zq[half - 1 - j] = -0.5 * (lo + hi);
+        wq[half - 1 - j] = w;
+    }
+    return (int)(2 * half);
+}
+
+static long long an_naz(double R0, double pixarea) {   // bbarolo/galmod.py:345-346
+    const double circ_pix = 2 * M_PI * R0 / sqrt(pixarea);
+    return std::max((long long)(3 * circ_pix + 0.5), 16LL);
+}
+
+void bbh_an_samples(const double *R0, int nsub, const GridDev *g, std::vector<int> &sbase, std::vector<int> &ssub,
+                    std::vector<double> &cs) {
+    sbase.assign(nsub + 1, 0);
+    long long n = 0;
+    for (int ir = 0; ir < nsub; ir++) {
+        sbase[ir] = (int)n;
+        n += 2 * an_naz(R0[ir], g->pixarea);
+    }
+    sbase[nsub] = (int)n;
+    ssub.resize(n ? n : 1);
+    cs.resize(2 * (n ? n : 1));
+    for (int ir = 0; ir < nsub; ir++) {
+        const long long naz = an_naz(R0[ir], g->pixarea);
+        const double daz = 2 * M_PI / (double)naz;
+        const double cd = cos(daz), sd = sin(daz);
+        for (int kr = 0; kr < 2; kr++) {
+            const double az0 = 2 * M_PI * (0.5 * ((kr + 1) % 2) + 0.25) / (double)naz;
+            double caz = cos(az0), saz = sin(az0);
+            for (long long ka = 0; ka < naz; ka++) {
+                if (ka > 0) {
+                    const double c2 = caz * cd - saz * sd, s2 = saz * cd + caz * sd;
+                    caz = c2;
+                    saz = s2;
+                }
+                const long long q = sbase[ir] + kr * naz + ka;
+                ssub[q] = ir;
+                cs[2 * q] = caz;
+                cs[2 * q + 1] = saz;
+            }
+        }
+    }
+}
+
+int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0, int blo1, int bhi0, int bhi1,
+                const double *cd2i, int maps, const int64_t *widx, const double *wval, AnSub *out,
+                std::vector<double> &zq, std::vector<double> &wq) {
+#define SR(r, i) sr[(size_t)(r) * nsub + (i)]
+    const int nb = nzq > 1 ? nzq : 1;
+    std::vector<double> tz(nb), tw(nb);
+    const double pixsize = sqrt(g->pixarea);
+    double cmax = 0.0, lsum = 0.0, bound = 0.0;
+    for (int k = 0; k < g->nz; k++) cmax = std::max(cmax, fabs(cd2i[k]));
+    for (int nl = 0; nl < g->nlines; nl++) lsum += fabs(g->relint[nl]);
+    for (int ir = 0; ir < nsub; ir++) {
+        AnSub &S = out[ir];
+        memset(&S, 0, sizeof S);
+        S.sub = ir;
+        const double R0 = SR(0, ir), dens = SR(5, ir);
+        S.active = maps ? (widx[2 * ir] >= 0 || widx[2 * ir + 1] >= 0) : dens != 0;
+        const double ring_area_pix = 2 * M_PI * R0 * g->radsep / g->pixarea;
+        const long long naz = an_naz(R0, g->pixarea);
+        const int nrad = 2;
+        S.naz = (int)naz;
+        S.vrot = SR(1, ir); S.vrad = SR(2, ir); S.vvert = SR(3, ir);
+        const double sig = std::max(sqrt(SR(4, ir) * SR(4, ir) + g->sig_instr * g->sig_instr), 1e-6 * fabs(g->chwidth));
+        S.inv = 1.0 / sig;
+        S.K = (long long)(5.0 * sig / g->chwidth) + 2;
+        S.z0 = SR(6, ir); S.dvdz = SR(7, ir); S.zcyl = SR(8, ir);
+        S.sinc = sin(SR(9, ir));
+        S.cinc = cos(SR(9, ir));
+        const double phi = SR(10, ir);
+        S.spa = sin(phi) * cos(g->crota2) + cos(phi) * sin(g->crota2);
+        S.cpa = cos(phi) * cos(g->crota2) - sin(phi) * sin(g->crota2);
+        S.xpos = SR(11, ir); S.ypos = SR(12, ir); S.vsys = SR(13, ir);
+        S.wrec = SR(14, ir); S.wapp = SR(15, ir);
+        S.zq_off = (int)zq.size();
+        if (S.active) {
+            S.nzz = bbh_zgrid(tz.data(), tw.data(), nzq, g->ltype, S.z0, S.sinc, pixsize, S.dvdz, sig, R0, g->radsep,
+                              S.xpos, S.ypos, g->cdelt0, g->cdelt1, blo0, blo1, bhi0, bhi1, g->zstep);
+            zq.insert(zq.end(), tz.begin(), tz.begin() + S.nzz);
+            wq.insert(wq.end(), tw.begin(), tw.begin() + S.nzz);
+        }
+        S.fluxsc = maps ? ring_area_pix * g->pixarea / (double)(naz * nrad)
+                        : dens * ring_area_pix * g->pixarea / (double)(naz * nrad);
+        for (int nl = 0; nl < g->nlines; nl++) S.a[nl] = g->relint[nl] * S.fluxsc;
+        S.zdep = 0;
+        if (!maps && S.active && S.dvdz != 0 && S.nzz > 1)
+            for (int kz = 0; kz < S.nzz; kz++)
+                if (fabs(tz[kz] * S.z0) > S.zcyl) { S.zdep = 1; break; }
+        const double r_inner = R0 - 0.5 * g->radsep;
+        for (int kr = 0; kr < nrad; kr++) {
+            const double u = (kr + 0.5) / nrad;
+            S.R[kr] = sqrt(r_inner * r_inner + 2.0 * g->radsep * R0 * u);
+        }
+        if (!S.active) continue;
+        // every deposit of the sub-ring is at most |fluxsc| x |wside| x (line: sum of relint x max cd2i; map:
+        // max wval) per sample, the vertical weights and the channel profile summing to at most 1
+        const double ws = std::max(fabs(S.wrec), fabs(S.wapp));
+        double per = lsum * cmax;
+        if (maps) per = std::max(fabs(wval[2 * ir]), fabs(wval[2 * ir + 1]));
+        bound += fabs(S.fluxsc) * ws * per * (double)(naz * nrad);
+    }
+#undef SR
+    if (!std::isfinite(bound)) return -10000;
+    if (bound == 0) return 0;
+    int ex = 0;
+    frexp(bound * 1.01, &ex);       // bound * 1.01 < 2^ex
+    return std::min(62 - ex, 1000);
 }

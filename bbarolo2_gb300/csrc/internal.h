@@ -4,6 +4,10 @@
 #include <stdint.h>
 #include <stddef.h>
 
+#ifdef __cplusplus
+#include <vector>
+#endif
+
 #define BBGPU_MAXL 4          // emission lines supported by the device path
 #define BBGPU_MAXK 63         // largest beam kernel side
 #define BBGPU_NSR 16          // rows of a sub-ring table
@@ -24,12 +28,14 @@ struct SubMC {
     int nc, nv, cloud_base, active;
 };
 
-// Per (member, sub-ring) parameters of the ANALYTIC deposit.
-struct SubAN {
-    double xpos, ypos, spa, cpa, sinc, cinc, z0, zcyl, dvdz, vrot, vrad, vvert, vsys, sig, wrec, wapp, R0;
-    double fluxsc, r_inner, cd, sd;
-    int naz, K, nzz, zq_off;        // azimuths, line half-window, vertical samples (offset in the zq table)
-    int zdep, active, sample_base, pad;
+// Per (member, sub-ring) parameters of the ANALYTIC deposit (bbarolo/galmod.py:347-374), float64 as the
+// reference. fluxsc: dens * ring area / samples for models, ring area / samples for ring maps.
+struct AnSub {
+    double xpos, ypos, spa, cpa, sinc, cinc, z0, zcyl, dvdz, vrot, vrad, vvert, vsys, inv, wrec, wapp, fluxsc;
+    double R[2];                    // radius of the two radial samples
+    double a[BBGPU_MAXL];           // relint[nl] * fluxsc (times wside at deposit)
+    long long K;                    // half-width of the line profile in channels
+    int naz, nzz, zq_off, zdep, active, sub;
 };
 
 // The constants of a context, as the kernels see them.
@@ -76,6 +82,21 @@ uint64_t bbh_layout_key(uint64_t seed, int ltype, int nsub, const int *nc, const
 void bbh_cloud_counts(const double *sr, int nsub, const int64_t *nv_in, const GridDev *g, int *nc, int *nv);
 // SubMC of one table; returns the exponent e of the fixed-point unit 2^-e of its deposits
 int bbh_submc(const double *sr, int nsub, const int *nc, const int *nv, const GridDev *g, SubMC *out);
+// ANALYTIC: the vertical samples of a sub-ring (bbarolo/galmod.py:276-323); returns their number
+int bbh_zgrid(double *zq, double *wq, int nmax, int ltype, double z0, double sinc, double pixsize, double dvdz,
+              double sig, double R0, double radsep, double xpos, double ypos, double cdelt0, double cdelt1,
+              long long blo0, long long blo1, long long bhi0, long long bhi1, double zstep);
+// ANALYTIC: the azimuthal samples of the sub-rings of radii R0 (they depend on R0 and the pixel area only):
+// sbase (nsub + 1) first sample of each sub-ring, ssub the sub-ring of each sample, cs (2 per sample) the
+// cos/sin of its azimuth from the reference's rotation recurrence (bbarolo/galmod.py:384-391)
+void bbh_an_samples(const double *R0, int nsub, const GridDev *g, std::vector<int> &sbase, std::vector<int> &ssub,
+                    std::vector<double> &cs);
+// ANALYTIC: the AnSub of each sub-ring of a table (maps: ring-map mode, active where widx has a ring), their
+// vertical samples appended to zq/wq; returns the fixed-point exponent e (deposits in units of 2^-e) or
+// -10000 when the total flux is not finite
+int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0, int blo1, int bhi0, int bhi1,
+                const double *cd2i, int maps, const int64_t *widx, const double *wval, AnSub *out,
+                std::vector<double> &zq, std::vector<double> &wq);
 // The pixels of a ring for the CLASSIC residual (bbarolo/galfit.py:62-93): inside flags and weights (bsy, bsx)
 void bbh_norm_footprint(int bsy, int bsx, double x0, double y0, double phi, double inc, double r1, double r2,
                         double wpow, int side, int foot, double hmax, uint8_t *inside, double *wmap);

@@ -99,3 +99,17 @@ void launch_norm_pix(cudaStream_t s, double *model, const float *data, const uin
                      const double *wmap, int bsy, int bsx, int nz, int ftype, const double *chan_noise,
                      double data_noise, int normtype, double factor_azim, const double *P, const long long *ilo,
                      const long long *ihi, int ky, const double *thr, double *part);
+
+// ---- ANALYTIC (analytic.cu)
+// dynamic shared memory of launch_an_model (the host keeps it within AN_SMEM_MAX)
+#define AN_SMEM_MAX (200 * 1024)
+size_t an_smem_bytes(int nz, int nlines);
+void launch_an_model(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase, const int *ssub,
+                     const double *cs, long long nsamp, int nb, const double *zq, const double *wq,
+                     const double *vedges, const double *cd2i, const double *ptab, const MemberDev *mem,
+                     long long *out64, long long mstride);
+void launch_an_maps(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase, const int *ssub,
+                    const double *cs, long long nsamp, const double *zq, const double *wq, const long long *widx,
+                    const double *wval, const MemberDev &M, long long *maps64);
+void launch_fix_to_model(cudaStream_t s, const long long *in, const MemberDev *mem, int nb, long long mstride, int nz,
+                         float *model, double *model64);

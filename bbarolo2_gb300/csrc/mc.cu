@@ -20,19 +20,12 @@
 #include <math.h>
 #include <stdint.h>
 
+#include "devmath.cuh"
 #include "kernels.h"
 
-#define C_MS 2.99792458e08
 #define ERR_LAYOUT 1
 
 namespace {
-
-// bbarolo/galmod.py:38-46
-__device__ __forceinline__ long long lround_ref(double x) {
-    if (!(fabs(x) < 1e18)) return -(1LL << 62);
-    if (x >= 0) return (long long)__dadd_rn(x, 0.5);
-    return -(long long)__dadd_rn(-x, 0.5);
-}
 
 // floor(v + 0.5) if it equals the reference's rounding of the exact value (|error of v| < eps)
 __device__ __forceinline__ bool round_fast(float v, float eps, int &out) {
@@ -47,20 +40,6 @@ __device__ __forceinline__ bool round_fast(float v, float eps, int &out) {
 
 // 2^-18: 64 float32 units of roundoff per unit of magnitude (the fast paths have fewer than 12 roundings)
 #define EPS_REL 3.814697265625e-06f
-
-// bbarolo/galmod.py:49-62
-__device__ __forceinline__ double velgrid_exact(double v, const GridDev &g, int nl) {
-    double w;
-    if (g.axtyp == 4) w = v;
-    else {
-        double f0 = g.lfreq0[nl];
-        if (g.velsys == 1) w = __dmul_rn(f0, __dsub_rn(1.0, __ddiv_rn(v, C_MS)));
-        else if (g.velsys == 2) w = __dmul_rn(f0, __ddiv_rn(C_MS, __dadd_rn(C_MS, v)));
-        else w = __dmul_rn(f0, __dsqrt_rn(__ddiv_rn(__dsub_rn(C_MS, v), __dadd_rn(C_MS, v))));
-        if (g.axtyp == 2) w = __ddiv_rn(C_MS, w);
-    }
-    return __dsub_rn(__dadd_rn(__ddiv_rn(__dsub_rn(w, g.crval3), g.cdelt3), g.crpix3), 1.0);
-}
 
 // the exact pixel of a cloud (bbarolo/galmod.py:133-137)
 __device__ __forceinline__ void pixel_exact(const SubMC &S, const GridDev &g, const double *cd, long long &g0,

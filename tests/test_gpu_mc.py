@@ -11,34 +11,7 @@ import golden_io as G
 pytestmark = pytest.mark.gpu
 
 
-class _Ctx:
-    """A device context set up from the scalars of a fixture case."""
-
-    def __init__(self, meta, arrs, nm):
-        from bbarolo2_gb300 import _lib
-        self.L = _lib
-        self.c = _lib.Context(0)
-        g = _lib.Grid()
-        m = meta
-        g.nx, g.ny, g.nz = m["dimx"], m["dimy"], m["nz"]
-        g.nlines = arrs[nm + "/lfreq0"].size
-        g.axtyp, g.velsys, g.ltype, g.cmode = m["axtyp"], m["velsys"], m["ltype"], m["cmode"]
-        g.radsep, g.cdens, g.pixarea = m["radsep"], m["cdens"], m["pixarea"]
-        g.cdelt0, g.cdelt1, g.crota2 = m["cdelt0"], m["cdelt1"], m["crota2"]
-        g.sig_instr, g.crval3, g.cdelt3, g.crpix3 = m["sig_instr"], m["crval3"], m["cdelt3"], m["crpix3"]
-        g.chwidth, g.zstep, g.scalefactor = m["chmin"], m["zstep"], 1.0
-        cd2i = np.ascontiguousarray(arrs[nm + "/cd2i"])
-        lf = np.ascontiguousarray(arrs[nm + "/lfreq0"])
-        ri = np.ascontiguousarray(arrs[nm + "/relint"])
-        ve = np.ascontiguousarray(arrs[nm + "/vedges"])
-        self.c.check(self.c.L.bbgpu_set_grid(self.c.h, g, _lib.ptr(cd2i), _lib.ptr(lf), _lib.ptr(ri), _lib.ptr(ve)))
-
-    def mc(self, out, sr, lo, hi, seed, nv, blo, bhi):
-        sr = np.ascontiguousarray(sr)
-        nv = np.ascontiguousarray(nv, np.int64)
-        self.c.check(self.c.L.bbgpu_galmod_mc(self.c.h, self.L.ptr(out), self.L.ptr(sr), sr.shape[1], lo, hi, seed,
-                                              self.L.ptr(nv), blo[0], blo[1], bhi[0], bhi[1]))
-        return out
+_Ctx = G.DeviceCase
 
 
 def _cases():
