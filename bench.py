@@ -126,11 +126,12 @@ def algorithmic(dm, L, sr, nv, descs):
     ky, kx = dm.cfield.shape
     taps = int(np.count_nonzero(dm.cfield))
     vox = sum((int(d["bhi0"]) - int(d["blo0"])) * (int(d["bhi1"]) - int(d["blo1"])) * nz for d in descs)
-    # MC: per member, the velocity samples read (4 B each), the clouds (16 B), the model written (4 B/voxel)
+    # MC deposit: the clouds (16 B) and their velocity deviates (4 B each) are one table shared by the batch,
+    # read once; each member's model is written once (4 B per voxel)
     from bbarolo2_gb300.galmod import cloud_counts
     ncl, nsubcl = cloud_counts(st, sr[0], nv[0])
     B = len(descs)
-    mc_bytes = B * (4 * nsubcl + 16 * ncl) + 4 * vox
+    mc_bytes = 4 * nsubcl + 16 * ncl + 4 * vox
     conv_flops = 2.0 * taps * vox
     conv_bytes = 4 * vox * 2 + vox // 1        # model read + data read (+ mask folded in the data)
     return dict(mc_deposit=("hbm", mc_bytes), conv_resid=("tensor", conv_flops), conv_bytes=conv_bytes,
