@@ -22,7 +22,8 @@ SYMBOLS = ("bbgpu_ctx_create", "bbgpu_ctx_destroy", "bbgpu_last_error", "bbgpu_v
            "bbgpu_ring_maps_analytic", "bbgpu_convolve", "bbgpu_conv_sparse", "bbgpu_sumsq_residuals",
            "bbgpu_residuals_fracerr", "bbgpu_norm", "bbgpu_eval_upload", "bbgpu_eval_run", "bbgpu_eval_download",
            "bbgpu_eval_batch", "bbgpu_eval_model", "bbgpu_sync", "bbgpu_set_option", "bbgpu_launch_count",
-           "bbgpu_last_run_times", "bbgpu_kernel_name", "bbgpu_transfer_bytes", "bbgpu_sumsq_residuals_noalloc")
+           "bbgpu_last_run_times", "bbgpu_kernel_name", "bbgpu_transfer_bytes", "bbgpu_sumsq_residuals_noalloc",
+           "bbgpu_set_profile", "bbgpu_eval_upload_profile", "bbgpu_eval_profile", "bbgpu_solve_profile")
 
 
 class Grid(C.Structure):
@@ -95,6 +96,10 @@ def load(path=None):
         "bbgpu_kernel_name": (C.c_char_p, [i]),
         "bbgpu_transfer_bytes": (i, [vp, vp, vp]),
         "bbgpu_sumsq_residuals_noalloc": (i, [vp, vp, vp, i, vp, i, i, i, d, d, vp, vp]),
+        "bbgpu_set_profile": (i, [vp, i, i, i, i, i, vp, vp, vp, vp, d, d, d, d]),
+        "bbgpu_eval_upload_profile": (i, [vp, i, vp, vp, vp]),
+        "bbgpu_eval_profile": (i, [vp, vp, vp]),
+        "bbgpu_solve_profile": (i, [vp, vp, vp, i, i, vp, d, d, d, vp, vp]),
     }
     for name, (res, args) in proto.items():
         f = getattr(L, name)

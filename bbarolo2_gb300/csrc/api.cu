@@ -21,9 +21,9 @@
 
 #define BBGPU_VERSION 1
 #define NLAYOUT 4
-#define NTIMER 6
+#define NTIMER 7
 
-static const char *KNAMES[NTIMER] = {"mc_bin", "scan_tiles", "mc_scatter", "mc_deposit", "conv_resid",
+static const char *KNAMES[NTIMER] = {"profile", "mc_bin", "scan_tiles", "mc_scatter", "mc_deposit", "conv_resid",
                                      "reduce_partials"};
 
 struct LayoutEntry {
@@ -91,6 +91,32 @@ struct bbgpu_ctx {
     size_t d_out2_cap = 0;
     int *d_err = nullptr;
     long long mstride = 0;
+    // flux normalisation (bbgpu_set_profile, bbgpu_eval_upload_profile)
+    bool prof_set = false, prof_uploaded = false;
+    ProfBox pbox{};
+    ProfConst pc{};
+    double mapscale = 1.0;
+    int npix_used = 0, nent = 0, nsm = 0;
+    long long pnsamp = 0;
+    int *d_ppix = nullptr, *d_lc = nullptr, *d_ord = nullptr, *d_p0 = nullptr, *d_ent = nullptr;
+    double *d_pw = nullptr, *d_pwy = nullptr, *d_lv = nullptr;
+    unsigned char *d_near = nullptr;
+    AnSub *d_psub = nullptr;
+    size_t d_psub_cap = 0;
+    int *d_psbase = nullptr, *d_pssub = nullptr, *d_pwidx = nullptr, *d_pfix = nullptr, *d_pp = nullptr,
+        *d_pstat = nullptr;
+    size_t d_psbase_cap = 0, d_pssub_cap = 0, d_pwidx_cap = 0, d_pfix_cap = 0, d_pp_cap = 0, d_pstat_cap = 0;
+    double *d_pcs = nullptr, *d_pzq = nullptr, *d_pwval = nullptr, *d_rap = nullptr, *d_gpart = nullptr,
+           *d_gh = nullptr, *d_px = nullptr, *d_ppart = nullptr;
+    size_t d_pcs_cap = 0, d_pzq_cap = 0, d_pwval_cap = 0, d_rap_cap = 0, d_gpart_cap = 0, d_gh_cap = 0,
+           d_px_cap = 0, d_ppart_cap = 0;
+    float *d_pzqf = nullptr, *d_pwqf = nullptr, *d_pwvalf = nullptr, *d_maps32 = nullptr, *d_K = nullptr;
+    size_t d_pzqf_cap = 0, d_pwqf_cap = 0, d_pwvalf_cap = 0, d_maps32_cap = 0, d_K_cap = 0;
+    long long *d_maps64 = nullptr;
+    size_t d_maps64_cap = 0;
+    MemberDev *d_pmem = nullptr;
+    size_t d_pmem_cap = 0;
+    std::vector<MemberDev> pmem_host;
     // options
     bool keep_smoothed = false, timing = false, want64 = false;
     int lean = 0;                 // the batch qualifies for the lean deposit kernel
@@ -356,6 +382,15 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
     cudaFree(ctx->d_tcount); cudaFree(ctx->d_toff); cudaFree(ctx->d_tcur); cudaFree(ctx->d_model); cudaFree(ctx->d_scan);
     cudaFree(ctx->d_smooth); cudaFree(ctx->d_model64); cudaFree(ctx->d_partial); cudaFree(ctx->d_out2);
     cudaFree(ctx->d_err);
+    for (void *q : {(void *)ctx->d_ppix, (void *)ctx->d_lc, (void *)ctx->d_ord, (void *)ctx->d_p0, (void *)ctx->d_ent,
+                    (void *)ctx->d_pw, (void *)ctx->d_pwy, (void *)ctx->d_lv, (void *)ctx->d_near, (void *)ctx->d_psub,
+                    (void *)ctx->d_psbase, (void *)ctx->d_pssub, (void *)ctx->d_pwidx, (void *)ctx->d_pfix,
+                    (void *)ctx->d_pp, (void *)ctx->d_pstat, (void *)ctx->d_pcs, (void *)ctx->d_pzq,
+                    (void *)ctx->d_pwval, (void *)ctx->d_rap, (void *)ctx->d_gpart, (void *)ctx->d_gh,
+                    (void *)ctx->d_px, (void *)ctx->d_ppart, (void *)ctx->d_pzqf, (void *)ctx->d_pwqf,
+                    (void *)ctx->d_pwvalf, (void *)ctx->d_maps32, (void *)ctx->d_K, (void *)ctx->d_maps64,
+                    (void *)ctx->d_pmem})
+        cudaFree(q);
     cudaFreeHost(ctx->h_sub); cudaFreeHost(ctx->h_mem); cudaFreeHost(ctx->h_out2); cudaFreeHost(ctx->h_err);
     for (int i = 0; i <= NTIMER; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
@@ -526,6 +561,7 @@ extern "C" int bbgpu_set_cube(bbgpu_ctx *ctx, const float *data, const uint8_t *
 // ------------------------------------------------------------------------------------------- batches
 static int batch_prepare(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const double *sr, const int64_t *nv,
                          const bbgpu_eval_desc *descs, bool need_cube) {
+    ctx->prof_uploaded = false;       // (a new batch: its ring maps come with bbgpu_eval_upload_profile)
     if (!ctx->grid_set) return fail(ctx, BBGPU_ERR_STATE, "evaluation before set_grid");
     if (need_cube && !ctx->cube_set) return fail(ctx, BBGPU_ERR_STATE, "evaluation before set_cube");
     if (galmodtype != BBGPU_MC) return fail(ctx, BBGPU_ERR_ARG, "galmodtype %d not supported by the batch path", galmodtype);
@@ -619,6 +655,41 @@ static int batch_prepare(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const
     return 0;
 }
 
+// The flux normalisation of the batch (bbarolo/bayesian/likelihood.py:595-596): ring maps, beam convolution,
+// normal equations, the profile solve and the densities of the model's sub-rings, all on the device.
+static int profile_run(bbgpu_ctx *ctx) {
+    const GridDev &g = ctx->g;
+    cudaStream_t s = ctx->stream;
+    const ProfBox &bx = ctx->pbox;
+    const int nb = ctx->nb, n = ctx->pc.n;
+    const long long per = bx.npix * bx.nrp;
+    CK(cudaMemsetAsync(ctx->d_maps64, 0, sizeof(long long) * (size_t)nb * per, s));
+    launch_an_maps_fast(s, g, ctx->d_psub, ctx->nsm, ctx->d_psbase, ctx->d_pssub, ctx->d_pcs, ctx->pnsamp, nb,
+                        ctx->d_pzq, ctx->d_pzqf, ctx->d_pwqf, ctx->d_pwidx, ctx->d_pwvalf, bx, ctx->d_pfix,
+                        ctx->d_maps64);
+    CKL();
+    launch_maps_to_f32(s, ctx->d_maps64, ctx->d_pfix, nb, per, (float)ctx->mapscale, ctx->d_maps32);
+    CKL();
+    if (ctx->kernel_set) {
+        launch_conv_resid(s, g, ctx->d_pmem, ctx->pmem_host.data(), nb, ctx->d_maps32, per, bx.nrp, ctx->d_taps,
+                          ctx->ky, ctx->kx, ctx->kxw, ctx->d_K, 2, 0, ctx->d_ppart);
+        CKL();
+    }
+    const float *K = ctx->kernel_set ? ctx->d_K : ctx->d_maps32;
+    launch_prof_gram(s, K, bx, ctx->d_ppix, ctx->d_pw, ctx->d_pwy, ctx->npix_used, ctx->d_ent, ctx->d_ent + ctx->nent,
+                     ctx->nent, nb, ctx->d_gpart, ctx->d_gh);
+    ctx->launches += 2;
+    CKL();
+    launch_prof_solve(s, ctx->d_gh, ctx->pc, ctx->d_lc, ctx->d_lv, ctx->d_ord, ctx->d_near, ctx->d_p0, nb, ctx->d_px,
+                      ctx->d_pp, ctx->d_pstat);
+    CKL();
+    launch_mc_dens(s, g, ctx->d_sub, ctx->nsub, ctx->d_mem, nb, ctx->d_px, n, ctx->d_pwidx, ctx->d_pwval, ctx->d_rap,
+                   ctx->d_err);
+    CKL();
+    (void)per;
+    return 0;
+}
+
 static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
     if (!ctx->uploaded) return fail(ctx, BBGPU_ERR_STATE, "run before upload");
     const GridDev &g = ctx->g;
@@ -626,23 +697,28 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
     cudaStream_t s = ctx->stream;
     const bool tm = ctx->timing;
     if (tm) CK(cudaEventRecord(ctx->ev[0], s));
+    if (ctx->prof_uploaded) {
+        int rc = profile_run(ctx);
+        if (rc) return rc;
+    }
+    if (tm) CK(cudaEventRecord(ctx->ev[1], s));
     CK(cudaMemsetAsync(ctx->d_tcount, 0, sizeof(int) * (size_t)(ctx->ntile_total * NOWN + 1), s));
     launch_mc_bin(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->nb, ctx->tx, ctx->ty, ctx->d_pix, ctx->d_tcount,
                   ctx->d_err);
     CKL();
-    if (tm) CK(cudaEventRecord(ctx->ev[1], s));
+    if (tm) CK(cudaEventRecord(ctx->ev[2], s));
     launch_scan_tiles(s, ctx->d_tcount, ctx->d_toff, ctx->d_tcur, ctx->ntile_total * NOWN, ctx->d_scan);
     CKL();
-    if (tm) CK(cudaEventRecord(ctx->ev[2], s));
+    if (tm) CK(cudaEventRecord(ctx->ev[3], s));
     launch_mc_scatter(s, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->nb, ctx->tx, ctx->ty, ctx->d_pix, ctx->d_tcur,
                       ctx->d_bucket);
     CKL();
-    if (tm) CK(cudaEventRecord(ctx->ev[3], s));
+    if (tm) CK(cudaEventRecord(ctx->ev[4], s));
     launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->tx, ctx->ty,
                       ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig, ctx->d_cd2if, ctx->d_cd2i,
                       ctx->d_model, ctx->mstride, ctx->want64 ? ctx->d_model64 : nullptr, ctx->d_err, ctx->lean);
     CKL();
-    if (tm) CK(cudaEventRecord(ctx->ev[4], s));
+    if (tm) CK(cudaEventRecord(ctx->ev[5], s));
     const bool conv = ctx->kernel_set;
     if (do_resid || ctx->keep_smoothed) {
         launch_conv_resid(s, g, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->d_model, ctx->mstride, g.nz,
@@ -650,14 +726,14 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
                           conv ? 1 : 0, do_resid ? 1 : 0, ctx->d_partial);
         CKL();
     }
-    if (tm) CK(cudaEventRecord(ctx->ev[5], s));
+    if (tm) CK(cudaEventRecord(ctx->ev[6], s));
     if (do_resid) {
         launch_reduce_partials(s, ctx->d_partial, ctx->npart, ctx->nb, ctx->d_out2);
         CKL();
     }
     if (tm) {
-        CK(cudaEventRecord(ctx->ev[6], s));
-        CK(cudaEventSynchronize(ctx->ev[6]));
+        CK(cudaEventRecord(ctx->ev[7], s));
+        CK(cudaEventSynchronize(ctx->ev[7]));
         for (int i = 0; i < NTIMER; i++) {
             float ms = 0.f;
             cudaEventElapsedTime(&ms, ctx->ev[i], ctx->ev[i + 1]);
@@ -674,6 +750,10 @@ static int check_err(bbgpu_ctx *ctx) {
     if (*ctx->h_err) {
         int e = *ctx->h_err;
         CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+        if (e & ERR_PROFILE_LAYOUT)
+            return fail(ctx, BBGPU_ERR_KERNEL,
+                        "the deconvolved density profile changed the MC cloud layout of a member (a ring density "
+                        "at zero, or above the 10-clouds-per-pixel floor): evaluate that member with its densities");
         return fail(ctx, BBGPU_ERR_KERNEL, "kernel error flag 0x%x (cloud layout inconsistent with the sub-rings)", e);
     }
     return 0;
@@ -1115,5 +1195,257 @@ extern "C" int bbgpu_norm(bbgpu_ctx *ctx, double *model, int bsy, int bsx, int n
     }
     if (nt - nb == 0) *out = INFINITY;
     else *out = pow(1 + (double)nb / (double)nt, bweight) * minfunc / (double)(nt - nb);
+    return BBGPU_OK;
+}
+
+// ------------------------------------------------------------------------------------------- flux normalisation
+static int profile_consts(bbgpu_ctx *ctx, const double *radii, int n, double smooth, double corr, double floor_,
+                          std::vector<int> &ent) {
+    std::vector<int> lc(3 * (n > 2 ? n - 2 : 1)), ord(n);
+    std::vector<double> lv(3 * (n > 2 ? n - 2 : 1));
+    std::vector<unsigned char> nr(n > 2 ? n - 2 : 1);
+    double d = 0.0, norm = 0.0;
+    bbh_profile_consts(radii, n, lc.data(), lv.data(), ord.data(), nr.data(), &d, &norm);
+    ctx->pc.n = n;
+    ctx->pc.smooth = smooth;
+    ctx->pc.corr = corr;
+    ctx->pc.floor_ = floor_;
+    ctx->pc.norm = norm;
+    ctx->pc.d = d;
+    // entries of the packed normal equations: G (i <= j), then h
+    const int ng = n * (n + 1) / 2;
+    ctx->nent = ng + n;
+    ent.assign(2 * ctx->nent, -1);
+    int e = 0;
+    for (int i = 0; i < n; i++)
+        for (int j = i; j < n; j++, e++) {
+            ent[e] = i;
+            ent[ctx->nent + e] = j;
+        }
+    for (int i = 0; i < n; i++, e++) ent[e] = i;
+    std::vector<int> p0(n, 1);
+    cudaFree(ctx->d_lc); cudaFree(ctx->d_lv); cudaFree(ctx->d_ord); cudaFree(ctx->d_near); cudaFree(ctx->d_p0);
+    cudaFree(ctx->d_ent);
+    ctx->d_lc = nullptr; ctx->d_lv = nullptr; ctx->d_ord = nullptr; ctx->d_near = nullptr; ctx->d_p0 = nullptr;
+    ctx->d_ent = nullptr;
+    CK(cudaMalloc(&ctx->d_lc, lc.size() * sizeof(int)));
+    CK(cudaMalloc(&ctx->d_lv, lv.size() * sizeof(double)));
+    CK(cudaMalloc(&ctx->d_ord, ord.size() * sizeof(int)));
+    CK(cudaMalloc(&ctx->d_near, nr.size()));
+    CK(cudaMalloc(&ctx->d_p0, n * sizeof(int)));
+    CK(cudaMalloc(&ctx->d_ent, ent.size() * sizeof(int)));
+    CK(cudaMemcpy(ctx->d_lc, lc.data(), lc.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_lv, lv.data(), lv.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_ord, ord.data(), ord.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_near, nr.data(), nr.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_p0, p0.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_ent, ent.data(), ent.size() * sizeof(int), cudaMemcpyHostToDevice));
+    return 0;
+}
+
+#define PROF_NMAX 64
+
+extern "C" int bbgpu_set_profile(bbgpu_ctx *ctx, int nr, int blo0, int blo1, int bhi0, int bhi1, const double *ymap,
+                                 const double *rms, const uint8_t *ok, const double *radii, double smooth,
+                                 double corr, double floor_, double mapscale) {
+    if (!ctx) return BBGPU_ERR_ARG;
+    if (!ctx->grid_set) return fail(ctx, BBGPU_ERR_STATE, "set_profile before set_grid");
+    const GridDev &g = ctx->g;
+    const int n = nr + 1;
+    if (!ymap || !rms || !ok || !radii || nr < 1 || n > PROF_NMAX || blo0 < 0 || blo1 < 0 || bhi0 > g.nx ||
+        bhi1 > g.ny || bhi0 <= blo0 || bhi1 <= blo1)
+        return fail(ctx, BBGPU_ERR_ARG, "set_profile: invalid arguments (1 to %d rings, a box inside the cube)",
+                    PROF_NMAX - 1);
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ProfBox &b = ctx->pbox;
+    b.blo0 = blo0; b.blo1 = blo1; b.bhi0 = bhi0; b.bhi1 = bhi1;
+    b.bx = bhi0 - blo0; b.by = bhi1 - blo1; b.nrp = n;
+    b.npix = (long long)b.bx * b.by;
+    // the pixels used (bbarolo/profile.py:76-79): in the region, rms > 0, finite data
+    std::vector<int> pix;
+    std::vector<double> w, wy;
+    double bb = 0.0;
+    for (long long p = 0; p < b.npix; p++) {
+        const double sg = rms[p], y = ymap[p];
+        if (!ok[p] || !(sg > 0) || !std::isfinite(y)) continue;
+        pix.push_back((int)p);
+        w.push_back(1.0 / (sg * sg));
+        wy.push_back(y / (sg * sg));
+        const double bv = y / sg;
+        bb += bv * bv;
+    }
+    ctx->npix_used = (int)pix.size();
+    ctx->pc.m = (int)pix.size();
+    ctx->pc.bb = bb;
+    ctx->mapscale = mapscale;
+    cudaFree(ctx->d_ppix); cudaFree(ctx->d_pw); cudaFree(ctx->d_pwy);
+    ctx->d_ppix = nullptr; ctx->d_pw = nullptr; ctx->d_pwy = nullptr;
+    const size_t np1 = pix.size() ? pix.size() : 1;
+    CK(cudaMalloc(&ctx->d_ppix, np1 * sizeof(int)));
+    CK(cudaMalloc(&ctx->d_pw, np1 * sizeof(double)));
+    CK(cudaMalloc(&ctx->d_pwy, np1 * sizeof(double)));
+    if (pix.size()) {
+        CK(cudaMemcpy(ctx->d_ppix, pix.data(), pix.size() * sizeof(int), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(ctx->d_pw, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(ctx->d_pwy, wy.data(), wy.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    std::vector<int> ent;
+    int rc = profile_consts(ctx, radii, n, smooth, corr, floor_, ent);
+    if (rc) return rc;
+    ctx->prof_set = true;
+    ctx->prof_uploaded = false;
+    return BBGPU_OK;
+}
+
+extern "C" int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *sr_maps, const int64_t *widx,
+                                         const double *wval) {
+    if (!ctx) return BBGPU_ERR_ARG;
+    if (!ctx->prof_set) return fail(ctx, BBGPU_ERR_STATE, "eval_upload_profile before set_profile");
+    if (!ctx->uploaded || ctx->galmodtype != BBGPU_MC)
+        return fail(ctx, BBGPU_ERR_STATE, "eval_upload_profile before eval_upload of an MC batch");
+    const int nb = ctx->nb, nsub = ctx->nsub, n = ctx->pc.n;
+    if (!sr_maps || !widx || !wval || nsm < nsub) return fail(ctx, BBGPU_ERR_ARG, "eval_upload_profile: invalid arguments");
+    for (int i = 0; i < 2 * nsm; i++)
+        if (widx[i] >= n) return fail(ctx, BBGPU_ERR_ARG, "eval_upload_profile: ring index %lld >= %d", (long long)widx[i], n);
+    const GridDev &g = ctx->g;
+    CK(cudaSetDevice(ctx->device));
+    // the sub-ring radii are shared by the batch (one table of azimuthal samples)
+    for (int k = 1; k < nb; k++)
+        if (memcmp(sr_maps + (size_t)k * BBGPU_NSR * nsm, sr_maps, sizeof(double) * nsm))
+            return fail(ctx, BBGPU_ERR_ARG, "eval_upload_profile: member %d has other sub-ring radii", k);
+    bool thick = false;
+    for (int k = 0; k < nb && !thick; k++)
+        for (int i = 0; i < nsm; i++)
+            if (sr_maps[(size_t)k * BBGPU_NSR * nsm + 6 * (size_t)nsm + i] > 0) { thick = true; break; }
+    const int nzq = thick ? 1024 : 1;
+    const ProfBox &bx = ctx->pbox;
+    std::vector<AnSub> subs((size_t)nb * nsm);
+    std::vector<double> zq, wq;
+    std::vector<int> fix(nb);
+    for (int k = 0; k < nb; k++) {
+        const int e = bbh_an_subs(sr_maps + (size_t)k * BBGPU_NSR * nsm, nsm, &g, nzq, bx.blo0, bx.blo1, bx.bhi0,
+                                  bx.bhi1, ctx->h_cd2i.data(), 1, widx, wval, subs.data() + (size_t)k * nsm, zq, wq);
+        if (e == -10000) return fail(ctx, BBGPU_ERR_ARG, "eval_upload_profile: member %d: weights not finite", k);
+        fix[k] = std::min(e, 100);
+    }
+    std::vector<int> sbase, ssub;
+    std::vector<double> cs;
+    bbh_an_samples(sr_maps, nsm, &g, sbase, ssub, cs);
+    ctx->pnsamp = sbase[nsm];
+    std::vector<float> zqf(zq.size() ? zq.size() : 1), wqf(wq.size() ? wq.size() : 1), wvalf(2 * (size_t)nsm);
+    for (size_t i = 0; i < zq.size(); i++) { zqf[i] = (float)zq[i]; wqf[i] = (float)wq[i]; }
+    std::vector<int> wi(2 * (size_t)nsm);
+    for (int i = 0; i < 2 * nsm; i++) { wvalf[i] = (float)wval[i]; wi[i] = (int)widx[i]; }
+    // ring area of each model sub-ring (bbarolo/galmod.py:107), for the densities of the MC model
+    std::vector<double> rap(nsub ? nsub : 1);
+    for (int i = 0; i < nsub; i++) rap[i] = 2 * M_PI * sr_maps[i] * g.radsep / g.pixarea;
+    const long long per = bx.npix * bx.nrp;
+    int rc;
+    if ((rc = dgrow(ctx, &ctx->d_psub, &ctx->d_psub_cap, subs.size()))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_psbase, &ctx->d_psbase_cap, sbase.size()))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_pssub, &ctx->d_pssub_cap, ssub.size()))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_pcs, &ctx->d_pcs_cap, cs.size()))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_pzq, &ctx->d_pzq_cap, zq.size() + 1))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_pzqf, &ctx->d_pzqf_cap, zqf.size()))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_pwqf, &ctx->d_pwqf_cap, wqf.size()))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_pwidx, &ctx->d_pwidx_cap, wi.size()))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_pwvalf, &ctx->d_pwvalf_cap, wvalf.size()))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_pwval, &ctx->d_pwval_cap, 2 * (size_t)nsm))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_rap, &ctx->d_rap_cap, rap.size()))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_pfix, &ctx->d_pfix_cap, (size_t)nb))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_maps64, &ctx->d_maps64_cap, (size_t)nb * per))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_maps32, &ctx->d_maps32_cap, (size_t)nb * per))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_K, &ctx->d_K_cap, (size_t)nb * per))) return rc;
+    const int nt = prof_gram_tiles(ctx->npix_used);
+    if ((rc = dgrow(ctx, &ctx->d_gpart, &ctx->d_gpart_cap, (size_t)nb * (nt ? nt : 1) * ctx->nent))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_gh, &ctx->d_gh_cap, (size_t)nb * ctx->nent))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_px, &ctx->d_px_cap, (size_t)nb * n))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_pp, &ctx->d_pp_cap, (size_t)nb * n))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_pstat, &ctx->d_pstat_cap, (size_t)nb))) return rc;
+    // the maps' convolution: one member descriptor per member, the likelihood box
+    ctx->pmem_host.assign(nb, MemberDev{});
+    for (auto &M : ctx->pmem_host) {
+        M.blo0 = bx.blo0; M.blo1 = bx.blo1; M.bhi0 = bx.bhi0; M.bhi1 = bx.bhi1; M.bx = bx.bx; M.by = bx.by;
+    }
+    const int npart = conv_resid_npart(ctx->pmem_host.data(), nb, bx.nrp);
+    if ((rc = dgrow(ctx, &ctx->d_pmem, &ctx->d_pmem_cap, (size_t)nb))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_ppart, &ctx->d_ppart_cap, (size_t)2 * nb * (npart ? npart : 1)))) return rc;
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(ctx->d_psub, subs.data(), sizeof(AnSub) * subs.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->d_psbase, sbase.data(), sizeof(int) * sbase.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->d_pssub, ssub.data(), sizeof(int) * ssub.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->d_pcs, cs.data(), sizeof(double) * cs.size(), cudaMemcpyHostToDevice, s));
+    if (zq.size()) CK(cudaMemcpyAsync(ctx->d_pzq, zq.data(), sizeof(double) * zq.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->d_pzqf, zqf.data(), sizeof(float) * zqf.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->d_pwqf, wqf.data(), sizeof(float) * wqf.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->d_pwidx, wi.data(), sizeof(int) * wi.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->d_pwvalf, wvalf.data(), sizeof(float) * wvalf.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->d_pwval, wval, sizeof(double) * 2 * (size_t)nsm, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->d_rap, rap.data(), sizeof(double) * rap.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->d_pfix, fix.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->d_pmem, ctx->pmem_host.data(), sizeof(MemberDev) * nb, cudaMemcpyHostToDevice, s));
+    ctx->h2d += (long long)(sizeof(AnSub) * subs.size() + sizeof(double) * (cs.size() + zq.size()) +
+                            sizeof(float) * (zqf.size() + wqf.size()));
+    // (the host vectors go out of scope: finish the copies first)
+    CK(cudaStreamSynchronize(s));
+    ctx->nsm = nsm;
+    ctx->prof_uploaded = true;
+    ctx->ran = false;
+    return BBGPU_OK;
+}
+
+extern "C" int bbgpu_eval_profile(bbgpu_ctx *ctx, double *x, int *status) {
+    if (!ctx || !x) return BBGPU_ERR_ARG;
+    if (!ctx->ran || !ctx->prof_uploaded) return fail(ctx, BBGPU_ERR_STATE, "eval_profile: no profile computed");
+    CK(cudaSetDevice(ctx->device));
+    const int nb = ctx->nb, n = ctx->pc.n;
+    CK(cudaMemcpyAsync(x, ctx->d_px, sizeof(double) * (size_t)nb * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (status) CK(cudaMemcpyAsync(status, ctx->d_pstat, sizeof(int) * nb, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return BBGPU_OK;
+}
+
+extern "C" int bbgpu_solve_profile(bbgpu_ctx *ctx, const double *A, const double *b, int m, int n, const double *radii,
+                                   double smooth, double corr, double floor_, double *x, int *status) {
+    if (!ctx) return BBGPU_ERR_ARG;
+    if (!A || !b || !radii || !x || m < 1 || n < 1 || n > PROF_NMAX)
+        return fail(ctx, BBGPU_ERR_ARG, "solve_profile: invalid arguments (1 to %d unknowns)", PROF_NMAX);
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    // (the profile constants of the batch path are replaced)
+    ctx->prof_set = false;
+    ctx->prof_uploaded = false;
+    std::vector<int> ent;
+    int rc = profile_consts(ctx, radii, n, smooth, corr, floor_, ent);
+    if (rc) return rc;
+    double bb = 0.0;
+    for (int i = 0; i < m; i++) bb += b[i] * b[i];
+    ctx->pc.m = m;
+    ctx->pc.bb = bb;
+    ProfBox bx{};
+    bx.nrp = n;
+    bx.npix = m;
+    DevBufs B;
+    double *dA = nullptr, *db = nullptr, *dpart = nullptr, *dgh = nullptr, *dx = nullptr;
+    int *dpp = nullptr, *dst = nullptr;
+    const int nt = prof_gram_tiles(m);
+    if (!B.get(&dA, sizeof(double) * (size_t)m * n) || !B.get(&db, sizeof(double) * m) ||
+        !B.get(&dpart, sizeof(double) * (size_t)nt * ctx->nent) || !B.get(&dgh, sizeof(double) * ctx->nent) ||
+        !B.get(&dx, sizeof(double) * n) || !B.get(&dpp, sizeof(int) * n) || !B.get(&dst, sizeof(int)))
+        return fail(ctx, BBGPU_ERR_NOMEM, "solve_profile: allocation failed");
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(dA, A, sizeof(double) * (size_t)m * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(db, b, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+    launch_prof_gram64(s, dA, bx, db, m, ctx->d_ent, ctx->d_ent + ctx->nent, ctx->nent, dpart, dgh);
+    ctx->launches += 2;
+    CKL();
+    launch_prof_solve(s, dgh, ctx->pc, ctx->d_lc, ctx->d_lv, ctx->d_ord, ctx->d_near, ctx->d_p0, 1, dx, dpp, dst);
+    CKL();
+    int st = 0;
+    CK(cudaMemcpyAsync(x, dx, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&st, dst, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (status) *status = st;
     return BBGPU_OK;
 }

@@ -491,6 +491,20 @@ int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0,
             const double u = (kr + 0.5) / nrad;
             S.R[kr] = sqrt(r_inner * r_inner + 2.0 * g->radsep * R0 * u);
         }
+        S.P1 = (float)(S.spa / g->cdelt0);
+        S.P2 = (float)(S.cinc * S.cpa / g->cdelt0);
+        S.P3 = (float)(S.sinc * S.cpa / g->cdelt0);
+        S.Q1 = (float)(S.cpa / g->cdelt1);
+        S.Q2 = (float)(S.cinc * S.spa / g->cdelt1);
+        S.Q3 = (float)(-S.sinc * S.spa / g->cdelt1);
+        S.xposf = (float)S.xpos;
+        S.yposf = (float)S.ypos;
+        S.z0f = (float)S.z0;
+        S.fluxscf = (float)S.fluxsc;
+        S.wrecf = (float)S.wrec;
+        S.wappf = (float)S.wapp;
+        S.Rf[0] = (float)S.R[0];
+        S.Rf[1] = (float)S.R[1];
         if (!S.active) continue;
         // every deposit of the sub-ring is at most |fluxsc| x |wside| x (line: sum of relint x max cd2i; map:
         // max wval) per sample, the vertical weights and the channel profile summing to at most 1
@@ -505,4 +519,64 @@ int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0,
     int ex = 0;
     frexp(bound * 1.01, &ex);       // bound * 1.01 < 2^ex
     return std::min(62 - ex, 1000);
+}
+
+// ------------------------------------------------------------------------------------------- profile prior
+// The second differences of the profile at the radii R (n: the rings then the exterior annulus), as
+// bbarolo/profile.py:60-85 and :141-151: for row i (0 .. n-3) the columns lc[3i..3i+2] and weights lv[3i..3i+2];
+// ord the order of the radii; near[i] when the radii around row i are closer than a quarter of the median ring
+// distance d (bbarolo/profile.py:134-136); norm the sum of the squared weights of the relative prior.
+static void second_differences(double d1, double d2, double *w) {
+    w[0] = (1. / d1) * 2. / (d1 + d2);
+    w[1] = (-1. / d1 - 1. / d2) * 2. / (d1 + d2);
+    w[2] = (1. / d2) * 2. / (d1 + d2);
+}
+
+void bbh_profile_consts(const double *R, int n, int *lc, double *lv, int *ord, unsigned char *near, double *d,
+                        double *norm) {
+    std::vector<int> o(n);
+    for (int i = 0; i < n; i++) o[i] = i;
+    std::stable_sort(o.begin(), o.end(), [&](int a, int b) { return R[a] < R[b]; });
+    std::vector<double> Rs(n);
+    for (int i = 0; i < n; i++) {
+        Rs[i] = R[o[i]];
+        ord[i] = o[i];
+    }
+    double mx = R[0], mn = R[0];
+    for (int i = 1; i < n; i++) {
+        mx = std::max(mx, R[i]);
+        mn = std::min(mn, R[i]);
+    }
+    const double tiny = 1e-6 * std::max(mx - mn, 1e-300);
+    // the distances between the rings (all but the last radius), sorted
+    std::vector<double> rr(R, R + (n > 1 ? n - 1 : 0));
+    std::sort(rr.begin(), rr.end());
+    std::vector<double> dr;
+    for (size_t i = 1; i < rr.size(); i++) dr.push_back(rr[i] - rr[i - 1]);
+    double dmin = tiny;
+    if (n > 2 && !dr.empty()) dmin = std::max(0.25 * *std::min_element(dr.begin(), dr.end()), tiny);
+    double med = 0.0;
+    if (!dr.empty()) {
+        std::vector<double> s = dr;
+        std::sort(s.begin(), s.end());
+        const size_t m = s.size();
+        med = m % 2 ? s[m / 2] : (s[m / 2 - 1] + s[m / 2]) / 2.0;
+    }
+    *d = med;
+    double nrm = 0.0;
+    for (int i = 1; i < n - 1; i++) {
+        const double d1 = std::max(Rs[i] - Rs[i - 1], tiny), d2 = std::max(Rs[i + 1] - Rs[i], tiny);
+        double w[3];
+        second_differences(d1, d2, w);
+        for (int a = 0; a < 3; a++) {
+            lc[3 * (i - 1) + a] = o[i - 1 + a];
+            lv[3 * (i - 1) + a] = w[a];
+        }
+        double wr[3];
+        second_differences(std::max(d1, dmin), std::max(d2, dmin), wr);
+        nrm += (wr[0] * wr[0] + wr[1] * wr[1]) + wr[2] * wr[2];
+        const double dl = Rs[i] - Rs[i - 1], dh = Rs[i + 1] - Rs[i];
+        near[i - 1] = std::min(dl, dh) < 0.25 * med;
+    }
+    *norm = nrm;
 }

@@ -36,6 +36,11 @@ struct AnSub {
     double a[BBGPU_MAXL];           // relint[nl] * fluxsc (times wside at deposit)
     long long K;                    // half-width of the line profile in channels
     int naz, nzz, zq_off, zdep, active, sub;
+    // float32 fast path of the pixels (ring maps of the flux normalisation; error bounded in the kernel):
+    // x pixel = xposf + (R caz P1 - R saz P2) + z P3, y pixel = yposf + (R caz Q1 + R saz Q2) + z Q3
+    float P1, P2, P3, Q1, Q2, Q3, xposf, yposf, z0f, fluxscf, wrecf, wappf;
+    float Rf[2];
+    float pad_f[2];
 };
 
 // The constants of a context, as the kernels see them.
@@ -97,6 +102,11 @@ void bbh_an_samples(const double *R0, int nsub, const GridDev *g, std::vector<in
 int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0, int blo1, int bhi0, int bhi1,
                 const double *cd2i, int maps, const int64_t *widx, const double *wval, AnSub *out,
                 std::vector<double> &zq, std::vector<double> &wq);
+// The second-difference prior of the deconvolved profile at the radii R (n) (bbarolo/profile.py:60-151):
+// rows (n - 2) x 3 columns lc and weights lv, the order of the radii, the "near" rows, the median ring
+// distance d and the norm of the relative prior
+void bbh_profile_consts(const double *R, int n, int *lc, double *lv, int *ord, unsigned char *near, double *d,
+                        double *norm);
 // The pixels of a ring for the CLASSIC residual (bbarolo/galfit.py:62-93): inside flags and weights (bsy, bsx)
 void bbh_norm_footprint(int bsy, int bsx, double x0, double y0, double phi, double inc, double r1, double r2,
                         double wpow, int side, int foot, double hmax, uint8_t *inside, double *wmap);

@@ -113,3 +113,36 @@ void launch_an_maps(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsu
                     const double *wval, const MemberDev &M, long long *maps64);
 void launch_fix_to_model(cudaStream_t s, const long long *in, const MemberDev *mem, int nb, long long mstride, int nz,
                          float *model, double *model64);
+
+// ---- flux normalisation (profile.cu)
+#define ERR_PROFILE_LAYOUT 4      // a deconvolved density changed the MC cloud layout of a member
+// the likelihood box of the ring maps: (by, bx) pixels x nrp maps, ring fastest
+struct ProfBox {
+    int blo0, blo1, bhi0, bhi1, bx, by, nrp, pad;
+    long long npix;
+};
+// the constants of solve_profile shared by a batch
+struct ProfConst {
+    int n, m;                     // unknowns (rings + exterior annulus), pixels used
+    double bb;                    // b.b
+    double smooth, corr, floor_, norm, d;
+};
+void launch_an_maps_fast(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase,
+                         const int *ssub, const double *cs, long long nsamp, int nb, const double *zq,
+                         const float *zqf, const float *wqf, const int *widx, const float *wvalf, const ProfBox &box,
+                         const int *fix_exp, long long *maps64);
+void launch_maps_to_f32(cudaStream_t s, const long long *in, const int *fix_exp, int nb, long long per_member,
+                        float scale, float *out);
+int prof_gram_tiles(int npix_used);
+void launch_prof_gram(cudaStream_t s, const float *K, const ProfBox &box, const int *pix, const double *wpix,
+                      const double *wy, int npix_used, const int *ent_i, const int *ent_j, int nent, int nb,
+                      double *part, double *gh);
+// one system A (m, n) row-major (box.nrp = n, box.npix = m), b (m): packed G = A^T A, h = A^T b
+void launch_prof_gram64(cudaStream_t s, const double *A, const ProfBox &box, const double *b, int m, const int *ent_i,
+                        const int *ent_j, int nent, double *part, double *gh);
+size_t prof_solve_smem(int n);
+void launch_prof_solve(cudaStream_t s, const double *gh, const ProfConst &pc, const int *lc, const double *lv,
+                       const int *ord, const unsigned char *near, const int *p0, int nb, double *x, int *pout,
+                       int *status);
+void launch_mc_dens(cudaStream_t s, const GridDev &g, SubMC *sub, int nsub, MemberDev *mem, int nb, const double *x,
+                    int nx, const int *widx, const double *wval, const double *rap, int *err);

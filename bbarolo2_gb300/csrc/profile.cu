@@ -1,0 +1,644 @@
+// The flux normalisation of the batched likelihood on the device: the deconvolved density profile of
+// Bayesian3DFIT (bbarolo/bayesian/density.py:39-88, bbarolo/profile.py:33-138) for every member of a batch.
+//
+//   k_an_maps_fast   the total-intensity map of each ring with unit density (the ANALYTIC samples of
+//                    _ring_maps_analytic, bbarolo/galmod.py:468-536), one warp per (member, azimuth sample),
+//                    lanes over heights: pixels in float32 with a rounding bound (float64 near a boundary, so
+//                    every sample lands on the reference's pixel), run weights in float32, 64-bit fixed-point
+//                    sums (deterministic); maps (member, pixel, ring) ring-fastest in the likelihood box;
+//   k_maps_to_f32    x mean(cd2i) sum(relint) x scale factor, float32 (then the beam convolution of
+//                    k_conv_resid with the rings as channels);
+//   k_prof_gram      the normal equations of the weighted least squares: G = A^T A, h = A^T b over the pixels
+//                    used (A = maps / rms), exact float64 products of the float32 maps, fixed-order sums;
+//   k_prof_solve     one CTA per member: solve_profile's two non-negative least-squares solves with the
+//                    smoothness prior, Lawson-Hanson on the normal equations (Cholesky of the passive set),
+//                    warm-started from a passive set;
+//   k_mc_dens        the densities of the model's sub-rings (ring weights) into the MC sub-ring constants
+//                    (flux per sub-cloud, fixed-point deposits and exponent), checking the cloud layout.
+//
+// The maps need float32 accuracy only: the system is well conditioned (cond(A) ~ 1e2 on the 160x160x128
+// workload) and float32 map errors move the densities by ~1e-8; the Gram matrix squares the condition number
+// and is therefore accumulated in float64.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "devmath.cuh"
+#include "kernels.h"
+
+#define FULL 0xffffffffu
+#define MW_WPB 8            // warps per CTA of k_an_maps_fast
+#define EPS_REL 3.814697265625e-06f
+#define GRAM_TP 128         // pixels per CTA of k_prof_gram
+
+namespace {
+
+__device__ __forceinline__ bool round_fast(float v, float eps, int &out) {
+    if (!(fabsf(v) < 1.0e6f)) return false;
+    const float f = v + 0.5f;
+    const float fl = floorf(f);
+    const float d = f - fl;
+    if (d < eps || d > 1.0f - eps) return false;
+    out = (int)fl;
+    return true;
+}
+
+__device__ __forceinline__ int clamp_pix(long long v) {
+    return v < -(1LL << 30) ? -(1 << 30) : (v > (1LL << 30) ? (1 << 30) : (int)v);
+}
+
+// ------------------------------------------------------------------------------------------- ring maps
+__global__ void __launch_bounds__(MW_WPB * 32) k_an_maps_fast(GridDev g, const AnSub *__restrict__ subs, int nsub,
+                                                              const int *__restrict__ sbase,
+                                                              const int *__restrict__ ssub,
+                                                              const double2 *__restrict__ cs, long long nsamp,
+                                                              int nb, const double *__restrict__ zq,
+                                                              const float *__restrict__ zqf,
+                                                              const float *__restrict__ wqf,
+                                                              const int *__restrict__ widx,
+                                                              const float *__restrict__ wvalf,
+                                                              ProfBox box, const int *__restrict__ fix_exp,
+                                                              unsigned long long *__restrict__ maps64) {
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long gs = (long long)blockIdx.x * MW_WPB + w;
+    if (gs >= nsamp * nb) return;
+    const int k = (int)(gs / nsamp);
+    const long long s = gs - (long long)k * nsamp;
+    const int ir = ssub[s];
+    const AnSub &S = subs[(size_t)k * nsub + ir];
+    if (!S.active) return;
+    const int kr = (int)(s - sbase[ir]) >= S.naz ? 1 : 0;
+    const double2 c = cs[s];
+    const double wside = c.x >= 0.0 ? S.wrec : S.wapp;
+    if (wside == 0.0) return;
+    const float wsidef = c.x >= 0.0 ? S.wrecf : S.wappf;
+    const float Rf = S.Rf[kr];
+    const float a1 = Rf * (float)c.x, a2 = Rf * (float)c.y;
+    const float t1 = a1 * S.P1, t2 = a2 * S.P2, u1 = a1 * S.Q1, u2 = a2 * S.Q2;
+    const float bxf = S.xposf + (t1 - t2), byf = S.yposf + (u1 + u2);
+    const int nzz = S.nzz;
+    const int e = fix_exp[k];
+    const int i0 = widx[2 * ir], i1 = widx[2 * ir + 1];
+    const float v0 = i0 >= 0 ? S.fluxscf * wvalf[2 * ir] * wsidef : 0.f;
+    const float v1 = i1 >= 0 ? S.fluxscf * wvalf[2 * ir + 1] * wsidef : 0.f;
+    unsigned long long *out = maps64 + (size_t)k * box.npix * box.nrp;
+    // the run carried over from the previous chunk of heights
+    int cg0 = 0, cg1 = 0;
+    float cws = 0.f;
+    bool copen = false;
+    for (int base = 0; base < nzz; base += 32) {
+        const int cnt = min(32, nzz - base);
+        const bool valid = lane < cnt;
+        int g0 = 0, g1 = 0;
+        float wv = 0.f;
+        if (valid) {
+            const int kz = S.zq_off + base + lane;
+            const float zf = nzz > 1 ? zqf[kz] * S.z0f : 0.f;
+            const float t3 = zf * S.P3, u3 = zf * S.Q3;
+            const float gx = bxf + t3, gy = byf + u3;
+            const float ex = (fabsf(S.xposf) + fabsf(t1) + fabsf(t2) + fabsf(t3) + 1.0f) * EPS_REL;
+            const float ey = (fabsf(S.yposf) + fabsf(u1) + fabsf(u2) + fabsf(u3) + 1.0f) * EPS_REL;
+            if (!(round_fast(gx, ex, g0) && round_fast(gy, ey, g1))) {
+                // bbarolo/galmod.py:514-517 in the reference's float64 operations
+                const double R = S.R[kr];
+                const double x = __dmul_rn(R, c.x);
+                const double yb = __dmul_rn(__dmul_rn(R, c.y), S.cinc);
+                const double z = nzz > 1 ? __dmul_rn(zq[kz], S.z0) : 0.0;
+                const double y = __dsub_rn(yb, __dmul_rn(z, S.sinc));
+                g0 = clamp_pix(lround_ref(__dadd_rn(S.xpos, __ddiv_rn(__dsub_rn(__dmul_rn(x, S.spa), __dmul_rn(y, S.cpa)),
+                                                                      g.cdelt0))));
+                g1 = clamp_pix(lround_ref(__dadd_rn(S.ypos, __ddiv_rn(__dadd_rn(__dmul_rn(x, S.cpa), __dmul_rn(y, S.spa)),
+                                                                      g.cdelt1))));
+            }
+            wv = wqf[kz];
+        }
+        // runs of equal pixels: heads, then a segmented inclusive sum of the weights (fixed tree)
+        const int pg0 = __shfl_up_sync(FULL, g0, 1), pg1 = __shfl_up_sync(FULL, g1, 1);
+        bool head = lane == 0 ? !(copen && g0 == cg0 && g1 == cg1) : (g0 != pg0 || g1 != pg1);
+        if (lane == 0 && !head) wv += cws;
+        float v = wv;
+        bool f = head || lane == 0;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const float ov = __shfl_up_sync(FULL, v, d);
+            const bool of = __shfl_up_sync(FULL, f, d);
+            if (lane >= d && !f) {
+                v += ov;
+                f = of;
+            }
+        }
+        const bool nhead = __shfl_down_sync(FULL, head ? 1 : 0, 1) != 0;
+        const bool last_chunk = base + 32 >= nzz;
+        const bool run_end = valid && (lane == cnt - 1 ? last_chunk : nhead);
+        if (run_end && g0 >= box.blo0 && g0 < box.bhi0 && g1 >= box.blo1 && g1 < box.bhi1) {
+            unsigned long long *o = out + ((size_t)(g1 - box.blo1) * box.bx + (size_t)(g0 - box.blo0)) * box.nrp;
+            if (i0 >= 0) {
+                const long long q = __float2ll_rn(ldexpf(v0 * v, e));
+                if (q) atomicAdd(o + i0, (unsigned long long)q);
+            }
+            if (i1 >= 0) {
+                const long long q = __float2ll_rn(ldexpf(v1 * v, e));
+                if (q) atomicAdd(o + i1, (unsigned long long)q);
+            }
+        }
+        // carry the last run of the chunk
+        cg0 = __shfl_sync(FULL, g0, cnt - 1);
+        cg1 = __shfl_sync(FULL, g1, cnt - 1);
+        cws = __shfl_sync(FULL, v, cnt - 1);
+        copen = true;
+    }
+}
+
+// maps (member, pixel, ring) int64 units 2^-e -> float32 x scale
+__global__ void k_maps_to_f32(const long long *__restrict__ in, const int *__restrict__ fix_exp, long long per_member,
+                              float scale, float *__restrict__ out) {
+    const int k = blockIdx.y;
+    const float sc = ldexpf(scale, -fix_exp[k]);
+    const long long *src = in + (size_t)k * per_member;
+    float *dst = out + (size_t)k * per_member;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < per_member;
+         i += (long long)gridDim.x * blockDim.x)
+        dst[i] = (float)src[i] * sc;
+}
+
+// ------------------------------------------------------------------------------------------- Gram matrix
+// CTA (tile of GRAM_TP used pixels, member k). Entry e < n(n+1)/2: G[i][j] (i <= j, row-major packed upper),
+// then h[i]. Partial sums per tile, summed over the tiles in order by k_prof_gram_reduce. pix == nullptr: the
+// pixels 0 .. npix_used - 1; wpix == nullptr: unit weights.
+template <class T>
+__global__ void __launch_bounds__(256) k_prof_gram(const T *__restrict__ K, ProfBox box, const int *__restrict__ pix,
+                                                   const double *__restrict__ wpix, const double *__restrict__ wy,
+                                                   int npix_used, const int *__restrict__ ent_i,
+                                                   const int *__restrict__ ent_j, int nent,
+                                                   double *__restrict__ part) {
+    extern __shared__ double gsm[];
+    const int n = box.nrp;
+    double *ws = gsm;                                       // GRAM_TP weights, GRAM_TP weighted data
+    double *wys = ws + GRAM_TP;
+    T *Ks = (T *)(wys + GRAM_TP);                           // GRAM_TP x n
+    const int k = blockIdx.y, t = blockIdx.x;
+    const int p0 = t * GRAM_TP;
+    const int np = min(GRAM_TP, npix_used - p0);
+    const T *Kk = K + (size_t)k * box.npix * n;
+    for (int i = threadIdx.x; i < np * n; i += blockDim.x) {
+        const int pp = i / n, r = i - pp * n;
+        const long long q = pix ? pix[p0 + pp] : p0 + pp;
+        Ks[i] = Kk[(size_t)q * n + r];
+    }
+    for (int i = threadIdx.x; i < np; i += blockDim.x) {
+        ws[i] = wpix ? wpix[p0 + i] : 1.0;
+        wys[i] = wy[p0 + i];
+    }
+    __syncthreads();
+    double *out = part + ((size_t)k * gridDim.x + t) * nent;
+    for (int e = threadIdx.x; e < nent; e += blockDim.x) {
+        const int i = ent_i[e], j = ent_j[e];
+        double acc = 0.0;
+        if (j >= 0) {
+            for (int pp = 0; pp < np; pp++) {
+                const T a = Ks[pp * n + i], b = Ks[pp * n + j];
+                if (a != T(0) && b != T(0)) acc = fma(ws[pp], (double)a * (double)b, acc);
+            }
+        } else {
+            for (int pp = 0; pp < np; pp++) {
+                const T a = Ks[pp * n + i];
+                if (a != T(0)) acc = fma(wys[pp], (double)a, acc);
+            }
+        }
+        out[e] = acc;
+    }
+}
+
+__global__ void k_prof_gram_reduce(const double *__restrict__ part, int ntile, int nent, double *__restrict__ gh) {
+    const int k = blockIdx.y;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nent) return;
+    double acc = 0.0;
+    for (int t = 0; t < ntile; t++) acc += part[((size_t)k * ntile + t) * nent + e];
+    gh[(size_t)k * nent + e] = acc;
+}
+
+// ------------------------------------------------------------------------------------------- NNLS
+// Shared state of one member's solve (one CTA, PS_THREADS threads).
+#define PS_THREADS 128
+
+struct Solver {
+    int n;
+    double *H;      // n x n (the normal matrix of the current system)
+    double *F;      // factor of the passive block, n x n
+    double *g;      // right-hand side
+    double *x, *z, *w;
+    int *P, *idx;   // passive flags, passive indices
+    int *blocked;
+    int *sflag;     // shared scalars
+    double *sval;
+};
+
+// Cholesky of H[P,P] into F and solve F F^T z_P = g_P; false if the block is not positive definite.
+__device__ bool chol_solve(Solver &S, int p) {
+    const int tid = threadIdx.x;
+    const int n = S.n;
+    for (int e = tid; e < p * p; e += blockDim.x) {
+        const int a = e / p, b = e - a * p;
+        S.F[a * n + b] = S.H[S.idx[a] * n + S.idx[b]];
+    }
+    if (tid == 0) S.sflag[0] = 1;
+    __syncthreads();
+    for (int c = 0; c < p; c++) {
+        if (tid == 0) {
+            const double d = S.F[c * n + c];
+            if (!(d > 0.0)) S.sflag[0] = 0;
+            S.F[c * n + c] = d > 0.0 ? sqrt(d) : 1.0;
+        }
+        __syncthreads();
+        const double dc = S.F[c * n + c];
+        for (int r = c + 1 + tid; r < p; r += blockDim.x) S.F[r * n + c] /= dc;
+        __syncthreads();
+        const int m = p - c - 1;
+        for (int e = tid; e < m * m; e += blockDim.x) {
+            const int r = c + 1 + e / m, q = c + 1 + e % m;
+            if (q <= r) S.F[r * n + q] -= S.F[r * n + c] * S.F[q * n + c];
+        }
+        __syncthreads();
+    }
+    const bool ok = S.sflag[0] != 0;
+    // forward then back substitution (one warp; lanes over the dot products)
+    if (tid < 32) {
+        for (int r = 0; r < p; r++) {
+            double acc = 0.0;
+            for (int q = tid; q < r; q += 32) acc += S.F[r * n + q] * S.z[q];
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(FULL, acc, o);
+            if (tid == 0) S.z[r] = (S.g[S.idx[r]] - acc) / S.F[r * n + r];
+            __syncwarp();
+        }
+        for (int r = p - 1; r >= 0; r--) {
+            double acc = 0.0;
+            for (int q = r + 1 + tid; q < p; q += 32) acc += S.F[q * n + r] * S.z[q];
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(FULL, acc, o);
+            if (tid == 0) S.z[r] = (S.z[r] - acc) / S.F[r * n + r];
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    return ok;
+}
+
+__device__ int gather_passive(Solver &S) {
+    if (threadIdx.x == 0) {
+        int p = 0;
+        for (int j = 0; j < S.n; j++)
+            if (S.P[j]) S.idx[p++] = j;
+        S.sflag[1] = p;
+    }
+    __syncthreads();
+    return S.sflag[1];
+}
+
+// min 1/2 x^T H x - g^T x subject to x >= 0 (Lawson-Hanson), starting from the passive set in S.P.
+// Returns 0, or 1 if a passive block was not positive definite, 2 if the iteration limit was reached.
+__device__ int nnls(Solver &S) {
+    const int n = S.n, tid = threadIdx.x;
+    int status = 0;
+    for (int j = tid; j < n; j += blockDim.x) {
+        S.x[j] = 0.0;
+        S.blocked[j] = 0;
+    }
+    __syncthreads();
+    // warm start: drop the non-positive components until the passive least squares is positive
+    for (int it = 0; it <= n; it++) {
+        const int p = gather_passive(S);
+        if (p == 0) break;
+        if (!chol_solve(S, p)) {
+            status = 1;
+            for (int j = tid; j < n; j += blockDim.x) S.P[j] = 0;
+            __syncthreads();
+            break;
+        }
+        if (tid == 0) {
+            int bad = 0;
+            for (int a = 0; a < p; a++)
+                if (!(S.z[a] > 0.0)) {
+                    S.P[S.idx[a]] = 0;
+                    bad = 1;
+                }
+            if (!bad)
+                for (int a = 0; a < p; a++) S.x[S.idx[a]] = S.z[a];
+            S.sflag[2] = bad;
+        }
+        __syncthreads();
+        if (!S.sflag[2]) break;
+    }
+    double gmax = 0.0;
+    for (int j = 0; j < n; j++) gmax = fmax(gmax, fabs(S.g[j]));
+    const double tol = 1e-12 * (gmax > 0 ? gmax : 1.0);
+    for (int outer = 0; outer < 3 * n; outer++) {
+        // w = g - H x
+        for (int j = tid; j < n; j += blockDim.x) {
+            double acc = S.g[j];
+            for (int q = 0; q < n; q++) acc -= S.H[j * n + q] * S.x[q];
+            S.w[j] = acc;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            int t = -1;
+            double best = tol;
+            for (int j = 0; j < n; j++)
+                if (!S.P[j] && !S.blocked[j] && S.w[j] > best) {
+                    best = S.w[j];
+                    t = j;
+                }
+            S.sflag[3] = t;
+            if (t >= 0) S.P[t] = 1;
+        }
+        __syncthreads();
+        const int t = S.sflag[3];
+        if (t < 0) return status;
+        for (int inner = 0; inner < 3 * n; inner++) {
+            const int p = gather_passive(S);
+            if (!chol_solve(S, p)) {
+                status |= 1;
+                if (tid == 0) {
+                    S.P[t] = 0;
+                    S.blocked[t] = 1;
+                }
+                __syncthreads();
+                break;
+            }
+            if (tid == 0) {
+                int allpos = 1, tpos = 1;
+                for (int a = 0; a < p; a++)
+                    if (!(S.z[a] > 0.0)) {
+                        allpos = 0;
+                        if (S.idx[a] == t) tpos = 0;
+                    }
+                if (allpos) {
+                    for (int j = 0; j < n; j++) S.x[j] = 0.0;
+                    for (int a = 0; a < p; a++) S.x[S.idx[a]] = S.z[a];
+                    for (int j = 0; j < n; j++) S.blocked[j] = 0;
+                    S.sflag[4] = 1;
+                } else if (inner == 0 && !tpos) {
+                    // the entering variable is not positive in the least squares: numerically at its bound
+                    S.P[t] = 0;
+                    S.blocked[t] = 1;
+                    S.sflag[4] = 1;
+                } else {
+                    double alpha = 2.0;
+                    for (int a = 0; a < p; a++)
+                        if (!(S.z[a] > 0.0)) {
+                            const int j = S.idx[a];
+                            const double den = S.x[j] - S.z[a];
+                            const double al = den > 0.0 ? S.x[j] / den : 0.0;
+                            alpha = fmin(alpha, al);
+                        }
+                    for (int a = 0; a < p; a++) {
+                        const int j = S.idx[a];
+                        S.x[j] += alpha * (S.z[a] - S.x[j]);
+                        if (!(S.x[j] > 0.0)) {
+                            S.x[j] = 0.0;
+                            S.P[j] = 0;
+                        }
+                    }
+                    S.sflag[4] = 0;
+                }
+            }
+            __syncthreads();
+            if (S.sflag[4]) break;
+        }
+    }
+    return status | 2;
+}
+
+// H = G + sum_i wi^2 L_i^T L_i (L_i: the 3 weights of second difference i at columns lc[i][0..2])
+__device__ void build_H(Solver &S, const double *G, const int *lc, const double *lv, const double *wr, int nrow) {
+    const int n = S.n;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) S.H[e] = G[e];
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int i = 0; i < nrow; i++) {
+            const double w2 = wr[i] * wr[i];
+            for (int a = 0; a < 3; a++)
+                for (int b = 0; b < 3; b++)
+                    S.H[lc[3 * i + a] * n + lc[3 * i + b]] += w2 * lv[3 * i + a] * lv[3 * i + b];
+        }
+    __syncthreads();
+}
+
+// One CTA per member: solve_profile (bbarolo/profile.py:91-138) on the normal equations gh (packed G, h).
+__global__ void __launch_bounds__(PS_THREADS) k_prof_solve(const double *__restrict__ gh, ProfConst pc,
+                                                           const int *__restrict__ lc, const double *__restrict__ lv,
+                                                           const int *__restrict__ ord,
+                                                           const unsigned char *__restrict__ near,
+                                                           const int *__restrict__ p0, double *__restrict__ xout,
+                                                           int *__restrict__ pout, int *__restrict__ status) {
+    extern __shared__ double psm[];
+    const int n = pc.n, k = blockIdx.x, tid = threadIdx.x;
+    Solver S;
+    S.n = n;
+    double *G = psm;
+    S.H = G + n * n;
+    S.F = S.H + n * n;
+    S.g = S.F + n * n;
+    S.x = S.g + n;
+    S.z = S.x + n;
+    S.w = S.z + n;
+    double *wr = S.w + n;                       // n weights of the prior rows
+    double *x0 = wr + n;
+    S.sval = x0 + n;
+    S.P = (int *)(S.sval + 8);
+    S.idx = S.P + n;
+    S.blocked = S.idx + n;
+    S.sflag = S.blocked + n;
+    const int nent = n * (n + 1) / 2;
+    const double *ghk = gh + (size_t)k * (nent + n);
+    for (int e = tid; e < nent; e += blockDim.x) {
+        // packed upper row-major: row i holds (i, i..n-1)
+        int i = 0, rem = e;
+        while (rem >= n - i) {
+            rem -= n - i;
+            i++;
+        }
+        const int j = i + rem;
+        G[i * n + j] = ghk[e];
+        G[j * n + i] = ghk[e];
+    }
+    for (int j = tid; j < n; j += blockDim.x) {
+        S.g[j] = ghk[nent + j];
+        S.P[j] = p0[j];
+    }
+    __syncthreads();
+    int st = 0;
+    const int nrow = n - 2;
+    if (!(pc.smooth != 0.0) || n < 3) {
+        build_H(S, G, lc, lv, wr, 0);
+        st = nnls(S);
+    } else {
+        double traa = 0.0;
+        for (int j = 0; j < n; j++) traa += G[j * n + j];
+        const double srel = sqrt(0.1 * traa / fmax(pc.norm, 1e-300));
+        for (int i = tid; i < nrow; i += blockDim.x) wr[i] = srel;
+        __syncthreads();
+        build_H(S, G, lc, lv, wr, nrow);
+        st = nnls(S);
+        for (int j = tid; j < n; j += blockDim.x) x0[j] = S.x[j];
+        __syncthreads();
+        if (tid == 0) {
+            double xm = 0.0;
+            for (int j = 0; j < n - 1; j++) xm += x0[j];
+            xm /= (double)(n - 1);
+            S.sval[0] = xm;
+            if (xm > 0) {
+                // the reduced chi2 of the first solution, sum (b - A x0)^2 = b.b - 2 x0.h + x0^T G x0
+                double xh = 0.0, xgx = 0.0;
+                for (int a = 0; a < n; a++) {
+                    xh += x0[a] * S.g[a];
+                    double r = 0.0;
+                    for (int b = 0; b < n; b++) r += G[a * n + b] * x0[b];
+                    xgx += x0[a] * r;
+                }
+                const double chi2 = (pc.bb - 2.0 * xh + xgx) / fmax((double)(pc.m - n), 1.0);
+                const double corr = fmax(pc.corr, 1.0) * fmax(chi2, 1.0);
+                for (int i = 0; i < nrow; i++) {
+                    const double xc = fmax(x0[ord[i + 1]], 0.1 * xm);
+                    double wi = sqrt(corr) * pc.d * pc.d / (pc.smooth * xc);
+                    wi = fmax(wi, sqrt(pc.floor_) * srel);
+                    if (near[i]) wi = srel;
+                    wr[i] = wi;
+                }
+            }
+        }
+        __syncthreads();
+        if (S.sval[0] > 0) {
+            for (int j = tid; j < n; j += blockDim.x) S.P[j] = x0[j] > 0.0;
+            __syncthreads();
+            build_H(S, G, lc, lv, wr, nrow);
+            st |= nnls(S);
+        }
+    }
+    for (int j = tid; j < n; j += blockDim.x) {
+        xout[(size_t)k * n + j] = S.x[j];
+        pout[(size_t)k * n + j] = S.x[j] > 0.0;
+    }
+    if (tid == 0) status[k] = st;
+}
+
+// ------------------------------------------------------------------------------------------- model densities
+// One CTA per member: dens of the model's sub-rings from the ring densities x (the ring weights), then the
+// dens-dependent fields of the MC sub-ring constants (bbarolo/galmod.py:107-122) and the fixed-point exponent.
+// Flags ERR_PROFILE_LAYOUT in err when a density changes the cloud layout (a sub-ring switched off, or a
+// cloud count above the 10-per-pixel floor).
+__global__ void k_mc_dens(GridDev g, SubMC *__restrict__ sub, int nsub, MemberDev *__restrict__ mem,
+                          const double *__restrict__ x, int nx, const int *__restrict__ widx,
+                          const double *__restrict__ wval, const double *__restrict__ rap, int *err) {
+    __shared__ double red[256];
+    const int k = blockIdx.x, tid = threadIdx.x;
+    const double *xk = x + (size_t)k * nx;
+    double bound = 0.0;
+    for (int ir = tid; ir < nsub; ir += blockDim.x) {
+        SubMC &S = sub[(size_t)k * nsub + ir];
+        double dens = 0.0;
+        for (int m = 0; m < 2; m++) {
+            const int r = widx[2 * ir + m];
+            if (r >= 0) dens += wval[2 * ir + m] * xk[r];
+        }
+        const double ra = rap[ir];
+        const bool act = dens != 0.0;
+        int bad = act != (S.active != 0);
+        if (act && S.active) {
+            const double dp = g.cmode == 1 ? dens : (g.cmode == 2 ? __dmul_rn(dens, dens) : pow(dens, (double)g.cmode));
+            const double cd = __dmul_rn(g.cdens, dp);
+            long long nc = lround_ref(__dmul_rn(cd, ra));
+            if ((double)lround_ref(__ddiv_rn((double)nc, ra)) < 10.) nc = lround_ref(__dmul_rn(10.0, ra));
+            if (nc != S.nc) bad = 1;
+            const double fl = (double)(float)__ddiv_rn(__dmul_rn(__dmul_rn(dens, ra), g.pixarea),
+                                                       (double)((long long)S.nc * S.nv));
+            const double wmax = fmax(fabs(S.wrec), fabs(S.wapp));
+            for (int nl = 0; nl < g.nlines && nl < BBGPU_MAXL; nl++) {
+                S.valrel[nl] = __dmul_rn(g.relint[nl], fl);
+                bound += (double)S.nc * (double)S.nv * fabs(S.valrel[nl]) * wmax;
+            }
+        }
+        if (bad) atomicOr(err, ERR_PROFILE_LAYOUT);
+    }
+    red[tid] = bound;
+    __syncthreads();
+    for (int d = blockDim.x / 2; d > 0; d >>= 1) {
+        if (tid < d) red[tid] += red[tid + d];
+        __syncthreads();
+    }
+    const double B = red[0];
+    const int e = B > 0 ? (int)floor(62.0 - log2(B)) : 0;
+    const double Q = ldexp(1.0, e);
+    for (int ir = tid; ir < nsub; ir += blockDim.x) {
+        SubMC &S = sub[(size_t)k * nsub + ir];
+        if (!S.active) continue;
+        for (int nl = 0; nl < g.nlines && nl < BBGPU_MAXL; nl++) {
+            S.fix[0][nl] = llrint(S.valrel[nl] * S.wrec * Q);
+            S.fix[1][nl] = llrint(S.valrel[nl] * S.wapp * Q);
+        }
+    }
+    if (tid == 0) mem[k].fix_exp = e;
+}
+
+}  // namespace
+
+void launch_an_maps_fast(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase,
+                         const int *ssub, const double *cs, long long nsamp, int nb, const double *zq,
+                         const float *zqf, const float *wqf, const int *widx, const float *wvalf, const ProfBox &box,
+                         const int *fix_exp, long long *maps64) {
+    const long long nw = nsamp * nb;
+    if (nw == 0) return;
+    k_an_maps_fast<<<(unsigned)((nw + MW_WPB - 1) / MW_WPB), MW_WPB * 32, 0, s>>>(
+        g, subs, nsub, sbase, ssub, (const double2 *)cs, nsamp, nb, zq, zqf, wqf, widx, wvalf, box, fix_exp,
+        (unsigned long long *)maps64);
+}
+
+void launch_maps_to_f32(cudaStream_t s, const long long *in, const int *fix_exp, int nb, long long per_member,
+                        float scale, float *out) {
+    if (nb == 0 || per_member == 0) return;
+    dim3 grid((unsigned)std::min<long long>((per_member + 255) / 256, 1024), nb);
+    k_maps_to_f32<<<grid, 256, 0, s>>>(in, fix_exp, per_member, scale, out);
+}
+
+int prof_gram_tiles(int npix_used) { return (npix_used + GRAM_TP - 1) / GRAM_TP; }
+
+template <class T>
+static void prof_gram(cudaStream_t s, const T *K, const ProfBox &box, const int *pix, const double *wpix,
+                      const double *wy, int npix_used, const int *ent_i, const int *ent_j, int nent, int nb,
+                      double *part, double *gh) {
+    const int nt = prof_gram_tiles(npix_used);
+    if (nb == 0 || nt == 0) return;
+    const size_t smem = (size_t)GRAM_TP * box.nrp * sizeof(T) + 2 * GRAM_TP * sizeof(double);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_prof_gram<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_prof_gram<T><<<dim3(nt, nb), 256, smem, s>>>(K, box, pix, wpix, wy, npix_used, ent_i, ent_j, nent, part);
+    k_prof_gram_reduce<<<dim3((nent + 127) / 128, nb), 128, 0, s>>>(part, nt, nent, gh);
+}
+
+void launch_prof_gram(cudaStream_t s, const float *K, const ProfBox &box, const int *pix, const double *wpix,
+                      const double *wy, int npix_used, const int *ent_i, const int *ent_j, int nent, int nb,
+                      double *part, double *gh) {
+    prof_gram<float>(s, K, box, pix, wpix, wy, npix_used, ent_i, ent_j, nent, nb, part, gh);
+}
+
+void launch_prof_gram64(cudaStream_t s, const double *A, const ProfBox &box, const double *b, int m, const int *ent_i,
+                        const int *ent_j, int nent, double *part, double *gh) {
+    prof_gram<double>(s, A, box, nullptr, nullptr, b, m, ent_i, ent_j, nent, 1, part, gh);
+}
+
+size_t prof_solve_smem(int n) { return (size_t)(3 * n * n + 6 * n + 8) * sizeof(double) + (size_t)(4 * n + 8) * sizeof(int); }
+
+void launch_prof_solve(cudaStream_t s, const double *gh, const ProfConst &pc, const int *lc, const double *lv,
+                       const int *ord, const unsigned char *near, const int *p0, int nb, double *x, int *pout,
+                       int *status) {
+    if (nb == 0) return;
+    const size_t smem = prof_solve_smem(pc.n);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_prof_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_prof_solve<<<nb, PS_THREADS, smem, s>>>(gh, pc, lc, lv, ord, near, p0, x, pout, status);
+}
+
+void launch_mc_dens(cudaStream_t s, const GridDev &g, SubMC *sub, int nsub, MemberDev *mem, int nb, const double *x,
+                    int nx, const int *widx, const double *wval, const double *rap, int *err) {
+    if (nb == 0) return;
+    k_mc_dens<<<nb, 256, 0, s>>>(g, sub, nsub, mem, x, nx, widx, wval, rap, err);
+}

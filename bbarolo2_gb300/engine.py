@@ -15,7 +15,7 @@ import numpy as np
 
 from . import _lib
 from .beam import BeamKernel
-from .galmod import (GalmodSetup, ZSTEP_BEAM, ZSTEP_COARSE, ZSTEP_FINE, ZSAMPLES_MAX, arcsconv, model_rings,
+from .galmod import (GalmodSetup, ZSTEP_BEAM, ZSTEP_COARSE, ZSTEP_FINE, ZSAMPLES_MAX, arcsconv, model_rings, model_rows,
                      outer_edge, ringmode_name, seed32, subrings_batch)
 from .rings import RING_KEYS
 
@@ -172,30 +172,75 @@ class DiskModel:
                                                  1 if threshold else 0))
         return out
 
+    # ------------------------------------------------------------------------------------------ ring maps
+    def _ring_weights(self, rings, ringmode):
+        """(widx, wval) (nsub, 2): the ring(s) whose density each sub-ring interpolates and the weights
+        (``bbarolo/galmod.py:1285-1315``), computed with unit densities through ``subrings``; cached."""
+        key = (tuple(np.asarray(rings.radii, float)), float(rings.radsep), ringmode, getattr(rings, "edge", None),
+               float(getattr(rings, "edgewidth", 0.)), rings.thick(),
+               tuple(np.asarray(rings.fthick, float)) if rings.thick() else ())
+        cache = self.__dict__.setdefault("_wcache", {})
+        if key in cache:
+            return cache[key]
+        st = self.setup
+        cols = []
+        for r in range(rings.nr):
+            rr = rings.copy()
+            rr.dens = np.zeros(rings.nr)
+            rr.dens[r] = 1.
+            cols.append(st.subrings(model_rings(rr, ringmode, st.radsep))[0][5])
+        W = np.array(cols).T
+        nsub = W.shape[0]
+        widx = np.full((nsub, 2), -1, np.int64)
+        wval = np.zeros((nsub, 2))
+        for s in range(nsub):
+            nz = np.flatnonzero(W[s] != 0)
+            if len(nz) > 2:
+                raise RuntimeError("ring_maps: a sub-ring depends on more than two rings.")
+            widx[s, :len(nz)] = nz
+            wval[s, :len(nz)] = W[s, nz]
+        if len(cache) > 64:
+            cache.clear()
+        cache[key] = (widx, wval)
+        return widx, wval
+
+    @property
+    def mapscale(self):
+        """The factor of the ring maps: mean(cd2i) x sum(relint) (x the beam scale factor when smoothing)."""
+        st = self.setup
+        f = float(np.mean(st.cd2i)) * float(np.sum(st.relint))
+        return f * self.scalefactor if self.cfield is not None else f
+
+    def ring_maps(self, rings, blo=None, bhi=None, ringmode=None):
+        """Total-intensity maps (nr, ny, nx) of each ring with unit density, convolved with the beam when
+        smoothing is on (``bbarolo/galmod.py:1317-1345``): the ANALYTIC samples deposited on the device, the
+        convolution on the device (float32, within 1e-6 of the peak of the float64 maps)."""
+        if blo is None or bhi is None:
+            blo, bhi = (0, 0), (self.cin.DimX(), self.cin.DimY())
+        mode = self.ringmode if ringmode is None else ringmode_name(ringmode)
+        st = self.setup
+        mr = model_rings(rings, mode, st.radsep)
+        mr = mr.copy() if mr is rings else mr
+        mr.dens = np.ones(mr.nr)
+        sr, _ = st.subrings(mr)
+        widx, wval = self._ring_weights(rings, mode)
+        out = np.zeros((rings.nr, bhi[1] - blo[1], bhi[0] - blo[0]))
+        if sr.shape[1]:
+            sr = np.ascontiguousarray(sr)
+            nzq = 1 if not np.any(sr[6] > 0) else ZSAMPLES_MAX
+            self.ctx.check(self.ctx.L.bbgpu_ring_maps_analytic(self.ctx.h, _lib.ptr(out), out.shape[0], _lib.ptr(sr),
+                                                               sr.shape[1], _lib.ptr(widx), _lib.ptr(wval), nzq,
+                                                               int(blo[0]), int(blo[1]), int(bhi[0]), int(bhi[1])))
+        out *= float(np.mean(st.cd2i)) * float(np.sum(st.relint))
+        if self.cfield is not None and out.size:
+            out = self.convolve_planes(out) * self.scalefactor
+        return out
+
     def model_rows(self, rows, proto, ringmode=None):
         """Ring-value rows (B, 17, nr) of ring sets like ``proto`` -> the rows of their model rings (with the
         ring convention) and the model-ring prototype."""
         mode = self.ringmode if ringmode is None else ringmode_name(ringmode)
-        probe = proto.copy()
-        probe.radii = np.asarray(proto.radii, float)
-        mr = model_rings(probe, mode, self.setup.radsep)
-        if mr is probe:
-            return np.asarray(rows, float), probe
-        # the model rings repeat the first/last ring (CENTRED) or shift the end radii (SHIFTED)
-        idx = []
-        for r in mr.radii:
-            j = np.flatnonzero(np.asarray(proto.radii) == r)
-            idx.append(int(j[0]) if j.size else -1)
-        nr = proto.nr
-        if idx and idx[0] == -1:
-            idx[0] = 0
-        if idx and idx[-1] == -1:
-            idx[-1] = nr - 1
-        if any(i < 0 for i in idx):
-            raise ValueError("model_rows: ring convention not representable")
-        out = np.asarray(rows, float)[:, :, idx].copy()
-        out[:, 0, :] = mr.radii
-        return out, mr
+        return model_rows(rows, proto, mode, self.setup.radsep)
 
 
 class BatchLikelihood:
@@ -240,6 +285,74 @@ class BatchLikelihood:
         Lb, Hb = self.likebox
         self._dm2_box = self._boxsum(Lb, Hb)
         self.nvox = int(valid[:, Lb[1]:Hb[1], Lb[0]:Hb[0]].sum()) if nvox is None else int(nvox)
+        self._prof = None
+        self._data = d
+
+    def set_profile(self, proto, data_map, rms_map, ok_map, smooth=0.3, corr=1., floor=None, beam_arcsec=None):
+        """Recompute the density profile of the rings at every evaluation, as Bayesian3DFIT does when DENS is not
+        fitted and the geometry is free (``bbarolo/bayesian/likelihood.py:595-596``,
+        ``bbarolo/bayesian/density.py:39-88``): the ring maps of each member, their convolution, the weighted
+        least squares against data_map (noise rms_map, pixels ok_map; all of the likelihood box) and the
+        non-negative solve with the smoothness prior (``bbarolo/profile.py:91-138``), on the device, before its
+        MC model. proto: the rings (radii and options) of the batches to come."""
+        from . import profile as P
+        dm = self.model
+        Lb, Hb = self.likebox
+        shape = (Hb[1] - Lb[1], Hb[0] - Lb[0])
+        y = np.ascontiguousarray(data_map, np.float64)
+        s = np.ascontiguousarray(rms_map, np.float64)
+        ok = np.ascontiguousarray(ok_map, dtype=bool)
+        if y.shape != shape or s.shape != shape or ok.shape != shape:
+            raise ValueError(f"set_profile: the maps must have the shape of the likelihood box {shape}")
+        ext, w = P.exterior_ring(dm, proto, beam_arcsec)
+        Rc = np.ascontiguousarray(np.r_[np.asarray(proto.radii, float), float(ext.radii[0])])
+        ctx = dm.ctx
+        ctx.check(ctx.L.bbgpu_set_profile(ctx.h, proto.nr, int(Lb[0]), int(Lb[1]), int(Hb[0]), int(Hb[1]),
+                                          _lib.ptr(y), _lib.ptr(s), _lib.ptr(ok.view(np.uint8)), _lib.ptr(Rc),
+                                          float(smooth or 0.), float(corr),
+                                          float(P.DENSPROF_FLOOR if floor is None else floor), dm.mapscale))
+        wm = dm._ring_weights(proto, dm.ringmode)
+        we = dm._ring_weights(ext, "CENTRED")
+        widx = np.ascontiguousarray(np.concatenate([wm[0], np.where(we[0] >= 0, we[0] + proto.nr, -1)]), np.int64)
+        wval = np.ascontiguousarray(np.concatenate([wm[1], we[1]]))
+        self._prof = dict(nr=proto.nr, ext=ext, widx=widx, wval=wval, radii=np.asarray(proto.radii, float).copy(),
+                          y=y, rms=s, ok=ok, Rc=Rc, smooth=float(smooth or 0.), corr=float(corr),
+                          floor=P.DENSPROF_FLOOR if floor is None else float(floor))
+
+    def data_maps(self):
+        """(data_mom0, map_rms, ok) of the likelihood box, as Bayesian3DFIT builds them
+        (``bbarolo/bayesian/likelihood.py:180-188, 206-221``, ``bbarolo/bayesian/density.py:80-83``): the sum of
+        the data in the voxels of the likelihood, sigma x sqrt(their number) (channels independent), and the
+        pixels of the region with such voxels."""
+        d = self._data
+        lm = self.mask if self.mask is not None else np.ones(d.shape, bool)
+        v = lm & np.isfinite(d) & (d != 0)
+        mom0 = np.where(v, d, 0.).astype(np.float64).sum(axis=0)
+        nvox = v.sum(axis=0)
+        rms = self.sigma * np.sqrt(nvox.astype(np.float64))
+        ok = nvox > 0
+        if self.region is not None:
+            ok &= self.region
+        Lb, Hb = self.likebox
+        sl = (slice(Lb[1], Hb[1]), slice(Lb[0], Hb[0]))
+        return mom0[sl], rms[sl], ok[sl]
+
+    def profile_maps(self, rows):
+        """The sub-ring tables of the ring maps of a batch (B, 16, nsm): the model's sub-rings, then those of the
+        exterior annulus (the values of each member's last ring, ``bbarolo/profile.py:66-69``)."""
+        dm = self.model
+        P = self._prof
+        ext = P["ext"]
+        rows = np.asarray(rows, float)
+        er = np.zeros(rows.shape[:2] + (1,))
+        keep = [RING_KEYS.index(k) for k in ("xpos", "ypos", "vsys", "vrot", "vdisp", "z0", "inc", "phi",
+                                             "z0thick", "fthick", "vdispthick")]
+        er[:, keep, 0] = rows[:, keep, -1]
+        er[:, RING_KEYS.index("radii"), 0] = ext.radii[0]
+        er[:, RING_KEYS.index("dens"), 0] = 1.
+        emr_rows, emr = dm.model_rows(er, ext, ringmode="CENTRED")
+        sre, _ = subrings_batch(dm.setup, emr, emr_rows)
+        return sre
 
     def _boxsum(self, blo, bhi):
         S = self._dm2_sat
@@ -269,6 +382,10 @@ class BatchLikelihood:
             boxes.append((blo, bhi))
             descs[k] = (blo[0], blo[1], bhi[0], bhi[1], s, self.maskmode, 1 if self.region is not None else 0,
                         self.sigma ** 2, (self.eps or 0.) ** 2)
+        if self._prof is not None:
+            if not np.array_equal(np.asarray(proto.radii, float), self._prof["radii"]):
+                raise ValueError("the radii differ from those given to set_profile")
+            self._maps_sr = np.ascontiguousarray(np.concatenate([sr, self.profile_maps(rows)], axis=2))
         return sr, nv, descs, boxes
 
     def evaluate(self, rows, proto, seed=None, galmodtype=None):
@@ -284,9 +401,28 @@ class BatchLikelihood:
         ss = np.zeros(B)
         lg = np.zeros(B)
         ctx = dm.ctx
-        ctx.check(ctx.L.bbgpu_eval_batch(ctx.h, _lib.ANALYTIC if gt == "ANALYTIC" else _lib.MC, B, nsub,
-                                         _lib.ptr(sr), _lib.ptr(nv), _lib.ptr(descs), _lib.ptr(ss), _lib.ptr(lg)))
+        code = _lib.ANALYTIC if gt == "ANALYTIC" else _lib.MC
+        if self._prof is None:
+            ctx.check(ctx.L.bbgpu_eval_batch(ctx.h, code, B, nsub, _lib.ptr(sr), _lib.ptr(nv), _lib.ptr(descs),
+                                             _lib.ptr(ss), _lib.ptr(lg)))
+            return ss, lg
+        ctx.check(ctx.L.bbgpu_eval_upload(ctx.h, code, B, nsub, _lib.ptr(sr), _lib.ptr(nv), _lib.ptr(descs)))
+        P = self._prof
+        ms = self._maps_sr
+        ctx.check(ctx.L.bbgpu_eval_upload_profile(ctx.h, ms.shape[2], _lib.ptr(ms), _lib.ptr(P["widx"]),
+                                                  _lib.ptr(P["wval"])))
+        ctx.check(ctx.L.bbgpu_eval_run(ctx.h))
+        ctx.check(ctx.L.bbgpu_eval_download(ctx.h, _lib.ptr(ss), _lib.ptr(lg)))
         return ss, lg
+
+    def last_profile(self):
+        """(x (B, nr + 1), status (B)) of the last evaluation: the ring densities (and the exterior annulus)."""
+        ctx = self.model.ctx
+        B = len(self._maps_sr)
+        x = np.zeros((B, self._prof["nr"] + 1))
+        st = np.zeros(B, np.int32)
+        ctx.check(ctx.L.bbgpu_eval_profile(ctx.h, _lib.ptr(x), _lib.ptr(st)))
+        return x, st
 
     def finish(self, ss, lg, boxes):
         s2 = self.sigma ** 2

@@ -160,6 +160,31 @@ def model_rings(rings, mode="CENTRED", subring=0.):
     return out
 
 
+def model_rows(rows, proto, mode, radsep):
+    """Ring-value rows (B, 17, nr) of ring sets like ``proto`` -> (the rows of their model rings with the ring
+    convention ``mode`` (``model_rings``), the model-ring prototype): CENTRED repeats the first/last ring at the
+    added half rings, SHIFTED moves the end radii, NODES keeps the rings."""
+    probe = proto.copy()
+    probe.radii = np.asarray(proto.radii, float)
+    mr = model_rings(probe, mode, radsep)
+    if mr is probe:
+        return np.asarray(rows, float), probe
+    idx = []
+    for r in mr.radii:
+        j = np.flatnonzero(np.asarray(proto.radii) == r)
+        idx.append(int(j[0]) if j.size else -1)
+    nr = proto.nr
+    if idx and idx[0] == -1:
+        idx[0] = 0
+    if idx and idx[-1] == -1:
+        idx[-1] = nr - 1
+    if any(i < 0 for i in idx):
+        raise ValueError("model_rows: ring convention not representable")
+    out = np.asarray(rows, float)[:, :, idx].copy()
+    out[:, 0, :] = mr.radii
+    return out, mr
+
+
 def outer_edge(rings, mode="CENTRED"):
     mode = ringmode_name(mode)
     if mode == "NODES":

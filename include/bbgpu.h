@@ -113,6 +113,30 @@ int bbgpu_norm(bbgpu_ctx *ctx, double *model, int bsy, int bsx, int nz, const fl
                double data_noise, double bweight, int normtype, const double *pre, const int64_t *ilo,
                const int64_t *ihi, int ky, const double *thr, int foot, double hmax, double *out);
 
+/* ---- flux normalisation of the batched likelihood ------------------------------------------------------ */
+/* The deconvolved density profile of each member, recomputed on the device at every evaluation, as
+ * Bayesian3DFIT does when DENS is not fitted and the geometry is free (bbarolo/bayesian/likelihood.py:595-596,
+ * bbarolo/bayesian/density.py:39-88, bbarolo/profile.py:33-138). Set once per fit: the likelihood box, the data
+ * map ymap, its noise rms and the pixels to use ok (all (bhi1-blo1, bhi0-blo0)), the radii of the nr rings and of
+ * the exterior annulus (nr + 1, nr + 1 <= 64), the prior (smooth, corr, floor as solve_profile) and mapscale =
+ * mean(cd2i) x sum(relint) x the beam scale factor (DiskModel.ring_maps). */
+int bbgpu_set_profile(bbgpu_ctx *ctx, int nr, int blo0, int blo1, int bhi0, int bhi1, const double *ymap,
+                      const double *rms, const uint8_t *ok, const double *radii, double smooth, double corr,
+                      double floor_, double mapscale);
+/* Per MC batch, after bbgpu_eval_upload: the sub-rings of the ring maps of every member, sr_maps (nb, 16, nsm):
+ * the model's sub-rings (the first nsub, as uploaded) then those of the exterior annulus; widx, wval (nsm, 2)
+ * the map of each sub-ring and its weight (-1: none). eval_run then computes the maps, their convolution, the
+ * normal equations and the profile, and sets the densities of the model's sub-rings before the MC model. */
+int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *sr_maps, const int64_t *widx,
+                              const double *wval);
+/* The densities of the last run: x (nb, nr + 1), status (nb; 0 = converged, or NULL). */
+int bbgpu_eval_profile(bbgpu_ctx *ctx, double *x, int *status);
+/* solve_profile(A, b, radii, smooth, corr, floor) on the device: A (m, n) row-major, b (m), radii (n); x (n).
+ * status: 0 converged, 1 a passive block not positive definite, 2 iteration limit (or NULL).
+ * (Replaces the profile constants set by bbgpu_set_profile.) */
+int bbgpu_solve_profile(bbgpu_ctx *ctx, const double *A, const double *b, int m, int n, const double *radii,
+                        double smooth, double corr, double floor_, double *x, int *status);
+
 /* ---- batched likelihood path ------------------------------------------------------------------------- */
 /* A batch of nb evaluations of the same sub-ring count nsub: sr (nb, 16, nsub) float64, nv (nb, nsub) int64,
  * descs (nb). The GALMOD model (galmodtype), the beam convolution (if a kernel is set), the threshold and

@@ -292,9 +292,55 @@ def gen_ringmaps():
     save("ringmaps.npz", **arrays)
 
 
+# ---------------------------------------------------------------------------------------------- PROFILE
+def gen_profile():
+    """profile_system + solve_profile (bbarolo/profile.py:33-138) on two geometries: the maps of the rings and of
+    the exterior annulus, the system (A, b, ok, Rc) and the densities with and without the smoothness prior."""
+    P = ns.profile
+    arrays, index = {}, []
+    cases = [("flat", cube64(ltype=2), rings64(z0=10., dens=np.linspace(3., 0.5, 8), inc=np.linspace(50., 70., 8)),
+              "CENTRED", ((5, 8), (60, 58))),
+             ("warp", cube64(ltype=1, crota=15.), rings64(z0=0., inc=np.linspace(40., 65., 8),
+                                                           phi=np.linspace(30., 55., 8)), "NODES", ((0, 0), (64, 64)))]
+    for name, cube, r, mode, (blo, bhi) in cases:
+        dm = G.DiskModel(cube, ringmode=mode, galmodtype="ANALYTIC")
+        mom0 = dm.array(r, blo, bhi).sum(axis=0)
+        g = np.random.default_rng(3)
+        rms = np.full(mom0.shape, 0.01 * mom0.max())
+        y = mom0 + g.normal(0, 1, mom0.shape) * rms
+        ok = mom0 > 0.002 * mom0.max()
+        h = cube.Head()
+        beam = abs(h.Bmaj()) * 3600.
+        A, b, okk, Rc = P.profile_system(dm, r, (blo, bhi), y, rms, ok, beam_arcsec=beam)
+        # the maps of the rings and of the exterior annulus (as profile_system builds them)
+        K = dm.ring_maps(r, blo, bhi)
+        edge = G.outer_edge(r, dm.ringmode)
+        rext = edge + beam
+        ext = ns.rings.Rings().setRings(radii=[rext], xpos=r.xpos[-1], ypos=r.ypos[-1], vsys=r.vsys[-1],
+                                        vrot=r.vrot[-1], vdisp=r.vdisp[-1], z0=r.z0[-1], inc=r.inc[-1],
+                                        phi=r.phi[-1], dens=1., radsep=2. * beam, z0thick=r.z0thick[-1],
+                                        fthick=r.fthick[-1], vdispthick=r.vdispthick[-1])
+        ext.twolayer = r.thick()
+        ext.edgeapp = ext.edgerec = -1.
+        K = np.concatenate([K, dm.ring_maps(ext, blo, bhi, ringmode="CENTRED")])
+        # (A and b are exactly maps[:, okk].T / rms[okk] and y[okk] / rms[okk]: not stored)
+        assert np.array_equal(K[:, okk].T / rms[okk, None], A) and np.array_equal(y[okk] / rms[okk], b)
+        assert Rc[-1] == rext
+        arrays[name + "/y"], arrays[name + "/rms"], arrays[name + "/ok"] = y, rms, ok
+        arrays[name + "/okk"], arrays[name + "/Rc"], arrays[name + "/maps"] = okk, Rc, K
+        for smooth, corr in ((0.3, 1.0), (0.3, 4.0), (0.0, 1.0), (1.0, 2.0)):
+            arrays[name + f"/x_{smooth}_{corr}"] = P.solve_profile(A, b, Rc, smooth, corr)
+        index.append(dict(name=name, mode=mode, blo=list(blo), bhi=list(bhi), beam_arcsec=beam,
+                          rings={k: np.asarray(getattr(r, k), float).tolist()
+                                 for k in ("radii", "xpos", "ypos", "vsys", "vrot", "vdisp", "dens", "z0", "inc",
+                                           "phi")}))
+    arrays["index"] = np.array(json.dumps(index))
+    save("profile.npz", **arrays)
+
+
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["rng", "subrings", "beam_conv", "residuals", "classic", "ringmaps", "models"]
+    which = sys.argv[1:] or ["rng", "subrings", "beam_conv", "residuals", "classic", "ringmaps", "models", "profile"]
     for w in which:
         print(w)
         {"rng": gen_rng, "subrings": gen_subrings, "beam_conv": gen_beam_conv, "residuals": gen_residuals,
-         "classic": gen_classic, "ringmaps": gen_ringmaps, "models": gen_models}[w]()
+         "classic": gen_classic, "ringmaps": gen_ringmaps, "models": gen_models, "profile": gen_profile}[w]()

@@ -117,3 +117,23 @@ def test_ring_maps_raw(oracle_lib):
                                       m["bhi"][0], m["bhi"][1], m["ltype"], m["nzq"], m["sig_instr"], m["chmin"],
                                       m["zstep"])
         assert np.array_equal(raw, z[mode + "/raw"]), mode
+
+
+def test_profile_solve_matches_reference():
+    """The oracle's restatement of solve_profile against the reference's densities (bbarolo/profile.py:91-138)."""
+    import json
+    from oracle import profile as P
+    z = G.load("profile.npz")
+    for m in json.loads(str(z["index"])):
+        nm = m["name"]
+        okk, rms, y = z[nm + "/okk"], z[nm + "/rms"], z[nm + "/y"]
+        A = z[nm + "/maps"][:, okk].T / rms[okk, None]
+        b = y[okk] / rms[okk]
+        for smooth, corr in ((0.3, 1.0), (0.3, 4.0), (0.0, 1.0), (1.0, 2.0)):
+            x = P.solve_profile(A, b, z[nm + "/Rc"], smooth, corr)
+            ref = z[nm + f"/x_{smooth}_{corr}"]
+            np.testing.assert_allclose(x, ref, rtol=1e-12, atol=1e-15 * np.abs(ref).max())
+    z = G.load("ringmaps.npz")
+    A, b, R = z["profile/A"], z["profile/b"], z["profile/radii"]
+    np.testing.assert_allclose(P.solve_profile(A, b, R, 0.3, 4.0), z["profile/x_smooth"], rtol=1e-12, atol=1e-15)
+    np.testing.assert_allclose(P.solve_profile(A, b, R, 0.0), z["profile/x_nosmooth"], rtol=1e-12, atol=1e-15)
