@@ -29,7 +29,6 @@
 #include "kernels.h"
 
 #define FULL 0xffffffffu
-#define MW_WPB 8            // warps per CTA of k_an_maps_fast
 #define EPS_REL 3.814697265625e-06f
 #define GRAM_TP 128         // pixels per CTA of k_prof_gram
 
@@ -50,19 +49,26 @@ __device__ __forceinline__ int clamp_pix(long long v) {
 }
 
 // ------------------------------------------------------------------------------------------- ring maps
-__global__ void __launch_bounds__(MW_WPB * 32) k_an_maps_fast(GridDev g, const AnSub *__restrict__ subs, int nsub,
-                                                              const int *__restrict__ sbase,
-                                                              const int *__restrict__ ssub,
-                                                              const double2 *__restrict__ cs, long long nsamp,
-                                                              int nb, const double *__restrict__ zq,
-                                                              const float *__restrict__ zqf,
-                                                              const float *__restrict__ wqf,
-                                                              const int *__restrict__ widx,
-                                                              const float *__restrict__ wvalf,
-                                                              ProfBox box, const int *__restrict__ fix_exp,
-                                                              unsigned long long *__restrict__ maps64) {
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const long long gs = (long long)blockIdx.x * MW_WPB + w;
+// One thread per (member, azimuth sample); its heights in order, consecutive heights in one pixel merged into
+// a run (the reference's order), each run deposited into the maps of its one or two rings.
+//
+// The pixel is computed in float32 as xpos + R caz P1 - R saz P2 + z P3 (and the same for y). Counting the
+// roundings (R, caz, the coefficients, z0 and the height each rounded to float32, then 2 products per term and 3
+// sums), the float32 value is within 8u (|xpos| + |t1| + |t2| + |t3|) + u (|x| + 1/2) of the exact one, u = 2^-24;
+// the reference's float64 value is within 1e-12 of it. MAPS_EPS = 16u (twice that bound): when the float32 value
+// lies within MAPS_EPS x (|xpos| + |t1| + |t2| + |t3| + 1) of a half-integer, the pixel is recomputed with the
+// reference's float64 operations.
+#define MAPS_EPS 9.5367431640625e-07f
+
+__global__ void __launch_bounds__(256) k_an_maps_fast(GridDev g, const AnSub *__restrict__ subs, int nsub,
+                                                      const int *__restrict__ sbase, const int *__restrict__ ssub,
+                                                      const double2 *__restrict__ cs, long long nsamp, int nb,
+                                                      const double *__restrict__ zq, const float *__restrict__ zqf,
+                                                      const float *__restrict__ wqf, const int *__restrict__ widx,
+                                                      const float *__restrict__ wvalf, ProfBox box,
+                                                      const int *__restrict__ fix_exp,
+                                                      unsigned long long *__restrict__ maps64) {
+    const long long gs = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gs >= nsamp * nb) return;
     const int k = (int)(gs / nsamp);
     const long long s = gs - (long long)k * nsamp;
@@ -71,84 +77,63 @@ __global__ void __launch_bounds__(MW_WPB * 32) k_an_maps_fast(GridDev g, const A
     if (!S.active) return;
     const int kr = (int)(s - sbase[ir]) >= S.naz ? 1 : 0;
     const double2 c = cs[s];
-    const double wside = c.x >= 0.0 ? S.wrec : S.wapp;
-    if (wside == 0.0) return;
-    const float wsidef = c.x >= 0.0 ? S.wrecf : S.wappf;
+    const bool rec = c.x >= 0.0;
+    if ((rec ? S.wrec : S.wapp) == 0.0) return;
+    const float wsidef = rec ? S.wrecf : S.wappf;
     const float Rf = S.Rf[kr];
     const float a1 = Rf * (float)c.x, a2 = Rf * (float)c.y;
     const float t1 = a1 * S.P1, t2 = a2 * S.P2, u1 = a1 * S.Q1, u2 = a2 * S.Q2;
     const float bxf = S.xposf + (t1 - t2), byf = S.yposf + (u1 + u2);
-    const int nzz = S.nzz;
+    const float xa = fabsf(S.xposf) + fabsf(t1) + fabsf(t2) + 1.0f, ya = fabsf(S.yposf) + fabsf(u1) + fabsf(u2) + 1.0f;
+    const int nzz = S.nzz, off = S.zq_off;
+    const float z0f = S.z0f, P3 = S.P3, Q3 = S.Q3;
     const int e = fix_exp[k];
     const int i0 = widx[2 * ir], i1 = widx[2 * ir + 1];
-    const float v0 = i0 >= 0 ? S.fluxscf * wvalf[2 * ir] * wsidef : 0.f;
-    const float v1 = i1 >= 0 ? S.fluxscf * wvalf[2 * ir + 1] * wsidef : 0.f;
+    const float v0 = i0 >= 0 ? ldexpf(S.fluxscf * wvalf[2 * ir] * wsidef, e) : 0.f;
+    const float v1 = i1 >= 0 ? ldexpf(S.fluxscf * wvalf[2 * ir + 1] * wsidef, e) : 0.f;
     unsigned long long *out = maps64 + (size_t)k * box.npix * box.nrp;
-    // the run carried over from the previous chunk of heights
-    int cg0 = 0, cg1 = 0;
-    float cws = 0.f;
-    bool copen = false;
-    for (int base = 0; base < nzz; base += 32) {
-        const int cnt = min(32, nzz - base);
-        const bool valid = lane < cnt;
-        int g0 = 0, g1 = 0;
-        float wv = 0.f;
-        if (valid) {
-            const int kz = S.zq_off + base + lane;
-            const float zf = nzz > 1 ? zqf[kz] * S.z0f : 0.f;
-            const float t3 = zf * S.P3, u3 = zf * S.Q3;
-            const float gx = bxf + t3, gy = byf + u3;
-            const float ex = (fabsf(S.xposf) + fabsf(t1) + fabsf(t2) + fabsf(t3) + 1.0f) * EPS_REL;
-            const float ey = (fabsf(S.yposf) + fabsf(u1) + fabsf(u2) + fabsf(u3) + 1.0f) * EPS_REL;
-            if (!(round_fast(gx, ex, g0) && round_fast(gy, ey, g1))) {
-                // bbarolo/galmod.py:514-517 in the reference's float64 operations
-                const double R = S.R[kr];
-                const double x = __dmul_rn(R, c.x);
-                const double yb = __dmul_rn(__dmul_rn(R, c.y), S.cinc);
-                const double z = nzz > 1 ? __dmul_rn(zq[kz], S.z0) : 0.0;
-                const double y = __dsub_rn(yb, __dmul_rn(z, S.sinc));
-                g0 = clamp_pix(lround_ref(__dadd_rn(S.xpos, __ddiv_rn(__dsub_rn(__dmul_rn(x, S.spa), __dmul_rn(y, S.cpa)),
-                                                                      g.cdelt0))));
-                g1 = clamp_pix(lround_ref(__dadd_rn(S.ypos, __ddiv_rn(__dadd_rn(__dmul_rn(x, S.cpa), __dmul_rn(y, S.spa)),
-                                                                      g.cdelt1))));
-            }
-            wv = wqf[kz];
+    auto emit = [&](int g0, int g1, float ws) {
+        if (g0 < box.blo0 || g0 >= box.bhi0 || g1 < box.blo1 || g1 >= box.bhi1) return;
+        unsigned long long *o = out + ((size_t)(g1 - box.blo1) * box.bx + (size_t)(g0 - box.blo0)) * box.nrp;
+        if (i0 >= 0) {
+            const long long q = (long long)rintf(v0 * ws);
+            if (q) atomicAdd(o + i0, (unsigned long long)q);
         }
-        // runs of equal pixels: heads, then a segmented inclusive sum of the weights (fixed tree)
-        const int pg0 = __shfl_up_sync(FULL, g0, 1), pg1 = __shfl_up_sync(FULL, g1, 1);
-        bool head = lane == 0 ? !(copen && g0 == cg0 && g1 == cg1) : (g0 != pg0 || g1 != pg1);
-        if (lane == 0 && !head) wv += cws;
-        float v = wv;
-        bool f = head || lane == 0;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const float ov = __shfl_up_sync(FULL, v, d);
-            const bool of = __shfl_up_sync(FULL, f, d);
-            if (lane >= d && !f) {
-                v += ov;
-                f = of;
-            }
+        if (i1 >= 0) {
+            const long long q = (long long)rintf(v1 * ws);
+            if (q) atomicAdd(o + i1, (unsigned long long)q);
         }
-        const bool nhead = __shfl_down_sync(FULL, head ? 1 : 0, 1) != 0;
-        const bool last_chunk = base + 32 >= nzz;
-        const bool run_end = valid && (lane == cnt - 1 ? last_chunk : nhead);
-        if (run_end && g0 >= box.blo0 && g0 < box.bhi0 && g1 >= box.blo1 && g1 < box.bhi1) {
-            unsigned long long *o = out + ((size_t)(g1 - box.blo1) * box.bx + (size_t)(g0 - box.blo0)) * box.nrp;
-            if (i0 >= 0) {
-                const long long q = __float2ll_rn(ldexpf(v0 * v, e));
-                if (q) atomicAdd(o + i0, (unsigned long long)q);
-            }
-            if (i1 >= 0) {
-                const long long q = __float2ll_rn(ldexpf(v1 * v, e));
-                if (q) atomicAdd(o + i1, (unsigned long long)q);
-            }
+    };
+    int rg0 = 0, rg1 = 0;
+    float rws = 0.f;
+    for (int kz = 0; kz < nzz; kz++) {
+        const float zf = nzz > 1 ? zqf[off + kz] * z0f : 0.f;
+        const float t3 = zf * P3, u3 = zf * Q3;
+        int g0, g1;
+        if (!(round_fast(bxf + t3, (xa + fabsf(t3)) * MAPS_EPS, g0) &&
+              round_fast(byf + u3, (ya + fabsf(u3)) * MAPS_EPS, g1))) {
+            // bbarolo/galmod.py:514-517 in the reference's float64 operations
+            const double R = S.R[kr];
+            const double x = __dmul_rn(R, c.x);
+            const double yb = __dmul_rn(__dmul_rn(R, c.y), S.cinc);
+            const double z = nzz > 1 ? __dmul_rn(zq[off + kz], S.z0) : 0.0;
+            const double y = __dsub_rn(yb, __dmul_rn(z, S.sinc));
+            g0 = clamp_pix(lround_ref(
+                __dadd_rn(S.xpos, __ddiv_rn(__dsub_rn(__dmul_rn(x, S.spa), __dmul_rn(y, S.cpa)), g.cdelt0))));
+            g1 = clamp_pix(lround_ref(
+                __dadd_rn(S.ypos, __ddiv_rn(__dadd_rn(__dmul_rn(x, S.cpa), __dmul_rn(y, S.spa)), g.cdelt1))));
         }
-        // carry the last run of the chunk
-        cg0 = __shfl_sync(FULL, g0, cnt - 1);
-        cg1 = __shfl_sync(FULL, g1, cnt - 1);
-        cws = __shfl_sync(FULL, v, cnt - 1);
-        copen = true;
+        const float w = wqf[off + kz];
+        if (kz > 0 && g0 == rg0 && g1 == rg1) {
+            rws += w;
+        } else {
+            if (kz > 0) emit(rg0, rg1, rws);
+            rg0 = g0;
+            rg1 = g1;
+            rws = w;
+        }
     }
+    if (nzz > 0) emit(rg0, rg1, rws);
 }
 
 // maps (member, pixel, ring) int64 units 2^-e -> float32 x scale
@@ -165,8 +150,10 @@ __global__ void k_maps_to_f32(const long long *__restrict__ in, const int *__res
 
 // ------------------------------------------------------------------------------------------- Gram matrix
 // CTA (tile of GRAM_TP used pixels, member k). Entry e < n(n+1)/2: G[i][j] (i <= j, row-major packed upper),
-// then h[i]. Partial sums per tile, summed over the tiles in order by k_prof_gram_reduce. pix == nullptr: the
-// pixels 0 .. npix_used - 1; wpix == nullptr: unit weights.
+// then h[i]. The tile is staged in shared memory as float64 (the maps and the maps times the pixel weights) with
+// the range of rings not zero at each pixel, so that each product is one float64 FMA over the band of rings that
+// overlap there. Partial sums per tile, summed over the tiles in order by k_prof_gram_reduce.
+// pix == nullptr: the pixels 0 .. npix_used - 1; wpix == nullptr: unit weights.
 template <class T>
 __global__ void __launch_bounds__(256) k_prof_gram(const T *__restrict__ K, ProfBox box, const int *__restrict__ pix,
                                                    const double *__restrict__ wpix, const double *__restrict__ wy,
@@ -175,9 +162,10 @@ __global__ void __launch_bounds__(256) k_prof_gram(const T *__restrict__ K, Prof
                                                    double *__restrict__ part) {
     extern __shared__ double gsm[];
     const int n = box.nrp;
-    double *ws = gsm;                                       // GRAM_TP weights, GRAM_TP weighted data
-    double *wys = ws + GRAM_TP;
-    T *Ks = (T *)(wys + GRAM_TP);                           // GRAM_TP x n
+    double *Kd = gsm;                                       // GRAM_TP x n maps
+    double *Kw = Kd + GRAM_TP * n;                          // GRAM_TP x n maps x pixel weight
+    double *wys = Kw + GRAM_TP * n;                         // GRAM_TP weighted data
+    int *lo = (int *)(wys + GRAM_TP), *hi = lo + GRAM_TP;   // rings not zero at the pixel: lo .. hi
     const int k = blockIdx.y, t = blockIdx.x;
     const int p0 = t * GRAM_TP;
     const int np = min(GRAM_TP, npix_used - p0);
@@ -185,11 +173,21 @@ __global__ void __launch_bounds__(256) k_prof_gram(const T *__restrict__ K, Prof
     for (int i = threadIdx.x; i < np * n; i += blockDim.x) {
         const int pp = i / n, r = i - pp * n;
         const long long q = pix ? pix[p0 + pp] : p0 + pp;
-        Ks[i] = Kk[(size_t)q * n + r];
+        const double v = (double)Kk[(size_t)q * n + r];
+        Kd[i] = v;
+        Kw[i] = v * (wpix ? wpix[p0 + pp] : 1.0);
     }
-    for (int i = threadIdx.x; i < np; i += blockDim.x) {
-        ws[i] = wpix ? wpix[p0 + i] : 1.0;
-        wys[i] = wy[p0 + i];
+    for (int i = threadIdx.x; i < np; i += blockDim.x) wys[i] = wy[p0 + i];
+    __syncthreads();
+    for (int pp = threadIdx.x; pp < np; pp += blockDim.x) {
+        int a = n, b = -1;
+        for (int r = 0; r < n; r++)
+            if (Kd[pp * n + r] != 0.0) {
+                a = min(a, r);
+                b = r;
+            }
+        lo[pp] = a;
+        hi[pp] = b;
     }
     __syncthreads();
     double *out = part + ((size_t)k * gridDim.x + t) * nent;
@@ -197,15 +195,11 @@ __global__ void __launch_bounds__(256) k_prof_gram(const T *__restrict__ K, Prof
         const int i = ent_i[e], j = ent_j[e];
         double acc = 0.0;
         if (j >= 0) {
-            for (int pp = 0; pp < np; pp++) {
-                const T a = Ks[pp * n + i], b = Ks[pp * n + j];
-                if (a != T(0) && b != T(0)) acc = fma(ws[pp], (double)a * (double)b, acc);
-            }
+            for (int pp = 0; pp < np; pp++)
+                if (lo[pp] <= i && j <= hi[pp]) acc = fma(Kw[pp * n + i], Kd[pp * n + j], acc);
         } else {
-            for (int pp = 0; pp < np; pp++) {
-                const T a = Ks[pp * n + i];
-                if (a != T(0)) acc = fma(wys[pp], (double)a, acc);
-            }
+            for (int pp = 0; pp < np; pp++)
+                if (lo[pp] <= i && i <= hi[pp]) acc = fma(wys[pp], Kd[pp * n + i], acc);
         }
         out[e] = acc;
     }
@@ -589,7 +583,7 @@ void launch_an_maps_fast(cudaStream_t s, const GridDev &g, const AnSub *subs, in
                          const int *fix_exp, long long *maps64) {
     const long long nw = nsamp * nb;
     if (nw == 0) return;
-    k_an_maps_fast<<<(unsigned)((nw + MW_WPB - 1) / MW_WPB), MW_WPB * 32, 0, s>>>(
+    k_an_maps_fast<<<(unsigned)((nw + 255) / 256), 256, 0, s>>>(
         g, subs, nsub, sbase, ssub, (const double2 *)cs, nsamp, nb, zq, zqf, wqf, widx, wvalf, box, fix_exp,
         (unsigned long long *)maps64);
 }
@@ -609,7 +603,7 @@ static void prof_gram(cudaStream_t s, const T *K, const ProfBox &box, const int 
                       double *part, double *gh) {
     const int nt = prof_gram_tiles(npix_used);
     if (nb == 0 || nt == 0) return;
-    const size_t smem = (size_t)GRAM_TP * box.nrp * sizeof(T) + 2 * GRAM_TP * sizeof(double);
+    const size_t smem = (size_t)(2 * GRAM_TP * box.nrp + GRAM_TP) * sizeof(double) + 2 * GRAM_TP * sizeof(int);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_prof_gram<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_prof_gram<T><<<dim3(nt, nb), 256, smem, s>>>(K, box, pix, wpix, wy, npix_used, ent_i, ent_j, nent, part);
     k_prof_gram_reduce<<<dim3((nent + 127) / 128, nb), 128, 0, s>>>(part, nt, nent, gh);

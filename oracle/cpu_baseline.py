@@ -52,7 +52,6 @@ def fft_convolve(data, kernel):
 
 
 def _init(payload):
-    os.environ.setdefault("OMP_NUM_THREADS", "1")
     _W.update(payload)
     from oracle import oracle
     oracle.lib()
@@ -139,8 +138,21 @@ class Pool:
     def __init__(self, payload, cores=None):
         self.cores = int(cores or os.cpu_count() or 1)
         ctx = mp.get_context("spawn")
-        self.pool = ctx.Pool(self.cores, initializer=_init, initargs=(payload,))
-        self.pool.map(_noop, range(self.cores))
+        # one BLAS / OpenMP thread per process, as the reference's pool (the workers inherit the environment
+        # before they import numpy)
+        keys = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS", "BLIS_NUM_THREADS")
+        old = {k: os.environ.get(k) for k in keys}
+        for k in keys:
+            os.environ[k] = "1"
+        try:
+            self.pool = ctx.Pool(self.cores, initializer=_init, initargs=(payload,))
+            self.pool.map(_noop, range(self.cores))
+        finally:
+            for k, v in old.items():
+                if v is None:
+                    os.environ.pop(k, None)
+                else:
+                    os.environ[k] = v
 
     def run(self, members):
         """Evaluates the members (indices); returns (sums of squares, wall seconds)."""
