@@ -116,6 +116,10 @@ struct bbgpu_ctx {
     size_t d_maps64_cap = 0;
     MemberDev *d_pmem = nullptr;
     size_t d_pmem_cap = 0;
+    ZgridCache zcache;                 // vertical grids of the ring maps (host), mirrored in d_pzq/d_pzqf/d_pwqf
+    std::string samp_key;              // the sub-ring radii of the sample table on the device
+    AnSub *h_psub = nullptr;           // pinned staging of the sub-ring constants
+    size_t h_psub_cap = 0;
     std::vector<MemberDev> pmem_host;
     // options
     bool keep_smoothed = false, timing = false, want64 = false;
@@ -391,6 +395,7 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
                     (void *)ctx->d_pwvalf, (void *)ctx->d_maps32, (void *)ctx->d_K, (void *)ctx->d_maps64,
                     (void *)ctx->d_pmem})
         cudaFree(q);
+    cudaFreeHost(ctx->h_psub);
     cudaFreeHost(ctx->h_sub); cudaFreeHost(ctx->h_mem); cudaFreeHost(ctx->h_out2); cudaFreeHost(ctx->h_err);
     for (int i = 0; i <= NTIMER; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
@@ -507,6 +512,9 @@ extern "C" int bbgpu_set_grid(bbgpu_ctx *ctx, const bbgpu_grid *gr, const double
             bbh_layout_free(&E.host);
             E.valid = false;
         }
+    ctx->zcache.clear();
+    ctx->samp_key.clear();
+    ctx->prof_set = ctx->prof_uploaded = false;
     ctx->grid_set = true;
     ctx->uploaded = ctx->ran = false;
     return BBGPU_OK;
@@ -1013,9 +1021,10 @@ extern "C" int bbgpu_galmod_analytic(bbgpu_ctx *ctx, double *out, const double *
     for (int r = 0; r < BBGPU_NSR; r++)
         for (int i = 0; i < ns; i++) s2[(size_t)r * ns + i] = sr[(size_t)r * nsub + ring_lo + i];
     std::vector<AnSub> subs(ns);
-    std::vector<double> zq, wq;
+    ZgridCache zc;
     const int e = bbh_an_subs(s2.data(), ns, &g, nzq, blo0, blo1, bhi0, bhi1, ctx->h_cd2i.data(), 0, nullptr, nullptr,
-                              subs.data(), zq, wq);
+                              subs.data(), zc);
+    const std::vector<double> &zq = zc.zq, &wq = zc.wq;
     if (e == -10000) return fail(ctx, BBGPU_ERR_ARG, "galmod_analytic: the total flux is not finite");
     DevBufs B;
     AnDev D;
@@ -1056,9 +1065,10 @@ extern "C" int bbgpu_ring_maps_analytic(bbgpu_ctx *ctx, double *out, int nr, con
     if (nsub == 0 || nr == 0 || by == 0 || bx == 0) return BBGPU_OK;
     const GridDev &g = ctx->g;
     std::vector<AnSub> subs(nsub);
-    std::vector<double> zq, wq;
+    ZgridCache zc;
     const int e = bbh_an_subs(sr, nsub, &g, nzq, blo0, blo1, bhi0, bhi1, ctx->h_cd2i.data(), 1, widx, wval,
-                              subs.data(), zq, wq);
+                              subs.data(), zc);
+    const std::vector<double> &zq = zc.zq, &wq = zc.wq;
     if (e == -10000) return fail(ctx, BBGPU_ERR_ARG, "ring_maps_analytic: the weights are not finite");
     DevBufs B;
     AnDev D;
@@ -1293,6 +1303,8 @@ extern "C" int bbgpu_set_profile(bbgpu_ctx *ctx, int nr, int blo0, int blo1, int
     std::vector<int> ent;
     int rc = profile_consts(ctx, radii, n, smooth, corr, floor_, ent);
     if (rc) return rc;
+    ctx->zcache.clear();
+    ctx->samp_key.clear();
     ctx->prof_set = true;
     ctx->prof_uploaded = false;
     return BBGPU_OK;
@@ -1320,35 +1332,71 @@ extern "C" int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *
             if (sr_maps[(size_t)k * BBGPU_NSR * nsm + 6 * (size_t)nsm + i] > 0) { thick = true; break; }
     const int nzq = thick ? 1024 : 1;
     const ProfBox &bx = ctx->pbox;
-    std::vector<AnSub> subs((size_t)nb * nsm);
-    std::vector<double> zq, wq;
+    int rc;
+    if ((rc = hgrow(ctx, &ctx->h_psub, &ctx->h_psub_cap, (size_t)nb * nsm))) return rc;
+    ZgridCache &zc = ctx->zcache;
+    if (zc.zq.size() > ((size_t)1 << 24)) zc.clear();
+    const size_t zold = zc.uploaded;
     std::vector<int> fix(nb);
     for (int k = 0; k < nb; k++) {
         const int e = bbh_an_subs(sr_maps + (size_t)k * BBGPU_NSR * nsm, nsm, &g, nzq, bx.blo0, bx.blo1, bx.bhi0,
-                                  bx.bhi1, ctx->h_cd2i.data(), 1, widx, wval, subs.data() + (size_t)k * nsm, zq, wq);
+                                  bx.bhi1, ctx->h_cd2i.data(), 1, widx, wval, ctx->h_psub + (size_t)k * nsm, zc);
         if (e == -10000) return fail(ctx, BBGPU_ERR_ARG, "eval_upload_profile: member %d: weights not finite", k);
         fix[k] = std::min(e, 100);
     }
-    std::vector<int> sbase, ssub;
-    std::vector<double> cs;
-    bbh_an_samples(sr_maps, nsm, &g, sbase, ssub, cs);
-    ctx->pnsamp = sbase[nsm];
-    std::vector<float> zqf(zq.size() ? zq.size() : 1), wqf(wq.size() ? wq.size() : 1), wvalf(2 * (size_t)nsm);
-    for (size_t i = 0; i < zq.size(); i++) { zqf[i] = (float)zq[i]; wqf[i] = (float)wq[i]; }
+    cudaStream_t s = ctx->stream;
+    // the table of azimuthal samples (radii of the sub-rings): uploaded when the radii change
+    std::string skey((const char *)sr_maps, sizeof(double) * nsm);
+    skey.append((const char *)&g.pixarea, sizeof(double));
+    if (skey != ctx->samp_key) {
+        std::vector<int> sbase, ssub;
+        std::vector<double> cs;
+        bbh_an_samples(sr_maps, nsm, &g, sbase, ssub, cs);
+        if ((rc = dgrow(ctx, &ctx->d_psbase, &ctx->d_psbase_cap, sbase.size()))) return rc;
+        if ((rc = dgrow(ctx, &ctx->d_pssub, &ctx->d_pssub_cap, ssub.size()))) return rc;
+        if ((rc = dgrow(ctx, &ctx->d_pcs, &ctx->d_pcs_cap, cs.size()))) return rc;
+        CK(cudaMemcpy(ctx->d_psbase, sbase.data(), sizeof(int) * sbase.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(ctx->d_pssub, ssub.data(), sizeof(int) * ssub.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(ctx->d_pcs, cs.data(), sizeof(double) * cs.size(), cudaMemcpyHostToDevice));
+        ctx->pnsamp = sbase[nsm];
+        ctx->samp_key = skey;
+        ctx->h2d += (long long)(sizeof(int) * (sbase.size() + ssub.size()) + sizeof(double) * cs.size());
+    }
+    // the vertical grids: the new ones appended on the device (the table grows with a copy of the old part)
+    const size_t nz1 = zc.zq.size() + 1;
+    if (zc.uploaded == 0 || nz1 > ctx->d_pzq_cap) {
+        if (nz1 > ctx->d_pzq_cap) {
+            for (void *q : {(void *)ctx->d_pzq, (void *)ctx->d_pzqf, (void *)ctx->d_pwqf}) cudaFree(q);
+            ctx->d_pzq = nullptr; ctx->d_pzqf = nullptr; ctx->d_pwqf = nullptr;
+            ctx->d_pzq_cap = ctx->d_pzqf_cap = ctx->d_pwqf_cap = 0;
+            if ((rc = dgrow(ctx, &ctx->d_pzq, &ctx->d_pzq_cap, 2 * nz1))) return rc;
+            if ((rc = dgrow(ctx, &ctx->d_pzqf, &ctx->d_pzqf_cap, 2 * nz1))) return rc;
+            if ((rc = dgrow(ctx, &ctx->d_pwqf, &ctx->d_pwqf_cap, 2 * nz1))) return rc;
+        }
+        zc.uploaded = 0;
+    }
+    if (zc.zq.size() > zc.uploaded) {
+        const size_t a0 = zc.uploaded, m = zc.zq.size() - a0;
+        std::vector<float> zf(m), wf(m);
+        for (size_t i = 0; i < m; i++) {
+            zf[i] = (float)zc.zq[a0 + i];
+            wf[i] = (float)zc.wq[a0 + i];
+        }
+        CK(cudaMemcpy(ctx->d_pzq + a0, zc.zq.data() + a0, sizeof(double) * m, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(ctx->d_pzqf + a0, zf.data(), sizeof(float) * m, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(ctx->d_pwqf + a0, wf.data(), sizeof(float) * m, cudaMemcpyHostToDevice));
+        ctx->h2d += (long long)(16 * m);
+        zc.uploaded = zc.zq.size();
+    }
+    (void)zold;
+    std::vector<float> wvalf(2 * (size_t)nsm);
     std::vector<int> wi(2 * (size_t)nsm);
     for (int i = 0; i < 2 * nsm; i++) { wvalf[i] = (float)wval[i]; wi[i] = (int)widx[i]; }
     // ring area of each model sub-ring (bbarolo/galmod.py:107), for the densities of the MC model
     std::vector<double> rap(nsub ? nsub : 1);
     for (int i = 0; i < nsub; i++) rap[i] = 2 * M_PI * sr_maps[i] * g.radsep / g.pixarea;
     const long long per = bx.npix * bx.nrp;
-    int rc;
-    if ((rc = dgrow(ctx, &ctx->d_psub, &ctx->d_psub_cap, subs.size()))) return rc;
-    if ((rc = dgrow(ctx, &ctx->d_psbase, &ctx->d_psbase_cap, sbase.size()))) return rc;
-    if ((rc = dgrow(ctx, &ctx->d_pssub, &ctx->d_pssub_cap, ssub.size()))) return rc;
-    if ((rc = dgrow(ctx, &ctx->d_pcs, &ctx->d_pcs_cap, cs.size()))) return rc;
-    if ((rc = dgrow(ctx, &ctx->d_pzq, &ctx->d_pzq_cap, zq.size() + 1))) return rc;
-    if ((rc = dgrow(ctx, &ctx->d_pzqf, &ctx->d_pzqf_cap, zqf.size()))) return rc;
-    if ((rc = dgrow(ctx, &ctx->d_pwqf, &ctx->d_pwqf_cap, wqf.size()))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_psub, &ctx->d_psub_cap, (size_t)nb * nsm))) return rc;
     if ((rc = dgrow(ctx, &ctx->d_pwidx, &ctx->d_pwidx_cap, wi.size()))) return rc;
     if ((rc = dgrow(ctx, &ctx->d_pwvalf, &ctx->d_pwvalf_cap, wvalf.size()))) return rc;
     if ((rc = dgrow(ctx, &ctx->d_pwval, &ctx->d_pwval_cap, 2 * (size_t)nsm))) return rc;
@@ -1371,22 +1419,14 @@ extern "C" int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *
     const int npart = conv_resid_npart(ctx->pmem_host.data(), nb, bx.nrp);
     if ((rc = dgrow(ctx, &ctx->d_pmem, &ctx->d_pmem_cap, (size_t)nb))) return rc;
     if ((rc = dgrow(ctx, &ctx->d_ppart, &ctx->d_ppart_cap, (size_t)2 * nb * (npart ? npart : 1)))) return rc;
-    cudaStream_t s = ctx->stream;
-    CK(cudaMemcpyAsync(ctx->d_psub, subs.data(), sizeof(AnSub) * subs.size(), cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(ctx->d_psbase, sbase.data(), sizeof(int) * sbase.size(), cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(ctx->d_pssub, ssub.data(), sizeof(int) * ssub.size(), cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(ctx->d_pcs, cs.data(), sizeof(double) * cs.size(), cudaMemcpyHostToDevice, s));
-    if (zq.size()) CK(cudaMemcpyAsync(ctx->d_pzq, zq.data(), sizeof(double) * zq.size(), cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(ctx->d_pzqf, zqf.data(), sizeof(float) * zqf.size(), cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(ctx->d_pwqf, wqf.data(), sizeof(float) * wqf.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->d_psub, ctx->h_psub, sizeof(AnSub) * (size_t)nb * nsm, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(ctx->d_pwidx, wi.data(), sizeof(int) * wi.size(), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(ctx->d_pwvalf, wvalf.data(), sizeof(float) * wvalf.size(), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(ctx->d_pwval, wval, sizeof(double) * 2 * (size_t)nsm, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(ctx->d_rap, rap.data(), sizeof(double) * rap.size(), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(ctx->d_pfix, fix.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(ctx->d_pmem, ctx->pmem_host.data(), sizeof(MemberDev) * nb, cudaMemcpyHostToDevice, s));
-    ctx->h2d += (long long)(sizeof(AnSub) * subs.size() + sizeof(double) * (cs.size() + zq.size()) +
-                            sizeof(float) * (zqf.size() + wqf.size()));
+    ctx->h2d += (long long)(sizeof(AnSub) * (size_t)nb * nsm + sizeof(int) * nb);
     // (the host vectors go out of scope: finish the copies first)
     CK(cudaStreamSynchronize(s));
     ctx->nsm = nsm;

@@ -440,9 +440,34 @@ void bbh_an_samples(const double *R0, int nsub, const GridDev *g, std::vector<in
     }
 }
 
+// The grid of _zgrid's inputs, from the cache or computed and appended to it: (offset, samples).
+static std::pair<int, int> zgrid_cached(ZgridCache &zc, std::vector<double> &tz, std::vector<double> &tw, int nzq,
+                                        int ltype, double z0, double sinc, double pixsize, double dvdz, double sig,
+                                        double R0, double radsep, double xpos, double ypos, double cdelt0,
+                                        double cdelt1, long long blo0, long long blo1, long long bhi0, long long bhi1,
+                                        double zstep) {
+    std::string key;
+    if (z0 <= 0 || nzq < 2 || fabs(sinc) < 1e-6) {
+        key = "thin";
+    } else {
+        const double dv[] = {z0, sinc, pixsize, dvdz, sig, R0, radsep, xpos, ypos, cdelt0, cdelt1, zstep};
+        const long long iv[] = {nzq, ltype, blo0, blo1, bhi0, bhi1};
+        key.assign((const char *)dv, sizeof dv);
+        key.append((const char *)iv, sizeof iv);
+    }
+    auto it = zc.map.find(key);
+    if (it != zc.map.end()) return it->second;
+    const int n = bbh_zgrid(tz.data(), tw.data(), nzq, ltype, z0, sinc, pixsize, dvdz, sig, R0, radsep, xpos, ypos,
+                            cdelt0, cdelt1, blo0, blo1, bhi0, bhi1, zstep);
+    const std::pair<int, int> v((int)zc.zq.size(), n);
+    zc.zq.insert(zc.zq.end(), tz.begin(), tz.begin() + n);
+    zc.wq.insert(zc.wq.end(), tw.begin(), tw.begin() + n);
+    zc.map.emplace(key, v);
+    return v;
+}
+
 int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0, int blo1, int bhi0, int bhi1,
-                const double *cd2i, int maps, const int64_t *widx, const double *wval, AnSub *out,
-                std::vector<double> &zq, std::vector<double> &wq) {
+                const double *cd2i, int maps, const int64_t *widx, const double *wval, AnSub *out, ZgridCache &zc) {
 #define SR(r, i) sr[(size_t)(r) * nsub + (i)]
     const int nb = nzq > 1 ? nzq : 1;
     std::vector<double> tz(nb), tw(nb);
@@ -472,12 +497,13 @@ int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0,
         S.cpa = cos(phi) * cos(g->crota2) - sin(phi) * sin(g->crota2);
         S.xpos = SR(11, ir); S.ypos = SR(12, ir); S.vsys = SR(13, ir);
         S.wrec = SR(14, ir); S.wapp = SR(15, ir);
-        S.zq_off = (int)zq.size();
+        S.zq_off = 0;
         if (S.active) {
-            S.nzz = bbh_zgrid(tz.data(), tw.data(), nzq, g->ltype, S.z0, S.sinc, pixsize, S.dvdz, sig, R0, g->radsep,
-                              S.xpos, S.ypos, g->cdelt0, g->cdelt1, blo0, blo1, bhi0, bhi1, g->zstep);
-            zq.insert(zq.end(), tz.begin(), tz.begin() + S.nzz);
-            wq.insert(wq.end(), tw.begin(), tw.begin() + S.nzz);
+            const std::pair<int, int> zg = zgrid_cached(zc, tz, tw, nzq, g->ltype, S.z0, S.sinc, pixsize, S.dvdz, sig,
+                                                        R0, g->radsep, S.xpos, S.ypos, g->cdelt0, g->cdelt1, blo0,
+                                                        blo1, bhi0, bhi1, g->zstep);
+            S.zq_off = zg.first;
+            S.nzz = zg.second;
         }
         S.fluxsc = maps ? ring_area_pix * g->pixarea / (double)(naz * nrad)
                         : dens * ring_area_pix * g->pixarea / (double)(naz * nrad);
@@ -485,7 +511,7 @@ int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0,
         S.zdep = 0;
         if (!maps && S.active && S.dvdz != 0 && S.nzz > 1)
             for (int kz = 0; kz < S.nzz; kz++)
-                if (fabs(tz[kz] * S.z0) > S.zcyl) { S.zdep = 1; break; }
+                if (fabs(zc.zq[S.zq_off + kz] * S.z0) > S.zcyl) { S.zdep = 1; break; }
         const double r_inner = R0 - 0.5 * g->radsep;
         for (int kr = 0; kr < nrad; kr++) {
             const double u = (kr + 0.5) / nrad;

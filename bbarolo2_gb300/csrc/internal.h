@@ -5,6 +5,8 @@
 #include <stddef.h>
 
 #ifdef __cplusplus
+#include <string>
+#include <unordered_map>
 #include <vector>
 #endif
 
@@ -99,9 +101,21 @@ void bbh_an_samples(const double *R0, int nsub, const GridDev *g, std::vector<in
 // ANALYTIC: the AnSub of each sub-ring of a table (maps: ring-map mode, active where widx has a ring), their
 // vertical samples appended to zq/wq; returns the fixed-point exponent e (deposits in units of 2^-e) or
 // -10000 when the total flux is not finite
+// The vertical sample grids of the ANALYTIC sub-rings, shared by all the sub-rings with the same inputs of _zgrid:
+// one table (append-only), each grid stored once (the fits change few geometries between evaluations).
+struct ZgridCache {
+    std::unordered_map<std::string, std::pair<int, int>> map;   // inputs -> (offset, samples)
+    std::vector<double> zq, wq;
+    size_t uploaded = 0;                                         // entries already copied to the device
+    void clear() {
+        map.clear();
+        zq.clear();
+        wq.clear();
+        uploaded = 0;
+    }
+};
 int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0, int blo1, int bhi0, int bhi1,
-                const double *cd2i, int maps, const int64_t *widx, const double *wval, AnSub *out,
-                std::vector<double> &zq, std::vector<double> &wq);
+                const double *cd2i, int maps, const int64_t *widx, const double *wval, AnSub *out, ZgridCache &zc);
 // The second-difference prior of the deconvolved profile at the radii R (n) (bbarolo/profile.py:60-151):
 // rows (n - 2) x 3 columns lc and weights lv, the order of the radii, the "near" rows, the median ring
 // distance d and the norm of the relative prior

@@ -365,23 +365,49 @@ class BatchLikelihood:
         bhi = [max(min(bhi[0], Hb[0]), blo[0]), max(min(bhi[1], Hb[1]), blo[1])]
         return blo, bhi
 
+    def _boxes(self, rows, proto):
+        """The model boxes of a batch within the likelihood box (``model_box`` / ``DiskModel.box(final=True)``,
+        ``bbarolo/galmod.py:1224-1240``, ``bbarolo/bayesian/likelihood.py:429-436``), vectorised: (blo, bhi)
+        arrays (B, 2). The boxes depend on the last ring's centre and layer height only."""
+        dm = self.model
+        h = dm.cin.Head()
+        rows = np.asarray(rows, float)
+        K = {k: RING_KEYS.index(k) for k in ("xpos", "ypos", "z0", "z0thick", "fthick")}
+        ext0 = proto.radii[-1] + proto.radsep / 2.
+        ext0 = max(ext0, outer_edge(proto, dm.ringmode))
+        z0 = rows[:, K["z0"], -1]
+        if proto.thick():
+            zt = rows[:, K["z0thick"], -1]
+            zt = np.where(zt >= 0, zt, z0)
+            z0 = np.where(rows[:, K["fthick"], -1] > 0, np.maximum(z0, zt), z0)
+        ext = ext0 + 3 * z0
+        xdis = np.ceil(ext / (abs(h.Cdelt(0)) * dm.arcconv)).astype(np.int64)
+        ydis = np.ceil(ext / (abs(h.Cdelt(1)) * dm.arcconv)).astype(np.int64)
+        xpos = np.ceil(rows[:, K["xpos"], -1]).astype(np.int64)
+        ypos = np.ceil(rows[:, K["ypos"], -1]).astype(np.int64)
+        blo = np.stack([np.maximum(xpos - xdis, 0), np.maximum(ypos - ydis, 0)], axis=1)
+        bhi = np.stack([np.minimum(xpos + xdis + 1, dm.cin.DimX()), np.minimum(ypos + ydis + 1, dm.cin.DimY())], axis=1)
+        Lb, Hb = self.likebox
+        blo = np.maximum(blo, np.asarray(Lb, np.int64))
+        bhi = np.maximum(np.minimum(bhi, np.asarray(Hb, np.int64)), blo)
+        return blo, bhi
+
     def prepare(self, rows, proto, seed=None):
         """Host side of a batch: sub-ring tables, boxes and descriptors of the ring-value rows (B, 17, nr)."""
         dm = self.model
         mrows, mr = dm.model_rows(rows, proto)
         sr, nv = subrings_batch(dm.setup, mr, mrows)
         B = sr.shape[0]
-        descs = np.zeros(B, _lib.EVAL_DTYPE)
         s = seed32(dm.setup.iseed if seed is None else seed)
-        boxes = []
-        r = proto.copy()
-        for k in range(B):
-            for j, key in enumerate(RING_KEYS):
-                setattr(r, key, rows[k, j])
-            blo, bhi = self.model_box(r)
-            boxes.append((blo, bhi))
-            descs[k] = (blo[0], blo[1], bhi[0], bhi[1], s, self.maskmode, 1 if self.region is not None else 0,
-                        self.sigma ** 2, (self.eps or 0.) ** 2)
+        blo, bhi = self._boxes(rows, proto)
+        descs = np.zeros(B, _lib.EVAL_DTYPE)
+        descs["blo0"], descs["blo1"], descs["bhi0"], descs["bhi1"] = blo[:, 0], blo[:, 1], bhi[:, 0], bhi[:, 1]
+        descs["seed"] = s
+        descs["maskmode"] = self.maskmode
+        descs["use_region"] = 1 if self.region is not None else 0
+        descs["sigma2"] = self.sigma ** 2
+        descs["eps2"] = (self.eps or 0.) ** 2
+        boxes = [(list(map(int, blo[k])), list(map(int, bhi[k]))) for k in range(B)]
         if self._prof is not None:
             if not np.array_equal(np.asarray(proto.radii, float), self._prof["radii"]):
                 raise ValueError("the radii differ from those given to set_profile")

@@ -85,3 +85,34 @@ def test_subring_errors():
         st.subrings(r)
     with pytest.raises(galmod.BBaroloError):
         galmod.model_rings(rings.subset(np.array([0])), "NODES")
+
+
+def test_batch_boxes_match_model_box():
+    """The vectorised model boxes of a batch equal DiskModel.box(final=True) clipped to the likelihood box, ring
+    set by ring (bbarolo/bayesian/likelihood.py:429-436)."""
+    import types
+    from bbarolo2_gb300 import configs, engine
+    from bbarolo2_gb300.galmod import arcsconv, ring_rows_batch
+    from bbarolo2_gb300.rings import RING_KEYS
+    cube, rings = configs.global160()
+    g = np.random.default_rng(3)
+    for mode, thick in (("CENTRED", False), ("NODES", True), ("SHIFTED", False)):
+        r = rings.copy()
+        if thick:
+            r.fthick = np.full(r.nr, 0.3)
+            r.z0thick = np.full(r.nr, 25.)
+        fake = types.SimpleNamespace(cin=cube, ringmode=mode, arcconv=arcsconv(cube.Head().Cunit(0)))
+        rows = np.repeat(ring_rows_batch([r])[0][None], 12, axis=0)
+        rows[:, RING_KEYS.index("xpos")] += g.uniform(-20, 20, (12, 1))
+        rows[:, RING_KEYS.index("ypos")] += g.uniform(-20, 20, (12, 1))
+        rows[:, RING_KEYS.index("z0")] *= g.uniform(0.5, 3., (12, 1))
+        like = types.SimpleNamespace(model=fake, likebox=([7, 3], [150, 155]))
+        blo, bhi = engine.BatchLikelihood._boxes(like, rows, r)
+        for k in range(12):
+            rk = r.copy()
+            for j, key in enumerate(RING_KEYS):
+                setattr(rk, key, rows[k, j].copy())
+            lo, hi = engine.DiskModel.box(fake, rk, final=True)
+            lo = [max(lo[0], 7), max(lo[1], 3)]
+            hi = [max(min(hi[0], 150), lo[0]), max(min(hi[1], 155), lo[1])]
+            assert list(blo[k]) == lo and list(bhi[k]) == hi, (mode, k)
