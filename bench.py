@@ -125,6 +125,23 @@ def workload(batch):
     return dm, L, rings, rows, data, mask
 
 
+def max_over_ranks(t, dist):
+    """The largest of the ranks' times (replicas: the job ends with the slowest rank); t on one rank without
+    torch.distributed. NCCL reduces a CUDA tensor, gloo a CPU one."""
+    if not dist:
+        return t
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    x = torch.tensor([float(t)], dtype=torch.float64, device=dev)
+    dist.all_reduce(x, op=dist.ReduceOp.MAX)
+    return float(x.item())
+
+
+def throughput(units_per_rank, steps, world, t):
+    """Whole-job throughput of N replicas: the units of all ranks / the max-over-ranks time."""
+    return units_per_rank * steps * world / t
+
+
 def algorithmic(dm, L, sr, nv, descs):
     """Algorithmic bytes / flops per launch of the kernels (summed over the batch)."""
     st = dm.setup
@@ -207,16 +224,13 @@ def main():
     ctx.check(ctx.L.bbgpu_sync(ctx.h))
     dt = time.perf_counter() - t0
     launches = ctx.launches - l0
+    dt = max_over_ranks(dt, dist)
     if dist:
-        import torch
-        t = torch.tensor([dt], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dt = float(t.item())
         dist.barrier()
     ss = np.zeros(B)
     lg = np.zeros(B)
     ctx.check(ctx.L.bbgpu_eval_download(ctx.h, _lib.ptr(ss), _lib.ptr(lg)))
-    value = B * args.steps * world / dt
+    value = throughput(B, args.steps, world, dt)
     # ---- per-kernel device times (CUDA events on the context's stream)
     ctx.set_option(_lib.OPT_TIMING, 1)
     ktimes = {}
@@ -235,14 +249,10 @@ def main():
     for _ in range(args.steps):
         out = L.evaluate(rows, rings, seed=1)
     te = time.perf_counter() - t0
-    if dist:
-        import torch
-        t = torch.tensor([te], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        te = float(t.item())
+    te = max_over_ranks(te, dist)
     h2d, d2h = ctx.transfer_bytes()
     clocks = clk.stop()
-    e2e = B * args.steps * world / te
+    e2e = throughput(B, args.steps, world, te)
     # ---- roofline of the dominant kernel
     hbm, bf16, src = peaks()
     alg = algorithmic(dm, L, sr, nv, descs)
