@@ -106,6 +106,8 @@ struct bbgpu_ctx {
     int *d_psbase = nullptr, *d_pssub = nullptr, *d_pwidx = nullptr, *d_pfix = nullptr, *d_pp = nullptr,
         *d_pstat = nullptr;
     size_t d_psbase_cap = 0, d_pssub_cap = 0, d_pwidx_cap = 0, d_pfix_cap = 0, d_pp_cap = 0, d_pstat_cap = 0;
+    float *d_pcsf = nullptr;
+    size_t d_pcsf_cap = 0;
     double *d_pcs = nullptr, *d_pzq = nullptr, *d_pwval = nullptr, *d_rap = nullptr, *d_gpart = nullptr,
            *d_gh = nullptr, *d_px = nullptr, *d_ppart = nullptr;
     size_t d_pcs_cap = 0, d_pzq_cap = 0, d_pwval_cap = 0, d_rap_cap = 0, d_gpart_cap = 0, d_gh_cap = 0,
@@ -388,7 +390,7 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
     cudaFree(ctx->d_err);
     for (void *q : {(void *)ctx->d_ppix, (void *)ctx->d_lc, (void *)ctx->d_ord, (void *)ctx->d_p0, (void *)ctx->d_ent,
                     (void *)ctx->d_pw, (void *)ctx->d_pwy, (void *)ctx->d_lv, (void *)ctx->d_near, (void *)ctx->d_psub,
-                    (void *)ctx->d_psbase, (void *)ctx->d_pssub, (void *)ctx->d_pwidx, (void *)ctx->d_pfix,
+                    (void *)ctx->d_psbase, (void *)ctx->d_pssub, (void *)ctx->d_pcsf, (void *)ctx->d_pwidx, (void *)ctx->d_pfix,
                     (void *)ctx->d_pp, (void *)ctx->d_pstat, (void *)ctx->d_pcs, (void *)ctx->d_pzq,
                     (void *)ctx->d_pwval, (void *)ctx->d_rap, (void *)ctx->d_gpart, (void *)ctx->d_gh,
                     (void *)ctx->d_px, (void *)ctx->d_ppart, (void *)ctx->d_pzqf, (void *)ctx->d_pwqf,
@@ -672,7 +674,7 @@ static int profile_run(bbgpu_ctx *ctx) {
     const int nb = ctx->nb, n = ctx->pc.n;
     const long long per = bx.npix * bx.nrp;
     CK(cudaMemsetAsync(ctx->d_maps64, 0, sizeof(long long) * (size_t)nb * per, s));
-    launch_an_maps_fast(s, g, ctx->d_psub, ctx->nsm, ctx->d_psbase, ctx->d_pssub, ctx->d_pcs, ctx->pnsamp, nb,
+    launch_an_maps_fast(s, g, ctx->d_psub, ctx->nsm, ctx->d_psbase, ctx->d_pssub, ctx->d_pcs, ctx->d_pcsf, ctx->pnsamp, nb,
                         ctx->d_pzq, ctx->d_pzqf, ctx->d_pwqf, ctx->d_pwidx, ctx->d_pwvalf, bx, ctx->d_pfix,
                         ctx->d_maps64);
     CKL();
@@ -1355,6 +1357,10 @@ extern "C" int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *
         if ((rc = dgrow(ctx, &ctx->d_psbase, &ctx->d_psbase_cap, sbase.size()))) return rc;
         if ((rc = dgrow(ctx, &ctx->d_pssub, &ctx->d_pssub_cap, ssub.size()))) return rc;
         if ((rc = dgrow(ctx, &ctx->d_pcs, &ctx->d_pcs_cap, cs.size()))) return rc;
+        std::vector<float> csf;
+        bbh_an_samples_f32(cs, csf);
+        if ((rc = dgrow(ctx, &ctx->d_pcsf, &ctx->d_pcsf_cap, csf.size()))) return rc;
+        CK(cudaMemcpy(ctx->d_pcsf, csf.data(), sizeof(float) * csf.size(), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(ctx->d_psbase, sbase.data(), sizeof(int) * sbase.size(), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(ctx->d_pssub, ssub.data(), sizeof(int) * ssub.size(), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(ctx->d_pcs, cs.data(), sizeof(double) * cs.size(), cudaMemcpyHostToDevice));

@@ -466,6 +466,17 @@ static std::pair<int, int> zgrid_cached(ZgridCache &zc, std::vector<double> &tz,
     return v;
 }
 
+void bbh_an_samples_f32(const std::vector<double> &cs, std::vector<float> &csf) {
+    csf.resize(cs.size());
+    for (size_t q = 0; q + 1 < cs.size(); q += 2) {
+        float cx = (float)cs[q];
+        cx = cs[q] >= 0.0 ? fabsf(cx) : -fabsf(cx);    // (a negative value that rounds to -0 keeps its sign)
+        if (cs[q] < 0.0 && cx == 0.0f) cx = -1e-30f;
+        csf[q] = cx;
+        csf[q + 1] = (float)cs[q + 1];
+    }
+}
+
 int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0, int blo1, int bhi0, int bhi1,
                 const double *cd2i, int maps, const int64_t *widx, const double *wval, AnSub *out, ZgridCache &zc) {
 #define SR(r, i) sr[(size_t)(r) * nsub + (i)]
@@ -517,20 +528,27 @@ int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0,
             const double u = (kr + 0.5) / nrad;
             S.R[kr] = sqrt(r_inner * r_inner + 2.0 * g->radsep * R0 * u);
         }
-        S.P1 = (float)(S.spa / g->cdelt0);
-        S.P2 = (float)(S.cinc * S.cpa / g->cdelt0);
-        S.P3 = (float)(S.sinc * S.cpa / g->cdelt0);
-        S.Q1 = (float)(S.cpa / g->cdelt1);
-        S.Q2 = (float)(S.cinc * S.spa / g->cdelt1);
-        S.Q3 = (float)(-S.sinc * S.spa / g->cdelt1);
-        S.xposf = (float)S.xpos;
-        S.yposf = (float)S.ypos;
-        S.z0f = (float)S.z0;
+        {
+            auto split = [](double v, float &hi, float &lo) {
+                hi = (float)v;
+                lo = (float)(v - (double)hi);
+            };
+            split(S.spa / g->cdelt0, S.P1, S.P1l);
+            split(S.cinc * S.cpa / g->cdelt0, S.P2, S.P2l);
+            split(S.sinc * S.cpa / g->cdelt0, S.P3, S.P3l);
+            split(S.cpa / g->cdelt1, S.Q1, S.Q1l);
+            split(S.cinc * S.spa / g->cdelt1, S.Q2, S.Q2l);
+            split(-S.sinc * S.spa / g->cdelt1, S.Q3, S.Q3l);
+            split(S.xpos, S.xposf, S.xposl);
+            split(S.ypos, S.yposf, S.yposl);
+            split(S.z0, S.z0f, S.z0l);
+            split(S.R[0], S.Rf[0], S.Rl[0]);
+            split(S.R[1], S.Rf[1], S.Rl[1]);
+        }
+        S.wzero = (S.wrec == 0.0 ? 1 : 0) | (S.wapp == 0.0 ? 2 : 0);
         S.fluxscf = (float)S.fluxsc;
         S.wrecf = (float)S.wrec;
         S.wappf = (float)S.wapp;
-        S.Rf[0] = (float)S.R[0];
-        S.Rf[1] = (float)S.R[1];
         if (!S.active) continue;
         // every deposit of the sub-ring is at most |fluxsc| x |wside| x (line: sum of relint x max cd2i; map:
         // max wval) per sample, the vertical weights and the channel profile summing to at most 1

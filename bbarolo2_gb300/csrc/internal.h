@@ -42,7 +42,11 @@ struct AnSub {
     // x pixel = xposf + (R caz P1 - R saz P2) + z P3, y pixel = yposf + (R caz Q1 + R saz Q2) + z Q3
     float P1, P2, P3, Q1, Q2, Q3, xposf, yposf, z0f, fluxscf, wrecf, wappf;
     float Rf[2];
-    float pad_f[2];
+    // the float32 residuals of the same constants (value - float32 value): the float-float evaluation of the
+    // pixel (about 44 bits) when the float32 one is too close to a rounding boundary
+    float P1l, P2l, P3l, Q1l, Q2l, Q3l, xposl, yposl, z0l;
+    float Rl[2];
+    int wzero;                      // bit 0: wrec == 0, bit 1: wapp == 0 (the float64 tests, done on the host)
 };
 
 // The constants of a context, as the kernels see them.
@@ -98,6 +102,9 @@ int bbh_zgrid(double *zq, double *wq, int nmax, int ltype, double z0, double sin
 // cos/sin of its azimuth from the reference's rotation recurrence (bbarolo/galmod.py:384-391)
 void bbh_an_samples(const double *R0, int nsub, const GridDev *g, std::vector<int> &sbase, std::vector<int> &ssub,
                     std::vector<double> &cs);
+// float32 copy of cs with the half of each sample in the sign bit of its cosine: +0 / positive for caz >= 0
+// (receding half, the reference's test on the float64 value), negative for caz < 0
+void bbh_an_samples_f32(const std::vector<double> &cs, std::vector<float> &csf);
 // ANALYTIC: the AnSub of each sub-ring of a table (maps: ring-map mode, active where widx has a ring), their
 // vertical samples appended to zq/wq; returns the fixed-point exponent e (deposits in units of 2^-e) or
 // -10000 when the total flux is not finite

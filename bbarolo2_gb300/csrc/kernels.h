@@ -128,7 +128,7 @@ struct ProfConst {
     double smooth, corr, floor_, norm, d;
 };
 void launch_an_maps_fast(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase,
-                         const int *ssub, const double *cs, long long nsamp, int nb, const double *zq,
+                         const int *ssub, const double *cs, const float *csf, long long nsamp, int nb, const double *zq,
                          const float *zqf, const float *wqf, const int *widx, const float *wvalf, const ProfBox &box,
                          const int *fix_exp, long long *maps64);
 void launch_maps_to_f32(cudaStream_t s, const long long *in, const int *fix_exp, int nb, long long per_member,

@@ -36,16 +36,31 @@ namespace {
 
 __device__ __forceinline__ bool round_fast(float v, float eps, int &out) {
     if (!(fabsf(v) < 1.0e6f)) return false;
-    const float f = v + 0.5f;
-    const float fl = floorf(f);
-    const float d = f - fl;
+    const float f = __fadd_rn(v, 0.5f);
+    float fl;
+    const int i = floor_small(f, fl);
+    const float d = __fsub_rn(f, fl);
     if (d < eps || d > 1.0f - eps) return false;
-    out = (int)fl;
+    out = i;
     return true;
 }
 
 __device__ __forceinline__ int clamp_pix(long long v) {
     return v < -(1LL << 30) ? -(1 << 30) : (v > (1LL << 30) ? (1 << 30) : (int)v);
+}
+
+// The pixel of a sample at height zq z0 in float-float (x = xpos + R caz P1 - R saz P2 + z P3, y likewise);
+// false if either coordinate is within 1e-6 of a rounding boundary.
+__device__ __noinline__ bool pixel_ff(const AnSub &S, int kr, double2 c, double zq, int &g0, int &g1) {
+    const ff R = {S.Rf[kr], S.Rl[kr]};
+    const ff A = ff_mul(R, ff_of(c.x)), B = ff_mul(R, ff_of(c.y));
+    const ff z = ff_mul(ff_of(zq), ff{S.z0f, S.z0l});
+    const ff T2 = ff_mul(B, ff{S.P2, S.P2l});
+    const ff x = ff_add(ff_add(ff_add(ff{S.xposf, S.xposl}, ff_mul(A, ff{S.P1, S.P1l})), ff{-T2.hi, -T2.lo}),
+                        ff_mul(z, ff{S.P3, S.P3l}));
+    const ff y = ff_add(ff_add(ff_add(ff{S.yposf, S.yposl}, ff_mul(A, ff{S.Q1, S.Q1l})), ff_mul(B, ff{S.Q2, S.Q2l})),
+                        ff_mul(z, ff{S.Q3, S.Q3l}));
+    return ff_round(x, g0) && ff_round(y, g1);
 }
 
 // ------------------------------------------------------------------------------------------- ring maps
@@ -62,7 +77,8 @@ __device__ __forceinline__ int clamp_pix(long long v) {
 
 __global__ void __launch_bounds__(256) k_an_maps_fast(GridDev g, const AnSub *__restrict__ subs, int nsub,
                                                       const int *__restrict__ sbase, const int *__restrict__ ssub,
-                                                      const double2 *__restrict__ cs, long long nsamp, int nb,
+                                                      const double2 *__restrict__ cs, const float2 *__restrict__ csf,
+                                                      long long nsamp, int nb,
                                                       const double *__restrict__ zq, const float *__restrict__ zqf,
                                                       const float *__restrict__ wqf, const int *__restrict__ widx,
                                                       const float *__restrict__ wvalf, ProfBox box,
@@ -76,12 +92,13 @@ __global__ void __launch_bounds__(256) k_an_maps_fast(GridDev g, const AnSub *__
     const AnSub &S = subs[(size_t)k * nsub + ir];
     if (!S.active) return;
     const int kr = (int)(s - sbase[ir]) >= S.naz ? 1 : 0;
-    const double2 c = cs[s];
-    const bool rec = c.x >= 0.0;
-    if ((rec ? S.wrec : S.wapp) == 0.0) return;
+    const float2 cf = csf[s];
+    const float cxf = cf.x, cyf = cf.y;
+    const bool rec = cxf >= 0.0f;                    // (the sign of the float32 table is the float64 test's)
+    if (S.wzero & (rec ? 1 : 2)) return;
     const float wsidef = rec ? S.wrecf : S.wappf;
     const float Rf = S.Rf[kr];
-    const float a1 = Rf * (float)c.x, a2 = Rf * (float)c.y;
+    const float a1 = Rf * cxf, a2 = Rf * cyf;
     const float t1 = a1 * S.P1, t2 = a2 * S.P2, u1 = a1 * S.Q1, u2 = a2 * S.Q2;
     const float bxf = S.xposf + (t1 - t2), byf = S.yposf + (u1 + u2);
     const float xa = fabsf(S.xposf) + fabsf(t1) + fabsf(t2) + 1.0f, ya = fabsf(S.yposf) + fabsf(u1) + fabsf(u2) + 1.0f;
@@ -96,11 +113,11 @@ __global__ void __launch_bounds__(256) k_an_maps_fast(GridDev g, const AnSub *__
         if (g0 < box.blo0 || g0 >= box.bhi0 || g1 < box.blo1 || g1 >= box.bhi1) return;
         unsigned long long *o = out + ((size_t)(g1 - box.blo1) * box.bx + (size_t)(g0 - box.blo0)) * box.nrp;
         if (i0 >= 0) {
-            const long long q = (long long)rintf(v0 * ws);
+            const long long q = f32_to_ll(v0 * ws);
             if (q) atomicAdd(o + i0, (unsigned long long)q);
         }
         if (i1 >= 0) {
-            const long long q = (long long)rintf(v1 * ws);
+            const long long q = f32_to_ll(v1 * ws);
             if (q) atomicAdd(o + i1, (unsigned long long)q);
         }
     };
@@ -111,8 +128,10 @@ __global__ void __launch_bounds__(256) k_an_maps_fast(GridDev g, const AnSub *__
         const float t3 = zf * P3, u3 = zf * Q3;
         int g0, g1;
         if (!(round_fast(bxf + t3, (xa + fabsf(t3)) * MAPS_EPS, g0) &&
-              round_fast(byf + u3, (ya + fabsf(u3)) * MAPS_EPS, g1))) {
+              round_fast(byf + u3, (ya + fabsf(u3)) * MAPS_EPS, g1)) &&
+            !pixel_ff(S, kr, cs[s], nzz > 1 ? zq[off + kz] : 0.0, g0, g1)) {
             // bbarolo/galmod.py:514-517 in the reference's float64 operations
+            const double2 c = cs[s];
             const double R = S.R[kr];
             const double x = __dmul_rn(R, c.x);
             const double yb = __dmul_rn(__dmul_rn(R, c.y), S.cinc);
@@ -145,7 +164,7 @@ __global__ void k_maps_to_f32(const long long *__restrict__ in, const int *__res
     float *dst = out + (size_t)k * per_member;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < per_member;
          i += (long long)gridDim.x * blockDim.x)
-        dst[i] = (float)src[i] * sc;
+        dst[i] = ll_to_f32(src[i]) * sc;
 }
 
 // ------------------------------------------------------------------------------------------- Gram matrix
@@ -578,13 +597,14 @@ __global__ void k_mc_dens(GridDev g, SubMC *__restrict__ sub, int nsub, MemberDe
 }  // namespace
 
 void launch_an_maps_fast(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase,
-                         const int *ssub, const double *cs, long long nsamp, int nb, const double *zq,
+                         const int *ssub, const double *cs, const float *csf, long long nsamp, int nb, const double *zq,
                          const float *zqf, const float *wqf, const int *widx, const float *wvalf, const ProfBox &box,
                          const int *fix_exp, long long *maps64) {
     const long long nw = nsamp * nb;
     if (nw == 0) return;
     k_an_maps_fast<<<(unsigned)((nw + 255) / 256), 256, 0, s>>>(
-        g, subs, nsub, sbase, ssub, (const double2 *)cs, nsamp, nb, zq, zqf, wqf, widx, wvalf, box, fix_exp,
+        g, subs, nsub, sbase, ssub, (const double2 *)cs, (const float2 *)csf, nsamp, nb, zq, zqf, wqf, widx, wvalf, box,
+        fix_exp,
         (unsigned long long *)maps64);
 }
 
