@@ -125,6 +125,28 @@ def workload(batch):
     return dm, L, rings, rows, data, mask
 
 
+# ncu summaries (profiles/) with the DRAM traffic of a kernel's launch at the default batch
+TRAFFIC = {"mc_deposit": "k_mc_deposit_lean.global160_b161.dram.txt"}
+
+
+def measured_traffic(kernel, batch):
+    """DRAM bytes (read + write) of one launch of the kernel at this batch, from its committed ncu summary, or
+    None (not captured at this batch)."""
+    name = TRAFFIC.get(kernel)
+    if not name:
+        return None
+    try:
+        vals = {}
+        with open(os.path.join(ROOT, "profiles", name)) as f:
+            for line in f:
+                if "=" in line and not line.startswith(" "):
+                    k, v = line.split("=", 1)
+                    vals[k.strip()] = v.strip()
+        return int(vals["traffic_bytes_per_launch"]) if int(vals["batch"]) == batch else None
+    except (OSError, KeyError, ValueError):
+        return None
+
+
 def max_over_ranks(t, dist):
     """The largest of the ranks' times (replicas: the job ends with the slowest rank); t on one rank without
     torch.distributed. NCCL reduces a CUDA tensor, gloo a CPU one."""
@@ -265,7 +287,8 @@ def main():
         nbytes = alg["mc_deposit"][1] if dom == "mc_deposit" else alg["conv_bytes"]
         achieved = nbytes / (kt[dom] * 1e-3) / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                "traffic": None, "kernel": dom, "peak_source": src}
+                "traffic": measured_traffic(dom, B), "kernel": dom, "peak_source": src,
+                "algorithmic_bytes": nbytes}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (f64 reduction; bit-exact int cloud indices)", "data": "synthetic",
