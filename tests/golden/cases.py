@@ -79,3 +79,15 @@ def case(name):
         if nm == name:
             return cube, rings, mode
     raise KeyError(name)
+
+
+def galfit_par():
+    """The 3DFIT parameters of the CLASSIC fit fixture: the defaults of bbarolo/params.py, FREE "VROT VDISP",
+    one stage, no errors."""
+    import types
+    return types.SimpleNamespace(FREE="VROT VDISP", DELTAVROT=1000.0, MINVDISP=0.1, MAXVDISP=1000.0, DELTAINC=5.0,
+                                 DELTAPHI=15.0, TOL=1e-3, FTYPE=2, WFUNC=2, SIDE="B", BWEIGHT=1.0, NORM="AZIM",
+                                 NORMALCUBE=True, TWOSTAGE=False, flagERRORS=False, STARTRAD=0, DENSFLUX=True,
+                                 CDENS=10, CMODE=1, ISEED=1, LTYPE=1, NV=-1, REDSHIFT=0.0, EMPTY=True,
+                                 RESTWAVE=[-1.0], RESTFREQ=[-1.0], RELINT=[1.0], SM=True, RADMAXA=-1.0,
+                                 RADMAXR=-1.0)

@@ -80,7 +80,7 @@ def gen_rng():
 
 
 # ---------------------------------------------------------------------------------------------- cases
-from cases import cube64, rings64, mc_cases, subring_cases  # noqa: E402
+from cases import cube64, galfit_par, rings64, mc_cases, subring_cases  # noqa: E402
 
 
 def run_model(galmodtype, case):
@@ -227,12 +227,17 @@ def gen_classic():
     ihi = np.full(ky, kx // 2, np.int64)
     arrays["norm/ilo"], arrays["norm/ihi"] = ilo, ihi
     x0, y0 = 32. - blo[0], 32. - blo[1]
+    r1, r2 = 3.5, 8.0                  # (pixels: the annulus of the rings in the 17 x 17 box)
+    # The kernel runs here as Python: a float32 scalar added to a Python float accumulator stays float32 under
+    # NumPy 2's promotion rules, where numba accumulates in float64. The data are therefore passed as float64
+    # (exact conversions): the numba kernel's arithmetic on the float32 data.
+    data64 = data_T.astype(np.float64)
     res = []
     for normtype in (0, 1, 2):
         for ftype in (1, 2, 3, 4):
             for wpow, side, foot in ((2., 0, 0), (1., 1, 0), (-1., 2, 0), (0., 0, 1)):
                 m = cs.copy()
-                v = gf._norm(m, data_T, mask_T, 0, 0, x0, y0, 45., 55., 25., 55., wpow, side, ftype,
+                v = gf._norm(m, data64, mask_T, 0, 0, x0, y0, 45., 55., r1, r2, wpow, side, ftype,
                              chan_noise, 0.001, 1.0, normtype, np.zeros((0, 0, 0)), np.zeros(0, np.int64),
                              np.zeros(0, np.int64), np.zeros(0), np.zeros((0, 0, 0)), foot, 4.0)
                 res.append([normtype, ftype, wpow, side, foot, 0, v, float(np.sum(m))])
@@ -241,12 +246,12 @@ def gen_classic():
     for normtype in (0, 1):
         m = cs.copy()
         P = np.zeros((ky, mod.shape[1] + 1, 64))
-        v = gf._norm(m, data_T, mask_T, 0, 0, x0, y0, 45., 55., 25., 55., 2., 0, 2, chan_noise, 0.001,
+        v = gf._norm(m, data64, mask_T, 0, 0, x0, y0, 45., 55., r1, r2, 2., 0, 2, chan_noise, 0.001,
                      1.0, normtype, mod, ilo, ihi, thr, P, 0, 4.0)
         res.append([normtype, 2, 2., 0, 0, 1, v, float(np.sum(m))])
     arrays["norm/thr"] = thr
     arrays["norm/results"] = np.array(res, float)
-    arrays["norm/meta"] = np.array(json.dumps(dict(blo=list(blo), bhi=list(bhi), x0=x0, y0=y0)))
+    arrays["norm/meta"] = np.array(json.dumps(dict(blo=list(blo), bhi=list(bhi), x0=x0, y0=y0, r1=r1, r2=r2)))
     save("classic.npz", **arrays)
 
 
@@ -338,9 +343,93 @@ def gen_profile():
     save("profile.npz", **arrays)
 
 
+# ---------------------------------------------------------------------------------------------- CLASSIC fit
+GALFIT_RINGS = (1, 2, 3)
+GALFIT_CROP = (12, 52)          # (the fits of these rings read the data in [12, 52)^2 only)
+
+
+def gen_galfit():
+    """The CLASSIC fit of single rings (bbarolo/galfit.py:736-1160: _fit_ring, minimize, _mtry, func3D,
+    getFuncValue, _norm_value; first stage, one thread, no REVERSE passes) on the 64^3 mock: the reference's
+    Galfit set up as Galfit.setup does, with the cube statistics given (the noise of the mock) and the VROT
+    band check left out (the cube of the fixture has no spectral-axis conversion). Recorded: each ring's fit
+    (converged, minimum, VROT, VDISP) and the sequence of its function values."""
+    import threading
+    gf = ns.galfit
+    cube, rings = configs.classic64()
+    dm = G.DiskModel(cube)
+    full = dm.array(rings, seed=1)
+    g = np.random.default_rng(1)
+    sigma = 0.01 * float(full.max())
+    data = (full + g.normal(0, sigma, full.shape)).astype(np.float32)
+    mask = full > 0.02 * full.max()
+    par = galfit_par()
+    inr = rings.copy()
+    inr.vrot = np.full(inr.nr, 120.)
+    inr.vdisp = np.full(inr.nr, 8.)
+    F = gf.Galfit()
+    F.cin, F.par, F.inr, F.verb = cube, par, inr.copy(), 0
+    F.arcconv = G.arcsconv(cube.Head().Cunit(0))
+    F.chan_noise = np.ones(cube.DimZ())
+    F.data_noise = sigma
+    F.wpow = par.WFUNC
+    F.setFree()
+    F.mask = mask
+    F.mask_T = np.ascontiguousarray(mask.transpose(1, 2, 0))
+    F.mask2D = mask.sum(axis=0).astype(np.int32)
+    F.norms = ["AZIM", "AZIM", "AZIM"]
+    P = gf
+    F.maxs, F.mins = np.zeros(P.MAXPAR), np.zeros(P.MAXPAR)
+    F.maxs[P.VROT] = inr.vrot.max() + par.DELTAVROT
+    F.mins[P.VROT] = max(inr.vrot.min() - par.DELTAVROT, 0)
+    F.maxs[P.VDISP], F.mins[P.VDISP] = par.MAXVDISP, par.MINVDISP
+    F.model = G.DiskModel(cube, par=par, densflux=True)
+    h = cube.Head()
+    F.pixScale = ((abs(h.Cdelt(0)) * F.arcconv) + (abs(h.Cdelt(1)) * F.arcconv)) / 2.
+    F._rngs, F._tls, F._ringstat = {}, threading.local(), {}
+    F._check_vrot = lambda ir: True
+    # galfit(): stage 1 with the data normalised (NORMALCUBE)
+    F.n_galfit = 1
+    F.outr = F.inr.copy()
+    scaling = 10. / float(data.max())
+    # (float64 copies of the float32 data: the arithmetic of the numba kernels, see gen_classic)
+    F.data_T = np.ascontiguousarray((data * scaling).astype(np.float32).transpose(1, 2, 0)).astype(np.float64)
+    F.data_noise = sigma * scaling
+    nr = inr.nr
+    errors = np.zeros((nr, 2, F.nfree))
+    fitok = [False] * nr
+    F._cstat = np.full(nr, F.CS_NONE)
+    F._pass = 0
+    calls = []
+    f3 = F.func3D
+
+    def counted(dring, zpar, ctx=None):
+        v = f3(dring, zpar, ctx)
+        calls[-1].append((float(zpar[0]), float(zpar[1]), float(v)))
+        return v
+    F.func3D = counted
+    res = []
+    for ir in GALFIT_RINGS:
+        calls.append([])
+        t0 = time.time()
+        F._fit_ring(ir, errors, fitok, 1)
+        st = F._ringstat.get(ir, ("", None))
+        res.append([ir, 1.0 if fitok[ir] else 0.0, st[1] if st[1] is not None else np.nan, F.outr.vrot[ir],
+                    F.outr.vdisp[ir], len(calls[-1])])
+        print(f"  ring {ir}: {res[-1]} ({time.time() - t0:.0f} s)")
+    a, b = GALFIT_CROP
+    arrays = dict(data=np.ascontiguousarray(data[:, a:b, a:b]), mask=np.ascontiguousarray(mask[:, a:b, a:b]),
+                  results=np.array(res, float), scaling=np.array(scaling), sigma=np.array(sigma))
+    for k, c in zip(GALFIT_RINGS, calls):
+        arrays[f"calls_{k}"] = np.array(c, float)
+    arrays["index"] = np.array(json.dumps(dict(crop=list(GALFIT_CROP), rings=list(GALFIT_RINGS),
+                                               par=vars(par), vrot0=120., vdisp0=8.)))
+    save("galfit.npz", **arrays)
+
+
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["rng", "subrings", "beam_conv", "residuals", "classic", "ringmaps", "models", "profile"]
+    which = sys.argv[1:] or ["rng", "subrings", "beam_conv", "residuals", "classic", "ringmaps", "models", "profile", "galfit"]
     for w in which:
         print(w)
         {"rng": gen_rng, "subrings": gen_subrings, "beam_conv": gen_beam_conv, "residuals": gen_residuals,
-         "classic": gen_classic, "ringmaps": gen_ringmaps, "models": gen_models, "profile": gen_profile}[w]()
+         "classic": gen_classic, "ringmaps": gen_ringmaps, "models": gen_models, "profile": gen_profile, "galfit": gen_galfit}[w]()

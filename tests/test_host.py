@@ -116,3 +116,27 @@ def test_batch_boxes_match_model_box():
             lo = [max(lo[0], 7), max(lo[1], 3)]
             hi = [max(min(hi[0], 150), lo[0]), max(min(hi[1], 155), lo[1])]
             assert list(blo[k]) == lo and list(bhi[k]) == hi, (mode, k)
+
+
+def test_count_ring_pixels_matches_reference_rule():
+    """The annulus pixel count of a ring (``_count_ring_pixels``) on a box crossing the cube edge."""
+    from bbarolo2_gb300.galfit import _count_ring_pixels
+    m = np.zeros((30, 40), np.int32)
+    m[5:20, 10:35] = 3
+    nt, ni = _count_ring_pixels(m, 2, 3, 39, 32, 20.5, 12.0, 30., 50., 4., 9.)
+    # the same count written out pixel by pixel
+    import math
+    F = math.pi / 180.
+    sphi, cphi, cinc = math.sin(F * 30.), math.cos(F * 30.), math.cos(F * 50.)
+    t = i = 0
+    for y in range(3, 33):
+        for x in range(2, 40):
+            xx, yy = x - 2, y - 3
+            xr = -(xx - 20.5) * sphi + (yy - 12.0) * cphi
+            yr = (-(xx - 20.5) * cphi - (yy - 12.0) * sphi) / cinc
+            r = math.sqrt(xr * xr + yr * yr)
+            if 4. <= r <= 9.:
+                t += 1
+                if y < 30 and x < 40 and m[y, x] > 0:
+                    i += 1
+    assert (nt, ni) == (t, i)

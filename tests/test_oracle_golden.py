@@ -99,7 +99,7 @@ def test_classic_norm(oracle_lib):
         m = z["norm/model"].copy()
         pre = z["conv_sparse/model"] if trunc else None
         thr = z["norm/thr"] if trunc else np.zeros(0)
-        v = oracle_lib.norm(m, z["norm/data_T"], z["norm/mask_T"], 0, 0, meta["x0"], meta["y0"], 45., 55., 25., 55.,
+        v = oracle_lib.norm(m, z["norm/data_T"], z["norm/mask_T"], 0, 0, meta["x0"], meta["y0"], 45., 55., meta["r1"], meta["r2"],
                             wpow, int(side), int(ftype), z["norm/chan_noise"], 0.001, 1.0, int(normtype), pre,
                             ilo if trunc else np.zeros(0, np.int64), ihi if trunc else np.zeros(0, np.int64), thr,
                             None, int(foot), 4.0)
