@@ -527,7 +527,10 @@ __global__ void __launch_bounds__(256) k_mc_deposit(GridDev g, LayoutDev L, cons
 // The common case in a lean kernel: a linear channel map, one line, at most 128 samples per cloud (4 per
 // lane). Same entries, lists, staging and run-length deposit as k_mc_deposit; the rare clouds outside the
 // fast criteria go through the per-sample path.
-__global__ void __launch_bounds__(256, 2) k_mc_deposit_lean(GridDev g, LayoutDev L, const SubMC *__restrict__ sub,
+#ifndef LEAN_MINB
+#define LEAN_MINB 3       // resident CTAs per SM of the lean deposit (registers: 65536 / (256 x LEAN_MINB))
+#endif
+__global__ void __launch_bounds__(256, LEAN_MINB) k_mc_deposit_lean(GridDev g, LayoutDev L, const SubMC *__restrict__ sub,
                                                            int nsub, const MemberDev *__restrict__ mem, int tx, int ty,
                                                            const int *__restrict__ offset,
                                                            const int *__restrict__ count,
