@@ -53,14 +53,20 @@ __global__ void __launch_bounds__(256) k_conv_resid(GridDev g, const MemberDev *
         for (int i = threadIdx.x; i < ky * KXW; i += blockDim.x) sk[i] = taps[i];
     const float *mk = model + (size_t)k * mstride;
     int any = 0;
-    for (int q = warp; q < H * W; q += NW) {
-        const int r = q / W, col = q - r * W;
-        const int yy = y0 - hy + r, xx = x0 - hx + col;
-        float v = 0.0f;
-        if (zok && col < TO + kx_eff - 1 && yy >= 0 && yy < M.by && xx >= 0 && xx < M.bx)
-            v = mk[((size_t)yy * M.bx + xx) * nz + z];
-        S[(size_t)q * ZB + lane] = v;
-        any |= v != 0.0f;
+    // (rows of the input tile by warp, columns in order: no index division)
+    for (int r = warp; r < H; r += NW) {
+        const int yy = y0 - hy + r;
+        const bool rok = zok && yy >= 0 && yy < M.by;
+        const float *src = mk + ((size_t)(rok ? yy : 0) * M.bx) * nz + z;
+        float *dst = S + (size_t)r * W * ZB + lane;
+#pragma unroll 4
+        for (int col = 0; col < W; col++) {
+            const int xx = x0 - hx + col;
+            float v = 0.0f;
+            if (rok && col < TO + kx_eff - 1 && xx >= 0 && xx < M.bx) v = src[(size_t)xx * nz];
+            dst[col * ZB] = v;
+            any |= v != 0.0f;
+        }
     }
     const int nonempty = __syncthreads_or(any);
     float acc[2][TO];

@@ -13,6 +13,26 @@
 
 #include "internal.h"
 
+#include <unordered_map>
+
+// sin and cos of an angle from the C library, remembered per value: a batch repeats the inclinations and
+// position angles of its members' sub-rings (the values are the library's, computed once each).
+static void sincos_memo(double x, double &s, double &c) {
+    thread_local std::unordered_map<uint64_t, std::pair<double, double>> memo;
+    uint64_t key;
+    memcpy(&key, &x, sizeof key);
+    auto it = memo.find(key);
+    if (it != memo.end()) {
+        s = it->second.first;
+        c = it->second.second;
+        return;
+    }
+    s = sin(x);
+    c = cos(x);
+    if (memo.size() > 65536) memo.clear();
+    memo.emplace(key, std::make_pair(s, c));
+}
+
 namespace {
 
 // ---------------------------------------------------------------- ziggurat tables (bbarolo/_rng.py:17-38)
@@ -261,10 +281,13 @@ int bbh_submc(const double *sr, int nsub, const int *nc, const int *nv, const Gr
         S.vdisptmp = sqrt(R_(4) * R_(4) + g->sig_instr * g->sig_instr);
         S.vrot = R_(1); S.vrad = R_(2); S.vvert = R_(3);
         S.z0 = R_(6); S.dvdz = R_(7); S.zcyl = R_(8);
-        S.sinc = sin(R_(9)); S.cinc = cos(R_(9));
+        sincos_memo(R_(9), S.sinc, S.cinc);
         double phi = R_(10);
-        S.spa = sin(phi) * cos(g->crota2) + cos(phi) * sin(g->crota2);
-        S.cpa = cos(phi) * cos(g->crota2) - sin(phi) * sin(g->crota2);
+        double sphi, cphi, scr, ccr;
+        sincos_memo(phi, sphi, cphi);
+        sincos_memo(g->crota2, scr, ccr);
+        S.spa = sphi * ccr + cphi * scr;
+        S.cpa = cphi * ccr - sphi * scr;
         S.xpos = R_(11); S.ypos = R_(12); S.vsys = R_(13);
         S.wrec = R_(14); S.wapp = R_(15);
 #undef R_
@@ -501,11 +524,13 @@ int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0,
         S.inv = 1.0 / sig;
         S.K = (long long)(5.0 * sig / g->chwidth) + 2;
         S.z0 = SR(6, ir); S.dvdz = SR(7, ir); S.zcyl = SR(8, ir);
-        S.sinc = sin(SR(9, ir));
-        S.cinc = cos(SR(9, ir));
+        sincos_memo(SR(9, ir), S.sinc, S.cinc);
         const double phi = SR(10, ir);
-        S.spa = sin(phi) * cos(g->crota2) + cos(phi) * sin(g->crota2);
-        S.cpa = cos(phi) * cos(g->crota2) - sin(phi) * sin(g->crota2);
+        double sphi, cphi, scr, ccr;
+        sincos_memo(phi, sphi, cphi);
+        sincos_memo(g->crota2, scr, ccr);
+        S.spa = sphi * ccr + cphi * scr;
+        S.cpa = cphi * ccr - sphi * scr;
         S.xpos = SR(11, ir); S.ypos = SR(12, ir); S.vsys = SR(13, ir);
         S.wrec = SR(14, ir); S.wapp = SR(15, ir);
         S.zq_off = 0;
