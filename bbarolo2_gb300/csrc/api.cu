@@ -606,7 +606,8 @@ static int batch_prepare(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const
         if (d.blo0 < 0 || d.blo1 < 0 || d.bhi0 > g.nx || d.bhi1 > g.ny || d.bhi0 < d.blo0 || d.bhi1 < d.blo1)
             return fail(ctx, BBGPU_ERR_ARG, "eval: member %d: box outside the cube", k);
         SubMC *S = ctx->h_sub + (size_t)k * nsub;
-        int e = bbh_submc(sr + (size_t)k * BBGPU_NSR * nsub, nsub, nc0.data(), nv0.data(), &g, S);
+        int e = bbh_submc(sr + (size_t)k * BBGPU_NSR * nsub, nsub, nc0.data(), nv0.data(), &g, S,
+                          k ? sr : nullptr, k ? ctx->h_sub : nullptr);
         MemberDev &M = ctx->mem_host[k];
         memset(&M, 0, sizeof M);
         M.blo0 = d.blo0; M.blo1 = d.blo1; M.bhi0 = d.bhi0; M.bhi1 = d.bhi1;
@@ -1342,7 +1343,8 @@ extern "C" int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *
     std::vector<int> fix(nb);
     for (int k = 0; k < nb; k++) {
         const int e = bbh_an_subs(sr_maps + (size_t)k * BBGPU_NSR * nsm, nsm, &g, nzq, bx.blo0, bx.blo1, bx.bhi0,
-                                  bx.bhi1, ctx->h_cd2i.data(), 1, widx, wval, ctx->h_psub + (size_t)k * nsm, zc);
+                                  bx.bhi1, ctx->h_cd2i.data(), 1, widx, wval, ctx->h_psub + (size_t)k * nsm, zc,
+                                  k ? sr_maps : nullptr, k ? ctx->h_psub : nullptr);
         if (e == -10000) return fail(ctx, BBGPU_ERR_ARG, "eval_upload_profile: member %d: weights not finite", k);
         fix[k] = std::min(e, 100);
     }

@@ -265,10 +265,28 @@ void bbh_cloud_counts(const double *sr, int nsub, const int64_t *nv_in, const Gr
 
 // The per-sub-ring constants of one member (bbarolo/galmod.py:111-127 and the cloud loop's invariants).
 // Returns e: the deposits are fixed-point numbers in units of 2^-e.
-int bbh_submc(const double *sr, int nsub, const int *nc, const int *nv, const GridDev *g, SubMC *out) {
+// true if sub-ring ir of the tables a and b (16 rows, nsub columns) holds the same values
+static bool same_column(const double *a, const double *b, int nsub, int ir) {
+    if (!b) return false;
+    for (int r = 0; r < BBGPU_NSR; r++)
+        if (memcmp(a + (size_t)r * nsub + ir, b + (size_t)r * nsub + ir, sizeof(double))) return false;
+    return true;
+}
+
+int bbh_submc(const double *sr, int nsub, const int *nc, const int *nv, const GridDev *g, SubMC *out,
+              const double *sr_ref, const SubMC *out_ref) {
     double bound = 0.;
     for (int ir = 0; ir < nsub; ir++) {
         SubMC &S = out[ir];
+        if (out_ref && same_column(sr, sr_ref, nsub, ir)) {     // (the values of another member: same constants)
+            S = out_ref[ir];
+            if (S.active) {
+                const double wmax = fmax(fabs(S.wrec), fabs(S.wapp));
+                for (int nl = 0; nl < g->nlines && nl < BBGPU_MAXL; nl++)
+                    bound += (double)nc[ir] * (double)nv[ir] * fabs(S.valrel[nl]) * wmax;
+            }
+            continue;
+        }
         memset(&S, 0, sizeof S);
 #define R_(row) sr[(size_t)(row) * nsub + ir]
         double R0 = R_(0), dens = R_(5);
@@ -501,7 +519,8 @@ void bbh_an_samples_f32(const std::vector<double> &cs, std::vector<float> &csf) 
 }
 
 int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0, int blo1, int bhi0, int bhi1,
-                const double *cd2i, int maps, const int64_t *widx, const double *wval, AnSub *out, ZgridCache &zc) {
+                const double *cd2i, int maps, const int64_t *widx, const double *wval, AnSub *out, ZgridCache &zc,
+                const double *sr_ref, const AnSub *out_ref) {
 #define SR(r, i) sr[(size_t)(r) * nsub + (i)]
     const int nb = nzq > 1 ? nzq : 1;
     std::vector<double> tz(nb), tw(nb);
@@ -511,6 +530,16 @@ int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0,
     for (int nl = 0; nl < g->nlines; nl++) lsum += fabs(g->relint[nl]);
     for (int ir = 0; ir < nsub; ir++) {
         AnSub &S = out[ir];
+        if (out_ref && same_column(sr, sr_ref, nsub, ir)) {     // (the values of another member: same constants)
+            S = out_ref[ir];
+            if (S.active) {
+                const double ws = std::max(fabs(S.wrec), fabs(S.wapp));
+                double per = lsum * cmax;
+                if (maps) per = std::max(fabs(wval[2 * ir]), fabs(wval[2 * ir + 1]));
+                bound += fabs(S.fluxsc) * ws * per * (double)((long long)S.naz * 2);
+            }
+            continue;
+        }
         memset(&S, 0, sizeof S);
         S.sub = ir;
         const double R0 = SR(0, ir), dens = SR(5, ir);
