@@ -21,10 +21,12 @@
 
 #define BBGPU_VERSION 1
 #define NLAYOUT 4
-#define NTIMER 7
+#define NTIMER 10
 
-static const char *KNAMES[NTIMER] = {"profile", "mc_bin", "scan_tiles", "mc_scatter", "mc_deposit", "conv_resid",
-                                     "reduce_partials"};
+// the timed stages of a batch: the flux normalisation (ring maps, their beam convolution, the normal equations,
+// the solves and the sub-ring densities), then the MC model, its convolution and the residual reduction
+static const char *KNAMES[NTIMER] = {"prof_maps", "prof_conv", "prof_gram", "prof_solve", "mc_bin", "scan_tiles",
+                                     "mc_scatter", "mc_deposit", "conv_resid", "reduce_partials"};
 
 struct LayoutEntry {
     LayoutHost host;
@@ -668,7 +670,7 @@ static int batch_prepare(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const
 
 // The flux normalisation of the batch (bbarolo/bayesian/likelihood.py:595-596): ring maps, beam convolution,
 // normal equations, the profile solve and the densities of the model's sub-rings, all on the device.
-static int profile_run(bbgpu_ctx *ctx) {
+static int profile_run(bbgpu_ctx *ctx, bool tm) {
     const GridDev &g = ctx->g;
     cudaStream_t s = ctx->stream;
     const ProfBox &bx = ctx->pbox;
@@ -681,22 +683,26 @@ static int profile_run(bbgpu_ctx *ctx) {
     CKL();
     launch_maps_to_f32(s, ctx->d_maps64, ctx->d_pfix, nb, per, (float)ctx->mapscale, ctx->d_maps32);
     CKL();
+    if (tm) CK(cudaEventRecord(ctx->ev[1], s));
     if (ctx->kernel_set) {
         launch_conv_resid(s, g, ctx->d_pmem, ctx->pmem_host.data(), nb, ctx->d_maps32, per, bx.nrp, ctx->d_taps,
                           ctx->ky, ctx->kx, ctx->kxw, ctx->d_K, 2, 0, ctx->d_ppart);
         CKL();
     }
+    if (tm) CK(cudaEventRecord(ctx->ev[2], s));
     const float *K = ctx->kernel_set ? ctx->d_K : ctx->d_maps32;
     launch_prof_gram(s, K, bx, ctx->d_ppix, ctx->d_pw, ctx->d_pwy, ctx->npix_used, ctx->d_ent, ctx->d_ent + ctx->nent,
                      ctx->nent, nb, ctx->d_gpart, ctx->d_gh);
     ctx->launches += 2;
     CKL();
+    if (tm) CK(cudaEventRecord(ctx->ev[3], s));
     launch_prof_solve(s, ctx->d_gh, ctx->pc, ctx->d_lc, ctx->d_lv, ctx->d_ord, ctx->d_near, ctx->d_p0, nb, ctx->d_px,
                       ctx->d_pp, ctx->d_pstat);
     CKL();
     launch_mc_dens(s, g, ctx->d_sub, ctx->nsub, ctx->d_mem, nb, ctx->d_px, n, ctx->d_pwidx, ctx->d_pwval, ctx->d_rap,
                    ctx->d_err);
     CKL();
+    if (tm) CK(cudaEventRecord(ctx->ev[4], s));
     (void)per;
     return 0;
 }
@@ -709,27 +715,28 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
     const bool tm = ctx->timing;
     if (tm) CK(cudaEventRecord(ctx->ev[0], s));
     if (ctx->prof_uploaded) {
-        int rc = profile_run(ctx);
+        int rc = profile_run(ctx, tm);
         if (rc) return rc;
+    } else if (tm) {
+        for (int i = 1; i <= 4; i++) CK(cudaEventRecord(ctx->ev[i], s));
     }
-    if (tm) CK(cudaEventRecord(ctx->ev[1], s));
     CK(cudaMemsetAsync(ctx->d_tcount, 0, sizeof(int) * (size_t)(ctx->ntile_total * NOWN + 1), s));
     launch_mc_bin(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->nb, ctx->tx, ctx->ty, ctx->d_pix, ctx->d_tcount,
                   ctx->d_err);
     CKL();
-    if (tm) CK(cudaEventRecord(ctx->ev[2], s));
+    if (tm) CK(cudaEventRecord(ctx->ev[5], s));
     launch_scan_tiles(s, ctx->d_tcount, ctx->d_toff, ctx->d_tcur, ctx->ntile_total * NOWN, ctx->d_scan);
     CKL();
-    if (tm) CK(cudaEventRecord(ctx->ev[3], s));
+    if (tm) CK(cudaEventRecord(ctx->ev[6], s));
     launch_mc_scatter(s, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->nb, ctx->tx, ctx->ty, ctx->d_pix, ctx->d_tcur,
                       ctx->d_bucket);
     CKL();
-    if (tm) CK(cudaEventRecord(ctx->ev[4], s));
+    if (tm) CK(cudaEventRecord(ctx->ev[7], s));
     launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->tx, ctx->ty,
                       ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig, ctx->d_cd2if, ctx->d_cd2i,
                       ctx->d_model, ctx->mstride, ctx->want64 ? ctx->d_model64 : nullptr, ctx->d_err, ctx->lean);
     CKL();
-    if (tm) CK(cudaEventRecord(ctx->ev[5], s));
+    if (tm) CK(cudaEventRecord(ctx->ev[8], s));
     const bool conv = ctx->kernel_set;
     if (do_resid || ctx->keep_smoothed) {
         launch_conv_resid(s, g, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->d_model, ctx->mstride, g.nz,
@@ -737,14 +744,14 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
                           conv ? 1 : 0, do_resid ? 1 : 0, ctx->d_partial);
         CKL();
     }
-    if (tm) CK(cudaEventRecord(ctx->ev[6], s));
+    if (tm) CK(cudaEventRecord(ctx->ev[9], s));
     if (do_resid) {
         launch_reduce_partials(s, ctx->d_partial, ctx->npart, ctx->nb, ctx->d_out2);
         CKL();
     }
     if (tm) {
-        CK(cudaEventRecord(ctx->ev[7], s));
-        CK(cudaEventSynchronize(ctx->ev[7]));
+        CK(cudaEventRecord(ctx->ev[10], s));
+        CK(cudaEventSynchronize(ctx->ev[10]));
         for (int i = 0; i < NTIMER; i++) {
             float ms = 0.f;
             cudaEventElapsedTime(&ms, ctx->ev[i], ctx->ev[i + 1]);

@@ -22,12 +22,23 @@ constexpr int TO = 16;        // output tile side (pixels)
 constexpr int ZB = 32;        // channels per CTA (one per lane)
 constexpr int NW = 8;         // warps per CTA: two output rows each
 
+// cp.async of 16 (or 4) bytes into shared memory; src_size 0 fills the destination with zeros (the halo
+// outside the box), without reading the source.
+__device__ __forceinline__ void cp_async_zfill16(float *dst, const float *src, bool ok) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(ok ? 16 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_zfill4(float *dst, const float *src, bool ok) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(ok ? 4 : 0) : "memory");
+}
+
 template <int KXW>
-__global__ void __launch_bounds__(256) k_conv_resid(GridDev g, const MemberDev *__restrict__ mem,
-                                                    const float *__restrict__ model, long long mstride, int nz,
-                                                    const float *__restrict__ taps, int ky, int kx,
-                                                    float *__restrict__ smoothed, int do_conv, int do_resid,
-                                                    double *__restrict__ partial, int npart) {
+__global__ void __launch_bounds__(256, 2) k_conv_resid(GridDev g, const MemberDev *__restrict__ mem,
+                                                       const float *__restrict__ model, long long mstride, int nz,
+                                                       const float *__restrict__ taps, int ky, int kx,
+                                                       float *__restrict__ smoothed, int do_conv, int do_resid,
+                                                       double *__restrict__ partial, int npart) {
     extern __shared__ float sm[];
     constexpr int W = TO + KXW - 1;
     const int k = blockIdx.x;
@@ -42,7 +53,7 @@ __global__ void __launch_bounds__(256) k_conv_resid(GridDev g, const MemberDev *
     }
     const int ky_eff = do_conv ? ky : 1, kx_eff = do_conv ? kx : 1;
     const int hy = ky_eff / 2, hx = kx_eff / 2;
-    const int H = TO + ky_eff - 1;
+    const int H = TO + ky_eff - 1, ncol = TO + kx_eff - 1;
     float *S = sm;                          // H x W x ZB
     float *sk = sm + (size_t)H * W * ZB;    // ky x KXW taps
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -52,23 +63,54 @@ __global__ void __launch_bounds__(256) k_conv_resid(GridDev g, const MemberDev *
     if (do_conv)
         for (int i = threadIdx.x; i < ky * KXW; i += blockDim.x) sk[i] = taps[i];
     const float *mk = model + (size_t)k * mstride;
-    int any = 0;
-    // (rows of the input tile by warp, columns in order: no index division)
-    for (int r = warp; r < H; r += NW) {
-        const int yy = y0 - hy + r;
-        const bool rok = zok && yy >= 0 && yy < M.by;
-        const float *src = mk + ((size_t)(rok ? yy : 0) * M.bx) * nz + z;
-        float *dst = S + (size_t)r * W * ZB + lane;
-#pragma unroll 4
-        for (int col = 0; col < W; col++) {
-            const int xx = x0 - hx + col;
-            float v = 0.0f;
-            if (rok && col < TO + kx_eff - 1 && xx >= 0 && xx < M.bx) v = src[(size_t)xx * nz];
-            dst[col * ZB] = v;
-            any |= v != 0.0f;
+    // the input tile with its halo, asynchronously: 16-byte copies of 4 channels when the rows of channels are
+    // 16-byte aligned (nz a multiple of 4), else 4-byte copies; zeros outside the box and past nz
+    const bool vec = (nz & 3) == 0 && (((uintptr_t)mk) & 15) == 0;
+    if (vec) {
+        for (int c = threadIdx.x; c < H * W * (ZB / 4); c += blockDim.x) {
+            const int q = c & (ZB / 4 - 1), rc = c / (ZB / 4);
+            const int r = rc / W, col = rc - r * W;
+            const int yy = y0 - hy + r, xx = x0 - hx + col, zz = zb * ZB + 4 * q;
+            const bool ok = col < ncol && yy >= 0 && yy < M.by && xx >= 0 && xx < M.bx && zz < nz;
+            cp_async_zfill16(S + (size_t)rc * ZB + 4 * q, ok ? mk + ((size_t)yy * M.bx + xx) * nz + zz : mk, ok);
+        }
+    } else {
+        for (int c = threadIdx.x; c < H * W * ZB; c += blockDim.x) {
+            const int l = c & (ZB - 1), rc = c / ZB;
+            const int r = rc / W, col = rc - r * W;
+            const int yy = y0 - hy + r, xx = x0 - hx + col, zz = zb * ZB + l;
+            const bool ok = col < ncol && yy >= 0 && yy < M.by && xx >= 0 && xx < M.bx && zz < nz;
+            cp_async_zfill4(S + c, ok ? mk + ((size_t)yy * M.bx + xx) * nz + zz : mk, ok);
         }
     }
-    const int nonempty = __syncthreads_or(any);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    // the data of this thread's output voxels, loaded while the tile arrives
+    const int ty0 = warp * 2;
+    float dv[2][TO];
+#pragma unroll
+    for (int rr = 0; rr < 2; rr++) {
+        const int y = y0 + ty0 + rr;
+#pragma unroll
+        for (int x = 0; x < TO; x++) {
+            const int xx = x0 + x;
+            dv[rr][x] = (do_resid && zok && y < M.by && xx < M.bx)
+                            ? __ldg(&M.deff[((size_t)(y + M.blo1) * g.nx + (xx + M.blo0)) * g.nz + z])
+                            : 0.0f;
+        }
+    }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    __syncthreads();
+    // all-zero input (empty channels, corners of the box): no convolution
+    unsigned any = 0;
+    if (vec) {
+        for (int c = threadIdx.x; c < H * W * (ZB / 4); c += blockDim.x) {
+            const uint4 v = *(const uint4 *)(S + (size_t)c * 4);
+            any |= (v.x | v.y | v.z | v.w) << 1;
+        }
+    } else {
+        for (int c = threadIdx.x; c < H * W * ZB; c += blockDim.x) any |= __float_as_uint(S[c]) << 1;
+    }
+    const int nonempty = __syncthreads_or(any != 0);
     float acc[2][TO];
 #pragma unroll
     for (int rr = 0; rr < 2; rr++)
@@ -76,26 +118,34 @@ __global__ void __launch_bounds__(256) k_conv_resid(GridDev g, const MemberDev *
         for (int x = 0; x < TO; x++) acc[rr][x] = 0.0f;
     if (nonempty) {
         if (do_conv) {
-            for (int a = 0; a < ky; a++) {
+            // input row ty0 + i feeds output row ty0 with kernel row i and output row ty0 + 1 with kernel row
+            // i - 1: each input row is read from shared memory once (the sums run over the kernel rows in order)
+            for (int i = 0; i <= ky; i++) {
+                const float *row = S + (size_t)((ty0 + i) * W) * ZB + lane;
+                float win[W];
 #pragma unroll
-                for (int rr = 0; rr < 2; rr++) {
-                    const int ty = warp * 2 + rr;
-                    const float *row = S + (size_t)((ty + a) * W) * ZB + lane;
-                    float win[W];
-#pragma unroll
-                    for (int j = 0; j < W; j++) win[j] = row[j * ZB];
+                for (int j = 0; j < W; j++) win[j] = row[j * ZB];
+                if (i < ky) {
 #pragma unroll
                     for (int b = 0; b < KXW; b++) {
-                        const float kv = sk[a * KXW + b];
+                        const float kv = sk[i * KXW + b];
 #pragma unroll
-                        for (int x = 0; x < TO; x++) acc[rr][x] = fmaf(kv, win[x + b], acc[rr][x]);
+                        for (int x = 0; x < TO; x++) acc[0][x] = fmaf(kv, win[x + b], acc[0][x]);
+                    }
+                }
+                if (i > 0) {
+#pragma unroll
+                    for (int b = 0; b < KXW; b++) {
+                        const float kv = sk[(i - 1) * KXW + b];
+#pragma unroll
+                        for (int x = 0; x < TO; x++) acc[1][x] = fmaf(kv, win[x + b], acc[1][x]);
                     }
                 }
             }
         } else {
 #pragma unroll
             for (int rr = 0; rr < 2; rr++) {
-                const int ty = warp * 2 + rr;
+                const int ty = ty0 + rr;
 #pragma unroll
                 for (int x = 0; x < TO; x++) acc[rr][x] = S[(size_t)(ty * W + x) * ZB + lane];
             }
@@ -117,7 +167,7 @@ __global__ void __launch_bounds__(256) k_conv_resid(GridDev g, const MemberDev *
             if (do_conv == 1) m = m < 1.0e-12f ? 0.0f : m * scale;
             if (smoothed) smoothed[(size_t)k * mstride + ((size_t)y * M.bx + xx) * nz + z] = m;
             if (do_resid) {
-                const float d = M.deff[((size_t)(y + M.blo1) * g.nx + (xx + M.blo0)) * g.nz + z];
+                const float d = dv[rr][x];
                 if (d == d) {
                     const float r = d - m;
                     if (fr && m != 0.0f) {

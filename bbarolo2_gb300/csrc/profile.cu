@@ -2,10 +2,11 @@
 // Bayesian3DFIT (bbarolo/bayesian/density.py:39-88, bbarolo/profile.py:33-138) for every member of a batch.
 //
 //   k_an_maps_fast   the total-intensity map of each ring with unit density (the ANALYTIC samples of
-//                    _ring_maps_analytic, bbarolo/galmod.py:468-536), one warp per (member, azimuth sample),
-//                    lanes over heights: pixels in float32 with a rounding bound (float64 near a boundary, so
-//                    every sample lands on the reference's pixel), run weights in float32, 64-bit fixed-point
-//                    sums (deterministic); maps (member, pixel, ring) ring-fastest in the likelihood box;
+//                    _ring_maps_analytic, bbarolo/galmod.py:468-536), one thread per (member, azimuth sample),
+//                    its heights in order: pixels in float32 with a rounding bound (float64 near a boundary, so
+//                    every sample lands on the reference's pixel), run weights in float32, runs queued in shared
+//                    memory and deposited by the whole warp, 64-bit fixed-point sums (deterministic); maps
+//                    (member, pixel, ring) ring-fastest in the likelihood box;
 //   k_maps_to_f32    x mean(cd2i) sum(relint) x scale factor, float32 (then the beam convolution of
 //                    k_conv_resid with the rings as channels);
 //   k_prof_gram      the normal equations of the weighted least squares: G = A^T A, h = A^T b over the pixels
@@ -73,86 +74,127 @@ __device__ __noinline__ bool pixel_ff(const AnSub &S, int kr, double2 c, double 
 // the reference's float64 value is within 1e-12 of it. MAPS_EPS = 16u (twice that bound): when the float32 value
 // lies within MAPS_EPS x (|xpos| + |t1| + |t2| + |t3| + 1) of a half-integer, the pixel is recomputed with the
 // reference's float64 operations.
+//
+// The finished runs of a thread wait in a shared-memory queue (pixel, weight) and are deposited by the whole
+// warp at once when a queue is full and at the end: the warp's loop over heights then carries no divergent
+// deposit code, and each drain pass keeps all lanes busy. The sums are 64-bit fixed point, so the order of
+// the deposits does not change the maps.
 #define MAPS_EPS 9.5367431640625e-07f
+#define MAPS_TB 128         // threads per CTA
+#define MAPS_QD 16          // queued runs per thread
 
-__global__ void __launch_bounds__(256) k_an_maps_fast(GridDev g, const AnSub *__restrict__ subs, int nsub,
-                                                      const int *__restrict__ sbase, const int *__restrict__ ssub,
-                                                      const double2 *__restrict__ cs, const float2 *__restrict__ csf,
-                                                      long long nsamp, int nb,
-                                                      const double *__restrict__ zq, const float *__restrict__ zqf,
-                                                      const float *__restrict__ wqf, const int *__restrict__ widx,
-                                                      const float *__restrict__ wvalf, ProfBox box,
-                                                      const int *__restrict__ fix_exp,
-                                                      unsigned long long *__restrict__ maps64) {
-    const long long gs = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gs >= nsamp * nb) return;
-    const int k = (int)(gs / nsamp);
-    const long long s = gs - (long long)k * nsamp;
-    const int ir = ssub[s];
-    const AnSub &S = subs[(size_t)k * nsub + ir];
-    if (!S.active) return;
-    const int kr = (int)(s - sbase[ir]) >= S.naz ? 1 : 0;
-    const float2 cf = csf[s];
-    const float cxf = cf.x, cyf = cf.y;
-    const bool rec = cxf >= 0.0f;                    // (the sign of the float32 table is the float64 test's)
-    if (S.wzero & (rec ? 1 : 2)) return;
-    const float wsidef = rec ? S.wrecf : S.wappf;
-    const float Rf = S.Rf[kr];
-    const float a1 = Rf * cxf, a2 = Rf * cyf;
-    const float t1 = a1 * S.P1, t2 = a2 * S.P2, u1 = a1 * S.Q1, u2 = a2 * S.Q2;
-    const float bxf = S.xposf + (t1 - t2), byf = S.yposf + (u1 + u2);
-    const float xa = fabsf(S.xposf) + fabsf(t1) + fabsf(t2) + 1.0f, ya = fabsf(S.yposf) + fabsf(u1) + fabsf(u2) + 1.0f;
-    const int nzz = S.nzz, off = S.zq_off;
-    const float z0f = S.z0f, P3 = S.P3, Q3 = S.Q3;
-    const int e = fix_exp[k];
-    const int i0 = widx[2 * ir], i1 = widx[2 * ir + 1];
-    const float v0 = i0 >= 0 ? ldexpf(S.fluxscf * wvalf[2 * ir] * wsidef, e) : 0.f;
-    const float v1 = i1 >= 0 ? ldexpf(S.fluxscf * wvalf[2 * ir + 1] * wsidef, e) : 0.f;
-    unsigned long long *out = maps64 + (size_t)k * box.npix * box.nrp;
-    auto emit = [&](int g0, int g1, float ws) {
-        if (g0 < box.blo0 || g0 >= box.bhi0 || g1 < box.blo1 || g1 >= box.bhi1) return;
-        unsigned long long *o = out + ((size_t)(g1 - box.blo1) * box.bx + (size_t)(g0 - box.blo0)) * box.nrp;
-        if (i0 >= 0) {
-            const long long q = f32_to_ll(v0 * ws);
-            if (q) atomicAdd(o + i0, (unsigned long long)q);
-        }
-        if (i1 >= 0) {
-            const long long q = f32_to_ll(v1 * ws);
-            if (q) atomicAdd(o + i1, (unsigned long long)q);
-        }
-    };
-    int rg0 = 0, rg1 = 0;
-    float rws = 0.f;
-    for (int kz = 0; kz < nzz; kz++) {
-        const float zf = nzz > 1 ? zqf[off + kz] * z0f : 0.f;
-        const float t3 = zf * P3, u3 = zf * Q3;
-        int g0, g1;
-        if (!(round_fast(bxf + t3, (xa + fabsf(t3)) * MAPS_EPS, g0) &&
-              round_fast(byf + u3, (ya + fabsf(u3)) * MAPS_EPS, g1)) &&
-            !pixel_ff(S, kr, cs[s], nzz > 1 ? zq[off + kz] : 0.0, g0, g1)) {
-            // bbarolo/galmod.py:514-517 in the reference's float64 operations
-            const double2 c = cs[s];
-            const double R = S.R[kr];
-            const double x = __dmul_rn(R, c.x);
-            const double yb = __dmul_rn(__dmul_rn(R, c.y), S.cinc);
-            const double z = nzz > 1 ? __dmul_rn(zq[off + kz], S.z0) : 0.0;
-            const double y = __dsub_rn(yb, __dmul_rn(z, S.sinc));
-            g0 = clamp_pix(lround_ref(
-                __dadd_rn(S.xpos, __ddiv_rn(__dsub_rn(__dmul_rn(x, S.spa), __dmul_rn(y, S.cpa)), g.cdelt0))));
-            g1 = clamp_pix(lround_ref(
-                __dadd_rn(S.ypos, __ddiv_rn(__dadd_rn(__dmul_rn(x, S.cpa), __dmul_rn(y, S.spa)), g.cdelt1))));
-        }
-        const float w = wqf[off + kz];
-        if (kz > 0 && g0 == rg0 && g1 == rg1) {
-            rws += w;
-        } else {
-            if (kz > 0) emit(rg0, rg1, rws);
-            rg0 = g0;
-            rg1 = g1;
-            rws = w;
+__global__ void __launch_bounds__(MAPS_TB) k_an_maps_fast(GridDev g, const AnSub *__restrict__ subs, int nsub,
+                                                          const int *__restrict__ sbase, const int *__restrict__ ssub,
+                                                          const double2 *__restrict__ cs,
+                                                          const float2 *__restrict__ csf, long long nsamp, int nb,
+                                                          const double *__restrict__ zq,
+                                                          const float *__restrict__ zqf,
+                                                          const float *__restrict__ wqf, const int *__restrict__ widx,
+                                                          const float *__restrict__ wvalf, ProfBox box,
+                                                          const int *__restrict__ fix_exp,
+                                                          unsigned long long *__restrict__ maps64) {
+    __shared__ uint2 runq[MAPS_QD][MAPS_TB];
+    const int tid = threadIdx.x;
+    const long long gs = (long long)blockIdx.x * MAPS_TB + tid;
+    // this thread's sample; nzz = 0: nothing to deposit (the thread still takes part in the warp's drains)
+    int k = 0, kr = 0, nzz = 0, off = 0, i0 = -1, i1 = -1;
+    long long s = 0;
+    const AnSub *S = subs;
+    float bxf = 0.f, byf = 0.f, xa = 0.f, ya = 0.f, z0f = 0.f, P3 = 0.f, Q3 = 0.f, v0 = 0.f, v1 = 0.f;
+    if (gs < nsamp * nb) {
+        k = (int)(gs / nsamp);
+        s = gs - (long long)k * nsamp;
+        const int ir = ssub[s];
+        S = subs + (size_t)k * nsub + ir;
+        const float2 cf = csf[s];
+        const bool rec = cf.x >= 0.0f;                // (the sign of the float32 table is the float64 test's)
+        if (S->active && !(S->wzero & (rec ? 1 : 2))) {
+            kr = (int)(s - sbase[ir]) >= S->naz ? 1 : 0;
+            const float wsidef = rec ? S->wrecf : S->wappf;
+            const float Rf = S->Rf[kr];
+            const float a1 = Rf * cf.x, a2 = Rf * cf.y;
+            const float t1 = a1 * S->P1, t2 = a2 * S->P2, u1 = a1 * S->Q1, u2 = a2 * S->Q2;
+            bxf = S->xposf + (t1 - t2);
+            byf = S->yposf + (u1 + u2);
+            xa = fabsf(S->xposf) + fabsf(t1) + fabsf(t2) + 1.0f;
+            ya = fabsf(S->yposf) + fabsf(u1) + fabsf(u2) + 1.0f;
+            nzz = S->nzz;
+            off = S->zq_off;
+            z0f = S->z0f;
+            P3 = S->P3;
+            Q3 = S->Q3;
+            const int e = fix_exp[k];
+            i0 = widx[2 * ir];
+            i1 = widx[2 * ir + 1];
+            v0 = i0 >= 0 ? ldexpf(S->fluxscf * wvalf[2 * ir] * wsidef, e) : 0.f;
+            v1 = i1 >= 0 ? ldexpf(S->fluxscf * wvalf[2 * ir + 1] * wsidef, e) : 0.f;
         }
     }
-    if (nzz > 0) emit(rg0, rg1, rws);
+    unsigned long long *out = maps64 + (size_t)k * box.npix * box.nrp;
+    int cnt = 0;
+    auto push = [&](int g0, int g1, float ws) {
+        const unsigned px = (unsigned)(g0 - box.blo0), py = (unsigned)(g1 - box.blo1);
+        if (px < (unsigned)box.bx && py < (unsigned)box.by) {
+            runq[cnt][tid] = make_uint2(py * (unsigned)box.bx + px, __float_as_uint(ws));
+            cnt++;
+        }
+    };
+    auto drain = [&]() {
+        const int m = __reduce_max_sync(FULL, cnt);
+        for (int j = 0; j < m; j++) {
+            if (j < cnt) {
+                const uint2 r = runq[j][tid];
+                unsigned long long *o = out + (size_t)r.x * box.nrp;
+                const float ws = __uint_as_float(r.y);
+                if (i0 >= 0) {
+                    const long long q = f32_to_ll(v0 * ws);
+                    if (q) atomicAdd(o + i0, (unsigned long long)q);
+                }
+                if (i1 >= 0) {
+                    const long long q = f32_to_ll(v1 * ws);
+                    if (q) atomicAdd(o + i1, (unsigned long long)q);
+                }
+            }
+        }
+        cnt = 0;
+    };
+    const int nzmax = __reduce_max_sync(FULL, nzz);
+    int rg0 = 0, rg1 = 0;
+    float rws = 0.f;
+    for (int kz = 0; kz < nzmax; kz++) {
+        if (kz < nzz) {
+            const float zf = nzz > 1 ? zqf[off + kz] * z0f : 0.f;
+            const float t3 = zf * P3, u3 = zf * Q3;
+            int g0, g1;
+            if (!(round_fast(bxf + t3, (xa + fabsf(t3)) * MAPS_EPS, g0) &&
+                  round_fast(byf + u3, (ya + fabsf(u3)) * MAPS_EPS, g1)) &&
+                !pixel_ff(*S, kr, cs[s], nzz > 1 ? zq[off + kz] : 0.0, g0, g1)) {
+                // bbarolo/galmod.py:514-517 in the reference's float64 operations
+                const double2 c = cs[s];
+                const double R = S->R[kr];
+                const double x = __dmul_rn(R, c.x);
+                const double yb = __dmul_rn(__dmul_rn(R, c.y), S->cinc);
+                const double z = nzz > 1 ? __dmul_rn(zq[off + kz], S->z0) : 0.0;
+                const double y = __dsub_rn(yb, __dmul_rn(z, S->sinc));
+                g0 = clamp_pix(lround_ref(
+                    __dadd_rn(S->xpos, __ddiv_rn(__dsub_rn(__dmul_rn(x, S->spa), __dmul_rn(y, S->cpa)), g.cdelt0))));
+                g1 = clamp_pix(lround_ref(
+                    __dadd_rn(S->ypos, __ddiv_rn(__dadd_rn(__dmul_rn(x, S->cpa), __dmul_rn(y, S->spa)), g.cdelt1))));
+            }
+            const float w = wqf[off + kz];
+            if (kz > 0 && g0 == rg0 && g1 == rg1) {
+                rws += w;
+            } else {
+                if (kz > 0) push(rg0, rg1, rws);
+                rg0 = g0;
+                rg1 = g1;
+                rws = w;
+            }
+        }
+        if (__any_sync(FULL, cnt == MAPS_QD)) drain();    // (at most one push per height: room for the next)
+    }
+    if (nzz > 0) push(rg0, rg1, rws);
+    drain();
 }
 
 // maps (member, pixel, ring) int64 units 2^-e -> float32 x scale
@@ -602,7 +644,7 @@ void launch_an_maps_fast(cudaStream_t s, const GridDev &g, const AnSub *subs, in
                          const int *fix_exp, long long *maps64) {
     const long long nw = nsamp * nb;
     if (nw == 0) return;
-    k_an_maps_fast<<<(unsigned)((nw + 255) / 256), 256, 0, s>>>(
+    k_an_maps_fast<<<(unsigned)((nw + MAPS_TB - 1) / MAPS_TB), MAPS_TB, 0, s>>>(
         g, subs, nsub, sbase, ssub, (const double2 *)cs, (const float2 *)csf, nsamp, nb, zq, zqf, wqf, widx, wvalf, box,
         fix_exp,
         (unsigned long long *)maps64);

@@ -278,7 +278,7 @@ def main():
     # ---- roofline of the dominant kernel
     hbm, bf16, src = peaks()
     alg = algorithmic(dm, L, sr, nv, descs)
-    dom = max((k for k in kt if k != "profile"), key=kt.get)     # (the profile stage is several kernels)
+    dom = max((k for k in kt if not k.startswith("prof_")), key=kt.get)   # (the MC model and its convolution)
     if dom == "conv_resid":
         achieved = alg["conv_resid"][1] / (kt[dom] * 1e-3) / 1e12
         roof = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16,

@@ -27,7 +27,7 @@ def test_exports_every_declared_symbol():
 def test_version_and_no_device_errors():
     L = _lib.load(build.build())
     assert L.bbgpu_version() >= 1
-    assert L.bbgpu_kernel_name(0) == b"profile" and L.bbgpu_kernel_name(1) == b"mc_bin"
+    assert L.bbgpu_kernel_name(0) == b"prof_maps" and L.bbgpu_kernel_name(4) == b"mc_bin"
     # a null context is rejected, not dereferenced
     assert L.bbgpu_set_kernel(None, None, 3, 3) == _lib.ERR_ARG
     assert L.bbgpu_eval_run(None) == _lib.ERR_ARG
