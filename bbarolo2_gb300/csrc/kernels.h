@@ -47,8 +47,10 @@ struct ZigDev {
 
 // ---- MC (mc.cu)
 // For every (member, cloud): its pixel in the member's box (or -1) and the count of clouds per tile.
-// Tile lists are split by owner warp (NOWN per tile): list index = (tile_off + tile) * NOWN + owner.
-#define NOWN 8
+// Tile lists are split by pixel (NOWN per tile, tiles of at most 64 pixels): list index = (tile_off + tile) * NOWN
+// + (lp % 8) * 8 + lp / 8 for pixel lp of the tile, so that the lists of the pixels lp = w (mod 8), owned by
+// warp w of the deposit, are contiguous.
+#define NOWN 64
 void launch_mc_bin(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
                    const MemberDev *mem, int nb, int tx, int ty, int *pix, int *tile_count, int *err);
 // Exclusive scan of n list counts into offsets (and cursors); scratch holds (n + 1023) / 1024 ints.

@@ -91,6 +91,18 @@ __device__ __forceinline__ bool cloud_pixel(const SubMC &S, const GridDev &g, co
     return ix >= M.blo0 && ix < M.bhi0 && iy >= M.blo1 && iy < M.bhi1;
 }
 
+// the list of pixel lp of a tile (see NOWN): the lists of warp w's pixels (lp = w mod 8) are contiguous
+__device__ __forceinline__ int list_slot(int lp) { return (lp & 7) * 8 + (lp >> 3); }
+
+// this warp's clouds in a tile: the concatenated lists of its pixels (begin, count)
+__device__ __forceinline__ void warp_lists(const int *__restrict__ offset, const int *__restrict__ count, int lbase,
+                                           int warp, int &beg, int &n) {
+    beg = offset[lbase + 8 * warp];
+    n = 0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) n += count[lbase + 8 * warp + j];
+}
+
 __global__ void k_mc_bin(GridDev g, LayoutDev L, const SubMC *__restrict__ sub, int nsub,
                          const MemberDev *__restrict__ mem, int nb, int tx, int ty, int *__restrict__ pix,
                          int *__restrict__ tile_count, int *err) {
@@ -115,8 +127,8 @@ __global__ void k_mc_bin(GridDev g, LayoutDev L, const SubMC *__restrict__ sub, 
     }
     int px = ix - M.blo0, py = iy - M.blo1;
     pix[idx] = py * M.bx + px;
-    const int owner = ((py % ty) * tx + (px % tx)) % NOWN;
-    atomicAdd(&tile_count[(M.tile_off + (py / ty) * M.ntx + px / tx) * NOWN + owner], 1);
+    const int lp = (py % ty) * tx + (px % tx);
+    atomicAdd(&tile_count[(M.tile_off + (py / ty) * M.ntx + px / tx) * NOWN + list_slot(lp)], 1);
 }
 
 // The deposit entry of a (member, cloud) in its tile's list: computed here, one thread per entry.
@@ -126,7 +138,7 @@ struct __align__(16) Entry {
     int meta;       // nv | pixel in the tile << 16 | half << 24
     float tc;       // channel of the cloud's velocity (line 0, float32 with the bound epsc)
     long long fix;  // fixed-point flux of one sample (line 0)
-    float epsc;     // rounding bound of tc
+    float eps;      // rounding bound of the float32 channel of every sample of the cloud (line 0)
     float sg;       // channels per unit normal deviate
 };
 
@@ -157,7 +169,7 @@ __global__ void k_mc_scatter(LayoutDev L, const SubMC *__restrict__ sub, int nsu
     const MemberDev &M = mem[k];
     int py = p / M.bx, px = p - py * M.bx;
     const int lp = (py % ty) * tx + (px % tx);
-    int slot = atomicAdd(&cursor[(M.tile_off + (py / ty) * M.ntx + px / tx) * NOWN + lp % NOWN], 1);
+    int slot = atomicAdd(&cursor[(M.tile_off + (py / ty) * M.ntx + px / tx) * NOWN + list_slot(lp)], 1);
     const float4 cf = L.cf[c];
     const int half = cf.y >= 0.0f ? 0 : 1;
     const int ir = L.sub[c];
@@ -167,9 +179,13 @@ __global__ void k_mc_scatter(LayoutDev L, const SubMC *__restrict__ sub, int nsu
     e.c = c;
     e.pb = (int)(L.pbase[ir] + (long long)(c - L.cloud_base[ir]) * ((nv + 3) & ~3));
     e.meta = (nv & 0xffff) | (lp << 16) | (half << 24);
-    cloud_centre(S, cf, 0, e.tc, e.epsc);
+    float epsc;
+    cloud_centre(S, cf, 0, e.tc, epsc);
     e.fix = S.fix[half][0];
     e.sg = S.sg[0];
+    // the cloud's largest |normal| is at an end of its sorted run
+    const float nmax = fmaxf(fabsf(__ldg(&L.nf[e.pb])), fabsf(__ldg(&L.nf[e.pb + nv - 1])));
+    e.eps = fmaf(nmax, fabsf(e.sg) * EPS_REL, epsc);
     bucket[slot] = e;
 }
 
@@ -422,8 +438,8 @@ __global__ void __launch_bounds__(256) k_mc_deposit(GridDev g, LayoutDev L, cons
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int lst = (M.tile_off + t) * NOWN + warp;              // this warp's list: the clouds of its pixels
-    const int beg = offset[lst], n = count[lst];
+    int beg, n;                                                  // this warp's list: the clouds of its pixels
+    warp_lists(offset, count, (M.tile_off + t) * NOWN, warp, beg, n);
     const bool fast_ok = g.fast_ok;
     const SubMC *__restrict__ subk = sub + (size_t)k * nsub;
     float *slots = stg + warp * DEPTH * WB;
@@ -462,17 +478,14 @@ __global__ void __launch_bounds__(256) k_mc_deposit(GridDev g, LayoutDev L, cons
         const int c = en.c;
         const int nv = en.meta & 0xffff, lp = (en.meta >> 16) & 255, half = en.meta >> 24;
         unsigned long long *row = tile + (size_t)lp * nz;
-        const float tc = en.tc, sg = en.sg, epsc = en.epsc;
+        const float tc = en.tc, sg = en.sg;
         const long long fix = en.fix;
-        const float epsn = fabsf(sg) * EPS_REL;
         const float span = 10.0f * fabsf(sg) + 2.0f;
         const int m = span <= 32.0f ? 1 : (span <= 64.0f ? 2 : 4);
         const bool fast = fast_ok && nv <= WB && fabsf(tc) < 1.0e5f;
         const int ws = fast ? (int)floorf(tc + 0.5f) - 16 * m : 0;
         if (fast) {
-            // one rounding bound for the cloud: its largest |normal| is at an end of the sorted run
-            const float nmax = fmaxf(fabsf(w[0]), fabsf(w[nv - 1]));
-            const float eps = fmaf(nmax, epsn, epsc);
+            const float eps = en.eps;
             const int E = (nv + 31) >> 5;
             if (E <= 1) deposit_runs<1>(g, L, zig, subk, w, c, (unsigned)en.pb, nv, tc, sg, eps, fix, row, lane, err);
             else if (E <= 2) deposit_runs<2>(g, L, zig, subk, w, c, (unsigned)en.pb, nv, tc, sg, eps, fix, row, lane, err);
@@ -578,7 +591,8 @@ __global__ void __launch_bounds__(256, LEAN_MINB) k_mc_deposit_lean(GridDev g, L
         for (int z = threadIdx.x; z < nz; z += blockDim.x) chs[z] = ldexpf(cd2if[z], -fe);
     }
     __syncthreads();
-    const int beg = offset[lbase + warp], n = count[lbase + warp];
+    int beg, n;
+    warp_lists(offset, count, lbase, warp, beg, n);
     float *slots = stg + warp * DEPTH * WB;
     int pa = lane < n ? __ldg(&bucket[beg + lane].pb) : 0, ma = lane < n ? __ldg(&bucket[beg + lane].meta) : 0;
     int pn = 32 + lane < n ? __ldg(&bucket[beg + 32 + lane].pb) : 0;
@@ -609,9 +623,7 @@ __global__ void __launch_bounds__(256, LEAN_MINB) k_mc_deposit_lean(GridDev g, L
         const long long fix = en.fix;
         if (nv <= 32 * E && fabsf(tc) < 1.0e5f) {
             const float4 nn = *(const float4 *)(w + 4 * lane);     // (zeros past nv: masked below)
-            const float nmax = fmaxf(fabsf(w[0]), fabsf(w[nv - 1]));
-            const float eps = fmaf(nmax, fabsf(sg) * EPS_REL, en.epsc);
-            const float hw = 0.5f - eps;
+            const float hw = 0.5f - en.eps;
             const int i0 = lane * E;
             const float nv4[4] = {nn.x, nn.y, nn.z, nn.w};
             int ch[E];
@@ -659,7 +671,7 @@ __global__ void __launch_bounds__(256, LEAN_MINB) k_mc_deposit_lean(GridDev g, L
         } else {
             const int ir = __ldg(&L.sub[en.c]);
             const SubMC &S = sub[(size_t)k * nsub + ir];
-            deposit_per_sample(g, L, zig, S, en.c, (unsigned)en.pb, stream_base(L, en.c, ir, nv), nv, tc, sg, en.epsc,
+            deposit_per_sample(g, L, zig, S, en.c, (unsigned)en.pb, stream_base(L, en.c, ir, nv), nv, tc, sg, en.eps,
                                fabsf(sg) * EPS_REL, fix, 0, true, row, bins[warp], bins[warp] + 128, lane, err);
         }
         __syncwarp();
@@ -684,6 +696,299 @@ __global__ void __launch_bounds__(256, LEAN_MINB) k_mc_deposit_lean(GridDev g, L
             const float lo = (float)(unsigned)(v & 0xffffffffLL);
             o[z] = (hi + lo) * chs[z];
         }
+    }
+}
+
+// A cloud of the pixel-owned deposit (nv = 0: none).
+struct PxCloud {
+    int c, pb, nv;
+    float tc, sg, eps;
+    long long fix;
+};
+
+__device__ __forceinline__ void px_entry(const Entry *__restrict__ bucket, int beg, int n, int j, PxCloud &p) {
+    if (j < n) {
+        const Entry en = bucket[beg + j];
+        p.c = en.c;
+        p.pb = en.pb;
+        p.nv = en.meta & 0xffff;
+        p.tc = en.tc;
+        p.sg = en.sg;
+        p.eps = en.eps;
+        p.fix = en.fix;
+    } else {
+        p.c = 0; p.pb = 0; p.nv = 0; p.tc = 0.0f; p.sg = 0.0f; p.eps = 0.0f; p.fix = 0;
+    }
+}
+
+// this lane's (up to) SPL sorted samples of the cloud, 16-byte loads (the runs are padded to 4 samples)
+template <int SPL>
+__device__ __forceinline__ void px_samples(const LayoutDev &L, const PxCloud &p, int i0, float4 (&w)[SPL / 4]) {
+    const float4 *src = (const float4 *)(L.nf + (unsigned)p.pb + i0);
+#pragma unroll
+    for (int s = 0; s < SPL / 4; s++)
+        w[s] = i0 + 4 * s < p.nv ? __ldg(src + s) : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// The exact channel of sample i of a cloud (its float32 channel was too close to a half-integer).
+__device__ __noinline__ int px_exact(const GridDev &g, const LayoutDev &L, const ZigDev *zig,
+                                     const SubMC *__restrict__ subk, int c, int pb, int nv, int i, int *err) {
+    const int ir = __ldg(&L.sub[c]);
+    const double nx = normal_exact(L, zig, stream_base(L, c, ir, nv), L.ord[(unsigned)pb + i], __ldg(&L.slow_base[c]),
+                                   err);
+    const long long is = channel_exact_raw(subk[ir], g, L.cd + 4 * (size_t)c, nx, 0);
+    return is < -0x3fffffffLL ? -0x3fffffff : (is > 0x3fffffffLL ? 0x3fffffff : (int)is);
+}
+
+// Run-length counting of one channel: a run that ends is added to the row, except the lane's first run, kept
+// in (fch, fcnt) (see k_mc_deposit_px).
+struct PxRuns {
+    int cur, cnt, fch, fcnt;
+    __device__ __forceinline__ void take(int ch, long long fix, int nz, unsigned long long *row) {
+        if (ch != cur) {
+            if (cur != (int)0x80000000) {
+                if (fch == (int)0x80000000) {
+                    fch = cur;
+                    fcnt = cnt;
+                } else if ((unsigned)cur < (unsigned)nz) {
+                    row[cur] += (unsigned long long)(fix * (long long)cnt);
+                }
+            }
+            cur = ch;
+            cnt = 0;
+        }
+        cnt++;
+    }
+};
+
+// A sample whose exact channel is deferred: added by the warp, with the other deferred samples, between clouds.
+struct __align__(16) PxDefer {
+    int c, pb, nv, i;       // cloud, its sorted normals, their count, the sample
+    long long fix;          // fixed-point flux of the sample
+    int row;                // its row in the tile (offset in sums)
+    int pad;
+};
+#define PX_QCAP 64          // deferred samples per warp (at most 32 join per cloud step)
+
+// The deferred samples of the warp: their exact channels (a lane each) added to the rows with shared-memory
+// atomics (two samples may share a channel); the queue is emptied.
+__device__ __forceinline__ void px_flush(const GridDev &g, const LayoutDev &L, const ZigDev *zig,
+                                         const SubMC *__restrict__ subk, PxDefer *qe, int *qn,
+                                         unsigned long long *tile, int lane, int *err) {
+    __syncwarp();
+    const int nq = *qn;
+    for (int b = 0; b < nq; b += 32) {
+        const int e = b + lane;
+        if (e < nq) {
+            const PxDefer x = qe[e];
+            const int ch = px_exact(g, L, zig, subk, x.c, x.pb, x.nv, x.i, err);
+            if ((unsigned)ch < (unsigned)g.nz) atomicAdd(tile + x.row + ch, (unsigned long long)x.fix);
+        }
+    }
+    __syncwarp();
+    if (lane == 0) *qn = 0;
+    __syncwarp();
+}
+
+// The channels of this lane's SPL samples counted into the pixel's row (see k_mc_deposit_px). The float32
+// channels are binned relative to c0 = (channel of the lane's first sample) - 1 into a register histogram of 12
+// five-bit counts (a bin holds at most 31 samples unless all 32 of a 32-sample lane share one channel, counted
+// apart); a sample too close to a half-integer is left out and deferred to the warp's queue. A lane with more
+// than one such sample, a channel beyond the 12 bins (the channels of the samples are non-decreasing, so the
+// last one tells) or a centre out of range counts its samples one by one, with the exact channels where needed.
+// The lowest non-empty bin (the lane's first run, which the previous lane may share) is added in the ordered
+// pass of the group's LPP lanes; the other bins at once.
+template <int SPL>
+__device__ __forceinline__ void px_count(const GridDev &g, const LayoutDev &L, const ZigDev *zig,
+                                         const SubMC *__restrict__ subk, const PxCloud &p, const float4 (&w)[SPL / 4],
+                                         int i0, int q, unsigned long long *tile, int rowoff, PxDefer *qe, int *qn,
+                                         int *err) {
+    constexpr int LPP = 128 / SPL;
+    const int nz = g.nz;
+    unsigned long long *row = tile + rowoff;
+    const int m = min(SPL, p.nv - i0);                      // this lane's samples (<= 0: none)
+    const bool fastc = fabsf(p.tc) < 1.0e5f;
+    const float hw = 0.5f - p.eps;
+    const float tc = p.tc, sg = p.sg;
+    const long long fix = p.fix;
+    const float fl0 = floorf(fmaf(w[0].x, sg, tc) + 0.5f) - 1.0f;
+    const float hwf = fastc ? hw : -1.0f;                  // (a centre out of range: no sample passes)
+    // straight-line code (selects, no branches): bins 0..5 in lo, 6..11 in hi, five bits each
+    unsigned lo = 0, hi = 0, need = 0;
+    int dlast = 0;
+#pragma unroll
+    for (int s = 0; s < SPL / 4; s++) {
+        const float vv[4] = {w[s].x, w[s].y, w[s].z, w[s].w};
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int i = 4 * s + e;
+            const float f = fmaf(vv[e], sg, tc) + 0.5f;
+            const float fl = floorf(f);
+            const bool in = i < m;
+            const bool ok = fabsf(f - fl - 0.5f) <= hwf;
+            const int d = __float_as_int((fl - fl0) + 12582912.0f) - 0x4B400000;   // (exact: small integers)
+            need |= (in & !ok) ? 1u << i : 0u;
+            const unsigned dd = (in & ok) ? (unsigned)d : 31u;
+            lo += dd < 6u ? 1u << (5 * dd) : 0u;
+            hi += dd - 6u < 6u ? 1u << (5 * (dd - 6u)) : 0u;
+            dlast = (in & ok) ? d : dlast;
+        }
+    }
+    const unsigned long long H = (unsigned long long)lo | ((unsigned long long)hi << 30);
+    int fch = (int)0x80000000, fcnt = 0;
+    if (__popc(need) <= 1 && (unsigned)dlast < 12u) {
+        if (need) {
+            const int slot = atomicAdd(qn, 1);
+            qe[slot] = PxDefer{p.c, p.pb, p.nv, i0 + __ffs(need) - 1, fix, rowoff, 0};
+        }
+        if (H) {
+            const int c0 = (int)fl0;
+            const int ntake = m - (need ? 1 : 0);
+            const int blo = (__ffsll((long long)H) - 1) / 5;
+            // all 32 samples in one channel: 32 overflows its five bits into a single carry bit of H
+            const bool one = SPL == 32 && ntake == 32 && H == 1ull << (5 * dlast + 5);
+            fch = c0 + (one ? dlast : blo);
+            fcnt = one ? 32 : (int)((H >> (5 * blo)) & 31);
+#pragma unroll
+            for (int b = 0; b < 12; b++) {
+                const int cnt = (int)((H >> (5 * b)) & 31);
+                const int ch = c0 + b;
+                const bool put = !one & (cnt != 0) & (b != blo) & ((unsigned)ch < (unsigned)nz);
+                if (put) row[ch] += (unsigned long long)(fix * (long long)cnt);
+            }
+        }
+    } else {
+        PxRuns r{(int)0x80000000, 0, (int)0x80000000, 0};
+        for (int i = 0; i < m; i++) {
+            const float f = fmaf(__ldg(&L.nf[(unsigned)p.pb + i0 + i]), sg, tc) + 0.5f;
+            const float fl = floorf(f);
+            int c = (int)fl;
+            if (!(fastc && fabsf(f - fl - 0.5f) <= hw)) c = px_exact(g, L, zig, subk, p.c, p.pb, p.nv, i0 + i, err);
+            r.take(c, fix, nz, row);
+        }
+        // the open run: the lane's first run if it is the only one, else its last (a channel no other lane adds)
+        if (r.cur != (int)0x80000000) {
+            if (r.fch == (int)0x80000000) {
+                r.fch = r.cur;
+                r.fcnt = r.cnt;
+            } else if ((unsigned)r.cur < (unsigned)nz) {
+                row[r.cur] += (unsigned long long)(fix * (long long)r.cnt);
+            }
+        }
+        fch = r.fch;
+        fcnt = r.fcnt;
+    }
+#pragma unroll
+    for (int qq = 0; qq < LPP; qq++) {
+        __syncwarp();
+        if (q == qq && (unsigned)fch < (unsigned)nz) row[fch] += (unsigned long long)(fix * (long long)fcnt);
+    }
+    __syncwarp();
+}
+
+// The common case (a linear channel map, one line, at most 128 samples per cloud) with the tile's pixels owned
+// by groups of LPP = 128 / SPL lanes: warp w owns the pixels lp = w + 8 grp of the tile (TP = 8 x 32 / LPP
+// pixels), and a group takes the clouds of its pixel one after another, so a warp advances 32 / LPP clouds at a
+// time. Lane q of a group counts the samples SPL q .. SPL q + SPL - 1 of the cloud in their sorted order (float32
+// channels within the rounding bound of the cloud); the samples of the next cloud are loaded during the count.
+// The channels are monotone along the sorted samples, so the lanes of a group can only meet on the channel of a
+// run that crosses from one lane's samples into the next lane's: every lane's channels but its lowest are added
+// at once (distinct channels), and the lowest ones in lane order.
+// A sample within the bound of a half-integer (about one in a thousand) waits in the warp's queue; when the
+// queue fills, its exact float64 channels are computed a lane each and added with shared-memory atomics.
+// Rows: stride nz + 2 G sums (G pixels per warp) and a skew of 2 grp sums, so that equal channels of the warp's
+// pixels fall in different banks.
+#ifndef PX_MINB
+#define PX_MINB 3         // resident CTAs per SM
+#endif
+template <int SPL>
+__global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, LayoutDev L, const SubMC *__restrict__ sub,
+                                                              int nsub, const MemberDev *__restrict__ mem, int tx,
+                                                              int ty, const int *__restrict__ offset,
+                                                              const int *__restrict__ count,
+                                                              const Entry *__restrict__ bucket,
+                                                              const ZigDev *__restrict__ zig,
+                                                              const float *__restrict__ cd2if,
+                                                              float *__restrict__ model, long long mstride,
+                                                              int *err) {
+    constexpr int LPP = 128 / SPL;
+    extern __shared__ unsigned long long tile[];           // TP rows of fixed-point sums, queues, nz scales
+    const int k = blockIdx.x;
+    const int t = blockIdx.y;
+    const int ntx = mem[k].ntx;
+    if (t >= ntx * mem[k].nty) return;
+    constexpr int G = 32 / LPP;                             // pixels per warp
+    const int nz = g.nz, RS = nz + 2 * G;
+    const int TP = tx * ty;
+    const int tyi = t / ntx, txi = t - tyi * ntx;
+    const int x0 = txi * tx, y0 = tyi * ty;
+    const int bx = mem[k].bx, by = mem[k].by;
+    const int lbase = (mem[k].tile_off + t) * NOWN;
+    float *mout = model + (size_t)k * mstride;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    {
+        int any = 0;
+        if (threadIdx.x < NOWN) any = count[lbase + threadIdx.x] != 0;
+        if (!__syncthreads_or(any)) {
+            for (int lp = warp; lp < TP; lp += 8) {
+                const int py = y0 + lp / tx, px = x0 + lp % tx;
+                if (py >= by || px >= bx) continue;
+                float *o = mout + ((size_t)py * bx + px) * nz;
+                for (int z = lane; z < nz; z += 32) o[z] = 0.0f;
+            }
+            return;
+        }
+    }
+    PxDefer *qall = (PxDefer *)(tile + (size_t)TP * RS);   // (16-byte aligned: TP RS is even)
+    int *qns = (int *)(qall + 8 * PX_QCAP);
+    float *chs = (float *)(qns + 8);
+    {
+        const int nt = TP * RS;
+        if (threadIdx.x < 8) qns[threadIdx.x] = 0;
+        ulonglong2 *t2 = (ulonglong2 *)tile;
+        for (int i = threadIdx.x; i < nt / 2; i += blockDim.x) t2[i] = make_ulonglong2(0ULL, 0ULL);
+        const int fe = mem[k].fix_exp;
+        for (int z = threadIdx.x; z < nz; z += blockDim.x) chs[z] = ldexpf(cd2if[z], -fe);
+    }
+    __syncthreads();
+    const int grp = lane / LPP, q = lane % LPP;
+    const int lp = warp + 8 * grp;
+    const bool own = lp < TP;
+    const int beg = own ? offset[lbase + 8 * warp + grp] : 0;
+    const int n = own ? count[lbase + 8 * warp + grp] : 0;
+    const int rowoff = (own ? lp : 0) * RS + 2 * grp;
+    PxDefer *qe = qall + warp * PX_QCAP;
+    int *qn = qns + warp;
+    const SubMC *__restrict__ subk = sub + (size_t)k * nsub;
+    const int nj = __reduce_max_sync(0xffffffffu, n);
+    const int i0 = SPL * q;                                 // this lane's samples: i0 .. min(i0 + SPL, nv) - 1
+    // software pipeline: the samples of the next cloud and the entry after it are loaded during a count
+    PxCloud ca, cb;
+    float4 wa[SPL / 4], wb[SPL / 4];
+    px_entry(bucket, beg, n, 0, ca);
+    px_samples<SPL>(L, ca, i0, wa);
+    px_entry(bucket, beg, n, 1, cb);
+    for (int j = 0; j < nj; j++) {
+        px_samples<SPL>(L, cb, i0, wb);
+        PxCloud cn;
+        px_entry(bucket, beg, n, j + 2, cn);
+        px_count<SPL>(g, L, zig, subk, ca, wa, i0, q, tile, rowoff, qe, qn, err);
+        __syncwarp();
+        if (*qn > PX_QCAP - 32) px_flush(g, L, zig, subk, qe, qn, tile, lane, err);
+        ca = cb;
+        cb = cn;
+#pragma unroll
+        for (int s = 0; s < SPL / 4; s++) wa[s] = wb[s];
+    }
+    __syncwarp();
+    if (*qn) px_flush(g, L, zig, subk, qe, qn, tile, lane, err);
+    __syncthreads();
+    for (int p = warp; p < TP; p += 8) {
+        const int py = y0 + p / tx, px = x0 + p % tx;
+        if (py >= by || px >= bx) continue;
+        const unsigned long long *src = tile + (size_t)p * RS + 2 * (p >> 3);
+        float *o = mout + ((size_t)py * bx + px) * nz;
+        for (int z = lane; z < nz; z += 32) o[z] = ll_to_f32((long long)src[z]) * chs[z];
     }
 }
 
@@ -805,6 +1110,29 @@ void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, con
         if (smem > 48 * 1024 && smem > cfg_lean) {
             cudaFuncSetAttribute(k_mc_deposit_lean, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             cfg_lean = smem;
+        }
+        const int TP = tx * ty;
+        if (TP == 64 || TP == 32) {
+            // pixel-owned deposit: 8 (TP 64) or 4 (TP 32) pixels per warp
+            const size_t smem_px = (size_t)TP * (g.nz + TP / 4) * sizeof(unsigned long long) +
+                                   (size_t)8 * PX_QCAP * sizeof(PxDefer) + 8 * sizeof(int) +
+                                   (size_t)g.nz * sizeof(float);
+            static size_t cfg32 = 0, cfg16 = 0;
+            size_t &cfg = TP == 64 ? cfg32 : cfg16;
+            if (smem_px > 48 * 1024 && smem_px > cfg) {
+                if (TP == 64)
+                    cudaFuncSetAttribute(k_mc_deposit_px<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_px);
+                else
+                    cudaFuncSetAttribute(k_mc_deposit_px<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_px);
+                cfg = smem_px;
+            }
+            if (TP == 64)
+                k_mc_deposit_px<32><<<grid, 256, smem_px, s>>>(g, L, sub, nsub, mem, tx, ty, offset, count,
+                                                               (const Entry *)bucket, zig, cd2if, model, mstride, err);
+            else
+                k_mc_deposit_px<16><<<grid, 256, smem_px, s>>>(g, L, sub, nsub, mem, tx, ty, offset, count,
+                                                               (const Entry *)bucket, zig, cd2if, model, mstride, err);
+            return;
         }
         k_mc_deposit_lean<<<grid, 256, smem, s>>>(g, L, sub, nsub, mem, tx, ty, offset, count, (const Entry *)bucket,
                                                  zig, cd2if, model, mstride, err);

@@ -110,3 +110,49 @@ def test_batch_path_models_bit_exact(gpu_lib, oracle_lib, wl):
                              st.cd2i)
         assert np.array_equal(got != 0, ref != 0), k
         np.testing.assert_allclose(got, ref, rtol=1e-6, atol=0)
+
+
+def _batch_vs_oracle(oracle_lib, cube, rings):
+    """The batch path's float32 models of three ring sets against the oracle (same voxels, float32 values)."""
+    from bbarolo2_gb300 import _lib, engine
+    from bbarolo2_gb300.galmod import ring_rows_batch
+    dm = engine.DiskModel(cube)
+    st = dm.setup
+    L = engine.BatchLikelihood(dm, np.ones(cube.array.shape, np.float32), None, maskmode=0, sigma=1.0)
+    rows = ring_rows_batch([rings] * 3)
+    rows[1, 4] *= 1.07
+    rows[2, 12] += 3.0
+    sr, nv, descs, boxes = L.prepare(rows, rings, seed=3)
+    L.run(sr, nv, descs)
+    for k in range(3):
+        (blo, bhi) = boxes[k]
+        by, bx = bhi[1] - blo[1], bhi[0] - blo[0]
+        got = np.zeros((by, bx, st.nsubs), np.float32)
+        dm.ctx.check(dm.ctx.L.bbgpu_eval_model(dm.ctx.h, k, 0, _lib.ptr(got), by, bx, st.nsubs))
+        ref = np.zeros((by, bx, st.nsubs))
+        oracle_lib.galmod_mc(ref, sr[k], 0, sr.shape[2], 3, st.radsep, nv[k], st.cdens, st.cmode, st.pixarea,
+                             st.cdelt[0], st.cdelt[1], st.crota2, blo[0], blo[1], bhi[0], bhi[1], st.ltype,
+                             st.sig_instr, st.axtyp, st.velsys, st.lfreq0, st.crval3, st.cdelt3, st.crpix3, st.relint,
+                             st.cd2i)
+        assert np.array_equal(got != 0, ref != 0), k
+        np.testing.assert_allclose(got, ref, rtol=1e-6, atol=0)
+
+
+@pytest.mark.parametrize("variant", ["narrow", "broad", "descending"])
+def test_batch_path_line_widths_and_axis(gpu_lib, oracle_lib, variant):
+    """The batch deposit counts each cloud's samples per channel in runs: lines so narrow that the 32 samples
+    of a lane share one channel (vdisp 0.2 km/s in 5 km/s channels), so broad that a lane's samples spread over
+    more than 12 channels (vdisp 90 km/s), and a channel axis that decreases with velocity (samples in
+    descending order)."""
+    from bbarolo2_gb300 import configs
+    from bbarolo2_gb300.cube import Cube, Params
+    cube, rings = configs.classic64(galmodtype="MC")
+    if variant == "narrow":
+        rings.vdisp[:] = 0.2
+    elif variant == "broad":
+        rings.vdisp[:] = 90.
+    else:
+        par = Params(CDENS=10, ISEED=1, LTYPE=1, galmodtype="MC")
+        cube = Cube.empty(64, 64, 64, [-10. / 3600., 10. / 3600., -5.], beam=30. / 3600., par=par,
+                          crpix=[33., 33., 33.], crval=[60., 0., 1000.], cunit=("deg", "deg", "km/s"))
+    _batch_vs_oracle(oracle_lib, cube, rings)
