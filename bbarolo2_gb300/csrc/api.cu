@@ -21,12 +21,13 @@
 
 #define BBGPU_VERSION 1
 #define NLAYOUT 4
-#define NTIMER 10
+#define NTIMER 11
 
 // the timed stages of a batch: the flux normalisation (ring maps, their beam convolution, the normal equations,
-// the solves and the sub-ring densities), then the MC model, its convolution and the residual reduction
+// the solves and the sub-ring densities), then the MC model (or the ANALYTIC one), its convolution and the
+// residual reduction
 static const char *KNAMES[NTIMER] = {"prof_maps", "prof_conv", "prof_gram", "prof_solve", "mc_bin", "scan_tiles",
-                                     "mc_scatter", "mc_deposit", "conv_resid", "reduce_partials"};
+                                     "mc_scatter", "mc_deposit", "an_model", "conv_resid", "reduce_partials"};
 
 struct LayoutEntry {
     LayoutHost host;
@@ -125,6 +126,19 @@ struct bbgpu_ctx {
     AnSub *h_psub = nullptr;           // pinned staging of the sub-ring constants
     size_t h_psub_cap = 0;
     std::vector<MemberDev> pmem_host;
+    // ANALYTIC batches: sub-ring constants per member, the sample table of the model's sub-rings, their vertical
+    // grids (host cache mirrored on the device) and the fixed-point models
+    AnSub *h_asub = nullptr, *d_asub = nullptr;
+    size_t h_asub_cap = 0, d_asub_cap = 0;
+    int *d_asbase = nullptr, *d_assub = nullptr;
+    size_t d_asbase_cap = 0, d_assub_cap = 0;
+    double *d_acs = nullptr, *d_azq = nullptr, *d_awq = nullptr;
+    size_t d_acs_cap = 0, d_azq_cap = 0, d_awq_cap = 0;
+    long long *d_model_fx = nullptr;
+    size_t d_model_fx_cap = 0;
+    long long ansamp = 0;
+    std::string asamp_key;
+    ZgridCache azcache;
     // options
     bool keep_smoothed = false, timing = false, want64 = false;
     int lean = 0;                 // the batch qualifies for the lean deposit kernel
@@ -399,6 +413,10 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
                     (void *)ctx->d_pwvalf, (void *)ctx->d_maps32, (void *)ctx->d_K, (void *)ctx->d_maps64,
                     (void *)ctx->d_pmem})
         cudaFree(q);
+    for (void *q : {(void *)ctx->d_asub, (void *)ctx->d_asbase, (void *)ctx->d_assub, (void *)ctx->d_acs,
+                    (void *)ctx->d_azq, (void *)ctx->d_awq, (void *)ctx->d_model_fx})
+        cudaFree(q);
+    cudaFreeHost(ctx->h_asub);
     cudaFreeHost(ctx->h_psub);
     cudaFreeHost(ctx->h_sub); cudaFreeHost(ctx->h_mem); cudaFreeHost(ctx->h_out2); cudaFreeHost(ctx->h_err);
     for (int i = 0; i <= NTIMER; i++)
@@ -571,13 +589,142 @@ extern "C" int bbgpu_set_cube(bbgpu_ctx *ctx, const float *data, const uint8_t *
 }
 
 // ------------------------------------------------------------------------------------------- batches
+// The member descriptor of a batch (box, residual options, data view).
+static int member_desc(bbgpu_ctx *ctx, int k, const bbgpu_eval_desc &d, int fix_exp, bool need_cube, MemberDev &M) {
+    const GridDev &g = ctx->g;
+    if (d.blo0 < 0 || d.blo1 < 0 || d.bhi0 > g.nx || d.bhi1 > g.ny || d.bhi0 < d.blo0 || d.bhi1 < d.blo1)
+        return fail(ctx, BBGPU_ERR_ARG, "eval: member %d: box outside the cube", k);
+    if (d.eps2 > 0 && !(d.sigma2 > 0)) return fail(ctx, BBGPU_ERR_ARG, "eval: member %d: eps2 > 0 needs sigma2 > 0", k);
+    memset(&M, 0, sizeof M);
+    M.blo0 = d.blo0; M.blo1 = d.blo1; M.bhi0 = d.bhi0; M.bhi1 = d.bhi1;
+    M.bx = d.bhi0 - d.blo0; M.by = d.bhi1 - d.blo1;
+    M.fix_exp = fix_exp;
+    M.maskmode = d.maskmode;
+    M.use_region = d.use_region;
+    M.sigma2 = d.sigma2;
+    M.eps2 = d.eps2;
+    M.sigma2f = (float)d.sigma2;
+    M.eps2f = (float)d.eps2;
+    if (need_cube) {
+        int rc = ensure_deff(ctx, d.maskmode, d.use_region);
+        if (rc) return rc;
+        M.deff = ctx->d_deff[d.maskmode][d.use_region ? 1 : 0];
+    }
+    return 0;
+}
+
+// An ANALYTIC batch (bbarolo/galmod.py:326-465 per member): the sub-ring constants of every member on the host
+// (vertical grids shared through a cache), the azimuthal samples of the shared radii, all uploaded; the members
+// may differ in every ring value but the radii.
+static int batch_prepare_analytic(bbgpu_ctx *ctx, int nb, int nsub, const double *sr, const bbgpu_eval_desc *descs,
+                                  bool need_cube) {
+    const GridDev &g = ctx->g;
+    if (!ctx->d_vedges) return fail(ctx, BBGPU_ERR_STATE, "eval: ANALYTIC batch, but set_grid was given no channel edges");
+    if (an_smem_bytes(g.nz, g.nlines) > AN_SMEM_MAX)
+        return fail(ctx, BBGPU_ERR_ARG, "eval: %d channels x %d lines above the ANALYTIC kernel's limit", g.nz, g.nlines);
+    for (int k = 1; k < nb; k++)
+        if (memcmp(sr + (size_t)k * BBGPU_NSR * nsub, sr, sizeof(double) * nsub))
+            return fail(ctx, BBGPU_ERR_ARG, "eval: member %d has other radii: evaluate it in another batch", k);
+    int rc;
+    if ((rc = hgrow(ctx, &ctx->h_asub, &ctx->h_asub_cap, (size_t)nb * (nsub ? nsub : 1)))) return rc;
+    if ((rc = hgrow(ctx, &ctx->h_mem, &ctx->h_mem_cap, (size_t)nb))) return rc;
+    ctx->mem_host.resize(nb);
+    ZgridCache &zc = ctx->azcache;
+    if (zc.zq.size() > ((size_t)1 << 24)) zc.clear();
+    int nzq0 = 1;
+    for (int k = 0; k < nb; k++) {
+        const bbgpu_eval_desc &d = descs[k];
+        const double *s = sr + (size_t)k * BBGPU_NSR * nsub;
+        int nzq = 1;                                // bbarolo/galmod.py:912: vertical samples for a thick layer
+        for (int i = 0; i < nsub; i++)
+            if (s[6 * (size_t)nsub + i] > 0) { nzq = 1024; break; }
+        if (k == 0) nzq0 = nzq;
+        // the constants of a sub-ring whose column equals member 0's are member 0's when the box and the vertical
+        // sampling are the same (the vertical grid depends on the box)
+        const bool reuse = k > 0 && nzq == nzq0 && d.blo0 == descs[0].blo0 && d.blo1 == descs[0].blo1 &&
+                           d.bhi0 == descs[0].bhi0 && d.bhi1 == descs[0].bhi1;
+        if (d.blo0 < 0 || d.blo1 < 0 || d.bhi0 > g.nx || d.bhi1 > g.ny || d.bhi0 < d.blo0 || d.bhi1 < d.blo1)
+            return fail(ctx, BBGPU_ERR_ARG, "eval: member %d: box outside the cube", k);
+        const int e = bbh_an_subs(s, nsub, &g, nzq, d.blo0, d.blo1, d.bhi0, d.bhi1, ctx->h_cd2i.data(), 0, nullptr,
+                                  nullptr, ctx->h_asub + (size_t)k * nsub, zc, reuse ? sr : nullptr,
+                                  reuse ? ctx->h_asub : nullptr);
+        if (e == -10000) return fail(ctx, BBGPU_ERR_ARG, "eval: member %d: the total flux is not finite", k);
+        if ((rc = member_desc(ctx, k, d, e, need_cube, ctx->mem_host[k]))) return rc;
+        ctx->h_mem[k] = ctx->mem_host[k];
+    }
+    ctx->nb = nb;
+    ctx->nsub = nsub;
+    ctx->galmodtype = BBGPU_ANALYTIC;
+    ctx->lean = 0;
+    ctx->ntile_total = 0;
+    ctx->mstride = (long long)g.nx * g.ny * g.nz;
+    ctx->npart = conv_resid_npart(ctx->mem_host.data(), nb, g.nz);
+    ctx->h2d = 0;
+    // the azimuthal samples of the radii (uploaded when the radii change)
+    std::string key((const char *)sr, sizeof(double) * nsub);
+    key.append((const char *)&g.pixarea, sizeof(double));
+    if (key != ctx->asamp_key) {
+        std::vector<int> sbase, ssub;
+        std::vector<double> cs;
+        bbh_an_samples(sr, nsub, &g, sbase, ssub, cs);
+        if ((rc = dgrow(ctx, &ctx->d_asbase, &ctx->d_asbase_cap, sbase.size()))) return rc;
+        if ((rc = dgrow(ctx, &ctx->d_assub, &ctx->d_assub_cap, ssub.size() ? ssub.size() : 1))) return rc;
+        if ((rc = dgrow(ctx, &ctx->d_acs, &ctx->d_acs_cap, cs.size() ? cs.size() : 1))) return rc;
+        CK(cudaMemcpy(ctx->d_asbase, sbase.data(), sizeof(int) * sbase.size(), cudaMemcpyHostToDevice));
+        if (ssub.size()) CK(cudaMemcpy(ctx->d_assub, ssub.data(), sizeof(int) * ssub.size(), cudaMemcpyHostToDevice));
+        if (cs.size()) CK(cudaMemcpy(ctx->d_acs, cs.data(), sizeof(double) * cs.size(), cudaMemcpyHostToDevice));
+        ctx->ansamp = sbase[nsub];
+        ctx->asamp_key = key;
+        ctx->h2d += (long long)(sizeof(int) * (sbase.size() + ssub.size()) + sizeof(double) * cs.size());
+    }
+    // the vertical grids: the new ones appended on the device (the table grows with a copy of the whole)
+    const size_t nz1 = zc.zq.size() + 1;
+    if (zc.uploaded == 0 || nz1 > ctx->d_azq_cap) {
+        if (nz1 > ctx->d_azq_cap) {
+            cudaFree(ctx->d_azq);
+            cudaFree(ctx->d_awq);
+            ctx->d_azq = ctx->d_awq = nullptr;
+            ctx->d_azq_cap = ctx->d_awq_cap = 0;
+            if ((rc = dgrow(ctx, &ctx->d_azq, &ctx->d_azq_cap, 2 * nz1))) return rc;
+            if ((rc = dgrow(ctx, &ctx->d_awq, &ctx->d_awq_cap, 2 * nz1))) return rc;
+        }
+        zc.uploaded = 0;
+    }
+    if (zc.zq.size() > zc.uploaded) {
+        const size_t a0 = zc.uploaded, m = zc.zq.size() - a0;
+        CK(cudaMemcpy(ctx->d_azq + a0, zc.zq.data() + a0, sizeof(double) * m, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(ctx->d_awq + a0, zc.wq.data() + a0, sizeof(double) * m, cudaMemcpyHostToDevice));
+        ctx->h2d += (long long)(16 * m);
+        zc.uploaded = zc.zq.size();
+    }
+    if ((rc = dgrow(ctx, &ctx->d_asub, &ctx->d_asub_cap, (size_t)nb * (nsub ? nsub : 1)))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_mem, &ctx->d_mem_cap, (size_t)nb))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_model, &ctx->d_model_cap, (size_t)nb * ctx->mstride))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_model_fx, &ctx->d_model_fx_cap, (size_t)nb * ctx->mstride))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_partial, &ctx->d_partial_cap, (size_t)2 * nb * (ctx->npart ? ctx->npart : 1)))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_out2, &ctx->d_out2_cap, (size_t)2 * nb))) return rc;
+    if ((rc = hgrow(ctx, &ctx->h_out2, &ctx->h_out2_cap, (size_t)2 * nb))) return rc;
+    if (ctx->keep_smoothed)
+        if ((rc = dgrow(ctx, &ctx->d_smooth, &ctx->d_smooth_cap, (size_t)nb * ctx->mstride))) return rc;
+    if (ctx->want64)
+        if ((rc = dgrow(ctx, &ctx->d_model64, &ctx->d_model64_cap, (size_t)nb * ctx->mstride))) return rc;
+    CK(cudaMemcpyAsync(ctx->d_asub, ctx->h_asub, sizeof(AnSub) * (size_t)nb * nsub, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_mem, ctx->h_mem, sizeof(MemberDev) * (size_t)nb, cudaMemcpyHostToDevice, ctx->stream));
+    ctx->h2d += (long long)(sizeof(AnSub) * (size_t)nb * nsub + sizeof(MemberDev) * (size_t)nb);
+    ctx->uploaded = true;
+    ctx->ran = false;
+    return 0;
+}
+
 static int batch_prepare(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const double *sr, const int64_t *nv,
                          const bbgpu_eval_desc *descs, bool need_cube) {
     ctx->prof_uploaded = false;       // (a new batch: its ring maps come with bbgpu_eval_upload_profile)
     if (!ctx->grid_set) return fail(ctx, BBGPU_ERR_STATE, "evaluation before set_grid");
     if (need_cube && !ctx->cube_set) return fail(ctx, BBGPU_ERR_STATE, "evaluation before set_cube");
-    if (galmodtype != BBGPU_MC) return fail(ctx, BBGPU_ERR_ARG, "galmodtype %d not supported by the batch path", galmodtype);
+    if (galmodtype != BBGPU_MC && galmodtype != BBGPU_ANALYTIC)
+        return fail(ctx, BBGPU_ERR_ARG, "galmodtype %d not supported by the batch path", galmodtype);
     if (nb < 1 || nsub < 0 || !sr || !nv || !descs) return fail(ctx, BBGPU_ERR_ARG, "eval: invalid batch");
+    if (galmodtype == BBGPU_ANALYTIC) return batch_prepare_analytic(ctx, nb, nsub, sr, descs, need_cube);
     const GridDev &g = ctx->g;
     std::vector<int> nc0(nsub), nv0(nsub), nc(nsub), nvv(nsub);
     std::vector<double> R0(nsub);
@@ -611,25 +758,11 @@ static int batch_prepare(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const
         int e = bbh_submc(sr + (size_t)k * BBGPU_NSR * nsub, nsub, nc0.data(), nv0.data(), &g, S,
                           k ? sr : nullptr, k ? ctx->h_sub : nullptr);
         MemberDev &M = ctx->mem_host[k];
-        memset(&M, 0, sizeof M);
-        M.blo0 = d.blo0; M.blo1 = d.blo1; M.bhi0 = d.bhi0; M.bhi1 = d.bhi1;
-        M.bx = d.bhi0 - d.blo0; M.by = d.bhi1 - d.blo1;
+        if ((rc = member_desc(ctx, k, d, e, need_cube, M))) return rc;
         M.ntx = (M.bx + ctx->tx - 1) / ctx->tx;
         M.nty = (M.by + ctx->ty - 1) / ctx->ty;
         M.tile_off = toff;
         toff += M.ntx * M.nty;
-        M.fix_exp = e;
-        M.maskmode = d.maskmode;
-        M.use_region = d.use_region;
-        M.sigma2 = d.sigma2;
-        M.eps2 = d.eps2;
-        M.sigma2f = (float)d.sigma2;
-        M.eps2f = (float)d.eps2;
-        if (d.eps2 > 0 && !(d.sigma2 > 0)) return fail(ctx, BBGPU_ERR_ARG, "eval: member %d: eps2 > 0 needs sigma2 > 0", k);
-        if (need_cube) {
-            if ((rc = ensure_deff(ctx, d.maskmode, d.use_region))) return rc;
-            M.deff = ctx->d_deff[d.maskmode][d.use_region ? 1 : 0];
-        }
         ctx->h_mem[k] = M;
     }
     ctx->nb = nb;
@@ -699,8 +832,16 @@ static int profile_run(bbgpu_ctx *ctx, bool tm) {
     launch_prof_solve(s, ctx->d_gh, ctx->pc, ctx->d_lc, ctx->d_lv, ctx->d_ord, ctx->d_near, ctx->d_p0, nb, ctx->d_px,
                       ctx->d_pp, ctx->d_pstat);
     CKL();
-    launch_mc_dens(s, g, ctx->d_sub, ctx->nsub, ctx->d_mem, nb, ctx->d_px, n, ctx->d_pwidx, ctx->d_pwval, ctx->d_rap,
-                   ctx->d_err);
+    if (ctx->galmodtype == BBGPU_ANALYTIC) {
+        double lsum = 0.0, cmax = 0.0;
+        for (int nl = 0; nl < g.nlines; nl++) lsum += fabs(g.relint[nl]);
+        for (double c : ctx->h_cd2i) cmax = std::max(cmax, fabs(c));
+        launch_an_dens(s, g, ctx->d_asub, ctx->nsub, ctx->d_mem, nb, ctx->d_px, n, ctx->d_pwidx, ctx->d_pwval,
+                       ctx->d_rap, lsum * cmax, ctx->d_err);
+    } else {
+        launch_mc_dens(s, g, ctx->d_sub, ctx->nsub, ctx->d_mem, nb, ctx->d_px, n, ctx->d_pwidx, ctx->d_pwval,
+                       ctx->d_rap, ctx->d_err);
+    }
     CKL();
     if (tm) CK(cudaEventRecord(ctx->ev[4], s));
     (void)per;
@@ -710,7 +851,6 @@ static int profile_run(bbgpu_ctx *ctx, bool tm) {
 static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
     if (!ctx->uploaded) return fail(ctx, BBGPU_ERR_STATE, "run before upload");
     const GridDev &g = ctx->g;
-    const LayoutDev &L = ctx->cur->dev;
     cudaStream_t s = ctx->stream;
     const bool tm = ctx->timing;
     if (tm) CK(cudaEventRecord(ctx->ev[0], s));
@@ -720,23 +860,41 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
     } else if (tm) {
         for (int i = 1; i <= 4; i++) CK(cudaEventRecord(ctx->ev[i], s));
     }
-    CK(cudaMemsetAsync(ctx->d_tcount, 0, sizeof(int) * (size_t)(ctx->ntile_total * NOWN + 1), s));
-    launch_mc_bin(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->nb, ctx->tx, ctx->ty, ctx->d_pix, ctx->d_tcount,
-                  ctx->d_err);
-    CKL();
-    if (tm) CK(cudaEventRecord(ctx->ev[5], s));
-    launch_scan_tiles(s, ctx->d_tcount, ctx->d_toff, ctx->d_tcur, ctx->ntile_total * NOWN, ctx->d_scan);
-    CKL();
-    if (tm) CK(cudaEventRecord(ctx->ev[6], s));
-    launch_mc_scatter(s, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->nb, ctx->tx, ctx->ty, ctx->d_pix, ctx->d_tcur,
-                      ctx->d_bucket);
-    CKL();
-    if (tm) CK(cudaEventRecord(ctx->ev[7], s));
-    launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->tx, ctx->ty,
-                      ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig, ctx->d_cd2if, ctx->d_cd2i,
-                      ctx->d_model, ctx->mstride, ctx->want64 ? ctx->d_model64 : nullptr, ctx->d_err, ctx->lean);
-    CKL();
-    if (tm) CK(cudaEventRecord(ctx->ev[8], s));
+    if (ctx->galmodtype == BBGPU_ANALYTIC) {
+        if (tm)
+            for (int i = 5; i <= 8; i++) CK(cudaEventRecord(ctx->ev[i], s));
+        CK(cudaMemsetAsync(ctx->d_model_fx, 0, sizeof(long long) * (size_t)ctx->nb * ctx->mstride, s));
+        launch_an_model(s, g, ctx->d_asub, ctx->nsub, ctx->d_asbase, ctx->d_assub, ctx->d_acs, ctx->ansamp, ctx->nb,
+                        ctx->d_azq, ctx->d_awq, ctx->d_vedges, ctx->d_cd2i, ctx->d_ptab, ctx->d_mem, ctx->d_model_fx,
+                        ctx->mstride);
+        CKL();
+        launch_fix_to_model(s, ctx->d_model_fx, ctx->d_mem, ctx->nb, ctx->mstride, g.nz, ctx->d_model,
+                            ctx->want64 ? ctx->d_model64 : nullptr);
+        CKL();
+        if (tm) CK(cudaEventRecord(ctx->ev[9], s));
+    } else {
+        const LayoutDev &L = ctx->cur->dev;
+        CK(cudaMemsetAsync(ctx->d_tcount, 0, sizeof(int) * (size_t)(ctx->ntile_total * NOWN + 1), s));
+        launch_mc_bin(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->nb, ctx->tx, ctx->ty, ctx->d_pix,
+                      ctx->d_tcount, ctx->d_err);
+        CKL();
+        if (tm) CK(cudaEventRecord(ctx->ev[5], s));
+        launch_scan_tiles(s, ctx->d_tcount, ctx->d_toff, ctx->d_tcur, ctx->ntile_total * NOWN, ctx->d_scan);
+        CKL();
+        if (tm) CK(cudaEventRecord(ctx->ev[6], s));
+        launch_mc_scatter(s, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->nb, ctx->tx, ctx->ty, ctx->d_pix, ctx->d_tcur,
+                          ctx->d_bucket);
+        CKL();
+        if (tm) CK(cudaEventRecord(ctx->ev[7], s));
+        launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->tx, ctx->ty,
+                          ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig, ctx->d_cd2if, ctx->d_cd2i,
+                          ctx->d_model, ctx->mstride, ctx->want64 ? ctx->d_model64 : nullptr, ctx->d_err, ctx->lean);
+        CKL();
+        if (tm) {
+            CK(cudaEventRecord(ctx->ev[8], s));
+            CK(cudaEventRecord(ctx->ev[9], s));
+        }
+    }
     const bool conv = ctx->kernel_set;
     if (do_resid || ctx->keep_smoothed) {
         launch_conv_resid(s, g, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->d_model, ctx->mstride, g.nz,
@@ -744,14 +902,14 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
                           conv ? 1 : 0, do_resid ? 1 : 0, ctx->d_partial);
         CKL();
     }
-    if (tm) CK(cudaEventRecord(ctx->ev[9], s));
+    if (tm) CK(cudaEventRecord(ctx->ev[10], s));
     if (do_resid) {
         launch_reduce_partials(s, ctx->d_partial, ctx->npart, ctx->nb, ctx->d_out2);
         CKL();
     }
     if (tm) {
-        CK(cudaEventRecord(ctx->ev[10], s));
-        CK(cudaEventSynchronize(ctx->ev[10]));
+        CK(cudaEventRecord(ctx->ev[11], s));
+        CK(cudaEventSynchronize(ctx->ev[11]));
         for (int i = 0; i < NTIMER; i++) {
             float ms = 0.f;
             cudaEventElapsedTime(&ms, ctx->ev[i], ctx->ev[i + 1]);
@@ -1324,8 +1482,7 @@ extern "C" int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *
                                          const double *wval) {
     if (!ctx) return BBGPU_ERR_ARG;
     if (!ctx->prof_set) return fail(ctx, BBGPU_ERR_STATE, "eval_upload_profile before set_profile");
-    if (!ctx->uploaded || ctx->galmodtype != BBGPU_MC)
-        return fail(ctx, BBGPU_ERR_STATE, "eval_upload_profile before eval_upload of an MC batch");
+    if (!ctx->uploaded) return fail(ctx, BBGPU_ERR_STATE, "eval_upload_profile before eval_upload");
     const int nb = ctx->nb, nsub = ctx->nsub, n = ctx->pc.n;
     if (!sr_maps || !widx || !wval || nsm < nsub) return fail(ctx, BBGPU_ERR_ARG, "eval_upload_profile: invalid arguments");
     for (int i = 0; i < 2 * nsm; i++)

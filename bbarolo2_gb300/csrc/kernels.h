@@ -148,3 +148,7 @@ void launch_prof_solve(cudaStream_t s, const double *gh, const ProfConst &pc, co
                        int *status);
 void launch_mc_dens(cudaStream_t s, const GridDev &g, SubMC *sub, int nsub, MemberDev *mem, int nb, const double *x,
                     int nx, const int *widx, const double *wval, const double *rap, int *err);
+// the densities of the ANALYTIC model's sub-rings into its constants (fluxsc, line amplitudes, exponent);
+// per = sum |relint| x max |cd2i| (the deposit bound of a sample of unit flux)
+void launch_an_dens(cudaStream_t s, const GridDev &g, AnSub *sub, int nsub, MemberDev *mem, int nb, const double *x,
+                    int nx, const int *widx, const double *wval, const double *rap, double per, int *err);

@@ -15,7 +15,8 @@
 //                    smoothness prior, Lawson-Hanson on the normal equations (Cholesky of the passive set),
 //                    warm-started from a passive set;
 //   k_mc_dens        the densities of the model's sub-rings (ring weights) into the MC sub-ring constants
-//                    (flux per sub-cloud, fixed-point deposits and exponent), checking the cloud layout.
+//                    (flux per sub-cloud, fixed-point deposits and exponent), checking the cloud layout;
+//   k_an_dens        the same for an ANALYTIC model (flux per sample, line amplitudes, exponent).
 //
 // The maps need float32 accuracy only: the system is well conditioned (cond(A) ~ 1e2 on the 160x160x128
 // workload) and float32 map errors move the densities by ~1e-8; the Gram matrix squares the condition number
@@ -636,7 +637,63 @@ __global__ void k_mc_dens(GridDev g, SubMC *__restrict__ sub, int nsub, MemberDe
     if (tid == 0) mem[k].fix_exp = e;
 }
 
+// The ANALYTIC counterpart of k_mc_dens (one CTA per member): fluxsc = dens x ring area / (2 naz)
+// (bbarolo/galmod.py:367), the line amplitudes relint x fluxsc, and the member's fixed-point exponent from the
+// bound of its deposits (as the host's). A sub-ring at zero density deposits nothing; one that the host set up
+// as empty (no vertical grid) but whose density is not zero is an error.
+__global__ void k_an_dens(GridDev g, AnSub *__restrict__ sub, int nsub, MemberDev *__restrict__ mem,
+                          const double *__restrict__ x, int nx, const int *__restrict__ widx,
+                          const double *__restrict__ wval, const double *__restrict__ rap, double per, int *err) {
+    __shared__ double red[256];
+    const int k = blockIdx.x, tid = threadIdx.x;
+    const double *xk = x + (size_t)k * nx;
+    double bound = 0.0;
+    for (int ir = tid; ir < nsub; ir += blockDim.x) {
+        AnSub &S = sub[(size_t)k * nsub + ir];
+        double dens = 0.0;
+        for (int m = 0; m < 2; m++) {
+            const int r = widx[2 * ir + m];
+            if (r >= 0) dens += wval[2 * ir + m] * xk[r];
+        }
+        if (!S.active) {
+            if (dens != 0.0) atomicOr(err, ERR_PROFILE_LAYOUT);
+            continue;
+        }
+        if (dens == 0.0) {
+            S.active = 0;
+            continue;
+        }
+        const double fl = __ddiv_rn(__dmul_rn(__dmul_rn(dens, rap[ir]), g.pixarea), (double)((long long)S.naz * 2));
+        S.fluxsc = fl;
+        S.fluxscf = (float)fl;
+        for (int nl = 0; nl < g.nlines && nl < BBGPU_MAXL; nl++) S.a[nl] = __dmul_rn(g.relint[nl], fl);
+        bound += fabs(fl) * fmax(fabs(S.wrec), fabs(S.wapp)) * per * (double)((long long)S.naz * 2);
+    }
+    red[tid] = bound;
+    __syncthreads();
+    for (int d = blockDim.x / 2; d > 0; d >>= 1) {
+        if (tid < d) red[tid] += red[tid + d];
+        __syncthreads();
+    }
+    if (tid == 0) {
+        const double B = red[0];
+        int e = 0;
+        if (B > 0.0) {
+            int ex = 0;
+            frexp(B * 1.01, &ex);                   // B x 1.01 < 2^ex
+            e = min(62 - ex, 1000);
+        }
+        mem[k].fix_exp = e;
+    }
+}
+
 }  // namespace
+
+void launch_an_dens(cudaStream_t s, const GridDev &g, AnSub *sub, int nsub, MemberDev *mem, int nb, const double *x,
+                    int nx, const int *widx, const double *wval, const double *rap, double per, int *err) {
+    if (nb == 0) return;
+    k_an_dens<<<nb, 256, 0, s>>>(g, sub, nsub, mem, x, nx, widx, wval, rap, per, err);
+}
 
 void launch_an_maps_fast(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase,
                          const int *ssub, const double *cs, const float *csf, long long nsamp, int nb, const double *zq,

@@ -208,6 +208,7 @@ def main():
     ap.add_argument("--batch", type=int, default=161)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-analytic", action="store_true", help="skip the ANALYTIC GALMOD leg")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -301,6 +302,8 @@ def main():
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "kernel_ms": kt, "roofline": roof, "clocks": clocks,
             "logL_sample": [float(out[0]), float(out[1])]}
+    if not args.no_analytic:
+        line["analytic"] = analytic_leg(ctx, L, rows, rings, sr, nv, descs, args, dist, world)
     if rank == 0 and not args.no_cpu:
         vals, cores, n = cpu_leg(dm, L, rows, rings, data, mask)
         line["cpu_baseline"] = {"value": float(np.median(vals)), "unit": UNIT, "cores": cores, "kind": "port",
@@ -311,6 +314,42 @@ def main():
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def analytic_leg(ctx, L, rows, rings, sr, nv, descs, args, dist, world):
+    """The same batch with the ANALYTIC GALMOD (the reference's default for GLOBAL): device-resident evaluations/s,
+    the stage times, and end to end through the Python API."""
+    from bbarolo2_gb300 import _lib
+    B = rows.shape[0]
+    steps = max(1, args.steps // 2)
+    ctx.check(ctx.L.bbgpu_eval_upload(ctx.h, _lib.ANALYTIC, B, sr.shape[2], _lib.ptr(sr), _lib.ptr(nv),
+                                      _lib.ptr(descs)))
+    ms = L._maps_sr
+    ctx.check(ctx.L.bbgpu_eval_upload_profile(ctx.h, ms.shape[2], _lib.ptr(ms), _lib.ptr(L._prof["widx"]),
+                                              _lib.ptr(L._prof["wval"])))
+    for _ in range(args.warmup):
+        ctx.check(ctx.L.bbgpu_eval_run(ctx.h))
+    ctx.check(ctx.L.bbgpu_sync(ctx.h))
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ctx.check(ctx.L.bbgpu_eval_run(ctx.h))
+    ctx.check(ctx.L.bbgpu_sync(ctx.h))
+    dt = max_over_ranks(time.perf_counter() - t0, dist)
+    ctx.set_option(_lib.OPT_TIMING, 1)
+    ctx.check(ctx.L.bbgpu_eval_run(ctx.h))
+    kt = {k: v for k, v in ctx.run_times().items() if v > 0}
+    ctx.set_option(_lib.OPT_TIMING, 0)
+    L.evaluate(rows, rings, seed=1, galmodtype="ANALYTIC")
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        out = L.evaluate(rows, rings, seed=1, galmodtype="ANALYTIC")
+    te = max_over_ranks(time.perf_counter() - t0, dist)
+    return {"value": throughput(B, steps, world, dt), "unit": UNIT, "steps": steps, "ms_per_step": 1e3 * dt / steps,
+            "e2e": throughput(B, steps, world, te), "kernel_ms": kt, "logL_sample": [float(out[0]), float(out[1])]}
 
 
 def reference_arm(args, world):

@@ -13,7 +13,8 @@ With a profile in the payload, each evaluation first recomputes the deconvolved 
 (``bbarolo/bayesian/likelihood.py:595-596``): the ring maps (``_ring_maps_analytic`` through its C restatement,
 times mean(cd2i) sum(relint), FFT convolution, times the scale factor), the weighted least squares and
 ``solve_profile`` (``oracle/profile.py``), the model's sub-rings with the new densities (the package's host
-``subrings_batch``, bit-equal to the reference's ``subrings``), then the MC model.
+``subrings_batch``, bit-equal to the reference's ``subrings``), then the MC model (or, with ``galmodtype``
+ANALYTIC in the payload, the ANALYTIC model ``_galmod_analytic`` through its C restatement).
 One evaluation per process, as the reference's fork pool (``bbarolo/bayesian/sampling.py:184-193``), with the
 FFT on one worker thread; throughput = evaluations / wall time over all processes.
 """
@@ -100,17 +101,25 @@ def evaluate(k):
     if P.get("prof") is not None:
         sr, nv = model_table(k, profile_dens(k))
     m = np.zeros((bhi[1] - blo[1], bhi[0] - blo[0], st["nz"]))
-    O.galmod_mc(m, sr, 0, sr.shape[1], P["seed"], st["radsep"], nv, st["cdens"], st["cmode"],
-                st["pixarea"], st["cdelt0"], st["cdelt1"], st["crota2"], blo[0], blo[1], bhi[0], bhi[1], st["ltype"],
-                st["sig_instr"], st["axtyp"], st["velsys"], P["lfreq0"], st["crval3"], st["cdelt3"], st["crpix3"],
-                P["relint"], P["cd2i"])
+    if P.get("galmodtype", "MC") == "ANALYTIC":
+        nzq = 1 if not np.any(sr[6] > 0) else 1024      # (bbarolo/galmod.py:912)
+        O.galmod_analytic(m, sr, 0, sr.shape[1], st["radsep"], st["cdens"], st["pixarea"], st["cdelt0"],
+                          st["cdelt1"], st["crota2"], blo[0], blo[1], bhi[0], bhi[1], st["ltype"], st["sig_instr"],
+                          P["vedges"], P["relint"], P["cd2i"], nzq, st["axtyp"], st["velsys"], P["lfreq0"],
+                          st["crval3"], st["cdelt3"], st["crpix3"], st["chwidth"], None, st["zstep"])
+    else:
+        O.galmod_mc(m, sr, 0, sr.shape[1], P["seed"], st["radsep"], nv, st["cdens"], st["cmode"],
+                    st["pixarea"], st["cdelt0"], st["cdelt1"], st["crota2"], blo[0], blo[1], bhi[0], bhi[1],
+                    st["ltype"], st["sig_instr"], st["axtyp"], st["velsys"], P["lfreq0"], st["crval3"], st["cdelt3"],
+                    st["crpix3"], P["relint"], P["cd2i"])
     sm = fft_convolve(np.ascontiguousarray(m.transpose(2, 0, 1)), P["kernel"])
     sm[sm < 1e-12] = 0.
     sl = (slice(None), slice(blo[1], bhi[1]), slice(blo[0], bhi[0]))
     return O.sumsq_residuals(sm, P["data"][sl], P["mask"][sl], P["maskmode"], None)
 
 
-def setup_payload(dm, sr, nv, boxes, seed, data, mask, maskmode, like=None, rows=None, proto=None):
+def setup_payload(dm, sr, nv, boxes, seed, data, mask, maskmode, like=None, rows=None, proto=None,
+                  galmodtype="MC"):
     """The worker payload of a batch; like: a BatchLikelihood with a profile (set_profile) to recompute it."""
     st = dm.setup
     P = dict(setup=dict(nz=st.nsubs, radsep=st.radsep, cdens=st.cdens, cmode=st.cmode, pixarea=st.pixarea,
@@ -118,7 +127,8 @@ def setup_payload(dm, sr, nv, boxes, seed, data, mask, maskmode, like=None, rows
                         sig_instr=st.sig_instr, axtyp=st.axtyp, velsys=st.velsys, crval3=st.crval3,
                         cdelt3=st.cdelt3, crpix3=st.crpix3, chwidth=st._chmin, zstep=st.zstep),
              sr=sr, nv=nv, boxes=boxes, seed=seed, lfreq0=st.lfreq0, relint=st.relint, cd2i=st.cd2i,
-             kernel=dm.cfield, data=data, mask=mask, maskmode=maskmode, prof=None)
+             kernel=dm.cfield, data=data, mask=mask, maskmode=maskmode, prof=None, galmodtype=galmodtype.upper(),
+             vedges=st._vedges_lines)
     if like is not None and like._prof is not None:
         from bbarolo2_gb300.rings import RING_KEYS
         pr = like._prof

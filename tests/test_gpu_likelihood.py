@@ -23,13 +23,20 @@ def _setup(wl, noise=0.01, seed=0):
     return dm, rings, data, mask, sigma, O
 
 
-def _oracle_ss(dm, O, sr, nv, box, seed, data, mask, maskmode):
+def _oracle_ss(dm, O, sr, nv, box, seed, data, mask, maskmode, galmodtype="MC"):
     st = dm.setup
     (blo, bhi) = box
     m = np.zeros((bhi[1] - blo[1], bhi[0] - blo[0], st.nsubs))
-    O.galmod_mc(m, sr, 0, sr.shape[1], seed, st.radsep, nv, st.cdens, st.cmode, st.pixarea, st.cdelt[0],
-                st.cdelt[1], st.crota2, blo[0], blo[1], bhi[0], bhi[1], st.ltype, st.sig_instr, st.axtyp, st.velsys,
-                st.lfreq0, st.crval3, st.cdelt3, st.crpix3, st.relint, st.cd2i)
+    if galmodtype == "ANALYTIC":
+        nzq = 1 if not np.any(sr[6] > 0) else 1024
+        O.galmod_analytic(m, sr, 0, sr.shape[1], st.radsep, st.cdens, st.pixarea, st.cdelt[0], st.cdelt[1],
+                          st.crota2, blo[0], blo[1], bhi[0], bhi[1], st.ltype, st.sig_instr, st._vedges_lines,
+                          st.relint, st.cd2i, nzq, st.axtyp, st.velsys, st.lfreq0, st.crval3, st.cdelt3, st.crpix3,
+                          st._chmin, None, st.zstep)
+    else:
+        O.galmod_mc(m, sr, 0, sr.shape[1], seed, st.radsep, nv, st.cdens, st.cmode, st.pixarea, st.cdelt[0],
+                    st.cdelt[1], st.crota2, blo[0], blo[1], bhi[0], bhi[1], st.ltype, st.sig_instr, st.axtyp,
+                    st.velsys, st.lfreq0, st.crval3, st.cdelt3, st.crpix3, st.relint, st.cd2i)
     sm = O.conv_same(m.transpose(2, 0, 1), dm.cfield, dm.scalefactor)
     sl = (slice(None), slice(blo[1], bhi[1]), slice(blo[0], bhi[0]))
     return O.sumsq_residuals(sm, data[sl], mask[sl], maskmode, None)
@@ -57,6 +64,32 @@ def test_batch_likelihood_vs_oracle(gpu_lib, wl, maskmode):
     np.testing.assert_array_equal(ss, ss2)
     lg = L.finish(ss, np.zeros(5), boxes)
     assert np.argmax(lg) == 0
+
+
+@pytest.mark.parametrize("wl,nb", [("classic64", 5), ("global160", 3)])
+def test_batch_likelihood_analytic_vs_oracle(gpu_lib, wl, nb):
+    """The ANALYTIC model in the batch path: members that differ in every ring value but the radii (including the
+    layer height, which changes the vertical grids and the boxes)."""
+    from bbarolo2_gb300 import engine
+    from bbarolo2_gb300.galmod import ring_rows_batch
+    from bbarolo2_gb300.rings import RING_KEYS
+    dm, rings, data, mask, sigma, O = _setup(wl)
+    L = engine.BatchLikelihood(dm, data, mask, maskmode=2, sigma=sigma)
+    g = np.random.default_rng(5)
+    rows = ring_rows_batch([rings] * nb)
+    rows[1:, 4] *= 1 + 0.05 * g.standard_normal((nb - 1, rings.nr))
+    rows[1, 5] *= 1.3
+    rows[2, RING_KEYS.index("z0")] += 6.
+    if nb > 3:
+        rows[3, 12] += 4.
+        rows[4, 13] -= 6.
+    sr, nv, descs, boxes = L.prepare(rows, rings, seed=1)
+    ss, _ = L.run(sr, nv, descs, galmodtype="ANALYTIC")
+    for k in range(nb):
+        ref = _oracle_ss(dm, O, sr[k], nv[k], boxes[k], 1, data, mask, 2, galmodtype="ANALYTIC")
+        assert abs(ss[k] - ref) <= SS_RTOL * ref, (k, ss[k], ref)
+    ss2, _ = L.run(sr, nv, descs, galmodtype="ANALYTIC")
+    np.testing.assert_array_equal(ss, ss2)
 
 
 def test_fracerr_and_region(gpu_lib):

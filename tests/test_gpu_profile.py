@@ -111,14 +111,16 @@ def _batch_workload(B=5):
     return dm, L, rings, rows, data
 
 
-def test_batch_profile_vs_oracle(gpu_lib, oracle_lib):
+@pytest.mark.parametrize("galmodtype", ["MC", "ANALYTIC"])
+def test_batch_profile_vs_oracle(gpu_lib, oracle_lib, galmodtype):
     from oracle import cpu_baseline as CB
     dm, L, rings, rows, data = _batch_workload()
-    ll = L.evaluate(rows, rings, seed=1)
+    ll = L.evaluate(rows, rings, seed=1, galmodtype=galmodtype)
     x, st = L.last_profile()
     assert np.all(st == 0), st
     sr, nv, descs, boxes = L.prepare(rows, rings, seed=1)
-    P = CB.setup_payload(dm, sr, nv, boxes, 1, data, L.mask, L.maskmode, like=L, rows=rows, proto=rings)
+    P = CB.setup_payload(dm, sr, nv, boxes, 1, data, L.mask, L.maskmode, like=L, rows=rows, proto=rings,
+                         galmodtype=galmodtype)
     CB._W.clear()
     CB._W.update(P)
     for k in range(len(rows)):
@@ -128,5 +130,5 @@ def test_batch_profile_vs_oracle(gpu_lib, oracle_lib):
         ll_ref = L.finish(np.array([ss]), np.zeros(1), [boxes[k]])[0]
         assert abs(ll[k] - ll_ref) <= SS_RTOL * abs(ll_ref), (k, ll[k], ll_ref)
     # the profile is recomputed at each run: a second evaluation gives the same values
-    ll2 = L.evaluate(rows, rings, seed=1)
+    ll2 = L.evaluate(rows, rings, seed=1, galmodtype=galmodtype)
     np.testing.assert_array_equal(ll, ll2)
