@@ -14,6 +14,7 @@
 #include <math.h>
 #include <stdint.h>
 
+#include "anpix.cuh"
 #include "devmath.cuh"
 #include "kernels.h"
 
@@ -31,10 +32,6 @@ __device__ __forceinline__ double phi_interp(double t, const double *__restrict_
     const int k = (int)x;
     const double t0 = tab[k], t1 = tab[k + 1];
     return __dadd_rn(t0, __dmul_rn(__dsub_rn(x, (double)k), __dsub_rn(t1, t0)));
-}
-
-__device__ __forceinline__ int clamp_pix(long long v) {
-    return v < -(1LL << 30) ? -(1 << 30) : (v > (1LL << 30) ? (1 << 30) : (int)v);
 }
 
 // bbarolo/galmod.py:400-406: the pixel of the vertical sample at height z (z = 0 for a thin layer)
@@ -167,7 +164,8 @@ __global__ void __launch_bounds__(AN_WPB * 32) k_an_model(GridDev g, const AnSub
                                                           const double *__restrict__ cd2i,
                                                           const double *__restrict__ ptab,
                                                           const MemberDev *__restrict__ mem,
-                                                          unsigned long long *__restrict__ out64, long long mstride) {
+                                                          unsigned long long *__restrict__ out64, long long mstride,
+                                                          int skip_fast) {
     extern __shared__ double an_smem[];
     __shared__ AnWarp wsm[AN_WPB];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -178,6 +176,7 @@ __global__ void __launch_bounds__(AN_WPB * 32) k_an_model(GridDev g, const AnSub
     double caz, saz, R;
     if (!an_sample(gs, nsamp, nsub, subs, sbase, ssub, cs, k, Sp, caz, saz, R)) return;
     const AnSub &S = *Sp;
+    if (skip_fast && S.anfast) return;                 // (k_an_model_fast's samples)
     const double wside = caz >= 0.0 ? S.wrec : S.wapp;
     if (wside == 0.0) return;
     const MemberDev &M = mem[k];
@@ -263,6 +262,155 @@ __global__ void __launch_bounds__(AN_WPB * 32) k_an_model(GridDev g, const AnSub
     }
 }
 
+// ------------------------------------------------------------------------------ the model's float32 path
+// Sub-rings with one line on a linear channel map and a velocity independent of the height (anfast): one warp
+// per (member, azimuth sample).
+//   pixels  lanes over heights, float32 with a rounding bound and exact fallbacks (sample_pixel), the reference's
+//           pixel of every height;
+//   runs    consecutive heights in one pixel (a ballot of the run starts), their weights by a segmented scan
+//           (float32), a run crossing a pass of 32 heights carried to the next pass;
+//   line    computed at the first run in the box: the velocity in float64 in the reference's order, its channel
+//           kc exactly (float64 linear map, the reference's _velgrid within 1e-9 of a half-integer), then the
+//           channel-integrated profile over kc - K .. kc + K in float32: the edges relative to a reference
+//           velocity in float-float (so that (edge - v) / sig keeps ~1e-7), the normal CDF from the reference's
+//           table (float32 copy, linear interpolation as _phi);
+//   deposit lanes over channels, 64-bit fixed-point atomics of profile x amplitude x run weight (float32
+//           products, each rounded to the unit 2^-e: exact and order-independent sums).
+#define ANF_WPB 8
+
+__device__ __forceinline__ float phi_f32(float t, const float *__restrict__ tab) {
+    const float x = (t + 6.0f) * 512.0f;
+    if (!(x > 0.0f)) return 0.0f;
+    if (x >= (float)(PHI_N - 1)) return 1.0f;
+    const int k = (int)x;
+    const float t0 = __ldg(tab + k), t1 = __ldg(tab + k + 1);
+    return fmaf(x - (float)k, t1 - t0, t0);
+}
+
+__global__ void __launch_bounds__(ANF_WPB * 32) k_an_model_fast(GridDev g, const AnSub *__restrict__ subs, int nsub,
+                                                                const int *__restrict__ sbase,
+                                                                const int *__restrict__ ssub,
+                                                                const double2 *__restrict__ cs,
+                                                                const float2 *__restrict__ csf, long long nsamp,
+                                                                int nb, const double *__restrict__ zq,
+                                                                const float *__restrict__ zqf,
+                                                                const float *__restrict__ wqf,
+                                                                const float2 *__restrict__ vef,
+                                                                const float *__restrict__ cd2if,
+                                                                const float *__restrict__ ptabf,
+                                                                const MemberDev *__restrict__ mem,
+                                                                unsigned long long *__restrict__ out64,
+                                                                long long mstride) {
+    extern __shared__ float anf_smem[];                     // per warp: the CDF at the edges, the profile
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long gs = (long long)blockIdx.x * ANF_WPB + w;
+    if (gs >= nsamp * nb) return;
+    const int k = (int)(gs / nsamp);
+    const long long s = gs - (long long)k * nsamp;
+    const int ir = ssub[s];
+    const AnSub &S = subs[(size_t)k * nsub + ir];
+    if (!S.active || !S.anfast) return;
+    const float2 cf = csf[s];
+    const bool rec = cf.x >= 0.0f;                          // (the sign of the float32 table is the float64 test's)
+    if (S.wzero & (rec ? 1 : 2)) return;
+    const int kr = (int)(s - sbase[ir]) >= S.naz ? 1 : 0;
+    const PixF px = pix_setup(S, kr, cf);
+    const MemberDev &M = mem[k];
+    const int nz = g.nz, nzz = S.nzz, off = S.zq_off;
+    float *phe = anf_smem + (size_t)w * 2 * (nz + 2);
+    float *prof = phe + nz + 2;
+    unsigned long long *o64 = out64 + (size_t)k * mstride;
+    int k0 = 0, nk = -1;                                    // the line's channels (nk < 0: not computed yet)
+    auto line = [&]() {
+        // bbarolo/galmod.py:407 and :410 (_velgrid, _lround)
+        const double2 c = cs[s];
+        const double vplane = __dadd_rn(__dadd_rn(S.vsys, __dmul_rn(__dadd_rn(__dmul_rn(S.vrot, c.x),
+                                                                              __dmul_rn(S.vrad, c.y)), S.sinc)),
+                                        __dmul_rn(S.vvert, S.cinc));
+        const double chd = __dadd_rn(__dmul_rn(vplane, g.ia0), g.ib0);
+        const double fr = __dsub_rn(chd, floor(chd));
+        const long long kc = fabs(__dsub_rn(fr, 0.5)) > 1e-9 ? (long long)floor(__dadd_rn(chd, 0.5))
+                                                              : lround_ref(velgrid_exact(vplane, g, 0));
+        long long a0 = kc - S.K, a1 = kc + S.K + 1;
+        if (a0 < 0) a0 = 0;
+        if (a1 > nz) a1 = nz;
+        if (a1 <= a0) {
+            nk = 0;
+            return;
+        }
+        k0 = (int)a0;
+        nk = (int)(a1 - a0);
+        const double vr = __dsub_rn(vplane, g.vref);
+        const float vrh = (float)vr, vrl = (float)__dsub_rn(vr, (double)vrh);
+        const float amp = (float)__dmul_rn(__dmul_rn(S.a[0], rec ? S.wrec : S.wapp), ldexp(1.0, M.fix_exp));
+        for (int j = lane; j <= nk; j += 32) {
+            const float2 e = __ldg(vef + k0 + j);
+            const float t = (__fsub_rn(e.x, vrh) + __fsub_rn(e.y, vrl)) * S.invf;
+            phe[j] = phi_f32(t, ptabf);
+        }
+        __syncwarp();
+        for (int j = lane; j < nk; j += 32) prof[j] = fabsf(phe[j + 1] - phe[j]) * __ldg(cd2if + k0 + j) * amp;
+        __syncwarp();
+    };
+    auto deposit = [&](int g0, int g1, float ws) {          // (warp-uniform arguments)
+        if (g0 < M.blo0 || g0 >= M.bhi0 || g1 < M.blo1 || g1 >= M.bhi1) return;
+        if (nk < 0) line();
+        if (nk == 0) return;
+        unsigned long long *o = o64 + ((size_t)(g1 - M.blo1) * M.bx + (size_t)(g0 - M.blo0)) * nz + k0;
+        for (int j = lane; j < nk; j += 32) {
+            const long long q = f32_to_ll(prof[j] * ws);
+            if (q) atomicAdd(o + j, (unsigned long long)q);
+        }
+    };
+    bool open = false;                                      // a run carried from the previous pass
+    int cg0 = 0, cg1 = 0;
+    float cws = 0.0f;
+    for (int base = 0; base < nzz; base += 32) {
+        const int cnt = min(32, nzz - base);
+        const bool valid = lane < cnt;
+        int g0 = 0x7fffffff, g1 = 0x7fffffff;
+        float wv = 0.0f;
+        if (valid) {
+            sample_pixel(S, px, kr, cs + s, nzz, nzz > 1 ? zqf[off + base + lane] : 0.f, zq + off + base + lane,
+                         g.cdelt0, g.cdelt1, g0, g1);
+            wv = wqf[off + base + lane];
+        }
+        const int pg0 = __shfl_up_sync(FULL, g0, 1), pg1 = __shfl_up_sync(FULL, g1, 1);
+        const bool start = valid && (lane == 0 ? (!open || g0 != cg0 || g1 != cg1) : (g0 != pg0 || g1 != pg1));
+        const unsigned smask = __ballot_sync(FULL, start);
+        if (open && (smask & 1u)) {                         // the carried run ended with the previous pass
+            deposit(cg0, cg1, cws);
+            open = false;
+        }
+        // segmented inclusive scan of the weights (a segment: from a run start to the lane before the next)
+        const unsigned upto = smask & (0xffffffffu >> (31 - lane));
+        const int head = upto ? 31 - __clz(upto) : 0;
+        float v = wv;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const float t = __shfl_up_sync(FULL, v, d);
+            if (lane - d >= head) v += t;
+        }
+        if (!upto && open) v += cws;                        // (the lanes that continue the carried run)
+        const bool nstart = lane < 31 && ((smask >> (lane + 1)) & 1u);
+        const bool last = lane == cnt - 1;
+        const bool final_pass = base + 32 >= nzz;
+        const bool done = valid && ((!last && nstart) || (last && final_pass));
+        unsigned dmask = __ballot_sync(FULL, done);
+        while (dmask) {
+            const int e = __ffs(dmask) - 1;
+            dmask &= dmask - 1;
+            deposit(__shfl_sync(FULL, g0, e), __shfl_sync(FULL, g1, e), __shfl_sync(FULL, v, e));
+        }
+        if (!final_pass) {
+            cg0 = __shfl_sync(FULL, g0, cnt - 1);
+            cg1 = __shfl_sync(FULL, g1, cnt - 1);
+            cws = __shfl_sync(FULL, v, cnt - 1);
+            open = true;
+        }
+    }
+}
+
 // Ring maps: maps64 (nr, by, bx) += fixed-point weights of the runs (bbarolo/galmod.py:518-529).
 __global__ void __launch_bounds__(AN_WPB * 32) k_an_maps(GridDev g, const AnSub *__restrict__ subs, int nsub,
                                                          const int *__restrict__ sbase, const int *__restrict__ ssub,
@@ -326,14 +474,30 @@ size_t an_smem_bytes(int nz, int nlines) { return (size_t)AN_WPB * nlines * (nz 
 void launch_an_model(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase, const int *ssub,
                      const double *cs, long long nsamp, int nb, const double *zq, const double *wq,
                      const double *vedges, const double *cd2i, const double *ptab, const MemberDev *mem,
-                     long long *out64, long long mstride) {
+                     long long *out64, long long mstride, int skip_fast) {
     const long long nw = nsamp * nb;
     if (nw == 0) return;
     const size_t smem = an_smem_bytes(g.nz, g.nlines);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_an_model, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_an_model<<<(unsigned)((nw + AN_WPB - 1) / AN_WPB), AN_WPB * 32, smem, s>>>(
         g, subs, nsub, sbase, ssub, (const double2 *)cs, nsamp, nb, zq, wq, vedges, cd2i, ptab, mem,
-        (unsigned long long *)out64, mstride);
+        (unsigned long long *)out64, mstride, skip_fast);
+}
+
+size_t an_fast_smem_bytes(int nz) { return (size_t)ANF_WPB * 2 * (nz + 2) * sizeof(float); }
+
+void launch_an_model_fast(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase,
+                          const int *ssub, const double *cs, const float *csf, long long nsamp, int nb,
+                          const double *zq, const float *zqf, const float *wqf, const float *vef, const float *cd2if,
+                          const float *ptabf, const MemberDev *mem, long long *out64, long long mstride) {
+    const long long nw = nsamp * nb;
+    if (nw == 0) return;
+    const size_t smem = an_fast_smem_bytes(g.nz);
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(k_an_model_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_an_model_fast<<<(unsigned)((nw + ANF_WPB - 1) / ANF_WPB), ANF_WPB * 32, smem, s>>>(
+        g, subs, nsub, sbase, ssub, (const double2 *)cs, (const float2 *)csf, nsamp, nb, zq, zqf, wqf,
+        (const float2 *)vef, cd2if, ptabf, mem, (unsigned long long *)out64, mstride);
 }
 
 void launch_an_maps(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase, const int *ssub,

@@ -1,0 +1,94 @@
+// Pixels of the ANALYTIC samples (bbarolo/galmod.py:400-406 and :514-517) in float32 with a rounding bound, shared
+// by the ring maps and the model's fast path.
+//
+// The pixel is computed in float32 as xpos + R caz P1 - R saz P2 + z P3 (and the same for y). Counting the
+// roundings (R, caz, the coefficients, z0 and the height each rounded to float32, then 2 products per term and 3
+// sums), the float32 value is within 8u (|xpos| + |t1| + |t2| + |t3|) + u (|x| + 1/2) of the exact one, u = 2^-24;
+// the reference's float64 value is within 1e-12 of it. MAPS_EPS = 16u (twice that bound): when the float32 value
+// lies within MAPS_EPS x (|xpos| + |t1| + |t2| + |t3| + 1) of a half-integer, the pixel is recomputed in
+// float-float (pixel_ff) and, if that is too close as well, with the reference's float64 operations.
+#pragma once
+
+#include "devmath.cuh"
+#include "internal.h"
+
+#define MAPS_EPS 9.5367431640625e-07f
+
+namespace {
+
+__device__ __forceinline__ bool round_fast(float v, float eps, int &out) {
+    if (!(fabsf(v) < 1.0e6f)) return false;
+    const float f = __fadd_rn(v, 0.5f);
+    float fl;
+    const int i = floor_small(f, fl);
+    const float d = __fsub_rn(f, fl);
+    if (d < eps || d > 1.0f - eps) return false;
+    out = i;
+    return true;
+}
+
+__device__ __forceinline__ int clamp_pix(long long v) {
+    return v < -(1LL << 30) ? -(1 << 30) : (v > (1LL << 30) ? (1 << 30) : (int)v);
+}
+
+// The pixel of a sample at height zq z0 in float-float (x = xpos + R caz P1 - R saz P2 + z P3, y likewise);
+// false if either coordinate is within 1e-6 of a rounding boundary.
+__device__ __noinline__ bool pixel_ff(const AnSub &S, int kr, double2 c, double zq, int &g0, int &g1) {
+    const ff R = {S.Rf[kr], S.Rl[kr]};
+    const ff A = ff_mul(R, ff_of(c.x)), B = ff_mul(R, ff_of(c.y));
+    const ff z = ff_mul(ff_of(zq), ff{S.z0f, S.z0l});
+    const ff T2 = ff_mul(B, ff{S.P2, S.P2l});
+    const ff x = ff_add(ff_add(ff_add(ff{S.xposf, S.xposl}, ff_mul(A, ff{S.P1, S.P1l})), ff{-T2.hi, -T2.lo}),
+                        ff_mul(z, ff{S.P3, S.P3l}));
+    const ff y = ff_add(ff_add(ff_add(ff{S.yposf, S.yposl}, ff_mul(A, ff{S.Q1, S.Q1l})), ff_mul(B, ff{S.Q2, S.Q2l})),
+                        ff_mul(z, ff{S.Q3, S.Q3l}));
+    return ff_round(x, g0) && ff_round(y, g1);
+}
+
+// The float32 part of a sample's pixels: x = bxf + zf P3, y = byf + zf Q3 with their magnitude sums xa, ya.
+struct PixF {
+    float bxf, byf, xa, ya, z0f, P3, Q3;
+};
+
+__device__ __forceinline__ PixF pix_setup(const AnSub &S, int kr, float2 cf) {
+    const float Rf = S.Rf[kr];
+    const float a1 = Rf * cf.x, a2 = Rf * cf.y;
+    const float t1 = a1 * S.P1, t2 = a2 * S.P2, u1 = a1 * S.Q1, u2 = a2 * S.Q2;
+    PixF p;
+    p.bxf = S.xposf + (t1 - t2);
+    p.byf = S.yposf + (u1 + u2);
+    p.xa = fabsf(S.xposf) + fabsf(t1) + fabsf(t2) + 1.0f;
+    p.ya = fabsf(S.yposf) + fabsf(u1) + fabsf(u2) + 1.0f;
+    p.z0f = S.z0f;
+    p.P3 = S.P3;
+    p.Q3 = S.Q3;
+    return p;
+}
+
+// The reference's pixel of a height (zqf its float32 value, *zqp the float64 one; float32 when safely away from
+// a boundary); cp: the sample's cos/sin in float64.
+__device__ __forceinline__ void sample_pixel(const AnSub &S, const PixF &p, int kr, const double2 *cp, int nzz,
+                                             float zqf, const double *zqp, double cdelt0, double cdelt1, int &g0,
+                                             int &g1) {
+    const float zf = nzz > 1 ? zqf * p.z0f : 0.f;
+    const float t3 = zf * p.P3, u3 = zf * p.Q3;
+    if (round_fast(p.bxf + t3, (p.xa + fabsf(t3)) * MAPS_EPS, g0) &&
+        round_fast(p.byf + u3, (p.ya + fabsf(u3)) * MAPS_EPS, g1))
+        return;
+    const double2 c = *cp;
+    const double zq = nzz > 1 ? *zqp : 0.0;
+    if (!pixel_ff(S, kr, c, zq, g0, g1)) {
+        // bbarolo/galmod.py:514-517 in the reference's float64 operations
+        const double R = S.R[kr];
+        const double x = __dmul_rn(R, c.x);
+        const double yb = __dmul_rn(__dmul_rn(R, c.y), S.cinc);
+        const double z = nzz > 1 ? __dmul_rn(zq, S.z0) : 0.0;
+        const double y = __dsub_rn(yb, __dmul_rn(z, S.sinc));
+        g0 = clamp_pix(lround_ref(
+            __dadd_rn(S.xpos, __ddiv_rn(__dsub_rn(__dmul_rn(x, S.spa), __dmul_rn(y, S.cpa)), cdelt0))));
+        g1 = clamp_pix(lround_ref(
+            __dadd_rn(S.ypos, __ddiv_rn(__dadd_rn(__dmul_rn(x, S.cpa), __dmul_rn(y, S.spa)), cdelt1))));
+    }
+}
+
+}  // namespace

@@ -48,6 +48,8 @@ struct bbgpu_ctx {
     std::vector<double> h_cd2i;
     double *d_vedges = nullptr;   // channel edges per line (nlines, nz + 1): ANALYTIC models
     double *d_ptab = nullptr;     // normal CDF table of the ANALYTIC line profiles
+    float *d_ptabf = nullptr;     // (float32 copy: the model's fast path)
+    float2 *d_vef = nullptr;      // channel edges of line 0 - vref, float-float (nz + 1): the model's fast path
     ZigDev *d_zig = nullptr;
     float *d_taps = nullptr;
     int ky = 0, kx = 0, kxw = 0;
@@ -134,6 +136,8 @@ struct bbgpu_ctx {
     size_t d_asbase_cap = 0, d_assub_cap = 0;
     double *d_acs = nullptr, *d_azq = nullptr, *d_awq = nullptr;
     size_t d_acs_cap = 0, d_azq_cap = 0, d_awq_cap = 0;
+    float *d_acsf = nullptr, *d_azqf = nullptr, *d_awqf = nullptr;
+    size_t d_acsf_cap = 0, d_azqf_cap = 0, d_awqf_cap = 0;
     long long *d_model_fx = nullptr;
     size_t d_model_fx_cap = 0;
     long long ansamp = 0;
@@ -396,7 +400,7 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
             bbh_layout_free(&E.host);
         }
     cudaFree(ctx->d_cd2i); cudaFree(ctx->d_cd2if); cudaFree(ctx->d_zig); cudaFree(ctx->d_taps);
-    cudaFree(ctx->d_vedges); cudaFree(ctx->d_ptab);
+    cudaFree(ctx->d_vedges); cudaFree(ctx->d_ptab); cudaFree(ctx->d_ptabf); cudaFree(ctx->d_vef);
     cudaFree(ctx->d_data); cudaFree(ctx->d_mask); cudaFree(ctx->d_region);
     for (auto &a : ctx->d_deff)
         for (auto &b : a) cudaFree(b);
@@ -414,7 +418,8 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
                     (void *)ctx->d_pmem})
         cudaFree(q);
     for (void *q : {(void *)ctx->d_asub, (void *)ctx->d_asbase, (void *)ctx->d_assub, (void *)ctx->d_acs,
-                    (void *)ctx->d_azq, (void *)ctx->d_awq, (void *)ctx->d_model_fx})
+                    (void *)ctx->d_azq, (void *)ctx->d_awq, (void *)ctx->d_model_fx, (void *)ctx->d_acsf,
+                    (void *)ctx->d_azqf, (void *)ctx->d_awqf})
         cudaFree(q);
     cudaFreeHost(ctx->h_asub);
     cudaFreeHost(ctx->h_psub);
@@ -496,6 +501,14 @@ extern "C" int bbgpu_set_grid(bbgpu_ctx *ctx, const bbgpu_grid *gr, const double
         }
     }
     g.fast_ok = (g.axtyp == 4 && g.nlines == 1) || (g.axtyp == 3 && g.velsys == 1);
+    if (g.axtyp == 4) {
+        g.ia0 = g.ia;
+        g.ib0 = g.ib;
+    } else {
+        g.ia0 = -lfreq0[0] / (2.99792458e08 * g.cdelt3);
+        g.ib0 = (lfreq0[0] - g.crval3) / g.cdelt3 + g.crpix3 - 1;
+    }
+    g.vref = g.nz > 0 && vedges ? vedges[g.nz / 2] : 0.0;    // (the middle channel edge of line 0)
     std::vector<float> cf(g.nz);
     for (int i = 0; i < g.nz; i++) cf[i] = (float)cd2i[i];
     cudaFree(ctx->d_cd2i);
@@ -508,17 +521,30 @@ extern "C" int bbgpu_set_grid(bbgpu_ctx *ctx, const bbgpu_grid *gr, const double
     CK(cudaMemcpy(ctx->d_cd2if, cf.data(), g.nz * sizeof(float), cudaMemcpyHostToDevice));
     ctx->h_cd2i.assign(cd2i, cd2i + g.nz);
     cudaFree(ctx->d_vedges);
+    cudaFree(ctx->d_vef);
     ctx->d_vedges = nullptr;
+    ctx->d_vef = nullptr;
     if (vedges) {
         const size_t ne = (size_t)g.nlines * (g.nz + 1);
         CK(cudaMalloc(&ctx->d_vedges, ne * sizeof(double)));
         CK(cudaMemcpy(ctx->d_vedges, vedges, ne * sizeof(double), cudaMemcpyHostToDevice));
+        std::vector<float2> vef(g.nz + 1);
+        for (int k = 0; k <= g.nz; k++) {
+            const double d = vedges[k] - g.vref;
+            vef[k].x = (float)d;
+            vef[k].y = (float)(d - (double)vef[k].x);
+        }
+        CK(cudaMalloc(&ctx->d_vef, vef.size() * sizeof(float2)));
+        CK(cudaMemcpy(ctx->d_vef, vef.data(), vef.size() * sizeof(float2), cudaMemcpyHostToDevice));
     }
     if (!ctx->d_ptab) {
         std::vector<double> tab(6146);
         bbh_phi_table(tab.data());
+        std::vector<float> tf(tab.begin(), tab.end());
         CK(cudaMalloc(&ctx->d_ptab, tab.size() * sizeof(double)));
         CK(cudaMemcpy(ctx->d_ptab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CK(cudaMalloc(&ctx->d_ptabf, tf.size() * sizeof(float)));
+        CK(cudaMemcpy(ctx->d_ptabf, tf.data(), tf.size() * sizeof(float), cudaMemcpyHostToDevice));
     }
     // deposit tile: pixels x channels of 8-byte sums within 56 KB (3 CTAs per SM with the staging buffers)
     int tp = 57344 / (8 * g.nz);
@@ -670,6 +696,10 @@ static int batch_prepare_analytic(bbgpu_ctx *ctx, int nb, int nsub, const double
         if ((rc = dgrow(ctx, &ctx->d_asbase, &ctx->d_asbase_cap, sbase.size()))) return rc;
         if ((rc = dgrow(ctx, &ctx->d_assub, &ctx->d_assub_cap, ssub.size() ? ssub.size() : 1))) return rc;
         if ((rc = dgrow(ctx, &ctx->d_acs, &ctx->d_acs_cap, cs.size() ? cs.size() : 1))) return rc;
+        std::vector<float> csf;
+        bbh_an_samples_f32(cs, csf);
+        if ((rc = dgrow(ctx, &ctx->d_acsf, &ctx->d_acsf_cap, csf.size() ? csf.size() : 1))) return rc;
+        if (csf.size()) CK(cudaMemcpy(ctx->d_acsf, csf.data(), sizeof(float) * csf.size(), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(ctx->d_asbase, sbase.data(), sizeof(int) * sbase.size(), cudaMemcpyHostToDevice));
         if (ssub.size()) CK(cudaMemcpy(ctx->d_assub, ssub.data(), sizeof(int) * ssub.size(), cudaMemcpyHostToDevice));
         if (cs.size()) CK(cudaMemcpy(ctx->d_acs, cs.data(), sizeof(double) * cs.size(), cudaMemcpyHostToDevice));
@@ -681,20 +711,29 @@ static int batch_prepare_analytic(bbgpu_ctx *ctx, int nb, int nsub, const double
     const size_t nz1 = zc.zq.size() + 1;
     if (zc.uploaded == 0 || nz1 > ctx->d_azq_cap) {
         if (nz1 > ctx->d_azq_cap) {
-            cudaFree(ctx->d_azq);
-            cudaFree(ctx->d_awq);
+            for (void *q : {(void *)ctx->d_azq, (void *)ctx->d_awq, (void *)ctx->d_azqf, (void *)ctx->d_awqf}) cudaFree(q);
             ctx->d_azq = ctx->d_awq = nullptr;
-            ctx->d_azq_cap = ctx->d_awq_cap = 0;
+            ctx->d_azqf = ctx->d_awqf = nullptr;
+            ctx->d_azq_cap = ctx->d_awq_cap = ctx->d_azqf_cap = ctx->d_awqf_cap = 0;
             if ((rc = dgrow(ctx, &ctx->d_azq, &ctx->d_azq_cap, 2 * nz1))) return rc;
             if ((rc = dgrow(ctx, &ctx->d_awq, &ctx->d_awq_cap, 2 * nz1))) return rc;
+            if ((rc = dgrow(ctx, &ctx->d_azqf, &ctx->d_azqf_cap, 2 * nz1))) return rc;
+            if ((rc = dgrow(ctx, &ctx->d_awqf, &ctx->d_awqf_cap, 2 * nz1))) return rc;
         }
         zc.uploaded = 0;
     }
     if (zc.zq.size() > zc.uploaded) {
         const size_t a0 = zc.uploaded, m = zc.zq.size() - a0;
+        std::vector<float> zf(m), wf(m);
+        for (size_t i = 0; i < m; i++) {
+            zf[i] = (float)zc.zq[a0 + i];
+            wf[i] = (float)zc.wq[a0 + i];
+        }
         CK(cudaMemcpy(ctx->d_azq + a0, zc.zq.data() + a0, sizeof(double) * m, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(ctx->d_awq + a0, zc.wq.data() + a0, sizeof(double) * m, cudaMemcpyHostToDevice));
-        ctx->h2d += (long long)(16 * m);
+        CK(cudaMemcpy(ctx->d_azqf + a0, zf.data(), sizeof(float) * m, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(ctx->d_awqf + a0, wf.data(), sizeof(float) * m, cudaMemcpyHostToDevice));
+        ctx->h2d += (long long)(24 * m);
         zc.uploaded = zc.zq.size();
     }
     if ((rc = dgrow(ctx, &ctx->d_asub, &ctx->d_asub_cap, (size_t)nb * (nsub ? nsub : 1)))) return rc;
@@ -864,9 +903,13 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
         if (tm)
             for (int i = 5; i <= 8; i++) CK(cudaEventRecord(ctx->ev[i], s));
         CK(cudaMemsetAsync(ctx->d_model_fx, 0, sizeof(long long) * (size_t)ctx->nb * ctx->mstride, s));
+        launch_an_model_fast(s, g, ctx->d_asub, ctx->nsub, ctx->d_asbase, ctx->d_assub, ctx->d_acs, ctx->d_acsf,
+                             ctx->ansamp, ctx->nb, ctx->d_azq, ctx->d_azqf, ctx->d_awqf, (const float *)ctx->d_vef,
+                             ctx->d_cd2if, ctx->d_ptabf, ctx->d_mem, ctx->d_model_fx, ctx->mstride);
+        CKL();
         launch_an_model(s, g, ctx->d_asub, ctx->nsub, ctx->d_asbase, ctx->d_assub, ctx->d_acs, ctx->ansamp, ctx->nb,
                         ctx->d_azq, ctx->d_awq, ctx->d_vedges, ctx->d_cd2i, ctx->d_ptab, ctx->d_mem, ctx->d_model_fx,
-                        ctx->mstride);
+                        ctx->mstride, 1);
         CKL();
         launch_fix_to_model(s, ctx->d_model_fx, ctx->d_mem, ctx->nb, ctx->mstride, g.nz, ctx->d_model,
                             ctx->want64 ? ctx->d_model64 : nullptr);
@@ -1209,7 +1252,7 @@ extern "C" int bbgpu_galmod_analytic(bbgpu_ctx *ctx, double *out, const double *
     CK(cudaMemcpyAsync(dm, &M, sizeof M, cudaMemcpyHostToDevice, s));
     CK(cudaMemsetAsync(o64, 0, n * sizeof(long long), s));
     launch_an_model(s, g, D.subs, ns, D.sbase, D.ssub, D.cs, D.nsamp, 1, D.zq, D.wq, ctx->d_vedges, ctx->d_cd2i,
-                    ctx->d_ptab, dm, o64, (long long)n);
+                    ctx->d_ptab, dm, o64, (long long)n, 0);
     CKL();
     std::vector<long long> h(n);
     CK(cudaMemcpyAsync(h.data(), o64, n * sizeof(long long), cudaMemcpyDeviceToHost, s));

@@ -600,6 +600,8 @@ int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0,
             split(S.R[1], S.Rf[1], S.Rl[1]);
         }
         S.wzero = (S.wrec == 0.0 ? 1 : 0) | (S.wapp == 0.0 ? 2 : 0);
+        S.invf = (float)S.inv;
+        S.anfast = !maps && !S.zdep && g->nlines == 1 && g->fast_ok;
         S.fluxscf = (float)S.fluxsc;
         S.wrecf = (float)S.wrec;
         S.wappf = (float)S.wapp;

@@ -47,6 +47,10 @@ struct AnSub {
     float P1l, P2l, P3l, Q1l, Q2l, Q3l, xposl, yposl, z0l;
     float Rl[2];
     int wzero;                      // bit 0: wrec == 0, bit 1: wapp == 0 (the float64 tests, done on the host)
+    // float32 fast path of a model (one line, a linear channel map, a velocity independent of the height):
+    // anfast = 1 when it applies, invf = 1 / sig
+    int anfast;
+    float invf;
 };
 
 // The constants of a context, as the kernels see them.
@@ -58,6 +62,9 @@ struct GridDev {
     double scalefactor, ia, ib;
     double lfreq0[BBGPU_MAXL], relint[BBGPU_MAXL];
     float lia[BBGPU_MAXL], lib[BBGPU_MAXL];  // channel = v * lia + lib per line (fast path)
+    // ANALYTIC fast path (one line, linear map): channel = v ia0 + ib0 in float64 (ia0, ib0 of line 0), and the
+    // reference velocity vref (the channel edges are kept relative to it in float-float)
+    double ia0, ib0, vref;
 };
 
 // A parsed MC stream (host copy): everything about the clouds that does not depend on the ring parameters.

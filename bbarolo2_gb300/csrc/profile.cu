@@ -27,6 +27,7 @@
 
 #include <algorithm>
 
+#include "anpix.cuh"
 #include "devmath.cuh"
 #include "kernels.h"
 
@@ -36,51 +37,15 @@
 
 namespace {
 
-__device__ __forceinline__ bool round_fast(float v, float eps, int &out) {
-    if (!(fabsf(v) < 1.0e6f)) return false;
-    const float f = __fadd_rn(v, 0.5f);
-    float fl;
-    const int i = floor_small(f, fl);
-    const float d = __fsub_rn(f, fl);
-    if (d < eps || d > 1.0f - eps) return false;
-    out = i;
-    return true;
-}
-
-__device__ __forceinline__ int clamp_pix(long long v) {
-    return v < -(1LL << 30) ? -(1 << 30) : (v > (1LL << 30) ? (1 << 30) : (int)v);
-}
-
-// The pixel of a sample at height zq z0 in float-float (x = xpos + R caz P1 - R saz P2 + z P3, y likewise);
-// false if either coordinate is within 1e-6 of a rounding boundary.
-__device__ __noinline__ bool pixel_ff(const AnSub &S, int kr, double2 c, double zq, int &g0, int &g1) {
-    const ff R = {S.Rf[kr], S.Rl[kr]};
-    const ff A = ff_mul(R, ff_of(c.x)), B = ff_mul(R, ff_of(c.y));
-    const ff z = ff_mul(ff_of(zq), ff{S.z0f, S.z0l});
-    const ff T2 = ff_mul(B, ff{S.P2, S.P2l});
-    const ff x = ff_add(ff_add(ff_add(ff{S.xposf, S.xposl}, ff_mul(A, ff{S.P1, S.P1l})), ff{-T2.hi, -T2.lo}),
-                        ff_mul(z, ff{S.P3, S.P3l}));
-    const ff y = ff_add(ff_add(ff_add(ff{S.yposf, S.yposl}, ff_mul(A, ff{S.Q1, S.Q1l})), ff_mul(B, ff{S.Q2, S.Q2l})),
-                        ff_mul(z, ff{S.Q3, S.Q3l}));
-    return ff_round(x, g0) && ff_round(y, g1);
-}
-
 // ------------------------------------------------------------------------------------------- ring maps
 // One thread per (member, azimuth sample); its heights in order, consecutive heights in one pixel merged into
-// a run (the reference's order), each run deposited into the maps of its one or two rings.
-//
-// The pixel is computed in float32 as xpos + R caz P1 - R saz P2 + z P3 (and the same for y). Counting the
-// roundings (R, caz, the coefficients, z0 and the height each rounded to float32, then 2 products per term and 3
-// sums), the float32 value is within 8u (|xpos| + |t1| + |t2| + |t3|) + u (|x| + 1/2) of the exact one, u = 2^-24;
-// the reference's float64 value is within 1e-12 of it. MAPS_EPS = 16u (twice that bound): when the float32 value
-// lies within MAPS_EPS x (|xpos| + |t1| + |t2| + |t3| + 1) of a half-integer, the pixel is recomputed with the
-// reference's float64 operations.
+// a run (the reference's order), each run deposited into the maps of its one or two rings. The pixels:
+// sample_pixel (float32 with a rounding bound, exact fallbacks).
 //
 // The finished runs of a thread wait in a shared-memory queue (pixel, weight) and are deposited by the whole
 // warp at once when a queue is full and at the end: the warp's loop over heights then carries no divergent
 // deposit code, and each drain pass keeps all lanes busy. The sums are 64-bit fixed point, so the order of
 // the deposits does not change the maps.
-#define MAPS_EPS 9.5367431640625e-07f
 #define MAPS_TB 128         // threads per CTA
 #define MAPS_QD 16          // queued runs per thread
 
@@ -101,7 +66,8 @@ __global__ void __launch_bounds__(MAPS_TB) k_an_maps_fast(GridDev g, const AnSub
     int k = 0, kr = 0, nzz = 0, off = 0, i0 = -1, i1 = -1;
     long long s = 0;
     const AnSub *S = subs;
-    float bxf = 0.f, byf = 0.f, xa = 0.f, ya = 0.f, z0f = 0.f, P3 = 0.f, Q3 = 0.f, v0 = 0.f, v1 = 0.f;
+    PixF px{};
+    float v0 = 0.f, v1 = 0.f;
     if (gs < nsamp * nb) {
         k = (int)(gs / nsamp);
         s = gs - (long long)k * nsamp;
@@ -112,18 +78,9 @@ __global__ void __launch_bounds__(MAPS_TB) k_an_maps_fast(GridDev g, const AnSub
         if (S->active && !(S->wzero & (rec ? 1 : 2))) {
             kr = (int)(s - sbase[ir]) >= S->naz ? 1 : 0;
             const float wsidef = rec ? S->wrecf : S->wappf;
-            const float Rf = S->Rf[kr];
-            const float a1 = Rf * cf.x, a2 = Rf * cf.y;
-            const float t1 = a1 * S->P1, t2 = a2 * S->P2, u1 = a1 * S->Q1, u2 = a2 * S->Q2;
-            bxf = S->xposf + (t1 - t2);
-            byf = S->yposf + (u1 + u2);
-            xa = fabsf(S->xposf) + fabsf(t1) + fabsf(t2) + 1.0f;
-            ya = fabsf(S->yposf) + fabsf(u1) + fabsf(u2) + 1.0f;
+            px = pix_setup(*S, kr, cf);
             nzz = S->nzz;
             off = S->zq_off;
-            z0f = S->z0f;
-            P3 = S->P3;
-            Q3 = S->Q3;
             const int e = fix_exp[k];
             i0 = widx[2 * ir];
             i1 = widx[2 * ir + 1];
@@ -164,24 +121,9 @@ __global__ void __launch_bounds__(MAPS_TB) k_an_maps_fast(GridDev g, const AnSub
     float rws = 0.f;
     for (int kz = 0; kz < nzmax; kz++) {
         if (kz < nzz) {
-            const float zf = nzz > 1 ? zqf[off + kz] * z0f : 0.f;
-            const float t3 = zf * P3, u3 = zf * Q3;
             int g0, g1;
-            if (!(round_fast(bxf + t3, (xa + fabsf(t3)) * MAPS_EPS, g0) &&
-                  round_fast(byf + u3, (ya + fabsf(u3)) * MAPS_EPS, g1)) &&
-                !pixel_ff(*S, kr, cs[s], nzz > 1 ? zq[off + kz] : 0.0, g0, g1)) {
-                // bbarolo/galmod.py:514-517 in the reference's float64 operations
-                const double2 c = cs[s];
-                const double R = S->R[kr];
-                const double x = __dmul_rn(R, c.x);
-                const double yb = __dmul_rn(__dmul_rn(R, c.y), S->cinc);
-                const double z = nzz > 1 ? __dmul_rn(zq[off + kz], S->z0) : 0.0;
-                const double y = __dsub_rn(yb, __dmul_rn(z, S->sinc));
-                g0 = clamp_pix(lround_ref(
-                    __dadd_rn(S->xpos, __ddiv_rn(__dsub_rn(__dmul_rn(x, S->spa), __dmul_rn(y, S->cpa)), g.cdelt0))));
-                g1 = clamp_pix(lround_ref(
-                    __dadd_rn(S->ypos, __ddiv_rn(__dadd_rn(__dmul_rn(x, S->cpa), __dmul_rn(y, S->spa)), g.cdelt1))));
-            }
+            sample_pixel(*S, px, kr, cs + s, nzz, nzz > 1 ? zqf[off + kz] : 0.f, zq + off + kz, g.cdelt0, g.cdelt1,
+                         g0, g1);
             const float w = wqf[off + kz];
             if (kz > 0 && g0 == rg0 && g1 == rg1) {
                 rws += w;
