@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(ANF_WPB * 32) k_an_model_fast(GridDev g, const
     const bool rec = cf.x >= 0.0f;                          // (the sign of the float32 table is the float64 test's)
     if (S.wzero & (rec ? 1 : 2)) return;
     const int kr = (int)(s - sbase[ir]) >= S.naz ? 1 : 0;
-    const PixF px = pix_setup(S, kr, cf);
+    const PixF px = pix_setup(S, kr, cf, zqf + S.zq_off, S.nzz);
     const MemberDev &M = mem[k];
     const int nz = g.nz, nzz = S.nzz, off = S.zq_off;
     float *phe = anf_smem + (size_t)w * 2 * (nz + 2);

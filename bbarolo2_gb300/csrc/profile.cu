@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(MAPS_TB) k_an_maps_fast(GridDev g, const AnSub
         if (S->active && !(S->wzero & (rec ? 1 : 2))) {
             kr = (int)(s - sbase[ir]) >= S->naz ? 1 : 0;
             const float wsidef = rec ? S->wrecf : S->wappf;
-            px = pix_setup(*S, kr, cf);
+            px = pix_setup(*S, kr, cf, zqf + S->zq_off, S->nzz);
             nzz = S->nzz;
             off = S->zq_off;
             const int e = fix_exp[k];
