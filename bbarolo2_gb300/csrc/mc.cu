@@ -791,18 +791,18 @@ __device__ __forceinline__ void px_flush(const GridDev &g, const LayoutDev &L, c
 }
 
 // The channels of this lane's SPL samples counted into the pixel's row (see k_mc_deposit_px). The float32
-// channels are binned relative to c0 = (channel of the lane's first sample) - 1 into a register histogram of 12
-// five-bit counts (a bin holds at most 31 samples unless all 32 of a 32-sample lane share one channel, counted
-// apart); a sample too close to a half-integer is left out and deferred to the warp's queue. A lane with more
-// than one such sample, a channel beyond the 12 bins (the channels of the samples are non-decreasing, so the
-// last one tells) or a centre out of range counts its samples one by one, with the exact channels where needed.
+// channels are binned relative to c0 = (channel of the lane's first sample) - 1 into a register histogram of 11
+// five-bit counts, one table increment per sample (a bin holds at most 31 samples unless all 32 of a 32-sample
+// lane share one channel, counted apart); a sample too close to a half-integer is left out and deferred to the
+// warp's queue. A lane with more than one such sample, a channel beyond the 11 bins (counted in the top bits) or
+// a centre out of range counts its samples one by one, with the exact channels where needed.
 // The lowest non-empty bin (the lane's first run, which the previous lane may share) is added in the ordered
 // pass of the group's LPP lanes; the other bins at once.
 template <int SPL>
 __device__ __forceinline__ void px_count(const GridDev &g, const LayoutDev &L, const ZigDev *zig,
                                          const SubMC *__restrict__ subk, const PxCloud &p, const float4 (&w)[SPL / 4],
                                          int i0, int q, unsigned long long *tile, int rowoff, PxDefer *qe, int *qn,
-                                         int *err) {
+                                         const unsigned long long *inc, int *err) {
     constexpr int LPP = 128 / SPL;
     const int nz = g.nz;
     unsigned long long *row = tile + rowoff;
@@ -813,8 +813,10 @@ __device__ __forceinline__ void px_count(const GridDev &g, const LayoutDev &L, c
     const long long fix = p.fix;
     const float fl0 = floorf(fmaf(w[0].x, sg, tc) + 0.5f) - 1.0f;
     const float hwf = fastc ? hw : -1.0f;                  // (a centre out of range: no sample passes)
-    // straight-line code (selects, no branches): bins 0..5 in lo, 6..11 in hi, five bits each
-    unsigned lo = 0, hi = 0, need = 0;
+    // straight-line code: each sample adds inc[min(channel - c0, 30)] (bins 0..10 five bits each, a channel
+    // beyond them one unit of bits 55..63; index 31: a sample left out)
+    unsigned long long H = 0;
+    unsigned need = 0;
     int dlast = 0;
 #pragma unroll
     for (int s = 0; s < SPL / 4; s++) {
@@ -828,15 +830,12 @@ __device__ __forceinline__ void px_count(const GridDev &g, const LayoutDev &L, c
             const bool ok = fabsf(f - fl - 0.5f) <= hwf;
             const int d = __float_as_int((fl - fl0) + 12582912.0f) - 0x4B400000;   // (exact: small integers)
             need |= (in & !ok) ? 1u << i : 0u;
-            const unsigned dd = (in & ok) ? (unsigned)d : 31u;
-            lo += dd < 6u ? 1u << (5 * dd) : 0u;
-            hi += dd - 6u < 6u ? 1u << (5 * (dd - 6u)) : 0u;
-            dlast = (in & ok) ? d : dlast;
+            H += inc[(in & ok) ? min((unsigned)d, 30u) : 31u];
+            if (SPL == 32) dlast = (in & ok) ? d : dlast;
         }
     }
-    const unsigned long long H = (unsigned long long)lo | ((unsigned long long)hi << 30);
     int fch = (int)0x80000000, fcnt = 0;
-    if (__popc(need) <= 1 && (unsigned)dlast < 12u) {
+    if (__popc(need) <= 1 && (H >> 55) == 0) {
         if (need) {
             const int slot = atomicAdd(qn, 1);
             qe[slot] = PxDefer{p.c, p.pb, p.nv, i0 + __ffs(need) - 1, fix, rowoff, 0};
@@ -850,7 +849,7 @@ __device__ __forceinline__ void px_count(const GridDev &g, const LayoutDev &L, c
             fch = c0 + (one ? dlast : blo);
             fcnt = one ? 32 : (int)((H >> (5 * blo)) & 31);
 #pragma unroll
-            for (int b = 0; b < 12; b++) {
+            for (int b = 0; b < 11; b++) {
                 const int cnt = (int)((H >> (5 * b)) & 31);
                 const int ch = c0 + b;
                 const bool put = !one & (cnt != 0) & (b != blo) & ((unsigned)ch < (unsigned)nz);
@@ -913,10 +912,12 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
                                                               int *err) {
     constexpr int LPP = 128 / SPL;
     extern __shared__ unsigned long long tile[];           // TP rows of fixed-point sums, queues, nz scales
+    __shared__ unsigned long long inc[32];                 // the histogram increments of px_count
     const int k = blockIdx.x;
     const int t = blockIdx.y;
     const int ntx = mem[k].ntx;
     if (t >= ntx * mem[k].nty) return;
+    if (threadIdx.x < 32) inc[threadIdx.x] = threadIdx.x < 11 ? 1ull << (5 * threadIdx.x) : (threadIdx.x < 31 ? 1ull << 55 : 0ull);
     constexpr int G = 32 / LPP;                             // pixels per warp
     const int nz = g.nz, RS = nz + 2 * G;
     const int TP = tx * ty;
@@ -972,7 +973,7 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
         px_samples<SPL>(L, cb, i0, wb);
         PxCloud cn;
         px_entry(bucket, beg, n, j + 2, cn);
-        px_count<SPL>(g, L, zig, subk, ca, wa, i0, q, tile, rowoff, qe, qn, err);
+        px_count<SPL>(g, L, zig, subk, ca, wa, i0, q, tile, rowoff, qe, qn, inc, err);
         __syncwarp();
         if (*qn > PX_QCAP - 32) px_flush(g, L, zig, subk, qe, qn, tile, lane, err);
         ca = cb;
