@@ -796,8 +796,8 @@ __device__ __forceinline__ void px_flush(const GridDev &g, const LayoutDev &L, c
 // lane share one channel, counted apart); a sample too close to a half-integer is left out and deferred to the
 // warp's queue. A lane with more than one such sample, a channel beyond the 11 bins (counted in the top bits) or
 // a centre out of range counts its samples one by one, with the exact channels where needed.
-// The lowest non-empty bin (the lane's first run, which the previous lane may share) is added in the ordered
-// pass of the group's LPP lanes; the other bins at once.
+// The lowest non-empty bin (the lane's first run, which the previous lane may share) is added after the group's
+// lanes have merged equal ones; the other bins at once.
 template <int SPL>
 __device__ __forceinline__ void px_count(const GridDev &g, const LayoutDev &L, const ZigDev *zig,
                                          const SubMC *__restrict__ subk, const PxCloud &p, const float4 (&w)[SPL / 4],
@@ -877,11 +877,17 @@ __device__ __forceinline__ void px_count(const GridDev &g, const LayoutDev &L, c
         fch = r.fch;
         fcnt = r.fcnt;
     }
+    // the lowest runs of the group's lanes: their channels are non-decreasing along the lanes, so equal ones are
+    // consecutive; a segmented scan sums them and the last lane of each segment adds the sum (one add per channel)
+    __syncwarp();
+    int v = fcnt;
 #pragma unroll
-    for (int qq = 0; qq < LPP; qq++) {
-        __syncwarp();
-        if (q == qq && (unsigned)fch < (unsigned)nz) row[fch] += (unsigned long long)(fix * (long long)fcnt);
+    for (int d = 1; d < LPP; d <<= 1) {
+        const int c2 = __shfl_up_sync(0xffffffffu, fch, d), v2 = __shfl_up_sync(0xffffffffu, v, d);
+        if (q >= d && c2 == fch) v += v2;
     }
+    const int cn = __shfl_down_sync(0xffffffffu, fch, 1);
+    if ((q == LPP - 1 || cn != fch) && (unsigned)fch < (unsigned)nz) row[fch] += (unsigned long long)(fix * (long long)v);
     __syncwarp();
 }
 
@@ -892,7 +898,7 @@ __device__ __forceinline__ void px_count(const GridDev &g, const LayoutDev &L, c
 // channels within the rounding bound of the cloud); the samples of the next cloud are loaded during the count.
 // The channels are monotone along the sorted samples, so the lanes of a group can only meet on the channel of a
 // run that crosses from one lane's samples into the next lane's: every lane's channels but its lowest are added
-// at once (distinct channels), and the lowest ones in lane order.
+// at once (distinct channels), and the lowest ones after a segmented scan over the group's lanes.
 // A sample within the bound of a half-integer (about one in a thousand) waits in the warp's queue; when the
 // queue fills, its exact float64 channels are computed a lane each and added with shared-memory atomics.
 // Rows: stride nz + 2 G sums (G pixels per warp) and a skew of 2 grp sums, so that equal channels of the warp's
