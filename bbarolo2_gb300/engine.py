@@ -407,7 +407,7 @@ class BatchLikelihood:
         descs["use_region"] = 1 if self.region is not None else 0
         descs["sigma2"] = self.sigma ** 2
         descs["eps2"] = (self.eps or 0.) ** 2
-        boxes = [(list(map(int, blo[k])), list(map(int, bhi[k]))) for k in range(B)]
+        boxes = list(zip(blo.tolist(), bhi.tolist()))
         if self._prof is not None:
             if not np.array_equal(np.asarray(proto.radii, float), self._prof["radii"]):
                 raise ValueError("the radii differ from those given to set_profile")
@@ -451,13 +451,17 @@ class BatchLikelihood:
         return x, st
 
     def finish(self, ss, lg, boxes):
+        """log L of the members from their sums (ss, lg) in their boxes and the data outside them."""
         s2 = self.sigma ** 2
-        out = np.empty(len(ss))
-        for k, (blo, bhi) in enumerate(boxes):
-            ss_out = max(self._dm2_box - self._boxsum(blo, bhi), 0.)
-            if self.eps is not None and self.eps > 0:
-                res = 0.5 * (ss[k] + ss_out / s2) + 0.5 * self.nvox * math.log(2. * math.pi * s2) + 0.5 * lg[k]
-            else:
-                res = 0.5 * (ss[k] + ss_out) / s2 + 0.5 * self.nvox * math.log(2. * math.pi * s2)
-            out[k] = -self.likefactor * res
-        return out
+        b = np.asarray(boxes, np.int64).reshape(len(ss), 2, 2)          # (member, lo/hi, x/y)
+        S = self._dm2_sat
+        inside = S[b[:, 1, 1], b[:, 1, 0]] - S[b[:, 0, 1], b[:, 1, 0]] - S[b[:, 1, 1], b[:, 0, 0]] + \
+            S[b[:, 0, 1], b[:, 0, 0]]
+        ss_out = np.maximum(self._dm2_box - inside, 0.)
+        ss = np.asarray(ss, float)
+        const = 0.5 * self.nvox * math.log(2. * math.pi * s2)
+        if self.eps is not None and self.eps > 0:
+            res = 0.5 * (ss + ss_out / s2) + const + 0.5 * np.asarray(lg, float)
+        else:
+            res = 0.5 * (ss + ss_out) / s2 + const
+        return -self.likefactor * res

@@ -169,10 +169,8 @@ def model_rows(rows, proto, mode, radsep):
     mr = model_rings(probe, mode, radsep)
     if mr is probe:
         return np.asarray(rows, float), probe
-    idx = []
-    for r in mr.radii:
-        j = np.flatnonzero(np.asarray(proto.radii) == r)
-        idx.append(int(j[0]) if j.size else -1)
+    eq = np.asarray(mr.radii, float)[:, None] == np.asarray(proto.radii, float)[None, :]
+    idx = np.where(eq.any(axis=1), eq.argmax(axis=1), -1).tolist()     # (the first equal radius, or -1)
     nr = proto.nr
     if idx and idx[0] == -1:
         idx[0] = 0
@@ -226,6 +224,7 @@ class SubringGrid:
         self.i1 = i1
         if nr > 1:
             self.dur = rad[i1] - rad[i1 - 1]
+            self._dseg = rad[1:] - rad[:-1]
         else:
             self.dur = np.ones(self.nsub)
 
@@ -236,9 +235,12 @@ class SubringGrid:
         nr = V.shape[-1]
         i1 = self.i1
         if nr > 1:
-            v0 = V[..., i1 - 1]
-            slope = (V[..., i1] - v0) / self.dur
-            vals = v0 + slope * self.dr
+            # the slope of each segment once (dur depends on the segment only), then gathered per sub-ring
+            seg = (V[..., 1:] - V[..., :-1]) / self._dseg
+            vals = np.take(V, i1 - 1, axis=-1)
+            slope = np.take(seg, i1 - 1, axis=-1)
+            slope *= self.dr
+            vals += slope
         else:
             vals = V[..., i1 - 1] + np.zeros(V.shape[:-1] + (self.nsub,)) * self.dr
         if self.const.any():
