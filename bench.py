@@ -126,7 +126,7 @@ def workload(batch):
 
 
 # ncu summaries (profiles/) with the DRAM traffic of a kernel's launch at the default batch
-TRAFFIC = {"mc_deposit": "k_mc_deposit_lean.global160_b161.dram.txt"}
+TRAFFIC = {"mc_deposit": "k_mc_deposit_px.global160_b161.dram.txt"}
 
 
 def measured_traffic(kernel, batch):
