@@ -269,8 +269,8 @@ __global__ void __launch_bounds__(AN_WPB * 32) k_an_model(GridDev g, const AnSub
 //           pixel of every height;
 //   runs    consecutive heights in one pixel (a ballot of the run starts), their weights by a segmented scan
 //           (float32), a run crossing a pass of 32 heights carried to the next pass;
-//   line    computed at the first run in the box: the velocity in float64 in the reference's order, its channel
-//           kc exactly (float64 linear map, the reference's _velgrid within 1e-9 of a half-integer), then the
+//   line    computed at the first run in the box: the velocity and its channel in float-float (the reference's
+//           float64 _velgrid within 1e-6 of a channel boundary), the centre channel kc exact, then the
 //           channel-integrated profile over kc - K .. kc + K in float32: the edges relative to a reference
 //           velocity in float-float (so that (edge - v) / sig keeps ~1e-7), the normal CDF from the reference's
 //           table (float32 copy, linear interpolation as _phi);
@@ -291,7 +291,8 @@ __global__ void __launch_bounds__(ANF_WPB * 32) k_an_model_fast(GridDev g, const
                                                                 const int *__restrict__ sbase,
                                                                 const int *__restrict__ ssub,
                                                                 const double2 *__restrict__ cs,
-                                                                const float2 *__restrict__ csf, long long nsamp,
+                                                                const float2 *__restrict__ csf,
+                                                                const float4 *__restrict__ csff, long long nsamp,
                                                                 int nb, const double *__restrict__ zq,
                                                                 const float *__restrict__ zqf,
                                                                 const float *__restrict__ wqf,
@@ -322,15 +323,26 @@ __global__ void __launch_bounds__(ANF_WPB * 32) k_an_model_fast(GridDev g, const
     unsigned long long *o64 = out64 + (size_t)k * mstride;
     int k0 = 0, nk = -1;                                    // the line's channels (nk < 0: not computed yet)
     auto line = [&]() {
-        // bbarolo/galmod.py:407 and :410 (_velgrid, _lround)
-        const double2 c = cs[s];
-        const double vplane = __dadd_rn(__dadd_rn(S.vsys, __dmul_rn(__dadd_rn(__dmul_rn(S.vrot, c.x),
-                                                                              __dmul_rn(S.vrad, c.y)), S.sinc)),
-                                        __dmul_rn(S.vvert, S.cinc));
-        const double chd = __dadd_rn(__dmul_rn(vplane, g.ia0), g.ib0);
-        const double fr = __dsub_rn(chd, floor(chd));
-        const long long kc = fabs(__dsub_rn(fr, 0.5)) > 1e-9 ? (long long)floor(__dadd_rn(chd, 0.5))
-                                                              : lround_ref(velgrid_exact(vplane, g, 0));
+        // bbarolo/galmod.py:407 and :410 (_velgrid, _lround) in float-float (about 44 bits: the channel and the
+        // velocity relative to vref within ~1e-11 of the reference's float64 values); within 1e-6 of a channel
+        // boundary the reference's float64 operations decide the centre channel
+        const float4 cq = csff[s];
+        const ff caz{cq.x, cq.y}, saz{cq.z, cq.w};
+        ff v = ff_add(ff_mul(ff{S.vroth, S.vrotl}, caz), ff_mul(ff{S.vradh, S.vradl}, saz));
+        v = ff_add(ff_mul(v, ff{S.sinch, S.sincl}), ff_mul(ff{S.vverth, S.vvertl}, ff{S.cinch, S.cincl}));
+        v = ff_add(ff{S.vsysh, S.vsysl}, v);
+        const ff chd = ff_add(ff_mul(v, ff{g.ia0h, g.ia0l}), ff{g.ib0h, g.ib0l});
+        int kci;
+        long long kc;
+        if (ff_round(chd, kci)) {
+            kc = kci;
+        } else {
+            const double2 c = cs[s];
+            const double vplane = __dadd_rn(__dadd_rn(S.vsys, __dmul_rn(__dadd_rn(__dmul_rn(S.vrot, c.x),
+                                                                                  __dmul_rn(S.vrad, c.y)), S.sinc)),
+                                            __dmul_rn(S.vvert, S.cinc));
+            kc = lround_ref(velgrid_exact(vplane, g, 0));
+        }
         long long a0 = kc - S.K, a1 = kc + S.K + 1;
         if (a0 < 0) a0 = 0;
         if (a1 > nz) a1 = nz;
@@ -340,9 +352,9 @@ __global__ void __launch_bounds__(ANF_WPB * 32) k_an_model_fast(GridDev g, const
         }
         k0 = (int)a0;
         nk = (int)(a1 - a0);
-        const double vr = __dsub_rn(vplane, g.vref);
-        const float vrh = (float)vr, vrl = (float)__dsub_rn(vr, (double)vrh);
-        const float amp = (float)__dmul_rn(__dmul_rn(S.a[0], rec ? S.wrec : S.wapp), ldexp(1.0, M.fix_exp));
+        const ff vr = ff_add(v, ff{-g.vrefh, -g.vrefl});
+        const float vrh = vr.hi, vrl = vr.lo;
+        const float amp = ldexpf(S.af * (rec ? S.wrecf : S.wappf), M.fix_exp);
         for (int j = lane; j <= nk; j += 32) {
             const float2 e = __ldg(vef + k0 + j);
             const float t = (__fsub_rn(e.x, vrh) + __fsub_rn(e.y, vrl)) * S.invf;
@@ -487,7 +499,8 @@ void launch_an_model(cudaStream_t s, const GridDev &g, const AnSub *subs, int ns
 size_t an_fast_smem_bytes(int nz) { return (size_t)ANF_WPB * 2 * (nz + 2) * sizeof(float); }
 
 void launch_an_model_fast(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase,
-                          const int *ssub, const double *cs, const float *csf, long long nsamp, int nb,
+                          const int *ssub, const double *cs, const float *csf, const float *csff, long long nsamp,
+                          int nb,
                           const double *zq, const float *zqf, const float *wqf, const float *vef, const float *cd2if,
                           const float *ptabf, const MemberDev *mem, long long *out64, long long mstride) {
     const long long nw = nsamp * nb;
@@ -496,7 +509,8 @@ void launch_an_model_fast(cudaStream_t s, const GridDev &g, const AnSub *subs, i
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(k_an_model_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_an_model_fast<<<(unsigned)((nw + ANF_WPB - 1) / ANF_WPB), ANF_WPB * 32, smem, s>>>(
-        g, subs, nsub, sbase, ssub, (const double2 *)cs, (const float2 *)csf, nsamp, nb, zq, zqf, wqf,
+        g, subs, nsub, sbase, ssub, (const double2 *)cs, (const float2 *)csf, (const float4 *)csff, nsamp, nb, zq,
+        zqf, wqf,
         (const float2 *)vef, cd2if, ptabf, mem, (unsigned long long *)out64, mstride);
 }
 

@@ -138,6 +138,8 @@ struct bbgpu_ctx {
     size_t d_acs_cap = 0, d_azq_cap = 0, d_awq_cap = 0;
     float *d_acsf = nullptr, *d_azqf = nullptr, *d_awqf = nullptr;
     size_t d_acsf_cap = 0, d_azqf_cap = 0, d_awqf_cap = 0;
+    float4 *d_acsff = nullptr;         // cos, sin of the model's samples in float-float
+    size_t d_acsff_cap = 0;
     long long *d_model_fx = nullptr;
     size_t d_model_fx_cap = 0;
     long long ansamp = 0;
@@ -419,7 +421,7 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
         cudaFree(q);
     for (void *q : {(void *)ctx->d_asub, (void *)ctx->d_asbase, (void *)ctx->d_assub, (void *)ctx->d_acs,
                     (void *)ctx->d_azq, (void *)ctx->d_awq, (void *)ctx->d_model_fx, (void *)ctx->d_acsf,
-                    (void *)ctx->d_azqf, (void *)ctx->d_awqf})
+                    (void *)ctx->d_azqf, (void *)ctx->d_awqf, (void *)ctx->d_acsff})
         cudaFree(q);
     cudaFreeHost(ctx->h_asub);
     cudaFreeHost(ctx->h_psub);
@@ -509,6 +511,15 @@ extern "C" int bbgpu_set_grid(bbgpu_ctx *ctx, const bbgpu_grid *gr, const double
         g.ib0 = (lfreq0[0] - g.crval3) / g.cdelt3 + g.crpix3 - 1;
     }
     g.vref = g.nz > 0 && vedges ? vedges[g.nz / 2] : 0.0;    // (the middle channel edge of line 0)
+    {
+        auto split = [](double v, float &hi, float &lo) {
+            hi = (float)v;
+            lo = (float)(v - (double)hi);
+        };
+        split(g.ia0, g.ia0h, g.ia0l);
+        split(g.ib0, g.ib0h, g.ib0l);
+        split(g.vref, g.vrefh, g.vrefl);
+    }
     std::vector<float> cf(g.nz);
     for (int i = 0; i < g.nz; i++) cf[i] = (float)cd2i[i];
     cudaFree(ctx->d_cd2i);
@@ -700,6 +711,17 @@ static int batch_prepare_analytic(bbgpu_ctx *ctx, int nb, int nsub, const double
         bbh_an_samples_f32(cs, csf);
         if ((rc = dgrow(ctx, &ctx->d_acsf, &ctx->d_acsf_cap, csf.size() ? csf.size() : 1))) return rc;
         if (csf.size()) CK(cudaMemcpy(ctx->d_acsf, csf.data(), sizeof(float) * csf.size(), cudaMemcpyHostToDevice));
+        std::vector<float4> csff(cs.size() / 2);
+        for (size_t q = 0; q < csff.size(); q++) {
+            const double c = cs[2 * q], sn = cs[2 * q + 1];
+            csff[q].x = (float)c;
+            csff[q].y = (float)(c - (double)csff[q].x);
+            csff[q].z = (float)sn;
+            csff[q].w = (float)(sn - (double)csff[q].z);
+        }
+        if ((rc = dgrow(ctx, &ctx->d_acsff, &ctx->d_acsff_cap, csff.size() ? csff.size() : 1))) return rc;
+        if (csff.size())
+            CK(cudaMemcpy(ctx->d_acsff, csff.data(), sizeof(float4) * csff.size(), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(ctx->d_asbase, sbase.data(), sizeof(int) * sbase.size(), cudaMemcpyHostToDevice));
         if (ssub.size()) CK(cudaMemcpy(ctx->d_assub, ssub.data(), sizeof(int) * ssub.size(), cudaMemcpyHostToDevice));
         if (cs.size()) CK(cudaMemcpy(ctx->d_acs, cs.data(), sizeof(double) * cs.size(), cudaMemcpyHostToDevice));
@@ -904,8 +926,9 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
             for (int i = 5; i <= 8; i++) CK(cudaEventRecord(ctx->ev[i], s));
         CK(cudaMemsetAsync(ctx->d_model_fx, 0, sizeof(long long) * (size_t)ctx->nb * ctx->mstride, s));
         launch_an_model_fast(s, g, ctx->d_asub, ctx->nsub, ctx->d_asbase, ctx->d_assub, ctx->d_acs, ctx->d_acsf,
-                             ctx->ansamp, ctx->nb, ctx->d_azq, ctx->d_azqf, ctx->d_awqf, (const float *)ctx->d_vef,
-                             ctx->d_cd2if, ctx->d_ptabf, ctx->d_mem, ctx->d_model_fx, ctx->mstride);
+                             (const float *)ctx->d_acsff, ctx->ansamp, ctx->nb, ctx->d_azq, ctx->d_azqf, ctx->d_awqf,
+                             (const float *)ctx->d_vef, ctx->d_cd2if, ctx->d_ptabf, ctx->d_mem, ctx->d_model_fx,
+                             ctx->mstride);
         CKL();
         launch_an_model(s, g, ctx->d_asub, ctx->nsub, ctx->d_asbase, ctx->d_assub, ctx->d_acs, ctx->ansamp, ctx->nb,
                         ctx->d_azq, ctx->d_awq, ctx->d_vedges, ctx->d_cd2i, ctx->d_ptab, ctx->d_mem, ctx->d_model_fx,

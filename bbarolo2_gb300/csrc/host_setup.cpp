@@ -602,6 +602,19 @@ int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0,
         S.wzero = (S.wrec == 0.0 ? 1 : 0) | (S.wapp == 0.0 ? 2 : 0);
         S.invf = (float)S.inv;
         S.anfast = !maps && !S.zdep && g->nlines == 1 && g->fast_ok;
+        {
+            auto split = [](double v, float &hi, float &lo) {
+                hi = (float)v;
+                lo = (float)(v - (double)hi);
+            };
+            split(S.vsys, S.vsysh, S.vsysl);
+            split(S.vrot, S.vroth, S.vrotl);
+            split(S.vrad, S.vradh, S.vradl);
+            split(S.vvert, S.vverth, S.vvertl);
+            split(S.sinc, S.sinch, S.sincl);
+            split(S.cinc, S.cinch, S.cincl);
+            S.af = (float)S.a[0];
+        }
         S.fluxscf = (float)S.fluxsc;
         S.wrecf = (float)S.wrec;
         S.wappf = (float)S.wapp;

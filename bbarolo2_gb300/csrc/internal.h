@@ -51,6 +51,9 @@ struct AnSub {
     // anfast = 1 when it applies, invf = 1 / sig
     int anfast;
     float invf;
+    // float-float (hi, lo) copies of the velocity terms and the line amplitude relint[0] fluxsc in float32 (the
+    // fast path's line without float64 arithmetic)
+    float vsysh, vsysl, vroth, vrotl, vradh, vradl, vverth, vvertl, sinch, sincl, cinch, cincl, af;
 };
 
 // The constants of a context, as the kernels see them.
@@ -65,6 +68,7 @@ struct GridDev {
     // ANALYTIC fast path (one line, linear map): channel = v ia0 + ib0 in float64 (ia0, ib0 of line 0), and the
     // reference velocity vref (the channel edges are kept relative to it in float-float)
     double ia0, ib0, vref;
+    float ia0h, ia0l, ib0h, ib0l, vrefh, vrefl;  // (float-float copies)
 };
 
 // A parsed MC stream (host copy): everything about the clouds that does not depend on the ring parameters.

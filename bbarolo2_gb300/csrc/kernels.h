@@ -111,11 +111,13 @@ void launch_an_model(cudaStream_t s, const GridDev &g, const AnSub *subs, int ns
                      const double *vedges, const double *cd2i, const double *ptab, const MemberDev *mem,
                      long long *out64, long long mstride, int skip_fast);
 // the float32 path of the ANALYTIC model (sub-rings with anfast; launch_an_model with skip_fast does the others):
-// csf, zqf, wqf float32 copies of the sample and vertical tables, vef (nz + 1) float-float channel edges of line 0
+// csf, zqf, wqf float32 copies of the sample and vertical tables, csff (float4 per sample) its cos and sin in
+// float-float, vef (nz + 1) float-float channel edges of line 0
 // relative to g.vref, ptabf the normal CDF table in float32
 size_t an_fast_smem_bytes(int nz);
 void launch_an_model_fast(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase,
-                          const int *ssub, const double *cs, const float *csf, long long nsamp, int nb,
+                          const int *ssub, const double *cs, const float *csf, const float *csff, long long nsamp,
+                          int nb,
                           const double *zq, const float *zqf, const float *wqf, const float *vef, const float *cd2if,
                           const float *ptabf, const MemberDev *mem, long long *out64, long long mstride);
 void launch_an_maps(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase, const int *ssub,

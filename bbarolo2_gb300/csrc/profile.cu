@@ -609,6 +609,7 @@ __global__ void k_an_dens(GridDev g, AnSub *__restrict__ sub, int nsub, MemberDe
         S.fluxsc = fl;
         S.fluxscf = (float)fl;
         for (int nl = 0; nl < g.nlines && nl < BBGPU_MAXL; nl++) S.a[nl] = __dmul_rn(g.relint[nl], fl);
+        S.af = (float)S.a[0];
         bound += fabs(fl) * fmax(fabs(S.wrec), fabs(S.wapp)) * per * (double)((long long)S.naz * 2);
     }
     red[tid] = bound;
