@@ -128,6 +128,9 @@ struct bbgpu_ctx {
     AnSub *h_psub = nullptr;           // pinned staging of the sub-ring constants
     size_t h_psub_cap = 0;
     std::vector<MemberDev> pmem_host;
+    // per (member, sub-ring): 1 where the member's constants are member 0's (filled on the device)
+    signed char *h_reuse = nullptr, *d_reuse = nullptr, *h_preuse = nullptr, *d_preuse = nullptr;
+    size_t h_reuse_cap = 0, d_reuse_cap = 0, h_preuse_cap = 0, d_preuse_cap = 0;
     // ANALYTIC batches: sub-ring constants per member, the sample table of the model's sub-rings, their vertical
     // grids (host cache mirrored on the device) and the fixed-point models
     AnSub *h_asub = nullptr, *d_asub = nullptr;
@@ -424,6 +427,10 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
                     (void *)ctx->d_azqf, (void *)ctx->d_awqf, (void *)ctx->d_acsff})
         cudaFree(q);
     cudaFreeHost(ctx->h_asub);
+    cudaFreeHost(ctx->h_reuse);
+    cudaFreeHost(ctx->h_preuse);
+    cudaFree(ctx->d_reuse);
+    cudaFree(ctx->d_preuse);
     cudaFreeHost(ctx->h_psub);
     cudaFreeHost(ctx->h_sub); cudaFreeHost(ctx->h_mem); cudaFreeHost(ctx->h_out2); cudaFreeHost(ctx->h_err);
     for (int i = 0; i <= NTIMER; i++)
@@ -665,6 +672,7 @@ static int batch_prepare_analytic(bbgpu_ctx *ctx, int nb, int nsub, const double
     int rc;
     if ((rc = hgrow(ctx, &ctx->h_asub, &ctx->h_asub_cap, (size_t)nb * (nsub ? nsub : 1)))) return rc;
     if ((rc = hgrow(ctx, &ctx->h_mem, &ctx->h_mem_cap, (size_t)nb))) return rc;
+    if ((rc = hgrow(ctx, &ctx->h_reuse, &ctx->h_reuse_cap, (size_t)nb * (nsub ? nsub : 1)))) return rc;
     ctx->mem_host.resize(nb);
     ZgridCache &zc = ctx->azcache;
     if (zc.zq.size() > ((size_t)1 << 24)) zc.clear();
@@ -682,9 +690,11 @@ static int batch_prepare_analytic(bbgpu_ctx *ctx, int nb, int nsub, const double
                            d.bhi0 == descs[0].bhi0 && d.bhi1 == descs[0].bhi1;
         if (d.blo0 < 0 || d.blo1 < 0 || d.bhi0 > g.nx || d.bhi1 > g.ny || d.bhi0 < d.blo0 || d.bhi1 < d.blo1)
             return fail(ctx, BBGPU_ERR_ARG, "eval: member %d: box outside the cube", k);
+        signed char *ru = ctx->h_reuse + (size_t)k * nsub;
+        memset(ru, 0, (size_t)nsub);
         const int e = bbh_an_subs(s, nsub, &g, nzq, d.blo0, d.blo1, d.bhi0, d.bhi1, ctx->h_cd2i.data(), 0, nullptr,
                                   nullptr, ctx->h_asub + (size_t)k * nsub, zc, reuse ? sr : nullptr,
-                                  reuse ? ctx->h_asub : nullptr);
+                                  reuse ? ctx->h_asub : nullptr, reuse ? ru : nullptr);
         if (e == -10000) return fail(ctx, BBGPU_ERR_ARG, "eval: member %d: the total flux is not finite", k);
         if ((rc = member_desc(ctx, k, d, e, need_cube, ctx->mem_host[k]))) return rc;
         ctx->h_mem[k] = ctx->mem_host[k];
@@ -769,9 +779,13 @@ static int batch_prepare_analytic(bbgpu_ctx *ctx, int nb, int nsub, const double
         if ((rc = dgrow(ctx, &ctx->d_smooth, &ctx->d_smooth_cap, (size_t)nb * ctx->mstride))) return rc;
     if (ctx->want64)
         if ((rc = dgrow(ctx, &ctx->d_model64, &ctx->d_model64_cap, (size_t)nb * ctx->mstride))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_reuse, &ctx->d_reuse_cap, (size_t)nb * (nsub ? nsub : 1)))) return rc;
     CK(cudaMemcpyAsync(ctx->d_asub, ctx->h_asub, sizeof(AnSub) * (size_t)nb * nsub, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(ctx->d_mem, ctx->h_mem, sizeof(MemberDev) * (size_t)nb, cudaMemcpyHostToDevice, ctx->stream));
-    ctx->h2d += (long long)(sizeof(AnSub) * (size_t)nb * nsub + sizeof(MemberDev) * (size_t)nb);
+    CK(cudaMemcpyAsync(ctx->d_reuse, ctx->h_reuse, (size_t)nb * nsub, cudaMemcpyHostToDevice, ctx->stream));
+    launch_fill_copy(ctx->stream, ctx->d_asub, sizeof(AnSub), nsub, nb, ctx->d_reuse);
+    CKL();
+    ctx->h2d += (long long)((sizeof(AnSub) + 1) * (size_t)nb * nsub + sizeof(MemberDev) * (size_t)nb);
     ctx->uploaded = true;
     ctx->ran = false;
     return 0;
@@ -809,6 +823,8 @@ static int batch_prepare(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const
     ctx->cur = E;
     if ((rc = hgrow(ctx, &ctx->h_sub, &ctx->h_sub_cap, (size_t)nb * (nsub ? nsub : 1)))) return rc;
     if ((rc = hgrow(ctx, &ctx->h_mem, &ctx->h_mem_cap, (size_t)nb))) return rc;
+    if ((rc = hgrow(ctx, &ctx->h_reuse, &ctx->h_reuse_cap, (size_t)nb * (nsub ? nsub : 1)))) return rc;
+    memset(ctx->h_reuse, 0, (size_t)nsub);
     ctx->mem_host.resize(nb);
     int toff = 0;
     for (int k = 0; k < nb; k++) {
@@ -817,7 +833,7 @@ static int batch_prepare(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const
             return fail(ctx, BBGPU_ERR_ARG, "eval: member %d: box outside the cube", k);
         SubMC *S = ctx->h_sub + (size_t)k * nsub;
         int e = bbh_submc(sr + (size_t)k * BBGPU_NSR * nsub, nsub, nc0.data(), nv0.data(), &g, S,
-                          k ? sr : nullptr, k ? ctx->h_sub : nullptr);
+                          k ? sr : nullptr, k ? ctx->h_sub : nullptr, k ? ctx->h_reuse + (size_t)k * nsub : nullptr);
         MemberDev &M = ctx->mem_host[k];
         if ((rc = member_desc(ctx, k, d, e, need_cube, M))) return rc;
         M.ntx = (M.bx + ctx->tx - 1) / ctx->tx;
@@ -854,9 +870,13 @@ static int batch_prepare(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const
         if ((rc = dgrow(ctx, &ctx->d_smooth, &ctx->d_smooth_cap, (size_t)nb * ctx->mstride))) return rc;
     if (ctx->want64)
         if ((rc = dgrow(ctx, &ctx->d_model64, &ctx->d_model64_cap, (size_t)nb * ctx->mstride))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_reuse, &ctx->d_reuse_cap, (size_t)nb * (nsub ? nsub : 1)))) return rc;
     CK(cudaMemcpyAsync(ctx->d_sub, ctx->h_sub, sizeof(SubMC) * (size_t)nb * nsub, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(ctx->d_mem, ctx->h_mem, sizeof(MemberDev) * (size_t)nb, cudaMemcpyHostToDevice, ctx->stream));
-    ctx->h2d = (long long)(sizeof(SubMC) * (size_t)nb * nsub + sizeof(MemberDev) * (size_t)nb);
+    CK(cudaMemcpyAsync(ctx->d_reuse, ctx->h_reuse, (size_t)nb * nsub, cudaMemcpyHostToDevice, ctx->stream));
+    launch_fill_submc(ctx->stream, ctx->d_sub, nsub, nb, ctx->d_reuse, ctx->d_mem, g.nlines);
+    CKL();
+    ctx->h2d = (long long)((sizeof(SubMC) + 1) * (size_t)nb * nsub + sizeof(MemberDev) * (size_t)nb);
     ctx->uploaded = true;
     ctx->ran = false;
     return 0;
@@ -1567,6 +1587,8 @@ extern "C" int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *
     const ProfBox &bx = ctx->pbox;
     int rc;
     if ((rc = hgrow(ctx, &ctx->h_psub, &ctx->h_psub_cap, (size_t)nb * nsm))) return rc;
+    if ((rc = hgrow(ctx, &ctx->h_preuse, &ctx->h_preuse_cap, (size_t)nb * nsm))) return rc;
+    memset(ctx->h_preuse, 0, (size_t)nsm);
     ZgridCache &zc = ctx->zcache;
     if (zc.zq.size() > ((size_t)1 << 24)) zc.clear();
     const size_t zold = zc.uploaded;
@@ -1574,7 +1596,8 @@ extern "C" int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *
     for (int k = 0; k < nb; k++) {
         const int e = bbh_an_subs(sr_maps + (size_t)k * BBGPU_NSR * nsm, nsm, &g, nzq, bx.blo0, bx.blo1, bx.bhi0,
                                   bx.bhi1, ctx->h_cd2i.data(), 1, widx, wval, ctx->h_psub + (size_t)k * nsm, zc,
-                                  k ? sr_maps : nullptr, k ? ctx->h_psub : nullptr);
+                                  k ? sr_maps : nullptr, k ? ctx->h_psub : nullptr,
+                                  k ? ctx->h_preuse + (size_t)k * nsm : nullptr);
         if (e == -10000) return fail(ctx, BBGPU_ERR_ARG, "eval_upload_profile: member %d: weights not finite", k);
         fix[k] = std::min(e, 100);
     }
@@ -1657,7 +1680,11 @@ extern "C" int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *
     const int npart = conv_resid_npart(ctx->pmem_host.data(), nb, bx.nrp);
     if ((rc = dgrow(ctx, &ctx->d_pmem, &ctx->d_pmem_cap, (size_t)nb))) return rc;
     if ((rc = dgrow(ctx, &ctx->d_ppart, &ctx->d_ppart_cap, (size_t)2 * nb * (npart ? npart : 1)))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_preuse, &ctx->d_preuse_cap, (size_t)nb * nsm))) return rc;
     CK(cudaMemcpyAsync(ctx->d_psub, ctx->h_psub, sizeof(AnSub) * (size_t)nb * nsm, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->d_preuse, ctx->h_preuse, (size_t)nb * nsm, cudaMemcpyHostToDevice, s));
+    launch_fill_copy(s, ctx->d_psub, sizeof(AnSub), nsm, nb, ctx->d_preuse);
+    CKL();
     CK(cudaMemcpyAsync(ctx->d_pwidx, wi.data(), sizeof(int) * wi.size(), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(ctx->d_pwvalf, wvalf.data(), sizeof(float) * wvalf.size(), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(ctx->d_pwval, wval, sizeof(double) * 2 * (size_t)nsm, cudaMemcpyHostToDevice, s));

@@ -274,16 +274,19 @@ static bool same_column(const double *a, const double *b, int nsub, int ir) {
 }
 
 int bbh_submc(const double *sr, int nsub, const int *nc, const int *nv, const GridDev *g, SubMC *out,
-              const double *sr_ref, const SubMC *out_ref) {
+              const double *sr_ref, const SubMC *out_ref, signed char *reused) {
     double bound = 0.;
     for (int ir = 0; ir < nsub; ir++) {
         SubMC &S = out[ir];
+        if (reused) reused[ir] = 0;
         if (out_ref && same_column(sr, sr_ref, nsub, ir)) {     // (the values of another member: same constants)
-            S = out_ref[ir];
-            if (S.active) {
-                const double wmax = fmax(fabs(S.wrec), fabs(S.wapp));
+            const SubMC &T = out_ref[ir];
+            if (reused) reused[ir] = 1;
+            else S = T;
+            if (T.active) {
+                const double wmax = fmax(fabs(T.wrec), fabs(T.wapp));
                 for (int nl = 0; nl < g->nlines && nl < BBGPU_MAXL; nl++)
-                    bound += (double)nc[ir] * (double)nv[ir] * fabs(S.valrel[nl]) * wmax;
+                    bound += (double)nc[ir] * (double)nv[ir] * fabs(T.valrel[nl]) * wmax;
             }
             continue;
         }
@@ -340,6 +343,10 @@ int bbh_submc(const double *sr, int nsub, const int *nc, const int *nv, const Gr
     double Q = bound > 0 ? ldexp(1.0, (int)floor(62.0 - log2(bound))) : 1.0;
     int cb = 0;
     for (int ir = 0; ir < nsub; ir++) {
+        if (reused && reused[ir]) {                              // (set on the device: k_fill_submc)
+            cb += out_ref[ir].active ? out_ref[ir].nc : 0;
+            continue;
+        }
         SubMC &S = out[ir];
         S.cloud_base = cb;
         cb += S.active ? S.nc : 0;
@@ -520,7 +527,7 @@ void bbh_an_samples_f32(const std::vector<double> &cs, std::vector<float> &csf) 
 
 int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0, int blo1, int bhi0, int bhi1,
                 const double *cd2i, int maps, const int64_t *widx, const double *wval, AnSub *out, ZgridCache &zc,
-                const double *sr_ref, const AnSub *out_ref) {
+                const double *sr_ref, const AnSub *out_ref, signed char *reused) {
 #define SR(r, i) sr[(size_t)(r) * nsub + (i)]
     const int nb = nzq > 1 ? nzq : 1;
     std::vector<double> tz(nb), tw(nb);
@@ -530,13 +537,16 @@ int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0,
     for (int nl = 0; nl < g->nlines; nl++) lsum += fabs(g->relint[nl]);
     for (int ir = 0; ir < nsub; ir++) {
         AnSub &S = out[ir];
+        if (reused) reused[ir] = 0;
         if (out_ref && same_column(sr, sr_ref, nsub, ir)) {     // (the values of another member: same constants)
-            S = out_ref[ir];
-            if (S.active) {
-                const double ws = std::max(fabs(S.wrec), fabs(S.wapp));
+            const AnSub &T = out_ref[ir];
+            if (reused) reused[ir] = 1;
+            else S = T;
+            if (T.active) {
+                const double ws = std::max(fabs(T.wrec), fabs(T.wapp));
                 double per = lsum * cmax;
                 if (maps) per = std::max(fabs(wval[2 * ir]), fabs(wval[2 * ir + 1]));
-                bound += fabs(S.fluxsc) * ws * per * (double)((long long)S.naz * 2);
+                bound += fabs(T.fluxsc) * ws * per * (double)((long long)T.naz * 2);
             }
             continue;
         }

@@ -103,9 +103,10 @@ uint64_t bbh_layout_key(uint64_t seed, int ltype, int nsub, const int *nc, const
 // nc and nv of each sub-ring of a table (the reference's cloud count)
 void bbh_cloud_counts(const double *sr, int nsub, const int64_t *nv_in, const GridDev *g, int *nc, int *nv);
 // SubMC of one table; returns the exponent e of the fixed-point unit 2^-e of its deposits
-// (sr_ref, out_ref: another member's table and constants, reused for the columns that are equal; may be NULL)
+// (sr_ref, out_ref: another member's table and constants, reused for the columns that are equal; may be NULL;
+// reused: when given, those columns are only marked (1) and left unwritten, for the device to fill)
 int bbh_submc(const double *sr, int nsub, const int *nc, const int *nv, const GridDev *g, SubMC *out,
-              const double *sr_ref = nullptr, const SubMC *out_ref = nullptr);
+              const double *sr_ref = nullptr, const SubMC *out_ref = nullptr, signed char *reused = nullptr);
 // ANALYTIC: the vertical samples of a sub-ring (bbarolo/galmod.py:276-323); returns their number
 int bbh_zgrid(double *zq, double *wq, int nmax, int ltype, double z0, double sinc, double pixsize, double dvdz,
               double sig, double R0, double radsep, double xpos, double ypos, double cdelt0, double cdelt1,
@@ -136,7 +137,7 @@ struct ZgridCache {
 };
 int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0, int blo1, int bhi0, int bhi1,
                 const double *cd2i, int maps, const int64_t *widx, const double *wval, AnSub *out, ZgridCache &zc,
-                const double *sr_ref = nullptr, const AnSub *out_ref = nullptr);
+                const double *sr_ref = nullptr, const AnSub *out_ref = nullptr, signed char *reused = nullptr);
 // The second-difference prior of the deconvolved profile at the radii R (n) (bbarolo/profile.py:60-151):
 // rows (n - 2) x 3 columns lc and weights lv, the order of the radii, the "near" rows, the median ring
 // distance d and the norm of the relative prior

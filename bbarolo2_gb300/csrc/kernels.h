@@ -162,3 +162,9 @@ void launch_mc_dens(cudaStream_t s, const GridDev &g, SubMC *sub, int nsub, Memb
 // per = sum |relint| x max |cd2i| (the deposit bound of a sample of unit flux)
 void launch_an_dens(cudaStream_t s, const GridDev &g, AnSub *sub, int nsub, MemberDev *mem, int nb, const double *x,
                     int nx, const int *widx, const double *wval, const double *rap, double per, int *err);
+
+// The entries of a batch's per-(member, sub-ring) constants that repeat member 0's (reused = 1, left unwritten by
+// the host): SubMC with the member's fixed-point deposits, or a plain copy of any 8-byte-word structure.
+void launch_fill_submc(cudaStream_t s, SubMC *sub, int nsub, int nb, const signed char *reused, const MemberDev *mem,
+                       int nlines);
+void launch_fill_copy(cudaStream_t s, void *base, size_t elt_bytes, int nsub, int nb, const signed char *reused);

@@ -999,6 +999,34 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
     }
 }
 
+// The constants of the sub-rings that a member shares with member 0 (reused = 1; the host left them unwritten):
+// member 0's, with the fixed-point deposits of the member's own exponent (the host's llrint(valrel w Q)).
+__global__ void k_fill_submc(SubMC *__restrict__ sub, int nsub, int nb, const signed char *__restrict__ reused,
+                             const MemberDev *__restrict__ mem, int nlines) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)nb * nsub) return;
+    if (!reused[i]) return;
+    const int k = (int)(i / nsub), ir = (int)(i - (long long)k * nsub);
+    SubMC S = sub[ir];
+    if (S.active) {
+        const double Q = ldexp(1.0, mem[k].fix_exp);
+        for (int nl = 0; nl < nlines && nl < BBGPU_MAXL; nl++) {
+            S.fix[0][nl] = __double2ll_rn(__dmul_rn(__dmul_rn(S.valrel[nl], S.wrec), Q));
+            S.fix[1][nl] = __double2ll_rn(__dmul_rn(__dmul_rn(S.valrel[nl], S.wapp), Q));
+        }
+    }
+    sub[i] = S;
+}
+
+// A plain copy of member 0's entry into the entries marked reused (structures of 8-byte words).
+__global__ void k_fill_copy(unsigned long long *__restrict__ base, int words, int nsub, int nb,
+                            const signed char *__restrict__ reused) {
+    const long long i = (long long)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    if (i >= (long long)nb * nsub || !reused[i]) return;
+    const int ir = (int)(i % nsub);
+    for (int w = threadIdx.x & 31; w < words; w += 32) base[(size_t)i * words + w] = base[(size_t)ir * words + w];
+}
+
 // exclusive scan of n counts in three passes: block sums, scan of the sums, block scans
 __global__ void k_scan_a(const int *__restrict__ count, int n, int *__restrict__ bsum) {
     __shared__ int r[32];
@@ -1147,4 +1175,18 @@ void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, con
     }
     k_mc_deposit<<<grid, 256, smem, s>>>(g, L, sub, nsub, mem, tx, ty, offset, count, (const Entry *)bucket, zig, cd2if,
                                         cd2i, model, mstride, model64, err);
+}
+
+void launch_fill_submc(cudaStream_t s, SubMC *sub, int nsub, int nb, const signed char *reused, const MemberDev *mem,
+                       int nlines) {
+    const long long n = (long long)nb * nsub;
+    if (n == 0) return;
+    k_fill_submc<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(sub, nsub, nb, reused, mem, nlines);
+}
+
+void launch_fill_copy(cudaStream_t s, void *base, size_t elt_bytes, int nsub, int nb, const signed char *reused) {
+    const long long n = (long long)nb * nsub;
+    if (n == 0) return;
+    k_fill_copy<<<(unsigned)((n + 7) / 8), 256, 0, s>>>((unsigned long long *)base, (int)(elt_bytes / 8), nsub, nb,
+                                                       reused);
 }
