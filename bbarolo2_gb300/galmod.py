@@ -530,10 +530,11 @@ def subrings_batch(setup, proto, rows):
         V += [fth, np.where(z0t >= 0, z0t, z0) / 60., np.where(vdt >= 0, vdt, vdisp) * 1000.]
     V = np.stack(V, axis=1)                                    # (B, nrow, nr)
     nsub = g.nsub
-    sr = np.empty((B, V.shape[1] + 1, nsub))
+    # (a thin layer's table is built in place: 16 rows, the side weights in rows 14-15)
+    sr = np.empty((B, 16 if not thick else V.shape[1] + 1, nsub))
     sr[:, 0] = g.radii
     if nsub:
-        sr[:, 1:] = g.interpolate(V)
+        sr[:, 1:V.shape[1] + 1] = g.interpolate(V)
     edge = getattr(proto, "edge", None)
     if edge is not None and nsub:
         sr[:, 5] *= edge_weights(sr[0, 0] * 60., setup.radsep * 60., float(edge),
@@ -550,7 +551,10 @@ def subrings_batch(setup, proto, rows):
     for k, e in enumerate(setup.side_edges(proto)[::-1]):
         if e is not None and sr.shape[2]:
             side[k] = edge_weights(sr[0, 0] * 60., setup.radsep * 60., e)
-    sr = np.concatenate([sr[:, :14], np.broadcast_to(side, (B, 2, sr.shape[2]))], axis=1)
+    if sr.shape[1] == 16:
+        sr[:, 14:16] = side
+    else:
+        sr = np.concatenate([sr[:, :14], np.broadcast_to(side, (B, 2, sr.shape[2]))], axis=1)
     nvtmp = setup.nvpar if setup.nvpar >= 1 else setup.nsubs
     nv = np.where(sr[:, 4] == 0, 1, nvtmp).astype(np.int64)
     return np.ascontiguousarray(sr), np.ascontiguousarray(nv)
