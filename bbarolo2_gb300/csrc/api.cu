@@ -267,7 +267,7 @@ static int upload_layout(bbgpu_ctx *ctx, LayoutEntry &E) {
             np += (long long)H.nc[ir] * ((H.nv[ir] + 3) & ~3);
         }
         size_t nsc = (size_t)(np ? np : 1);
-        std::vector<float> nf(nsc, 0.0f);
+        std::vector<float> nf(nsc, __builtin_nanf(""));       // (the padding: NaN, which no channel test passes)
         std::vector<uint16_t> ord(nsc, 0);
         std::vector<double> val;
         std::vector<int> idx;

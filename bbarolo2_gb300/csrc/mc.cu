@@ -721,13 +721,15 @@ __device__ __forceinline__ void px_entry(const Entry *__restrict__ bucket, int b
     }
 }
 
-// this lane's (up to) SPL sorted samples of the cloud, 16-byte loads (the runs are padded to 4 samples)
+// this lane's (up to) SPL sorted samples of the cloud, 16-byte loads (the runs are padded to 4 samples with NaN;
+// the samples past the cloud are NaN as well)
 template <int SPL>
 __device__ __forceinline__ void px_samples(const LayoutDev &L, const PxCloud &p, int i0, float4 (&w)[SPL / 4]) {
     const float4 *src = (const float4 *)(L.nf + (unsigned)p.pb + i0);
 #pragma unroll
     for (int s = 0; s < SPL / 4; s++)
-        w[s] = i0 + 4 * s < p.nv ? __ldg(src + s) : make_float4(0.f, 0.f, 0.f, 0.f);
+        w[s] = i0 + 4 * s < p.nv ? __ldg(src + s) : make_float4(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000),
+                                                             __int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
 }
 
 // The exact channel of sample i of a cloud (its float32 channel was too close to a half-integer).
@@ -811,7 +813,11 @@ __device__ __forceinline__ void px_count(const GridDev &g, const LayoutDev &L, c
     const float hw = 0.5f - p.eps;
     const float tc = p.tc, sg = p.sg;
     const long long fix = p.fix;
-    const float fl0 = floorf(fmaf(w[0].x, sg, tc) + 0.5f) - 1.0f;
+    // f = sample x sg + (tc + 1/2): the half folded into the centre (one rounding in place of another, within the
+    // same bound); samples past the cloud are NaN, which fail the test below and add the empty increment
+    const float tc5 = tc + 0.5f;
+    const float fl0 = floorf(fmaf(w[0].x, sg, tc5)) - 1.0f;
+    const float fl0m = fl0 - 12582912.0f;                  // (exact: an integer below 2^24 in magnitude)
     const float hwf = fastc ? hw : -1.0f;                  // (a centre out of range: no sample passes)
     // straight-line code: each sample adds inc[min(channel - c0, 30)] (bins 0..10 five bits each, a channel
     // beyond them one unit of bits 55..63; index 31: a sample left out)
@@ -824,16 +830,16 @@ __device__ __forceinline__ void px_count(const GridDev &g, const LayoutDev &L, c
 #pragma unroll
         for (int e = 0; e < 4; e++) {
             const int i = 4 * s + e;
-            const float f = fmaf(vv[e], sg, tc) + 0.5f;
+            const float f = fmaf(vv[e], sg, tc5);
             const float fl = floorf(f);
-            const bool in = i < m;
             const bool ok = fabsf(f - fl - 0.5f) <= hwf;
-            const int d = __float_as_int((fl - fl0) + 12582912.0f) - 0x4B400000;   // (exact: small integers)
-            need |= (in & !ok) ? 1u << i : 0u;
-            H += inc[(in & ok) ? min((unsigned)d, 30u) : 31u];
-            if (SPL == 32) dlast = (in & ok) ? d : dlast;
+            const int d = __float_as_int(fl - fl0m) - 0x4B400000;      // (exact: small integers)
+            need |= ok ? 0u : 1u << i;
+            H += inc[ok ? min((unsigned)d, 30u) : 31u];
+            if (SPL == 32) dlast = ok ? d : dlast;
         }
     }
+    need &= m >= 32 ? 0xffffffffu : (m > 0 ? (1u << m) - 1u : 0u);
     int fch = (int)0x80000000, fcnt = 0;
     if (__popc(need) <= 1 && (H >> 55) == 0) {
         if (need) {
