@@ -127,3 +127,27 @@ def test_layout_mismatch_is_rejected(gpu_lib):
     descs[1]["seed"] = 7
     with pytest.raises(_lib.DeviceError, match="another cloud layout"):
         L.run(sr, nv, descs)
+
+
+@pytest.mark.parametrize("galmodtype", ["MC", "ANALYTIC"])
+def test_batch_members_equal_single_evaluations(gpu_lib, galmodtype):
+    """Members whose sub-ring columns equal member 0's share its constants (the host marks them, the device fills
+    them with the member's own fixed-point unit): each member of a mixed batch gives exactly the log L of its
+    evaluation alone, with and without the flux normalisation."""
+    from bbarolo2_gb300 import engine
+    from bbarolo2_gb300.galmod import ring_rows_batch
+    from bbarolo2_gb300.rings import RING_KEYS
+    dm, rings, data, mask, sigma, O = _setup("classic64")
+    L = engine.BatchLikelihood(dm, data, mask, maskmode=2, sigma=sigma)
+    rows = ring_rows_batch([rings] * 4)
+    rows[1, RING_KEYS.index("vrot"), 3] += 7.          # one column changed
+    rows[2, RING_KEYS.index("inc"), :] += 2.           # every column changed
+    rows[3, RING_KEYS.index("dens"), 5] *= 1.5         # another fixed-point unit
+    for prof in (False, True):
+        if prof:
+            mom0, mrms, ok = L.data_maps()
+            L.set_profile(rings, mom0, mrms, ok, smooth=0.3, corr=2.0, beam_arcsec=30.)
+        whole = L.evaluate(rows, rings, seed=1, galmodtype=galmodtype)
+        for k in range(4):
+            alone = L.evaluate(rows[k:k + 1], rings, seed=1, galmodtype=galmodtype)
+            assert whole[k] == alone[0], (prof, k, whole[k], alone[0])
