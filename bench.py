@@ -90,7 +90,6 @@ class Clocks:
 def workload(batch):
     """The device model, likelihood and one batch of ring-value rows (base + one step per free parameter)."""
     from bbarolo2_gb300 import configs, engine
-    from bbarolo2_gb300.galmod import ring_rows_batch
     from scipy import ndimage
     cube, rings = configs.global160(galmodtype="MC")
     dm = engine.DiskModel(cube)
@@ -113,16 +112,25 @@ def workload(batch):
     beam_area = math.pi * bmaj * bmin / (4. * math.log(2.)) / abs(h.Cdelt(0) * h.Cdelt(1))
     mom0, mrms, ok = L.data_maps()
     L.set_profile(rings, mom0, mrms, ok, smooth=0.3, corr=beam_area, beam_arcsec=bmaj * 3600.)
+    return dm, L, rings, step_rows(rings, batch), data, mask
+
+
+def step_rows(rings, batch):
+    """The ring values of a gradient batch: the base point, then one step of VROT, VDISP, INC or PA of one ring
+    per member: forward steps (GLOBAL's Jacobian columns, 1 + 160 points), then backward steps (a
+    central-difference gradient, 2n + 1 = 321 points)."""
+    from bbarolo2_gb300.galmod import ring_rows_batch
     base = ring_rows_batch([rings])[0]
     rows = np.repeat(base[None], batch, axis=0)
     free = [(4, 2.0), (5, 0.5), (12, 0.5), (13, 0.5)]       # vrot, vdisp, inc, phi steps
     k = 1
-    for j in range(rings.nr):
-        for row, step in free:
-            if k < batch:
-                rows[k, row, j] += step
-                k += 1
-    return dm, L, rings, rows, data, mask
+    for sign in (1.0, -1.0):
+        for j in range(rings.nr):
+            for row, step in free:
+                if k < batch:
+                    rows[k, row, j] += sign * step
+                    k += 1
+    return rows
 
 
 # ncu summaries (profiles/) with the DRAM traffic of a kernel's launch at the default batch
@@ -209,6 +217,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-analytic", action="store_true", help="skip the ANALYTIC GALMOD leg")
+    ap.add_argument("--no-central", action="store_true", help="skip the 321-point central-difference batch")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -304,6 +313,8 @@ def main():
             "logL_sample": [float(out[0]), float(out[1])]}
     if not args.no_analytic:
         line["analytic"] = analytic_leg(ctx, L, rows, rings, sr, nv, descs, args, dist, world)
+    if B == 161 and not args.no_central:
+        line["central_321"] = central_leg(ctx, L, rings, args, dist, world)
     if rank == 0 and not args.no_cpu:
         vals, cores, n = cpu_leg(dm, L, rows, rings, data, mask)
         line["cpu_baseline"] = {"value": float(np.median(vals)), "unit": UNIT, "cores": cores, "kind": "port",
@@ -314,6 +325,39 @@ def main():
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def central_leg(ctx, L, rings, args, dist, world):
+    """The central-difference gradient batch of the same problem (2n + 1 = 321 points, MC): device-resident
+    evaluations/s and end to end."""
+    from bbarolo2_gb300 import _lib
+    rows = step_rows(rings, 321)
+    sr, nv, descs, boxes = L.prepare(rows, rings, seed=1)
+    B = rows.shape[0]
+    steps = max(1, args.steps // 2)
+    ctx.check(ctx.L.bbgpu_eval_upload(ctx.h, _lib.MC, B, sr.shape[2], _lib.ptr(sr), _lib.ptr(nv), _lib.ptr(descs)))
+    ms = L._maps_sr
+    ctx.check(ctx.L.bbgpu_eval_upload_profile(ctx.h, ms.shape[2], _lib.ptr(ms), _lib.ptr(L._prof["widx"]),
+                                              _lib.ptr(L._prof["wval"])))
+    for _ in range(args.warmup):
+        ctx.check(ctx.L.bbgpu_eval_run(ctx.h))
+    ctx.check(ctx.L.bbgpu_sync(ctx.h))
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ctx.check(ctx.L.bbgpu_eval_run(ctx.h))
+    ctx.check(ctx.L.bbgpu_sync(ctx.h))
+    dt = max_over_ranks(time.perf_counter() - t0, dist)
+    L.evaluate(rows, rings, seed=1)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        L.evaluate(rows, rings, seed=1)
+    te = max_over_ranks(time.perf_counter() - t0, dist)
+    return {"batch": B, "value": throughput(B, steps, world, dt), "unit": UNIT, "steps": steps,
+            "ms_per_step": 1e3 * dt / steps, "e2e": throughput(B, steps, world, te)}
 
 
 def analytic_leg(ctx, L, rows, rings, sr, nv, descs, args, dist, world):
