@@ -1539,6 +1539,28 @@ extern "C" int bbgpu_set_profile(bbgpu_ctx *ctx, int nr, int blo0, int blo1, int
         const double bv = y / sg;
         bb += bv * bv;
     }
+    // the used pixels in blocks of 8 x 16 (the tiles of the normal equations then cover compact patches, crossed
+    // by few rings); within a block in raster order
+    {
+        std::vector<int> order(pix.size());
+        for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
+        const int bx16 = (b.bx + 15) / 16;
+        auto key = [&](int i) {
+            const int p = pix[i], py = p / b.bx, px = p - py * b.bx;
+            return ((long long)(py / 8) * bx16 + px / 16) * 128 + (py % 8) * 16 + px % 16;
+        };
+        std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return key(a) < key(c); });
+        std::vector<int> p2(pix.size());
+        std::vector<double> w2(w.size()), wy2(wy.size());
+        for (size_t i = 0; i < order.size(); i++) {
+            p2[i] = pix[order[i]];
+            w2[i] = w[order[i]];
+            wy2[i] = wy[order[i]];
+        }
+        pix.swap(p2);
+        w.swap(w2);
+        wy.swap(wy2);
+    }
     ctx->npix_used = (int)pix.size();
     ctx->pc.m = (int)pix.size();
     ctx->pc.bb = bb;

@@ -156,7 +156,9 @@ __global__ void k_maps_to_f32(const long long *__restrict__ in, const int *__res
 // CTA (tile of GRAM_TP used pixels, member k). Entry e < n(n+1)/2: G[i][j] (i <= j, row-major packed upper),
 // then h[i]. The tile is staged in shared memory as float64 (the maps and the maps times the pixel weights) with
 // the range of rings not zero at each pixel, so that each product is one float64 FMA over the band of rings that
-// overlap there. Partial sums per tile, summed over the tiles in order by k_prof_gram_reduce.
+// overlap there; the entries outside the union of the tile's bands (the used pixels come in compact blocks, so
+// the union is narrow) are zero without a loop. Partial sums per tile, summed over the tiles in order by
+// k_prof_gram_reduce.
 // pix == nullptr: the pixels 0 .. npix_used - 1; wpix == nullptr: unit weights.
 template <class T>
 __global__ void __launch_bounds__(256) k_prof_gram(const T *__restrict__ K, ProfBox box, const int *__restrict__ pix,
@@ -183,6 +185,9 @@ __global__ void __launch_bounds__(256) k_prof_gram(const T *__restrict__ K, Prof
     }
     for (int i = threadIdx.x; i < np; i += blockDim.x) wys[i] = wy[p0 + i];
     __syncthreads();
+    __shared__ int band[2];                                 // the tile's rings: band[0] .. band[1]
+    if (threadIdx.x == 0) { band[0] = n; band[1] = -1; }
+    __syncthreads();
     for (int pp = threadIdx.x; pp < np; pp += blockDim.x) {
         int a = n, b = -1;
         for (int r = 0; r < n; r++)
@@ -192,18 +197,25 @@ __global__ void __launch_bounds__(256) k_prof_gram(const T *__restrict__ K, Prof
             }
         lo[pp] = a;
         hi[pp] = b;
+        if (b >= a) {
+            atomicMin(&band[0], a);
+            atomicMax(&band[1], b);
+        }
     }
     __syncthreads();
+    const int blo = band[0], bhi = band[1];
     double *out = part + ((size_t)k * gridDim.x + t) * nent;
     for (int e = threadIdx.x; e < nent; e += blockDim.x) {
         const int i = ent_i[e], j = ent_j[e];
         double acc = 0.0;
         if (j >= 0) {
-            for (int pp = 0; pp < np; pp++)
-                if (lo[pp] <= i && j <= hi[pp]) acc = fma(Kw[pp * n + i], Kd[pp * n + j], acc);
+            if (i >= blo && j <= bhi)                       // (an entry outside the tile's rings sums to zero)
+                for (int pp = 0; pp < np; pp++)
+                    if (lo[pp] <= i && j <= hi[pp]) acc = fma(Kw[pp * n + i], Kd[pp * n + j], acc);
         } else {
-            for (int pp = 0; pp < np; pp++)
-                if (lo[pp] <= i && i <= hi[pp]) acc = fma(wys[pp], Kd[pp * n + i], acc);
+            if (i >= blo && i <= bhi)
+                for (int pp = 0; pp < np; pp++)
+                    if (lo[pp] <= i && i <= hi[pp]) acc = fma(wys[pp], Kd[pp * n + i], acc);
         }
         out[e] = acc;
     }
