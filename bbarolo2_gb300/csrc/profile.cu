@@ -49,7 +49,10 @@ namespace {
 #define MAPS_TB 128         // threads per CTA
 #define MAPS_QD 16          // queued runs per thread
 
-__global__ void __launch_bounds__(MAPS_TB) k_an_maps_fast(GridDev g, const AnSub *__restrict__ subs, int nsub,
+#ifndef MAPS_MINB
+#define MAPS_MINB 8         // resident CTAs per SM (64 registers)
+#endif
+__global__ void __launch_bounds__(MAPS_TB, MAPS_MINB) k_an_maps_fast(GridDev g, const AnSub *__restrict__ subs, int nsub,
                                                           const int *__restrict__ sbase, const int *__restrict__ ssub,
                                                           const double2 *__restrict__ cs,
                                                           const float2 *__restrict__ csf, long long nsamp, int nb,
