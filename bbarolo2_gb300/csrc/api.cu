@@ -150,7 +150,8 @@ struct bbgpu_ctx {
     ZgridCache azcache;
     // options
     bool keep_smoothed = false, timing = false, want64 = false;
-    int lean = 0;                 // the batch qualifies for the lean deposit kernel
+    int lean = 0;                 // the batch qualifies for the fast deposit kernels (one line, a linear channel
+                                  // map, at most 128 samples per cloud)
     long long launches = 0;
     long long h2d = 0, d2h = 0;
     cudaEvent_t ev[NTIMER + 1] = {};

@@ -60,7 +60,8 @@ void launch_scan_tiles(cudaStream_t s, const int *count, int *offset, int *curso
 void launch_mc_scatter(cudaStream_t s, const LayoutDev &L, const SubMC *sub, int nsub, const MemberDev *mem, int nb,
                        int tx, int ty, const int *pix, int *cursor, void *bucket);
 // Deposits the clouds of every tile into a shared-memory fixed-point tile and writes the model
-// (by, bx, nz) float32 of each member at model + k * mstride (and, if model64, float64 sums).
+// (by, bx, nz) float32 of each member at model + k * mstride (and, if model64, float64 sums); lean: the batch
+// qualifies for the fast kernels (one line, a linear channel map, at most 128 samples per cloud).
 void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
                        const MemberDev *mem, const MemberDev *mem_host, int nb, int tx, int ty,
                        const int *offset, const int *count, const void *bucket, const ZigDev *zig,

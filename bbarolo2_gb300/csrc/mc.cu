@@ -5,11 +5,18 @@
 // its radius R, cos/sin of its azimuth and its layer deviate, per sub-cloud the first word of its normal
 // deviate (the values of the rare normals that took the slow path of the ziggurat in a side list).
 //
-// Per evaluation two kernels place the clouds:
-//   k_mc_bin      pixel of every cloud in the member's box, and the count of clouds per pixel tile;
-//   k_mc_scatter  the clouds of each tile gathered into a bucket (counting sort by tile);
-//   k_mc_deposit  one CTA per (member, tile): every sub-cloud of the tile's clouds is added, in 64-bit fixed
-//                 point, to a shared-memory tile (pixels x channels), written once to HBM at the end.
+// Per evaluation the kernels place the clouds:
+//   k_mc_bin      pixel of every cloud in the member's box, and the count of clouds per pixel;
+//   k_scan_*      the offsets of the per-pixel lists (64 lists per tile of at most 64 pixels);
+//   k_mc_scatter  the entry of every cloud (its pixel, sorted normals, channel centre and rounding bound, fixed-point
+//                 flux) into its pixel's list (a counting sort);
+//   deposit       one CTA per (member, tile): every sub-cloud of the tile's clouds is added, in 64-bit fixed
+//                 point, to a shared-memory tile (pixels x channels), written once to HBM at the end:
+//                 k_mc_deposit_px  the common case (a linear channel map, one line, at most 128 samples per
+//                                  cloud, tiles of 32 or 64 pixels): pixel-owned lane groups;
+//                 k_mc_deposit_lean  the same criteria on smaller tiles (more than 224 channels): a warp per
+//                                  cloud;
+//                 k_mc_deposit     everything else (several lines, non-linear axes, float64 output).
 // Fixed-point sums are exact and independent of the order of the deposits: the model is deterministic.
 //
 // Indices are bit-exact with the reference: each pixel and channel is first computed in float32 with a
