@@ -2,7 +2,9 @@
 // bbarolo/galmod.py:1273-1283, bbarolo/bayesian/likelihood.py:22-77).
 //
 // The model of a member is (by, bx, nz) float32: channels fastest, so that a warp holds 32 channels of one
-// pixel and every load and store is a 128-byte line. One CTA computes a 16 x 16 pixel tile of 32 channels:
+// pixel and every load and store is a 128-byte line. One CTA computes a 16 x 16 pixel tile of 32 channels (or,
+// when 16-channel blocks pad the channels less, as the 41 ring maps of the flux normalisation, a 16 x 32 tile of
+// 16 channels, the two half-warps on the two halves of the rows):
 // the input tile with its halo (zero outside the box: the reference convolves the box with zero padding) is
 // staged in shared memory, each thread accumulates two output rows of 16 pixels for its channel over the
 // kernel rows, from a register window of the input row (float32 FMAs; the taps are broadcast from shared
@@ -18,9 +20,8 @@
 
 namespace {
 
-constexpr int TO = 16;        // output tile side (pixels)
-constexpr int ZB = 32;        // channels per CTA (one per lane)
-constexpr int NW = 8;         // warps per CTA: two output rows each
+constexpr int TO = 16;        // output tile width (pixels); tile height 16 (ZB = 32) or 32 (ZB = 16)
+constexpr int NW = 8;         // warps per CTA: two output rows of each half-warp group
 
 // cp.async of 16 (or 4) bytes into shared memory; src_size 0 fills the destination with zeros (the halo
 // outside the box), without reading the source.
@@ -33,7 +34,7 @@ __device__ __forceinline__ void cp_async_zfill4(float *dst, const float *src, bo
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(ok ? 4 : 0) : "memory");
 }
 
-template <int KXW>
+template <int KXW, int ZB>
 __global__ void __launch_bounds__(256, 2) k_conv_resid(GridDev g, const MemberDev *__restrict__ mem,
                                                        const float *__restrict__ model, long long mstride, int nz,
                                                        const float *__restrict__ taps, int ky, int kx,
@@ -41,9 +42,10 @@ __global__ void __launch_bounds__(256, 2) k_conv_resid(GridDev g, const MemberDe
                                                        double *__restrict__ partial, int npart) {
     extern __shared__ float sm[];
     constexpr int W = TO + KXW - 1;
+    constexpr int TOY = TO * (32 / ZB);     // tile rows: 32 / ZB groups of lanes, 16 rows each
     const int k = blockIdx.x;
     const MemberDev &M = mem[k];
-    const int ntx = (M.bx + TO - 1) / TO, nty = (M.by + TO - 1) / TO;
+    const int ntx = (M.bx + TO - 1) / TO, nty = (M.by + TOY - 1) / TOY;
     const int t = blockIdx.y, zb = blockIdx.z;
     const int nzb = gridDim.z;
     double *pout = partial + 2 * ((size_t)k * npart + (size_t)t * nzb + zb);
@@ -53,12 +55,13 @@ __global__ void __launch_bounds__(256, 2) k_conv_resid(GridDev g, const MemberDe
     }
     const int ky_eff = do_conv ? ky : 1, kx_eff = do_conv ? kx : 1;
     const int hy = ky_eff / 2, hx = kx_eff / 2;
-    const int H = TO + ky_eff - 1, ncol = TO + kx_eff - 1;
+    const int H = TOY + ky_eff - 1, ncol = TO + kx_eff - 1;
     float *S = sm;                          // H x W x ZB
     float *sk = sm + (size_t)H * W * ZB;    // ky x KXW taps
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int y0 = (t / ntx) * TO, x0 = (t % ntx) * TO;
-    const int z = zb * ZB + lane;
+    const int ch = lane % ZB, grp = lane / ZB;
+    const int y0 = (t / ntx) * TOY, x0 = (t % ntx) * TO;
+    const int z = zb * ZB + ch;
     const bool zok = z < nz;
     if (do_conv)
         for (int i = threadIdx.x; i < ky * KXW; i += blockDim.x) sk[i] = taps[i];
@@ -85,7 +88,7 @@ __global__ void __launch_bounds__(256, 2) k_conv_resid(GridDev g, const MemberDe
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
     // the data of this thread's output voxels, loaded while the tile arrives
-    const int ty0 = warp * 2;
+    const int ty0 = grp * 16 + warp * 2;
     float dv[2][TO];
 #pragma unroll
     for (int rr = 0; rr < 2; rr++) {
@@ -121,7 +124,7 @@ __global__ void __launch_bounds__(256, 2) k_conv_resid(GridDev g, const MemberDe
             // input row ty0 + i feeds output row ty0 with kernel row i and output row ty0 + 1 with kernel row
             // i - 1: each input row is read from shared memory once (the sums run over the kernel rows in order)
             for (int i = 0; i <= ky; i++) {
-                const float *row = S + (size_t)((ty0 + i) * W) * ZB + lane;
+                const float *row = S + (size_t)((ty0 + i) * W) * ZB + ch;
                 float win[W];
 #pragma unroll
                 for (int j = 0; j < W; j++) win[j] = row[j * ZB];
@@ -147,7 +150,7 @@ __global__ void __launch_bounds__(256, 2) k_conv_resid(GridDev g, const MemberDe
             for (int rr = 0; rr < 2; rr++) {
                 const int ty = ty0 + rr;
 #pragma unroll
-                for (int x = 0; x < TO; x++) acc[rr][x] = S[(size_t)(ty * W + x) * ZB + lane];
+                for (int x = 0; x < TO; x++) acc[rr][x] = S[(size_t)(ty * W + x) * ZB + ch];
             }
         }
     }
@@ -157,7 +160,7 @@ __global__ void __launch_bounds__(256, 2) k_conv_resid(GridDev g, const MemberDe
     const bool fr = M.eps2 > 0.0;
 #pragma unroll
     for (int rr = 0; rr < 2; rr++) {
-        const int y = y0 + warp * 2 + rr;
+        const int y = y0 + ty0 + rr;
         if (y >= M.by || !zok) continue;
 #pragma unroll
         for (int x = 0; x < TO; x++) {
@@ -218,20 +221,25 @@ __global__ void k_reduce_partials(const double *__restrict__ partial, int npart,
     if (threadIdx.x == 0) { out2[2 * k] = sa[0]; out2[2 * k + 1] = sb[0]; }
 }
 
-template <int KXW>
+// the channel block of a cube: 16 lanes when it pads the channels less than 32 (e.g. 41 ring maps: 48 against
+// 64), else 32
+int conv_zb(int nz) { return ((nz + 15) / 16) * 16 < ((nz + 31) / 32) * 32 ? 16 : 32; }
+
+template <int KXW, int ZB>
 void launch_t(cudaStream_t s, const GridDev &g, const MemberDev *mem, int nb, int maxt, int nzb, const float *model,
               long long mstride, int nz, const float *taps, int ky, int kx, float *smoothed, int do_conv,
               int do_resid, double *partial, int npart) {
     const int kye = do_conv ? ky : 1;
-    size_t smem = (size_t)(TO + kye - 1) * (TO + KXW - 1) * ZB * sizeof(float) + (size_t)ky * KXW * sizeof(float);
+    constexpr int TOY = TO * (32 / ZB);
+    size_t smem = (size_t)(TOY + kye - 1) * (TO + KXW - 1) * ZB * sizeof(float) + (size_t)ky * KXW * sizeof(float);
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {
-        cudaFuncSetAttribute(k_conv_resid<KXW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_conv_resid<KXW, ZB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         configured = smem;
     }
     dim3 grid(nb, maxt, nzb);
-    k_conv_resid<KXW><<<grid, 256, smem, s>>>(g, mem, model, mstride, nz, taps, ky, kx, smoothed, do_conv, do_resid,
-                                             partial, npart);
+    k_conv_resid<KXW, ZB><<<grid, 256, smem, s>>>(g, mem, model, mstride, nz, taps, ky, kx, smoothed, do_conv,
+                                                 do_resid, partial, npart);
 }
 
 }  // namespace
@@ -250,24 +258,39 @@ int conv_taps(const double *k, int ky, int kx, float *taps) {
     return kxw;
 }
 
-int conv_resid_npart(const MemberDev *mem_host, int nb, int nz) {
-    int maxt = 0;
+// tiles of the largest member box (TO x TOY pixels) and channel blocks of a cube
+static void conv_grid(const MemberDev *mem_host, int nb, int nz, int &maxt, int &nzb) {
+    const int zbw = conv_zb(nz), toy = TO * (32 / zbw);
+    maxt = 0;
     for (int k = 0; k < nb; k++)
-        maxt = max(maxt, ((mem_host[k].bx + TO - 1) / TO) * ((mem_host[k].by + TO - 1) / TO));
-    return maxt * ((nz + ZB - 1) / ZB);
+        maxt = max(maxt, ((mem_host[k].bx + TO - 1) / TO) * ((mem_host[k].by + toy - 1) / toy));
+    nzb = (nz + zbw - 1) / zbw;
+}
+
+int conv_resid_npart(const MemberDev *mem_host, int nb, int nz) {
+    int maxt, nzb;
+    conv_grid(mem_host, nb, nz, maxt, nzb);
+    return maxt * nzb;
 }
 
 void launch_conv_resid(cudaStream_t s, const GridDev &g, const MemberDev *mem, const MemberDev *mem_host, int nb,
                        const float *model, long long mstride, int nz, const float *taps, int ky, int kx, int kxw,
                        float *smoothed, int do_conv, int do_resid, double *partial) {
-    int maxt = 0;
-    for (int k = 0; k < nb; k++)
-        maxt = max(maxt, ((mem_host[k].bx + TO - 1) / TO) * ((mem_host[k].by + TO - 1) / TO));
+    int maxt, nzb;
+    conv_grid(mem_host, nb, nz, maxt, nzb);
     if (nb == 0 || maxt == 0) return;
-    const int nzb = (nz + ZB - 1) / ZB;
     const int npart = maxt * nzb;
     if (!do_conv) kxw = 1;
-#define CASE(W) case W: launch_t<W>(s, g, mem, nb, maxt, nzb, model, mstride, nz, taps, ky, kx, smoothed, do_conv, do_resid, partial, npart); break;
+    const bool z16 = conv_zb(nz) == 16;
+#define CASE(W)                                                                                                    \
+    case W:                                                                                                        \
+        if (z16)                                                                                                   \
+            launch_t<W, 16>(s, g, mem, nb, maxt, nzb, model, mstride, nz, taps, ky, kx, smoothed, do_conv, do_resid, \
+                            partial, npart);                                                                       \
+        else                                                                                                       \
+            launch_t<W, 32>(s, g, mem, nb, maxt, nzb, model, mstride, nz, taps, ky, kx, smoothed, do_conv, do_resid, \
+                            partial, npart);                                                                       \
+        break;
     switch (kxw) {
         CASE(1) CASE(3) CASE(5) CASE(7) CASE(9) CASE(11) CASE(13) CASE(15) CASE(17) CASE(21) CASE(25) CASE(31)
         default: break;
