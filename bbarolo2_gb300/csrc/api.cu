@@ -123,6 +123,16 @@ struct bbgpu_ctx {
     size_t d_maps64_cap = 0;
     MemberDev *d_pmem = nullptr;
     size_t d_pmem_cap = 0;
+    // rows of the maps (the members with a profile of their own, nu of them) and the segments of the maps
+    // kernel's threads (bbgpu_eval_upload_profile); the solutions of the rows go to the members by prof_of
+    int nu = 0, nseg = 0;
+    long long mtot = 0;
+    long long *d_mstart = nullptr;
+    int *d_mseg = nullptr, *d_uidx = nullptr, *d_ubase = nullptr, *d_prof_of = nullptr, *d_pstatu = nullptr;
+    double *d_pxu = nullptr;
+    size_t d_mstart_cap = 0, d_mseg_cap = 0, d_uidx_cap = 0, d_ubase_cap = 0, d_prof_of_cap = 0, d_pstatu_cap = 0,
+           d_pxu_cap = 0;
+    std::vector<int> psbase_host;      // first sample of each sub-ring in the sample table on the device
     ZgridCache zcache;                 // vertical grids of the ring maps (host), mirrored in d_pzq/d_pzqf/d_pwqf
     std::string samp_key;              // the sub-ring radii of the sample table on the device
     AnSub *h_psub = nullptr;           // pinned staging of the sub-ring constants
@@ -150,6 +160,7 @@ struct bbgpu_ctx {
     ZgridCache azcache;
     // options
     bool keep_smoothed = false, timing = false, want64 = false;
+    bool share_maps = true;       // ring maps of members that differ from member 0 in few sub-rings: shared
     int lean = 0;                 // the batch qualifies for the fast deposit kernels (one line, a linear channel
                                   // map, at most 128 samples per cloud)
     long long launches = 0;
@@ -421,7 +432,8 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
                     (void *)ctx->d_pwval, (void *)ctx->d_rap, (void *)ctx->d_gpart, (void *)ctx->d_gh,
                     (void *)ctx->d_px, (void *)ctx->d_ppart, (void *)ctx->d_pzqf, (void *)ctx->d_pwqf,
                     (void *)ctx->d_pwvalf, (void *)ctx->d_maps32, (void *)ctx->d_K, (void *)ctx->d_maps64,
-                    (void *)ctx->d_pmem})
+                    (void *)ctx->d_pmem, (void *)ctx->d_mstart, (void *)ctx->d_mseg, (void *)ctx->d_uidx,
+                    (void *)ctx->d_ubase, (void *)ctx->d_prof_of, (void *)ctx->d_pstatu, (void *)ctx->d_pxu})
         cudaFree(q);
     for (void *q : {(void *)ctx->d_asub, (void *)ctx->d_asbase, (void *)ctx->d_assub, (void *)ctx->d_acs,
                     (void *)ctx->d_azq, (void *)ctx->d_awq, (void *)ctx->d_model_fx, (void *)ctx->d_acsf,
@@ -472,6 +484,7 @@ extern "C" int bbgpu_set_option(bbgpu_ctx *ctx, int opt, int value) {
     switch (opt) {
         case 1: ctx->keep_smoothed = value != 0; break;
         case 2: ctx->timing = value != 0; break;
+        case 3: ctx->share_maps = value != 0; break;
         default: return fail(ctx, BBGPU_ERR_ARG, "unknown option %d", opt);
     }
     return BBGPU_OK;
@@ -889,30 +902,33 @@ static int profile_run(bbgpu_ctx *ctx, bool tm) {
     const GridDev &g = ctx->g;
     cudaStream_t s = ctx->stream;
     const ProfBox &bx = ctx->pbox;
-    const int nb = ctx->nb, n = ctx->pc.n;
+    const int nb = ctx->nb, n = ctx->pc.n, nu = ctx->nu;
     const long long per = bx.npix * bx.nrp;
-    CK(cudaMemsetAsync(ctx->d_maps64, 0, sizeof(long long) * (size_t)nb * per, s));
-    launch_an_maps_fast(s, g, ctx->d_psub, ctx->nsm, ctx->d_psbase, ctx->d_pssub, ctx->d_pcs, ctx->d_pcsf, ctx->pnsamp, nb,
-                        ctx->d_pzq, ctx->d_pzqf, ctx->d_pwqf, ctx->d_pwidx, ctx->d_pwvalf, bx, ctx->d_pfix,
-                        ctx->d_maps64);
+    CK(cudaMemsetAsync(ctx->d_maps64, 0, sizeof(long long) * (size_t)nu * per, s));
+    launch_an_maps_fast(s, g, ctx->d_psub, ctx->nsm, ctx->d_psbase, ctx->d_pssub, ctx->d_pcs, ctx->d_pcsf,
+                        ctx->d_mstart, ctx->d_mseg, ctx->nseg, ctx->mtot, ctx->d_pzq, ctx->d_pzqf, ctx->d_pwqf,
+                        ctx->d_pwidx, ctx->d_pwvalf, bx, ctx->d_pfix, ctx->d_maps64);
     CKL();
-    launch_maps_to_f32(s, ctx->d_maps64, ctx->d_pfix, nb, per, (float)ctx->mapscale, ctx->d_maps32);
+    launch_maps_to_f32(s, ctx->d_maps64, ctx->d_pfix, ctx->d_uidx, ctx->d_ubase, nu, per, (float)ctx->mapscale,
+                       ctx->d_maps32);
     CKL();
     if (tm) CK(cudaEventRecord(ctx->ev[1], s));
     if (ctx->kernel_set) {
-        launch_conv_resid(s, g, ctx->d_pmem, ctx->pmem_host.data(), nb, ctx->d_maps32, per, bx.nrp, ctx->d_taps,
+        launch_conv_resid(s, g, ctx->d_pmem, ctx->pmem_host.data(), nu, ctx->d_maps32, per, bx.nrp, ctx->d_taps,
                           ctx->ky, ctx->kx, ctx->kxw, ctx->d_K, 2, 0, ctx->d_ppart);
         CKL();
     }
     if (tm) CK(cudaEventRecord(ctx->ev[2], s));
     const float *K = ctx->kernel_set ? ctx->d_K : ctx->d_maps32;
     launch_prof_gram(s, K, bx, ctx->d_ppix, ctx->d_pw, ctx->d_pwy, ctx->npix_used, ctx->d_ent, ctx->d_ent + ctx->nent,
-                     ctx->nent, nb, ctx->d_gpart, ctx->d_gh);
+                     ctx->nent, nu, ctx->d_gpart, ctx->d_gh);
     ctx->launches += 2;
     CKL();
     if (tm) CK(cudaEventRecord(ctx->ev[3], s));
-    launch_prof_solve(s, ctx->d_gh, ctx->pc, ctx->d_lc, ctx->d_lv, ctx->d_ord, ctx->d_near, ctx->d_p0, nb, ctx->d_px,
-                      ctx->d_pp, ctx->d_pstat);
+    launch_prof_solve(s, ctx->d_gh, ctx->pc, ctx->d_lc, ctx->d_lv, ctx->d_ord, ctx->d_near, ctx->d_p0, nu,
+                      ctx->d_pxu, ctx->d_pp, ctx->d_pstatu);
+    CKL();
+    launch_prof_gather(s, ctx->d_pxu, ctx->d_pstatu, ctx->d_prof_of, nb, n, ctx->d_px, ctx->d_pstat);
     CKL();
     if (ctx->galmodtype == BBGPU_ANALYTIC) {
         double lsum = 0.0, cmax = 0.0;
@@ -1643,9 +1659,63 @@ extern "C" int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *
         CK(cudaMemcpy(ctx->d_pssub, ssub.data(), sizeof(int) * ssub.size(), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(ctx->d_pcs, cs.data(), sizeof(double) * cs.size(), cudaMemcpyHostToDevice));
         ctx->pnsamp = sbase[nsm];
+        ctx->psbase_host = sbase;
         ctx->samp_key = skey;
         ctx->h2d += (long long)(sizeof(int) * (sbase.size() + ssub.size()) + sizeof(double) * cs.size());
     }
+    // The rows of the maps. A member whose ring-map constants are member 0's in every sub-ring (a step of a
+    // velocity or the density) has member 0's maps and so its profile: it takes member 0's solution. A member
+    // that differs in a few sub-rings (a step of one ring's geometry), with the same fixed-point exponent, gets
+    // a row holding the difference from member 0's maps: its deposits of those sub-rings and member 0's negated,
+    // summed with member 0's row when the maps are converted (exact: 64-bit fixed point, the same units).
+    // Every other member gets a row of its own over every sample.
+    std::vector<int> uidx, ubase, prof_of(nb), mseg;
+    std::vector<long long> mstart;
+    {
+        const std::vector<int> &sb = ctx->psbase_host;
+        long long tot = 0;
+        auto seg = [&](int u, int k, int ir, int sign, long long cnt) {
+            if (cnt <= 0) return;
+            mstart.push_back(tot);
+            mseg.insert(mseg.end(), {u, k, ir, sign});
+            tot += cnt;
+        };
+        std::vector<int> ch;
+        for (int k = 0; k < nb; k++) {
+            bool delta = false;
+            if (ctx->share_maps && k > 0 && fix[k] == fix[0]) {
+                const double *sk = sr_maps + (size_t)k * BBGPU_NSR * nsm;
+                long long nch = 0;
+                ch.clear();
+                for (int i = 0; i < nsm; i++)
+                    if (!bbh_map_column_same(sk, sr_maps, nsm, i)) {
+                        ch.push_back(i);
+                        nch += sb[i + 1] - sb[i];
+                    }
+                if (ch.empty()) {
+                    prof_of[k] = 0;
+                    continue;
+                }
+                delta = 2 * nch < ctx->pnsamp;
+            }
+            const int u = (int)uidx.size();
+            prof_of[k] = u;
+            uidx.push_back(k);
+            ubase.push_back(delta ? 0 : -1);
+            if (delta) {
+                for (int i : ch) {
+                    seg(u, k, i, 1, sb[i + 1] - sb[i]);
+                    seg(u, 0, i, -1, sb[i + 1] - sb[i]);
+                }
+            } else {
+                seg(u, k, -1, 1, ctx->pnsamp);
+            }
+        }
+        ctx->mtot = tot;
+        mstart.push_back(tot);
+    }
+    ctx->nu = (int)uidx.size();
+    ctx->nseg = (int)mstart.size() - 1;
     // the vertical grids: the new ones appended on the device (the table grows with a copy of the old part)
     const size_t nz1 = zc.zq.size() + 1;
     if (zc.uploaded == 0 || nz1 > ctx->d_pzq_cap) {
@@ -1695,6 +1765,13 @@ extern "C" int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *
     if ((rc = dgrow(ctx, &ctx->d_px, &ctx->d_px_cap, (size_t)nb * n))) return rc;
     if ((rc = dgrow(ctx, &ctx->d_pp, &ctx->d_pp_cap, (size_t)nb * n))) return rc;
     if ((rc = dgrow(ctx, &ctx->d_pstat, &ctx->d_pstat_cap, (size_t)nb))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_pxu, &ctx->d_pxu_cap, (size_t)nb * n))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_pstatu, &ctx->d_pstatu_cap, (size_t)nb))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_mstart, &ctx->d_mstart_cap, mstart.size()))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_mseg, &ctx->d_mseg_cap, mseg.size() + 4))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_uidx, &ctx->d_uidx_cap, uidx.size()))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_ubase, &ctx->d_ubase_cap, ubase.size()))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_prof_of, &ctx->d_prof_of_cap, prof_of.size()))) return rc;
     // the maps' convolution: one member descriptor per member, the likelihood box
     ctx->pmem_host.assign(nb, MemberDev{});
     for (auto &M : ctx->pmem_host) {
@@ -1714,7 +1791,13 @@ extern "C" int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *
     CK(cudaMemcpyAsync(ctx->d_rap, rap.data(), sizeof(double) * rap.size(), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(ctx->d_pfix, fix.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(ctx->d_pmem, ctx->pmem_host.data(), sizeof(MemberDev) * nb, cudaMemcpyHostToDevice, s));
-    ctx->h2d += (long long)(sizeof(AnSub) * (size_t)nb * nsm + sizeof(int) * nb);
+    CK(cudaMemcpyAsync(ctx->d_mstart, mstart.data(), sizeof(long long) * mstart.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->d_mseg, mseg.data(), sizeof(int) * mseg.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->d_uidx, uidx.data(), sizeof(int) * uidx.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->d_ubase, ubase.data(), sizeof(int) * ubase.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->d_prof_of, prof_of.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s));
+    ctx->h2d += (long long)(sizeof(AnSub) * (size_t)nb * nsm + sizeof(int) * nb + sizeof(long long) * mstart.size() +
+                            sizeof(int) * (mseg.size() + uidx.size() + ubase.size() + nb));
     // (the host vectors go out of scope: finish the copies first)
     CK(cudaStreamSynchronize(s));
     ctx->nsm = nsm;

@@ -273,6 +273,13 @@ static bool same_column(const double *a, const double *b, int nsub, int ir) {
     return true;
 }
 
+bool bbh_map_column_same(const double *a, const double *b, int nsub, int ir) {
+    auto same = [&](int r) { return !memcmp(a + (size_t)r * nsub + ir, b + (size_t)r * nsub + ir, sizeof(double)); };
+    for (int r : {0, 6, 7, 9, 10, 11, 12, 14, 15})
+        if (!same(r)) return false;
+    return a[(size_t)7 * nsub + ir] == 0.0 || same(4);
+}
+
 int bbh_submc(const double *sr, int nsub, const int *nc, const int *nv, const GridDev *g, SubMC *out,
               const double *sr_ref, const SubMC *out_ref, signed char *reused) {
     double bound = 0.;

@@ -138,6 +138,11 @@ struct ZgridCache {
 int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0, int blo1, int bhi0, int bhi1,
                 const double *cd2i, int maps, const int64_t *widx, const double *wval, AnSub *out, ZgridCache &zc,
                 const double *sr_ref = nullptr, const AnSub *out_ref = nullptr, signed char *reused = nullptr);
+// true if sub-ring ir of the ring-map tables a and b (16 rows, nsub columns) gives the same ring-map constants
+// in bbh_an_subs (maps mode): the same radius, scale height, velocity gradient, inclination, position angle,
+// centre and side weights, and the same dispersion where a velocity gradient makes the vertical grid depend
+// on it (the velocities and the density do not enter a ring map)
+bool bbh_map_column_same(const double *a, const double *b, int nsub, int ir);
 // The second-difference prior of the deconvolved profile at the radii R (n) (bbarolo/profile.py:60-151):
 // rows (n - 2) x 3 columns lc and weights lv, the order of the radii, the "near" rows, the median ring
 // distance d and the norm of the relative prior

@@ -140,12 +140,18 @@ struct ProfConst {
     double bb;                    // b.b
     double smooth, corr, floor_, norm, d;
 };
+// The ring maps of a batch, by segments of threads: segment i (threads mstart[i] .. mstart[i+1]) is mseg[4i..4i+4)
+// = (row u of maps64, member whose sub-ring constants it takes, sub-ring (-1: every sample of the table), sign)
 void launch_an_maps_fast(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase,
-                         const int *ssub, const double *cs, const float *csf, long long nsamp, int nb, const double *zq,
-                         const float *zqf, const float *wqf, const int *widx, const float *wvalf, const ProfBox &box,
+                         const int *ssub, const double *cs, const float *csf, const long long *mstart,
+                         const int *mseg, int nseg, long long ntot, const double *zq, const float *zqf,
+                         const float *wqf, const int *widx, const float *wvalf, const ProfBox &box,
                          const int *fix_exp, long long *maps64);
-void launch_maps_to_f32(cudaStream_t s, const long long *in, const int *fix_exp, int nb, long long per_member,
-                        float scale, float *out);
+// rows u < nu of maps64 (member uidx[u]; plus row ubase[u] when >= 0) -> float32
+void launch_maps_to_f32(cudaStream_t s, const long long *in, const int *fix_exp, const int *uidx, const int *ubase,
+                        int nu, long long per_member, float scale, float *out);
+void launch_prof_gather(cudaStream_t s, const double *xu, const int *stu, const int *prof_of, int nb, int n, double *x,
+                        int *st);
 int prof_gram_tiles(int npix_used);
 void launch_prof_gram(cudaStream_t s, const float *K, const ProfBox &box, const int *pix, const double *wpix,
                       const double *wy, int npix_used, const int *ent_i, const int *ent_j, int nent, int nb,

@@ -55,7 +55,9 @@ namespace {
 __global__ void __launch_bounds__(MAPS_TB, MAPS_MINB) k_an_maps_fast(GridDev g, const AnSub *__restrict__ subs, int nsub,
                                                           const int *__restrict__ sbase, const int *__restrict__ ssub,
                                                           const double2 *__restrict__ cs,
-                                                          const float2 *__restrict__ csf, long long nsamp, int nb,
+                                                          const float2 *__restrict__ csf,
+                                                          const long long *__restrict__ mstart,
+                                                          const int4 *__restrict__ mseg, int nseg, long long ntot,
                                                           const double *__restrict__ zq,
                                                           const float *__restrict__ zqf,
                                                           const float *__restrict__ wqf, const int *__restrict__ widx,
@@ -66,15 +68,23 @@ __global__ void __launch_bounds__(MAPS_TB, MAPS_MINB) k_an_maps_fast(GridDev g, 
     const int tid = threadIdx.x;
     const long long gs = (long long)blockIdx.x * MAPS_TB + tid;
     // this thread's sample; nzz = 0: nothing to deposit (the thread still takes part in the warp's drains)
-    int k = 0, kr = 0, nzz = 0, off = 0, i0 = -1, i1 = -1;
+    int u = 0, kr = 0, nzz = 0, off = 0, i0 = -1, i1 = -1;
     long long s = 0;
     const AnSub *S = subs;
     PixF px{};
     float v0 = 0.f, v1 = 0.f;
-    if (gs < nsamp * nb) {
-        k = (int)(gs / nsamp);
-        s = gs - (long long)k * nsamp;
+    if (gs < ntot) {
+        int lo = 0, hi = nseg - 1;                    // the thread's segment: the last one starting at or before gs
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (mstart[mid] <= gs) lo = mid;
+            else hi = mid - 1;
+        }
+        const int4 sg = mseg[lo];
+        u = sg.x;
+        s = gs - mstart[lo] + (sg.z >= 0 ? sbase[sg.z] : 0);
         const int ir = ssub[s];
+        const int k = sg.y;
         S = subs + (size_t)k * nsub + ir;
         const float2 cf = csf[s];
         const bool rec = cf.x >= 0.0f;                // (the sign of the float32 table is the float64 test's)
@@ -85,13 +95,14 @@ __global__ void __launch_bounds__(MAPS_TB, MAPS_MINB) k_an_maps_fast(GridDev g, 
             nzz = S->nzz;
             off = S->zq_off;
             const int e = fix_exp[k];
+            const float sgn = (float)sg.w;            // (-1: the base member's deposits taken out, exactly)
             i0 = widx[2 * ir];
             i1 = widx[2 * ir + 1];
-            v0 = i0 >= 0 ? ldexpf(S->fluxscf * wvalf[2 * ir] * wsidef, e) : 0.f;
-            v1 = i1 >= 0 ? ldexpf(S->fluxscf * wvalf[2 * ir + 1] * wsidef, e) : 0.f;
+            v0 = i0 >= 0 ? sgn * ldexpf(S->fluxscf * wvalf[2 * ir] * wsidef, e) : 0.f;
+            v1 = i1 >= 0 ? sgn * ldexpf(S->fluxscf * wvalf[2 * ir + 1] * wsidef, e) : 0.f;
         }
     }
-    unsigned long long *out = maps64 + (size_t)k * box.npix * box.nrp;
+    unsigned long long *out = maps64 + (size_t)u * box.npix * box.nrp;
     int cnt = 0;
     auto push = [&](int g0, int g1, float ws) {
         const unsigned px = (unsigned)(g0 - box.blo0), py = (unsigned)(g1 - box.blo1);
@@ -143,16 +154,30 @@ __global__ void __launch_bounds__(MAPS_TB, MAPS_MINB) k_an_maps_fast(GridDev g, 
     drain();
 }
 
-// maps (member, pixel, ring) int64 units 2^-e -> float32 x scale
-__global__ void k_maps_to_f32(const long long *__restrict__ in, const int *__restrict__ fix_exp, long long per_member,
+// maps (row u, pixel, ring) int64 units 2^-e -> float32 x scale; a row with a base row holds the difference from
+// it (the sum, modulo 2^64, is the row's maps: exact whatever the order of the deposits)
+__global__ void k_maps_to_f32(const long long *__restrict__ in, const int *__restrict__ fix_exp,
+                              const int *__restrict__ uidx, const int *__restrict__ ubase, long long per_member,
                               float scale, float *__restrict__ out) {
-    const int k = blockIdx.y;
-    const float sc = ldexpf(scale, -fix_exp[k]);
-    const long long *src = in + (size_t)k * per_member;
-    float *dst = out + (size_t)k * per_member;
+    const int u = blockIdx.y;
+    const float sc = ldexpf(scale, -fix_exp[uidx[u]]);
+    const long long *src = in + (size_t)u * per_member;
+    const long long *bas = ubase[u] >= 0 ? in + (size_t)ubase[u] * per_member : nullptr;
+    float *dst = out + (size_t)u * per_member;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < per_member;
-         i += (long long)gridDim.x * blockDim.x)
-        dst[i] = ll_to_f32(src[i]) * sc;
+         i += (long long)gridDim.x * blockDim.x) {
+        long long v = src[i];
+        if (bas) v = (long long)((unsigned long long)v + (unsigned long long)bas[i]);
+        dst[i] = ll_to_f32(v) * sc;
+    }
+}
+
+// the solutions of the rows, to the members: x[k] = xu[prof_of[k]], status likewise
+__global__ void k_prof_gather(const double *__restrict__ xu, const int *__restrict__ stu,
+                              const int *__restrict__ prof_of, int n, double *__restrict__ x, int *__restrict__ st) {
+    const int k = blockIdx.x, u = prof_of[k];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) x[(size_t)k * n + i] = xu[(size_t)u * n + i];
+    if (threadIdx.x == 0) st[k] = stu[u];
 }
 
 // ------------------------------------------------------------------------------------------- Gram matrix
@@ -654,22 +679,27 @@ void launch_an_dens(cudaStream_t s, const GridDev &g, AnSub *sub, int nsub, Memb
 }
 
 void launch_an_maps_fast(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase,
-                         const int *ssub, const double *cs, const float *csf, long long nsamp, int nb, const double *zq,
-                         const float *zqf, const float *wqf, const int *widx, const float *wvalf, const ProfBox &box,
+                         const int *ssub, const double *cs, const float *csf, const long long *mstart,
+                         const int *mseg, int nseg, long long ntot, const double *zq, const float *zqf,
+                         const float *wqf, const int *widx, const float *wvalf, const ProfBox &box,
                          const int *fix_exp, long long *maps64) {
-    const long long nw = nsamp * nb;
-    if (nw == 0) return;
-    k_an_maps_fast<<<(unsigned)((nw + MAPS_TB - 1) / MAPS_TB), MAPS_TB, 0, s>>>(
-        g, subs, nsub, sbase, ssub, (const double2 *)cs, (const float2 *)csf, nsamp, nb, zq, zqf, wqf, widx, wvalf, box,
-        fix_exp,
-        (unsigned long long *)maps64);
+    if (ntot == 0 || nseg == 0) return;
+    k_an_maps_fast<<<(unsigned)((ntot + MAPS_TB - 1) / MAPS_TB), MAPS_TB, 0, s>>>(
+        g, subs, nsub, sbase, ssub, (const double2 *)cs, (const float2 *)csf, mstart, (const int4 *)mseg, nseg, ntot,
+        zq, zqf, wqf, widx, wvalf, box, fix_exp, (unsigned long long *)maps64);
 }
 
-void launch_maps_to_f32(cudaStream_t s, const long long *in, const int *fix_exp, int nb, long long per_member,
-                        float scale, float *out) {
-    if (nb == 0 || per_member == 0) return;
-    dim3 grid((unsigned)std::min<long long>((per_member + 255) / 256, 1024), nb);
-    k_maps_to_f32<<<grid, 256, 0, s>>>(in, fix_exp, per_member, scale, out);
+void launch_maps_to_f32(cudaStream_t s, const long long *in, const int *fix_exp, const int *uidx, const int *ubase,
+                        int nu, long long per_member, float scale, float *out) {
+    if (nu == 0 || per_member == 0) return;
+    dim3 grid((unsigned)std::min<long long>((per_member + 255) / 256, 1024), nu);
+    k_maps_to_f32<<<grid, 256, 0, s>>>(in, fix_exp, uidx, ubase, per_member, scale, out);
+}
+
+void launch_prof_gather(cudaStream_t s, const double *xu, const int *stu, const int *prof_of, int nb, int n, double *x,
+                        int *st) {
+    if (nb == 0) return;
+    k_prof_gather<<<nb, 64, 0, s>>>(xu, stu, prof_of, n, x, st);
 }
 
 int prof_gram_tiles(int npix_used) { return (npix_used + GRAM_TP - 1) / GRAM_TP; }

@@ -218,6 +218,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-analytic", action="store_true", help="skip the ANALYTIC GALMOD leg")
     ap.add_argument("--no-central", action="store_true", help="skip the 321-point central-difference batch")
+    ap.add_argument("--no-random", action="store_true",
+                    help="skip the batch of independent points and the gradient batch without shared ring maps")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -314,7 +316,10 @@ def main():
     if not args.no_analytic:
         line["analytic"] = analytic_leg(ctx, L, rows, rings, sr, nv, descs, args, dist, world)
     if B == 161 and not args.no_central:
-        line["central_321"] = central_leg(ctx, L, rings, args, dist, world)
+        line["central_321"] = batch_leg(ctx, L, rings, step_rows(rings, 321), args, dist, world)
+    if not args.no_random:
+        line["random"] = batch_leg(ctx, L, rings, random_rows(rings, B), args, dist, world)
+        line["unshared"] = batch_leg(ctx, L, rings, rows, args, dist, world, share=False)
     if rank == 0 and not args.no_cpu:
         vals, cores, n = cpu_leg(dm, L, rows, rings, data, mask)
         line["cpu_baseline"] = {"value": float(np.median(vals)), "unit": UNIT, "cores": cores, "kind": "port",
@@ -327,37 +332,58 @@ def main():
     return 0
 
 
-def central_leg(ctx, L, rings, args, dist, world):
-    """The central-difference gradient batch of the same problem (2n + 1 = 321 points, MC): device-resident
-    evaluations/s and end to end."""
+def random_rows(rings, batch, seed=2):
+    """Ring-value rows of independent points about the base point, as nested-sampling live points: every member
+    moves VROT, VDISP, INC and PA of every ring (uniform within 5 km/s, 1 km/s, 1 and 1 degree), so that no two
+    members share a ring map."""
+    from bbarolo2_gb300.galmod import ring_rows_batch
+    base = ring_rows_batch([rings])[0]
+    rows = np.repeat(base[None], batch, axis=0)
+    g = np.random.default_rng(seed)
+    for row, half in ((4, 5.0), (5, 1.0), (12, 1.0), (13, 1.0)):
+        rows[1:, row, :] += g.uniform(-half, half, (batch - 1, rings.nr))
+    return rows
+
+
+def batch_leg(ctx, L, rings, rows, args, dist, world, share=True):
+    """Another batch of the same problem (MC): device-resident evaluations/s and end to end. share=False
+    computes every member's flux normalisation from all its samples (no member shares member 0's ring maps)."""
     from bbarolo2_gb300 import _lib
-    rows = step_rows(rings, 321)
-    sr, nv, descs, boxes = L.prepare(rows, rings, seed=1)
-    B = rows.shape[0]
-    steps = max(1, args.steps // 2)
-    ctx.check(ctx.L.bbgpu_eval_upload(ctx.h, _lib.MC, B, sr.shape[2], _lib.ptr(sr), _lib.ptr(nv), _lib.ptr(descs)))
-    ms = L._maps_sr
-    ctx.check(ctx.L.bbgpu_eval_upload_profile(ctx.h, ms.shape[2], _lib.ptr(ms), _lib.ptr(L._prof["widx"]),
-                                              _lib.ptr(L._prof["wval"])))
-    for _ in range(args.warmup):
+    ctx.set_option(_lib.OPT_SHARE_MAPS, 1 if share else 0)
+    try:
+        sr, nv, descs, boxes = L.prepare(rows, rings, seed=1)
+        B = rows.shape[0]
+        steps = max(1, args.steps // 2)
+        ctx.check(ctx.L.bbgpu_eval_upload(ctx.h, _lib.MC, B, sr.shape[2], _lib.ptr(sr), _lib.ptr(nv),
+                                          _lib.ptr(descs)))
+        ms = L._maps_sr
+        ctx.check(ctx.L.bbgpu_eval_upload_profile(ctx.h, ms.shape[2], _lib.ptr(ms), _lib.ptr(L._prof["widx"]),
+                                                  _lib.ptr(L._prof["wval"])))
+        for _ in range(args.warmup):
+            ctx.check(ctx.L.bbgpu_eval_run(ctx.h))
+        ctx.check(ctx.L.bbgpu_sync(ctx.h))
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            ctx.check(ctx.L.bbgpu_eval_run(ctx.h))
+        ctx.check(ctx.L.bbgpu_sync(ctx.h))
+        dt = max_over_ranks(time.perf_counter() - t0, dist)
+        ctx.set_option(_lib.OPT_TIMING, 1)
         ctx.check(ctx.L.bbgpu_eval_run(ctx.h))
-    ctx.check(ctx.L.bbgpu_sync(ctx.h))
-    if dist:
-        dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        ctx.check(ctx.L.bbgpu_eval_run(ctx.h))
-    ctx.check(ctx.L.bbgpu_sync(ctx.h))
-    dt = max_over_ranks(time.perf_counter() - t0, dist)
-    L.evaluate(rows, rings, seed=1)
-    if dist:
-        dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(steps):
+        kt = {k: round(v, 4) for k, v in ctx.run_times().items() if k.startswith("prof_")}
+        ctx.set_option(_lib.OPT_TIMING, 0)
         L.evaluate(rows, rings, seed=1)
-    te = max_over_ranks(time.perf_counter() - t0, dist)
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            L.evaluate(rows, rings, seed=1)
+        te = max_over_ranks(time.perf_counter() - t0, dist)
+    finally:
+        ctx.set_option(_lib.OPT_SHARE_MAPS, 1)
     return {"batch": B, "value": throughput(B, steps, world, dt), "unit": UNIT, "steps": steps,
-            "ms_per_step": 1e3 * dt / steps, "e2e": throughput(B, steps, world, te)}
+            "ms_per_step": 1e3 * dt / steps, "e2e": throughput(B, steps, world, te), "profile_ms": kt}
 
 
 def analytic_leg(ctx, L, rows, rings, sr, nv, descs, args, dist, world):

@@ -154,7 +154,9 @@ int bbgpu_eval_batch(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const dou
 int bbgpu_eval_model(bbgpu_ctx *ctx, int k, int smoothed, float *out, int by, int bx, int nz);
 /* Synchronise the context's stream. */
 int bbgpu_sync(bbgpu_ctx *ctx);
-/* Options: 1 keep the smoothed models of a batch (for bbgpu_eval_model), 2 time the kernels of each run. */
+/* Options: 1 keep the smoothed models of a batch (for bbgpu_eval_model), 2 time the kernels of each run,
+ * 3 share the flux normalisation between members whose ring maps are the first member's up to a few sub-rings
+ * (default 1; the results are the same bit for bit, 0 computes every member's maps from all its samples). */
 int bbgpu_set_option(bbgpu_ctx *ctx, int option, int value);
 
 /* ---- without allocation ------------------------------------------------------------------------------- */

@@ -132,3 +132,49 @@ def test_batch_profile_vs_oracle(gpu_lib, oracle_lib, galmodtype):
     # the profile is recomputed at each run: a second evaluation gives the same values
     ll2 = L.evaluate(rows, rings, seed=1, galmodtype=galmodtype)
     np.testing.assert_array_equal(ll, ll2)
+
+
+@pytest.mark.parametrize("galmodtype", ["MC", "ANALYTIC"])
+def test_batch_profile_shared_members(gpu_lib, oracle_lib, galmodtype):
+    """A finite-difference batch (steps of one ring's VROT, VDISP, INC or PA): the members whose ring maps are
+    the base member's (velocity steps) share its profile, those that differ in a few sub-rings (geometry steps)
+    get member 0's maps plus the difference; both give, bit for bit, what every member computed from all its
+    samples gives, and the densities agree with the oracle's."""
+    from bbarolo2_gb300 import _lib
+    from bbarolo2_gb300.galmod import ring_rows_batch
+    from oracle import cpu_baseline as CB
+    dm, L, rings, _, data = _batch_workload()
+    base = ring_rows_batch([rings])[0]
+    steps = [(4, 5.0), (5, 1.0), (12, 2.0), (13, 3.0)]
+    rows = [base]
+    for j in (1, 4, 7):
+        for row, st in steps:
+            r = base.copy()
+            r[row, j] += st
+            rows.append(r)
+    rows = np.stack(rows)
+    ctx = dm.ctx
+    res = {}
+    for share in (0, 1):
+        ctx.set_option(_lib.OPT_SHARE_MAPS, share)
+        ll = L.evaluate(rows, rings, seed=1, galmodtype=galmodtype)
+        x, st = L.last_profile()
+        res[share] = (ll, x, st)
+    ctx.set_option(_lib.OPT_SHARE_MAPS, 1)
+    np.testing.assert_array_equal(res[0][0], res[1][0])
+    np.testing.assert_array_equal(res[0][1], res[1][1])
+    np.testing.assert_array_equal(res[0][2], res[1][2])
+    ll, x, st = res[1]
+    assert np.all(st == 0), st
+    sr, nv, descs, boxes = L.prepare(rows, rings, seed=1)
+    P = CB.setup_payload(dm, sr, nv, boxes, 1, data, L.mask, L.maskmode, like=L, rows=rows, proto=rings,
+                         galmodtype=galmodtype)
+    CB._W.clear()
+    CB._W.update(P)
+    for k in (0, 1, 3, 4, 11, 12):
+        xr = CB.profile_dens(k)
+        np.testing.assert_allclose(x[k], xr, rtol=DENS_RTOL, atol=DENS_RTOL * np.abs(xr).max())
+    # a batch of other members after it (the rows of the maps are rebuilt at every upload)
+    ll2 = L.evaluate(rows[::-1].copy(), rings, seed=1, galmodtype=galmodtype)
+    x2, _ = L.last_profile()
+    np.testing.assert_array_equal(x2, x[::-1])
