@@ -133,6 +133,18 @@ struct bbgpu_ctx {
     size_t d_mstart_cap = 0, d_mseg_cap = 0, d_uidx_cap = 0, d_ubase_cap = 0, d_prof_of_cap = 0, d_pstatu_cap = 0,
            d_pxu_cap = 0;
     std::vector<int> psbase_host;      // first sample of each sub-ring in the sample table on the device
+    std::vector<int> prof_of_host;     // the row of each member's profile (0: member 0's)
+    // MC: the (member, cloud) segments of the bin and scatter kernels, and the members of the two deposit
+    // launches (mc_n1 members with their own lists, then mc_n2 holding the difference from member 0's model,
+    // whose fixed-point sums are kept in d_base64); rebuilt before a run when mc_dirty
+    bool mc_dirty = true;
+    int mc_nseg = 0, mc_n1 = 0, mc_n2 = 0;
+    long long mc_ntot = 0;
+    std::vector<long long> h_cstart;
+    std::vector<int> h_cseg, h_klist;
+    long long *d_cstart = nullptr, *d_base64 = nullptr;
+    int *d_cseg = nullptr, *d_klist = nullptr;
+    size_t d_cstart_cap = 0, d_base64_cap = 0, d_cseg_cap = 0, d_klist_cap = 0;
     ZgridCache zcache;                 // vertical grids of the ring maps (host), mirrored in d_pzq/d_pzqf/d_pwqf
     std::string samp_key;              // the sub-ring radii of the sample table on the device
     AnSub *h_psub = nullptr;           // pinned staging of the sub-ring constants
@@ -160,7 +172,8 @@ struct bbgpu_ctx {
     ZgridCache azcache;
     // options
     bool keep_smoothed = false, timing = false, want64 = false;
-    bool share_maps = true;       // ring maps of members that differ from member 0 in few sub-rings: shared
+    bool share = true;            // members that differ from member 0 in a few sub-rings: computed as member 0's
+                                  // result plus the difference (ring maps, MC model)
     int lean = 0;                 // the batch qualifies for the fast deposit kernels (one line, a linear channel
                                   // map, at most 128 samples per cloud)
     long long launches = 0;
@@ -433,7 +446,8 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
                     (void *)ctx->d_px, (void *)ctx->d_ppart, (void *)ctx->d_pzqf, (void *)ctx->d_pwqf,
                     (void *)ctx->d_pwvalf, (void *)ctx->d_maps32, (void *)ctx->d_K, (void *)ctx->d_maps64,
                     (void *)ctx->d_pmem, (void *)ctx->d_mstart, (void *)ctx->d_mseg, (void *)ctx->d_uidx,
-                    (void *)ctx->d_ubase, (void *)ctx->d_prof_of, (void *)ctx->d_pstatu, (void *)ctx->d_pxu})
+                    (void *)ctx->d_ubase, (void *)ctx->d_prof_of, (void *)ctx->d_pstatu, (void *)ctx->d_pxu,
+                    (void *)ctx->d_cstart, (void *)ctx->d_base64, (void *)ctx->d_cseg, (void *)ctx->d_klist})
         cudaFree(q);
     for (void *q : {(void *)ctx->d_asub, (void *)ctx->d_asbase, (void *)ctx->d_assub, (void *)ctx->d_acs,
                     (void *)ctx->d_azq, (void *)ctx->d_awq, (void *)ctx->d_model_fx, (void *)ctx->d_acsf,
@@ -484,7 +498,10 @@ extern "C" int bbgpu_set_option(bbgpu_ctx *ctx, int opt, int value) {
     switch (opt) {
         case 1: ctx->keep_smoothed = value != 0; break;
         case 2: ctx->timing = value != 0; break;
-        case 3: ctx->share_maps = value != 0; break;
+        case 3:
+            ctx->share = value != 0;
+            ctx->mc_dirty = true;
+            break;
         default: return fail(ctx, BBGPU_ERR_ARG, "unknown option %d", opt);
     }
     return BBGPU_OK;
@@ -865,6 +882,7 @@ static int batch_prepare(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const
         ctx->lean = g.fast_ok && g.nlines == 1 && maxnv <= 128;
     }
     ctx->ntile_total = toff;
+    ctx->mc_dirty = true;
     ctx->mstride = (long long)g.nx * g.ny * g.nz;
     ctx->npart = conv_resid_npart(ctx->mem_host.data(), nb, g.nz);
     size_t ncl = (size_t)nb * (E->host.ncloud ? E->host.ncloud : 1);
@@ -946,6 +964,78 @@ static int profile_run(bbgpu_ctx *ctx, bool tm) {
     return 0;
 }
 
+// The (member, cloud) segments of an MC batch. A member k > 0 whose model is member 0's but for a few sub-rings
+// (the columns that differ from member 0's), with member 0's box and fixed-point exponent (the host's, or with a
+// flux normalisation member 0's profile: the same densities), is computed as member 0's fixed-point sums plus
+// the deposits of those sub-rings' clouds with its constants, minus the same clouds with member 0's (exact: the
+// sums are modulo 2^64 and equal clouds deposit equal integers). The deposit of such a member reads member 0's
+// sums, so it runs in a second launch. Every other member deposits all its clouds.
+static int mc_segments(bbgpu_ctx *ctx) {
+    const int nb = ctx->nb, nsub = ctx->nsub;
+    const LayoutHost &L = ctx->cur->host;
+    const long long ncl = L.ncloud;
+    std::vector<long long> &cs = ctx->h_cstart;
+    std::vector<int> &sg = ctx->h_cseg, &kl = ctx->h_klist;
+    cs.clear();
+    sg.clear();
+    kl.clear();
+    long long tot = 0;
+    auto seg = [&](int k, int src, int c0, int sign, long long n) {
+        if (n <= 0) return;
+        cs.push_back(tot);
+        sg.insert(sg.end(), {k, src, c0, sign});
+        tot += n;
+    };
+    const bool can = ctx->share && nb > 1 && mc_deposit_shares(ctx->lean, ctx->want64, ctx->tx, ctx->ty) &&
+                     (!ctx->prof_uploaded || (int)ctx->prof_of_host.size() == nb);
+    const MemberDev &M0 = ctx->mem_host[0];
+    std::vector<int> dl;
+    for (int k = 0; k < nb; k++) {
+        if (can && k > 0) {
+            const MemberDev &M = ctx->mem_host[k];
+            bool ok = M.blo0 == M0.blo0 && M.blo1 == M0.blo1 && M.bx == M0.bx && M.by == M0.by;
+            if (ok) ok = ctx->prof_uploaded ? ctx->prof_of_host[k] == 0 : M.fix_exp == M0.fix_exp;
+            if (ok) {
+                const signed char *ru = ctx->h_reuse + (size_t)k * nsub;
+                long long nch = 0;
+                for (int ir = 0; ir < nsub; ir++)
+                    if (!ru[ir]) nch += L.nc[ir];
+                if (2 * nch < ncl) {
+                    for (int ir = 0; ir < nsub; ir++)
+                        if (!ru[ir]) {
+                            seg(k, k, L.cloud_base[ir], 1, L.nc[ir]);
+                            seg(k, 0, L.cloud_base[ir], -1, L.nc[ir]);
+                        }
+                    dl.push_back(k);
+                    continue;
+                }
+            }
+        }
+        seg(k, k, 0, 1, ncl);
+        kl.push_back(k);
+    }
+    ctx->mc_n1 = (int)kl.size();
+    ctx->mc_n2 = (int)dl.size();
+    kl.insert(kl.end(), dl.begin(), dl.end());
+    cs.push_back(tot);
+    ctx->mc_nseg = (int)cs.size() - 1;
+    ctx->mc_ntot = tot;
+    int rc;
+    if ((rc = dgrow(ctx, &ctx->d_cstart, &ctx->d_cstart_cap, cs.size()))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_cseg, &ctx->d_cseg_cap, sg.size() + 4))) return rc;
+    if ((rc = dgrow(ctx, &ctx->d_klist, &ctx->d_klist_cap, kl.size()))) return rc;
+    if (ctx->mc_n2 &&
+        (rc = dgrow(ctx, &ctx->d_base64, &ctx->d_base64_cap, (size_t)M0.bx * M0.by * ctx->g.nz + 1)))
+        return rc;
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(ctx->d_cstart, cs.data(), sizeof(long long) * cs.size(), cudaMemcpyHostToDevice, s));
+    if (!sg.empty()) CK(cudaMemcpyAsync(ctx->d_cseg, sg.data(), sizeof(int) * sg.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->d_klist, kl.data(), sizeof(int) * kl.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));     // (the host vectors change with the next batch)
+    ctx->mc_dirty = false;
+    return 0;
+}
+
 static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
     if (!ctx->uploaded) return fail(ctx, BBGPU_ERR_STATE, "run before upload");
     const GridDev &g = ctx->g;
@@ -977,22 +1067,38 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
         if (tm) CK(cudaEventRecord(ctx->ev[9], s));
     } else {
         const LayoutDev &L = ctx->cur->dev;
+        if (ctx->mc_dirty) {
+            int rc = mc_segments(ctx);
+            if (rc) return rc;
+        }
         CK(cudaMemsetAsync(ctx->d_tcount, 0, sizeof(int) * (size_t)(ctx->ntile_total * NOWN + 1), s));
-        launch_mc_bin(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->nb, ctx->tx, ctx->ty, ctx->d_pix,
-                      ctx->d_tcount, ctx->d_err);
+        launch_mc_bin(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->d_cstart, ctx->d_cseg, ctx->mc_nseg,
+                      ctx->mc_ntot, ctx->tx, ctx->ty, ctx->d_pix, ctx->d_tcount, ctx->d_err);
         CKL();
         if (tm) CK(cudaEventRecord(ctx->ev[5], s));
         launch_scan_tiles(s, ctx->d_tcount, ctx->d_toff, ctx->d_tcur, ctx->ntile_total * NOWN, ctx->d_scan);
         CKL();
         if (tm) CK(cudaEventRecord(ctx->ev[6], s));
-        launch_mc_scatter(s, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->nb, ctx->tx, ctx->ty, ctx->d_pix, ctx->d_tcur,
-                          ctx->d_bucket);
+        launch_mc_scatter(s, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->d_cstart, ctx->d_cseg, ctx->mc_nseg,
+                          ctx->mc_ntot, ctx->tx, ctx->ty, ctx->d_pix, ctx->d_tcur, ctx->d_bucket);
         CKL();
         if (tm) CK(cudaEventRecord(ctx->ev[7], s));
-        launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->tx, ctx->ty,
-                          ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig, ctx->d_cd2if, ctx->d_cd2i,
-                          ctx->d_model, ctx->mstride, ctx->want64 ? ctx->d_model64 : nullptr, ctx->d_err, ctx->lean);
-        CKL();
+        if (ctx->mc_n2) {
+            for (int pass = 0; pass < 2; pass++) {
+                launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->tx,
+                                  ctx->ty, ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig, ctx->d_cd2if,
+                                  ctx->d_cd2i, ctx->d_model, ctx->mstride, nullptr, ctx->d_err, ctx->lean,
+                                  ctx->d_klist + (pass ? ctx->mc_n1 : 0), pass ? ctx->mc_n2 : ctx->mc_n1, pass,
+                                  ctx->d_base64);
+                CKL();
+            }
+        } else {
+            launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->tx,
+                              ctx->ty, ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig, ctx->d_cd2if,
+                              ctx->d_cd2i, ctx->d_model, ctx->mstride, ctx->want64 ? ctx->d_model64 : nullptr,
+                              ctx->d_err, ctx->lean);
+            CKL();
+        }
         if (tm) {
             CK(cudaEventRecord(ctx->ev[8], s));
             CK(cudaEventRecord(ctx->ev[9], s));
@@ -1029,6 +1135,10 @@ static int check_err(bbgpu_ctx *ctx) {
     if (*ctx->h_err) {
         int e = *ctx->h_err;
         CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+        if (e & ERR_SHARE)
+            return fail(ctx, BBGPU_ERR_KERNEL,
+                        "a member computed as a difference from member 0's model has another fixed-point exponent "
+                        "(disable option 3 for this batch)");
         if (e & ERR_PROFILE_LAYOUT)
             return fail(ctx, BBGPU_ERR_KERNEL,
                         "the deconvolved density profile changed the MC cloud layout of a member (a ring density "
@@ -1683,7 +1793,7 @@ extern "C" int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *
         std::vector<int> ch;
         for (int k = 0; k < nb; k++) {
             bool delta = false;
-            if (ctx->share_maps && k > 0 && fix[k] == fix[0]) {
+            if (ctx->share && k > 0 && fix[k] == fix[0]) {
                 const double *sk = sr_maps + (size_t)k * BBGPU_NSR * nsm;
                 long long nch = 0;
                 ch.clear();
@@ -1716,6 +1826,8 @@ extern "C" int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *
     }
     ctx->nu = (int)uidx.size();
     ctx->nseg = (int)mstart.size() - 1;
+    ctx->prof_of_host = prof_of;
+    ctx->mc_dirty = true;
     // the vertical grids: the new ones appended on the device (the table grows with a copy of the old part)
     const size_t nz1 = zc.zq.size() + 1;
     if (zc.uploaded == 0 || nz1 > ctx->d_pzq_cap) {

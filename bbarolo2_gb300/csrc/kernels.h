@@ -51,22 +51,34 @@ struct ZigDev {
 // + (lp % 8) * 8 + lp / 8 for pixel lp of the tile, so that the lists of the pixels lp = w (mod 8), owned by
 // warp w of the deposit, are contiguous.
 #define NOWN 64
+// The (member, cloud) pairs of a batch by segments of threads: segment i (threads cstart[i] .. cstart[i + 1]) is
+// cseg[4i .. 4i + 4) = (member whose tiles take the clouds, member whose constants place them, first cloud, sign
+// of the deposits); ntot = cstart[nseg]. A member's own clouds are one segment (k, k, 0, +1) of ncloud threads.
 void launch_mc_bin(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
-                   const MemberDev *mem, int nb, int tx, int ty, int *pix, int *tile_count, int *err);
+                   const MemberDev *mem, const long long *cstart, const int *cseg, int nseg, long long ntot, int tx,
+                   int ty, int *pix, int *tile_count, int *err);
 // Exclusive scan of n list counts into offsets (and cursors); scratch holds (n + 1023) / 1024 ints.
 void launch_scan_tiles(cudaStream_t s, const int *count, int *offset, int *cursor, int n, int *scratch);
 // bucket: 32-byte entries (Entry in mc.cu), one per in-box (member, cloud)
 #define ENTRY_BYTES 32
-void launch_mc_scatter(cudaStream_t s, const LayoutDev &L, const SubMC *sub, int nsub, const MemberDev *mem, int nb,
-                       int tx, int ty, const int *pix, int *cursor, void *bucket);
+void launch_mc_scatter(cudaStream_t s, const LayoutDev &L, const SubMC *sub, int nsub, const MemberDev *mem,
+                       const long long *cstart, const int *cseg, int nseg, long long ntot, int tx, int ty,
+                       const int *pix, int *cursor, void *bucket);
 // Deposits the clouds of every tile into a shared-memory fixed-point tile and writes the model
 // (by, bx, nz) float32 of each member at model + k * mstride (and, if model64, float64 sums); lean: the batch
 // qualifies for the fast kernels (one line, a linear channel map, at most 128 samples per cloud).
+// klist (nk members; nullptr: every member) selects the members of the launch. With base64 (the pixel-owned
+// kernel only, see mc_deposit_shares): delta = 0 leaves member 0's fixed-point sums in base64 (its box);
+// delta = 1 adds them to the members' lists, which hold the difference from member 0's model (same box and
+// exponent; ERR_SHARE otherwise).
+#define ERR_SHARE 8
+bool mc_deposit_shares(int lean, bool model64, int tx, int ty);
 void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
                        const MemberDev *mem, const MemberDev *mem_host, int nb, int tx, int ty,
                        const int *offset, const int *count, const void *bucket, const ZigDev *zig,
                        const float *cd2if, const double *cd2i, float *model, long long mstride, double *model64,
-                       int *err, int lean);
+                       int *err, int lean, const int *klist = nullptr, int nk = 0, int delta = 0,
+                       long long *base64 = nullptr);
 
 // ---- convolution + residual (conv.cu)
 // The taps of a beam kernel (ky, kx) as the conv kernels read them: flipped, float32, rows padded to the

@@ -110,15 +110,35 @@ __device__ __forceinline__ void warp_lists(const int *__restrict__ offset, const
     for (int j = 0; j < 8; j++) n += count[lbase + 8 * warp + j];
 }
 
+// The (member, cloud) of thread idx of the bin and scatter kernels: segment i (threads cstart[i] ..
+// cstart[i + 1]) is cseg[i] = (member whose tiles take the clouds, member whose constants place them, first
+// cloud, sign of the deposits): a member's own clouds, or, for a member that differs from member 0 in a few
+// sub-rings, the clouds of those sub-rings with its constants (+) and with member 0's (-).
+struct CloudSeg {
+    int k, src, c, sign;
+};
+__device__ __forceinline__ CloudSeg cloud_of(const long long *__restrict__ cstart, const int4 *__restrict__ cseg,
+                                             int nseg, long long idx) {
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (cstart[mid] <= idx) lo = mid;
+        else hi = mid - 1;
+    }
+    const int4 sg = cseg[lo];
+    return CloudSeg{sg.x, sg.y, sg.z + (int)(idx - cstart[lo]), sg.w};
+}
+
 __global__ void k_mc_bin(GridDev g, LayoutDev L, const SubMC *__restrict__ sub, int nsub,
-                         const MemberDev *__restrict__ mem, int nb, int tx, int ty, int *__restrict__ pix,
-                         int *__restrict__ tile_count, int *err) {
+                         const MemberDev *__restrict__ mem, const long long *__restrict__ cstart,
+                         const int4 *__restrict__ cseg, int nseg, long long ntot, int tx, int ty,
+                         int *__restrict__ pix, int *__restrict__ tile_count, int *err) {
     long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long long)nb * L.ncloud) return;
-    int k = (int)(idx / L.ncloud);
-    int c = (int)(idx - (long long)k * L.ncloud);
+    if (idx >= ntot) return;
+    const CloudSeg cl = cloud_of(cstart, cseg, nseg, idx);
+    const int k = cl.k, c = cl.c;
     int ir = L.sub[c];
-    const SubMC &S = sub[(size_t)k * nsub + ir];
+    const SubMC &S = sub[(size_t)cl.src * nsub + ir];
     const MemberDev &M = mem[k];
     if (!S.active || c - L.cloud_base[ir] >= S.nc) {
         atomicOr(err, ERR_LAYOUT);
@@ -142,7 +162,7 @@ __global__ void k_mc_bin(GridDev g, LayoutDev L, const SubMC *__restrict__ sub, 
 struct __align__(16) Entry {
     int c;          // cloud
     int pb;         // first of the cloud's sorted normals (padded layout)
-    int meta;       // nv | pixel in the tile << 16 | half << 24
+    int meta;       // nv | pixel in the tile << 16 | half << 24 | (placed with member 0's constants) << 25
     float tc;       // channel of the cloud's velocity (line 0, float32 with the bound epsc)
     long long fix;  // fixed-point flux of one sample (line 0)
     float eps;      // rounding bound of the float32 channel of every sample of the cloud (line 0)
@@ -165,14 +185,15 @@ __device__ __forceinline__ void cloud_centre(const SubMC &S, float4 cf, int nl, 
 }
 
 __global__ void k_mc_scatter(LayoutDev L, const SubMC *__restrict__ sub, int nsub, const MemberDev *__restrict__ mem,
-                             int nb, int tx, int ty, const int *__restrict__ pix, int *__restrict__ cursor,
+                             const long long *__restrict__ cstart, const int4 *__restrict__ cseg, int nseg,
+                             long long ntot, int tx, int ty, const int *__restrict__ pix, int *__restrict__ cursor,
                              Entry *__restrict__ bucket) {
     long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long long)nb * L.ncloud) return;
+    if (idx >= ntot) return;
     int p = pix[idx];
     if (p < 0) return;
-    int k = (int)(idx / L.ncloud);
-    int c = (int)(idx - (long long)k * L.ncloud);
+    const CloudSeg cl = cloud_of(cstart, cseg, nseg, idx);
+    const int k = cl.k, c = cl.c;
     const MemberDev &M = mem[k];
     int py = p / M.bx, px = p - py * M.bx;
     const int lp = (py % ty) * tx + (px % tx);
@@ -181,14 +202,14 @@ __global__ void k_mc_scatter(LayoutDev L, const SubMC *__restrict__ sub, int nsu
     const int half = cf.y >= 0.0f ? 0 : 1;
     const int ir = L.sub[c];
     const int nv = L.nvs[ir];
-    const SubMC &S = sub[(size_t)k * nsub + ir];
+    const SubMC &S = sub[(size_t)cl.src * nsub + ir];
     Entry e;
     e.c = c;
     e.pb = (int)(L.pbase[ir] + (long long)(c - L.cloud_base[ir]) * ((nv + 3) & ~3));
-    e.meta = (nv & 0xffff) | (lp << 16) | (half << 24);
+    e.meta = (nv & 0xffff) | (lp << 16) | (half << 24) | (cl.src != k ? 1 << 25 : 0);
     float epsc;
     cloud_centre(S, cf, 0, e.tc, epsc);
-    e.fix = S.fix[half][0];
+    e.fix = cl.sign < 0 ? -S.fix[half][0] : S.fix[half][0];
     e.sg = S.sg[0];
     // the cloud's largest |normal| is at an end of its sorted run
     const float nmax = fmaxf(fabsf(__ldg(&L.nf[e.pb])), fabsf(__ldg(&L.nf[e.pb + nv - 1])));
@@ -483,7 +504,7 @@ __global__ void __launch_bounds__(256) k_mc_deposit(GridDev g, LayoutDev L, cons
         const Entry en = ents[warp][i % DEPTH];
         const float *w = slots + (i % DEPTH) * WB;
         const int c = en.c;
-        const int nv = en.meta & 0xffff, lp = (en.meta >> 16) & 255, half = en.meta >> 24;
+        const int nv = en.meta & 0xffff, lp = (en.meta >> 16) & 255, half = (en.meta >> 24) & 1;
         unsigned long long *row = tile + (size_t)lp * nz;
         const float tc = en.tc, sg = en.sg;
         const long long fix = en.fix;
@@ -708,7 +729,7 @@ __global__ void __launch_bounds__(256, LEAN_MINB) k_mc_deposit_lean(GridDev g, L
 
 // A cloud of the pixel-owned deposit (nv = 0: none).
 struct PxCloud {
-    int c, pb, nv;
+    int c, pb, nv, src0;        // src0: placed with member 0's constants (a difference from member 0's model)
     float tc, sg, eps;
     long long fix;
 };
@@ -719,12 +740,13 @@ __device__ __forceinline__ void px_entry(const Entry *__restrict__ bucket, int b
         p.c = en.c;
         p.pb = en.pb;
         p.nv = en.meta & 0xffff;
+        p.src0 = (en.meta >> 25) & 1;
         p.tc = en.tc;
         p.sg = en.sg;
         p.eps = en.eps;
         p.fix = en.fix;
     } else {
-        p.c = 0; p.pb = 0; p.nv = 0; p.tc = 0.0f; p.sg = 0.0f; p.eps = 0.0f; p.fix = 0;
+        p.c = 0; p.pb = 0; p.nv = 0; p.src0 = 0; p.tc = 0.0f; p.sg = 0.0f; p.eps = 0.0f; p.fix = 0;
     }
 }
 
@@ -775,22 +797,22 @@ struct __align__(16) PxDefer {
     int c, pb, nv, i;       // cloud, its sorted normals, their count, the sample
     long long fix;          // fixed-point flux of the sample
     int row;                // its row in the tile (offset in sums)
-    int pad;
+    int src0;               // the cloud is placed with member 0's constants
 };
 #define PX_QCAP 64          // deferred samples per warp (at most 32 join per cloud step)
 
 // The deferred samples of the warp: their exact channels (a lane each) added to the rows with shared-memory
 // atomics (two samples may share a channel); the queue is emptied.
 __device__ __forceinline__ void px_flush(const GridDev &g, const LayoutDev &L, const ZigDev *zig,
-                                         const SubMC *__restrict__ subk, PxDefer *qe, int *qn,
-                                         unsigned long long *tile, int lane, int *err) {
+                                         const SubMC *__restrict__ subk, const SubMC *__restrict__ sub0, PxDefer *qe,
+                                         int *qn, unsigned long long *tile, int lane, int *err) {
     __syncwarp();
     const int nq = *qn;
     for (int b = 0; b < nq; b += 32) {
         const int e = b + lane;
         if (e < nq) {
             const PxDefer x = qe[e];
-            const int ch = px_exact(g, L, zig, subk, x.c, x.pb, x.nv, x.i, err);
+            const int ch = px_exact(g, L, zig, x.src0 ? sub0 : subk, x.c, x.pb, x.nv, x.i, err);
             if ((unsigned)ch < (unsigned)g.nz) atomicAdd(tile + x.row + ch, (unsigned long long)x.fix);
         }
     }
@@ -809,7 +831,8 @@ __device__ __forceinline__ void px_flush(const GridDev &g, const LayoutDev &L, c
 // lanes have merged equal ones; the other bins at once.
 template <int SPL>
 __device__ __forceinline__ void px_count(const GridDev &g, const LayoutDev &L, const ZigDev *zig,
-                                         const SubMC *__restrict__ subk, const PxCloud &p, const float4 (&w)[SPL / 4],
+                                         const SubMC *__restrict__ subk, const SubMC *__restrict__ sub0,
+                                         const PxCloud &p, const float4 (&w)[SPL / 4],
                                          int i0, int q, unsigned long long *tile, int rowoff, PxDefer *qe, int *qn,
                                          const unsigned long long *inc, int *err) {
     constexpr int LPP = 128 / SPL;
@@ -851,7 +874,7 @@ __device__ __forceinline__ void px_count(const GridDev &g, const LayoutDev &L, c
     if (__popc(need) <= 1 && (H >> 55) == 0) {
         if (need) {
             const int slot = atomicAdd(qn, 1);
-            qe[slot] = PxDefer{p.c, p.pb, p.nv, i0 + __ffs(need) - 1, fix, rowoff, 0};
+            qe[slot] = PxDefer{p.c, p.pb, p.nv, i0 + __ffs(need) - 1, fix, rowoff, p.src0};
         }
         if (H) {
             const int c0 = (int)fl0;
@@ -875,7 +898,8 @@ __device__ __forceinline__ void px_count(const GridDev &g, const LayoutDev &L, c
             const float f = fmaf(__ldg(&L.nf[(unsigned)p.pb + i0 + i]), sg, tc) + 0.5f;
             const float fl = floorf(f);
             int c = (int)fl;
-            if (!(fastc && fabsf(f - fl - 0.5f) <= hw)) c = px_exact(g, L, zig, subk, p.c, p.pb, p.nv, i0 + i, err);
+            if (!(fastc && fabsf(f - fl - 0.5f) <= hw))
+                c = px_exact(g, L, zig, p.src0 ? sub0 : subk, p.c, p.pb, p.nv, i0 + i, err);
             r.take(c, fix, nz, row);
         }
         // the open run: the lane's first run if it is the only one, else its last (a channel no other lane adds)
@@ -928,12 +952,17 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
                                                               const ZigDev *__restrict__ zig,
                                                               const float *__restrict__ cd2if,
                                                               float *__restrict__ model, long long mstride,
-                                                              int *err) {
+                                                              const int *__restrict__ klist, int delta,
+                                                              unsigned long long *__restrict__ base64, int *err) {
     constexpr int LPP = 128 / SPL;
     extern __shared__ unsigned long long tile[];           // TP rows of fixed-point sums, queues, nz scales
     __shared__ unsigned long long inc[32];                 // the histogram increments of px_count
-    const int k = blockIdx.x;
+    const int k = klist ? klist[blockIdx.x] : blockIdx.x;
     const int t = blockIdx.y;
+    // delta: the member's lists hold the difference from member 0's model (same box and exponent), whose sums
+    // are in base64; else member 0 (with base64) leaves its sums there
+    unsigned long long *wbase = !delta && k == 0 ? base64 : nullptr;
+    if (delta && threadIdx.x == 0 && blockIdx.y == 0 && mem[k].fix_exp != mem[0].fix_exp) atomicOr(err, ERR_SHARE);
     const int ntx = mem[k].ntx;
     if (t >= ntx * mem[k].nty) return;
     if (threadIdx.x < 32) inc[threadIdx.x] = threadIdx.x < 11 ? 1ull << (5 * threadIdx.x) : (threadIdx.x < 31 ? 1ull << 55 : 0ull);
@@ -953,8 +982,15 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
             for (int lp = warp; lp < TP; lp += 8) {
                 const int py = y0 + lp / tx, px = x0 + lp % tx;
                 if (py >= by || px >= bx) continue;
-                float *o = mout + ((size_t)py * bx + px) * nz;
-                for (int z = lane; z < nz; z += 32) o[z] = 0.0f;
+                const size_t v0 = ((size_t)py * bx + px) * nz;
+                float *o = mout + v0;
+                if (delta) {
+                    for (int z = lane; z < nz; z += 32) o[z] = model[v0 + z];   // (member 0's: same units)
+                } else {
+                    for (int z = lane; z < nz; z += 32) o[z] = 0.0f;
+                    if (wbase)
+                        for (int z = lane; z < nz; z += 32) wbase[v0 + z] = 0ULL;
+                }
             }
             return;
         }
@@ -992,23 +1028,30 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
         px_samples<SPL>(L, cb, i0, wb);
         PxCloud cn;
         px_entry(bucket, beg, n, j + 2, cn);
-        px_count<SPL>(g, L, zig, subk, ca, wa, i0, q, tile, rowoff, qe, qn, inc, err);
+        px_count<SPL>(g, L, zig, subk, sub, ca, wa, i0, q, tile, rowoff, qe, qn, inc, err);
         __syncwarp();
-        if (*qn > PX_QCAP - 32) px_flush(g, L, zig, subk, qe, qn, tile, lane, err);
+        if (*qn > PX_QCAP - 32) px_flush(g, L, zig, subk, sub, qe, qn, tile, lane, err);
         ca = cb;
         cb = cn;
 #pragma unroll
         for (int s = 0; s < SPL / 4; s++) wa[s] = wb[s];
     }
     __syncwarp();
-    if (*qn) px_flush(g, L, zig, subk, qe, qn, tile, lane, err);
+    if (*qn) px_flush(g, L, zig, subk, sub, qe, qn, tile, lane, err);
     __syncthreads();
     for (int p = warp; p < TP; p += 8) {
         const int py = y0 + p / tx, px = x0 + p % tx;
         if (py >= by || px >= bx) continue;
         const unsigned long long *src = tile + (size_t)p * RS + 2 * (p >> 3);
-        float *o = mout + ((size_t)py * bx + px) * nz;
-        for (int z = lane; z < nz; z += 32) o[z] = ll_to_f32((long long)src[z]) * chs[z];
+        const size_t v0 = ((size_t)py * bx + px) * nz;
+        float *o = mout + v0;
+        if (delta) {
+            for (int z = lane; z < nz; z += 32) o[z] = ll_to_f32((long long)(src[z] + base64[v0 + z])) * chs[z];
+        } else {
+            for (int z = lane; z < nz; z += 32) o[z] = ll_to_f32((long long)src[z]) * chs[z];
+            if (wbase)
+                for (int z = lane; z < nz; z += 32) wbase[v0 + z] = src[z];
+        }
     }
 }
 
@@ -1115,10 +1158,11 @@ __global__ void k_scan_c(const int *__restrict__ count, int n, const int *__rest
 }  // namespace
 
 void launch_mc_bin(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
-                   const MemberDev *mem, int nb, int tx, int ty, int *pix, int *tile_count, int *err) {
-    long long n = (long long)nb * L.ncloud;
-    if (n == 0) return;
-    k_mc_bin<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g, L, sub, nsub, mem, nb, tx, ty, pix, tile_count, err);
+                   const MemberDev *mem, const long long *cstart, const int *cseg, int nseg, long long ntot, int tx,
+                   int ty, int *pix, int *tile_count, int *err) {
+    if (ntot == 0 || nseg == 0) return;
+    k_mc_bin<<<(unsigned)((ntot + 255) / 256), 256, 0, s>>>(g, L, sub, nsub, mem, cstart, (const int4 *)cseg, nseg,
+                                                            ntot, tx, ty, pix, tile_count, err);
 }
 
 void launch_scan_tiles(cudaStream_t s, const int *count, int *offset, int *cursor, int n, int *scratch) {
@@ -1129,22 +1173,26 @@ void launch_scan_tiles(cudaStream_t s, const int *count, int *offset, int *curso
     k_scan_c<<<nb, 1024, 0, s>>>(count, n, scratch, offset, cursor);
 }
 
-void launch_mc_scatter(cudaStream_t s, const LayoutDev &L, const SubMC *sub, int nsub, const MemberDev *mem, int nb,
-                       int tx, int ty, const int *pix, int *cursor, void *bucket) {
-    long long n = (long long)nb * L.ncloud;
-    if (n == 0) return;
-    k_mc_scatter<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(L, sub, nsub, mem, nb, tx, ty, pix, cursor,
-                                                             (Entry *)bucket);
+void launch_mc_scatter(cudaStream_t s, const LayoutDev &L, const SubMC *sub, int nsub, const MemberDev *mem,
+                       const long long *cstart, const int *cseg, int nseg, long long ntot, int tx, int ty,
+                       const int *pix, int *cursor, void *bucket) {
+    if (ntot == 0 || nseg == 0) return;
+    k_mc_scatter<<<(unsigned)((ntot + 255) / 256), 256, 0, s>>>(L, sub, nsub, mem, cstart, (const int4 *)cseg, nseg,
+                                                                ntot, tx, ty, pix, cursor, (Entry *)bucket);
+}
+
+bool mc_deposit_shares(int lean, bool model64, int tx, int ty) {
+    return lean && !model64 && (tx * ty == 64 || tx * ty == 32);
 }
 
 void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
                        const MemberDev *mem, const MemberDev *mem_host, int nb, int tx, int ty,
                        const int *offset, const int *count, const void *bucket, const ZigDev *zig,
                        const float *cd2if, const double *cd2i, float *model, long long mstride, double *model64,
-                       int *err, int lean) {
+                       int *err, int lean, const int *klist, int nk, int delta, long long *base64) {
     int maxt = 0;
     for (int k = 0; k < nb; k++) maxt = max(maxt, mem_host[k].ntx * mem_host[k].nty);
-    if (maxt == 0 || nb == 0) return;
+    if (maxt == 0 || nb == 0 || (klist && nk == 0)) return;
     size_t smem = (size_t)tx * ty * g.nz * sizeof(unsigned long long) + 16 + (size_t)8 * DEPTH * WB * sizeof(float) +
                   (size_t)g.nz * sizeof(float);
     static size_t configured = 0;
@@ -1152,7 +1200,7 @@ void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, con
         cudaFuncSetAttribute(k_mc_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         configured = smem;
     }
-    dim3 grid(nb, maxt);
+    dim3 grid(klist ? nk : nb, maxt);
     if (lean && !model64) {
         static size_t cfg_lean = 0;
         if (smem > 48 * 1024 && smem > cfg_lean) {
@@ -1174,12 +1222,15 @@ void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, con
                     cudaFuncSetAttribute(k_mc_deposit_px<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_px);
                 cfg = smem_px;
             }
+            unsigned long long *b64 = (unsigned long long *)base64;
             if (TP == 64)
                 k_mc_deposit_px<32><<<grid, 256, smem_px, s>>>(g, L, sub, nsub, mem, tx, ty, offset, count,
-                                                               (const Entry *)bucket, zig, cd2if, model, mstride, err);
+                                                               (const Entry *)bucket, zig, cd2if, model, mstride,
+                                                               klist, delta, b64, err);
             else
                 k_mc_deposit_px<16><<<grid, 256, smem_px, s>>>(g, L, sub, nsub, mem, tx, ty, offset, count,
-                                                               (const Entry *)bucket, zig, cd2if, model, mstride, err);
+                                                               (const Entry *)bucket, zig, cd2if, model, mstride,
+                                                               klist, delta, b64, err);
             return;
         }
         k_mc_deposit_lean<<<grid, 256, smem, s>>>(g, L, sub, nsub, mem, tx, ty, offset, count, (const Entry *)bucket,

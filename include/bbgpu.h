@@ -155,8 +155,9 @@ int bbgpu_eval_model(bbgpu_ctx *ctx, int k, int smoothed, float *out, int by, in
 /* Synchronise the context's stream. */
 int bbgpu_sync(bbgpu_ctx *ctx);
 /* Options: 1 keep the smoothed models of a batch (for bbgpu_eval_model), 2 time the kernels of each run,
- * 3 share the flux normalisation between members whose ring maps are the first member's up to a few sub-rings
- * (default 1; the results are the same bit for bit, 0 computes every member's maps from all its samples). */
+ * 3 compute the members of a batch that differ from the first member in a few sub-rings (the steps of a
+ * finite-difference gradient) as the first member's ring maps, profile and MC model plus the difference (default
+ * 1; the results are the same bit for bit, 0 computes every member from all its samples and clouds). */
 int bbgpu_set_option(bbgpu_ctx *ctx, int option, int value);
 
 /* ---- without allocation ------------------------------------------------------------------------------- */

@@ -156,3 +156,52 @@ def test_batch_path_line_widths_and_axis(gpu_lib, oracle_lib, variant):
         cube = Cube.empty(64, 64, 64, [-10. / 3600., 10. / 3600., -5.], beam=30. / 3600., par=par,
                           crpix=[33., 33., 33.], crval=[60., 0., 1000.], cunit=("deg", "deg", "km/s"))
     _batch_vs_oracle(oracle_lib, cube, rings)
+
+
+@pytest.mark.parametrize("wl", ["classic64", "global160"])
+def test_batch_path_gradient_members_shared(gpu_lib, oracle_lib, wl):
+    """A finite-difference batch (one ring's VROT, VDISP, INC or PA stepped per member): the members that differ
+    from member 0 in a few sub-rings are computed as member 0's model plus the difference of those sub-rings'
+    clouds; their unsmoothed models are, bit for bit, those of the full computation (option 3 off), and agree
+    with the oracle's."""
+    from bbarolo2_gb300 import _lib, configs, engine
+    from bbarolo2_gb300.galmod import ring_rows_batch
+    cube, rings = configs.WORKLOADS[wl](galmodtype="MC")
+    dm = engine.DiskModel(cube)
+    st = dm.setup
+    L = engine.BatchLikelihood(dm, np.ones(cube.array.shape, np.float32), None, maskmode=0, sigma=1.0)
+    base = ring_rows_batch([rings])[0]
+    rows = [base]
+    for j in sorted({0, rings.nr // 3, rings.nr - 1}):
+        for row, step in ((4, 5.0), (5, 1.0), (12, 2.0), (13, 3.0)):
+            r = base.copy()
+            r[row, j] += step
+            rows.append(r)
+    rows = np.stack(rows)
+    sr, nv, descs, boxes = L.prepare(rows, rings, seed=2)
+    models = {}
+    for share in (0, 1):
+        dm.ctx.set_option(_lib.OPT_SHARE_MAPS, share)
+        ss, _ = L.run(sr, nv, descs)
+        ms = []
+        for k in range(len(rows)):
+            (blo, bhi) = boxes[k]
+            got = np.zeros((bhi[1] - blo[1], bhi[0] - blo[0], st.nsubs), np.float32)
+            dm.ctx.check(dm.ctx.L.bbgpu_eval_model(dm.ctx.h, k, 0, _lib.ptr(got), got.shape[0], got.shape[1],
+                                                   st.nsubs))
+            ms.append(got)
+        models[share] = (ss, ms)
+    dm.ctx.set_option(_lib.OPT_SHARE_MAPS, 1)
+    np.testing.assert_array_equal(models[0][0], models[1][0])
+    for k in range(len(rows)):
+        np.testing.assert_array_equal(models[0][1][k], models[1][1][k], err_msg=str(k))
+    for k in (1, 3, 5, len(rows) - 1):
+        (blo, bhi) = boxes[k]
+        got = models[1][1][k]
+        ref = np.zeros(got.shape)
+        oracle_lib.galmod_mc(ref, sr[k], 0, sr.shape[2], 2, st.radsep, nv[k], st.cdens, st.cmode, st.pixarea,
+                             st.cdelt[0], st.cdelt[1], st.crota2, blo[0], blo[1], bhi[0], bhi[1], st.ltype,
+                             st.sig_instr, st.axtyp, st.velsys, st.lfreq0, st.crval3, st.cdelt3, st.crpix3, st.relint,
+                             st.cd2i)
+        assert np.array_equal(got != 0, ref != 0), k
+        np.testing.assert_allclose(got, ref, rtol=1e-6, atol=0)
