@@ -22,8 +22,8 @@ SYMBOLS = ("bbgpu_ctx_create", "bbgpu_ctx_destroy", "bbgpu_last_error", "bbgpu_v
            "bbgpu_ring_maps_analytic", "bbgpu_convolve", "bbgpu_conv_sparse", "bbgpu_sumsq_residuals",
            "bbgpu_residuals_fracerr", "bbgpu_norm", "bbgpu_eval_upload", "bbgpu_eval_run", "bbgpu_eval_download",
            "bbgpu_eval_batch", "bbgpu_eval_model", "bbgpu_sync", "bbgpu_set_option", "bbgpu_launch_count",
-           "bbgpu_last_run_times", "bbgpu_kernel_name", "bbgpu_transfer_bytes", "bbgpu_sumsq_residuals_noalloc",
-           "bbgpu_set_profile", "bbgpu_eval_upload_profile", "bbgpu_eval_profile", "bbgpu_solve_profile")
+           "bbgpu_last_run_times", "bbgpu_kernel_name", "bbgpu_transfer_bytes", "bbgpu_shared_members",
+           "bbgpu_sumsq_residuals_noalloc", "bbgpu_set_profile", "bbgpu_eval_upload_profile", "bbgpu_eval_profile", "bbgpu_solve_profile")
 
 
 class Grid(C.Structure):
@@ -95,6 +95,7 @@ def load(path=None):
         "bbgpu_last_run_times": (i, [vp, vp, i]),
         "bbgpu_kernel_name": (C.c_char_p, [i]),
         "bbgpu_transfer_bytes": (i, [vp, vp, vp]),
+        "bbgpu_shared_members": (i, [vp, vp, vp, vp]),
         "bbgpu_sumsq_residuals_noalloc": (i, [vp, vp, vp, i, vp, i, i, i, d, d, vp, vp]),
         "bbgpu_set_profile": (i, [vp, i, i, i, i, i, vp, vp, vp, vp, d, d, d, d]),
         "bbgpu_eval_upload_profile": (i, [vp, i, vp, vp, vp]),
@@ -145,6 +146,12 @@ class Context:
     @property
     def launches(self):
         return int(self.L.bbgpu_launch_count(self.h))
+
+    def shared_members(self):
+        """(profiles computed, MC members with all their clouds, MC members as a difference) of the last batch."""
+        a, b, c = (C.c_int(0) for _ in range(3))
+        self.check(self.L.bbgpu_shared_members(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
 
     def run_times(self):
         t = np.zeros(16)

@@ -21,13 +21,14 @@
 
 #define BBGPU_VERSION 1
 #define NLAYOUT 4
-#define NTIMER 11
+#define NTIMER 12
 
 // the timed stages of a batch: the flux normalisation (ring maps, their beam convolution, the normal equations,
 // the solves and the sub-ring densities), then the MC model (or the ANALYTIC one), its convolution and the
-// residual reduction
-static const char *KNAMES[NTIMER] = {"prof_maps", "prof_conv", "prof_gram", "prof_solve", "mc_bin", "scan_tiles",
-                                     "mc_scatter", "mc_deposit", "an_model", "conv_resid", "reduce_partials"};
+// residual reduction (mc_deposit_delta: the members computed as a difference from member 0's model)
+static const char *KNAMES[NTIMER] = {"prof_maps", "prof_conv",  "prof_gram",  "prof_solve",
+                                     "mc_bin",    "scan_tiles", "mc_scatter", "mc_deposit",
+                                     "mc_deposit_delta", "an_model", "conv_resid", "reduce_partials"};
 
 struct LayoutEntry {
     LayoutHost host;
@@ -143,8 +144,9 @@ struct bbgpu_ctx {
     std::vector<long long> h_cstart;
     std::vector<int> h_cseg, h_klist;
     long long *d_cstart = nullptr, *d_base64 = nullptr;
-    int *d_cseg = nullptr, *d_klist = nullptr;
-    size_t d_cstart_cap = 0, d_base64_cap = 0, d_cseg_cap = 0, d_klist_cap = 0;
+    int *d_cseg = nullptr, *d_klist = nullptr, *d_tsrc = nullptr;
+    size_t d_cstart_cap = 0, d_base64_cap = 0, d_cseg_cap = 0, d_klist_cap = 0, d_tsrc_cap = 0;
+    std::vector<signed char> mc_isdelta;   // per member: computed as a difference (tiles shared with member 0)
     ZgridCache zcache;                 // vertical grids of the ring maps (host), mirrored in d_pzq/d_pzqf/d_pwqf
     std::string samp_key;              // the sub-ring radii of the sample table on the device
     AnSub *h_psub = nullptr;           // pinned staging of the sub-ring constants
@@ -447,7 +449,8 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
                     (void *)ctx->d_pwvalf, (void *)ctx->d_maps32, (void *)ctx->d_K, (void *)ctx->d_maps64,
                     (void *)ctx->d_pmem, (void *)ctx->d_mstart, (void *)ctx->d_mseg, (void *)ctx->d_uidx,
                     (void *)ctx->d_ubase, (void *)ctx->d_prof_of, (void *)ctx->d_pstatu, (void *)ctx->d_pxu,
-                    (void *)ctx->d_cstart, (void *)ctx->d_base64, (void *)ctx->d_cseg, (void *)ctx->d_klist})
+                    (void *)ctx->d_cstart, (void *)ctx->d_base64, (void *)ctx->d_cseg, (void *)ctx->d_klist,
+                    (void *)ctx->d_tsrc})
         cudaFree(q);
     for (void *q : {(void *)ctx->d_asub, (void *)ctx->d_asbase, (void *)ctx->d_assub, (void *)ctx->d_acs,
                     (void *)ctx->d_azq, (void *)ctx->d_awq, (void *)ctx->d_model_fx, (void *)ctx->d_acsf,
@@ -485,6 +488,15 @@ extern "C" int bbgpu_last_run_times(const bbgpu_ctx *ctx, double *times, int n) 
 }
 
 extern "C" const char *bbgpu_kernel_name(int i) { return (i >= 0 && i < NTIMER) ? KNAMES[i] : ""; }
+
+extern "C" int bbgpu_shared_members(const bbgpu_ctx *ctx, int *profiles, int *mc_full, int *mc_delta) {
+    if (!ctx) return BBGPU_ERR_ARG;
+    const bool mc = ctx->galmodtype == BBGPU_MC && !ctx->mc_dirty;
+    if (profiles) *profiles = ctx->prof_uploaded ? ctx->nu : 0;
+    if (mc_full) *mc_full = mc ? (ctx->mc_n1) : 0;
+    if (mc_delta) *mc_delta = mc ? ctx->mc_n2 : 0;
+    return BBGPU_OK;
+}
 
 extern "C" int bbgpu_transfer_bytes(const bbgpu_ctx *ctx, int64_t *h2d, int64_t *d2h) {
     if (!ctx) return BBGPU_ERR_ARG;
@@ -970,6 +982,12 @@ static int profile_run(bbgpu_ctx *ctx, bool tm) {
 // the deposits of those sub-rings' clouds with its constants, minus the same clouds with member 0's (exact: the
 // sums are modulo 2^64 and equal clouds deposit equal integers). The deposit of such a member reads member 0's
 // sums, so it runs in a second launch. Every other member deposits all its clouds.
+static int ilog2(int v) {
+    int e = 0;
+    while ((1 << (e + 1)) <= v) e++;
+    return e;
+}
+
 static int mc_segments(bbgpu_ctx *ctx) {
     const int nb = ctx->nb, nsub = ctx->nsub;
     const LayoutHost &L = ctx->cur->host;
@@ -990,6 +1008,7 @@ static int mc_segments(bbgpu_ctx *ctx) {
                      (!ctx->prof_uploaded || (int)ctx->prof_of_host.size() == nb);
     const MemberDev &M0 = ctx->mem_host[0];
     std::vector<int> dl;
+    ctx->mc_isdelta.assign(nb, 0);
     for (int k = 0; k < nb; k++) {
         if (can && k > 0) {
             const MemberDev &M = ctx->mem_host[k];
@@ -1007,6 +1026,7 @@ static int mc_segments(bbgpu_ctx *ctx) {
                             seg(k, 0, L.cloud_base[ir], -1, L.nc[ir]);
                         }
                     dl.push_back(k);
+                    ctx->mc_isdelta[k] = 1;
                     continue;
                 }
             }
@@ -1025,7 +1045,8 @@ static int mc_segments(bbgpu_ctx *ctx) {
     if ((rc = dgrow(ctx, &ctx->d_cseg, &ctx->d_cseg_cap, sg.size() + 4))) return rc;
     if ((rc = dgrow(ctx, &ctx->d_klist, &ctx->d_klist_cap, kl.size()))) return rc;
     if (ctx->mc_n2 &&
-        (rc = dgrow(ctx, &ctx->d_base64, &ctx->d_base64_cap, (size_t)M0.bx * M0.by * ctx->g.nz + 1)))
+        ((rc = dgrow(ctx, &ctx->d_base64, &ctx->d_base64_cap, (size_t)M0.bx * M0.by * ctx->g.nz + 1)) ||
+         (rc = dgrow(ctx, &ctx->d_tsrc, &ctx->d_tsrc_cap, (size_t)ctx->ntile_total + 1))))
         return rc;
     cudaStream_t s = ctx->stream;
     CK(cudaMemcpyAsync(ctx->d_cstart, cs.data(), sizeof(long long) * cs.size(), cudaMemcpyHostToDevice, s));
@@ -1050,7 +1071,7 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
     }
     if (ctx->galmodtype == BBGPU_ANALYTIC) {
         if (tm)
-            for (int i = 5; i <= 8; i++) CK(cudaEventRecord(ctx->ev[i], s));
+            for (int i = 5; i <= 9; i++) CK(cudaEventRecord(ctx->ev[i], s));
         CK(cudaMemsetAsync(ctx->d_model_fx, 0, sizeof(long long) * (size_t)ctx->nb * ctx->mstride, s));
         launch_an_model_fast(s, g, ctx->d_asub, ctx->nsub, ctx->d_asbase, ctx->d_assub, ctx->d_acs, ctx->d_acsf,
                              (const float *)ctx->d_acsff, ctx->ansamp, ctx->nb, ctx->d_azq, ctx->d_azqf, ctx->d_awqf,
@@ -1064,7 +1085,7 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
         launch_fix_to_model(s, ctx->d_model_fx, ctx->d_mem, ctx->nb, ctx->mstride, g.nz, ctx->d_model,
                             ctx->want64 ? ctx->d_model64 : nullptr);
         CKL();
-        if (tm) CK(cudaEventRecord(ctx->ev[9], s));
+        if (tm) CK(cudaEventRecord(ctx->ev[10], s));
     } else {
         const LayoutDev &L = ctx->cur->dev;
         if (ctx->mc_dirty) {
@@ -1084,41 +1105,48 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
         CKL();
         if (tm) CK(cudaEventRecord(ctx->ev[7], s));
         if (ctx->mc_n2) {
-            for (int pass = 0; pass < 2; pass++) {
-                launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->tx,
-                                  ctx->ty, ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig, ctx->d_cd2if,
-                                  ctx->d_cd2i, ctx->d_model, ctx->mstride, nullptr, ctx->d_err, ctx->lean,
-                                  ctx->d_klist + (pass ? ctx->mc_n1 : 0), pass ? ctx->mc_n2 : ctx->mc_n1, pass,
-                                  ctx->d_base64);
-                CKL();
-            }
+            launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->tx,
+                              ctx->ty, ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig, ctx->d_cd2if,
+                              ctx->d_cd2i, ctx->d_model, ctx->mstride, nullptr, ctx->d_err, ctx->lean, ctx->d_klist,
+                              ctx->mc_n1, 0, ctx->d_base64, ctx->d_tsrc);
+            CKL();
+            if (tm) CK(cudaEventRecord(ctx->ev[8], s));
+            launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->tx,
+                              ctx->ty, ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig, ctx->d_cd2if,
+                              ctx->d_cd2i, ctx->d_model, ctx->mstride, nullptr, ctx->d_err, ctx->lean,
+                              ctx->d_klist + ctx->mc_n1, ctx->mc_n2, 1, ctx->d_base64, ctx->d_tsrc);
+            CKL();
+            if (tm) CK(cudaEventRecord(ctx->ev[9], s));
         } else {
             launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->tx,
                               ctx->ty, ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig, ctx->d_cd2if,
                               ctx->d_cd2i, ctx->d_model, ctx->mstride, ctx->want64 ? ctx->d_model64 : nullptr,
                               ctx->d_err, ctx->lean);
             CKL();
+            if (tm) {
+                CK(cudaEventRecord(ctx->ev[8], s));
+                CK(cudaEventRecord(ctx->ev[9], s));
+            }
         }
-        if (tm) {
-            CK(cudaEventRecord(ctx->ev[8], s));
-            CK(cudaEventRecord(ctx->ev[9], s));
-        }
+        if (tm) CK(cudaEventRecord(ctx->ev[10], s));
     }
     const bool conv = ctx->kernel_set;
     if (do_resid || ctx->keep_smoothed) {
+        TileSrc ts{nullptr, 0, 0};
+        if (ctx->galmodtype == BBGPU_MC && ctx->mc_n2) ts = TileSrc{ctx->d_tsrc, ilog2(ctx->tx), ilog2(ctx->ty)};
         launch_conv_resid(s, g, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->d_model, ctx->mstride, g.nz,
                           ctx->d_taps, ctx->ky, ctx->kx, ctx->kxw, ctx->keep_smoothed ? ctx->d_smooth : nullptr,
-                          conv ? 1 : 0, do_resid ? 1 : 0, ctx->d_partial);
+                          conv ? 1 : 0, do_resid ? 1 : 0, ctx->d_partial, ts);
         CKL();
     }
-    if (tm) CK(cudaEventRecord(ctx->ev[10], s));
+    if (tm) CK(cudaEventRecord(ctx->ev[11], s));
     if (do_resid) {
         launch_reduce_partials(s, ctx->d_partial, ctx->npart, ctx->nb, ctx->d_out2);
         CKL();
     }
     if (tm) {
-        CK(cudaEventRecord(ctx->ev[11], s));
-        CK(cudaEventSynchronize(ctx->ev[11]));
+        CK(cudaEventRecord(ctx->ev[12], s));
+        CK(cudaEventSynchronize(ctx->ev[12]));
         for (int i = 0; i < NTIMER; i++) {
             float ms = 0.f;
             cudaEventElapsedTime(&ms, ctx->ev[i], ctx->ev[i + 1]);
@@ -1196,6 +1224,19 @@ extern "C" int bbgpu_eval_model(bbgpu_ctx *ctx, int k, int smoothed, float *out,
     CK(cudaSetDevice(ctx->device));
     CK(cudaMemcpyAsync(out, src, sizeof(float) * (size_t)by * bx * nz, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    if (!smoothed && ctx->galmodtype == BBGPU_MC && ctx->mc_n2 && k < (int)ctx->mc_isdelta.size() &&
+        ctx->mc_isdelta[k]) {
+        // the tiles the member shares with member 0 hold member 0's values (the same box)
+        const int nt = M.ntx * M.nty;
+        std::vector<int> ts(nt);
+        std::vector<float> m0((size_t)by * bx * nz);
+        CK(cudaMemcpy(ts.data(), ctx->d_tsrc + M.tile_off, sizeof(int) * nt, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(m0.data(), ctx->d_model, sizeof(float) * m0.size(), cudaMemcpyDeviceToHost));
+        for (int y = 0; y < by; y++)
+            for (int x = 0; x < bx; x++)
+                if (ts[(y / ctx->ty) * M.ntx + x / ctx->tx] == 0)
+                    memcpy(out + ((size_t)y * bx + x) * nz, m0.data() + ((size_t)y * bx + x) * nz, sizeof(float) * nz);
+    }
     return BBGPU_OK;
 }
 

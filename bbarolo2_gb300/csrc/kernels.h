@@ -67,10 +67,11 @@ void launch_mc_scatter(cudaStream_t s, const LayoutDev &L, const SubMC *sub, int
 // Deposits the clouds of every tile into a shared-memory fixed-point tile and writes the model
 // (by, bx, nz) float32 of each member at model + k * mstride (and, if model64, float64 sums); lean: the batch
 // qualifies for the fast kernels (one line, a linear channel map, at most 128 samples per cloud).
-// klist (nk members; nullptr: every member) selects the members of the launch. With base64 (the pixel-owned
-// kernel only, see mc_deposit_shares): delta = 0 leaves member 0's fixed-point sums in base64 (its box);
-// delta = 1 adds them to the members' lists, which hold the difference from member 0's model (same box and
-// exponent; ERR_SHARE otherwise).
+// klist (nk members; nullptr: every member) selects the members of the launch. With base64 and tsrc (the
+// pixel-owned kernel only, see mc_deposit_shares): delta = 0 leaves member 0's fixed-point sums in base64 (its
+// box); delta = 1 adds them to the members' lists, which hold the difference from member 0's model (same box and
+// exponent; ERR_SHARE otherwise), and leaves the tiles without entries unwritten. tsrc[tile_off + t] receives
+// the member whose model holds tile t of the member (itself, or 0 for a tile left unwritten).
 #define ERR_SHARE 8
 bool mc_deposit_shares(int lean, bool model64, int tx, int ty);
 void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
@@ -78,7 +79,7 @@ void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, con
                        const int *offset, const int *count, const void *bucket, const ZigDev *zig,
                        const float *cd2if, const double *cd2i, float *model, long long mstride, double *model64,
                        int *err, int lean, const int *klist = nullptr, int nk = 0, int delta = 0,
-                       long long *base64 = nullptr);
+                       long long *base64 = nullptr, int *tsrc = nullptr);
 
 // ---- convolution + residual (conv.cu)
 // The taps of a beam kernel (ky, kx) as the conv kernels read them: flipped, float32, rows padded to the
@@ -89,9 +90,20 @@ int conv_taps(const double *k, int ky, int kx, float *taps);
 // If smoothed is not NULL the convolved model is written there (same layout).
 // partial: (nb, npart) pairs (ss, lg), npart = tiles of the largest box x channel blocks (returned).
 int conv_resid_npart(const MemberDev *mem_host, int nb, int nz);
+// With a tile table (tsrc): the model of member k at a pixel is that of member tsrc[tile_off + (y >> shy) ntx +
+// (x >> shx)] (the MC deposit tiles of 2^shx x 2^shy pixels; a member computed as a difference from member 0
+// leaves the tiles it shares with member 0 unwritten).
+struct TileSrc {
+    const int *tsrc;
+    int shx, shy;
+};
 void launch_conv_resid(cudaStream_t s, const GridDev &g, const MemberDev *mem, const MemberDev *mem_host, int nb,
                        const float *model, long long mstride, int nz, const float *taps, int ky, int kx, int kxw,
-                       float *smoothed, int do_conv, int do_resid, double *partial);
+                       float *smoothed, int do_conv, int do_resid, double *partial, TileSrc ts = TileSrc{nullptr, 0, 0});
+// (the tile-table variant, conv_table.cu: maxt tiles and nzb channel blocks of ZB = 16 (z16) or 32 channels)
+void launch_conv_table(cudaStream_t s, const GridDev &g, const MemberDev *mem, int nb, int maxt, int nzb, bool z16,
+                       const float *model, long long mstride, int nz, const float *taps, int ky, int kx, int kxw,
+                       float *smoothed, int do_conv, int do_resid, double *partial, int npart, TileSrc ts);
 void launch_reduce_partials(cudaStream_t s, const double *partial, int npart, int nb, double *out2);
 
 // ---- layouts and stand-alone residuals (resid.cu)

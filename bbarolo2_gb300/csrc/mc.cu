@@ -27,6 +27,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "devmath.cuh"
 #include "kernels.h"
 
@@ -953,14 +955,16 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
                                                               const float *__restrict__ cd2if,
                                                               float *__restrict__ model, long long mstride,
                                                               const int *__restrict__ klist, int delta,
-                                                              unsigned long long *__restrict__ base64, int *err) {
+                                                              unsigned long long *__restrict__ base64,
+                                                              int *__restrict__ tsrc, int *err) {
     constexpr int LPP = 128 / SPL;
     extern __shared__ unsigned long long tile[];           // TP rows of fixed-point sums, queues, nz scales
     __shared__ unsigned long long inc[32];                 // the histogram increments of px_count
     const int k = klist ? klist[blockIdx.x] : blockIdx.x;
     const int t = blockIdx.y;
     // delta: the member's lists hold the difference from member 0's model (same box and exponent), whose sums
-    // are in base64; else member 0 (with base64) leaves its sums there
+    // are in base64, and a tile without entries is left unwritten (tsrc points the convolution to member 0's
+    // model there); else member 0 (with base64) leaves its sums there
     unsigned long long *wbase = !delta && k == 0 ? base64 : nullptr;
     if (delta && threadIdx.x == 0 && blockIdx.y == 0 && mem[k].fix_exp != mem[0].fix_exp) atomicOr(err, ERR_SHARE);
     const int ntx = mem[k].ntx;
@@ -979,22 +983,21 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
         int any = 0;
         if (threadIdx.x < NOWN) any = count[lbase + threadIdx.x] != 0;
         if (!__syncthreads_or(any)) {
+            if (tsrc && threadIdx.x == 0) tsrc[mem[k].tile_off + t] = delta ? 0 : k;
+            if (delta) return;
             for (int lp = warp; lp < TP; lp += 8) {
                 const int py = y0 + lp / tx, px = x0 + lp % tx;
                 if (py >= by || px >= bx) continue;
                 const size_t v0 = ((size_t)py * bx + px) * nz;
                 float *o = mout + v0;
-                if (delta) {
-                    for (int z = lane; z < nz; z += 32) o[z] = model[v0 + z];   // (member 0's: same units)
-                } else {
-                    for (int z = lane; z < nz; z += 32) o[z] = 0.0f;
-                    if (wbase)
-                        for (int z = lane; z < nz; z += 32) wbase[v0 + z] = 0ULL;
-                }
+                for (int z = lane; z < nz; z += 32) o[z] = 0.0f;
+                if (wbase)
+                    for (int z = lane; z < nz; z += 32) wbase[v0 + z] = 0ULL;
             }
             return;
         }
     }
+    if (tsrc && threadIdx.x == 0) tsrc[mem[k].tile_off + t] = k;
     PxDefer *qall = (PxDefer *)(tile + (size_t)TP * RS);   // (16-byte aligned: TP RS is even)
     int *qns = (int *)(qall + 8 * PX_QCAP);
     float *chs = (float *)(qns + 8);
@@ -1185,11 +1188,27 @@ bool mc_deposit_shares(int lean, bool model64, int tx, int ty) {
     return lean && !model64 && (tx * ty == 64 || tx * ty == 32);
 }
 
+// dynamic shared memory of the pixel-owned deposit (TP pixels a tile), the kernel configured for it once
+static size_t px_smem(const GridDev &g, int TP) {
+    const size_t smem_px = (size_t)TP * (g.nz + TP / 4) * sizeof(unsigned long long) +
+                           (size_t)8 * PX_QCAP * sizeof(PxDefer) + 8 * sizeof(int) + (size_t)g.nz * sizeof(float);
+    static size_t cfg32 = 0, cfg16 = 0;
+    size_t &cfg = TP == 64 ? cfg32 : cfg16;
+    if (smem_px > 48 * 1024 && smem_px > cfg) {
+        if (TP == 64)
+            cudaFuncSetAttribute(k_mc_deposit_px<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_px);
+        else
+            cudaFuncSetAttribute(k_mc_deposit_px<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_px);
+        cfg = smem_px;
+    }
+    return smem_px;
+}
+
 void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
                        const MemberDev *mem, const MemberDev *mem_host, int nb, int tx, int ty,
                        const int *offset, const int *count, const void *bucket, const ZigDev *zig,
                        const float *cd2if, const double *cd2i, float *model, long long mstride, double *model64,
-                       int *err, int lean, const int *klist, int nk, int delta, long long *base64) {
+                       int *err, int lean, const int *klist, int nk, int delta, long long *base64, int *tsrc) {
     int maxt = 0;
     for (int k = 0; k < nb; k++) maxt = max(maxt, mem_host[k].ntx * mem_host[k].nty);
     if (maxt == 0 || nb == 0 || (klist && nk == 0)) return;
@@ -1210,27 +1229,16 @@ void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, con
         const int TP = tx * ty;
         if (TP == 64 || TP == 32) {
             // pixel-owned deposit: 8 (TP 64) or 4 (TP 32) pixels per warp
-            const size_t smem_px = (size_t)TP * (g.nz + TP / 4) * sizeof(unsigned long long) +
-                                   (size_t)8 * PX_QCAP * sizeof(PxDefer) + 8 * sizeof(int) +
-                                   (size_t)g.nz * sizeof(float);
-            static size_t cfg32 = 0, cfg16 = 0;
-            size_t &cfg = TP == 64 ? cfg32 : cfg16;
-            if (smem_px > 48 * 1024 && smem_px > cfg) {
-                if (TP == 64)
-                    cudaFuncSetAttribute(k_mc_deposit_px<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_px);
-                else
-                    cudaFuncSetAttribute(k_mc_deposit_px<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_px);
-                cfg = smem_px;
-            }
+            const size_t smem_px = px_smem(g, TP);
             unsigned long long *b64 = (unsigned long long *)base64;
             if (TP == 64)
                 k_mc_deposit_px<32><<<grid, 256, smem_px, s>>>(g, L, sub, nsub, mem, tx, ty, offset, count,
                                                                (const Entry *)bucket, zig, cd2if, model, mstride,
-                                                               klist, delta, b64, err);
+                                                               klist, delta, b64, tsrc, err);
             else
                 k_mc_deposit_px<16><<<grid, 256, smem_px, s>>>(g, L, sub, nsub, mem, tx, ty, offset, count,
                                                                (const Entry *)bucket, zig, cd2if, model, mstride,
-                                                               klist, delta, b64, err);
+                                                               klist, delta, b64, tsrc, err);
             return;
         }
         k_mc_deposit_lean<<<grid, 256, smem, s>>>(g, L, sub, nsub, mem, tx, ty, offset, count, (const Entry *)bucket,

@@ -172,8 +172,9 @@ def throughput(units_per_rank, steps, world, t):
     return units_per_rank * steps * world / t
 
 
-def algorithmic(dm, L, sr, nv, descs):
-    """Algorithmic bytes / flops per launch of the kernels (summed over the batch)."""
+def algorithmic(dm, L, sr, nv, descs, mc_members=None):
+    """Algorithmic bytes / flops per launch of the kernels (summed over the batch; the first MC deposit launch
+    covers mc_members of them, the members that deposit all their clouds)."""
     st = dm.setup
     nz = st.nsubs
     ky, kx = dm.cfield.shape
@@ -184,7 +185,7 @@ def algorithmic(dm, L, sr, nv, descs):
     from bbarolo2_gb300.galmod import cloud_counts
     ncl, nsubcl = cloud_counts(st, sr[0], nv[0])
     B = len(descs)
-    mc_bytes = 4 * nsubcl + 16 * ncl + 4 * vox
+    mc_bytes = 4 * nsubcl + 16 * ncl + 4 * vox * (B if mc_members is None else mc_members) // B
     conv_flops = 2.0 * taps * vox
     conv_bytes = 4 * vox * 2 + vox // 1        # model read + data read (+ mask folded in the data)
     return dict(mc_deposit=("hbm", mc_bytes), conv_resid=("tensor", conv_flops), conv_bytes=conv_bytes,
@@ -289,7 +290,13 @@ def main():
     e2e = throughput(B, args.steps, world, te)
     # ---- roofline of the dominant kernel
     hbm, bf16, src = peaks()
-    alg = algorithmic(dm, L, sr, nv, descs)
+    # (the last run of the batch above: how many members were computed as a difference from member 0)
+    ctx.check(ctx.L.bbgpu_eval_upload(ctx.h, _lib.MC, B, sr.shape[2], _lib.ptr(sr), _lib.ptr(nv), _lib.ptr(descs)))
+    ctx.check(ctx.L.bbgpu_eval_upload_profile(ctx.h, ms.shape[2], _lib.ptr(ms), _lib.ptr(L._prof["widx"]),
+                                              _lib.ptr(L._prof["wval"])))
+    ctx.check(ctx.L.bbgpu_eval_run(ctx.h))
+    nprof, mc_full, mc_delta = ctx.shared_members()
+    alg = algorithmic(dm, L, sr, nv, descs, mc_full)
     dom = max((k for k in kt if not k.startswith("prof_")), key=kt.get)   # (the MC model and its convolution)
     if dom == "conv_resid":
         achieved = alg["conv_resid"][1] / (kt[dom] * 1e-3) / 1e12
@@ -309,7 +316,12 @@ def main():
                        "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (per-batch models 2 GB)",
                        "flux_normalisation": "deconvolved density profile recomputed at every evaluation (ring "
                                              "maps, beam, weighted NNLS with the smoothness prior), as the reference "
-                                             "with DENS not fitted and the geometry free"},
+                                             "with DENS not fitted and the geometry free",
+                       "shared": {"profiles_computed": nprof, "mc_members_full": mc_full,
+                                  "mc_members_difference": mc_delta,
+                                  "note": "members equal to the first but for a few sub-rings are computed as its "
+                                          "result plus the exact difference (bit-identical; 'unshared' below "
+                                          "computes every member in full)"}},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "kernel_ms": kt, "roofline": roof, "clocks": clocks,
             "logL_sample": [float(out[0]), float(out[1])]}
