@@ -23,7 +23,12 @@ __global__ void k_reduce_partials(const double *__restrict__ partial, int npart,
     const int k = blockIdx.x;
     const double *p = partial + 2 * (size_t)k * npart;
     double a = 0.0, b = 0.0;
-    for (int i = threadIdx.x; i < npart; i += 256) { a += p[2 * i]; b += p[2 * i + 1]; }
+    for (int i = threadIdx.x; i < npart; i += 256) {
+        // (-1: the tile's sums are member 0's, see the tile table of k_conv_resid)
+        const bool m0 = p[2 * i] == -1.0;
+        a += m0 ? partial[2 * i] : p[2 * i];
+        b += m0 ? partial[2 * i + 1] : p[2 * i + 1];
+    }
     sa[threadIdx.x] = a;
     sb[threadIdx.x] = b;
     __syncthreads();

@@ -83,6 +83,13 @@ __global__ void __launch_bounds__(256, 2) k_conv_resid(GridDev g, const MemberDe
         }
         uni = !__syncthreads_or(diff) && tny * tnx <= TS_MAX;
         if (uni) mk = model + (size_t)first * mstride;
+        // the whole input region is member 0's model (a member computed as a difference from it, away from the
+        // sub-rings that differ): the tile's sums are member 0's, taken by the reduction (sentinel -1: a sum of
+        // squares is never negative)
+        if (uni && first == 0 && k != 0 && !smoothed) {
+            if (threadIdx.x == 0) { pout[0] = -1.0; pout[1] = 0.0; }
+            return;
+        }
     }
     auto src = [&](int yy, int xx) -> const float * {
         if (!TS || uni) return mk;
