@@ -350,9 +350,14 @@ class BatchLikelihood:
         er[:, keep, 0] = rows[:, keep, -1]
         er[:, RING_KEYS.index("radii"), 0] = ext.radii[0]
         er[:, RING_KEYS.index("dens"), 0] = 1.
-        emr_rows, emr = dm.model_rows(er, ext, ringmode="CENTRED")
+        # (the members of a batch mostly share member 0's last ring: its table, and those of the others)
+        other = np.flatnonzero(np.any(er != er[:1], axis=(1, 2)))
+        pick = np.concatenate([[0], other])
+        emr_rows, emr = dm.model_rows(er[pick], ext, ringmode="CENTRED")
         sre, _ = subrings_batch(dm.setup, emr, emr_rows)
-        return sre
+        out = np.repeat(sre[:1], er.shape[0], axis=0)
+        out[other] = sre[1:]
+        return out
 
     def _boxsum(self, blo, bhi):
         S = self._dm2_sat

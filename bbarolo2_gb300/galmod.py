@@ -233,6 +233,39 @@ class SubringGrid:
         v0 + ((v1 - v0) / dur) * dr, constant rows before the first radius)."""
         V = np.asarray(V, float)
         nr = V.shape[-1]
+        if V.ndim == 3 and V.shape[0] > 8 and nr > 1 and self.nsub:
+            out = self._interpolate_steps(V)
+            if out is not None:
+                return out
+        return self._interpolate_all(V)
+
+    def _interpolate_steps(self, V):
+        """A batch whose members differ from member 0 in few rings (the steps of a finite-difference gradient):
+        member 0's values, and the same operations on the sub-rings next to a ring that differs (the values
+        are those of _interpolate_all, bit for bit); None when more than a quarter of the values differ."""
+        i1 = self.i1
+        D = np.any(V != V[:1], axis=1)                                   # (B, nr): rings that differ
+        if np.count_nonzero(D) * 4 > D.size:
+            return None
+        A = D[:, i1 - 1] | D[:, i1] | (self.const[None, :] & D[:, :1])   # (B, nsub): sub-rings that differ
+        bb, ss = np.nonzero(A)
+        if bb.size * 4 > A.size:
+            return None
+        out = np.repeat(self._interpolate_all(V[:1]), V.shape[0], axis=0)
+        if bb.size:
+            j = i1[ss]
+            v0 = V[bb, :, j - 1]                                         # (P, nrow)
+            sl = (V[bb, :, j] - v0) / self._dseg[j - 1][:, None]
+            sl *= self.dr[ss][:, None]
+            v = v0 + sl
+            c = self.const[ss]
+            if c.any():
+                v[c] = V[bb[c], :, 0]
+            out[bb, :, ss] = v
+        return out
+
+    def _interpolate_all(self, V):
+        nr = V.shape[-1]
         i1 = self.i1
         if nr > 1:
             # the slope of each segment once (dur depends on the segment only), then gathered per sub-ring

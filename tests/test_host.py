@@ -55,6 +55,31 @@ def test_subrings_batch_equal_single(case):
     assert np.array_equal(sr[1], s2) and np.array_equal(nv[1], n2)
 
 
+@pytest.mark.parametrize("case", _cases(), ids=lambda c: c[1]["name"])
+def test_subrings_batch_gradient_steps(case):
+    """A finite-difference batch (member 0, then one ring's value stepped per member, fewer than a quarter of
+    the values changed): the tables built from member 0's plus the sub-rings next to the stepped rings equal,
+    bit for bit, the per-set tables."""
+    z, m = case
+    cube, rings, mode = _rebuild(m["name"])
+    st = galmod.GalmodSetup(cube, densflux=True)
+    mr = galmod.model_rings(rings, mode, st.radsep)
+    base = galmod.ring_rows_batch([mr])[0]
+    rows = [base]
+    for j in range(mr.nr):
+        for row, step in ((4, 3.0), (12, 1.0)):
+            r = base.copy()
+            r[row, j] += step
+            rows.append(r)
+    rows = np.stack(rows)
+    sr, nv = galmod.subrings_batch(st, mr, rows)
+    for k in (0, 1, 2, len(rows) // 2, len(rows) - 1):
+        r2 = mr.copy()
+        r2.vrot, r2.inc = rows[k, 4].copy(), rows[k, 12].copy()
+        s2, n2 = st.subrings(r2)
+        assert np.array_equal(sr[k], s2) and np.array_equal(nv[k], n2), k
+
+
 @pytest.mark.parametrize("wl", ["classic64", "global160", "bayes256"])
 def test_beam_kernel(wl):
     z = G.load("beam_conv.npz")
