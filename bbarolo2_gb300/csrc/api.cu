@@ -126,8 +126,12 @@ struct bbgpu_ctx {
     size_t d_pmem_cap = 0;
     // rows of the maps (the members with a profile of their own, nu of them) and the segments of the maps
     // kernel's threads (bbgpu_eval_upload_profile); the solutions of the rows go to the members by prof_of
-    int nu = 0, nseg = 0;
+    int nu = 0, nseg = 0, nu_delta = 0;
     long long mtot = 0;
+    // rows with a base row: the 8 x 8 pixel blocks of their maps (blk), the tiles of their convolution (ktab)
+    // and the Gram tiles (gflag) that are row 0's
+    int *d_blk = nullptr, *d_ktab = nullptr, *d_gflag = nullptr;
+    size_t d_blk_cap = 0, d_ktab_cap = 0, d_gflag_cap = 0;
     long long *d_mstart = nullptr;
     int *d_mseg = nullptr, *d_uidx = nullptr, *d_ubase = nullptr, *d_prof_of = nullptr, *d_pstatu = nullptr;
     double *d_pxu = nullptr;
@@ -450,7 +454,7 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
                     (void *)ctx->d_pmem, (void *)ctx->d_mstart, (void *)ctx->d_mseg, (void *)ctx->d_uidx,
                     (void *)ctx->d_ubase, (void *)ctx->d_prof_of, (void *)ctx->d_pstatu, (void *)ctx->d_pxu,
                     (void *)ctx->d_cstart, (void *)ctx->d_base64, (void *)ctx->d_cseg, (void *)ctx->d_klist,
-                    (void *)ctx->d_tsrc})
+                    (void *)ctx->d_tsrc, (void *)ctx->d_blk, (void *)ctx->d_ktab, (void *)ctx->d_gflag})
         cudaFree(q);
     for (void *q : {(void *)ctx->d_asub, (void *)ctx->d_asbase, (void *)ctx->d_assub, (void *)ctx->d_acs,
                     (void *)ctx->d_azq, (void *)ctx->d_awq, (void *)ctx->d_model_fx, (void *)ctx->d_acsf,
@@ -939,19 +943,25 @@ static int profile_run(bbgpu_ctx *ctx, bool tm) {
                         ctx->d_mstart, ctx->d_mseg, ctx->nseg, ctx->mtot, ctx->d_pzq, ctx->d_pzqf, ctx->d_pwqf,
                         ctx->d_pwidx, ctx->d_pwvalf, bx, ctx->d_pfix, ctx->d_maps64);
     CKL();
+    const bool shared = ctx->nu_delta > 0 && per < (1LL << 31);      // (the block table indexes in 32 bits)
     launch_maps_to_f32(s, ctx->d_maps64, ctx->d_pfix, ctx->d_uidx, ctx->d_ubase, nu, per, (float)ctx->mapscale,
-                       ctx->d_maps32);
+                       ctx->d_maps32, shared ? ctx->d_blk : nullptr, bx);
     CKL();
+    if (shared) ctx->launches++;      // (the block table's initialisation)
+    int nct = 0, ntxc = 0, shx = 0, shy = 0;
+    conv_tile_shape(bx.nrp, bx.bx, bx.by, nct, ntxc, shx, shy);
     if (tm) CK(cudaEventRecord(ctx->ev[1], s));
     if (ctx->kernel_set) {
         launch_conv_resid(s, g, ctx->d_pmem, ctx->pmem_host.data(), nu, ctx->d_maps32, per, bx.nrp, ctx->d_taps,
-                          ctx->ky, ctx->kx, ctx->kxw, ctx->d_K, 2, 0, ctx->d_ppart);
+                          ctx->ky, ctx->kx, ctx->kxw, ctx->d_K, 2, 0, ctx->d_ppart,
+                          shared ? TileSrc{ctx->d_blk, 3, 3, ctx->d_ktab, nct} : TileSrc{nullptr, 0, 0, nullptr, 0});
         CKL();
     }
     if (tm) CK(cudaEventRecord(ctx->ev[2], s));
     const float *K = ctx->kernel_set ? ctx->d_K : ctx->d_maps32;
     launch_prof_gram(s, K, bx, ctx->d_ppix, ctx->d_pw, ctx->d_pwy, ctx->npix_used, ctx->d_ent, ctx->d_ent + ctx->nent,
-                     ctx->nent, nu, ctx->d_gpart, ctx->d_gh);
+                     ctx->nent, nu, ctx->d_gpart, ctx->d_gh,
+                     shared && ctx->kernel_set ? KRows{ctx->d_ktab, nct, ntxc, shx, shy, ctx->d_gflag} : KRows{});
     ctx->launches += 2;
     CKL();
     if (tm) CK(cudaEventRecord(ctx->ev[3], s));
@@ -1132,8 +1142,9 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
     }
     const bool conv = ctx->kernel_set;
     if (do_resid || ctx->keep_smoothed) {
-        TileSrc ts{nullptr, 0, 0};
-        if (ctx->galmodtype == BBGPU_MC && ctx->mc_n2) ts = TileSrc{ctx->d_tsrc, ilog2(ctx->tx), ilog2(ctx->ty)};
+        TileSrc ts{nullptr, 0, 0, nullptr, 0};
+        if (ctx->galmodtype == BBGPU_MC && ctx->mc_n2)
+            ts = TileSrc{ctx->d_tsrc, ilog2(ctx->tx), ilog2(ctx->ty), nullptr, 0};
         launch_conv_resid(s, g, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->d_model, ctx->mstride, g.nz,
                           ctx->d_taps, ctx->ky, ctx->kx, ctx->kxw, ctx->keep_smoothed ? ctx->d_smooth : nullptr,
                           conv ? 1 : 0, do_resid ? 1 : 0, ctx->d_partial, ts);
@@ -1867,6 +1878,8 @@ extern "C" int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *
     }
     ctx->nu = (int)uidx.size();
     ctx->nseg = (int)mstart.size() - 1;
+    ctx->nu_delta = 0;
+    for (int b : ubase) ctx->nu_delta += b >= 0;
     ctx->prof_of_host = prof_of;
     ctx->mc_dirty = true;
     // the vertical grids: the new ones appended on the device (the table grows with a copy of the old part)
@@ -1925,10 +1938,24 @@ extern "C" int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *
     if ((rc = dgrow(ctx, &ctx->d_uidx, &ctx->d_uidx_cap, uidx.size()))) return rc;
     if ((rc = dgrow(ctx, &ctx->d_ubase, &ctx->d_ubase_cap, ubase.size()))) return rc;
     if ((rc = dgrow(ctx, &ctx->d_prof_of, &ctx->d_prof_of_cap, prof_of.size()))) return rc;
-    // the maps' convolution: one member descriptor per member, the likelihood box
+    // the maps' convolution: one member descriptor per row, the likelihood box (and the row's 8 x 8 pixel blocks
+    // in the block table)
+    const int nbx8 = (bx.bx + 7) / 8, nblk8 = nbx8 * ((bx.by + 7) / 8);
     ctx->pmem_host.assign(nb, MemberDev{});
-    for (auto &M : ctx->pmem_host) {
+    for (int u = 0; u < nb; u++) {
+        MemberDev &M = ctx->pmem_host[u];
         M.blo0 = bx.blo0; M.blo1 = bx.blo1; M.bhi0 = bx.bhi0; M.bhi1 = bx.bhi1; M.bx = bx.bx; M.by = bx.by;
+        M.tile_off = u * nblk8;
+        M.ntx = nbx8;
+        M.nty = (bx.by + 7) / 8;
+    }
+    if (ctx->nu_delta) {
+        int nct, ntxc, shx, shy;
+        conv_tile_shape(bx.nrp, bx.bx, bx.by, nct, ntxc, shx, shy);
+        if ((rc = dgrow(ctx, &ctx->d_blk, &ctx->d_blk_cap, (size_t)ctx->nu * nblk8 + 1)) ||
+            (rc = dgrow(ctx, &ctx->d_ktab, &ctx->d_ktab_cap, (size_t)ctx->nu * nct + 1)) ||
+            (rc = dgrow(ctx, &ctx->d_gflag, &ctx->d_gflag_cap, (size_t)ctx->nu * (nt ? nt : 1) + 1)))
+            return rc;
     }
     const int npart = conv_resid_npart(ctx->pmem_host.data(), nb, bx.nrp);
     if ((rc = dgrow(ctx, &ctx->d_pmem, &ctx->d_pmem_cap, (size_t)nb))) return rc;

@@ -68,6 +68,14 @@ static void conv_grid(const MemberDev *mem_host, int nb, int nz, int &maxt, int 
     nzb = (nz + zbw - 1) / zbw;
 }
 
+void conv_tile_shape(int nz, int bx, int by, int &nct, int &ntx, int &shx, int &shy) {
+    const int toy = TO * (32 / conv_zb(nz));
+    ntx = (bx + TO - 1) / TO;
+    nct = ntx * ((by + toy - 1) / toy);
+    shx = 4;                               // (TO = 16)
+    shy = toy == 32 ? 5 : 4;
+}
+
 int conv_resid_npart(const MemberDev *mem_host, int nb, int nz) {
     int maxt, nzb;
     conv_grid(mem_host, nb, nz, maxt, nzb);

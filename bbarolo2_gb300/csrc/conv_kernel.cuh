@@ -86,7 +86,15 @@ __global__ void __launch_bounds__(256, 2) k_conv_resid(GridDev g, const MemberDe
         // the whole input region is member 0's model (a member computed as a difference from it, away from the
         // sub-rings that differ): the tile's sums are member 0's, taken by the reduction (sentinel -1: a sum of
         // squares is never negative)
-        if (uni && first == 0 && k != 0 && !smoothed) {
+        if (ts.kout) {
+            // (the ring maps: such a tile keeps member 0's output, which the normal equations read there)
+            const bool skip = uni && first == 0 && k != 0;
+            if (zb == 0 && threadIdx.x == 0) ts.kout[(size_t)k * ts.kstride + t] = skip ? 0 : k;
+            if (skip) {
+                if (threadIdx.x == 0) { pout[0] = 0.0; pout[1] = 0.0; }
+                return;
+            }
+        } else if (uni && first == 0 && k != 0 && !smoothed) {
             if (threadIdx.x == 0) { pout[0] = -1.0; pout[1] = 0.0; }
             return;
         }

@@ -90,16 +90,22 @@ int conv_taps(const double *k, int ky, int kx, float *taps);
 // If smoothed is not NULL the convolved model is written there (same layout).
 // partial: (nb, npart) pairs (ss, lg), npart = tiles of the largest box x channel blocks (returned).
 int conv_resid_npart(const MemberDev *mem_host, int nb, int nz);
+// the output tiles of the convolution of a (by, bx, nz) box: nct tiles, ntx a row, of 2^shx x 2^shy pixels
+void conv_tile_shape(int nz, int bx, int by, int &nct, int &ntx, int &shx, int &shy);
 // With a tile table (tsrc): the model of member k at a pixel is that of member tsrc[tile_off + (y >> shy) ntx +
 // (x >> shx)] (the MC deposit tiles of 2^shx x 2^shy pixels; a member computed as a difference from member 0
 // leaves the tiles it shares with member 0 unwritten).
+// With kout (the ring maps' convolution into K): a tile whose input lies wholly in member 0's is left unwritten,
+// and kout[k kstride + t] receives the member whose output holds tile t (0 there, else k).
 struct TileSrc {
     const int *tsrc;
     int shx, shy;
+    int *kout;
+    int kstride;
 };
 void launch_conv_resid(cudaStream_t s, const GridDev &g, const MemberDev *mem, const MemberDev *mem_host, int nb,
                        const float *model, long long mstride, int nz, const float *taps, int ky, int kx, int kxw,
-                       float *smoothed, int do_conv, int do_resid, double *partial, TileSrc ts = TileSrc{nullptr, 0, 0});
+                       float *smoothed, int do_conv, int do_resid, double *partial, TileSrc ts = TileSrc{nullptr, 0, 0, nullptr, 0});
 // (the tile-table variant, conv_table.cu: maxt tiles and nzb channel blocks of ZB = 16 (z16) or 32 channels)
 void launch_conv_table(cudaStream_t s, const GridDev &g, const MemberDev *mem, int nb, int maxt, int nzb, bool z16,
                        const float *model, long long mstride, int nz, const float *taps, int ky, int kx, int kxw,
@@ -171,15 +177,25 @@ void launch_an_maps_fast(cudaStream_t s, const GridDev &g, const AnSub *subs, in
                          const int *mseg, int nseg, long long ntot, const double *zq, const float *zqf,
                          const float *wqf, const int *widx, const float *wvalf, const ProfBox &box,
                          const int *fix_exp, long long *maps64);
-// rows u < nu of maps64 (member uidx[u]; plus row ubase[u] when >= 0) -> float32
+// rows u < nu of maps64 (member uidx[u]; plus row ubase[u] when >= 0) -> float32; with ptab (nu x the 8 x 8
+// pixel blocks of the box, row-major): the row whose maps hold each block (the row itself, or its base row where
+// their maps are equal)
 void launch_maps_to_f32(cudaStream_t s, const long long *in, const int *fix_exp, const int *uidx, const int *ubase,
-                        int nu, long long per_member, float scale, float *out);
+                        int nu, long long per_member, float scale, float *out, int *ptab, const ProfBox &box);
 void launch_prof_gather(cudaStream_t s, const double *xu, const int *stu, const int *prof_of, int nb, int n, double *x,
                         int *st);
 int prof_gram_tiles(int npix_used);
+// The rows of K that hold each convolution tile (ktab: nct tiles of 2^shx x 2^shy pixels, ntx a row, per row;
+// row 0's where a row's convolution left it unwritten), and gflag (rows x Gram tiles): 1 where a Gram tile took
+// row 0's sums. ktab == nullptr: every row's own K.
+struct KRows {
+    const int *ktab;
+    int nct, ntx, shx, shy;
+    int *gflag;
+};
 void launch_prof_gram(cudaStream_t s, const float *K, const ProfBox &box, const int *pix, const double *wpix,
                       const double *wy, int npix_used, const int *ent_i, const int *ent_j, int nent, int nb,
-                      double *part, double *gh);
+                      double *part, double *gh, KRows kr = KRows{});
 // one system A (m, n) row-major (box.nrp = n, box.npix = m), b (m): packed G = A^T A, h = A^T b
 void launch_prof_gram64(cudaStream_t s, const double *A, const ProfBox &box, const double *b, int m, const int *ent_i,
                         const int *ent_j, int nent, double *part, double *gh);

@@ -156,9 +156,12 @@ __global__ void __launch_bounds__(MAPS_TB, MAPS_MINB) k_an_maps_fast(GridDev g, 
 
 // maps (row u, pixel, ring) int64 units 2^-e -> float32 x scale; a row with a base row holds the difference from
 // it (the sum, modulo 2^64, is the row's maps: exact whatever the order of the deposits)
+// With a block table (ptab, initialised by k_ptab_init): a row with a base row marks the 8 x 8 pixel blocks
+// where its difference is not zero (there its maps are its own; elsewhere they are the base row's, bit for bit).
 __global__ void k_maps_to_f32(const long long *__restrict__ in, const int *__restrict__ fix_exp,
                               const int *__restrict__ uidx, const int *__restrict__ ubase, long long per_member,
-                              float scale, float *__restrict__ out) {
+                              float scale, float *__restrict__ out, int *__restrict__ ptab, int nblk, int nbx,
+                              int nrp, int bx) {
     const int u = blockIdx.y;
     const float sc = ldexpf(scale, -fix_exp[uidx[u]]);
     const long long *src = in + (size_t)u * per_member;
@@ -167,9 +170,23 @@ __global__ void k_maps_to_f32(const long long *__restrict__ in, const int *__res
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < per_member;
          i += (long long)gridDim.x * blockDim.x) {
         long long v = src[i];
-        if (bas) v = (long long)((unsigned long long)v + (unsigned long long)bas[i]);
+        if (bas) {
+            if (ptab && v != 0) {
+                const int q = (int)i / nrp, py = q / bx, px = q - py * bx;      // (per_member < 2^31)
+                ptab[(size_t)u * nblk + (py >> 3) * nbx + (px >> 3)] = u;
+            }
+            v = (long long)((unsigned long long)v + (unsigned long long)bas[i]);
+        }
         dst[i] = ll_to_f32(v) * sc;
     }
+}
+
+// the block table: a row with a base row starts with the base row's maps everywhere, the others with their own
+__global__ void k_ptab_init(int *__restrict__ ptab, const int *__restrict__ ubase, int nu, int nblk) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)nu * nblk) return;
+    const int u = (int)(i / nblk);
+    ptab[i] = ubase[u] >= 0 ? ubase[u] : u;
 }
 
 // the solutions of the rows, to the members: x[k] = xu[prof_of[k]], status likewise
@@ -193,21 +210,42 @@ __global__ void __launch_bounds__(256) k_prof_gram(const T *__restrict__ K, Prof
                                                    const double *__restrict__ wpix, const double *__restrict__ wy,
                                                    int npix_used, const int *__restrict__ ent_i,
                                                    const int *__restrict__ ent_j, int nent,
-                                                   double *__restrict__ part) {
+                                                   double *__restrict__ part, KRows kr) {
     extern __shared__ double gsm[];
     const int n = box.nrp;
     double *Kd = gsm;                                       // GRAM_TP x n maps
     double *Kw = Kd + GRAM_TP * n;                          // GRAM_TP x n maps x pixel weight
     double *wys = Kw + GRAM_TP * n;                         // GRAM_TP weighted data
     int *lo = (int *)(wys + GRAM_TP), *hi = lo + GRAM_TP;   // rings not zero at the pixel: lo .. hi
+    __shared__ int srow[GRAM_TP];                           // the row whose K holds each pixel
     const int k = blockIdx.y, t = blockIdx.x;
     const int p0 = t * GRAM_TP;
     const int np = min(GRAM_TP, npix_used - p0);
-    const T *Kk = K + (size_t)k * box.npix * n;
+    if (kr.ktab) {
+        // a row's convolution left the tiles it shares with row 0 unwritten: K of row 0 there (the same values);
+        // a tile of such pixels only has row 0's sums, taken by the reduction
+        int own = 0;
+        for (int pp = threadIdx.x; pp < np; pp += blockDim.x) {
+            const int q = pix ? pix[p0 + pp] : p0 + pp;
+            const int py = q / box.bx, px = q - py * box.bx;
+            const int r = kr.ktab[(size_t)k * kr.nct + (py >> kr.shy) * kr.ntx + (px >> kr.shx)];
+            srow[pp] = r;
+            own |= r != 0;
+        }
+        own = __syncthreads_or(own);
+        if (k != 0 && !own) {
+            if (threadIdx.x == 0) kr.gflag[(size_t)k * gridDim.x + t] = 1;
+            return;
+        }
+        if (threadIdx.x == 0) kr.gflag[(size_t)k * gridDim.x + t] = 0;
+    } else {
+        for (int pp = threadIdx.x; pp < np; pp += blockDim.x) srow[pp] = k;
+        __syncthreads();
+    }
     for (int i = threadIdx.x; i < np * n; i += blockDim.x) {
         const int pp = i / n, r = i - pp * n;
         const long long q = pix ? pix[p0 + pp] : p0 + pp;
-        const double v = (double)Kk[(size_t)q * n + r];
+        const double v = (double)K[((size_t)srow[pp] * box.npix + q) * n + r];
         Kd[i] = v;
         Kw[i] = v * (wpix ? wpix[p0 + pp] : 1.0);
     }
@@ -249,12 +287,16 @@ __global__ void __launch_bounds__(256) k_prof_gram(const T *__restrict__ K, Prof
     }
 }
 
-__global__ void k_prof_gram_reduce(const double *__restrict__ part, int ntile, int nent, double *__restrict__ gh) {
+__global__ void k_prof_gram_reduce(const double *__restrict__ part, int ntile, int nent, double *__restrict__ gh,
+                                   const int *__restrict__ gflag) {
     const int k = blockIdx.y;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nent) return;
     double acc = 0.0;
-    for (int t = 0; t < ntile; t++) acc += part[((size_t)k * ntile + t) * nent + e];
+    for (int t = 0; t < ntile; t++) {
+        const bool z = gflag && gflag[(size_t)k * ntile + t];      // (row 0's sums: see k_prof_gram)
+        acc += part[((size_t)(z ? 0 : k) * ntile + t) * nent + e];
+    }
     gh[(size_t)k * nent + e] = acc;
 }
 
@@ -690,10 +732,16 @@ void launch_an_maps_fast(cudaStream_t s, const GridDev &g, const AnSub *subs, in
 }
 
 void launch_maps_to_f32(cudaStream_t s, const long long *in, const int *fix_exp, const int *uidx, const int *ubase,
-                        int nu, long long per_member, float scale, float *out) {
+                        int nu, long long per_member, float scale, float *out, int *ptab, const ProfBox &box) {
     if (nu == 0 || per_member == 0) return;
+    const int nbx = (box.bx + 7) / 8, nblk = nbx * ((box.by + 7) / 8);
+    if (ptab) {
+        const long long n = (long long)nu * nblk;
+        k_ptab_init<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(ptab, ubase, nu, nblk);
+    }
     dim3 grid((unsigned)std::min<long long>((per_member + 255) / 256, 1024), nu);
-    k_maps_to_f32<<<grid, 256, 0, s>>>(in, fix_exp, uidx, ubase, per_member, scale, out);
+    k_maps_to_f32<<<grid, 256, 0, s>>>(in, fix_exp, uidx, ubase, per_member, scale, out, ptab, nblk, nbx, box.nrp,
+                                       box.bx);
 }
 
 void launch_prof_gather(cudaStream_t s, const double *xu, const int *stu, const int *prof_of, int nb, int n, double *x,
@@ -707,24 +755,24 @@ int prof_gram_tiles(int npix_used) { return (npix_used + GRAM_TP - 1) / GRAM_TP;
 template <class T>
 static void prof_gram(cudaStream_t s, const T *K, const ProfBox &box, const int *pix, const double *wpix,
                       const double *wy, int npix_used, const int *ent_i, const int *ent_j, int nent, int nb,
-                      double *part, double *gh) {
+                      double *part, double *gh, KRows kr) {
     const int nt = prof_gram_tiles(npix_used);
     if (nb == 0 || nt == 0) return;
     const size_t smem = (size_t)(2 * GRAM_TP * box.nrp + GRAM_TP) * sizeof(double) + 2 * GRAM_TP * sizeof(int);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_prof_gram<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_prof_gram<T><<<dim3(nt, nb), 256, smem, s>>>(K, box, pix, wpix, wy, npix_used, ent_i, ent_j, nent, part);
-    k_prof_gram_reduce<<<dim3((nent + 127) / 128, nb), 128, 0, s>>>(part, nt, nent, gh);
+    k_prof_gram<T><<<dim3(nt, nb), 256, smem, s>>>(K, box, pix, wpix, wy, npix_used, ent_i, ent_j, nent, part, kr);
+    k_prof_gram_reduce<<<dim3((nent + 127) / 128, nb), 128, 0, s>>>(part, nt, nent, gh, kr.ktab ? kr.gflag : nullptr);
 }
 
 void launch_prof_gram(cudaStream_t s, const float *K, const ProfBox &box, const int *pix, const double *wpix,
                       const double *wy, int npix_used, const int *ent_i, const int *ent_j, int nent, int nb,
-                      double *part, double *gh) {
-    prof_gram<float>(s, K, box, pix, wpix, wy, npix_used, ent_i, ent_j, nent, nb, part, gh);
+                      double *part, double *gh, KRows kr) {
+    prof_gram<float>(s, K, box, pix, wpix, wy, npix_used, ent_i, ent_j, nent, nb, part, gh, kr);
 }
 
 void launch_prof_gram64(cudaStream_t s, const double *A, const ProfBox &box, const double *b, int m, const int *ent_i,
                         const int *ent_j, int nent, double *part, double *gh) {
-    prof_gram<double>(s, A, box, nullptr, nullptr, b, m, ent_i, ent_j, nent, 1, part, gh);
+    prof_gram<double>(s, A, box, nullptr, nullptr, b, m, ent_i, ent_j, nent, 1, part, gh, KRows{});
 }
 
 size_t prof_solve_smem(int n) { return (size_t)(3 * n * n + 6 * n + 8) * sizeof(double) + (size_t)(4 * n + 8) * sizeof(int); }
