@@ -137,9 +137,9 @@ def step_rows(rings, batch):
 TRAFFIC = {"mc_deposit": "k_mc_deposit_px.global160_b161.dram.txt"}
 
 
-def measured_traffic(kernel, batch):
-    """DRAM bytes (read + write) of one launch of the kernel at this batch, from its committed ncu summary, or
-    None (not captured at this batch)."""
+def measured_traffic(kernel, batch, members=None):
+    """DRAM bytes (read + write) of one launch of the kernel at this batch (and number of members in the
+    launch), from its committed ncu summary, or None (not captured at this batch)."""
     name = TRAFFIC.get(kernel)
     if not name:
         return None
@@ -150,7 +150,9 @@ def measured_traffic(kernel, batch):
                 if "=" in line and not line.startswith(" "):
                     k, v = line.split("=", 1)
                     vals[k.strip()] = v.strip()
-        return int(vals["traffic_bytes_per_launch"]) if int(vals["batch"]) == batch else None
+        if int(vals["batch"]) != batch or (members is not None and int(vals.get("members", -1)) != members):
+            return None
+        return int(vals["traffic_bytes_per_launch"])
     except (OSError, KeyError, ValueError):
         return None
 
@@ -306,7 +308,8 @@ def main():
         nbytes = alg["mc_deposit"][1] if dom == "mc_deposit" else alg["conv_bytes"]
         achieved = nbytes / (kt[dom] * 1e-3) / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                "traffic": measured_traffic(dom, B), "kernel": dom, "peak_source": src,
+                "traffic": measured_traffic(dom, B, mc_full if dom == "mc_deposit" else None), "kernel": dom,
+                "peak_source": src,
                 "algorithmic_bytes": nbytes}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
