@@ -95,7 +95,7 @@ def load(path=None):
         "bbgpu_last_run_times": (i, [vp, vp, i]),
         "bbgpu_kernel_name": (C.c_char_p, [i]),
         "bbgpu_transfer_bytes": (i, [vp, vp, vp]),
-        "bbgpu_shared_members": (i, [vp, vp, vp, vp]),
+        "bbgpu_shared_members": (i, [vp, vp, vp, vp, vp]),
         "bbgpu_sumsq_residuals_noalloc": (i, [vp, vp, vp, i, vp, i, i, i, d, d, vp, vp]),
         "bbgpu_set_profile": (i, [vp, i, i, i, i, i, vp, vp, vp, vp, d, d, d, d]),
         "bbgpu_eval_upload_profile": (i, [vp, i, vp, vp, vp]),
@@ -148,10 +148,11 @@ class Context:
         return int(self.L.bbgpu_launch_count(self.h))
 
     def shared_members(self):
-        """(profiles computed, MC members with all their clouds, MC members as a difference) of the last batch."""
-        a, b, c = (C.c_int(0) for _ in range(3))
-        self.check(self.L.bbgpu_shared_members(self.h, C.byref(a), C.byref(b), C.byref(c)))
-        return a.value, b.value, c.value
+        """(profiles computed, MC members with all their clouds, MC members as a difference, MC members replaying
+        member 0's clouds) of the last batch."""
+        a, b, c, d = (C.c_int(0) for _ in range(4))
+        self.check(self.L.bbgpu_shared_members(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
+        return a.value, b.value, c.value, d.value
 
     def run_times(self):
         t = np.zeros(16)

@@ -33,6 +33,7 @@ static const char *KNAMES[NTIMER] = {"prof_maps", "prof_conv",  "prof_gram",  "p
 struct LayoutEntry {
     LayoutHost host;
     LayoutDev dev;
+    double zspan = 0.0;           // largest spread (max - min) of one cloud's normal deviates
     bool valid = false;
     long long last_use = 0;
 };
@@ -143,7 +144,14 @@ struct bbgpu_ctx {
     // launches (mc_n1 members with their own lists, then mc_n2 holding the difference from member 0's model,
     // whose fixed-point sums are kept in d_base64); rebuilt before a run when mc_dirty
     bool mc_dirty = true;
-    int mc_nseg = 0, mc_n1 = 0, mc_n2 = 0;
+    int mc_nseg = 0, mc_n1 = 0, mc_n2 = 0, mc_n3 = 0;   // (mc_n3: the members replaying member 0's clouds)
+    std::vector<signed char> mc_same_nd;   // per (member, sub-ring): member 0's column but for the density
+    std::vector<unsigned long long> h_chg; // per member: the sub-rings a replaying member deposits itself
+    int nchw = 0;
+    int *d_rp_c0 = nullptr;
+    uint32_t *d_rp_cnt = nullptr;
+    unsigned long long *d_chg = nullptr;
+    size_t d_rp_c0_cap = 0, d_rp_cnt_cap = 0, d_chg_cap = 0;
     long long mc_ntot = 0;
     std::vector<long long> h_cstart;
     std::vector<int> h_cseg, h_klist;
@@ -316,6 +324,7 @@ static int upload_layout(bbgpu_ctx *ctx, LayoutEntry &E) {
                 idx[i] = i;
             }
             std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return desc ? val[a] > val[b] : val[a] < val[b]; });
+            if (nv > 0) E.zspan = std::max(E.zspan, fabs(val[idx[nv - 1]] - val[idx[0]]));
             long long b0 = pbase[ir] + (long long)(c - H.cloud_base[ir]) * ((nv + 3) & ~3);
             for (int i = 0; i < nv; i++) {
                 nf[b0 + i] = (float)val[idx[i]];
@@ -454,7 +463,8 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
                     (void *)ctx->d_pmem, (void *)ctx->d_mstart, (void *)ctx->d_mseg, (void *)ctx->d_uidx,
                     (void *)ctx->d_ubase, (void *)ctx->d_prof_of, (void *)ctx->d_pstatu, (void *)ctx->d_pxu,
                     (void *)ctx->d_cstart, (void *)ctx->d_base64, (void *)ctx->d_cseg, (void *)ctx->d_klist,
-                    (void *)ctx->d_tsrc, (void *)ctx->d_blk, (void *)ctx->d_ktab, (void *)ctx->d_gflag})
+                    (void *)ctx->d_tsrc, (void *)ctx->d_blk, (void *)ctx->d_ktab, (void *)ctx->d_gflag,
+                    (void *)ctx->d_rp_c0, (void *)ctx->d_rp_cnt, (void *)ctx->d_chg})
         cudaFree(q);
     for (void *q : {(void *)ctx->d_asub, (void *)ctx->d_asbase, (void *)ctx->d_assub, (void *)ctx->d_acs,
                     (void *)ctx->d_azq, (void *)ctx->d_awq, (void *)ctx->d_model_fx, (void *)ctx->d_acsf,
@@ -493,12 +503,14 @@ extern "C" int bbgpu_last_run_times(const bbgpu_ctx *ctx, double *times, int n) 
 
 extern "C" const char *bbgpu_kernel_name(int i) { return (i >= 0 && i < NTIMER) ? KNAMES[i] : ""; }
 
-extern "C" int bbgpu_shared_members(const bbgpu_ctx *ctx, int *profiles, int *mc_full, int *mc_delta) {
+extern "C" int bbgpu_shared_members(const bbgpu_ctx *ctx, int *profiles, int *mc_full, int *mc_delta,
+                                    int *mc_replay) {
     if (!ctx) return BBGPU_ERR_ARG;
     const bool mc = ctx->galmodtype == BBGPU_MC && !ctx->mc_dirty;
     if (profiles) *profiles = ctx->prof_uploaded ? ctx->nu : 0;
-    if (mc_full) *mc_full = mc ? (ctx->mc_n1) : 0;
+    if (mc_full) *mc_full = mc ? ctx->mc_n1 : 0;
     if (mc_delta) *mc_delta = mc ? ctx->mc_n2 : 0;
+    if (mc_replay) *mc_replay = mc ? ctx->mc_n3 : 0;
     return BBGPU_OK;
 }
 
@@ -881,6 +893,12 @@ static int batch_prepare(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const
         SubMC *S = ctx->h_sub + (size_t)k * nsub;
         int e = bbh_submc(sr + (size_t)k * BBGPU_NSR * nsub, nsub, nc0.data(), nv0.data(), &g, S,
                           k ? sr : nullptr, k ? ctx->h_sub : nullptr, k ? ctx->h_reuse + (size_t)k * nsub : nullptr);
+        if (k == 0) ctx->mc_same_nd.assign((size_t)nb * nsub, 1);
+        else
+            for (int ir = 0; ir < nsub; ir++)
+                if (!ctx->h_reuse[(size_t)k * nsub + ir])
+                    ctx->mc_same_nd[(size_t)k * nsub + ir] =
+                        bbh_mc_column_same_but_dens(sr + (size_t)k * BBGPU_NSR * nsub, sr, nsub, ir) ? 1 : 0;
         MemberDev &M = ctx->mem_host[k];
         if ((rc = member_desc(ctx, k, d, e, need_cube, M))) return rc;
         M.ntx = (M.bx + ctx->tx - 1) / ctx->tx;
@@ -1017,8 +1035,15 @@ static int mc_segments(bbgpu_ctx *ctx) {
     const bool can = ctx->share && nb > 1 && mc_deposit_shares(ctx->lean, ctx->want64, ctx->tx, ctx->ty) &&
                      (!ctx->prof_uploaded || (int)ctx->prof_of_host.size() == nb);
     const MemberDev &M0 = ctx->mem_host[0];
-    std::vector<int> dl;
+    std::vector<int> dl, rl;
     ctx->mc_isdelta.assign(nb, 0);
+    // replay: the spread of a cloud's channels within the window (the layout's largest spread of normals times
+    // member 0's channels per unit normal)
+    double sgmax = 0.0;
+    for (int ir = 0; ir < nsub; ir++) sgmax = std::max(sgmax, (double)fabsf(ctx->h_sub[ir].sg[0]));
+    const bool rp_ok = can && ctx->cur->zspan * sgmax + 3.0 < (double)RP_W;
+    ctx->nchw = (nsub + 63) / 64;
+    ctx->h_chg.assign((size_t)nb * (ctx->nchw ? ctx->nchw : 1), 0ULL);
     for (int k = 0; k < nb; k++) {
         if (can && k > 0) {
             const MemberDev &M = ctx->mem_host[k];
@@ -1040,13 +1065,33 @@ static int mc_segments(bbgpu_ctx *ctx) {
                     continue;
                 }
             }
+            const bool box = M.blo0 == M0.blo0 && M.blo1 == M0.blo1 && M.bx == M0.bx && M.by == M0.by;
+            if (rp_ok && box) {
+                // member 0's clouds but for the flux, except in a few sub-rings (which it deposits itself)
+                const signed char *sn = ctx->mc_same_nd.data() + (size_t)k * nsub;
+                long long nch = 0;
+                for (int ir = 0; ir < nsub; ir++)
+                    if (!sn[ir]) nch += L.nc[ir];
+                if (2 * nch < ncl) {
+                    unsigned long long *cm = ctx->h_chg.data() + (size_t)k * ctx->nchw;
+                    for (int ir = 0; ir < nsub; ir++)
+                        if (!sn[ir]) {
+                            seg(k, k, L.cloud_base[ir], 1, L.nc[ir]);
+                            cm[ir >> 6] |= 1ULL << (ir & 63);
+                        }
+                    rl.push_back(k);
+                    continue;
+                }
+            }
         }
         seg(k, k, 0, 1, ncl);
         kl.push_back(k);
     }
     ctx->mc_n1 = (int)kl.size();
     ctx->mc_n2 = (int)dl.size();
+    ctx->mc_n3 = (int)rl.size();
     kl.insert(kl.end(), dl.begin(), dl.end());
+    kl.insert(kl.end(), rl.begin(), rl.end());
     cs.push_back(tot);
     ctx->mc_nseg = (int)cs.size() - 1;
     ctx->mc_ntot = tot;
@@ -1058,6 +1103,14 @@ static int mc_segments(bbgpu_ctx *ctx) {
         ((rc = dgrow(ctx, &ctx->d_base64, &ctx->d_base64_cap, (size_t)M0.bx * M0.by * ctx->g.nz + 1)) ||
          (rc = dgrow(ctx, &ctx->d_tsrc, &ctx->d_tsrc_cap, (size_t)ctx->ntile_total + 1))))
         return rc;
+    if (ctx->mc_n3) {
+        if ((rc = dgrow(ctx, &ctx->d_rp_c0, &ctx->d_rp_c0_cap, (size_t)ncl + 1)) ||
+            (rc = dgrow(ctx, &ctx->d_rp_cnt, &ctx->d_rp_cnt_cap, (size_t)ncl * (RP_W / 4) + 1)) ||
+            (rc = dgrow(ctx, &ctx->d_chg, &ctx->d_chg_cap, ctx->h_chg.size())))
+            return rc;
+        CK(cudaMemcpyAsync(ctx->d_chg, ctx->h_chg.data(), sizeof(unsigned long long) * ctx->h_chg.size(),
+                           cudaMemcpyHostToDevice, ctx->stream));
+    }
     cudaStream_t s = ctx->stream;
     CK(cudaMemcpyAsync(ctx->d_cstart, cs.data(), sizeof(long long) * cs.size(), cudaMemcpyHostToDevice, s));
     if (!sg.empty()) CK(cudaMemcpyAsync(ctx->d_cseg, sg.data(), sizeof(int) * sg.size(), cudaMemcpyHostToDevice, s));
@@ -1114,18 +1167,31 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
                           ctx->mc_ntot, ctx->tx, ctx->ty, ctx->d_pix, ctx->d_tcur, ctx->d_bucket);
         CKL();
         if (tm) CK(cudaEventRecord(ctx->ev[7], s));
-        if (ctx->mc_n2) {
+        if (ctx->mc_n2 || ctx->mc_n3) {
             launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->tx,
                               ctx->ty, ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig, ctx->d_cd2if,
                               ctx->d_cd2i, ctx->d_model, ctx->mstride, nullptr, ctx->d_err, ctx->lean, ctx->d_klist,
-                              ctx->mc_n1, 0, ctx->d_base64, ctx->d_tsrc);
+                              ctx->mc_n1, 0, ctx->mc_n2 ? ctx->d_base64 : nullptr, ctx->mc_n2 ? ctx->d_tsrc : nullptr);
             CKL();
             if (tm) CK(cudaEventRecord(ctx->ev[8], s));
-            launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->tx,
-                              ctx->ty, ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig, ctx->d_cd2if,
-                              ctx->d_cd2i, ctx->d_model, ctx->mstride, nullptr, ctx->d_err, ctx->lean,
-                              ctx->d_klist + ctx->mc_n1, ctx->mc_n2, 1, ctx->d_base64, ctx->d_tsrc);
-            CKL();
+            if (ctx->mc_n2) {
+                launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb,
+                                  ctx->tx, ctx->ty, ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig,
+                                  ctx->d_cd2if, ctx->d_cd2i, ctx->d_model, ctx->mstride, nullptr, ctx->d_err,
+                                  ctx->lean, ctx->d_klist + ctx->mc_n1, ctx->mc_n2, 1, ctx->d_base64, ctx->d_tsrc);
+                CKL();
+            }
+            if (ctx->mc_n3) {
+                launch_cloud_hist(s, g, L, ctx->d_sub, ctx->d_zig, ctx->d_rp_c0, ctx->d_rp_cnt, ctx->d_err);
+                CKL();
+                launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb,
+                                  ctx->tx, ctx->ty, ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig,
+                                  ctx->d_cd2if, ctx->d_cd2i, ctx->d_model, ctx->mstride, nullptr, ctx->d_err,
+                                  ctx->lean, ctx->d_klist + ctx->mc_n1 + ctx->mc_n2, ctx->mc_n3, 2, nullptr,
+                                  ctx->mc_n2 ? ctx->d_tsrc : nullptr,
+                                  Replay{ctx->d_rp_c0, ctx->d_rp_cnt, ctx->d_chg, ctx->nchw});
+                CKL();
+            }
             if (tm) CK(cudaEventRecord(ctx->ev[9], s));
         } else {
             launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->tx,

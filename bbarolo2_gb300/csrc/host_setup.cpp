@@ -273,6 +273,12 @@ static bool same_column(const double *a, const double *b, int nsub, int ir) {
     return true;
 }
 
+bool bbh_mc_column_same_but_dens(const double *a, const double *b, int nsub, int ir) {
+    for (int r = 0; r < BBGPU_NSR; r++)
+        if (r != 5 && memcmp(a + (size_t)r * nsub + ir, b + (size_t)r * nsub + ir, sizeof(double))) return false;
+    return true;
+}
+
 bool bbh_map_column_same(const double *a, const double *b, int nsub, int ir) {
     auto same = [&](int r) { return !memcmp(a + (size_t)r * nsub + ir, b + (size_t)r * nsub + ir, sizeof(double)); };
     for (int r : {0, 6, 7, 9, 10, 11, 12, 14, 15})

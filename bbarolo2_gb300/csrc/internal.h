@@ -143,6 +143,9 @@ int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0,
 // centre and side weights, and the same dispersion where a velocity gradient makes the vertical grid depend
 // on it (the velocities and the density do not enter a ring map)
 bool bbh_map_column_same(const double *a, const double *b, int nsub, int ir);
+// true if sub-ring ir of the MC tables a and b differs at most in the density (row 5): the same clouds, at the
+// same pixels and channels, with another flux
+bool bbh_mc_column_same_but_dens(const double *a, const double *b, int nsub, int ir);
 // The second-difference prior of the deconvolved profile at the radii R (n) (bbarolo/profile.py:60-151):
 // rows (n - 2) x 3 columns lc and weights lv, the order of the radii, the "near" rows, the median ring
 // distance d and the norm of the relative prior

@@ -74,12 +74,27 @@ void launch_mc_scatter(cudaStream_t s, const LayoutDev &L, const SubMC *sub, int
 // the member whose model holds tile t of the member (itself, or 0 for a tile left unwritten).
 #define ERR_SHARE 8
 bool mc_deposit_shares(int lean, bool model64, int tx, int ty);
+// delta = 2 (replay): the member's clouds in the sub-rings not marked in chg (nchw 64-bit words a member) are
+// member 0's clouds with the member's flux: the deposit adds member 0's channel counts of them (c0, cnt: the
+// window of RP_W channels of every cloud, k_cloud_hist) times the member's fixed-point flux; its own lists hold
+// the clouds of the marked sub-rings.
+#define RP_W 64
+struct Replay {
+    const int *c0;
+    const uint32_t *cnt;
+    const unsigned long long *chg;
+    int nchw;
+};
+// the channel windows of member 0's clouds (sub0: member 0's sub-ring constants): c0 (ncloud), cnt (ncloud x
+// RP_W / 4 words of byte counts)
+void launch_cloud_hist(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub0, const ZigDev *zig,
+                       int *c0, uint32_t *cnt, int *err);
 void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
                        const MemberDev *mem, const MemberDev *mem_host, int nb, int tx, int ty,
                        const int *offset, const int *count, const void *bucket, const ZigDev *zig,
                        const float *cd2if, const double *cd2i, float *model, long long mstride, double *model64,
                        int *err, int lean, const int *klist = nullptr, int nk = 0, int delta = 0,
-                       long long *base64 = nullptr, int *tsrc = nullptr);
+                       long long *base64 = nullptr, int *tsrc = nullptr, Replay rp = Replay{nullptr, nullptr, nullptr, 0});
 
 // ---- convolution + residual (conv.cu)
 // The taps of a beam kernel (ky, kx) as the conv kernels read them: flipped, float32, rows padded to the

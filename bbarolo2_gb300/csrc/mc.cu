@@ -945,6 +945,50 @@ __device__ __forceinline__ void px_count(const GridDev &g, const LayoutDev &L, c
 #ifndef PX_MINB
 #define PX_MINB 3         // resident CTAs per SM
 #endif
+// The channels of member 0's clouds, for the members that differ from it only in the flux of most sub-rings
+// (k_mc_deposit_px, delta = 2): a warp per cloud takes its samples' exact channels as the deposit does (float32
+// within the cloud's rounding bound, else the reference's float64 operations), c0 = the channel of the first
+// sorted sample (the channels do not decrease along the sorted samples), and the counts of the channels
+// c0 .. c0 + RP_W - 1 in bytes (at most 128 samples a cloud); a channel past the window raises ERR_SHARE (the host
+// bounds the spread of a cloud's channels below RP_W).
+__global__ void k_cloud_hist(GridDev g, LayoutDev L, const SubMC *__restrict__ sub0, const ZigDev *__restrict__ zig,
+                             int *__restrict__ c0out, uint32_t *__restrict__ cnt, int *err) {
+    __shared__ uint32_t h[8][RP_W / 4];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (c >= L.ncloud) return;
+    const int ir = __ldg(&L.sub[c]);
+    const SubMC &S = sub0[ir];
+    const int nv = __ldg(&L.nvs[ir]);
+    const int pb = (int)(L.pbase[ir] + (long long)(c - L.cloud_base[ir]) * ((nv + 3) & ~3));
+    float tc, epsc;
+    cloud_centre(S, L.cf[c], 0, tc, epsc);
+    const float sg = S.sg[0];
+    const float nmax = fmaxf(fabsf(__ldg(&L.nf[pb])), fabsf(__ldg(&L.nf[pb + nv - 1])));
+    const float eps = fmaf(nmax, fabsf(sg) * EPS_REL, epsc);
+    const bool fastc = fabsf(tc) < 1.0e5f;
+    const float hw = 0.5f - eps, tc5 = tc + 0.5f;
+    auto chan = [&](int i) -> int {
+        const float f = fmaf(__ldg(&L.nf[pb + i]), sg, tc5);
+        const float fl = floorf(f);
+        if (fastc && fabsf(f - fl - 0.5f) <= hw) return (int)fl;
+        return px_exact(g, L, zig, sub0, (int)c, pb, nv, i, err);
+    };
+    int first = 0;
+    if (lane == 0) first = chan(0);
+    const int cf0 = __shfl_sync(0xffffffffu, first, 0);
+    if (lane < RP_W / 4) h[warp][lane] = 0;
+    __syncwarp();
+    for (int i = lane; i < nv; i += 32) {
+        const int d = chan(i) - cf0;
+        if ((unsigned)d < (unsigned)RP_W) atomicAdd(&h[warp][d >> 2], 1u << (8 * (d & 3)));
+        else atomicOr(err, ERR_SHARE);
+    }
+    __syncwarp();
+    if (lane < RP_W / 4) cnt[(size_t)c * (RP_W / 4) + lane] = h[warp][lane];
+    if (lane == 0) c0out[c] = cf0;
+}
+
 template <int SPL>
 __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, LayoutDev L, const SubMC *__restrict__ sub,
                                                               int nsub, const MemberDev *__restrict__ mem, int tx,
@@ -956,7 +1000,7 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
                                                               float *__restrict__ model, long long mstride,
                                                               const int *__restrict__ klist, int delta,
                                                               unsigned long long *__restrict__ base64,
-                                                              int *__restrict__ tsrc, int *err) {
+                                                              int *__restrict__ tsrc, Replay rp, int *err) {
     constexpr int LPP = 128 / SPL;
     extern __shared__ unsigned long long tile[];           // TP rows of fixed-point sums, queues, nz scales
     __shared__ unsigned long long inc[32];                 // the histogram increments of px_count
@@ -966,7 +1010,8 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
     // are in base64, and a tile without entries is left unwritten (tsrc points the convolution to member 0's
     // model there); else member 0 (with base64) leaves its sums there
     unsigned long long *wbase = !delta && k == 0 ? base64 : nullptr;
-    if (delta && threadIdx.x == 0 && blockIdx.y == 0 && mem[k].fix_exp != mem[0].fix_exp) atomicOr(err, ERR_SHARE);
+    if (delta == 1 && threadIdx.x == 0 && blockIdx.y == 0 && mem[k].fix_exp != mem[0].fix_exp)
+        atomicOr(err, ERR_SHARE);
     const int ntx = mem[k].ntx;
     if (t >= ntx * mem[k].nty) return;
     if (threadIdx.x < 32) inc[threadIdx.x] = threadIdx.x < 11 ? 1ull << (5 * threadIdx.x) : (threadIdx.x < 31 ? 1ull << 55 : 0ull);
@@ -977,14 +1022,16 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
     const int x0 = txi * tx, y0 = tyi * ty;
     const int bx = mem[k].bx, by = mem[k].by;
     const int lbase = (mem[k].tile_off + t) * NOWN;
+    const int lbase0 = (mem[0].tile_off + t) * NOWN;       // (replay: member 0's lists of the same tile)
+    const bool replay = delta == 2;
     float *mout = model + (size_t)k * mstride;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     {
         int any = 0;
-        if (threadIdx.x < NOWN) any = count[lbase + threadIdx.x] != 0;
+        if (threadIdx.x < NOWN) any = count[lbase + threadIdx.x] != 0 || (replay && count[lbase0 + threadIdx.x] != 0);
         if (!__syncthreads_or(any)) {
-            if (tsrc && threadIdx.x == 0) tsrc[mem[k].tile_off + t] = delta ? 0 : k;
-            if (delta) return;
+            if (tsrc && threadIdx.x == 0) tsrc[mem[k].tile_off + t] = delta == 1 ? 0 : k;
+            if (delta == 1) return;
             for (int lp = warp; lp < TP; lp += 8) {
                 const int py = y0 + lp / tx, px = x0 + lp % tx;
                 if (py >= by || px >= bx) continue;
@@ -1019,6 +1066,38 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
     PxDefer *qe = qall + warp * PX_QCAP;
     int *qn = qns + warp;
     const SubMC *__restrict__ subk = sub + (size_t)k * nsub;
+    if (replay) {
+        // member 0's clouds of the pixel in the sub-rings where the member is member 0 but for the flux: their
+        // channel counts (k_cloud_hist) times the member's fixed-point flux; lane q of the group takes the
+        // channels c0 + RP_W / LPP q .. of the window
+        constexpr int CPL = RP_W / LPP, WPL = CPL / 4;      // channels, 32-bit words of counts per lane
+        const unsigned long long *chg = rp.chg + (size_t)k * rp.nchw;
+        unsigned long long *row = tile + rowoff;
+        const int beg0 = own ? offset[lbase0 + 8 * warp + grp] : 0;
+        const int n0 = own ? count[lbase0 + 8 * warp + grp] : 0;
+        const int nj0 = __reduce_max_sync(0xffffffffu, n0);
+        for (int j = 0; j < nj0; j++) {
+            if (j < n0) {
+                const int c = __ldg(&bucket[beg0 + j].c), meta = __ldg(&bucket[beg0 + j].meta);
+                const int ir = __ldg(&L.sub[c]);
+                if (!((__ldg(&chg[ir >> 6]) >> (ir & 63)) & 1ull)) {
+                    const long long fix = subk[ir].fix[(meta >> 24) & 1][0];
+                    const int cb = __ldg(&rp.c0[c]) + CPL * q;
+                    const uint32_t *cw = rp.cnt + (size_t)c * (RP_W / 4) + WPL * q;
+#pragma unroll
+                    for (int w = 0; w < WPL; w++) {
+                        const uint32_t v = __ldg(&cw[w]);
+#pragma unroll
+                        for (int b = 0; b < 4; b++) {
+                            const int cnt = (v >> (8 * b)) & 255, ch = cb + 4 * w + b;
+                            if (cnt && (unsigned)ch < (unsigned)nz) row[ch] += (unsigned long long)(fix * (long long)cnt);
+                        }
+                    }
+                }
+            }
+        }
+        __syncwarp();
+    }
     const int nj = __reduce_max_sync(0xffffffffu, n);
     const int i0 = SPL * q;                                 // this lane's samples: i0 .. min(i0 + SPL, nv) - 1
     // software pipeline: the samples of the next cloud and the entry after it are loaded during a count
@@ -1048,7 +1127,7 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
         const unsigned long long *src = tile + (size_t)p * RS + 2 * (p >> 3);
         const size_t v0 = ((size_t)py * bx + px) * nz;
         float *o = mout + v0;
-        if (delta) {
+        if (delta == 1) {
             for (int z = lane; z < nz; z += 32) o[z] = ll_to_f32((long long)(src[z] + base64[v0 + z])) * chs[z];
         } else {
             for (int z = lane; z < nz; z += 32) o[z] = ll_to_f32((long long)src[z]) * chs[z];
@@ -1160,6 +1239,13 @@ __global__ void k_scan_c(const int *__restrict__ count, int n, const int *__rest
 
 }  // namespace
 
+void launch_cloud_hist(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub0, const ZigDev *zig,
+                       int *c0, uint32_t *cnt, int *err) {
+    if (L.ncloud == 0) return;
+    const long long nt = 32LL * L.ncloud;
+    k_cloud_hist<<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(g, L, sub0, zig, c0, cnt, err);
+}
+
 void launch_mc_bin(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
                    const MemberDev *mem, const long long *cstart, const int *cseg, int nseg, long long ntot, int tx,
                    int ty, int *pix, int *tile_count, int *err) {
@@ -1208,7 +1294,8 @@ void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, con
                        const MemberDev *mem, const MemberDev *mem_host, int nb, int tx, int ty,
                        const int *offset, const int *count, const void *bucket, const ZigDev *zig,
                        const float *cd2if, const double *cd2i, float *model, long long mstride, double *model64,
-                       int *err, int lean, const int *klist, int nk, int delta, long long *base64, int *tsrc) {
+                       int *err, int lean, const int *klist, int nk, int delta, long long *base64, int *tsrc,
+                       Replay rp) {
     int maxt = 0;
     for (int k = 0; k < nb; k++) maxt = max(maxt, mem_host[k].ntx * mem_host[k].nty);
     if (maxt == 0 || nb == 0 || (klist && nk == 0)) return;
@@ -1234,11 +1321,11 @@ void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, con
             if (TP == 64)
                 k_mc_deposit_px<32><<<grid, 256, smem_px, s>>>(g, L, sub, nsub, mem, tx, ty, offset, count,
                                                                (const Entry *)bucket, zig, cd2if, model, mstride,
-                                                               klist, delta, b64, tsrc, err);
+                                                               klist, delta, b64, tsrc, rp, err);
             else
                 k_mc_deposit_px<16><<<grid, 256, smem_px, s>>>(g, L, sub, nsub, mem, tx, ty, offset, count,
                                                                (const Entry *)bucket, zig, cd2if, model, mstride,
-                                                               klist, delta, b64, tsrc, err);
+                                                               klist, delta, b64, tsrc, rp, err);
             return;
         }
         k_mc_deposit_lean<<<grid, 256, smem, s>>>(g, L, sub, nsub, mem, tx, ty, offset, count, (const Entry *)bucket,

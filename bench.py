@@ -297,7 +297,7 @@ def main():
     ctx.check(ctx.L.bbgpu_eval_upload_profile(ctx.h, ms.shape[2], _lib.ptr(ms), _lib.ptr(L._prof["widx"]),
                                               _lib.ptr(L._prof["wval"])))
     ctx.check(ctx.L.bbgpu_eval_run(ctx.h))
-    nprof, mc_full, mc_delta = ctx.shared_members()
+    nprof, mc_full, mc_delta, mc_replay = ctx.shared_members()
     alg = algorithmic(dm, L, sr, nv, descs, mc_full)
     dom = max((k for k in kt if not k.startswith("prof_")), key=kt.get)   # (the MC model and its convolution)
     if dom == "conv_resid":
@@ -321,7 +321,7 @@ def main():
                                              "maps, beam, weighted NNLS with the smoothness prior), as the reference "
                                              "with DENS not fitted and the geometry free",
                        "shared": {"profiles_computed": nprof, "mc_members_full": mc_full,
-                                  "mc_members_difference": mc_delta,
+                                  "mc_members_difference": mc_delta, "mc_members_replay": mc_replay,
                                   "note": "members equal to the first but for a few sub-rings are computed as its "
                                           "result plus the exact difference (bit-identical; 'unshared' below "
                                           "computes every member in full)"}},

@@ -183,8 +183,9 @@ const char *bbgpu_kernel_name(int i);
 /* Bytes copied host -> device and device -> host by the last bbgpu_eval_upload / bbgpu_eval_download. */
 int bbgpu_transfer_bytes(const bbgpu_ctx *ctx, int64_t *h2d, int64_t *d2h);
 /* How the last batch was shared (option 3): profiles computed (rows of ring maps), MC members that deposited all
- * their clouds, MC members computed as a difference from the first member's model. */
-int bbgpu_shared_members(const bbgpu_ctx *ctx, int *profiles, int *mc_full, int *mc_delta);
+ * their clouds, MC members computed as a difference from the first member's model, MC members that replayed the
+ * first member's clouds with their own flux. */
+int bbgpu_shared_members(const bbgpu_ctx *ctx, int *profiles, int *mc_full, int *mc_delta, int *mc_replay);
 
 #ifdef __cplusplus
 }
