@@ -148,7 +148,7 @@ struct bbgpu_ctx {
     std::vector<signed char> mc_same_nd;   // per (member, sub-ring): member 0's column but for the density
     std::vector<unsigned long long> h_chg; // per member: the sub-rings a replaying member deposits itself
     int nchw = 0;
-    int *d_rp_c0 = nullptr;
+    int *d_rp_c0 = nullptr;               // (2 ints a record of member 0's entries)
     uint32_t *d_rp_cnt = nullptr;
     unsigned long long *d_chg = nullptr;
     size_t d_rp_c0_cap = 0, d_rp_cnt_cap = 0, d_chg_cap = 0;
@@ -1104,7 +1104,7 @@ static int mc_segments(bbgpu_ctx *ctx) {
          (rc = dgrow(ctx, &ctx->d_tsrc, &ctx->d_tsrc_cap, (size_t)ctx->ntile_total + 1))))
         return rc;
     if (ctx->mc_n3) {
-        if ((rc = dgrow(ctx, &ctx->d_rp_c0, &ctx->d_rp_c0_cap, (size_t)ncl + 1)) ||
+        if ((rc = dgrow(ctx, &ctx->d_rp_c0, &ctx->d_rp_c0_cap, 2 * (size_t)ncl + 2)) ||
             (rc = dgrow(ctx, &ctx->d_rp_cnt, &ctx->d_rp_cnt_cap, (size_t)ncl * (RP_W / 4) + 1)) ||
             (rc = dgrow(ctx, &ctx->d_chg, &ctx->d_chg_cap, ctx->h_chg.size())))
             return rc;
@@ -1182,14 +1182,16 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
                 CKL();
             }
             if (ctx->mc_n3) {
-                launch_cloud_hist(s, g, L, ctx->d_sub, ctx->d_zig, ctx->d_rp_c0, ctx->d_rp_cnt, ctx->d_err);
+                const MemberDev &M0 = ctx->mem_host[0];
+                launch_cloud_hist(s, g, L, ctx->d_sub, ctx->d_zig, ctx->d_bucket, ctx->d_toff,
+                                  (M0.tile_off + M0.ntx * M0.nty) * NOWN, ctx->d_rp_c0, ctx->d_rp_cnt, ctx->d_err);
                 CKL();
                 launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb,
                                   ctx->tx, ctx->ty, ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig,
                                   ctx->d_cd2if, ctx->d_cd2i, ctx->d_model, ctx->mstride, nullptr, ctx->d_err,
                                   ctx->lean, ctx->d_klist + ctx->mc_n1 + ctx->mc_n2, ctx->mc_n3, 2, nullptr,
                                   ctx->mc_n2 ? ctx->d_tsrc : nullptr,
-                                  Replay{ctx->d_rp_c0, ctx->d_rp_cnt, ctx->d_chg, ctx->nchw});
+                                  Replay{(const int2 *)ctx->d_rp_c0, ctx->d_rp_cnt, ctx->d_chg, ctx->nchw});
                 CKL();
             }
             if (tm) CK(cudaEventRecord(ctx->ev[9], s));

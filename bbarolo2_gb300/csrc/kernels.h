@@ -80,15 +80,16 @@ bool mc_deposit_shares(int lean, bool model64, int tx, int ty);
 // the clouds of the marked sub-rings.
 #define RP_W 64
 struct Replay {
-    const int *c0;
+    const int2 *rec;
     const uint32_t *cnt;
     const unsigned long long *chg;
     int nchw;
 };
-// the channel windows of member 0's clouds (sub0: member 0's sub-ring constants): c0 (ncloud), cnt (ncloud x
-// RP_W / 4 words of byte counts)
+// the channel windows of member 0's clouds in the order of its entries (bucket[0 .. offset[nlist0]), nlist0 =
+// its lists; sub0: its sub-ring constants): rec (2 ints an entry: first channel, sub-ring | half << 16), cnt
+// (RP_W / 4 words of byte counts an entry); room for ncloud entries
 void launch_cloud_hist(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub0, const ZigDev *zig,
-                       int *c0, uint32_t *cnt, int *err);
+                       const void *bucket, const int *offset, int nlist0, int *rec, uint32_t *cnt, int *err);
 void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
                        const MemberDev *mem, const MemberDev *mem_host, int nb, int tx, int ty,
                        const int *offset, const int *count, const void *bucket, const ZigDev *zig,

@@ -946,17 +946,20 @@ __device__ __forceinline__ void px_count(const GridDev &g, const LayoutDev &L, c
 #define PX_MINB 3         // resident CTAs per SM
 #endif
 // The channels of member 0's clouds, for the members that differ from it only in the flux of most sub-rings
-// (k_mc_deposit_px, delta = 2): a warp per cloud takes its samples' exact channels as the deposit does (float32
-// within the cloud's rounding bound, else the reference's float64 operations), c0 = the channel of the first
-// sorted sample (the channels do not decrease along the sorted samples), and the counts of the channels
-// c0 .. c0 + RP_W - 1 in bytes (at most 128 samples a cloud); a channel past the window raises ERR_SHARE (the host
-// bounds the spread of a cloud's channels below RP_W).
+// (k_mc_deposit_px, delta = 2), in the order of member 0's entries (bucket[0 .. offset[nlist0]): member 0's lists
+// come first): a warp per entry takes its cloud's samples' exact channels as the deposit does (float32 within
+// the cloud's rounding bound, else the reference's float64 operations), c0 = the channel of the first sorted
+// sample (the channels do not decrease along the sorted samples), and the counts of the channels c0 .. c0 +
+// RP_W - 1 in bytes (at most 128 samples a cloud): rec[j] = (c0, sub-ring | half << 16), cnt[j] the counts. A
+// channel past the window raises ERR_SHARE (the host bounds the spread of a cloud's channels below RP_W).
 __global__ void k_cloud_hist(GridDev g, LayoutDev L, const SubMC *__restrict__ sub0, const ZigDev *__restrict__ zig,
-                             int *__restrict__ c0out, uint32_t *__restrict__ cnt, int *err) {
+                             const Entry *__restrict__ bucket, const int *__restrict__ offset, int nlist0,
+                             int2 *__restrict__ rec, uint32_t *__restrict__ cnt, int *err) {
     __shared__ uint32_t h[8][RP_W / 4];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (c >= L.ncloud) return;
+    const long long j = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (j >= __ldg(&offset[nlist0])) return;
+    const int c = __ldg(&bucket[j].c), half = (__ldg(&bucket[j].meta) >> 24) & 1;
     const int ir = __ldg(&L.sub[c]);
     const SubMC &S = sub0[ir];
     const int nv = __ldg(&L.nvs[ir]);
@@ -972,7 +975,7 @@ __global__ void k_cloud_hist(GridDev g, LayoutDev L, const SubMC *__restrict__ s
         const float f = fmaf(__ldg(&L.nf[pb + i]), sg, tc5);
         const float fl = floorf(f);
         if (fastc && fabsf(f - fl - 0.5f) <= hw) return (int)fl;
-        return px_exact(g, L, zig, sub0, (int)c, pb, nv, i, err);
+        return px_exact(g, L, zig, sub0, c, pb, nv, i, err);
     };
     int first = 0;
     if (lane == 0) first = chan(0);
@@ -985,8 +988,8 @@ __global__ void k_cloud_hist(GridDev g, LayoutDev L, const SubMC *__restrict__ s
         else atomicOr(err, ERR_SHARE);
     }
     __syncwarp();
-    if (lane < RP_W / 4) cnt[(size_t)c * (RP_W / 4) + lane] = h[warp][lane];
-    if (lane == 0) c0out[c] = cf0;
+    if (lane < RP_W / 4) cnt[(size_t)j * (RP_W / 4) + lane] = h[warp][lane];
+    if (lane == 0) rec[j] = make_int2(cf0, ir | (half << 16));
 }
 
 template <int SPL>
@@ -1068,25 +1071,41 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
     const SubMC *__restrict__ subk = sub + (size_t)k * nsub;
     if (replay) {
         // member 0's clouds of the pixel in the sub-rings where the member is member 0 but for the flux: their
-        // channel counts (k_cloud_hist) times the member's fixed-point flux; lane q of the group takes the
-        // channels c0 + RP_W / LPP q .. of the window
+        // channel counts (k_cloud_hist, in the order of member 0's entries) times the member's fixed-point flux;
+        // lane q of the group takes the channels c0 + RP_W / LPP q .. of the window; the next cloud's record
+        // and counts are loaded during the adds
         constexpr int CPL = RP_W / LPP, WPL = CPL / 4;      // channels, 32-bit words of counts per lane
         const unsigned long long *chg = rp.chg + (size_t)k * rp.nchw;
         unsigned long long *row = tile + rowoff;
         const int beg0 = own ? offset[lbase0 + 8 * warp + grp] : 0;
         const int n0 = own ? count[lbase0 + 8 * warp + grp] : 0;
         const int nj0 = __reduce_max_sync(0xffffffffu, n0);
-        for (int j = 0; j < nj0; j++) {
-            if (j < n0) {
-                const int c = __ldg(&bucket[beg0 + j].c), meta = __ldg(&bucket[beg0 + j].meta);
-                const int ir = __ldg(&L.sub[c]);
+        auto load = [&](int jj, int2 &r, uint32_t (&w)[WPL]) {
+            if (jj < n0) {
+                r = __ldg(&rp.rec[beg0 + jj]);
+                const uint32_t *cw = rp.cnt + (size_t)(beg0 + jj) * (RP_W / 4) + WPL * q;
+#pragma unroll
+                for (int x = 0; x < WPL; x++) w[x] = __ldg(&cw[x]);
+            } else {
+                r = make_int2(0, -1);
+            }
+        };
+        int2 ra;
+        uint32_t wa[WPL];
+        load(0, ra, wa);
+        for (int jj = 0; jj < nj0; jj++) {
+            int2 rb;
+            uint32_t wb[WPL];
+            load(jj + 1, rb, wb);
+            if (ra.y >= 0) {
+                const int ir = ra.y & 0xffff;
                 if (!((__ldg(&chg[ir >> 6]) >> (ir & 63)) & 1ull)) {
-                    const long long fix = subk[ir].fix[(meta >> 24) & 1][0];
-                    const int cb = __ldg(&rp.c0[c]) + CPL * q;
-                    const uint32_t *cw = rp.cnt + (size_t)c * (RP_W / 4) + WPL * q;
+                    const long long fix = subk[ir].fix[ra.y >> 16][0];
+                    const int cb = ra.x + CPL * q;
 #pragma unroll
                     for (int w = 0; w < WPL; w++) {
-                        const uint32_t v = __ldg(&cw[w]);
+                        const uint32_t v = wa[w];
+                        if (!v) continue;
 #pragma unroll
                         for (int b = 0; b < 4; b++) {
                             const int cnt = (v >> (8 * b)) & 255, ch = cb + 4 * w + b;
@@ -1095,6 +1114,9 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
                     }
                 }
             }
+            ra = rb;
+#pragma unroll
+            for (int w = 0; w < WPL; w++) wa[w] = wb[w];
         }
         __syncwarp();
     }
@@ -1240,10 +1262,11 @@ __global__ void k_scan_c(const int *__restrict__ count, int n, const int *__rest
 }  // namespace
 
 void launch_cloud_hist(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub0, const ZigDev *zig,
-                       int *c0, uint32_t *cnt, int *err) {
+                       const void *bucket, const int *offset, int nlist0, int *rec, uint32_t *cnt, int *err) {
     if (L.ncloud == 0) return;
     const long long nt = 32LL * L.ncloud;
-    k_cloud_hist<<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(g, L, sub0, zig, c0, cnt, err);
+    k_cloud_hist<<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(g, L, sub0, zig, (const Entry *)bucket, offset, nlist0,
+                                                             (int2 *)rec, cnt, err);
 }
 
 void launch_mc_bin(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
