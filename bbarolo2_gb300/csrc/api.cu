@@ -148,10 +148,10 @@ struct bbgpu_ctx {
     std::vector<signed char> mc_same_nd;   // per (member, sub-ring): member 0's column but for the density
     std::vector<unsigned long long> h_chg; // per member: the sub-rings a replaying member deposits itself
     int nchw = 0;
-    int *d_rp_c0 = nullptr;               // (2 ints a record of member 0's entries)
+    int *d_rp_c0 = nullptr, *d_rp_n = nullptr;   // (2 ints a record; records per list of member 0)
     uint32_t *d_rp_cnt = nullptr;
     unsigned long long *d_chg = nullptr;
-    size_t d_rp_c0_cap = 0, d_rp_cnt_cap = 0, d_chg_cap = 0;
+    size_t d_rp_c0_cap = 0, d_rp_cnt_cap = 0, d_chg_cap = 0, d_rp_n_cap = 0;
     long long mc_ntot = 0;
     std::vector<long long> h_cstart;
     std::vector<int> h_cseg, h_klist;
@@ -464,7 +464,7 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
                     (void *)ctx->d_ubase, (void *)ctx->d_prof_of, (void *)ctx->d_pstatu, (void *)ctx->d_pxu,
                     (void *)ctx->d_cstart, (void *)ctx->d_base64, (void *)ctx->d_cseg, (void *)ctx->d_klist,
                     (void *)ctx->d_tsrc, (void *)ctx->d_blk, (void *)ctx->d_ktab, (void *)ctx->d_gflag,
-                    (void *)ctx->d_rp_c0, (void *)ctx->d_rp_cnt, (void *)ctx->d_chg})
+                    (void *)ctx->d_rp_c0, (void *)ctx->d_rp_cnt, (void *)ctx->d_chg, (void *)ctx->d_rp_n})
         cudaFree(q);
     for (void *q : {(void *)ctx->d_asub, (void *)ctx->d_asbase, (void *)ctx->d_assub, (void *)ctx->d_acs,
                     (void *)ctx->d_azq, (void *)ctx->d_awq, (void *)ctx->d_model_fx, (void *)ctx->d_acsf,
@@ -1105,7 +1105,8 @@ static int mc_segments(bbgpu_ctx *ctx) {
         return rc;
     if (ctx->mc_n3) {
         if ((rc = dgrow(ctx, &ctx->d_rp_c0, &ctx->d_rp_c0_cap, 2 * (size_t)ncl + 2)) ||
-            (rc = dgrow(ctx, &ctx->d_rp_cnt, &ctx->d_rp_cnt_cap, (size_t)ncl * (RP_W / 4) + 1)) ||
+            (rc = dgrow(ctx, &ctx->d_rp_cnt, &ctx->d_rp_cnt_cap, (size_t)ncl * (RP_W / 2) + 1)) ||
+            (rc = dgrow(ctx, &ctx->d_rp_n, &ctx->d_rp_n_cap, (size_t)(M0.ntx * M0.nty) * NOWN + 1)) ||
             (rc = dgrow(ctx, &ctx->d_chg, &ctx->d_chg_cap, ctx->h_chg.size())))
             return rc;
         CK(cudaMemcpyAsync(ctx->d_chg, ctx->h_chg.data(), sizeof(unsigned long long) * ctx->h_chg.size(),
@@ -1183,15 +1184,17 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
             }
             if (ctx->mc_n3) {
                 const MemberDev &M0 = ctx->mem_host[0];
-                launch_cloud_hist(s, g, L, ctx->d_sub, ctx->d_zig, ctx->d_bucket, ctx->d_toff,
-                                  (M0.tile_off + M0.ntx * M0.nty) * NOWN, ctx->d_rp_c0, ctx->d_rp_cnt, ctx->d_err);
+                launch_replay_records(s, g, L, ctx->d_sub, ctx->d_zig, ctx->d_bucket, ctx->d_toff, ctx->d_tcount,
+                                      (M0.tile_off + M0.ntx * M0.nty) * NOWN, ctx->d_rp_c0, ctx->d_rp_cnt,
+                                      ctx->d_rp_n, ctx->d_err);
                 CKL();
                 launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb,
                                   ctx->tx, ctx->ty, ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig,
                                   ctx->d_cd2if, ctx->d_cd2i, ctx->d_model, ctx->mstride, nullptr, ctx->d_err,
                                   ctx->lean, ctx->d_klist + ctx->mc_n1 + ctx->mc_n2, ctx->mc_n3, 2, nullptr,
                                   ctx->mc_n2 ? ctx->d_tsrc : nullptr,
-                                  Replay{(const int2 *)ctx->d_rp_c0, ctx->d_rp_cnt, ctx->d_chg, ctx->nchw});
+                                  Replay{(const int2 *)ctx->d_rp_c0, ctx->d_rp_cnt, ctx->d_rp_n, ctx->d_chg,
+                                         ctx->nchw});
                 CKL();
             }
             if (tm) CK(cudaEventRecord(ctx->ev[9], s));

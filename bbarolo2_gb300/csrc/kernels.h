@@ -75,27 +75,29 @@ void launch_mc_scatter(cudaStream_t s, const LayoutDev &L, const SubMC *sub, int
 #define ERR_SHARE 8
 bool mc_deposit_shares(int lean, bool model64, int tx, int ty);
 // delta = 2 (replay): the member's clouds in the sub-rings not marked in chg (nchw 64-bit words a member) are
-// member 0's clouds with the member's flux: the deposit adds member 0's channel counts of them (c0, cnt: the
-// window of RP_W channels of every cloud, k_cloud_hist) times the member's fixed-point flux; its own lists hold
-// the clouds of the marked sub-rings.
+// member 0's clouds with the member's flux: the deposit adds member 0's channel counts of them (per pixel,
+// sub-ring and half, in windows of RP_W channels: launch_replay_records) times the member's fixed-point flux; its
+// own lists hold the clouds of the marked sub-rings.
 #define RP_W 64
 struct Replay {
     const int2 *rec;
     const uint32_t *cnt;
+    const int *nrec;
     const unsigned long long *chg;
     int nchw;
 };
-// the channel windows of member 0's clouds in the order of its entries (bucket[0 .. offset[nlist0]), nlist0 =
-// its lists; sub0: its sub-ring constants): rec (2 ints an entry: first channel, sub-ring | half << 16), cnt
-// (RP_W / 4 words of byte counts an entry); room for ncloud entries
-void launch_cloud_hist(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub0, const ZigDev *zig,
-                       const void *bucket, const int *offset, int nlist0, int *rec, uint32_t *cnt, int *err);
+// the channel counts of member 0's clouds summed per (list = pixel, sub-ring, half) (sub0: its sub-ring constants;
+// its nlist0 lists come first): rec (2 ints a record: first channel, sub-ring | half << 16) and cnt (RP_W / 2
+// words of two 16-bit counts a record) at the places of the list's entries, nrec (per list) their number
+void launch_replay_records(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub0,
+                           const ZigDev *zig, const void *bucket, const int *offset, const int *count, int nlist0,
+                           int *rec, uint32_t *cnt, int *nrec, int *err);
 void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
                        const MemberDev *mem, const MemberDev *mem_host, int nb, int tx, int ty,
                        const int *offset, const int *count, const void *bucket, const ZigDev *zig,
                        const float *cd2if, const double *cd2i, float *model, long long mstride, double *model64,
                        int *err, int lean, const int *klist = nullptr, int nk = 0, int delta = 0,
-                       long long *base64 = nullptr, int *tsrc = nullptr, Replay rp = Replay{nullptr, nullptr, nullptr, 0});
+                       long long *base64 = nullptr, int *tsrc = nullptr, Replay rp = Replay{nullptr, nullptr, nullptr, nullptr, 0});
 
 // ---- convolution + residual (conv.cu)
 // The taps of a beam kernel (ky, kx) as the conv kernels read them: flipped, float32, rows padded to the

@@ -946,50 +946,98 @@ __device__ __forceinline__ void px_count(const GridDev &g, const LayoutDev &L, c
 #define PX_MINB 3         // resident CTAs per SM
 #endif
 // The channels of member 0's clouds, for the members that differ from it only in the flux of most sub-rings
-// (k_mc_deposit_px, delta = 2), in the order of member 0's entries (bucket[0 .. offset[nlist0]): member 0's lists
-// come first): a warp per entry takes its cloud's samples' exact channels as the deposit does (float32 within
-// the cloud's rounding bound, else the reference's float64 operations), c0 = the channel of the first sorted
-// sample (the channels do not decrease along the sorted samples), and the counts of the channels c0 .. c0 +
-// RP_W - 1 in bytes (at most 128 samples a cloud): rec[j] = (c0, sub-ring | half << 16), cnt[j] the counts. A
-// channel past the window raises ERR_SHARE (the host bounds the spread of a cloud's channels below RP_W).
-__global__ void k_cloud_hist(GridDev g, LayoutDev L, const SubMC *__restrict__ sub0, const ZigDev *__restrict__ zig,
-                             const Entry *__restrict__ bucket, const int *__restrict__ offset, int nlist0,
-                             int2 *__restrict__ rec, uint32_t *__restrict__ cnt, int *err) {
-    __shared__ uint32_t h[8][RP_W / 4];
+// (k_mc_deposit_px, delta = 2), summed per (pixel, sub-ring, half): every cloud of such a group has the same
+// fixed-point flux in a member, so the member adds count x its flux per channel. A warp per list of member 0
+// (a pixel; its lists come first in the bucket, entries bucket[offset[l] .. + count[l]) for l < nlist0) takes its
+// clouds in turn: their samples' exact channels as the deposit computes them (float32 within the cloud's
+// rounding bound, else the reference's float64 operations), merged into an open record of the same sub-ring and
+// half whose window of RP_W channels holds the cloud (the channels do not decrease along a cloud's sorted
+// samples), else into a new one (RP_K open at most: when full they are written out). A record: rec = (first
+// channel, sub-ring | half << 16), cnt = RP_W 16-bit counts (at most 65535 samples a record); the records of a
+// list take the places of its entries, nrec[l] of them.
+#define RP_K 8
+__global__ void __launch_bounds__(256) k_replay_records(GridDev g, LayoutDev L, const SubMC *__restrict__ sub0,
+                                                        const ZigDev *__restrict__ zig,
+                                                        const Entry *__restrict__ bucket,
+                                                        const int *__restrict__ offset, const int *__restrict__ count,
+                                                        int nlist0, int2 *__restrict__ rec, uint32_t *__restrict__ cnt,
+                                                        int *__restrict__ nrec, int *err) {
+    __shared__ uint32_t h[8][RP_K][RP_W];
+    __shared__ int okey[8][RP_K], oc0[8][RP_K], otot[8][RP_K];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const long long j = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (j >= __ldg(&offset[nlist0])) return;
-    const int c = __ldg(&bucket[j].c), half = (__ldg(&bucket[j].meta) >> 24) & 1;
-    const int ir = __ldg(&L.sub[c]);
-    const SubMC &S = sub0[ir];
-    const int nv = __ldg(&L.nvs[ir]);
-    const int pb = (int)(L.pbase[ir] + (long long)(c - L.cloud_base[ir]) * ((nv + 3) & ~3));
-    float tc, epsc;
-    cloud_centre(S, L.cf[c], 0, tc, epsc);
-    const float sg = S.sg[0];
-    const float nmax = fmaxf(fabsf(__ldg(&L.nf[pb])), fabsf(__ldg(&L.nf[pb + nv - 1])));
-    const float eps = fmaf(nmax, fabsf(sg) * EPS_REL, epsc);
-    const bool fastc = fabsf(tc) < 1.0e5f;
-    const float hw = 0.5f - eps, tc5 = tc + 0.5f;
-    auto chan = [&](int i) -> int {
-        const float f = fmaf(__ldg(&L.nf[pb + i]), sg, tc5);
-        const float fl = floorf(f);
-        if (fastc && fabsf(f - fl - 0.5f) <= hw) return (int)fl;
-        return px_exact(g, L, zig, sub0, c, pb, nv, i, err);
+    const long long l = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (l >= nlist0) return;
+    const int beg = __ldg(&offset[l]), n = __ldg(&count[l]);
+    int used = 0, nr = 0;
+    auto flush = [&]() {
+        for (int r = 0; r < used; r++) {
+            // two 16-bit counts a word
+            const uint32_t v = h[warp][r][2 * lane] | (h[warp][r][2 * lane + 1] << 16);
+            cnt[(size_t)(beg + nr) * (RP_W / 2) + lane] = v;
+            if (lane == 0) rec[beg + nr] = make_int2(oc0[warp][r], okey[warp][r]);
+            nr++;
+        }
+        used = 0;
+        __syncwarp();
     };
-    int first = 0;
-    if (lane == 0) first = chan(0);
-    const int cf0 = __shfl_sync(0xffffffffu, first, 0);
-    if (lane < RP_W / 4) h[warp][lane] = 0;
-    __syncwarp();
-    for (int i = lane; i < nv; i += 32) {
-        const int d = chan(i) - cf0;
-        if ((unsigned)d < (unsigned)RP_W) atomicAdd(&h[warp][d >> 2], 1u << (8 * (d & 3)));
-        else atomicOr(err, ERR_SHARE);
+    for (int e = 0; e < n; e++) {
+        const int c = __ldg(&bucket[beg + e].c), half = (__ldg(&bucket[beg + e].meta) >> 24) & 1;
+        const int ir = __ldg(&L.sub[c]);
+        const SubMC &S = sub0[ir];
+        const int nv = __ldg(&L.nvs[ir]);
+        const int pb = (int)(L.pbase[ir] + (long long)(c - L.cloud_base[ir]) * ((nv + 3) & ~3));
+        float tc, epsc;
+        cloud_centre(S, L.cf[c], 0, tc, epsc);
+        const float sg = S.sg[0];
+        const float nmax = fmaxf(fabsf(__ldg(&L.nf[pb])), fabsf(__ldg(&L.nf[pb + nv - 1])));
+        const float eps = fmaf(nmax, fabsf(sg) * EPS_REL, epsc);
+        const bool fastc = fabsf(tc) < 1.0e5f;
+        const float hw = 0.5f - eps, tc5 = tc + 0.5f;
+        int ch[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int i = lane + 32 * u;
+            ch[u] = 0x7fffffff;
+            if (i < nv) {
+                const float f = fmaf(__ldg(&L.nf[pb + i]), sg, tc5);
+                const float fl = floorf(f);
+                ch[u] = (fastc && fabsf(f - fl - 0.5f) <= hw) ? (int)fl : px_exact(g, L, zig, sub0, c, pb, nv, i, err);
+            }
+        }
+        const int cmin = __shfl_sync(0xffffffffu, ch[0], 0);
+        const int last = nv - 1;
+        const int cmax = __shfl_sync(0xffffffffu, ch[last >> 5], last & 31);
+        const int key = ir | (half << 16);
+        // an open record of the key whose window holds the cloud (lane r tests record r)
+        bool fit = false;
+        if (lane < used)
+            fit = okey[warp][lane] == key && cmin >= oc0[warp][lane] && cmax < oc0[warp][lane] + RP_W &&
+                  otot[warp][lane] + nv <= 65535;
+        const unsigned m = __ballot_sync(0xffffffffu, fit);
+        int r;
+        if (m) {
+            r = __ffs(m) - 1;
+        } else {
+            if (used == RP_K) flush();
+            r = used++;
+            for (int x = lane; x < RP_W; x += 32) h[warp][r][x] = 0;
+            if (lane == 0) { okey[warp][r] = key; oc0[warp][r] = cmin; otot[warp][r] = 0; }
+            __syncwarp();
+        }
+        const int base = oc0[warp][r];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            if (lane + 32 * u < nv) {
+                const int d = ch[u] - base;
+                if ((unsigned)d < (unsigned)RP_W) atomicAdd(&h[warp][r][d], 1u);
+                else atomicOr(err, ERR_SHARE);
+            }
+        }
+        if (lane == 0) otot[warp][r] += nv;
+        __syncwarp();
     }
-    __syncwarp();
-    if (lane < RP_W / 4) cnt[(size_t)j * (RP_W / 4) + lane] = h[warp][lane];
-    if (lane == 0) rec[j] = make_int2(cf0, ir | (half << 16));
+    flush();
+    if (lane == 0) nrec[l] = nr;
 }
 
 template <int SPL>
@@ -1071,19 +1119,19 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
     const SubMC *__restrict__ subk = sub + (size_t)k * nsub;
     if (replay) {
         // member 0's clouds of the pixel in the sub-rings where the member is member 0 but for the flux: their
-        // channel counts (k_cloud_hist, in the order of member 0's entries) times the member's fixed-point flux;
-        // lane q of the group takes the channels c0 + RP_W / LPP q .. of the window; the next cloud's record
-        // and counts are loaded during the adds
-        constexpr int CPL = RP_W / LPP, WPL = CPL / 4;      // channels, 32-bit words of counts per lane
+        // channel counts summed per (sub-ring, half) (k_replay_records) times the member's fixed-point flux; lane
+        // q of the group takes the channels c0 + RP_W / LPP q .. of a record; the next record is loaded during
+        // the adds
+        constexpr int CPL = RP_W / LPP, WPL = CPL / 2;      // channels, 32-bit words (two counts) per lane
         const unsigned long long *chg = rp.chg + (size_t)k * rp.nchw;
         unsigned long long *row = tile + rowoff;
         const int beg0 = own ? offset[lbase0 + 8 * warp + grp] : 0;
-        const int n0 = own ? count[lbase0 + 8 * warp + grp] : 0;
+        const int n0 = own ? rp.nrec[lbase0 + 8 * warp + grp] : 0;
         const int nj0 = __reduce_max_sync(0xffffffffu, n0);
         auto load = [&](int jj, int2 &r, uint32_t (&w)[WPL]) {
             if (jj < n0) {
                 r = __ldg(&rp.rec[beg0 + jj]);
-                const uint32_t *cw = rp.cnt + (size_t)(beg0 + jj) * (RP_W / 4) + WPL * q;
+                const uint32_t *cw = rp.cnt + (size_t)(beg0 + jj) * (RP_W / 2) + WPL * q;
 #pragma unroll
                 for (int x = 0; x < WPL; x++) w[x] = __ldg(&cw[x]);
             } else {
@@ -1107,8 +1155,8 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
                         const uint32_t v = wa[w];
                         if (!v) continue;
 #pragma unroll
-                        for (int b = 0; b < 4; b++) {
-                            const int cnt = (v >> (8 * b)) & 255, ch = cb + 4 * w + b;
+                        for (int b = 0; b < 2; b++) {
+                            const int cnt = (v >> (16 * b)) & 0xffff, ch = cb + 2 * w + b;
                             if (cnt && (unsigned)ch < (unsigned)nz) row[ch] += (unsigned long long)(fix * (long long)cnt);
                         }
                     }
@@ -1261,12 +1309,13 @@ __global__ void k_scan_c(const int *__restrict__ count, int n, const int *__rest
 
 }  // namespace
 
-void launch_cloud_hist(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub0, const ZigDev *zig,
-                       const void *bucket, const int *offset, int nlist0, int *rec, uint32_t *cnt, int *err) {
-    if (L.ncloud == 0) return;
-    const long long nt = 32LL * L.ncloud;
-    k_cloud_hist<<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(g, L, sub0, zig, (const Entry *)bucket, offset, nlist0,
-                                                             (int2 *)rec, cnt, err);
+void launch_replay_records(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub0,
+                           const ZigDev *zig, const void *bucket, const int *offset, const int *count, int nlist0,
+                           int *rec, uint32_t *cnt, int *nrec, int *err) {
+    if (nlist0 <= 0) return;
+    const long long nt = 32LL * nlist0;
+    k_replay_records<<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(g, L, sub0, zig, (const Entry *)bucket, offset, count,
+                                                                 nlist0, (int2 *)rec, cnt, nrec, err);
 }
 
 void launch_mc_bin(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
