@@ -885,6 +885,7 @@ static int batch_prepare(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const
     if ((rc = hgrow(ctx, &ctx->h_reuse, &ctx->h_reuse_cap, (size_t)nb * (nsub ? nsub : 1)))) return rc;
     memset(ctx->h_reuse, 0, (size_t)nsub);
     ctx->mem_host.resize(nb);
+    std::vector<uint16_t> dmask;
     int toff = 0;
     for (int k = 0; k < nb; k++) {
         const bbgpu_eval_desc &d = descs[k];
@@ -893,12 +894,14 @@ static int batch_prepare(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const
         SubMC *S = ctx->h_sub + (size_t)k * nsub;
         int e = bbh_submc(sr + (size_t)k * BBGPU_NSR * nsub, nsub, nc0.data(), nv0.data(), &g, S,
                           k ? sr : nullptr, k ? ctx->h_sub : nullptr, k ? ctx->h_reuse + (size_t)k * nsub : nullptr);
-        if (k == 0) ctx->mc_same_nd.assign((size_t)nb * nsub, 1);
-        else
+        if (k == 0) {
+            ctx->mc_same_nd.assign((size_t)nb * nsub, 1);
+            dmask.resize((size_t)nsub);
+        } else {
+            bbh_column_diff(sr + (size_t)k * BBGPU_NSR * nsub, sr, nsub, dmask.data());
             for (int ir = 0; ir < nsub; ir++)
-                if (!ctx->h_reuse[(size_t)k * nsub + ir])
-                    ctx->mc_same_nd[(size_t)k * nsub + ir] =
-                        bbh_mc_column_same_but_dens(sr + (size_t)k * BBGPU_NSR * nsub, sr, nsub, ir) ? 1 : 0;
+                ctx->mc_same_nd[(size_t)k * nsub + ir] = (dmask[ir] & ~(1u << 5)) ? 0 : 1;
+        }
         MemberDev &M = ctx->mem_host[k];
         if ((rc = member_desc(ctx, k, d, e, need_cube, M))) return rc;
         M.ntx = (M.bx + ctx->tx - 1) / ctx->tx;
@@ -1914,14 +1917,16 @@ extern "C" int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *
             tot += cnt;
         };
         std::vector<int> ch;
+        std::vector<uint16_t> dm((size_t)nsm);
         for (int k = 0; k < nb; k++) {
             bool delta = false;
             if (ctx->share && k > 0 && fix[k] == fix[0]) {
                 const double *sk = sr_maps + (size_t)k * BBGPU_NSR * nsm;
                 long long nch = 0;
                 ch.clear();
+                bbh_column_diff(sk, sr_maps, nsm, dm.data());
                 for (int i = 0; i < nsm; i++)
-                    if (!bbh_map_column_same(sk, sr_maps, nsm, i)) {
+                    if (!bbh_map_same(dm[i], sk, nsm, i)) {
                         ch.push_back(i);
                         nch += sb[i + 1] - sb[i];
                     }

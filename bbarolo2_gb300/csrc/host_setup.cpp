@@ -265,34 +265,43 @@ void bbh_cloud_counts(const double *sr, int nsub, const int64_t *nv_in, const Gr
 
 // The per-sub-ring constants of one member (bbarolo/galmod.py:111-127 and the cloud loop's invariants).
 // Returns e: the deposits are fixed-point numbers in units of 2^-e.
-// true if sub-ring ir of the tables a and b (16 rows, nsub columns) holds the same values
-static bool same_column(const double *a, const double *b, int nsub, int ir) {
-    if (!b) return false;
-    for (int r = 0; r < BBGPU_NSR; r++)
-        if (memcmp(a + (size_t)r * nsub + ir, b + (size_t)r * nsub + ir, sizeof(double))) return false;
-    return true;
+void bbh_column_diff(const double *a, const double *b, int nsub, uint16_t *mask) {
+    memset(mask, 0, sizeof(uint16_t) * (size_t)nsub);
+    for (int r = 0; r < BBGPU_NSR; r++) {
+        const double *x = a + (size_t)r * nsub, *y = b + (size_t)r * nsub;
+        if (!memcmp(x, y, sizeof(double) * (size_t)nsub)) continue;       // (most rows of a step are equal)
+        for (int i = 0; i < nsub; i++) {
+            uint64_t u, v;
+            memcpy(&u, x + i, 8);
+            memcpy(&v, y + i, 8);
+            if (u != v) mask[i] |= (uint16_t)(1u << r);
+        }
+    }
 }
 
-bool bbh_mc_column_same_but_dens(const double *a, const double *b, int nsub, int ir) {
-    for (int r = 0; r < BBGPU_NSR; r++)
-        if (r != 5 && memcmp(a + (size_t)r * nsub + ir, b + (size_t)r * nsub + ir, sizeof(double))) return false;
-    return true;
+bool bbh_map_same(uint16_t m, const double *a, int nsub, int ir) {
+    const unsigned rows = (1u << 0) | (1u << 6) | (1u << 7) | (1u << 9) | (1u << 10) | (1u << 11) | (1u << 12) |
+                          (1u << 14) | (1u << 15);
+    return !(m & rows) && (a[(size_t)7 * nsub + ir] == 0.0 || !(m & (1u << 4)));
 }
 
-bool bbh_map_column_same(const double *a, const double *b, int nsub, int ir) {
-    auto same = [&](int r) { return !memcmp(a + (size_t)r * nsub + ir, b + (size_t)r * nsub + ir, sizeof(double)); };
-    for (int r : {0, 6, 7, 9, 10, 11, 12, 14, 15})
-        if (!same(r)) return false;
-    return a[(size_t)7 * nsub + ir] == 0.0 || same(4);
+// the rows that differ from the reference table's, per column (thread-local scratch), or nullptr without one
+static const uint16_t *diff_of(const double *sr, const double *sr_ref, int nsub) {
+    if (!sr_ref) return nullptr;
+    thread_local std::vector<uint16_t> d;
+    d.resize((size_t)nsub);
+    bbh_column_diff(sr, sr_ref, nsub, d.data());
+    return d.data();
 }
 
 int bbh_submc(const double *sr, int nsub, const int *nc, const int *nv, const GridDev *g, SubMC *out,
               const double *sr_ref, const SubMC *out_ref, signed char *reused) {
     double bound = 0.;
+    const uint16_t *diff = out_ref ? diff_of(sr, sr_ref, nsub) : nullptr;
     for (int ir = 0; ir < nsub; ir++) {
         SubMC &S = out[ir];
         if (reused) reused[ir] = 0;
-        if (out_ref && same_column(sr, sr_ref, nsub, ir)) {     // (the values of another member: same constants)
+        if (diff && !diff[ir]) {     // (the values of another member: same constants)
             const SubMC &T = out_ref[ir];
             if (reused) reused[ir] = 1;
             else S = T;
@@ -548,10 +557,11 @@ int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0,
     double cmax = 0.0, lsum = 0.0, bound = 0.0;
     for (int k = 0; k < g->nz; k++) cmax = std::max(cmax, fabs(cd2i[k]));
     for (int nl = 0; nl < g->nlines; nl++) lsum += fabs(g->relint[nl]);
+    const uint16_t *diff = out_ref ? diff_of(sr, sr_ref, nsub) : nullptr;
     for (int ir = 0; ir < nsub; ir++) {
         AnSub &S = out[ir];
         if (reused) reused[ir] = 0;
-        if (out_ref && same_column(sr, sr_ref, nsub, ir)) {     // (the values of another member: same constants)
+        if (diff && !diff[ir]) {     // (the values of another member: same constants)
             const AnSub &T = out_ref[ir];
             if (reused) reused[ir] = 1;
             else S = T;

@@ -138,14 +138,15 @@ struct ZgridCache {
 int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0, int blo1, int bhi0, int bhi1,
                 const double *cd2i, int maps, const int64_t *widx, const double *wval, AnSub *out, ZgridCache &zc,
                 const double *sr_ref = nullptr, const AnSub *out_ref = nullptr, signed char *reused = nullptr);
-// true if sub-ring ir of the ring-map tables a and b (16 rows, nsub columns) gives the same ring-map constants
-// in bbh_an_subs (maps mode): the same radius, scale height, velocity gradient, inclination, position angle,
-// centre and side weights, and the same dispersion where a velocity gradient makes the vertical grid depend
-// on it (the velocities and the density do not enter a ring map)
-bool bbh_map_column_same(const double *a, const double *b, int nsub, int ir);
-// true if sub-ring ir of the MC tables a and b differs at most in the density (row 5): the same clouds, at the
-// same pixels and channels, with another flux
-bool bbh_mc_column_same_but_dens(const double *a, const double *b, int nsub, int ir);
+// per column of the tables a and b (16 rows, nsub columns): the bit mask of the rows whose values differ (bitwise)
+void bbh_column_diff(const double *a, const double *b, int nsub, uint16_t *mask);
+// true if a column with the row mask m gives the same ring-map constants in bbh_an_subs (maps mode): the same
+// radius, scale height, velocity gradient, inclination, position angle, centre and side weights, and the same
+// dispersion where a velocity gradient makes the vertical grid depend on it (a: the column's table; the
+// velocities and the density do not enter a ring map)
+bool bbh_map_same(uint16_t m, const double *a, int nsub, int ir);
+// (an MC column with the row mask m differs at most in the density, row 5: the same clouds, at the same pixels
+// and channels, with another flux, when !(m & ~(1 << 5)))
 // The second-difference prior of the deconvolved profile at the radii R (n) (bbarolo/profile.py:60-151):
 // rows (n - 2) x 3 columns lc and weights lv, the order of the radii, the "near" rows, the median ring
 // distance d and the norm of the relative prior
