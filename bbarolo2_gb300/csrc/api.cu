@@ -21,14 +21,16 @@
 
 #define BBGPU_VERSION 1
 #define NLAYOUT 4
-#define NTIMER 12
+#define NTIMER 13
 
 // the timed stages of a batch: the flux normalisation (ring maps, their beam convolution, the normal equations,
 // the solves and the sub-ring densities), then the MC model (or the ANALYTIC one), its convolution and the
-// residual reduction (mc_deposit_delta: the members computed as a difference from member 0's model)
+// residual reduction (mc_deposit_delta: the members computed as a difference from member 0's model;
+// mc_replay: the members replaying member 0's clouds, with the records of member 0's channel counts)
 static const char *KNAMES[NTIMER] = {"prof_maps", "prof_conv",  "prof_gram",  "prof_solve",
                                      "mc_bin",    "scan_tiles", "mc_scatter", "mc_deposit",
-                                     "mc_deposit_delta", "an_model", "conv_resid", "reduce_partials"};
+                                     "mc_deposit_delta", "mc_replay", "an_model", "conv_resid",
+                                     "reduce_partials"};
 
 struct LayoutEntry {
     LayoutHost host;
@@ -1138,7 +1140,7 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
     }
     if (ctx->galmodtype == BBGPU_ANALYTIC) {
         if (tm)
-            for (int i = 5; i <= 9; i++) CK(cudaEventRecord(ctx->ev[i], s));
+            for (int i = 5; i <= 10; i++) CK(cudaEventRecord(ctx->ev[i], s));
         CK(cudaMemsetAsync(ctx->d_model_fx, 0, sizeof(long long) * (size_t)ctx->nb * ctx->mstride, s));
         launch_an_model_fast(s, g, ctx->d_asub, ctx->nsub, ctx->d_asbase, ctx->d_assub, ctx->d_acs, ctx->d_acsf,
                              (const float *)ctx->d_acsff, ctx->ansamp, ctx->nb, ctx->d_azq, ctx->d_azqf, ctx->d_awqf,
@@ -1152,7 +1154,7 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
         launch_fix_to_model(s, ctx->d_model_fx, ctx->d_mem, ctx->nb, ctx->mstride, g.nz, ctx->d_model,
                             ctx->want64 ? ctx->d_model64 : nullptr);
         CKL();
-        if (tm) CK(cudaEventRecord(ctx->ev[10], s));
+        if (tm) CK(cudaEventRecord(ctx->ev[11], s));
     } else {
         const LayoutDev &L = ctx->cur->dev;
         if (ctx->mc_dirty) {
@@ -1185,6 +1187,7 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
                                   ctx->lean, ctx->d_klist + ctx->mc_n1, ctx->mc_n2, 1, ctx->d_base64, ctx->d_tsrc);
                 CKL();
             }
+            if (tm) CK(cudaEventRecord(ctx->ev[9], s));
             if (ctx->mc_n3) {
                 const MemberDev &M0 = ctx->mem_host[0];
                 launch_replay_records(s, g, L, ctx->d_sub, ctx->d_zig, ctx->d_bucket, ctx->d_toff, ctx->d_tcount,
@@ -1200,7 +1203,7 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
                                          ctx->nchw});
                 CKL();
             }
-            if (tm) CK(cudaEventRecord(ctx->ev[9], s));
+            if (tm) CK(cudaEventRecord(ctx->ev[10], s));
         } else {
             launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->tx,
                               ctx->ty, ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig, ctx->d_cd2if,
@@ -1210,9 +1213,10 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
             if (tm) {
                 CK(cudaEventRecord(ctx->ev[8], s));
                 CK(cudaEventRecord(ctx->ev[9], s));
+                CK(cudaEventRecord(ctx->ev[10], s));
             }
         }
-        if (tm) CK(cudaEventRecord(ctx->ev[10], s));
+        if (tm) CK(cudaEventRecord(ctx->ev[11], s));
     }
     const bool conv = ctx->kernel_set;
     if (do_resid || ctx->keep_smoothed) {
@@ -1224,14 +1228,14 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
                           conv ? 1 : 0, do_resid ? 1 : 0, ctx->d_partial, ts);
         CKL();
     }
-    if (tm) CK(cudaEventRecord(ctx->ev[11], s));
+    if (tm) CK(cudaEventRecord(ctx->ev[12], s));
     if (do_resid) {
         launch_reduce_partials(s, ctx->d_partial, ctx->npart, ctx->nb, ctx->d_out2);
         CKL();
     }
     if (tm) {
-        CK(cudaEventRecord(ctx->ev[12], s));
-        CK(cudaEventSynchronize(ctx->ev[12]));
+        CK(cudaEventRecord(ctx->ev[13], s));
+        CK(cudaEventSynchronize(ctx->ev[13]));
         for (int i = 0; i < NTIMER; i++) {
             float ms = 0.f;
             cudaEventElapsedTime(&ms, ctx->ev[i], ctx->ev[i + 1]);

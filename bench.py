@@ -134,7 +134,8 @@ def step_rows(rings, batch):
 
 
 # ncu summaries (profiles/) with the DRAM traffic of a kernel's launch at the default batch
-TRAFFIC = {"mc_deposit": "k_mc_deposit_px.global160_b161.dram.txt"}
+TRAFFIC = {"mc_deposit": "k_mc_deposit_px.global160_b161.dram.txt", "mc_replay": "mc_replay.global160_b161.dram.txt",
+           "conv_resid": "k_conv_resid.global160_b161.dram.txt"}
 
 
 def measured_traffic(kernel, batch, members=None):
@@ -190,8 +191,15 @@ def algorithmic(dm, L, sr, nv, descs, mc_members=None):
     mc_bytes = 4 * nsubcl + 16 * ncl + 4 * vox * (B if mc_members is None else mc_members) // B
     conv_flops = 2.0 * taps * vox
     conv_bytes = 4 * vox * 2 + vox // 1        # model read + data read (+ mask folded in the data)
-    return dict(mc_deposit=("hbm", mc_bytes), conv_resid=("tensor", conv_flops), conv_bytes=conv_bytes,
-                deposits=B * nsubcl, voxels=vox, taps=taps, kernel=[ky, kx])
+    return dict(mc_deposit=("hbm", mc_bytes), conv_resid=("fp32", conv_flops), conv_bytes=conv_bytes,
+                deposits=B * nsubcl, voxels=vox, taps=taps, kernel=[ky, kx],
+                # per launch, for m members: the deposit reads the deviate table once and 16 B per cloud and
+                # member, and writes the models; the replay reads member 0's records of its channel counts
+                # (136 B a cloud) once and writes the models; the convolution reads the models and the data
+                # once (the data of the box is the same for all members)
+                mc_deposit_bytes=lambda m: 4 * nsubcl + 16 * ncl * m + 4 * vox * m // B,
+                mc_replay_bytes=lambda m: 136 * ncl + 4 * vox * m // B,
+                conv_resid_bytes=lambda m: 4 * vox * m // B + 4 * vox // B)
 
 
 def cpu_leg(dm, L, rows, rings, data, mask, cores=None, sample=None, steps=1):
@@ -299,18 +307,18 @@ def main():
     ctx.check(ctx.L.bbgpu_eval_run(ctx.h))
     nprof, mc_full, mc_delta, mc_replay = ctx.shared_members()
     alg = algorithmic(dm, L, sr, nv, descs, mc_full)
-    dom = max((k for k in kt if not k.startswith("prof_")), key=kt.get)   # (the MC model and its convolution)
+    # the longest of the MC model's and the convolution's stages that have a byte count: none of them runs on the
+    # tensor pipes (integer and f32 FMA work), so the line is their HBM fraction; the ncu summaries in profiles/
+    # give the pipes that bound them
+    members = {"mc_deposit": mc_full, "mc_replay": mc_replay, "conv_resid": B}
+    dom = max((k for k in members if k in kt and members[k]), key=kt.get)
+    nbytes = alg[dom + "_bytes"](members[dom])
+    achieved = nbytes / (kt[dom] * 1e-3) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": measured_traffic(dom, B, members[dom]), "kernel": dom, "peak_source": src,
+            "algorithmic_bytes": nbytes, "members": members[dom]}
     if dom == "conv_resid":
-        achieved = alg["conv_resid"][1] / (kt[dom] * 1e-3) / 1e12
-        roof = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16,
-                "traffic": None, "kernel": dom, "peak_source": src}
-    else:
-        nbytes = alg["mc_deposit"][1] if dom == "mc_deposit" else alg["conv_bytes"]
-        achieved = nbytes / (kt[dom] * 1e-3) / 1e9
-        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                "traffic": measured_traffic(dom, B, mc_full if dom == "mc_deposit" else None), "kernel": dom,
-                "peak_source": src,
-                "algorithmic_bytes": nbytes}
+        roof["f32_tflops"] = alg["conv_resid"][1] / (kt[dom] * 1e-3) / 1e12
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (f64 reduction; bit-exact int cloud indices)", "data": "synthetic",
