@@ -1191,8 +1191,8 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
             if (ctx->mc_n3) {
                 const MemberDev &M0 = ctx->mem_host[0];
                 launch_replay_records(s, g, L, ctx->d_sub, ctx->d_zig, ctx->d_bucket, ctx->d_toff, ctx->d_tcount,
-                                      (M0.tile_off + M0.ntx * M0.nty) * NOWN, ctx->d_rp_c0, ctx->d_rp_cnt,
-                                      ctx->d_rp_n, ctx->d_err);
+                                      (M0.tile_off + M0.ntx * M0.nty) * NOWN, ctx->tx * ctx->ty, ctx->d_rp_c0,
+                                      ctx->d_rp_cnt, ctx->d_rp_n, ctx->d_err);
                 CKL();
                 launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb,
                                   ctx->tx, ctx->ty, ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig,

@@ -87,11 +87,12 @@ struct Replay {
     int nchw;
 };
 // the channel counts of member 0's clouds summed per (list = pixel, sub-ring, half) (sub0: its sub-ring constants;
-// its nlist0 lists come first): rec (2 ints a record: first channel, sub-ring | half << 16) and cnt (RP_W / 2
-// words of two 16-bit counts a record) at the places of the list's entries, nrec (per list) their number
+// its nlist0 lists come first): rec (2 ints a record: first channel, sub-ring | half << 16 | extent << 17) and
+// cnt (RP_W / 2 words of two 16-bit counts a record, in the lane order of the deposit's tiles of tp pixels) at the
+// places of the list's entries, nrec (per list) their number
 void launch_replay_records(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub0,
                            const ZigDev *zig, const void *bucket, const int *offset, const int *count, int nlist0,
-                           int *rec, uint32_t *cnt, int *nrec, int *err);
+                           int tp, int *rec, uint32_t *cnt, int *nrec, int *err);
 void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
                        const MemberDev *mem, const MemberDev *mem_host, int nb, int tx, int ty,
                        const int *offset, const int *count, const void *bucket, const ZigDev *zig,

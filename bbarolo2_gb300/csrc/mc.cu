@@ -953,15 +953,17 @@ __device__ __forceinline__ void px_count(const GridDev &g, const LayoutDev &L, c
 // rounding bound, else the reference's float64 operations), merged into an open record of the same sub-ring and
 // half whose window of RP_W channels holds the cloud (the channels do not decrease along a cloud's sorted
 // samples), else into a new one (RP_K open at most: when full they are written out). A record: rec = (first
-// channel, sub-ring | half << 16), cnt = RP_W 16-bit counts (at most 65535 samples a record); the records of a
-// list take the places of its entries, nrec[l] of them.
+// channel c0, sub-ring | half << 16 | extent << 17: its channels c0 .. c0 + extent - 1), cnt = RP_W 16-bit counts
+// in the order of the lanes that add them (lpp lanes a group: channel c0 + d at (d % lpp) (RP_W / lpp) + d / lpp,
+// so that each lane's counts are contiguous); at most 65535 samples a record. The records of a list take the
+// places of its entries, nrec[l] of them.
 #define RP_K 8
 __global__ void __launch_bounds__(256) k_replay_records(GridDev g, LayoutDev L, const SubMC *__restrict__ sub0,
                                                         const ZigDev *__restrict__ zig,
                                                         const Entry *__restrict__ bucket,
                                                         const int *__restrict__ offset, const int *__restrict__ count,
-                                                        int nlist0, int2 *__restrict__ rec, uint32_t *__restrict__ cnt,
-                                                        int *__restrict__ nrec, int *err) {
+                                                        int nlist0, int lpp, int2 *__restrict__ rec,
+                                                        uint32_t *__restrict__ cnt, int *__restrict__ nrec, int *err) {
     __shared__ uint32_t h[8][RP_K][RP_W];
     __shared__ int okey[8][RP_K], oc0[8][RP_K], otot[8][RP_K];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -969,12 +971,22 @@ __global__ void __launch_bounds__(256) k_replay_records(GridDev g, LayoutDev L, 
     if (l >= nlist0) return;
     const int beg = __ldg(&offset[l]), n = __ldg(&count[l]);
     int used = 0, nr = 0;
+    const int per = RP_W / lpp;                            // counts a lane
     auto flush = [&]() {
         for (int r = 0; r < used; r++) {
-            // two 16-bit counts a word
-            const uint32_t v = h[warp][r][2 * lane] | (h[warp][r][2 * lane + 1] << 16);
+            // two 16-bit counts a word, position p = (d % lpp) per + d / lpp for channel c0 + d
+            uint32_t v = 0;
+#pragma unroll
+            for (int b = 0; b < 2; b++) {
+                const int p = 2 * lane + b, d = (p % per) * lpp + p / per;
+                v |= h[warp][r][d] << (16 * b);
+            }
             cnt[(size_t)(beg + nr) * (RP_W / 2) + lane] = v;
-            if (lane == 0) rec[beg + nr] = make_int2(oc0[warp][r], okey[warp][r]);
+            // the extent: the last channel with a count, plus one
+            const unsigned any = __ballot_sync(0xffffffffu, (h[warp][r][lane] | h[warp][r][lane + 32]) != 0);
+            const unsigned hi = __ballot_sync(0xffffffffu, h[warp][r][lane + 32] != 0);
+            const int ext = hi ? 64 - __clz(hi) : 32 - __clz(any);
+            if (lane == 0) rec[beg + nr] = make_int2(oc0[warp][r], okey[warp][r] | (ext << 17));
             nr++;
         }
         used = 0;
@@ -1120,8 +1132,8 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
     if (replay) {
         // member 0's clouds of the pixel in the sub-rings where the member is member 0 but for the flux: their
         // channel counts summed per (sub-ring, half) (k_replay_records) times the member's fixed-point flux; lane
-        // q of the group takes the channels c0 + RP_W / LPP q .. of a record; the next record is loaded during
-        // the adds
+        // q of the group takes the channels c0 + q + LPP i of a record's extent (its counts are contiguous in the
+        // record); the next record is loaded during the adds
         constexpr int CPL = RP_W / LPP, WPL = CPL / 2;      // channels, 32-bit words (two counts) per lane
         const unsigned long long *chg = rp.chg + (size_t)k * rp.nchw;
         unsigned long long *row = tile + rowoff;
@@ -1131,9 +1143,12 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
         auto load = [&](int jj, int2 &r, uint32_t (&w)[WPL]) {
             if (jj < n0) {
                 r = __ldg(&rp.rec[beg0 + jj]);
-                const uint32_t *cw = rp.cnt + (size_t)(beg0 + jj) * (RP_W / 2) + WPL * q;
+                const uint4 *cw = (const uint4 *)(rp.cnt + (size_t)(beg0 + jj) * (RP_W / 2) + WPL * q);
 #pragma unroll
-                for (int x = 0; x < WPL; x++) w[x] = __ldg(&cw[x]);
+                for (int x = 0; x < WPL / 4; x++) {
+                    const uint4 v = __ldg(&cw[x]);
+                    w[4 * x] = v.x; w[4 * x + 1] = v.y; w[4 * x + 2] = v.z; w[4 * x + 3] = v.w;
+                }
             } else {
                 r = make_int2(0, -1);
             }
@@ -1148,17 +1163,14 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
             if (ra.y >= 0) {
                 const int ir = ra.y & 0xffff;
                 if (!((__ldg(&chg[ir >> 6]) >> (ir & 63)) & 1ull)) {
-                    const long long fix = subk[ir].fix[ra.y >> 16][0];
-                    const int cb = ra.x + CPL * q;
+                    const long long fix = subk[ir].fix[(ra.y >> 16) & 1][0];
+                    const int ext = (ra.y >> 17) & 127;
+                    const int ni = (ext - q + LPP - 1) / LPP;  // this lane's channels in the extent
 #pragma unroll
-                    for (int w = 0; w < WPL; w++) {
-                        const uint32_t v = wa[w];
-                        if (!v) continue;
-#pragma unroll
-                        for (int b = 0; b < 2; b++) {
-                            const int cnt = (v >> (16 * b)) & 0xffff, ch = cb + 2 * w + b;
-                            if (cnt && (unsigned)ch < (unsigned)nz) row[ch] += (unsigned long long)(fix * (long long)cnt);
-                        }
+                    for (int x = 0; x < CPL; x++) {
+                        if (x >= ni) break;
+                        const int cnt = (wa[x >> 1] >> (16 * (x & 1))) & 0xffff, ch = ra.x + q + LPP * x;
+                        if (cnt && (unsigned)ch < (unsigned)nz) row[ch] += (unsigned long long)(fix * (long long)cnt);
                     }
                 }
             }
@@ -1311,11 +1323,12 @@ __global__ void k_scan_c(const int *__restrict__ count, int n, const int *__rest
 
 void launch_replay_records(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub0,
                            const ZigDev *zig, const void *bucket, const int *offset, const int *count, int nlist0,
-                           int *rec, uint32_t *cnt, int *nrec, int *err) {
+                           int tp, int *rec, uint32_t *cnt, int *nrec, int *err) {
     if (nlist0 <= 0) return;
     const long long nt = 32LL * nlist0;
+    const int lpp = tp == 64 ? 4 : 8;                      // lanes a pixel of k_mc_deposit_px (128 / SPL)
     k_replay_records<<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(g, L, sub0, zig, (const Entry *)bucket, offset, count,
-                                                                 nlist0, (int2 *)rec, cnt, nrec, err);
+                                                                 nlist0, lpp, (int2 *)rec, cnt, nrec, err);
 }
 
 void launch_mc_bin(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
