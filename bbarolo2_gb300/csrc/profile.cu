@@ -314,6 +314,7 @@ struct Solver {
     int *blocked;
     int *sflag;     // shared scalars
     double *sval;
+    double *rs;     // 1 / sqrt of the pivots of the factorisation
 };
 
 // Cholesky of H[P,P] into F and solve F F^T z_P = g_P; false if the block is not positive definite.
@@ -326,23 +327,40 @@ __device__ bool chol_solve(Solver &S, int p) {
     }
     if (tid == 0) S.sflag[0] = 1;
     __syncthreads();
+    // right-looking elimination on the unscaled columns (one barrier a column): the trailing block takes
+    // F[r][c] F[q][c] / F[c][c]; the columns are scaled to the Cholesky factor at the end, L[r][c] = F[r][c] /
+    // sqrt(F[c][c]), the diagonal sqrt(F[c][c]) (the same products as the scaled form, in another order)
     for (int c = 0; c < p; c++) {
-        if (tid == 0) {
-            const double d = S.F[c * n + c];
-            if (!(d > 0.0)) S.sflag[0] = 0;
-            S.F[c * n + c] = d > 0.0 ? sqrt(d) : 1.0;
+        const double d = S.F[c * n + c];
+        if (!(d > 0.0)) {
+            if (tid == 0) S.sflag[0] = 0;
+            if (tid == 0) S.F[c * n + c] = 1.0;
+            __syncthreads();
+            continue;
         }
-        __syncthreads();
-        const double dc = S.F[c * n + c];
-        for (int r = c + 1 + tid; r < p; r += blockDim.x) S.F[r * n + c] /= dc;
-        __syncthreads();
+        const double inv = 1.0 / d;
         const int m = p - c - 1;
         for (int e = tid; e < m * m; e += blockDim.x) {
             const int r = c + 1 + e / m, q = c + 1 + e % m;
-            if (q <= r) S.F[r * n + q] -= S.F[r * n + c] * S.F[q * n + c];
+            if (q <= r) S.F[r * n + q] -= S.F[r * n + c] * S.F[q * n + c] * inv;
         }
         __syncthreads();
     }
+    for (int c = tid; c < p; c += blockDim.x) {
+        const double d = S.F[c * n + c];
+        S.rs[c] = d > 0.0 ? 1.0 / sqrt(d) : 1.0;
+    }
+    __syncthreads();
+    for (int e = tid; e < p * p; e += blockDim.x) {
+        const int r = e / p, c = e - r * p;
+        if (r > c) S.F[r * n + c] *= S.rs[c];
+    }
+    __syncthreads();
+    for (int c = tid; c < p; c += blockDim.x) {
+        const double d = S.F[c * n + c];
+        S.F[c * n + c] = d > 0.0 ? sqrt(d) : 1.0;
+    }
+    __syncthreads();
     const bool ok = S.sflag[0] != 0;
     // forward then back substitution (one warp; lanes over the dot products)
     if (tid < 32) {
@@ -525,7 +543,8 @@ __global__ void __launch_bounds__(PS_THREADS) k_prof_solve(const double *__restr
     S.w = S.z + n;
     double *wr = S.w + n;                       // n weights of the prior rows
     double *x0 = wr + n;
-    S.sval = x0 + n;
+    S.rs = x0 + n;
+    S.sval = S.rs + n;
     S.P = (int *)(S.sval + 8);
     S.idx = S.P + n;
     S.blocked = S.idx + n;
@@ -775,7 +794,7 @@ void launch_prof_gram64(cudaStream_t s, const double *A, const ProfBox &box, con
     prof_gram<double>(s, A, box, nullptr, nullptr, b, m, ent_i, ent_j, nent, 1, part, gh, KRows{});
 }
 
-size_t prof_solve_smem(int n) { return (size_t)(3 * n * n + 6 * n + 8) * sizeof(double) + (size_t)(4 * n + 8) * sizeof(int); }
+size_t prof_solve_smem(int n) { return (size_t)(3 * n * n + 7 * n + 8) * sizeof(double) + (size_t)(4 * n + 8) * sizeof(int); }
 
 void launch_prof_solve(cudaStream_t s, const double *gh, const ProfConst &pc, const int *lc, const double *lv,
                        const int *ord, const unsigned char *near, const int *p0, int nb, double *x, int *pout,
