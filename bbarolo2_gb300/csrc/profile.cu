@@ -318,6 +318,15 @@ struct Solver {
 };
 
 // Cholesky of H[P,P] into F and solve F F^T z_P = g_P; false if the block is not positive definite.
+// 1 / d for d > 0 in float64 without a division: a float32 seed and two Newton steps (within an ulp or two of
+// the quotient; float64 division is slow on this part)
+__device__ __forceinline__ double rcp_newton(double d) {
+    double y = (double)(1.0f / (float)d);
+    y = y * (2.0 - d * y);
+    y = y * (2.0 - d * y);
+    return y;
+}
+
 __device__ bool chol_solve(Solver &S, int p) {
     const int tid = threadIdx.x;
     const int n = S.n;
@@ -338,7 +347,7 @@ __device__ bool chol_solve(Solver &S, int p) {
             __syncthreads();
             continue;
         }
-        const double inv = 1.0 / d;
+        const double inv = (d > 1e-30 && d < 1e30) ? rcp_newton(d) : 1.0 / d;
         const int m = p - c - 1;
         for (int e = tid; e < m * m; e += blockDim.x) {
             const int r = c + 1 + e / m, q = c + 1 + e % m;
@@ -368,14 +377,14 @@ __device__ bool chol_solve(Solver &S, int p) {
             double acc = 0.0;
             for (int q = tid; q < r; q += 32) acc += S.F[r * n + q] * S.z[q];
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(FULL, acc, o);
-            if (tid == 0) S.z[r] = (S.g[S.idx[r]] - acc) / S.F[r * n + r];
+            if (tid == 0) S.z[r] = (S.g[S.idx[r]] - acc) * S.rs[r];   // (F[r][r] = 1 / rs[r])
             __syncwarp();
         }
         for (int r = p - 1; r >= 0; r--) {
             double acc = 0.0;
             for (int q = r + 1 + tid; q < p; q += 32) acc += S.F[q * n + r] * S.z[q];
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(FULL, acc, o);
-            if (tid == 0) S.z[r] = (S.z[r] - acc) / S.F[r * n + r];
+            if (tid == 0) S.z[r] = (S.z[r] - acc) * S.rs[r];
             __syncwarp();
         }
     }
@@ -510,16 +519,24 @@ __device__ int nnls(Solver &S) {
 
 // H = G + sum_i wi^2 L_i^T L_i (L_i: the 3 weights of second difference i at columns lc[i][0..2])
 __device__ void build_H(Solver &S, const double *G, const int *lc, const double *lv, const double *wr, int nrow) {
+    // H = G + sum over the prior rows i of w_i^2 lv_i lv_i^T (columns lc_i); each entry takes its terms in the
+    // order of the rows (i, then a, then b), a thread an entry
     const int n = S.n;
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) S.H[e] = G[e];
-    __syncthreads();
-    if (threadIdx.x == 0)
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        const int j = e / n, q = e - j * n;
+        double h = G[e];
         for (int i = 0; i < nrow; i++) {
+            const int c0 = lc[3 * i], c1 = lc[3 * i + 1], c2 = lc[3 * i + 2];
+            if ((c0 != j && c1 != j && c2 != j) || (c0 != q && c1 != q && c2 != q)) continue;
             const double w2 = wr[i] * wr[i];
-            for (int a = 0; a < 3; a++)
+            for (int a = 0; a < 3; a++) {
+                if (lc[3 * i + a] != j) continue;
                 for (int b = 0; b < 3; b++)
-                    S.H[lc[3 * i + a] * n + lc[3 * i + b]] += w2 * lv[3 * i + a] * lv[3 * i + b];
+                    if (lc[3 * i + b] == q) h += w2 * lv[3 * i + a] * lv[3 * i + b];
+            }
         }
+        S.H[e] = h;
+    }
     __syncthreads();
 }
 
@@ -582,29 +599,38 @@ __global__ void __launch_bounds__(PS_THREADS) k_prof_solve(const double *__restr
         st = nnls(S);
         for (int j = tid; j < n; j += blockDim.x) x0[j] = S.x[j];
         __syncthreads();
+        // the reduced chi2 of the first solution, sum (b - A x0)^2 = b.b - 2 x0.h + x0^T G x0: the terms of each a
+        // by a thread (S.w), then summed in the order of a by thread 0
+        for (int a = tid; a < n; a += blockDim.x) {
+            double r = 0.0;
+            for (int b = 0; b < n; b++) r += G[a * n + b] * x0[b];
+            S.w[a] = x0[a] * r;
+        }
+        __syncthreads();
         if (tid == 0) {
             double xm = 0.0;
             for (int j = 0; j < n - 1; j++) xm += x0[j];
             xm /= (double)(n - 1);
             S.sval[0] = xm;
-            if (xm > 0) {
-                // the reduced chi2 of the first solution, sum (b - A x0)^2 = b.b - 2 x0.h + x0^T G x0
-                double xh = 0.0, xgx = 0.0;
-                for (int a = 0; a < n; a++) {
-                    xh += x0[a] * S.g[a];
-                    double r = 0.0;
-                    for (int b = 0; b < n; b++) r += G[a * n + b] * x0[b];
-                    xgx += x0[a] * r;
-                }
-                const double chi2 = (pc.bb - 2.0 * xh + xgx) / fmax((double)(pc.m - n), 1.0);
-                const double corr = fmax(pc.corr, 1.0) * fmax(chi2, 1.0);
-                for (int i = 0; i < nrow; i++) {
-                    const double xc = fmax(x0[ord[i + 1]], 0.1 * xm);
-                    double wi = sqrt(corr) * pc.d * pc.d / (pc.smooth * xc);
-                    wi = fmax(wi, sqrt(pc.floor_) * srel);
-                    if (near[i]) wi = srel;
-                    wr[i] = wi;
-                }
+            double xh = 0.0, xgx = 0.0;
+            for (int a = 0; a < n; a++) {
+                xh += x0[a] * S.g[a];
+                xgx += S.w[a];
+            }
+            const double chi2 = (pc.bb - 2.0 * xh + xgx) / fmax((double)(pc.m - n), 1.0);
+            const double corr = fmax(pc.corr, 1.0) * fmax(chi2, 1.0);
+            S.sval[1] = sqrt(corr) * pc.d * pc.d / pc.smooth;
+            S.sval[2] = sqrt(pc.floor_) * srel;
+        }
+        __syncthreads();
+        if (S.sval[0] > 0) {
+            const double xm = S.sval[0];
+            for (int i = tid; i < nrow; i += blockDim.x) {
+                const double xc = fmax(x0[ord[i + 1]], 0.1 * xm);
+                double wi = S.sval[1] / xc;
+                wi = fmax(wi, S.sval[2]);
+                if (near[i]) wi = srel;
+                wr[i] = wi;
             }
         }
         __syncthreads();
