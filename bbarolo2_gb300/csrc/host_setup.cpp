@@ -298,6 +298,8 @@ int bbh_submc(const double *sr, int nsub, const int *nc, const int *nv, const Gr
               const double *sr_ref, const SubMC *out_ref, signed char *reused) {
     double bound = 0.;
     const uint16_t *diff = out_ref ? diff_of(sr, sr_ref, nsub) : nullptr;
+    double scr, ccr;
+    sincos_memo(g->crota2, scr, ccr);
     for (int ir = 0; ir < nsub; ir++) {
         SubMC &S = out[ir];
         if (reused) reused[ir] = 0;
@@ -326,9 +328,8 @@ int bbh_submc(const double *sr, int nsub, const int *nc, const int *nv, const Gr
         S.z0 = R_(6); S.dvdz = R_(7); S.zcyl = R_(8);
         sincos_memo(R_(9), S.sinc, S.cinc);
         double phi = R_(10);
-        double sphi, cphi, scr, ccr;
+        double sphi, cphi;
         sincos_memo(phi, sphi, cphi);
-        sincos_memo(g->crota2, scr, ccr);
         S.spa = sphi * ccr + cphi * scr;
         S.cpa = cphi * ccr - sphi * scr;
         S.xpos = R_(11); S.ypos = R_(12); S.vsys = R_(13);
@@ -516,14 +517,17 @@ static std::pair<int, int> zgrid_cached(ZgridCache &zc, std::vector<double> &tz,
                                         double R0, double radsep, double xpos, double ypos, double cdelt0,
                                         double cdelt1, long long blo0, long long blo1, long long bhi0, long long bhi1,
                                         double zstep) {
-    std::string key;
+    ZKey key;
+    memset(&key, 0, sizeof key);
     if (z0 <= 0 || nzq < 2 || fabs(sinc) < 1e-6) {
-        key = "thin";
+        key.iv[0] = -1;
     } else {
-        const double dv[] = {z0, sinc, pixsize, dvdz, sig, R0, radsep, xpos, ypos, cdelt0, cdelt1, zstep};
+        // (the dispersion enters the grid only with a velocity gradient)
+        const double dv[] = {z0, sinc, pixsize, dvdz, dvdz != 0 ? sig : 0.0, R0, radsep, xpos, ypos, cdelt0, cdelt1,
+                             zstep};
         const long long iv[] = {nzq, ltype, blo0, blo1, bhi0, bhi1};
-        key.assign((const char *)dv, sizeof dv);
-        key.append((const char *)iv, sizeof iv);
+        memcpy(key.dv, dv, sizeof dv);
+        memcpy(key.iv, iv, sizeof iv);
     }
     auto it = zc.map.find(key);
     if (it != zc.map.end()) return it->second;
@@ -558,6 +562,8 @@ int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0,
     for (int k = 0; k < g->nz; k++) cmax = std::max(cmax, fabs(cd2i[k]));
     for (int nl = 0; nl < g->nlines; nl++) lsum += fabs(g->relint[nl]);
     const uint16_t *diff = out_ref ? diff_of(sr, sr_ref, nsub) : nullptr;
+    double scr, ccr;
+    sincos_memo(g->crota2, scr, ccr);
     for (int ir = 0; ir < nsub; ir++) {
         AnSub &S = out[ir];
         if (reused) reused[ir] = 0;
@@ -588,9 +594,8 @@ int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0,
         S.z0 = SR(6, ir); S.dvdz = SR(7, ir); S.zcyl = SR(8, ir);
         sincos_memo(SR(9, ir), S.sinc, S.cinc);
         const double phi = SR(10, ir);
-        double sphi, cphi, scr, ccr;
+        double sphi, cphi;
         sincos_memo(phi, sphi, cphi);
-        sincos_memo(g->crota2, scr, ccr);
         S.spa = sphi * ccr + cphi * scr;
         S.cpa = cphi * ccr - sphi * scr;
         S.xpos = SR(11, ir); S.ypos = SR(12, ir); S.vsys = SR(13, ir);

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <stdint.h>
+#include <string.h>
 #include <stddef.h>
 
 #ifdef __cplusplus
@@ -124,8 +125,25 @@ void bbh_an_samples_f32(const std::vector<double> &cs, std::vector<float> &csf);
 // -10000 when the total flux is not finite
 // The vertical sample grids of the ANALYTIC sub-rings, shared by all the sub-rings with the same inputs of _zgrid:
 // one table (append-only), each grid stored once (the fits change few geometries between evaluations).
+// the inputs of _zgrid (a thin layer: all zero but iv[0] = -1)
+struct ZKey {
+    double dv[12];
+    long long iv[6];
+    bool operator==(const ZKey &o) const { return !memcmp(this, &o, sizeof *this); }
+};
+struct ZKeyHash {
+    size_t operator()(const ZKey &k) const {
+        uint64_t h = 1469598103934665603ull, w[18];
+        memcpy(w, &k, sizeof w);
+        for (int i = 0; i < 18; i++) {
+            h = (h ^ w[i]) * 1099511628211ull;
+            h ^= h >> 29;
+        }
+        return (size_t)h;
+    }
+};
 struct ZgridCache {
-    std::unordered_map<std::string, std::pair<int, int>> map;   // inputs -> (offset, samples)
+    std::unordered_map<ZKey, std::pair<int, int>, ZKeyHash> map;   // inputs -> (offset, samples)
     std::vector<double> zq, wq;
     size_t uploaded = 0;                                         // entries already copied to the device
     void clear() {
