@@ -137,15 +137,38 @@ struct AnWarp {
     int k0[BBGPU_MAXL], nk[BBGPU_MAXL];
 };
 
-// The sample of this warp: member k, sub-ring S, cos/sin of its azimuth; false if nothing to deposit.
-__device__ __forceinline__ bool an_sample(long long gs, long long nsamp, int nsub, const AnSub *__restrict__ subs,
+// The (member, sample) of warp gs of a batch, by segments of warps: segment i (warps astart[i] .. astart[i + 1])
+// is aseg[i] = (member whose model takes the deposits, member whose constants make them, sub-ring (-1: every
+// sample of the table), sign of the deposits); s is the sample in the table.
+struct AnSeg {
+    int k, src, sign;
+    long long s;
+};
+__device__ __forceinline__ bool an_seg(long long gs, const long long *__restrict__ astart,
+                                       const int4 *__restrict__ aseg, int nseg, long long ntot,
+                                       const int *__restrict__ sbase, AnSeg &o) {
+    if (gs >= ntot) return false;
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (astart[mid] <= gs) lo = mid;
+        else hi = mid - 1;
+    }
+    const int4 sg = aseg[lo];
+    o.k = sg.x;
+    o.src = sg.y;
+    o.sign = sg.w;
+    o.s = gs - astart[lo] + (sg.z >= 0 ? sbase[sg.z] : 0);
+    return true;
+}
+
+// The sample s of member src: sub-ring S, cos/sin of its azimuth; false if nothing to deposit.
+__device__ __forceinline__ bool an_sample(long long s, int src, int nsub, const AnSub *__restrict__ subs,
                                           const int *__restrict__ sbase, const int *__restrict__ ssub,
-                                          const double2 *__restrict__ cs, int &k, const AnSub *&S, double &caz,
+                                          const double2 *__restrict__ cs, const AnSub *&S, double &caz,
                                           double &saz, double &R) {
-    k = (int)(gs / nsamp);
-    const long long s = gs - (long long)k * nsamp;
     const int ir = ssub[s];
-    S = subs + (size_t)k * nsub + ir;
+    S = subs + (size_t)src * nsub + ir;
     if (!S->active) return false;
     const int local = (int)(s - sbase[ir]);
     const double2 c = cs[s];
@@ -158,7 +181,9 @@ __device__ __forceinline__ bool an_sample(long long gs, long long nsamp, int nsu
 // Models: out64 (per member: box (by, bx, nz), stride mstride) += fixed-point deposits.
 __global__ void __launch_bounds__(AN_WPB * 32) k_an_model(GridDev g, const AnSub *__restrict__ subs, int nsub,
                                                           const int *__restrict__ sbase, const int *__restrict__ ssub,
-                                                          const double2 *__restrict__ cs, long long nsamp, int nb,
+                                                          const double2 *__restrict__ cs,
+                                                          const long long *__restrict__ astart,
+                                                          const int4 *__restrict__ aseg, int nseg, long long ntot,
                                                           const double *__restrict__ zq, const double *__restrict__ wq,
                                                           const double *__restrict__ vedges,
                                                           const double *__restrict__ cd2i,
@@ -170,11 +195,12 @@ __global__ void __launch_bounds__(AN_WPB * 32) k_an_model(GridDev g, const AnSub
     __shared__ AnWarp wsm[AN_WPB];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long gs = (long long)blockIdx.x * AN_WPB + w;
-    if (gs >= nsamp * nb) return;
-    int k;
+    AnSeg sg;
+    if (!an_seg(gs, astart, aseg, nseg, ntot, sbase, sg)) return;
+    const int k = sg.k;
     const AnSub *Sp;
     double caz, saz, R;
-    if (!an_sample(gs, nsamp, nsub, subs, sbase, ssub, cs, k, Sp, caz, saz, R)) return;
+    if (!an_sample(sg.s, sg.src, nsub, subs, sbase, ssub, cs, Sp, caz, saz, R)) return;
     const AnSub &S = *Sp;
     if (skip_fast && S.anfast) return;                 // (k_an_model_fast's samples)
     const double wside = caz >= 0.0 ? S.wrec : S.wapp;
@@ -183,7 +209,8 @@ __global__ void __launch_bounds__(AN_WPB * 32) k_an_model(GridDev g, const AnSub
     const int nz = g.nz, nl_n = g.nlines;
     double *pe = an_smem + (size_t)w * nl_n * (nz + 2);
     AnWarp &W = wsm[w];
-    const double fscale = ldexp(1.0, M.fix_exp);
+    // (a negative unit: the deposits of member 0's constants taken out of a difference, rounded symmetrically)
+    const double fscale = sg.sign < 0 ? -ldexp(1.0, M.fix_exp) : ldexp(1.0, M.fix_exp);
     unsigned long long *o64 = out64 + (size_t)k * mstride;
     const double x = __dmul_rn(R, caz);
     const double yb = __dmul_rn(__dmul_rn(R, saz), S.cinc);
@@ -292,8 +319,10 @@ __global__ void __launch_bounds__(ANF_WPB * 32) k_an_model_fast(GridDev g, const
                                                                 const int *__restrict__ ssub,
                                                                 const double2 *__restrict__ cs,
                                                                 const float2 *__restrict__ csf,
-                                                                const float4 *__restrict__ csff, long long nsamp,
-                                                                int nb, const double *__restrict__ zq,
+                                                                const float4 *__restrict__ csff,
+                                                                const long long *__restrict__ astart,
+                                                                const int4 *__restrict__ aseg, int nseg,
+                                                                long long ntot, const double *__restrict__ zq,
                                                                 const float *__restrict__ zqf,
                                                                 const float *__restrict__ wqf,
                                                                 const float2 *__restrict__ vef,
@@ -305,11 +334,12 @@ __global__ void __launch_bounds__(ANF_WPB * 32) k_an_model_fast(GridDev g, const
     extern __shared__ float anf_smem[];                     // per warp: the CDF at the edges, the profile
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long gs = (long long)blockIdx.x * ANF_WPB + w;
-    if (gs >= nsamp * nb) return;
-    const int k = (int)(gs / nsamp);
-    const long long s = gs - (long long)k * nsamp;
+    AnSeg sg;
+    if (!an_seg(gs, astart, aseg, nseg, ntot, sbase, sg)) return;
+    const int k = sg.k;
+    const long long s = sg.s;
     const int ir = ssub[s];
-    const AnSub &S = subs[(size_t)k * nsub + ir];
+    const AnSub &S = subs[(size_t)sg.src * nsub + ir];
     if (!S.active || !S.anfast) return;
     const float2 cf = csf[s];
     const bool rec = cf.x >= 0.0f;                          // (the sign of the float32 table is the float64 test's)
@@ -354,7 +384,7 @@ __global__ void __launch_bounds__(ANF_WPB * 32) k_an_model_fast(GridDev g, const
         nk = (int)(a1 - a0);
         const ff vr = ff_add(v, ff{-g.vrefh, -g.vrefl});
         const float vrh = vr.hi, vrl = vr.lo;
-        const float amp = ldexpf(S.af * (rec ? S.wrecf : S.wappf), M.fix_exp);
+        const float amp = (float)sg.sign * ldexpf(S.af * (rec ? S.wrecf : S.wappf), M.fix_exp);
         for (int j = lane; j <= nk; j += 32) {
             const float2 e = __ldg(vef + k0 + j);
             const float t = (__fsub_rn(e.x, vrh) + __fsub_rn(e.y, vrl)) * S.invf;
@@ -435,10 +465,9 @@ __global__ void __launch_bounds__(AN_WPB * 32) k_an_maps(GridDev g, const AnSub 
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long gs = (long long)blockIdx.x * AN_WPB + w;
     if (gs >= nsamp) return;
-    int k;
     const AnSub *Sp;
     double caz, saz, R;
-    if (!an_sample(gs, nsamp, nsub, subs, sbase, ssub, cs, k, Sp, caz, saz, R)) return;
+    if (!an_sample(gs, 0, nsub, subs, sbase, ssub, cs, Sp, caz, saz, R)) return;
     const AnSub &S = *Sp;
     const double wside = caz >= 0.0 ? S.wrec : S.wapp;
     if (wside == 0.0) return;
@@ -466,14 +495,19 @@ __global__ void __launch_bounds__(AN_WPB * 32) k_an_maps(GridDev g, const AnSub 
 }
 
 // fixed point (units 2^-e of member k) -> float32 model and, optionally, float64 copy
+// (mbase[k] >= 0: member k holds the difference from that member's sums, added modulo 2^64: the same box and unit)
 __global__ void k_fix_to_model(const long long *__restrict__ in, const MemberDev *__restrict__ mem, long long mstride,
-                               int nz, float *__restrict__ model, double *__restrict__ model64) {
+                               int nz, float *__restrict__ model, double *__restrict__ model64,
+                               const int *__restrict__ mbase) {
     const int k = blockIdx.y;
     const MemberDev &M = mem[k];
     const long long n = (long long)M.by * M.bx * nz;
     const double sc = ldexp(1.0, -M.fix_exp);
+    const long long *bas = mbase && mbase[k] >= 0 ? in + (size_t)mbase[k] * mstride : nullptr;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const double v = __dmul_rn((double)in[(size_t)k * mstride + i], sc);
+        long long q = in[(size_t)k * mstride + i];
+        if (bas) q = (long long)((unsigned long long)q + (unsigned long long)bas[i]);
+        const double v = __dmul_rn((double)q, sc);
         model[(size_t)k * mstride + i] = (float)v;
         if (model64) model64[(size_t)k * mstride + i] = v;
     }
@@ -484,33 +518,33 @@ __global__ void k_fix_to_model(const long long *__restrict__ in, const MemberDev
 size_t an_smem_bytes(int nz, int nlines) { return (size_t)AN_WPB * nlines * (nz + 2) * sizeof(double); }
 
 void launch_an_model(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase, const int *ssub,
-                     const double *cs, long long nsamp, int nb, const double *zq, const double *wq,
-                     const double *vedges, const double *cd2i, const double *ptab, const MemberDev *mem,
-                     long long *out64, long long mstride, int skip_fast) {
-    const long long nw = nsamp * nb;
-    if (nw == 0) return;
+                     const double *cs, const long long *astart, const int *aseg, int nseg, long long ntot,
+                     const double *zq, const double *wq, const double *vedges, const double *cd2i, const double *ptab,
+                     const MemberDev *mem, long long *out64, long long mstride, int skip_fast) {
+    const long long nw = ntot;
+    if (nw == 0 || nseg == 0) return;
     const size_t smem = an_smem_bytes(g.nz, g.nlines);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_an_model, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_an_model<<<(unsigned)((nw + AN_WPB - 1) / AN_WPB), AN_WPB * 32, smem, s>>>(
-        g, subs, nsub, sbase, ssub, (const double2 *)cs, nsamp, nb, zq, wq, vedges, cd2i, ptab, mem,
-        (unsigned long long *)out64, mstride, skip_fast);
+        g, subs, nsub, sbase, ssub, (const double2 *)cs, astart, (const int4 *)aseg, nseg, ntot, zq, wq, vedges, cd2i,
+        ptab, mem, (unsigned long long *)out64, mstride, skip_fast);
 }
 
 size_t an_fast_smem_bytes(int nz) { return (size_t)ANF_WPB * 2 * (nz + 2) * sizeof(float); }
 
 void launch_an_model_fast(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase,
-                          const int *ssub, const double *cs, const float *csf, const float *csff, long long nsamp,
-                          int nb,
+                          const int *ssub, const double *cs, const float *csf, const float *csff,
+                          const long long *astart, const int *aseg, int nseg, long long ntot,
                           const double *zq, const float *zqf, const float *wqf, const float *vef, const float *cd2if,
                           const float *ptabf, const MemberDev *mem, long long *out64, long long mstride) {
-    const long long nw = nsamp * nb;
-    if (nw == 0) return;
+    const long long nw = ntot;
+    if (nw == 0 || nseg == 0) return;
     const size_t smem = an_fast_smem_bytes(g.nz);
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(k_an_model_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_an_model_fast<<<(unsigned)((nw + ANF_WPB - 1) / ANF_WPB), ANF_WPB * 32, smem, s>>>(
-        g, subs, nsub, sbase, ssub, (const double2 *)cs, (const float2 *)csf, (const float4 *)csff, nsamp, nb, zq,
-        zqf, wqf,
+        g, subs, nsub, sbase, ssub, (const double2 *)cs, (const float2 *)csf, (const float4 *)csff, astart,
+        (const int4 *)aseg, nseg, ntot, zq, zqf, wqf,
         (const float2 *)vef, cd2if, ptabf, mem, (unsigned long long *)out64, mstride);
 }
 
@@ -523,8 +557,8 @@ void launch_an_maps(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsu
 }
 
 void launch_fix_to_model(cudaStream_t s, const long long *in, const MemberDev *mem, int nb, long long mstride, int nz,
-                         float *model, double *model64) {
+                         float *model, double *model64, const int *mbase) {
     if (nb == 0) return;
     dim3 grid(256, nb);
-    k_fix_to_model<<<grid, 256, 0, s>>>(in, mem, mstride, nz, model, model64);
+    k_fix_to_model<<<grid, 256, 0, s>>>(in, mem, mstride, nz, model, model64, mbase);
 }

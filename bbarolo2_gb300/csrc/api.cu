@@ -148,6 +148,16 @@ struct bbgpu_ctx {
     bool mc_dirty = true;
     int mc_nseg = 0, mc_n1 = 0, mc_n2 = 0, mc_n3 = 0;   // (mc_n3: the members replaying member 0's clouds)
     std::vector<signed char> mc_same_nd;   // per (member, sub-ring): member 0's column but for the density
+    // ANALYTIC: the (member, sample) segments of the model kernels and, per member, the member whose fixed-point
+    // sums it adds (-1: none); rebuilt before a run when an_dirty
+    bool an_dirty = true;
+    int an_nseg = 0, an_n2 = 0;
+    long long an_ntot = 0;
+    std::vector<long long> h_astart;
+    std::vector<int> h_aseg, h_mbase, asbase_host;
+    long long *d_astart = nullptr;
+    int *d_aseg = nullptr, *d_mbase = nullptr;
+    size_t d_astart_cap = 0, d_aseg_cap = 0, d_mbase_cap = 0;
     std::vector<unsigned long long> h_chg; // per member: the sub-rings a replaying member deposits itself
     int nchw = 0;
     int *d_rp_c0 = nullptr, *d_rp_n = nullptr;   // (2 ints a record; records per list of member 0)
@@ -466,7 +476,8 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
                     (void *)ctx->d_ubase, (void *)ctx->d_prof_of, (void *)ctx->d_pstatu, (void *)ctx->d_pxu,
                     (void *)ctx->d_cstart, (void *)ctx->d_base64, (void *)ctx->d_cseg, (void *)ctx->d_klist,
                     (void *)ctx->d_tsrc, (void *)ctx->d_blk, (void *)ctx->d_ktab, (void *)ctx->d_gflag,
-                    (void *)ctx->d_rp_c0, (void *)ctx->d_rp_cnt, (void *)ctx->d_chg, (void *)ctx->d_rp_n})
+                    (void *)ctx->d_rp_c0, (void *)ctx->d_rp_cnt, (void *)ctx->d_chg, (void *)ctx->d_rp_n,
+                    (void *)ctx->d_astart, (void *)ctx->d_aseg, (void *)ctx->d_mbase})
         cudaFree(q);
     for (void *q : {(void *)ctx->d_asub, (void *)ctx->d_asbase, (void *)ctx->d_assub, (void *)ctx->d_acs,
                     (void *)ctx->d_azq, (void *)ctx->d_awq, (void *)ctx->d_model_fx, (void *)ctx->d_acsf,
@@ -509,9 +520,10 @@ extern "C" int bbgpu_shared_members(const bbgpu_ctx *ctx, int *profiles, int *mc
                                     int *mc_replay) {
     if (!ctx) return BBGPU_ERR_ARG;
     const bool mc = ctx->galmodtype == BBGPU_MC && !ctx->mc_dirty;
+    const bool an = ctx->galmodtype == BBGPU_ANALYTIC && !ctx->an_dirty;
     if (profiles) *profiles = ctx->prof_uploaded ? ctx->nu : 0;
-    if (mc_full) *mc_full = mc ? ctx->mc_n1 : 0;
-    if (mc_delta) *mc_delta = mc ? ctx->mc_n2 : 0;
+    if (mc_full) *mc_full = mc ? ctx->mc_n1 : (an ? ctx->nb - ctx->an_n2 : 0);
+    if (mc_delta) *mc_delta = mc ? ctx->mc_n2 : (an ? ctx->an_n2 : 0);
     if (mc_replay) *mc_replay = mc ? ctx->mc_n3 : 0;
     return BBGPU_OK;
 }
@@ -531,6 +543,7 @@ extern "C" int bbgpu_set_option(bbgpu_ctx *ctx, int opt, int value) {
         case 3:
             ctx->share = value != 0;
             ctx->mc_dirty = true;
+            ctx->an_dirty = true;
             break;
         default: return fail(ctx, BBGPU_ERR_ARG, "unknown option %d", opt);
     }
@@ -763,6 +776,7 @@ static int batch_prepare_analytic(bbgpu_ctx *ctx, int nb, int nsub, const double
     ctx->nb = nb;
     ctx->nsub = nsub;
     ctx->galmodtype = BBGPU_ANALYTIC;
+    ctx->an_dirty = true;
     ctx->lean = 0;
     ctx->ntile_total = 0;
     ctx->mstride = (long long)g.nx * g.ny * g.nz;
@@ -797,6 +811,7 @@ static int batch_prepare_analytic(bbgpu_ctx *ctx, int nb, int nsub, const double
         if (ssub.size()) CK(cudaMemcpy(ctx->d_assub, ssub.data(), sizeof(int) * ssub.size(), cudaMemcpyHostToDevice));
         if (cs.size()) CK(cudaMemcpy(ctx->d_acs, cs.data(), sizeof(double) * cs.size(), cudaMemcpyHostToDevice));
         ctx->ansamp = sbase[nsub];
+        ctx->asbase_host = sbase;
         ctx->asamp_key = key;
         ctx->h2d += (long long)(sizeof(int) * (sbase.size() + ssub.size()) + sizeof(double) * cs.size());
     }
@@ -1126,6 +1141,73 @@ static int mc_segments(bbgpu_ctx *ctx) {
     return 0;
 }
 
+// The (member, sample) segments of an ANALYTIC batch. A member k > 0 whose columns differ from member 0's in a
+// few sub-rings, with member 0's box and fixed-point exponent (with a flux normalisation: member 0's profile), is
+// computed as member 0's fixed-point sums plus the deposits of those sub-rings' samples with its constants, minus
+// the same samples with member 0's (exact: the sums are modulo 2^64, the deposits rounded symmetrically); every
+// other member deposits all its samples.
+static int an_segments(bbgpu_ctx *ctx) {
+    const int nb = ctx->nb, nsub = ctx->nsub;
+    const long long ns = ctx->ansamp;
+    const std::vector<int> &sb = ctx->asbase_host;
+    std::vector<long long> &cs = ctx->h_astart;
+    std::vector<int> &sg = ctx->h_aseg, &mb = ctx->h_mbase;
+    cs.clear();
+    sg.clear();
+    mb.assign(nb, -1);
+    long long tot = 0;
+    auto seg = [&](int k, int src, int ir, int sign, long long n) {
+        if (n <= 0) return;
+        cs.push_back(tot);
+        sg.insert(sg.end(), {k, src, ir, sign});
+        tot += n;
+    };
+    const bool can = ctx->share && nb > 1 && (int)sb.size() == nsub + 1 &&
+                     (!ctx->prof_uploaded || (int)ctx->prof_of_host.size() == nb);
+    const MemberDev &M0 = ctx->mem_host[0];
+    int n2 = 0;
+    for (int k = 0; k < nb; k++) {
+        if (can && k > 0) {
+            const MemberDev &M = ctx->mem_host[k];
+            bool ok = M.blo0 == M0.blo0 && M.blo1 == M0.blo1 && M.bx == M0.bx && M.by == M0.by;
+            if (ok) ok = ctx->prof_uploaded ? ctx->prof_of_host[k] == 0 : M.fix_exp == M0.fix_exp;
+            if (ok) {
+                const signed char *ru = ctx->h_reuse + (size_t)k * nsub;
+                long long nch = 0;
+                for (int ir = 0; ir < nsub; ir++)
+                    if (!ru[ir]) nch += sb[ir + 1] - sb[ir];
+                if (2 * nch < ns) {
+                    for (int ir = 0; ir < nsub; ir++)
+                        if (!ru[ir]) {
+                            seg(k, k, ir, 1, sb[ir + 1] - sb[ir]);
+                            seg(k, 0, ir, -1, sb[ir + 1] - sb[ir]);
+                        }
+                    mb[k] = 0;
+                    n2++;
+                    continue;
+                }
+            }
+        }
+        seg(k, k, -1, 1, ns);
+    }
+    cs.push_back(tot);
+    ctx->an_nseg = (int)cs.size() - 1;
+    ctx->an_ntot = tot;
+    ctx->an_n2 = n2;
+    int rc;
+    if ((rc = dgrow(ctx, &ctx->d_astart, &ctx->d_astart_cap, cs.size())) ||
+        (rc = dgrow(ctx, &ctx->d_aseg, &ctx->d_aseg_cap, sg.size() + 4)) ||
+        (rc = dgrow(ctx, &ctx->d_mbase, &ctx->d_mbase_cap, (size_t)nb)))
+        return rc;
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(ctx->d_astart, cs.data(), sizeof(long long) * cs.size(), cudaMemcpyHostToDevice, s));
+    if (!sg.empty()) CK(cudaMemcpyAsync(ctx->d_aseg, sg.data(), sizeof(int) * sg.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->d_mbase, mb.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));     // (the host vectors change with the next batch)
+    ctx->an_dirty = false;
+    return 0;
+}
+
 static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
     if (!ctx->uploaded) return fail(ctx, BBGPU_ERR_STATE, "run before upload");
     const GridDev &g = ctx->g;
@@ -1141,18 +1223,22 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
     if (ctx->galmodtype == BBGPU_ANALYTIC) {
         if (tm)
             for (int i = 5; i <= 10; i++) CK(cudaEventRecord(ctx->ev[i], s));
+        if (ctx->an_dirty) {
+            int rc = an_segments(ctx);
+            if (rc) return rc;
+        }
         CK(cudaMemsetAsync(ctx->d_model_fx, 0, sizeof(long long) * (size_t)ctx->nb * ctx->mstride, s));
         launch_an_model_fast(s, g, ctx->d_asub, ctx->nsub, ctx->d_asbase, ctx->d_assub, ctx->d_acs, ctx->d_acsf,
-                             (const float *)ctx->d_acsff, ctx->ansamp, ctx->nb, ctx->d_azq, ctx->d_azqf, ctx->d_awqf,
-                             (const float *)ctx->d_vef, ctx->d_cd2if, ctx->d_ptabf, ctx->d_mem, ctx->d_model_fx,
-                             ctx->mstride);
+                             (const float *)ctx->d_acsff, ctx->d_astart, ctx->d_aseg, ctx->an_nseg, ctx->an_ntot,
+                             ctx->d_azq, ctx->d_azqf, ctx->d_awqf, (const float *)ctx->d_vef, ctx->d_cd2if,
+                             ctx->d_ptabf, ctx->d_mem, ctx->d_model_fx, ctx->mstride);
         CKL();
-        launch_an_model(s, g, ctx->d_asub, ctx->nsub, ctx->d_asbase, ctx->d_assub, ctx->d_acs, ctx->ansamp, ctx->nb,
-                        ctx->d_azq, ctx->d_awq, ctx->d_vedges, ctx->d_cd2i, ctx->d_ptab, ctx->d_mem, ctx->d_model_fx,
-                        ctx->mstride, 1);
+        launch_an_model(s, g, ctx->d_asub, ctx->nsub, ctx->d_asbase, ctx->d_assub, ctx->d_acs, ctx->d_astart,
+                        ctx->d_aseg, ctx->an_nseg, ctx->an_ntot, ctx->d_azq, ctx->d_awq, ctx->d_vedges, ctx->d_cd2i,
+                        ctx->d_ptab, ctx->d_mem, ctx->d_model_fx, ctx->mstride, 1);
         CKL();
         launch_fix_to_model(s, ctx->d_model_fx, ctx->d_mem, ctx->nb, ctx->mstride, g.nz, ctx->d_model,
-                            ctx->want64 ? ctx->d_model64 : nullptr);
+                            ctx->want64 ? ctx->d_model64 : nullptr, ctx->an_n2 ? ctx->d_mbase : nullptr);
         CKL();
         if (tm) CK(cudaEventRecord(ctx->ev[11], s));
     } else {
@@ -1551,8 +1637,16 @@ extern "C" int bbgpu_galmod_analytic(bbgpu_ctx *ctx, double *out, const double *
     cudaStream_t s = ctx->stream;
     CK(cudaMemcpyAsync(dm, &M, sizeof M, cudaMemcpyHostToDevice, s));
     CK(cudaMemsetAsync(o64, 0, n * sizeof(long long), s));
-    launch_an_model(s, g, D.subs, ns, D.sbase, D.ssub, D.cs, D.nsamp, 1, D.zq, D.wq, ctx->d_vedges, ctx->d_cd2i,
-                    ctx->d_ptab, dm, o64, (long long)n, 0);
+    long long *ast = nullptr;
+    int *asg = nullptr;
+    if (!B.get(&ast, 2 * sizeof(long long)) || !B.get(&asg, 4 * sizeof(int)))
+        return fail(ctx, BBGPU_ERR_NOMEM, "galmod_analytic: allocation failed");
+    const long long hst[2] = {0, D.nsamp};
+    const int hsg[4] = {0, 0, -1, 1};                   // (the member's own samples)
+    CK(cudaMemcpyAsync(ast, hst, sizeof hst, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(asg, hsg, sizeof hsg, cudaMemcpyHostToDevice, s));
+    launch_an_model(s, g, D.subs, ns, D.sbase, D.ssub, D.cs, ast, asg, 1, D.nsamp, D.zq, D.wq, ctx->d_vedges,
+                    ctx->d_cd2i, ctx->d_ptab, dm, o64, (long long)n, 0);
     CKL();
     std::vector<long long> h(n);
     CK(cudaMemcpyAsync(h.data(), o64, n * sizeof(long long), cudaMemcpyDeviceToHost, s));
@@ -1962,6 +2056,7 @@ extern "C" int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *
     for (int b : ubase) ctx->nu_delta += b >= 0;
     ctx->prof_of_host = prof_of;
     ctx->mc_dirty = true;
+    ctx->an_dirty = true;
     // the vertical grids: the new ones appended on the device (the table grows with a copy of the old part)
     const size_t nz1 = zc.zq.size() + 1;
     if (zc.uploaded == 0 || nz1 > ctx->d_pzq_cap) {

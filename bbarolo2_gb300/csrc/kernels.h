@@ -156,25 +156,29 @@ void launch_norm_pix(cudaStream_t s, double *model, const float *data, const uin
 // dynamic shared memory of launch_an_model (the host keeps it within AN_SMEM_MAX)
 #define AN_SMEM_MAX (200 * 1024)
 size_t an_smem_bytes(int nz, int nlines);
+// The ANALYTIC models of a batch by segments of warps (a warp a sample): segment i (warps astart[i] ..
+// astart[i + 1], ntot = astart[nseg]) is aseg[4i .. 4i + 4) = (member whose model takes the deposits, member whose
+// constants make them, sub-ring (-1: every sample of the table), sign of the deposits).
 void launch_an_model(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase, const int *ssub,
-                     const double *cs, long long nsamp, int nb, const double *zq, const double *wq,
-                     const double *vedges, const double *cd2i, const double *ptab, const MemberDev *mem,
-                     long long *out64, long long mstride, int skip_fast);
+                     const double *cs, const long long *astart, const int *aseg, int nseg, long long ntot,
+                     const double *zq, const double *wq, const double *vedges, const double *cd2i, const double *ptab,
+                     const MemberDev *mem, long long *out64, long long mstride, int skip_fast);
 // the float32 path of the ANALYTIC model (sub-rings with anfast; launch_an_model with skip_fast does the others):
 // csf, zqf, wqf float32 copies of the sample and vertical tables, csff (float4 per sample) its cos and sin in
 // float-float, vef (nz + 1) float-float channel edges of line 0
 // relative to g.vref, ptabf the normal CDF table in float32
 size_t an_fast_smem_bytes(int nz);
 void launch_an_model_fast(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase,
-                          const int *ssub, const double *cs, const float *csf, const float *csff, long long nsamp,
-                          int nb,
+                          const int *ssub, const double *cs, const float *csf, const float *csff,
+                          const long long *astart, const int *aseg, int nseg, long long ntot,
                           const double *zq, const float *zqf, const float *wqf, const float *vef, const float *cd2if,
                           const float *ptabf, const MemberDev *mem, long long *out64, long long mstride);
 void launch_an_maps(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase, const int *ssub,
                     const double *cs, long long nsamp, const double *zq, const double *wq, const long long *widx,
                     const double *wval, const MemberDev &M, long long *maps64);
+// mbase (nullable): per member, the member whose fixed-point sums are added (-1: none)
 void launch_fix_to_model(cudaStream_t s, const long long *in, const MemberDev *mem, int nb, long long mstride, int nz,
-                         float *model, double *model64);
+                         float *model, double *model64, const int *mbase = nullptr);
 
 // ---- flux normalisation (profile.cu)
 #define ERR_PROFILE_LAYOUT 4      // a deconvolved density changed the MC cloud layout of a member

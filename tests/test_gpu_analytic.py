@@ -141,3 +141,58 @@ def test_batch_path_analytic_models(gpu_lib, oracle_lib, variant):
                                    st.crval3, st.cdelt3, st.crpix3, st._chmin, None, st.zstep)
         np.testing.assert_allclose(got, ref, rtol=0, atol=1e-5 * ref.max())
         assert abs(got.sum() - ref.sum()) <= 1e-5 * ref.sum()
+
+
+@pytest.mark.parametrize("variant", ["thin", "thick_lag"])
+def test_batch_path_analytic_gradient_shared(gpu_lib, oracle_lib, variant):
+    """A finite-difference batch of the ANALYTIC model (one ring's VROT, VDISP, INC or PA stepped per member): the
+    members computed as member 0's model plus the difference of a few sub-rings' samples give, bit for bit, the
+    models computed from all their samples (option 3 off), and agree with the oracle's."""
+    from bbarolo2_gb300 import _lib, configs, engine
+    from bbarolo2_gb300.galmod import ring_rows_batch
+    cube, rings = configs.classic64(galmodtype="ANALYTIC")
+    if variant == "thick_lag":
+        rings.z0[:] = 12.
+        rings.dvdz[4:] = 6.
+        rings.zcyl[:] = 8.
+    dm = engine.DiskModel(cube)
+    st = dm.setup
+    L = engine.BatchLikelihood(dm, np.ones(cube.array.shape, np.float32), None, maskmode=0, sigma=1.0)
+    base = ring_rows_batch([rings])[0]
+    rows = [base]
+    for j in (1, 5):
+        for row, step in ((4, 5.0), (5, 1.0), (12, 2.0), (13, 3.0)):
+            r = base.copy()
+            r[row, j] += step
+            rows.append(r)
+    rows = np.stack(rows)
+    sr, nv, descs, boxes = L.prepare(rows, rings, seed=1)
+    models = {}
+    for share in (0, 1):
+        dm.ctx.set_option(_lib.OPT_SHARE_MAPS, share)
+        ss, _ = L.run(sr, nv, descs, galmodtype="ANALYTIC")
+        ms = []
+        for k in range(len(rows)):
+            (blo, bhi) = boxes[k]
+            got = np.zeros((bhi[1] - blo[1], bhi[0] - blo[0], st.nsubs), np.float32)
+            dm.ctx.check(dm.ctx.L.bbgpu_eval_model(dm.ctx.h, k, 0, _lib.ptr(got), got.shape[0], got.shape[1],
+                                                   st.nsubs))
+            ms.append(got)
+        models[share] = (ss, ms)
+        if share:
+            _, full, delta, _ = dm.ctx.shared_members()
+            assert delta > 0, (full, delta)
+    dm.ctx.set_option(_lib.OPT_SHARE_MAPS, 1)
+    np.testing.assert_array_equal(models[0][0], models[1][0])
+    for k in range(len(rows)):
+        np.testing.assert_array_equal(models[0][1][k], models[1][1][k], err_msg=str(k))
+    for k in (1, 2, 5):
+        (blo, bhi) = boxes[k]
+        got = models[1][1][k]
+        ref = np.zeros(got.shape)
+        nzq = 1 if not np.any(sr[k, 6] > 0) else 1024
+        oracle_lib.galmod_analytic(ref, sr[k], 0, sr.shape[2], st.radsep, st.cdens, st.pixarea, st.cdelt[0],
+                                   st.cdelt[1], st.crota2, blo[0], blo[1], bhi[0], bhi[1], st.ltype, st.sig_instr,
+                                   st._vedges_lines, st.relint, st.cd2i, nzq, st.axtyp, st.velsys, st.lfreq0,
+                                   st.crval3, st.cdelt3, st.crpix3, st._chmin, None, st.zstep)
+        np.testing.assert_allclose(got, ref, rtol=0, atol=1e-5 * ref.max())
