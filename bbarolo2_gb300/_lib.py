@@ -14,7 +14,7 @@ LIBPATH = os.path.join(HERE, "_build", "libbbgpu.so")
 
 OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_KERNEL = 0, -1, -2, -3, -4, -5
 MC, ANALYTIC = 0, 1
-OPT_KEEP_SMOOTHED, OPT_TIMING, OPT_SHARE_MAPS = 1, 2, 3
+OPT_KEEP_SMOOTHED, OPT_TIMING, OPT_SHARE = 1, 2, 3
 
 # every symbol of include/bbgpu.h (the ABI test checks that the library exports them all)
 SYMBOLS = ("bbgpu_ctx_create", "bbgpu_ctx_destroy", "bbgpu_last_error", "bbgpu_version", "bbgpu_set_grid",

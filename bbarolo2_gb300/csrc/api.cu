@@ -160,10 +160,10 @@ struct bbgpu_ctx {
     size_t d_astart_cap = 0, d_aseg_cap = 0, d_mbase_cap = 0;
     std::vector<unsigned long long> h_chg; // per member: the sub-rings a replaying member deposits itself
     int nchw = 0;
-    int *d_rp_c0 = nullptr, *d_rp_n = nullptr;   // (2 ints a record; records per list of member 0)
+    int *d_rp_rec = nullptr, *d_rp_n = nullptr;   // (2 ints a record; records per list of member 0)
     uint32_t *d_rp_cnt = nullptr;
     unsigned long long *d_chg = nullptr;
-    size_t d_rp_c0_cap = 0, d_rp_cnt_cap = 0, d_chg_cap = 0, d_rp_n_cap = 0;
+    size_t d_rp_rec_cap = 0, d_rp_cnt_cap = 0, d_chg_cap = 0, d_rp_n_cap = 0;
     long long mc_ntot = 0;
     std::vector<long long> h_cstart;
     std::vector<int> h_cseg, h_klist;
@@ -476,7 +476,7 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
                     (void *)ctx->d_ubase, (void *)ctx->d_prof_of, (void *)ctx->d_pstatu, (void *)ctx->d_pxu,
                     (void *)ctx->d_cstart, (void *)ctx->d_base64, (void *)ctx->d_cseg, (void *)ctx->d_klist,
                     (void *)ctx->d_tsrc, (void *)ctx->d_blk, (void *)ctx->d_ktab, (void *)ctx->d_gflag,
-                    (void *)ctx->d_rp_c0, (void *)ctx->d_rp_cnt, (void *)ctx->d_chg, (void *)ctx->d_rp_n,
+                    (void *)ctx->d_rp_rec, (void *)ctx->d_rp_cnt, (void *)ctx->d_chg, (void *)ctx->d_rp_n,
                     (void *)ctx->d_astart, (void *)ctx->d_aseg, (void *)ctx->d_mbase})
         cudaFree(q);
     for (void *q : {(void *)ctx->d_asub, (void *)ctx->d_asbase, (void *)ctx->d_assub, (void *)ctx->d_acs,
@@ -1124,7 +1124,7 @@ static int mc_segments(bbgpu_ctx *ctx) {
          (rc = dgrow(ctx, &ctx->d_tsrc, &ctx->d_tsrc_cap, (size_t)ctx->ntile_total + 1))))
         return rc;
     if (ctx->mc_n3) {
-        if ((rc = dgrow(ctx, &ctx->d_rp_c0, &ctx->d_rp_c0_cap, 2 * (size_t)ncl + 2)) ||
+        if ((rc = dgrow(ctx, &ctx->d_rp_rec, &ctx->d_rp_rec_cap, 2 * (size_t)ncl + 2)) ||
             (rc = dgrow(ctx, &ctx->d_rp_cnt, &ctx->d_rp_cnt_cap, (size_t)ncl * (RP_W / 2) + 1)) ||
             (rc = dgrow(ctx, &ctx->d_rp_n, &ctx->d_rp_n_cap, (size_t)(M0.ntx * M0.nty) * NOWN + 1)) ||
             (rc = dgrow(ctx, &ctx->d_chg, &ctx->d_chg_cap, ctx->h_chg.size())))
@@ -1277,7 +1277,7 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
             if (ctx->mc_n3) {
                 const MemberDev &M0 = ctx->mem_host[0];
                 launch_replay_records(s, g, L, ctx->d_sub, ctx->d_zig, ctx->d_bucket, ctx->d_toff, ctx->d_tcount,
-                                      (M0.tile_off + M0.ntx * M0.nty) * NOWN, ctx->tx * ctx->ty, ctx->d_rp_c0,
+                                      (M0.tile_off + M0.ntx * M0.nty) * NOWN, ctx->tx * ctx->ty, ctx->d_rp_rec,
                                       ctx->d_rp_cnt, ctx->d_rp_n, ctx->d_err);
                 CKL();
                 launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb,
@@ -1285,7 +1285,7 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
                                   ctx->d_cd2if, ctx->d_cd2i, ctx->d_model, ctx->mstride, nullptr, ctx->d_err,
                                   ctx->lean, ctx->d_klist + ctx->mc_n1 + ctx->mc_n2, ctx->mc_n3, 2, nullptr,
                                   ctx->mc_n2 ? ctx->d_tsrc : nullptr,
-                                  Replay{(const int2 *)ctx->d_rp_c0, ctx->d_rp_cnt, ctx->d_rp_n, ctx->d_chg,
+                                  Replay{(const int2 *)ctx->d_rp_rec, ctx->d_rp_cnt, ctx->d_rp_n, ctx->d_chg,
                                          ctx->nchw});
                 CKL();
             }

@@ -372,7 +372,7 @@ def batch_leg(ctx, L, rings, rows, args, dist, world, share=True):
     """Another batch of the same problem (MC): device-resident evaluations/s and end to end. share=False
     computes every member's flux normalisation from all its samples (no member shares member 0's ring maps)."""
     from bbarolo2_gb300 import _lib
-    ctx.set_option(_lib.OPT_SHARE_MAPS, 1 if share else 0)
+    ctx.set_option(_lib.OPT_SHARE, 1 if share else 0)
     try:
         sr, nv, descs, boxes = L.prepare(rows, rings, seed=1)
         B = rows.shape[0]
@@ -404,7 +404,7 @@ def batch_leg(ctx, L, rings, rows, args, dist, world, share=True):
             L.evaluate(rows, rings, seed=1)
         te = max_over_ranks(time.perf_counter() - t0, dist)
     finally:
-        ctx.set_option(_lib.OPT_SHARE_MAPS, 1)
+        ctx.set_option(_lib.OPT_SHARE, 1)
     return {"batch": B, "value": throughput(B, steps, world, dt), "unit": UNIT, "steps": steps,
             "ms_per_step": 1e3 * dt / steps, "e2e": throughput(B, steps, world, te), "profile_ms": kt}
 

@@ -169,7 +169,7 @@ def test_batch_path_analytic_gradient_shared(gpu_lib, oracle_lib, variant):
     sr, nv, descs, boxes = L.prepare(rows, rings, seed=1)
     models = {}
     for share in (0, 1):
-        dm.ctx.set_option(_lib.OPT_SHARE_MAPS, share)
+        dm.ctx.set_option(_lib.OPT_SHARE, share)
         ss, _ = L.run(sr, nv, descs, galmodtype="ANALYTIC")
         ms = []
         for k in range(len(rows)):
@@ -182,7 +182,7 @@ def test_batch_path_analytic_gradient_shared(gpu_lib, oracle_lib, variant):
         if share:
             _, full, delta, _ = dm.ctx.shared_members()
             assert delta > 0, (full, delta)
-    dm.ctx.set_option(_lib.OPT_SHARE_MAPS, 1)
+    dm.ctx.set_option(_lib.OPT_SHARE, 1)
     np.testing.assert_array_equal(models[0][0], models[1][0])
     for k in range(len(rows)):
         np.testing.assert_array_equal(models[0][1][k], models[1][1][k], err_msg=str(k))

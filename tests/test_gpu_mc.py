@@ -181,7 +181,7 @@ def test_batch_path_gradient_members_shared(gpu_lib, oracle_lib, wl):
     sr, nv, descs, boxes = L.prepare(rows, rings, seed=2)
     models = {}
     for share in (0, 1):
-        dm.ctx.set_option(_lib.OPT_SHARE_MAPS, share)
+        dm.ctx.set_option(_lib.OPT_SHARE, share)
         ss, _ = L.run(sr, nv, descs)
         ms = []
         for k in range(len(rows)):
@@ -191,7 +191,7 @@ def test_batch_path_gradient_members_shared(gpu_lib, oracle_lib, wl):
                                                    st.nsubs))
             ms.append(got)
         models[share] = (ss, ms)
-    dm.ctx.set_option(_lib.OPT_SHARE_MAPS, 1)
+    dm.ctx.set_option(_lib.OPT_SHARE, 1)
     np.testing.assert_array_equal(models[0][0], models[1][0])
     for k in range(len(rows)):
         np.testing.assert_array_equal(models[0][1][k], models[1][1][k], err_msg=str(k))

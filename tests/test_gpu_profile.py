@@ -156,7 +156,7 @@ def test_batch_profile_shared_members(gpu_lib, oracle_lib, galmodtype):
     ctx = dm.ctx
     res = {}
     for share in (0, 1):
-        ctx.set_option(_lib.OPT_SHARE_MAPS, share)
+        ctx.set_option(_lib.OPT_SHARE, share)
         ll = L.evaluate(rows, rings, seed=1, galmodtype=galmodtype)
         x, st = L.last_profile()
         res[share] = (ll, x, st)
@@ -165,7 +165,7 @@ def test_batch_profile_shared_members(gpu_lib, oracle_lib, galmodtype):
             assert nprof < len(rows)
             if galmodtype == "MC":    # (velocity steps as a difference, geometry steps replaying member 0's clouds)
                 assert delta > 0 and replay > 0, (full, delta, replay)
-    ctx.set_option(_lib.OPT_SHARE_MAPS, 1)
+    ctx.set_option(_lib.OPT_SHARE, 1)
     np.testing.assert_array_equal(res[0][0], res[1][0])
     np.testing.assert_array_equal(res[0][1], res[1][1])
     np.testing.assert_array_equal(res[0][2], res[1][2])
