@@ -348,10 +348,11 @@ __device__ bool chol_solve(Solver &S, int p) {
             continue;
         }
         const double inv = (d > 1e-30 && d < 1e30) ? rcp_newton(d) : 1.0 / d;
-        const int m = p - c - 1;
-        for (int e = tid; e < m * m; e += blockDim.x) {
-            const int r = c + 1 + e / m, q = c + 1 + e % m;
-            if (q <= r) S.F[r * n + q] -= S.F[r * n + c] * S.F[q * n + c] * inv;
+        // the trailing block's lower triangle: rows on the warps, columns on the lanes
+        const int nwarp = blockDim.x >> 5, wid = tid >> 5, ln = tid & 31;
+        for (int r = c + 1 + wid; r < p; r += nwarp) {
+            const double frc = S.F[r * n + c] * inv;
+            for (int q = c + 1 + ln; q <= r; q += 32) S.F[r * n + q] -= frc * S.F[q * n + c];
         }
         __syncthreads();
     }
