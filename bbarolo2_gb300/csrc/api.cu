@@ -162,7 +162,9 @@ struct bbgpu_ctx {
     int nchw = 0;
     int *d_rp_rec = nullptr, *d_rp_n = nullptr;   // (2 ints a record; records per list of member 0)
     uint32_t *d_rp_cnt = nullptr;
-    unsigned long long *d_chg = nullptr;
+    unsigned long long *d_chg = nullptr, *d_tmask = nullptr;
+    size_t d_tmask_cap = 0;
+    bool mc_records = false;              // member 0's records are built (replaying or difference members use them)
     size_t d_rp_rec_cap = 0, d_rp_cnt_cap = 0, d_chg_cap = 0, d_rp_n_cap = 0;
     long long mc_ntot = 0;
     std::vector<long long> h_cstart;
@@ -477,7 +479,7 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
                     (void *)ctx->d_cstart, (void *)ctx->d_base64, (void *)ctx->d_cseg, (void *)ctx->d_klist,
                     (void *)ctx->d_tsrc, (void *)ctx->d_blk, (void *)ctx->d_ktab, (void *)ctx->d_gflag,
                     (void *)ctx->d_rp_rec, (void *)ctx->d_rp_cnt, (void *)ctx->d_chg, (void *)ctx->d_rp_n,
-                    (void *)ctx->d_astart, (void *)ctx->d_aseg, (void *)ctx->d_mbase})
+                    (void *)ctx->d_astart, (void *)ctx->d_aseg, (void *)ctx->d_mbase, (void *)ctx->d_tmask})
         cudaFree(q);
     for (void *q : {(void *)ctx->d_asub, (void *)ctx->d_asbase, (void *)ctx->d_assub, (void *)ctx->d_acs,
                     (void *)ctx->d_azq, (void *)ctx->d_awq, (void *)ctx->d_model_fx, (void *)ctx->d_acsf,
@@ -1075,10 +1077,13 @@ static int mc_segments(bbgpu_ctx *ctx) {
                 for (int ir = 0; ir < nsub; ir++)
                     if (!ru[ir]) nch += L.nc[ir];
                 if (2 * nch < ncl) {
+                    // (with member 0's records, its clouds of the changed sub-rings are taken out by their counts)
+                    unsigned long long *cm = ctx->h_chg.data() + (size_t)k * ctx->nchw;
                     for (int ir = 0; ir < nsub; ir++)
                         if (!ru[ir]) {
                             seg(k, k, L.cloud_base[ir], 1, L.nc[ir]);
-                            seg(k, 0, L.cloud_base[ir], -1, L.nc[ir]);
+                            if (!rp_ok) seg(k, 0, L.cloud_base[ir], -1, L.nc[ir]);
+                            cm[ir >> 6] |= 1ULL << (ir & 63);
                         }
                     dl.push_back(k);
                     ctx->mc_isdelta[k] = 1;
@@ -1123,10 +1128,12 @@ static int mc_segments(bbgpu_ctx *ctx) {
         ((rc = dgrow(ctx, &ctx->d_base64, &ctx->d_base64_cap, (size_t)M0.bx * M0.by * ctx->g.nz + 1)) ||
          (rc = dgrow(ctx, &ctx->d_tsrc, &ctx->d_tsrc_cap, (size_t)ctx->ntile_total + 1))))
         return rc;
-    if (ctx->mc_n3) {
+    ctx->mc_records = rp_ok && (ctx->mc_n2 || ctx->mc_n3);
+    if (ctx->mc_records) {
         if ((rc = dgrow(ctx, &ctx->d_rp_rec, &ctx->d_rp_rec_cap, 2 * (size_t)ncl + 2)) ||
             (rc = dgrow(ctx, &ctx->d_rp_cnt, &ctx->d_rp_cnt_cap, (size_t)ncl * (RP_W / 2) + 1)) ||
             (rc = dgrow(ctx, &ctx->d_rp_n, &ctx->d_rp_n_cap, (size_t)(M0.ntx * M0.nty) * NOWN + 1)) ||
+            (rc = dgrow(ctx, &ctx->d_tmask, &ctx->d_tmask_cap, (size_t)(M0.ntx * M0.nty) * ctx->nchw + 1)) ||
             (rc = dgrow(ctx, &ctx->d_chg, &ctx->d_chg_cap, ctx->h_chg.size())))
             return rc;
         CK(cudaMemcpyAsync(ctx->d_chg, ctx->h_chg.data(), sizeof(unsigned long long) * ctx->h_chg.size(),
@@ -1266,27 +1273,30 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
                               ctx->mc_n1, 0, ctx->mc_n2 ? ctx->d_base64 : nullptr, ctx->mc_n2 ? ctx->d_tsrc : nullptr);
             CKL();
             if (tm) CK(cudaEventRecord(ctx->ev[8], s));
+            const Replay rp = ctx->mc_records ? Replay{(const int2 *)ctx->d_rp_rec, ctx->d_rp_cnt, ctx->d_rp_n,
+                                                       ctx->d_chg, ctx->nchw, ctx->d_tmask}
+                                              : Replay{nullptr, nullptr, nullptr, nullptr, 0, nullptr};
+            if (ctx->mc_records) {
+                const MemberDev &M0 = ctx->mem_host[0];
+                launch_replay_records(s, g, L, ctx->d_sub, ctx->d_zig, ctx->d_bucket, ctx->d_toff, ctx->d_tcount,
+                                      (M0.tile_off + M0.ntx * M0.nty) * NOWN, ctx->tx * ctx->ty, ctx->d_rp_rec,
+                                      ctx->d_rp_cnt, ctx->d_rp_n, ctx->d_tmask, ctx->nchw, ctx->d_err);
+                CKL();
+            }
             if (ctx->mc_n2) {
                 launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb,
                                   ctx->tx, ctx->ty, ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig,
                                   ctx->d_cd2if, ctx->d_cd2i, ctx->d_model, ctx->mstride, nullptr, ctx->d_err,
-                                  ctx->lean, ctx->d_klist + ctx->mc_n1, ctx->mc_n2, 1, ctx->d_base64, ctx->d_tsrc);
+                                  ctx->lean, ctx->d_klist + ctx->mc_n1, ctx->mc_n2, 1, ctx->d_base64, ctx->d_tsrc, rp);
                 CKL();
             }
             if (tm) CK(cudaEventRecord(ctx->ev[9], s));
             if (ctx->mc_n3) {
-                const MemberDev &M0 = ctx->mem_host[0];
-                launch_replay_records(s, g, L, ctx->d_sub, ctx->d_zig, ctx->d_bucket, ctx->d_toff, ctx->d_tcount,
-                                      (M0.tile_off + M0.ntx * M0.nty) * NOWN, ctx->tx * ctx->ty, ctx->d_rp_rec,
-                                      ctx->d_rp_cnt, ctx->d_rp_n, ctx->d_err);
-                CKL();
                 launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb,
                                   ctx->tx, ctx->ty, ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig,
                                   ctx->d_cd2if, ctx->d_cd2i, ctx->d_model, ctx->mstride, nullptr, ctx->d_err,
                                   ctx->lean, ctx->d_klist + ctx->mc_n1 + ctx->mc_n2, ctx->mc_n3, 2, nullptr,
-                                  ctx->mc_n2 ? ctx->d_tsrc : nullptr,
-                                  Replay{(const int2 *)ctx->d_rp_rec, ctx->d_rp_cnt, ctx->d_rp_n, ctx->d_chg,
-                                         ctx->nchw});
+                                  ctx->mc_n2 ? ctx->d_tsrc : nullptr, rp);
                 CKL();
             }
             if (tm) CK(cudaEventRecord(ctx->ev[10], s));

@@ -77,7 +77,8 @@ bool mc_deposit_shares(int lean, bool model64, int tx, int ty);
 // delta = 2 (replay): the member's clouds in the sub-rings not marked in chg (nchw 64-bit words a member) are
 // member 0's clouds with the member's flux: the deposit adds member 0's channel counts of them (per pixel,
 // sub-ring and half, in windows of RP_W channels: launch_replay_records) times the member's fixed-point flux; its
-// own lists hold the clouds of the marked sub-rings.
+// own lists hold the clouds of the marked sub-rings. delta = 1 with records: member 0's clouds of the marked
+// sub-rings are taken out of its sums by their counts times member 0's flux (the lists hold the member's own).
 #define RP_W 64
 struct Replay {
     const int2 *rec;
@@ -85,6 +86,7 @@ struct Replay {
     const int *nrec;
     const unsigned long long *chg;
     int nchw;
+    const unsigned long long *tmask;    // per tile of member 0: the sub-rings with clouds in it (nchw words)
 };
 // the channel counts of member 0's clouds summed per (list = pixel, sub-ring, half) (sub0: its sub-ring constants;
 // its nlist0 lists come first): rec (2 ints a record: first channel, sub-ring | half << 16 | extent << 17) and
@@ -92,13 +94,14 @@ struct Replay {
 // places of the list's entries, nrec (per list) their number
 void launch_replay_records(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub0,
                            const ZigDev *zig, const void *bucket, const int *offset, const int *count, int nlist0,
-                           int tp, int *rec, uint32_t *cnt, int *nrec, int *err);
+                           int tp, int *rec, uint32_t *cnt, int *nrec, unsigned long long *tmask, int nchw,
+                           int *err);
 void launch_mc_deposit(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
                        const MemberDev *mem, const MemberDev *mem_host, int nb, int tx, int ty,
                        const int *offset, const int *count, const void *bucket, const ZigDev *zig,
                        const float *cd2if, const double *cd2i, float *model, long long mstride, double *model64,
                        int *err, int lean, const int *klist = nullptr, int nk = 0, int delta = 0,
-                       long long *base64 = nullptr, int *tsrc = nullptr, Replay rp = Replay{nullptr, nullptr, nullptr, nullptr, 0});
+                       long long *base64 = nullptr, int *tsrc = nullptr, Replay rp = Replay{nullptr, nullptr, nullptr, nullptr, 0, nullptr});
 
 // ---- convolution + residual (conv.cu)
 // The taps of a beam kernel (ky, kx) as the conv kernels read them: flipped, float32, rows padded to the

@@ -963,7 +963,8 @@ __global__ void __launch_bounds__(256) k_replay_records(GridDev g, LayoutDev L, 
                                                         const Entry *__restrict__ bucket,
                                                         const int *__restrict__ offset, const int *__restrict__ count,
                                                         int nlist0, int lpp, int2 *__restrict__ rec,
-                                                        uint32_t *__restrict__ cnt, int *__restrict__ nrec, int *err) {
+                                                        uint32_t *__restrict__ cnt, int *__restrict__ nrec,
+                                                        unsigned long long *__restrict__ tmask, int nchw, int *err) {
     __shared__ uint32_t h[8][RP_K][RP_W];
     __shared__ int okey[8][RP_K], oc0[8][RP_K], otot[8][RP_K];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -986,7 +987,12 @@ __global__ void __launch_bounds__(256) k_replay_records(GridDev g, LayoutDev L, 
             const unsigned any = __ballot_sync(0xffffffffu, (h[warp][r][lane] | h[warp][r][lane + 32]) != 0);
             const unsigned hi = __ballot_sync(0xffffffffu, h[warp][r][lane + 32] != 0);
             const int ext = hi ? 64 - __clz(hi) : 32 - __clz(any);
-            if (lane == 0) rec[beg + nr] = make_int2(oc0[warp][r], okey[warp][r] | (ext << 17));
+            if (lane == 0) {
+                rec[beg + nr] = make_int2(oc0[warp][r], okey[warp][r] | (ext << 17));
+                // (the sub-rings with clouds in the tile)
+                const int ir = okey[warp][r] & 0xffff;
+                atomicOr(&tmask[(size_t)(l / NOWN) * nchw + (ir >> 6)], 1ull << (ir & 63));
+            }
             nr++;
         }
         used = 0;
@@ -1092,6 +1098,9 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
     {
         int any = 0;
         if (threadIdx.x < NOWN) any = count[lbase + threadIdx.x] != 0 || (replay && count[lbase0 + threadIdx.x] != 0);
+        // a difference with member 0's records: also the tiles where member 0 has clouds of the changed sub-rings
+        if (delta == 1 && rp.rec && threadIdx.x < rp.nchw)
+            any |= (rp.tmask[(size_t)t * rp.nchw + threadIdx.x] & rp.chg[(size_t)k * rp.nchw + threadIdx.x]) != 0;
         if (!__syncthreads_or(any)) {
             if (tsrc && threadIdx.x == 0) tsrc[mem[k].tile_off + t] = delta == 1 ? 0 : k;
             if (delta == 1) return;
@@ -1129,11 +1138,12 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
     PxDefer *qe = qall + warp * PX_QCAP;
     int *qn = qns + warp;
     const SubMC *__restrict__ subk = sub + (size_t)k * nsub;
-    if (replay) {
-        // member 0's clouds of the pixel in the sub-rings where the member is member 0 but for the flux: their
-        // channel counts summed per (sub-ring, half) (k_replay_records) times the member's fixed-point flux; lane
-        // q of the group takes the channels c0 + q + LPP i of a record's extent (its counts are contiguous in the
-        // record); the next record is loaded during the adds
+    if (replay || (delta == 1 && rp.rec)) {
+        // member 0's clouds of the pixel from its channel counts summed per (sub-ring, half) (k_replay_records):
+        // a replay adds those of the sub-rings where the member is member 0 but for the flux, times the member's
+        // fixed-point flux; a difference takes out those of the changed sub-rings, times member 0's (the member's
+        // own clouds of those sub-rings are in its lists). Lane q of the group takes the channels c0 + q + LPP i of
+        // a record's extent (its counts are contiguous in the record); the next record is loaded during the adds
         constexpr int CPL = RP_W / LPP, WPL = CPL / 2;      // channels, 32-bit words (two counts) per lane
         const unsigned long long *chg = rp.chg + (size_t)k * rp.nchw;
         unsigned long long *row = tile + rowoff;
@@ -1162,8 +1172,9 @@ __global__ void __launch_bounds__(256, PX_MINB) k_mc_deposit_px(GridDev g, Layou
             load(jj + 1, rb, wb);
             if (ra.y >= 0) {
                 const int ir = ra.y & 0xffff;
-                if (!((__ldg(&chg[ir >> 6]) >> (ir & 63)) & 1ull)) {
-                    const long long fix = subk[ir].fix[(ra.y >> 16) & 1][0];
+                const bool changed = (__ldg(&chg[ir >> 6]) >> (ir & 63)) & 1ull;
+                if (replay != changed) {
+                    const long long fix = replay ? subk[ir].fix[(ra.y >> 16) & 1][0] : -sub[ir].fix[(ra.y >> 16) & 1][0];
                     const int ext = (ra.y >> 17) & 127;
                     const int ni = (ext - q + LPP - 1) / LPP;  // this lane's channels in the extent
 #pragma unroll
@@ -1323,12 +1334,15 @@ __global__ void k_scan_c(const int *__restrict__ count, int n, const int *__rest
 
 void launch_replay_records(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub0,
                            const ZigDev *zig, const void *bucket, const int *offset, const int *count, int nlist0,
-                           int tp, int *rec, uint32_t *cnt, int *nrec, int *err) {
+                           int tp, int *rec, uint32_t *cnt, int *nrec, unsigned long long *tmask, int nchw,
+                           int *err) {
     if (nlist0 <= 0) return;
+    cudaMemsetAsync(tmask, 0, sizeof(unsigned long long) * (size_t)(nlist0 / NOWN) * nchw, s);
     const long long nt = 32LL * nlist0;
     const int lpp = tp == 64 ? 4 : 8;                      // lanes a pixel of k_mc_deposit_px (128 / SPL)
     k_replay_records<<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(g, L, sub0, zig, (const Entry *)bucket, offset, count,
-                                                                 nlist0, lpp, (int2 *)rec, cnt, nrec, err);
+                                                                 nlist0, lpp, (int2 *)rec, cnt, nrec, tmask, nchw,
+                                                                 err);
 }
 
 void launch_mc_bin(cudaStream_t s, const GridDev &g, const LayoutDev &L, const SubMC *sub, int nsub,
