@@ -158,15 +158,18 @@ def test_batch_path_line_widths_and_axis(gpu_lib, oracle_lib, variant):
     _batch_vs_oracle(oracle_lib, cube, rings)
 
 
-@pytest.mark.parametrize("wl", ["classic64", "global160"])
+@pytest.mark.parametrize("wl", ["classic64", "global160", "classic64_broad"])
 def test_batch_path_gradient_members_shared(gpu_lib, oracle_lib, wl):
     """A finite-difference batch (one ring's VROT, VDISP, INC or PA stepped per member): the members that differ
     from member 0 in a few sub-rings are computed as member 0's model plus the difference of those sub-rings'
-    clouds; their unsmoothed models are, bit for bit, those of the full computation (option 3 off), and agree
-    with the oracle's."""
+    clouds (member 0's taken out by its channel-count records, or, with lines broader than their window, deposited
+    again negated); their unsmoothed models are, bit for bit, those of the full computation (option 3 off), and
+    agree with the oracle's."""
     from bbarolo2_gb300 import _lib, configs, engine
     from bbarolo2_gb300.galmod import ring_rows_batch
-    cube, rings = configs.WORKLOADS[wl](galmodtype="MC")
+    cube, rings = configs.WORKLOADS[wl.replace("_broad", "")](galmodtype="MC")
+    if wl.endswith("_broad"):
+        rings.vdisp[:] = 90.                       # (a cloud's channels spread beyond the records' window)
     dm = engine.DiskModel(cube)
     st = dm.setup
     L = engine.BatchLikelihood(dm, np.ones(cube.array.shape, np.float32), None, maskmode=0, sigma=1.0)
