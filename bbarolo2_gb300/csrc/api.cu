@@ -1001,7 +1001,11 @@ static int profile_run(bbgpu_ctx *ctx, bool tm) {
     const float *K = ctx->kernel_set ? ctx->d_K : ctx->d_maps32;
     launch_prof_gram(s, K, bx, ctx->d_ppix, ctx->d_pw, ctx->d_pwy, ctx->npix_used, ctx->d_ent, ctx->d_ent + ctx->nent,
                      ctx->nent, nu, ctx->d_gpart, ctx->d_gh,
-                     shared && ctx->kernel_set ? KRows{ctx->d_ktab, nct, ntxc, shx, shy, ctx->d_gflag} : KRows{});
+                     shared && ctx->kernel_set
+                         ? KRows{ctx->d_ktab, nct, ntxc, shx, shy, ctx->d_gflag,
+                                 ctx->ky / 2 <= 8 && ctx->kx / 2 <= 8 ? ctx->d_blk : nullptr, (bx.bx + 7) / 8,
+                                 (bx.by + 7) / 8}
+                         : KRows{});
     ctx->launches += 2;
     CKL();
     if (tm) CK(cudaEventRecord(ctx->ev[3], s));

@@ -214,10 +214,14 @@ int prof_gram_tiles(int npix_used);
 // The rows of K that hold each convolution tile (ktab: nct tiles of 2^shx x 2^shy pixels, ntx a row, per row;
 // row 0's where a row's convolution left it unwritten), and gflag (rows x Gram tiles): 1 where a Gram tile took
 // row 0's sums. ktab == nullptr: every row's own K.
+// blk (nullable; the rows' 8 x 8 pixel blocks, nby x nbx a row: the row whose maps hold each) refines the test:
+// a pixel whose beam neighbourhood lies in blocks of row 0's maps has row 0's K.
 struct KRows {
     const int *ktab;
     int nct, ntx, shx, shy;
     int *gflag;
+    const int *blk;
+    int nbx, nby;
 };
 void launch_prof_gram(cudaStream_t s, const float *K, const ProfBox &box, const int *pix, const double *wpix,
                       const double *wy, int npix_used, const int *ent_i, const int *ent_j, int nent, int nb,

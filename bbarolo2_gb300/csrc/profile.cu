@@ -230,7 +230,21 @@ __global__ void __launch_bounds__(256) k_prof_gram(const T *__restrict__ K, Prof
             const int py = q / box.bx, px = q - py * box.bx;
             const int r = kr.ktab[(size_t)k * kr.nct + (py >> kr.shy) * kr.ntx + (px >> kr.shx)];
             srow[pp] = r;
-            own |= r != 0;
+            if (r != 0 && kr.blk) {
+                // the pixel's K is row 0's when no 8 x 8 block within the beam's reach (one block each way:
+                // half-widths of at most 8 pixels) holds the row's own maps
+                const int by0 = py >> 3, bx0 = px >> 3;
+                bool eq = true;
+                for (int dy = -1; dy <= 1 && eq; dy++)
+                    for (int dx = -1; dx <= 1; dx++) {
+                        const int yy = by0 + dy, xx = bx0 + dx;
+                        if (yy < 0 || xx < 0 || yy >= kr.nby || xx >= kr.nbx) continue;
+                        if (kr.blk[(size_t)k * kr.nby * kr.nbx + yy * kr.nbx + xx] != 0) { eq = false; break; }
+                    }
+                own |= !eq;
+            } else {
+                own |= r != 0;
+            }
         }
         own = __syncthreads_or(own);
         if (k != 0 && !own) {
