@@ -43,6 +43,10 @@ struct LayoutEntry {
 struct bbgpu_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    // the MC clouds' lists are built on a second stream of lower priority while the flux normalisation runs
+    // (joined before the deposits)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::string err;
     bool grid_set = false, kernel_set = false, cube_set = false;
     GridDev g{};
@@ -421,9 +425,18 @@ extern "C" int bbgpu_ctx_create(bbgpu_ctx **out, int device) {
     ctx = new (std::nothrow) bbgpu_ctx();
     if (!ctx) return BBGPU_ERR_NOMEM;
     ctx->device = device;
-    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    int prio_lo = 0, prio_hi = 0;
+    if (cudaSetDevice(device) != cudaSuccess || cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&ctx->stream, cudaStreamNonBlocking, prio_hi) != cudaSuccess) {
         cudaGetLastError();
         delete ctx;
+        return BBGPU_ERR_CUDA;
+    }
+    if (cudaStreamCreateWithPriority(&ctx->side, cudaStreamNonBlocking, prio_lo) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        bbgpu_ctx_destroy(ctx);
         return BBGPU_ERR_CUDA;
     }
     // ziggurat tables (fast-path bound kn fits 32 bits)
@@ -494,6 +507,9 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
     cudaFreeHost(ctx->h_sub); cudaFreeHost(ctx->h_mem); cudaFreeHost(ctx->h_out2); cudaFreeHost(ctx->h_err);
     for (int i = 0; i <= NTIMER; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     cudaGetLastError();
     delete ctx;
@@ -1219,14 +1235,59 @@ static int an_segments(bbgpu_ctx *ctx) {
     return 0;
 }
 
+// The MC clouds' tile lists on stream s: each (member, cloud) pair binned to its pixel, the lists' offsets, the
+// entries (their fixed-point fluxes left to k_entry_fix: they come from the flux normalisation, which may still
+// be running), and, when members replay member 0's clouds, member 0's channel counts. None of it reads what the
+// flux normalisation writes (the clouds' densities and fluxes, the members' exponents).
+static int mc_lists(bbgpu_ctx *ctx, cudaStream_t s, bool tm) {
+    const GridDev &g = ctx->g;
+    const LayoutDev &L = ctx->cur->dev;
+    CK(cudaMemsetAsync(ctx->d_tcount, 0, sizeof(int) * (size_t)(ctx->ntile_total * NOWN + 1), s));
+    launch_mc_bin(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->d_cstart, ctx->d_cseg, ctx->mc_nseg,
+                  ctx->mc_ntot, ctx->tx, ctx->ty, ctx->d_pix, ctx->d_tcount, ctx->d_err);
+    CKL();
+    if (tm) CK(cudaEventRecord(ctx->ev[5], s));
+    launch_scan_tiles(s, ctx->d_tcount, ctx->d_toff, ctx->d_tcur, ctx->ntile_total * NOWN, ctx->d_scan);
+    CKL();
+    if (tm) CK(cudaEventRecord(ctx->ev[6], s));
+    launch_mc_scatter(s, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->d_cstart, ctx->d_cseg, ctx->mc_nseg,
+                      ctx->mc_ntot, ctx->tx, ctx->ty, ctx->d_pix, ctx->d_tcur, ctx->d_bucket, 1);
+    CKL();
+    if (ctx->mc_records) {
+        const MemberDev &M0 = ctx->mem_host[0];
+        launch_replay_records(s, g, L, ctx->d_sub, ctx->d_zig, ctx->d_bucket, ctx->d_toff, ctx->d_tcount,
+                              (M0.tile_off + M0.ntx * M0.nty) * NOWN, ctx->tx * ctx->ty, ctx->d_rp_rec, ctx->d_rp_cnt,
+                              ctx->d_rp_n, ctx->d_tmask, ctx->nchw, ctx->d_err);
+        CKL();
+    }
+    return 0;
+}
+
 static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
     if (!ctx->uploaded) return fail(ctx, BBGPU_ERR_STATE, "run before upload");
     const GridDev &g = ctx->g;
     cudaStream_t s = ctx->stream;
     const bool tm = ctx->timing;
+    const bool mc = ctx->galmodtype != BBGPU_ANALYTIC;
+    if (mc && ctx->mc_dirty) {
+        int rc = mc_segments(ctx);
+        if (rc) return rc;
+    }
+    // with a flux normalisation (and the stage timers off), the MC lists are built on the second stream while
+    // it runs
+    const bool side = mc && ctx->prof_uploaded && !tm;
     if (tm) CK(cudaEventRecord(ctx->ev[0], s));
+    if (side) {
+        CK(cudaEventRecord(ctx->ev_fork, s));
+        CK(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+        int rc = mc_lists(ctx, ctx->side, false);
+        cudaError_t e = cudaEventRecord(ctx->ev_join, ctx->side);
+        if (rc) return rc;
+        if (e != cudaSuccess) return fail(ctx, BBGPU_ERR_CUDA, "cudaEventRecord: %s", cudaGetErrorString(e));
+    }
     if (ctx->prof_uploaded) {
         int rc = profile_run(ctx, tm);
+        if (side) cudaStreamWaitEvent(s, ctx->ev_join, 0);
         if (rc) return rc;
     } else if (tm) {
         for (int i = 1; i <= 4; i++) CK(cudaEventRecord(ctx->ev[i], s));
@@ -1254,20 +1315,12 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
         if (tm) CK(cudaEventRecord(ctx->ev[11], s));
     } else {
         const LayoutDev &L = ctx->cur->dev;
-        if (ctx->mc_dirty) {
-            int rc = mc_segments(ctx);
+        if (!side) {
+            int rc = mc_lists(ctx, s, tm);
             if (rc) return rc;
         }
-        CK(cudaMemsetAsync(ctx->d_tcount, 0, sizeof(int) * (size_t)(ctx->ntile_total * NOWN + 1), s));
-        launch_mc_bin(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->d_cstart, ctx->d_cseg, ctx->mc_nseg,
-                      ctx->mc_ntot, ctx->tx, ctx->ty, ctx->d_pix, ctx->d_tcount, ctx->d_err);
-        CKL();
-        if (tm) CK(cudaEventRecord(ctx->ev[5], s));
-        launch_scan_tiles(s, ctx->d_tcount, ctx->d_toff, ctx->d_tcur, ctx->ntile_total * NOWN, ctx->d_scan);
-        CKL();
-        if (tm) CK(cudaEventRecord(ctx->ev[6], s));
-        launch_mc_scatter(s, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->d_cstart, ctx->d_cseg, ctx->mc_nseg,
-                          ctx->mc_ntot, ctx->tx, ctx->ty, ctx->d_pix, ctx->d_tcur, ctx->d_bucket);
+        launch_entry_fix(s, ctx->d_sub, ctx->d_toff, ctx->d_tcount, ctx->ntile_total * NOWN, ctx->mc_ntot,
+                         ctx->d_bucket);
         CKL();
         if (tm) CK(cudaEventRecord(ctx->ev[7], s));
         if (ctx->mc_n2 || ctx->mc_n3) {
@@ -1280,13 +1333,6 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
             const Replay rp = ctx->mc_records ? Replay{(const int2 *)ctx->d_rp_rec, ctx->d_rp_cnt, ctx->d_rp_n,
                                                        ctx->d_chg, ctx->nchw, ctx->d_tmask}
                                               : Replay{nullptr, nullptr, nullptr, nullptr, 0, nullptr};
-            if (ctx->mc_records) {
-                const MemberDev &M0 = ctx->mem_host[0];
-                launch_replay_records(s, g, L, ctx->d_sub, ctx->d_zig, ctx->d_bucket, ctx->d_toff, ctx->d_tcount,
-                                      (M0.tile_off + M0.ntx * M0.nty) * NOWN, ctx->tx * ctx->ty, ctx->d_rp_rec,
-                                      ctx->d_rp_cnt, ctx->d_rp_n, ctx->d_tmask, ctx->nchw, ctx->d_err);
-                CKL();
-            }
             if (ctx->mc_n2) {
                 launch_mc_deposit(s, g, L, ctx->d_sub, ctx->nsub, ctx->d_mem, ctx->mem_host.data(), ctx->nb,
                                   ctx->tx, ctx->ty, ctx->d_toff, ctx->d_tcount, ctx->d_bucket, ctx->d_zig,

@@ -63,7 +63,11 @@ void launch_scan_tiles(cudaStream_t s, const int *count, int *offset, int *curso
 #define ENTRY_BYTES 32
 void launch_mc_scatter(cudaStream_t s, const LayoutDev &L, const SubMC *sub, int nsub, const MemberDev *mem,
                        const long long *cstart, const int *cseg, int nseg, long long ntot, int tx, int ty,
-                       const int *pix, int *cursor, void *bucket);
+                       const int *pix, int *cursor, void *bucket, int defer_fix);
+// The fixed-point flux of the entries of a scatter with defer_fix (after the sub-ring constants are final):
+// ntot bounds the entries (the (member, cloud) pairs), nlist lists
+void launch_entry_fix(cudaStream_t s, const SubMC *sub, const int *offset, const int *count, int nlist,
+                      long long ntot, void *bucket);
 // Deposits the clouds of every tile into a shared-memory fixed-point tile and writes the model
 // (by, bx, nz) float32 of each member at model + k * mstride (and, if model64, float64 sums); lean: the batch
 // qualifies for the fast kernels (one line, a linear channel map, at most 128 samples per cloud).

@@ -189,7 +189,7 @@ __device__ __forceinline__ void cloud_centre(const SubMC &S, float4 cf, int nl, 
 __global__ void k_mc_scatter(LayoutDev L, const SubMC *__restrict__ sub, int nsub, const MemberDev *__restrict__ mem,
                              const long long *__restrict__ cstart, const int4 *__restrict__ cseg, int nseg,
                              long long ntot, int tx, int ty, const int *__restrict__ pix, int *__restrict__ cursor,
-                             Entry *__restrict__ bucket) {
+                             Entry *__restrict__ bucket, int defer_fix) {
     long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= ntot) return;
     int p = pix[idx];
@@ -211,12 +211,28 @@ __global__ void k_mc_scatter(LayoutDev L, const SubMC *__restrict__ sub, int nsu
     e.meta = (nv & 0xffff) | (lp << 16) | (half << 24) | (cl.src != k ? 1 << 25 : 0);
     float epsc;
     cloud_centre(S, cf, 0, e.tc, epsc);
-    e.fix = cl.sign < 0 ? -S.fix[half][0] : S.fix[half][0];
+    // defer_fix: the fixed-point flux is not known yet (the flux normalisation computes it while the clouds are
+    // binned): the entry holds its sub-ring constants' index and sign, for k_entry_fix
+    if (defer_fix) e.fix = (long long)((size_t)cl.src * nsub + ir) * 2 + (cl.sign < 0 ? 1 : 0);
+    else e.fix = cl.sign < 0 ? -S.fix[half][0] : S.fix[half][0];
     e.sg = S.sg[0];
     // the cloud's largest |normal| is at an end of its sorted run
     const float nmax = fmaxf(fabsf(__ldg(&L.nf[e.pb])), fabsf(__ldg(&L.nf[e.pb + nv - 1])));
     e.eps = fmaf(nmax, fabsf(e.sg) * EPS_REL, epsc);
     bucket[slot] = e;
+}
+
+// The fixed-point flux of the entries that k_mc_scatter left as (sub-ring constants' index, sign): one thread
+// per entry of the lists (their number: the last list's offset plus its count).
+__global__ void k_entry_fix(const SubMC *__restrict__ sub, const int *__restrict__ offset,
+                            const int *__restrict__ count, int nlist, Entry *__restrict__ bucket) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long total = (long long)offset[nlist - 1] + count[nlist - 1];
+    if (i >= total) return;
+    Entry &e = bucket[i];
+    const long long v = e.fix;
+    const long long f = sub[(size_t)(v >> 1)].fix[(e.meta >> 24) & 1][0];
+    e.fix = (v & 1) ? -f : f;
 }
 
 // the exact channel of a sub-cloud (bbarolo/galmod.py:153-170), not clipped to the cube
@@ -1363,10 +1379,17 @@ void launch_scan_tiles(cudaStream_t s, const int *count, int *offset, int *curso
 
 void launch_mc_scatter(cudaStream_t s, const LayoutDev &L, const SubMC *sub, int nsub, const MemberDev *mem,
                        const long long *cstart, const int *cseg, int nseg, long long ntot, int tx, int ty,
-                       const int *pix, int *cursor, void *bucket) {
+                       const int *pix, int *cursor, void *bucket, int defer_fix) {
     if (ntot == 0 || nseg == 0) return;
     k_mc_scatter<<<(unsigned)((ntot + 255) / 256), 256, 0, s>>>(L, sub, nsub, mem, cstart, (const int4 *)cseg, nseg,
-                                                                ntot, tx, ty, pix, cursor, (Entry *)bucket);
+                                                                ntot, tx, ty, pix, cursor, (Entry *)bucket,
+                                                                defer_fix);
+}
+
+void launch_entry_fix(cudaStream_t s, const SubMC *sub, const int *offset, const int *count, int nlist,
+                      long long ntot, void *bucket) {
+    if (ntot == 0 || nlist == 0) return;
+    k_entry_fix<<<(unsigned)((ntot + 255) / 256), 256, 0, s>>>(sub, offset, count, nlist, (Entry *)bucket);
 }
 
 bool mc_deposit_shares(int lean, bool model64, int tx, int ty) {

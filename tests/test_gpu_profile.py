@@ -139,7 +139,8 @@ def test_batch_profile_shared_members(gpu_lib, oracle_lib, galmodtype):
     """A finite-difference batch (steps of one ring's VROT, VDISP, INC or PA): the members whose ring maps are
     the base member's (velocity steps) share its profile, those that differ in a few sub-rings (geometry steps)
     get member 0's maps plus the difference; both give, bit for bit, what every member computed from all its
-    samples gives, and the densities agree with the oracle's."""
+    samples gives, and the densities agree with the oracle's. The same with the stage timers on (the MC clouds'
+    lists then built on the context's stream after the flux normalisation, not beside it on the second stream)."""
     from bbarolo2_gb300 import _lib
     from bbarolo2_gb300.galmod import ring_rows_batch
     from oracle import cpu_baseline as CB
@@ -155,21 +156,27 @@ def test_batch_profile_shared_members(gpu_lib, oracle_lib, galmodtype):
     rows = np.stack(rows)
     ctx = dm.ctx
     res = {}
-    for share in (0, 1):
-        ctx.set_option(_lib.OPT_SHARE, share)
-        ll = L.evaluate(rows, rings, seed=1, galmodtype=galmodtype)
-        x, st = L.last_profile()
-        res[share] = (ll, x, st)
-        if share:
-            nprof, full, delta, replay = ctx.shared_members()
-            assert nprof < len(rows)
-            if galmodtype == "MC":    # (velocity steps as a difference, geometry steps replaying member 0's clouds)
-                assert delta > 0 and replay > 0, (full, delta, replay)
-    ctx.set_option(_lib.OPT_SHARE, 1)
-    np.testing.assert_array_equal(res[0][0], res[1][0])
-    np.testing.assert_array_equal(res[0][1], res[1][1])
-    np.testing.assert_array_equal(res[0][2], res[1][2])
-    ll, x, st = res[1]
+    try:
+        for share, timing in ((0, 0), (1, 0), (1, 1)):
+            ctx.set_option(_lib.OPT_SHARE, share)
+            ctx.set_option(_lib.OPT_TIMING, timing)
+            ll = L.evaluate(rows, rings, seed=1, galmodtype=galmodtype)
+            x, st = L.last_profile()
+            res[share, timing] = (ll, x, st)
+            if share:
+                nprof, full, delta, replay = ctx.shared_members()
+                assert nprof < len(rows)
+                if galmodtype == "MC":    # (velocity steps as a difference, geometry steps replaying member 0's)
+                    assert delta > 0 and replay > 0, (full, delta, replay)
+            if timing:
+                assert ctx.run_times()["prof_solve"] > 0
+    finally:
+        ctx.set_option(_lib.OPT_SHARE, 1)
+        ctx.set_option(_lib.OPT_TIMING, 0)
+    for key in ((0, 0), (1, 1)):
+        for i in range(3):
+            np.testing.assert_array_equal(res[key][i], res[1, 0][i])
+    ll, x, st = res[1, 0]
     assert np.all(st == 0), st
     sr, nv, descs, boxes = L.prepare(rows, rings, seed=1)
     P = CB.setup_payload(dm, sr, nv, boxes, 1, data, L.mask, L.maskmode, like=L, rows=rows, proto=rings,
