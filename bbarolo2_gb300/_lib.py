@@ -23,7 +23,8 @@ SYMBOLS = ("bbgpu_ctx_create", "bbgpu_ctx_destroy", "bbgpu_last_error", "bbgpu_v
            "bbgpu_residuals_fracerr", "bbgpu_norm", "bbgpu_eval_upload", "bbgpu_eval_run", "bbgpu_eval_download",
            "bbgpu_eval_batch", "bbgpu_eval_model", "bbgpu_sync", "bbgpu_set_option", "bbgpu_launch_count",
            "bbgpu_last_run_times", "bbgpu_kernel_name", "bbgpu_transfer_bytes", "bbgpu_shared_members",
-           "bbgpu_sumsq_residuals_noalloc", "bbgpu_set_profile", "bbgpu_eval_upload_profile", "bbgpu_eval_profile", "bbgpu_solve_profile")
+           "bbgpu_sumsq_residuals_noalloc", "bbgpu_set_profile", "bbgpu_eval_upload_profile", "bbgpu_eval_profile", "bbgpu_solve_profile",
+           "bbgpu_subrings_rows")
 
 
 class Grid(C.Structure):
@@ -70,6 +71,7 @@ def load(path=None):
     proto = {
         "bbgpu_ctx_create": (i, [C.POINTER(vp), i]),
         "bbgpu_ctx_destroy": (i, [vp]),
+        "bbgpu_subrings_rows": (i, [vp, i, i, i, vp, vp, vp, vp, vp, vp, vp, i64, vp, vp, vp, i]),
         "bbgpu_last_error": (C.c_char_p, [vp]),
         "bbgpu_version": (i, []),
         "bbgpu_set_grid": (i, [vp, C.POINTER(Grid), vp, vp, vp, vp]),

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <vector>
 
+#include "../../include/bbgpu.h"
 #include "internal.h"
 
 #include <unordered_map>
@@ -730,4 +731,86 @@ void bbh_profile_consts(const double *R, int n, int *lc, double *lv, int *ord, u
         near[i - 1] = std::min(dl, dh) < 0.25 * med;
     }
     *norm = nrm;
+}
+
+// The sub-ring tables of a batch of thin-disk ring sets on one radius grid (bbarolo/galmod.py:761-851, the
+// interpolation v0 + ((v1 - v0) / dur) dr per sub-ring, constant before the first radius), in the float64
+// operations and order of the reference: member 0 in full, every other member from member 0's table and the
+// sub-rings next to a ring whose values differ from member 0's (the rest are member 0's values).
+extern "C" int bbgpu_subrings_rows(const double *rows, int nb, int nr, int nsub, const int64_t *i1, const double *dr,
+                                   const double *dseg, const uint8_t *cst, const double *radii, const double *edgew,
+                                   const double *side, int64_t nvtmp, double *sr, int64_t *nv, double *ms, int nsm) {
+    if (nb < 1 || nr < 2 || nsub < 1 || !rows || !i1 || !dr || !dseg || !cst || !radii || !side || !sr || !nv ||
+        (ms && nsm < nsub))
+        return BBGPU_ERR_ARG;
+    for (int s = 0; s < nsub; s++)
+        if (i1[s] < 1 || i1[s] >= nr) return BBGPU_ERR_ARG;
+    constexpr int NV = 13;                     // interpolated rows 1 .. 13 of the table
+    // (the ring-value row of each interpolated row, RING_KEYS order, and its transform)
+    static const int src[NV] = {4, 6, 7, 5, 10, 11, 8, 9, 12, 13, 1, 2, 3};
+    const double d2r = 3.141592653589793 / 180.0;
+    std::vector<double> V0((size_t)NV * nr), V((size_t)NV * nr);
+    std::vector<unsigned char> D((size_t)nr);
+    auto values = [&](const double *rw, double *out) {
+        for (int f = 0; f < NV; f++) {
+            const double *x = rw + (size_t)src[f] * nr;
+            double *o = out + (size_t)f * nr;
+            for (int j = 0; j < nr; j++) {
+                const double v = x[j];
+                switch (f) {
+                    case 0: case 1: case 2: case 3: case 12: o[j] = v * 1000.; break;
+                    case 5: case 7: o[j] = v / 60.; break;
+                    case 6: o[j] = v * 1000. * 60.; break;
+                    case 8: case 9: o[j] = v * d2r; break;
+                    default: o[j] = v; break;
+                }
+            }
+        }
+    };
+    auto interp = [&](const double *Vv, int f, int s) -> double {
+        const double *v = Vv + (size_t)f * nr;
+        if (cst[s]) return v[0];
+        const int64_t j = i1[s];
+        const double v0 = v[j - 1];
+        return v0 + ((v[j] - v0) / dseg[j - 1]) * dr[s];
+    };
+    const size_t tsz = (size_t)BBGPU_NSR * nsub;
+    values(rows, V0.data());
+    for (int k = 0; k < nb; k++) {
+        double *t = sr + (size_t)k * tsz;
+        if (k == 0) {
+            memcpy(t, radii, sizeof(double) * nsub);
+            for (int f = 0; f < NV; f++)
+                for (int s = 0; s < nsub; s++) t[(size_t)(f + 1) * nsub + s] = interp(V0.data(), f, s);
+            if (edgew)
+                for (int s = 0; s < nsub; s++) t[(size_t)5 * nsub + s] *= edgew[s];
+            memcpy(t + (size_t)14 * nsub, side, sizeof(double) * 2 * nsub);
+        } else {
+            const double *rw = rows + (size_t)k * 17 * nr;
+            memcpy(t, sr, sizeof(double) * tsz);
+            // the rings whose values (of the interpolated rows) differ from member 0's
+            bool any = false;
+            for (int j = 0; j < nr; j++) D[j] = 0;
+            for (int f = 0; f < NV; f++) {
+                const double *a = rw + (size_t)src[f] * nr, *b = rows + (size_t)src[f] * nr;
+                if (!memcmp(a, b, sizeof(double) * nr)) continue;
+                for (int j = 0; j < nr; j++)
+                    if (memcmp(a + j, b + j, sizeof(double))) D[j] = 1, any = true;
+            }
+            if (any) {
+                values(rw, V.data());
+                for (int s = 0; s < nsub; s++) {
+                    const bool chg = cst[s] ? D[0] : (D[i1[s] - 1] || D[i1[s]]);
+                    if (!chg) continue;
+                    for (int f = 0; f < NV; f++) t[(size_t)(f + 1) * nsub + s] = interp(V.data(), f, s);
+                    if (edgew) t[(size_t)5 * nsub + s] *= edgew[s];
+                }
+            }
+        }
+        for (int s = 0; s < nsub; s++) nv[(size_t)k * nsub + s] = t[(size_t)4 * nsub + s] == 0.0 ? 1 : nvtmp;
+        if (ms)
+            for (int r = 0; r < BBGPU_NSR; r++)
+                memcpy(ms + ((size_t)k * BBGPU_NSR + r) * nsm, t + (size_t)r * nsub, sizeof(double) * nsub);
+    }
+    return BBGPU_OK;
 }

@@ -401,7 +401,16 @@ class BatchLikelihood:
         """Host side of a batch: sub-ring tables, boxes and descriptors of the ring-value rows (B, 17, nr)."""
         dm = self.model
         mrows, mr = dm.model_rows(rows, proto)
-        sr, nv = subrings_batch(dm.setup, mr, mrows)
+        ms = None
+        if self._prof is not None:
+            if not np.array_equal(np.asarray(proto.radii, float), self._prof["radii"]):
+                raise ValueError("the radii differ from those given to set_profile")
+            # the ring maps' tables: the model's sub-rings (written by subrings_batch), then the exterior's
+            pm = self.profile_maps(rows)
+            nsub = dm.setup.grid(mr).nsub
+            ms = np.empty((pm.shape[0], pm.shape[1], nsub + pm.shape[2]))
+            ms[:, :, nsub:] = pm
+        sr, nv = subrings_batch(dm.setup, mr, mrows, out_ms=ms)
         B = sr.shape[0]
         s = seed32(dm.setup.iseed if seed is None else seed)
         blo, bhi = self._boxes(rows, proto)
@@ -413,10 +422,8 @@ class BatchLikelihood:
         descs["sigma2"] = self.sigma ** 2
         descs["eps2"] = (self.eps or 0.) ** 2
         boxes = list(zip(blo.tolist(), bhi.tolist()))
-        if self._prof is not None:
-            if not np.array_equal(np.asarray(proto.radii, float), self._prof["radii"]):
-                raise ValueError("the radii differ from those given to set_profile")
-            self._maps_sr = np.ascontiguousarray(np.concatenate([sr, self.profile_maps(rows)], axis=2))
+        if ms is not None:
+            self._maps_sr = ms
         return sr, nv, descs, boxes
 
     def evaluate(self, rows, proto, seed=None, galmodtype=None):

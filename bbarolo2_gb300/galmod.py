@@ -537,12 +537,30 @@ def ring_rows_batch(rings_list):
     return np.stack([np.vstack([np.asarray(getattr(r, k), float) for k in RING_KEYS]) for r in rings_list])
 
 
-def subrings_batch(setup, proto, rows):
+_NATIVE = None
+
+
+def _native_subrings():
+    """The library's ``bbgpu_subrings_rows`` (C++), or None where the library is not built."""
+    global _NATIVE
+    if _NATIVE is None:
+        try:
+            from . import _lib
+            _NATIVE = _lib.load().bbgpu_subrings_rows
+        except Exception:
+            _NATIVE = False
+    return _NATIVE or None
+
+
+def subrings_batch(setup, proto, rows, out_ms=None, native=True):
     """Sub-ring tables of a batch of ring sets that share the radii and the options of ``proto`` (edges, thick
     layer, empty): rows (B, 17, nr) in RING_KEYS order -> (sr (B, 16, nsub), nv (B, nsub)).
 
     The same elementwise float64 operations as ``GalmodSetup.subrings`` (bit-equal tables), vectorised over
-    the batch: the fits change ring values, not radii, between evaluations."""
+    the batch: the fits change ring values, not radii, between evaluations. A thin disk of two or more rings
+    is tabulated in C++ (``bbgpu_subrings_rows``: the same operations, member 0 in full and the other members'
+    sub-rings next to a ring that differs from member 0's), native=False or a thick layer with numpy.
+    out_ms (B, 16, nsm) C-contiguous, nsm >= nsub: also receives the tables in its first nsub columns."""
     rows = np.asarray(rows, float)
     B = rows.shape[0]
     radii, xpos, ypos, vsys, vrot, vdisp, vrad, vvert, dvdz, zcyl, dens, z0, inc, phi, z0t, fth, vdt = \
@@ -555,6 +573,30 @@ def subrings_batch(setup, proto, rows):
         raise ValueError("GALMOD ERROR: Negative scale height not allowed.")
     thick = proto.thick() if hasattr(proto, "thick") else False
     g = setup.grid(proto)
+    nvtmp = setup.nvpar if setup.nvpar >= 1 else setup.nsubs
+    fn = _native_subrings() if native and not thick and g.nsub and rows.shape[2] > 1 else None
+    if fn is not None:
+        from . import _lib
+        edge = getattr(proto, "edge", None)
+        edgew = None if edge is None else np.ascontiguousarray(
+            edge_weights(g.radii * 60., setup.radsep * 60., float(edge), float(getattr(proto, "edgewidth", 0.))),
+            dtype=float)
+        side = np.ones((2, g.nsub))
+        for k, e in enumerate(setup.side_edges(proto)[::-1]):
+            if e is not None:
+                side[k] = edge_weights(g.radii * 60., setup.radsep * 60., e)
+        rows_c = np.ascontiguousarray(rows)
+        sr = np.empty((B, 16, g.nsub))
+        nv = np.empty((B, g.nsub), np.int64)
+        if out_ms is not None:
+            assert out_ms.flags.c_contiguous and out_ms.dtype == np.float64 and out_ms.shape[:2] == (B, 16) \
+                and out_ms.shape[2] >= g.nsub
+        rc = fn(_lib.ptr(rows_c), B, rows.shape[2], g.nsub, _lib.ptr(g.i1), _lib.ptr(g.dr), _lib.ptr(g._dseg),
+                _lib.ptr(g.const.view(np.uint8)), _lib.ptr(g.radii), _lib.ptr(edgew), _lib.ptr(side), int(nvtmp),
+                _lib.ptr(sr), _lib.ptr(nv), _lib.ptr(out_ms), 0 if out_ms is None else out_ms.shape[2])
+        if rc != 0:
+            raise ValueError(f"bbgpu_subrings_rows: status {rc}")
+        return sr, nv
     V = [vrot * 1000., vrad * 1000., vvert * 1000., vdisp * 1000., dens, z0 / 60., dvdz * 1000 * 60, zcyl / 60.,
          np.radians(inc), np.radians(phi), xpos, ypos, vsys * 1000.]
     if thick:
@@ -588,8 +630,9 @@ def subrings_batch(setup, proto, rows):
         sr[:, 14:16] = side
     else:
         sr = np.concatenate([sr[:, :14], np.broadcast_to(side, (B, 2, sr.shape[2]))], axis=1)
-    nvtmp = setup.nvpar if setup.nvpar >= 1 else setup.nsubs
     nv = np.where(sr[:, 4] == 0, 1, nvtmp).astype(np.int64)
+    if out_ms is not None:
+        out_ms[:, :, :sr.shape[2]] = sr
     return np.ascontiguousarray(sr), np.ascontiguousarray(nv)
 
 

@@ -174,6 +174,20 @@ int bbgpu_sumsq_residuals_noalloc(const double *model, const float *data, const 
                                   const uint8_t *region, int nz, int ny, int nx, double sigma2, double eps2,
                                   double *out2, void *stream);
 
+/* ---- host set-up ------------------------------------------------------------------------------------ */
+/* The sub-ring tables of a batch of thin-disk ring sets on one radius grid (bbarolo/galmod.py:761-851, the
+ * reference's float64 operations in its order; host only, no context): rows (nb, 17, nr) the model rings'
+ * values (radii, xpos, ypos, vsys, vrot, vdisp, vrad, vvert, dvdz, zcyl, dens, z0, inc, phi, z0thick, fthick,
+ * vdispthick), nr >= 2; the grid's nsub sub-rings: i1 (the ring after each sub-ring's segment, 1 .. nr-1), dr
+ * (offset from the segment's first ring), dseg (nr - 1 ring spacings), cst (1: before the first ring, the
+ * first ring's values), radii; edgew (nsub, NULL: none) the weights of the outer edge on the densities, side
+ * (2, nsub) the side weights; nvtmp the velocity samples of a sub-ring with a dispersion. Writes sr (nb, 16,
+ * nsub), nv (nb, nsub) and, if ms is not NULL, the same tables into the first nsub columns of ms (nb, 16,
+ * nsm). Replaces GalmodSetup.subrings per ring set (the vectorised subrings_batch of the engine). */
+int bbgpu_subrings_rows(const double *rows, int nb, int nr, int nsub, const int64_t *i1, const double *dr,
+                        const double *dseg, const uint8_t *cst, const double *radii, const double *edgew,
+                        const double *side, int64_t nvtmp, double *sr, int64_t *nv, double *ms, int nsm);
+
 /* ---- counters --------------------------------------------------------------------------------------- */
 /* Kernel launches issued by the context so far, and the device time (ms) of the last bbgpu_eval_run split
  * into its kernels: times[0..n) in the order of bbgpu_kernel_name(i). */

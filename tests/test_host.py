@@ -80,6 +80,49 @@ def test_subrings_batch_gradient_steps(case):
         assert np.array_equal(sr[k], s2) and np.array_equal(nv[k], n2), k
 
 
+@pytest.mark.parametrize("edges", [False, True])
+@pytest.mark.parametrize("case", _cases(), ids=lambda c: c[1]["name"])
+def test_subrings_batch_native(case, edges):
+    """The C++ tables (bbgpu_subrings_rows) against the numpy ones, bit for bit: random batches (every member
+    differs from member 0 in random rings), gradient batches, an outer edge and side edges, the copy into the
+    first columns of a wider table."""
+    if galmod._native_subrings() is None:
+        pytest.skip("library not built")
+    z, m = case
+    cube, rings, mode = _rebuild(m["name"])
+    st = galmod.GalmodSetup(cube, densflux=True)
+    mr = galmod.model_rings(rings, mode, st.radsep)
+    if edges:
+        mr.edge, mr.edgewidth = float(mr.radii[-1] * 60. * 0.8), 0.
+        mr.edgeapp, mr.edgerec = float(mr.radii[-1] * 60. * 0.7), float(mr.radii[-1] * 60. * 0.9)
+    if mr.thick() or mr.nr < 2:
+        pytest.skip("thick layer or one ring: numpy tables")
+    base = galmod.ring_rows_batch([mr])[0]
+    rng = np.random.default_rng(5)
+    rand = base[None].repeat(12, axis=0)
+    for k in range(1, 12):
+        sel = rng.random(mr.nr) < 0.3
+        for row in (1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13):
+            rand[k, row, sel] += rng.normal(0., 0.5, sel.sum()) * (1. + abs(base[row, sel]))
+        rand[k, 5] = np.abs(rand[k, 5])
+        rand[k, 10] = np.abs(rand[k, 10])
+        rand[k, 11] = np.abs(rand[k, 11])
+    rand[3, 5, :] = 0.                               # (no dispersion: one velocity sample)
+    grad = [base]
+    for j in range(mr.nr):
+        for row, step in ((4, 3.0), (12, 1.0), (10, 0.5)):
+            r = base.copy()
+            r[row, j] += step
+            grad.append(r)
+    for rows in (rand, np.stack(grad)):
+        sr0, nv0 = galmod.subrings_batch(st, mr, rows, native=False)
+        ms = np.full(sr0.shape[:2] + (sr0.shape[2] + 3,), 7.)
+        sr1, nv1 = galmod.subrings_batch(st, mr, rows, out_ms=ms)
+        assert np.array_equal(sr0.view(np.uint64), sr1.view(np.uint64))
+        assert np.array_equal(nv0, nv1)
+        assert np.array_equal(ms[:, :, :sr0.shape[2]], sr0) and np.all(ms[:, :, sr0.shape[2]:] == 7.)
+
+
 @pytest.mark.parametrize("wl", ["classic64", "global160", "bayes256"])
 def test_beam_kernel(wl):
     z = G.load("beam_conv.npz")
