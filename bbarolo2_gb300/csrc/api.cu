@@ -902,6 +902,11 @@ static int batch_prepare(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const
     uint64_t seed = descs[0].seed;
     for (int k = 1; k < nb; k++) {
         const double *s = sr + (size_t)k * BBGPU_NSR * nsub;
+        // (the counts are a function of the radii, densities and velocity samples: equal rows, equal counts)
+        if (descs[k].seed == seed && !memcmp(s, sr, sizeof(double) * nsub) &&
+            !memcmp(s + (size_t)5 * nsub, sr + (size_t)5 * nsub, sizeof(double) * nsub) &&
+            !memcmp(nv + (size_t)k * nsub, nv, sizeof(int64_t) * nsub))
+            continue;
         bbh_cloud_counts(s, nsub, nv + (size_t)k * nsub, &g, nc.data(), nvv.data());
         if (descs[k].seed != seed || memcmp(nc.data(), nc0.data(), sizeof(int) * nsub) ||
             memcmp(nvv.data(), nv0.data(), sizeof(int) * nsub) || memcmp(s, sr, sizeof(double) * nsub))
