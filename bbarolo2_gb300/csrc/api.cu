@@ -925,23 +925,23 @@ static int batch_prepare(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const
     if ((rc = hgrow(ctx, &ctx->h_reuse, &ctx->h_reuse_cap, (size_t)nb * (nsub ? nsub : 1)))) return rc;
     memset(ctx->h_reuse, 0, (size_t)nsub);
     ctx->mem_host.resize(nb);
-    std::vector<uint16_t> dmask;
+    std::vector<uint16_t> dmask((size_t)nsub);
+    ctx->mc_same_nd.assign((size_t)nb * nsub, 1);
     int toff = 0;
     for (int k = 0; k < nb; k++) {
         const bbgpu_eval_desc &d = descs[k];
         if (d.blo0 < 0 || d.blo1 < 0 || d.bhi0 > g.nx || d.bhi1 > g.ny || d.bhi0 < d.blo0 || d.bhi1 < d.blo1)
             return fail(ctx, BBGPU_ERR_ARG, "eval: member %d: box outside the cube", k);
         SubMC *S = ctx->h_sub + (size_t)k * nsub;
+        // (the rows of each column that differ from member 0's: the constants reused, and the columns that
+        // differ in the density only)
+        if (k) bbh_column_diff(sr + (size_t)k * BBGPU_NSR * nsub, sr, nsub, dmask.data());
         int e = bbh_submc(sr + (size_t)k * BBGPU_NSR * nsub, nsub, nc0.data(), nv0.data(), &g, S,
-                          k ? sr : nullptr, k ? ctx->h_sub : nullptr, k ? ctx->h_reuse + (size_t)k * nsub : nullptr);
-        if (k == 0) {
-            ctx->mc_same_nd.assign((size_t)nb * nsub, 1);
-            dmask.resize((size_t)nsub);
-        } else {
-            bbh_column_diff(sr + (size_t)k * BBGPU_NSR * nsub, sr, nsub, dmask.data());
+                          k ? sr : nullptr, k ? ctx->h_sub : nullptr, k ? ctx->h_reuse + (size_t)k * nsub : nullptr,
+                          k ? dmask.data() : nullptr);
+        if (k)
             for (int ir = 0; ir < nsub; ir++)
                 ctx->mc_same_nd[(size_t)k * nsub + ir] = (dmask[ir] & ~(1u << 5)) ? 0 : 1;
-        }
         MemberDev &M = ctx->mem_host[k];
         if ((rc = member_desc(ctx, k, d, e, need_cube, M))) return rc;
         M.ntx = (M.bx + ctx->tx - 1) / ctx->tx;
@@ -2031,11 +2031,15 @@ extern "C" int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *
     if (zc.zq.size() > ((size_t)1 << 24)) zc.clear();
     const size_t zold = zc.uploaded;
     std::vector<int> fix(nb);
+    // the rows of each column that differ from member 0's (the constants reused, the rows of the maps)
+    std::vector<uint16_t> pdiff((size_t)nb * nsm, 0);
     for (int k = 0; k < nb; k++) {
+        if (k) bbh_column_diff(sr_maps + (size_t)k * BBGPU_NSR * nsm, sr_maps, nsm, pdiff.data() + (size_t)k * nsm);
         const int e = bbh_an_subs(sr_maps + (size_t)k * BBGPU_NSR * nsm, nsm, &g, nzq, bx.blo0, bx.blo1, bx.bhi0,
                                   bx.bhi1, ctx->h_cd2i.data(), 1, widx, wval, ctx->h_psub + (size_t)k * nsm, zc,
                                   k ? sr_maps : nullptr, k ? ctx->h_psub : nullptr,
-                                  k ? ctx->h_preuse + (size_t)k * nsm : nullptr);
+                                  k ? ctx->h_preuse + (size_t)k * nsm : nullptr,
+                                  k ? pdiff.data() + (size_t)k * nsm : nullptr);
         if (e == -10000) return fail(ctx, BBGPU_ERR_ARG, "eval_upload_profile: member %d: weights not finite", k);
         fix[k] = std::min(e, 100);
     }
@@ -2080,14 +2084,13 @@ extern "C" int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *
             tot += cnt;
         };
         std::vector<int> ch;
-        std::vector<uint16_t> dm((size_t)nsm);
         for (int k = 0; k < nb; k++) {
             bool delta = false;
             if (ctx->share && k > 0 && fix[k] == fix[0]) {
                 const double *sk = sr_maps + (size_t)k * BBGPU_NSR * nsm;
+                const uint16_t *dm = pdiff.data() + (size_t)k * nsm;
                 long long nch = 0;
                 ch.clear();
-                bbh_column_diff(sk, sr_maps, nsm, dm.data());
                 for (int i = 0; i < nsm; i++)
                     if (!bbh_map_same(dm[i], sk, nsm, i)) {
                         ch.push_back(i);

@@ -296,9 +296,9 @@ static const uint16_t *diff_of(const double *sr, const double *sr_ref, int nsub)
 }
 
 int bbh_submc(const double *sr, int nsub, const int *nc, const int *nv, const GridDev *g, SubMC *out,
-              const double *sr_ref, const SubMC *out_ref, signed char *reused) {
+              const double *sr_ref, const SubMC *out_ref, signed char *reused, const uint16_t *diff_in) {
     double bound = 0.;
-    const uint16_t *diff = out_ref ? diff_of(sr, sr_ref, nsub) : nullptr;
+    const uint16_t *diff = out_ref ? (diff_in ? diff_in : diff_of(sr, sr_ref, nsub)) : nullptr;
     double scr, ccr;
     sincos_memo(g->crota2, scr, ccr);
     for (int ir = 0; ir < nsub; ir++) {
@@ -554,7 +554,7 @@ void bbh_an_samples_f32(const std::vector<double> &cs, std::vector<float> &csf) 
 
 int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0, int blo1, int bhi0, int bhi1,
                 const double *cd2i, int maps, const int64_t *widx, const double *wval, AnSub *out, ZgridCache &zc,
-                const double *sr_ref, const AnSub *out_ref, signed char *reused) {
+                const double *sr_ref, const AnSub *out_ref, signed char *reused, const uint16_t *diff_in) {
 #define SR(r, i) sr[(size_t)(r) * nsub + (i)]
     const int nb = nzq > 1 ? nzq : 1;
     std::vector<double> tz(nb), tw(nb);
@@ -562,7 +562,7 @@ int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0,
     double cmax = 0.0, lsum = 0.0, bound = 0.0;
     for (int k = 0; k < g->nz; k++) cmax = std::max(cmax, fabs(cd2i[k]));
     for (int nl = 0; nl < g->nlines; nl++) lsum += fabs(g->relint[nl]);
-    const uint16_t *diff = out_ref ? diff_of(sr, sr_ref, nsub) : nullptr;
+    const uint16_t *diff = out_ref ? (diff_in ? diff_in : diff_of(sr, sr_ref, nsub)) : nullptr;
     double scr, ccr;
     sincos_memo(g->crota2, scr, ccr);
     for (int ir = 0; ir < nsub; ir++) {
@@ -755,15 +755,22 @@ extern "C" int bbgpu_subrings_rows(const double *rows, int nb, int nr, int nsub,
         for (int f = 0; f < NV; f++) {
             const double *x = rw + (size_t)src[f] * nr;
             double *o = out + (size_t)f * nr;
-            for (int j = 0; j < nr; j++) {
-                const double v = x[j];
-                switch (f) {
-                    case 0: case 1: case 2: case 3: case 12: o[j] = v * 1000.; break;
-                    case 5: case 7: o[j] = v / 60.; break;
-                    case 6: o[j] = v * 1000. * 60.; break;
-                    case 8: case 9: o[j] = v * d2r; break;
-                    default: o[j] = v; break;
-                }
+            switch (f) {
+                case 0: case 1: case 2: case 3: case 12:
+                    for (int j = 0; j < nr; j++) o[j] = x[j] * 1000.;
+                    break;
+                case 5: case 7:
+                    for (int j = 0; j < nr; j++) o[j] = x[j] / 60.;
+                    break;
+                case 6:
+                    for (int j = 0; j < nr; j++) o[j] = x[j] * 1000. * 60.;
+                    break;
+                case 8: case 9:
+                    for (int j = 0; j < nr; j++) o[j] = x[j] * d2r;
+                    break;
+                default:
+                    memcpy(o, x, sizeof(double) * nr);
+                    break;
             }
         }
     };

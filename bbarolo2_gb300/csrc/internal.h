@@ -105,9 +105,11 @@ uint64_t bbh_layout_key(uint64_t seed, int ltype, int nsub, const int *nc, const
 void bbh_cloud_counts(const double *sr, int nsub, const int64_t *nv_in, const GridDev *g, int *nc, int *nv);
 // SubMC of one table; returns the exponent e of the fixed-point unit 2^-e of its deposits
 // (sr_ref, out_ref: another member's table and constants, reused for the columns that are equal; may be NULL;
-// reused: when given, those columns are only marked (1) and left unwritten, for the device to fill)
+// reused: when given, those columns are only marked (1) and left unwritten, for the device to fill; diff: when
+// given, bbh_column_diff(sr, sr_ref) computed by the caller)
 int bbh_submc(const double *sr, int nsub, const int *nc, const int *nv, const GridDev *g, SubMC *out,
-              const double *sr_ref = nullptr, const SubMC *out_ref = nullptr, signed char *reused = nullptr);
+              const double *sr_ref = nullptr, const SubMC *out_ref = nullptr, signed char *reused = nullptr,
+              const uint16_t *diff = nullptr);
 // ANALYTIC: the vertical samples of a sub-ring (bbarolo/galmod.py:276-323); returns their number
 int bbh_zgrid(double *zq, double *wq, int nmax, int ltype, double z0, double sinc, double pixsize, double dvdz,
               double sig, double R0, double radsep, double xpos, double ypos, double cdelt0, double cdelt1,
@@ -155,7 +157,8 @@ struct ZgridCache {
 };
 int bbh_an_subs(const double *sr, int nsub, const GridDev *g, int nzq, int blo0, int blo1, int bhi0, int bhi1,
                 const double *cd2i, int maps, const int64_t *widx, const double *wval, AnSub *out, ZgridCache &zc,
-                const double *sr_ref = nullptr, const AnSub *out_ref = nullptr, signed char *reused = nullptr);
+                const double *sr_ref = nullptr, const AnSub *out_ref = nullptr, signed char *reused = nullptr,
+                const uint16_t *diff = nullptr);
 // per column of the tables a and b (16 rows, nsub columns): the bit mask of the rows whose values differ (bitwise)
 void bbh_column_diff(const double *a, const double *b, int nsub, uint16_t *mask);
 // true if a column with the row mask m gives the same ring-map constants in bbh_an_subs (maps mode): the same
