@@ -337,9 +337,10 @@ class BatchLikelihood:
         sl = (slice(Lb[1], Hb[1]), slice(Lb[0], Hb[0]))
         return mom0[sl], rms[sl], ok[sl]
 
-    def profile_maps(self, rows):
-        """The sub-ring tables of the ring maps of a batch (B, 16, nsm): the model's sub-rings, then those of the
-        exterior annulus (the values of each member's last ring, ``bbarolo/profile.py:66-69``)."""
+    def profile_maps(self, rows, out=None):
+        """The sub-ring tables of the exterior annulus of the ring maps of a batch (B, 16, nse: the values of
+        each member's last ring, ``bbarolo/profile.py:66-69``); the ring maps' tables are the model's sub-rings,
+        then these. out (B, 16, nse), e.g. a view of the last columns of the maps' table, receives them."""
         dm = self.model
         P = self._prof
         ext = P["ext"]
@@ -355,7 +356,9 @@ class BatchLikelihood:
         pick = np.concatenate([[0], other])
         emr_rows, emr = dm.model_rows(er[pick], ext, ringmode="CENTRED")
         sre, _ = subrings_batch(dm.setup, emr, emr_rows)
-        out = np.repeat(sre[:1], er.shape[0], axis=0)
+        if out is None:
+            out = np.empty((er.shape[0],) + sre.shape[1:])
+        out[:] = sre[:1]
         out[other] = sre[1:]
         return out
 
@@ -406,10 +409,12 @@ class BatchLikelihood:
             if not np.array_equal(np.asarray(proto.radii, float), self._prof["radii"]):
                 raise ValueError("the radii differ from those given to set_profile")
             # the ring maps' tables: the model's sub-rings (written by subrings_batch), then the exterior's
-            pm = self.profile_maps(rows)
             nsub = dm.setup.grid(mr).nsub
-            ms = np.empty((pm.shape[0], pm.shape[1], nsub + pm.shape[2]))
-            ms[:, :, nsub:] = pm
+            nse = self._prof.get("nse")
+            if nse is None:
+                nse = self._prof["nse"] = self.profile_maps(rows[:1]).shape[2]
+            ms = np.empty((len(rows), 16, nsub + nse))
+            self.profile_maps(rows, out=ms[:, :, nsub:])
         sr, nv = subrings_batch(dm.setup, mr, mrows, out_ms=ms)
         B = sr.shape[0]
         s = seed32(dm.setup.iseed if seed is None else seed)

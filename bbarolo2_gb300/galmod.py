@@ -164,11 +164,15 @@ def model_rows(rows, proto, mode, radsep):
     """Ring-value rows (B, 17, nr) of ring sets like ``proto`` -> (the rows of their model rings with the ring
     convention ``mode`` (``model_rings``), the model-ring prototype): CENTRED repeats the first/last ring at the
     added half rings, SHIFTED moves the end radii, NODES keeps the rings."""
-    probe = proto.copy()
-    probe.radii = np.asarray(proto.radii, float)
-    mr = model_rings(probe, mode, radsep)
-    if mr is probe:
-        return np.asarray(rows, float), probe
+    if ringmode_name(mode) != "NODES" and proto.nr and isinstance(proto.radii, np.ndarray) and \
+            proto.radii.dtype == np.float64:
+        mr = model_rings(proto, mode, radsep)        # (a new ring set: proto is copied, not changed)
+    else:
+        probe = proto.copy()
+        probe.radii = np.asarray(proto.radii, float)
+        mr = model_rings(probe, mode, radsep)
+        if mr is probe:
+            return np.asarray(rows, float), probe
     eq = np.asarray(mr.radii, float)[:, None] == np.asarray(proto.radii, float)[None, :]
     idx = np.where(eq.any(axis=1), eq.argmax(axis=1), -1).tolist()     # (the first equal radius, or -1)
     nr = proto.nr
