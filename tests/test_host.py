@@ -208,3 +208,48 @@ def test_count_ring_pixels_matches_reference_rule():
                 if y < 30 and x < 40 and m[y, x] > 0:
                     i += 1
     assert (nt, ni) == (t, i)
+
+
+def test_prepare_maps_table(monkeypatch):
+    """BatchLikelihood.prepare (no device: a stub context): the ring maps' table is the model's sub-ring tables
+    followed by the exterior annulus' (written in place), bit for bit the tables of the numpy path, for a
+    finite-difference batch and a batch of independent points."""
+    from bbarolo2_gb300 import _lib, engine
+
+    class _Calls:
+        def __getattr__(self, name):
+            return lambda *a, **k: 0
+
+    class _StubContext:
+        def __init__(self, device=0):
+            self.L, self.h = _Calls(), None
+
+        def check(self, rc):
+            return rc
+
+    monkeypatch.setattr(_lib, "Context", _StubContext)
+    cube, rings = configs.global160(galmodtype="MC")
+    dm = engine.DiskModel(cube)
+    data = np.ones(cube.array.shape, np.float32)
+    L = engine.BatchLikelihood(dm, data, np.ones(cube.array.shape, bool), maskmode=2, sigma=1.0)
+    L.set_profile(rings, *L.data_maps(), smooth=0.3, corr=2.0, beam_arcsec=30.)
+    base = galmod.ring_rows_batch([rings])[0]
+    grad = [base]
+    for j in (0, rings.nr // 2, rings.nr - 1):
+        for row, step in ((4, 5.0), (12, 2.0), (13, 3.0)):
+            r = base.copy()
+            r[row, j] += step
+            grad.append(r)
+    rng = np.random.default_rng(7)
+    rand = np.repeat(base[None], 9, axis=0)
+    rand[1:, 4] += rng.normal(0., 5., rand[1:, 4].shape)
+    rand[1:, 12] += rng.normal(0., 2., rand[1:, 12].shape)
+    for rows in (np.stack(grad), rand):
+        sr, nv, _, _ = L.prepare(rows, rings, seed=1)
+        ms = L._maps_sr.copy()
+        assert np.array_equal(ms, np.concatenate([sr, L.profile_maps(rows)], axis=2))
+        monkeypatch.setattr(galmod, "_NATIVE", False)
+        sr0, nv0, _, _ = L.prepare(rows, rings, seed=1)
+        monkeypatch.setattr(galmod, "_NATIVE", None)
+        assert np.array_equal(sr.view(np.uint64), sr0.view(np.uint64)) and np.array_equal(nv, nv0)
+        assert np.array_equal(ms.view(np.uint64), L._maps_sr.view(np.uint64))
