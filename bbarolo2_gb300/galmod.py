@@ -592,9 +592,9 @@ def subrings_batch(setup, proto, rows, out_ms=None, native=True):
         rows_c = np.ascontiguousarray(rows)
         sr = np.empty((B, 16, g.nsub))
         nv = np.empty((B, g.nsub), np.int64)
-        if out_ms is not None:
-            assert out_ms.flags.c_contiguous and out_ms.dtype == np.float64 and out_ms.shape[:2] == (B, 16) \
-                and out_ms.shape[2] >= g.nsub
+        if out_ms is not None and not (out_ms.flags.c_contiguous and out_ms.dtype == np.float64 and
+                                       out_ms.shape[:2] == (B, 16) and out_ms.shape[2] >= g.nsub):
+            raise ValueError("subrings_batch: out_ms must be a C-contiguous float64 (B, 16, >= nsub) array")
         rc = fn(_lib.ptr(rows_c), B, rows.shape[2], g.nsub, _lib.ptr(g.i1), _lib.ptr(g.dr), _lib.ptr(g._dseg),
                 _lib.ptr(g.const.view(np.uint8)), _lib.ptr(g.radii), _lib.ptr(edgew), _lib.ptr(side), int(nvtmp),
                 _lib.ptr(sr), _lib.ptr(nv), _lib.ptr(out_ms), 0 if out_ms is None else out_ms.shape[2])
