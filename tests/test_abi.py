@@ -33,6 +33,32 @@ def test_version_and_no_device_errors():
     assert L.bbgpu_eval_run(None) == _lib.ERR_ARG
 
 
+def test_subrings_rows_argument_checks():
+    """The host-only table builder (no context, no GPU) rejects what it cannot tabulate, writing nothing."""
+    import numpy as np
+    L = _lib.load(build.build())
+    nb, nr, nsub = 2, 3, 4
+    rows = np.zeros((nb, 17, nr))
+    i1 = np.array([1, 1, 2, 2], np.int64)
+    dr, dseg, radii = np.zeros(nsub), np.ones(nr - 1), np.arange(nsub, dtype=float)
+    cst = np.zeros(nsub, np.uint8)
+    side = np.ones((2, nsub))
+    sr = np.full((nb, 16, nsub), 7.)
+    nv = np.zeros((nb, nsub), np.int64)
+    P = _lib.ptr
+
+    def call(nr_=nr, i1_=i1, ms=None, nsm=0):
+        return L.bbgpu_subrings_rows(P(rows), nb, nr_, nsub, P(i1_), P(dr), P(dseg), P(cst), P(radii), None,
+                                     P(side), 16, P(sr), P(nv), P(ms), nsm)
+
+    assert call(nr_=1) == _lib.ERR_ARG                              # one ring: the numpy path
+    assert call(i1_=np.array([1, 1, 2, 3], np.int64)) == _lib.ERR_ARG  # a segment past the last ring
+    assert call(ms=np.zeros((nb, 16, 2)), nsm=2) == _lib.ERR_ARG     # a maps table narrower than the tables
+    assert np.all(sr == 7.)
+    assert call() == _lib.OK
+    assert np.array_equal(sr[:, 0], np.broadcast_to(radii, (nb, nsub))) and np.all(nv == 1)
+
+
 def test_oracle_is_not_linked_by_the_product():
     """The product library does not reference the oracle's symbols (ref_*)."""
     import subprocess
