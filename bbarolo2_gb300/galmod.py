@@ -1,19 +1,20 @@
 """Host side of the GALMOD model: header-derived constants and the sub-ring tables the device kernels read.
 
-This module mirrors the model-setup part of ``bbarolo/galmod.py``:
+What this module computes, and the reference code whose numbers it reproduces:
 
-* ``GalmodSetup`` (``bbarolo/galmod.py:609-758``): cdelt in arcmin, pixel area, CROTA2, the spectral axis
-  (velocity / frequency / wavelength, radio / optical / relativistic), the instrumental dispersion, the channel
-  factor ``cd2i`` (float32-rounded as the reference) and the channel edges in velocity of each line;
-* ``GalmodSetup.subrings`` (``bbarolo/galmod.py:761-851``): rings -> sub-rings 0.75 pixel apart, with the
-  float32 accumulation of the sub-ring radii, linear interpolation of the ring values, the sharp/Gaussian
-  outer edge, the thick layer and the edge weights of the two halves (rows 14-15);
-* the ring conventions ``model_rings``/``edge_weights``/``outer_edge`` (``bbarolo/galmod.py:1043-1141``).
+* ``GalmodSetup``: the constants of ``bbarolo/galmod.py:609-758`` (pixel sizes in arcmin, the pixel area, CROTA2
+  in radians, the spectral axis in SI units with the reference frequency of each line, the instrumental
+  dispersion, the channel factor ``cd2i`` rounded to float32 and the channel edges in velocity). Here the
+  spectral axis is an object (``SpectralAxis``, one subclass per axis type) and the units are tables, but each
+  number is formed by the reference's float64 operations in the reference's order: the device results are
+  bit-exact only if these constants are;
+* ``GalmodSetup.subrings`` (``bbarolo/galmod.py:761-851``): rings -> sub-rings 0.75 pixel apart (``SubringGrid``:
+  float32 accumulation of the radii, linear interpolation of the ring values), the outer edge, the thick layer,
+  the side weights (rows 14-15);
+* the ring conventions (``RINGMODE``, ``bbarolo/galmod.py:1043-1141``) as ``RingConvention`` objects.
 
-The sub-ring table ``sr`` has the reference's layout (16, nsub), internal units (arcmin, m/s, radians),
-rows: radius, vrot, vrad, vvert, vdisp, dens, z0, dvdz, zcyl, inc, phi, xpos, ypos, vsys, wrec, wapp.
-All arithmetic is elementwise IEEE float64 in the reference's operation order, so the table is bit-equal
-to the reference's (checked against golden tables generated from the reference).
+The sub-ring table ``sr`` has the reference's layout (16, nsub), internal units (arcmin, m/s, radians), rows:
+radius, vrot, vrad, vvert, vdisp, dens, z0, dvdz, zcyl, inc, phi, xpos, ypos, vsys, wrec, wapp.
 """
 
 import math
@@ -22,10 +23,15 @@ import sys
 import numpy as np
 
 C_MS = 2.99792458e08
+# velocity, wavelength and frequency units: the number of units in km/s, m and Hz respectively
 VEL_UNITS = {"km/s": 1., "kms": 1., "m/s": 1E03, "ms": 1E03, "cm/s": 1E05}
 WAVE_UNITS = {"m": 1., "cm": 1E02, "mm": 1E03, "um": 1E06, "mum": 1E06, "micron": 1E06, "nm": 1E09,
               "a": 1E10, "angstrom": 1E10}
-_FREQ_UNITS = {"hz": 1., "khz": 1E03, "mhz": 1E06, "ghz": 1E09}
+_HZ_PER_UNIT = {"hz": 1., "khz": 1E03, "mhz": 1E06, "ghz": 1E09}
+# sky units (a substring of CUNIT) in arcmin and in arcsec
+_ARCMIN_PER = (("deg", 60.), ("arcs", 1 / 60.), ("arcm", 1.))
+_ARCSEC_PER = (("deg", 3600.), ("arcm", 60.), ("arcs", 1.))
+HI_FREQ = 0.1420405751786E10
 
 # vertical samples of the ANALYTIC model (bbarolo/galmod.py:262-273)
 ZSAMPLES_MAX = 1024
@@ -37,8 +43,6 @@ ZSTEP_BEAM = 3.0
 SR_R, SR_VROT, SR_VRAD, SR_VVERT, SR_VDISP, SR_DENS, SR_Z0, SR_DVDZ, SR_ZCYL, SR_INC, SR_PHI, SR_XPOS, \
     SR_YPOS, SR_VSYS, SR_WREC, SR_WAPP = range(16)
 
-RINGMODES = ("CENTRED", "NODES", "SHIFTED")
-
 
 class BBaroloError(ValueError):
     """Invalid input of the model path (the reference's ``bbarolo.bbutils.BBaroloError``)."""
@@ -49,115 +53,286 @@ def seed32(iseed):
     return int(iseed) & 0xFFFFFFFF
 
 
-def arcsconv(cunit):
+def _lookup(cunit, table, what):
     c = cunit.lower()
-    if "deg" in c:
-        return 3600.
-    if "arcm" in c:
-        return 60.
-    if "arcs" in c:
-        return 1.
-    raise ValueError(f"Conversion error (unknown CUNIT for RA-DEC): {cunit}. Cannot convert to ARCSEC.")
+    for key, f in table:
+        if key in c:
+            return f
+    raise BBaroloError(f"{what}: sky axis unit {cunit!r} is not degrees, arcminutes or arcseconds")
+
+
+def arcsconv(cunit):
+    """Arcseconds per unit of a sky axis (``bbarolo/bbutils.py:227-232``)."""
+    return _lookup(cunit, _ARCSEC_PER, "arcsconv")
+
+
+def arcmconv(cunit):
+    """Arcminutes per unit of a sky axis (the conversion of ``bbarolo/galmod.py:618-626``)."""
+    return _lookup(cunit, _ARCMIN_PER, "GALMOD")
+
+
+# Doppler conventions: velocity (m/s) of the ratio r = f / f0 of an observed to a reference frequency
+_DOPPLER = {1: lambda r: C_MS * (1 - r),                        # radio
+            2: lambda r: C_MS * (1 / r - 1),                    # optical
+            3: lambda r: C_MS * (1 - r * r) / (1 + r * r)}      # relativistic
+_VELDEF = {"radio": 1, "optical": 2, "relativistic": 3}
 
 
 def delta_vel(h):
-    """Channel width in km/s (``bbarolo/bbutils.py:159-180``): velocity axes directly; frequency and
-    wavelength axes as the mean width of the channels in velocity."""
-    dv = h.Cdelt(2)
-    nz = h.DimAx(2)
-    cu = h.Cunit(2).lower()
-    if cu in VEL_UNITS:
-        return dv / VEL_UNITS[cu]
-    k = np.arange(nz - 1)
-    lo = (k + 1 - h.Crpix(2)) * h.Cdelt(2) + h.Crval(2)
-    hi = (k + 2 - h.Crpix(2)) * h.Cdelt(2) + h.Crval(2)
-    vd = h.VelDef()
-    if cu in _FREQ_UNITS:
-        fc = _FREQ_UNITS[cu]
+    """Channel width in km/s (``bbarolo/bbutils.py:159-180``): a velocity axis directly, a frequency axis as its
+    radio width or the mean width of its channels in velocity."""
+    unit = h.Cunit(2).lower()
+    if unit in VEL_UNITS:
+        return h.Cdelt(2) / VEL_UNITS[unit]
+    if unit in _HZ_PER_UNIT:
+        hz = _HZ_PER_UNIT[unit]
         frest = h.Freq0() / (1 + h.Redshift())
-        if vd == "radio":
-            return -C_MS / 1000. * dv * fc / frest
-        return float(np.sum(_freq2vel(hi * fc, frest, vd) - _freq2vel(lo * fc, frest, vd)) / (nz - 1))
-    if cu in WAVE_UNITS:
+        vd = _VELDEF.get(h.VelDef(), 1)
+        if vd == 1:
+            return -(C_MS / 1000.) * h.Cdelt(2) * hz / frest
+        nz = h.DimAx(2)
+        k = np.arange(nz - 1)
+        lo = (k + 1 - h.Crpix(2)) * h.Cdelt(2) + h.Crval(2)
+        hi = (k + 2 - h.Crpix(2)) * h.Cdelt(2) + h.Crval(2)
+        kms = {1: lambda f: (C_MS / 1000.) * (1 - f / frest),
+               2: lambda f: (C_MS / 1000.) * (frest / f - 1),
+               3: lambda f: (C_MS / 1000.) * (1 - (f / frest) ** 2) / (1 + (f / frest) ** 2)}[vd]
+        return float(np.sum(kms(hi * hz) - kms(lo * hz)) / (nz - 1))
+    if unit in WAVE_UNITS:
         raise BBaroloError("delta_vel: wavelength axes need the rest wavelength of the cube (not supported)")
-    return dv
+    return h.Cdelt(2)
 
 
-def _freq2vel(f, f0, vd):
-    c = C_MS / 1000.
-    if vd == "radio":
-        return c * (1 - f / f0)
-    if vd == "optical":
-        return c * (f0 / f - 1)
-    r = (f / f0) ** 2
-    return c * (1 - r) / (1 + r)
+class SpectralAxis:
+    """The spectral axis of a cube in SI units (``bbarolo/galmod.py:630-700``): ``code`` (2 wavelength, 3 frequency,
+    4 velocity), ``crval``, ``cdelt``, ``crpix``, the reference frequency ``freq0`` of the first line, and the
+    lines (``lfreq0``: their reference frequencies, ``relint``: their relative intensities)."""
+
+    code = 0
+
+    def __init__(self, h, p, gm):
+        self.velsys = _VELDEF.get(h.VelDef(), 1)
+        self.crpix = h.Crpix(2)
+        self.redshift = p.getRedshift()
+        self.freq0 = HI_FREQ
+        self.lfreq0 = None
+        self.relint = np.array([1.])
+
+    @staticmethod
+    def of(h, p, gm):
+        kind = h.SpectralType()
+        for cls in (WavelengthAxis, FrequencyAxis, VelocityAxis):
+            if cls.matches(kind):
+                return cls(h, p, gm)
+        raise BBaroloError("GALMOD ERROR: unknown Spectral axis type. Check CTYPE3 and CUNIT3 keywords.")
+
+    def _lines(self, given, name, gm, to_freq):
+        """Several rest lines (RESTWAVE/RESTFREQ with more than one value): their frequencies and intensities."""
+        if len(given) > 1:
+            if len(gm.RELINT) != len(given):
+                raise BBaroloError(f"GALMOD ERROR: {name} gives {len(given)} lines, but RELINT has {len(gm.RELINT)} "
+                                   "values: give one relative intensity per line.")
+            self.lfreq0 = to_freq(np.asarray(given, float))
+            self.relint = np.array(gm.RELINT, float)
+
+    def velocity(self, w, freq0):
+        """Velocity (m/s) of axis values w (SI) for a line of reference frequency freq0."""
+        return _DOPPLER[self.velsys]((C_MS / w if self.code == 2 else w) / freq0)
+
+    def rest_wavelength(self, w):
+        """The wavelength (m) of the line at axis values w, and the flux-conversion factor of this axis type
+        (the column density of ``bbarolo/galmod.py:727-741``)."""
+        raise NotImplementedError
 
 
+class WavelengthAxis(SpectralAxis):
+    code = 2
+
+    @staticmethod
+    def matches(kind):
+        return kind == "wave"
+
+    def __init__(self, h, p, gm):
+        super().__init__(h, p, gm)
+        unit = h.Cunit(2).lower()
+        if unit not in WAVE_UNITS:
+            raise BBaroloError(f"GALMOD ERROR: unknown CUNIT3={unit}. Cannot convert to meters.")
+        to_m = 1. / WAVE_UNITS[unit]
+        self.crval, self.cdelt = h.Crval(2) * to_m, h.Cdelt(2) * to_m
+        restw = p.getRestwave()
+        z1 = 1 + self.redshift
+        self.freq0 = C_MS / (restw * z1 * to_m) if restw != -1 else C_MS / self.crval
+        self._lines(gm.RESTWAVE, "RESTWAVE", gm, lambda w: C_MS / (w * z1 * to_m))
+
+    def rest_wavelength(self, w):
+        return w, 2.588E04
+
+
+class FrequencyAxis(SpectralAxis):
+    code = 3
+
+    @staticmethod
+    def matches(kind):
+        return kind == "freq"
+
+    def __init__(self, h, p, gm):
+        super().__init__(h, p, gm)
+        unit = h.Cunit(2).lower()
+        hz = _HZ_PER_UNIT.get(unit)
+        if hz is None:
+            raise BBaroloError(f"GALMOD ERROR: unknown CUNIT3={unit}. Cannot convert to Hz.")
+        self.crval, self.cdelt = h.Crval(2) * hz, h.Cdelt(2) * hz
+        self.freq0 = h.Freq0() / (1 + self.redshift) or HI_FREQ
+        self._lines(gm.RESTFREQ, "RESTFREQ", gm, lambda f: f / (1 + self.redshift))
+
+    def rest_wavelength(self, w):
+        return C_MS / w, 3.8475E-06
+
+
+class VelocityAxis(SpectralAxis):
+    code = 4
+
+    @staticmethod
+    def matches(kind):
+        return "velo" in kind
+
+    def __init__(self, h, p, gm):
+        super().__init__(h, p, gm)
+        unit = h.Cunit(2).lower()
+        if unit not in VEL_UNITS:
+            raise BBaroloError(f"GALMOD ERROR: unknown CUNIT3={unit}. Cannot convert to m/s.")
+        to_ms = 1.0E03 / VEL_UNITS[unit]
+        self.freq0 = h.Freq0() / (1 + self.redshift) or HI_FREQ
+        self.crval, self.cdelt = h.Crval(2) * to_ms, h.Cdelt(2) * to_ms
+        if max(len(gm.RESTWAVE), len(gm.RESTFREQ)) > 1:
+            sys.stderr.write(" GALMOD WARNING: several lines (RESTWAVE/RESTFREQ) on a velocity axis: only one line "
+                             "is modelled.\n")
+
+    def velocity(self, w, freq0):
+        return w
+
+    def rest_wavelength(self, w):
+        shift = {1: lambda: self.freq0 * (1 - w / C_MS),
+                 2: lambda: self.freq0 * (C_MS / (C_MS + w)),
+                 3: lambda: self.freq0 * np.sqrt((C_MS - w) / (C_MS + w))}[self.velsys]
+        return C_MS / shift(), 1.823E-05
+
+
+# ------------------------------------------------------------------------------------------ outer edges
 def edge_weights(R, dr, edge, width=0.):
-    """Weights of the density of sub-rings at radii R (arcsec, dr wide) for an outer edge at ``edge``
-    (``bbarolo/galmod.py:1122-1131``): the fraction of each sub-ring within the edge (sharp), or a Gaussian
-    edge 1/2 erfc((R - edge) / (sqrt(2) width))."""
+    """The weights of sub-rings of radii R (arcsec), each dr wide, for a disk ending at the radius ``edge``
+    (``bbarolo/galmod.py:1122-1131``): the part of each sub-ring inside it for a sharp edge (width 0, and a step
+    for dr 0), else the Gaussian edge 1/2 erfc((R - edge) / (sqrt(2) width))."""
     R = np.asarray(R, float)
     if width > 0:
         from scipy.special import erfc
         return 0.5 * erfc((R - edge) / (math.sqrt(2.) * width))
-    if dr > 0:
-        return np.clip((edge - (R - dr / 2.)) / dr, 0., 1.)
-    return (R <= edge).astype(float)
+    if not dr > 0:
+        return (R <= edge).astype(float)
+    inside = (edge - (R - dr / 2.)) / dr
+    return np.clip(inside, 0., 1.)
+
+
+# ------------------------------------------------------------------------------------------ ring conventions
+class RingConvention:
+    """A ring convention (RINGMODE, ``bbarolo/galmod.py:1043-1141``): how the fitted rings map to the radii (used as
+    nodes of the linear interpolation) of their model, and where the disk ends."""
+
+    name = ""
+
+    def model(self, rings, subring):
+        raise NotImplementedError
+
+    def outer(self, rings):
+        raise NotImplementedError
+
+
+class _Nodes(RingConvention):
+    """The ring values sit at the radii; the disk covers the first to the last radius."""
+    name = "NODES"
+
+    def model(self, rings, subring):
+        if rings.nr == 1:
+            raise BBaroloError("RINGMODE NODES: a single ring makes an empty disk (the disk spans the first to the "
+                               "last radius); give two radii at least.")
+        return rings
+
+    def outer(self, rings):
+        return float(rings.radii[-1])
+
+
+class _Shifted(RingConvention):
+    """BBarolo 1.x: the first and last radius moved inwards and outwards by half of RADSEP."""
+    name = "SHIFTED"
+
+    def model(self, rings, subring):
+        if rings.nr == 1 and not rings.radsep > 0:
+            raise BBaroloError("RINGMODE SHIFTED: a single ring needs RADSEP > 0 (its width).")
+        half = rings.radsep / 2.
+        if rings.nr == 1:
+            out = rings.subset(np.array([0, 0]))
+            out.radii = np.array([rings.radii[0], rings.radii[0] + half], dtype=float)
+        else:
+            out = rings.copy()
+            out.radii[-1] += half
+        out.radii[0] = max(out.radii[0] - half, 0.)
+        return out
+
+    def outer(self, rings):
+        return float(rings.radii[-1] + rings.radsep / 2.)
+
+
+class _Centred(RingConvention):
+    """Each ring an annulus reaching halfway to its neighbours (the rings 3DFIT fits): the disk extends half a ring
+    beyond the first and last radius with their values, an extension narrower than one sub-ring left out."""
+    name = "CENTRED"
+
+    @staticmethod
+    def halves(rings):
+        R = rings.radii
+        if rings.nr > 1:
+            return (R[1] - R[0]) / 2., (R[-1] - R[-2]) / 2.
+        w = rings.radsep / 2. if rings.radsep > 0 else R[0] / 2.
+        return w, w
+
+    def model(self, rings, subring):
+        R = np.asarray(rings.radii, float)
+        first, last = self.halves(rings)
+        rin, rout = max(R[0] - first, 0.), R[-1] + last
+        pre = int(rin / 60. + subring < R[0] / 60.)       # (compared in arcmin, the sub-ring's unit)
+        post = int(R[-1] / 60. + subring < rout / 60.)
+        idx = np.r_[[0] * pre, np.arange(rings.nr), [rings.nr - 1] * post].astype(int)
+        out = rings.subset(idx)
+        out.radii = np.r_[[rin] * pre, R, [rout] * post].astype(float)
+        return out
+
+    def outer(self, rings):
+        return float(rings.radii[-1] + self.halves(rings)[1])
+
+
+CONVENTIONS = {c.name: c for c in (_Centred(), _Nodes(), _Shifted())}
+RINGMODES = tuple(CONVENTIONS)
 
 
 def ringmode_name(mode):
-    m = str(mode).strip().upper()
-    m = "CENTRED" if m == "CENTERED" else m
-    if m not in RINGMODES:
-        raise ValueError(f"Unknown ring convention {mode!r}: RINGMODE can be CENTRED, NODES or SHIFTED.")
+    """The canonical name of a ring convention (CENTERED accepted)."""
+    m = str(mode).strip().upper().replace("CENTERED", "CENTRED")
+    if m not in CONVENTIONS:
+        raise ValueError(f"RINGMODE {mode!r} unknown: the conventions are CENTRED, NODES and SHIFTED.")
     return m
 
 
-def _half_widths(rings):
-    R = rings.radii
-    if rings.nr == 1:
-        w = rings.radsep / 2. if rings.radsep > 0 else R[0] / 2.
-        return w, w
-    return (R[1] - R[0]) / 2., (R[-1] - R[-2]) / 2.
-
-
 def model_rings(rings, mode="CENTRED", subring=0.):
-    """The rings whose model (radii as nodes) is the model of ``rings`` with a ring convention
-    (``bbarolo/galmod.py:1066-1119``): CENTRED adds the inner and outer half rings with the values of the
-    first and last ring (unless narrower than one sub-ring), SHIFTED moves the first/last radius by half of
-    RADSEP, NODES returns the rings."""
-    mode = ringmode_name(mode)
-    if mode == "NODES" and rings.nr == 1:
-        raise BBaroloError("RINGMODE NODES needs two radii at least: the disk covers the first to the last radius "
-                           "(one ring gave an empty model).")
-    if mode == "SHIFTED" and rings.nr == 1 and not rings.radsep > 0:
-        raise BBaroloError("RINGMODE SHIFTED with one ring needs RADSEP > 0: the width of the ring.")
-    if mode == "NODES" or rings.nr == 0:
+    """The rings whose model (radii as nodes) is the model of ``rings`` under a ring convention; subring: the
+    sub-ring width in arcmin (GalmodSetup.radsep). A new ring set, or ``rings`` itself when nothing changes."""
+    if rings.nr == 0:
         return rings
-    r = rings.copy()
-    if mode == "SHIFTED":
-        if r.nr == 1:
-            r.addRing(r.radii[0] + r.radsep / 2., r.xpos[0], r.ypos[0], r.vsys[0], r.vrot[0], r.vdisp[0],
-                      r.vrad[0], r.vvert[0], r.dvdz[0], r.zcyl[0], r.dens[0], r.z0[0], r.inc[0], r.phi[0],
-                      r.z0thick[0], r.fthick[0], r.vdispthick[0])
-        else:
-            r.radii[-1] += r.radsep / 2.
-        r.radii[0] = max(r.radii[0] - r.radsep / 2., 0.)
-        return r
-    R = r.radii
-    w0, wn = _half_widths(r)
-    rin, rout = max(R[0] - w0, 0.), R[-1] + wn
-    idx, rad = list(range(r.nr)), list(R)
-    if rin / 60. + subring < R[0] / 60.:
-        idx.insert(0, 0)
-        rad.insert(0, rin)
-    if R[-1] / 60. + subring < rout / 60.:
-        idx.append(r.nr - 1)
-        rad.append(rout)
-    out = r.subset(np.array(idx))
-    out.radii = np.array(rad, dtype=float)
-    return out
+    return CONVENTIONS[ringmode_name(mode)].model(rings, subring)
+
+
+def outer_edge(rings, mode="CENTRED"):
+    """The outer radius (arcsec) of the disk of the rings under a ring convention."""
+    return CONVENTIONS[ringmode_name(mode)].outer(rings)
 
 
 def model_rows(rows, proto, mode, radsep):
@@ -185,15 +360,6 @@ def model_rows(rows, proto, mode, radsep):
     out = np.asarray(rows, float)[:, :, idx].copy()
     out[:, 0, :] = mr.radii
     return out, mr
-
-
-def outer_edge(rings, mode="CENTRED"):
-    mode = ringmode_name(mode)
-    if mode == "NODES":
-        return float(rings.radii[-1])
-    if mode == "SHIFTED":
-        return float(rings.radii[-1] + rings.radsep / 2.)
-    return float(rings.radii[-1] + _half_widths(rings)[1])
 
 
 class SubringGrid:
@@ -286,7 +452,9 @@ class SubringGrid:
 
 
 class GalmodSetup:
-    """Header-derived constants of the models of a cube (``bbarolo/galmod.py:609-758``)."""
+    """The constants of the models of a cube, computed once per cube (``bbarolo/galmod.py:609-758``): the sky
+    grid, the spectral axis (``SpectralAxis``), the line and cloud options of the GALMOD parameters, the channel
+    factor ``cd2i`` and the channel edges in velocity of each line."""
 
     def __init__(self, cube, gmpar=None, galmodtype=None, densflux=None):
         h = cube.Head()
@@ -294,85 +462,32 @@ class GalmodSetup:
         gm = p.gm if gmpar is None else gmpar
         self.nsubs = cube.DimZ()
         self.dimx, self.dimy = cube.DimX(), cube.DimY()
-        cdelt = [0., 0.]
-        arcmconv = 0.
-        for i in range(2):
-            cu = h.Cunit(i).lower()
-            if "deg" in cu:
-                arcmconv = 60.
-            elif "arcs" in cu:
-                arcmconv = 1 / 60.
-            elif "arcm" in cu:
-                arcmconv = 1.
-            else:
-                raise BBaroloError(f"GALMOD error (unknown CUNIT for RA-DEC): cannot convert to ARCMIN.\n{cu}")
-            cdelt[i] = h.Cdelt(i) * arcmconv
-        self.arcmconv = arcmconv
-        self.cdelt = cdelt
-        self.pixsize = [abs(cdelt[0]), abs(cdelt[1])]
+        # the sky grid in arcmin
+        conv = [arcmconv(h.Cunit(i)) for i in range(2)]
+        self.arcmconv = conv[1]
+        self.cdelt = [h.Cdelt(i) * conv[i] for i in range(2)]
+        self.pixsize = [abs(c) for c in self.cdelt]
         self.pixarea = self.pixsize[0] * self.pixsize[1]
         self.crota2 = h.Crota() * math.pi / 180.
+        self.radsep = 0.75 * min(self.pixsize)
         self.zstep = ZSTEP_FINE
-        reds = p.getRedshift()
-        cunit3 = h.Cunit(2).lower()
-        self.cdelt3, self.crval3, self.crpix3 = h.Cdelt(2), h.Crval(2), h.Crpix(2)
-        self.velsys = {"radio": 1, "optical": 2, "relativistic": 3}.get(h.VelDef(), 1)
-        sptype = h.SpectralType()
-        lfreq0 = None
-        self.relint = np.array([1.])
-        self.freq0 = 0.1420405751786E10
-        if sptype == "wave":
-            self.axtyp = 2
-            if cunit3 not in WAVE_UNITS:
-                raise BBaroloError(f"GALMOD ERROR: unknown CUNIT3={cunit3}. Cannot convert to meters.")
-            mconv = 1. / WAVE_UNITS[cunit3]
-            self.crval3 *= mconv
-            self.cdelt3 *= mconv
-            restw = p.getRestwave()
-            self.freq0 = C_MS / (restw * (1 + reds) * mconv) if restw != -1 else C_MS / self.crval3
-            if len(gm.RESTWAVE) > 1:
-                lfreq0 = C_MS / (np.asarray(gm.RESTWAVE, float) * (1 + reds) * mconv)
-                self.relint = _relint(gm.RELINT, len(gm.RESTWAVE), "RESTWAVE")
-        elif sptype == "freq":
-            self.axtyp = 3
-            hz = _FREQ_UNITS.get(cunit3)
-            if hz is None:
-                raise BBaroloError(f"GALMOD ERROR: unknown CUNIT3={cunit3}. Cannot convert to Hz.")
-            self.crval3 *= hz
-            self.cdelt3 *= hz
-            self.freq0 = h.Freq0() / (1 + reds)
-            if self.freq0 == 0:
-                self.freq0 = 0.1420405751786E10
-            if len(gm.RESTFREQ) > 1:
-                lfreq0 = np.asarray(gm.RESTFREQ, float) / (1 + reds)
-                self.relint = _relint(gm.RELINT, len(gm.RESTFREQ), "RESTFREQ")
-        elif "velo" in sptype:
-            self.axtyp = 4
-            if cunit3 not in VEL_UNITS:
-                raise BBaroloError(f"GALMOD ERROR: unknown CUNIT3={cunit3}. Cannot convert to m/s.")
-            msconv = 1.0E03 / VEL_UNITS[cunit3]
-            self.freq0 = h.Freq0() / (1 + reds)
-            if self.freq0 == 0:
-                self.freq0 = 0.1420405751786E10
-            self.crval3 *= msconv
-            self.cdelt3 *= msconv
-            if max(len(gm.RESTWAVE), len(gm.RESTFREQ)) > 1:
-                sys.stderr.write(" GALMOD WARNING: several lines (RESTWAVE/RESTFREQ) on a velocity axis: only one "
-                                 "line is modelled.\n")
-        else:
-            raise BBaroloError("GALMOD ERROR: unknown Spectral axis type. Check CTYPE3 and CUNIT3 keywords.")
-        nch = p.specres if getattr(p, "specres", -1) != -1 else p.linear
-        if nch == -1:
-            nch = 1. / (2 * math.sqrt(2 * math.log(2)))
+        # the spectral axis (SI) and the lines
+        ax = self.axis = SpectralAxis.of(h, p, gm)
+        self.axtyp, self.velsys = ax.code, ax.velsys
+        self.crval3, self.cdelt3, self.crpix3 = ax.crval, ax.cdelt, ax.crpix
+        self.freq0 = ax.freq0
+        self.lfreq0 = np.ascontiguousarray([ax.freq0] if ax.lfreq0 is None else ax.lfreq0, dtype=np.float64)
+        self.relint = np.ascontiguousarray(ax.relint, dtype=np.float64)
+        # the instrumental dispersion: SPECRES (or LINEAR) channels, by default the Gaussian of one channel's FWHM
+        per_channel = p.specres if getattr(p, "specres", -1) != -1 else p.linear
+        if per_channel == -1:
+            per_channel = 1. / (2 * math.sqrt(2 * math.log(2)))
         self.chwidth = abs(delta_vel(h)) * 1000
-        self.sig_instr = nch * self.chwidth
+        self.sig_instr = per_channel * self.chwidth
+        # the clouds and the lines
         self.ltype = gm.LTYPE
-        self.cmode = gm.CMODE
-        if self.cmode < 0 or self.cmode > 2:
-            self.cmode = 1
-        self.cdens = float(gm.CDENS)
-        if self.cdens < 0:
-            self.cdens = 1.
+        self.cmode = gm.CMODE if 0 <= gm.CMODE <= 2 else 1
+        self.cdens = float(gm.CDENS) if gm.CDENS >= 0 else 1.
         self.iseed = gm.ISEED
         self.empty = gm.EMPTY
         self.radmaxa = float(getattr(gm, "RADMAXA", -1.))
@@ -380,52 +495,30 @@ class GalmodSetup:
         self.densIsFlux = gm.DENSFLUX if densflux is None else densflux
         self.nvpar = gm.NV
         self.galmodtype = (galmodtype or getattr(p, "galmodtype", "MC")).upper()
-        self.radsep = 0.75 * min(self.pixsize)
-        if self.densIsFlux:
-            self.cd2i = np.full(self.nsubs, np.float32(3600. / self.chwidth * 1000.), dtype=np.float64)
-        else:
-            self.cd2i = self._nhi_to_rad()
-        self.lfreq0 = np.ascontiguousarray([self.freq0] if lfreq0 is None else lfreq0, dtype=np.float64)
-        self.relint = np.ascontiguousarray(self.relint, dtype=np.float64)
+        # flux per channel of a unit of DENS (arcsec^2 -> arcmin^2 and km/s -> m/s; float32 as the reference)
+        self.cd2i = np.full(self.nsubs, np.float32(3600. / self.chwidth * 1000.), dtype=np.float64) \
+            if self.densIsFlux else self._column_density_factor()
         self._vedges = self._velocity_edges()
         self._vedges_lines = np.ascontiguousarray([self._velocity_edges(f) for f in self.lfreq0])
         self._chmin = float(np.min(np.abs(np.diff(self._vedges)))) if self.nsubs > 0 else self.chwidth
         self._grid_cache = {}
 
-    def _nhi_to_rad(self):
-        """Column density (1E20 atoms/cm2) -> flux per channel (``bbarolo/galmod.py:727-741``)."""
-        jy, K = 1E-26, 1.3806488E-23
-        k = np.arange(self.nsubs)
-        w = self.crval3 + self.cdelt3 * (k + 1 - self.crpix3)
-        if self.axtyp == 2:
-            lab, fac = w, 2.588E04
-        elif self.axtyp == 3:
-            lab, fac = C_MS / w, 3.8475E-06
-        else:
-            f = self.freq0 * (1 - w / C_MS)
-            if self.velsys == 2:
-                f = self.freq0 * (C_MS / (C_MS + w))
-            if self.velsys == 3:
-                f = self.freq0 * np.sqrt((C_MS - w) / (C_MS + w))
-            lab, fac = C_MS / f, 1.823E-05
-        ddum = 2 * (K / jy) / (fac * lab * lab) / abs(self.cdelt3)
+    def _column_density_factor(self):
+        """The flux per channel of a column density of 1E20 atoms/cm^2 (``bbarolo/galmod.py:727-741``): 2 k_B /
+        (f lambda^2) per channel width, in the reference's order, rounded to float32."""
+        w = self.crval3 + self.cdelt3 * (np.arange(self.nsubs) + 1 - self.crpix3)
+        lam, fac = self.axis.rest_wavelength(w)
+        per_jy = 1.3806488E-23 / 1E-26
+        ddum = 2 * per_jy / (fac * lam * lam) / abs(self.cdelt3)
         return (ddum * (math.pi / (180.0 * 60.0)) ** 2).astype(np.float32).astype(np.float64)
 
     def _velocity_edges(self, freq0=None):
-        """Velocity (m/s) of the channel edges, k - 0.5 for k = 0..nz (``bbarolo/galmod.py:743-758``)."""
-        g = np.arange(self.nsubs + 1) - 0.5
-        w = (g + 1 - self.crpix3) * self.cdelt3 + self.crval3
-        if self.axtyp == 4:
-            return w
-        f = C_MS / w if self.axtyp == 2 else w
-        r = f / (self.freq0 if freq0 is None else freq0)
-        if self.velsys == 1:
-            v = C_MS * (1 - r)
-        elif self.velsys == 2:
-            v = C_MS * (1 / r - 1)
-        else:
-            v = C_MS * (1 - r * r) / (1 + r * r)
-        return np.ascontiguousarray(v, dtype=np.float64)
+        """The velocity (m/s) of the channel edges k - 0.5, k = 0..nz (``bbarolo/galmod.py:743-758``), for the line of
+        reference frequency freq0 (default: the first line)."""
+        edges = np.arange(self.nsubs + 1) - 0.5
+        w = (edges + 1 - self.crpix3) * self.cdelt3 + self.crval3
+        return np.ascontiguousarray(self.axis.velocity(w, self.freq0 if freq0 is None else freq0),
+                                    dtype=np.float64)
 
     def side_edges(self, rings):
         out = []
@@ -454,45 +547,10 @@ class GalmodSetup:
         return g
 
     def subrings(self, rings):
-        """Sub-ring table (16, nsub) float64 and NV per sub-ring (int64), as ``bbarolo/galmod.py:761-851``."""
-        if np.any(np.asarray(rings.vdisp) < 0):
-            raise ValueError("GALMOD ERROR: Negative velocity dispersion not allowed.")
-        if np.any(np.asarray(rings.dens) < 0):
-            raise ValueError("GALMOD ERROR: Negative column-density or flux are not allowed.")
-        if np.any(np.asarray(rings.z0) < 0):
-            raise ValueError("GALMOD ERROR: Negative scale height not allowed.")
-        thick = rings.thick() if hasattr(rings, "thick") else False
-        if thick:
-            ft = np.asarray(rings.fthick, float)
-            if np.any((ft < 0) | (ft > 1)):
-                raise ValueError("GALMOD ERROR: The fraction of gas in the thick layer (FTHICK) must be 0 to 1.")
-        g = self.grid(rings)
-        V = ring_value_rows(rings, thick)
-        nsub = g.nsub
-        sr = np.empty((V.shape[0] + 1, nsub))
-        sr[0] = g.radii
-        if nsub:
-            sr[1:] = g.interpolate(V)
-        edge = getattr(rings, "edge", None)
-        if edge is not None and nsub:
-            sr[5] *= edge_weights(sr[0] * 60., self.radsep * 60., float(edge),
-                                  float(getattr(rings, "edgewidth", 0.)))
-        if thick:
-            f = sr[14]
-            thin, thk = sr[:14].copy(), sr[:14].copy()
-            thin[5] *= 1. - f
-            thin[7] = 0.
-            thk[5] *= f
-            thk[6], thk[4] = sr[15], sr[16]
-            sr = np.concatenate([thin, thk], axis=1)
-        side = np.ones((2, sr.shape[1]))
-        for k, e in enumerate(self.side_edges(rings)[::-1]):
-            if e is not None and sr.shape[1]:
-                side[k] = edge_weights(sr[0] * 60., self.radsep * 60., e)
-        sr = np.concatenate([sr[:14], side])
-        nvtmp = self.nvpar if self.nvpar >= 1 else self.nsubs
-        nv = np.where(sr[4] == 0, 1, nvtmp).astype(np.int64)
-        return np.ascontiguousarray(sr), nv
+        """Sub-ring table (16, nsub) float64 and NV per sub-ring (int64) of a ring set (``bbarolo/galmod.py:761-851``):
+        the batch tabulation of ``subrings_batch`` for one member (numpy)."""
+        sr, nv = subrings_batch(self, rings, ring_rows_batch([rings]), native=False)
+        return sr[0], nv[0]
 
     def subcloud_flux(self, sr, nv):
         """Mean flux of one MC sub-cloud (``bbarolo/galmod.py:879-897``)."""
@@ -510,29 +568,6 @@ class GalmodSetup:
             unit = w[ok].sum() / np.sum(w[ok] / fsc)
         ri = self.relint
         return float(unit * np.sum(ri * ri) / np.sum(ri))
-
-
-def ring_value_rows(rings, thick):
-    """The ring values in internal units, one row per quantity (13 rows, 16 with a thick layer)."""
-    rows = [np.asarray(rings.vrot) * 1000., np.asarray(rings.vrad) * 1000.,
-            np.asarray(rings.vvert) * 1000., np.asarray(rings.vdisp) * 1000.,
-            np.asarray(rings.dens, float), np.asarray(rings.z0) / 60.,
-            np.asarray(rings.dvdz) * 1000 * 60, np.asarray(rings.zcyl) / 60.,
-            np.radians(np.asarray(rings.inc, float)), np.radians(np.asarray(rings.phi, float)),
-            np.asarray(rings.xpos, float), np.asarray(rings.ypos, float),
-            np.asarray(rings.vsys) * 1000.]
-    if thick:
-        vdt = np.asarray(rings.vdispthick, float)
-        vdt = np.where(vdt >= 0, vdt, np.asarray(rings.vdisp, float))
-        rows += [np.asarray(rings.fthick, float), rings.thick_z0() / 60., vdt * 1000.]
-    return np.vstack(rows).astype(float)
-
-
-def _relint(relint, nlines, name):
-    if len(relint) != nlines:
-        raise BBaroloError(f"GALMOD ERROR: {name} gives {nlines} lines, but RELINT has {len(relint)} values: give "
-                           "one relative intensity per line.")
-    return np.array(relint, float)
 
 
 def ring_rows_batch(rings_list):

@@ -253,3 +253,30 @@ def test_prepare_maps_table(monkeypatch):
         monkeypatch.setattr(galmod, "_NATIVE", None)
         assert np.array_equal(sr.view(np.uint64), sr0.view(np.uint64)) and np.array_equal(nv, nv0)
         assert np.array_equal(ms.view(np.uint64), L._maps_sr.view(np.uint64))
+
+
+@pytest.mark.parametrize("wl", ["classic64", "global160"])
+def test_oracle_host_setup_equals_package(wl):
+    """The package's host set-up (constants, sub-ring tables, boxes, beam kernel, ring weights) equals the plain
+    restatement of the reference under oracle/ on the benchmark workloads (the CPU reference arm uses the latter)."""
+    from bbarolo2_gb300 import configs, galmod
+    from bbarolo2_gb300.beam import BeamKernel
+    from oracle import host
+    cube, rings = configs.WORKLOADS[wl]()
+    st = galmod.GalmodSetup(cube)
+    ho = host.Setup(cube)
+    for a in ("pixarea", "crota2", "crval3", "cdelt3", "crpix3", "chwidth", "sig_instr", "radsep", "freq0"):
+        assert getattr(st, a) == getattr(ho, a), a
+    assert st.cdelt == ho.cdelt
+    np.testing.assert_array_equal(st.cd2i, ho.cd2i)
+    np.testing.assert_array_equal(st._vedges, ho.vedges)
+    assert st._chmin == ho.chmin
+    mr = galmod.model_rings(rings, "CENTRED", st.radsep)
+    mo = host.model_rings(rings, "CENTRED", ho.radsep)
+    np.testing.assert_array_equal(mr.radii, mo.radii)
+    sr, nv = st.subrings(mr)
+    so, no = host.subrings(ho, mo)
+    np.testing.assert_array_equal(sr, so)
+    np.testing.assert_array_equal(nv, no)
+    np.testing.assert_array_equal(BeamKernel.from_cube(cube).kernel, host.beam_kernel(cube))
+    assert galmod.outer_edge(rings, "CENTRED") == host.outer_edge_centred(rings)
