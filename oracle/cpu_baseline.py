@@ -12,9 +12,10 @@ With a profile in the payload, each evaluation first recomputes the deconvolved 
 ``Bayesian3DFIT._log_likelihood`` does when DENS is not fitted and the geometry is free
 (``bbarolo/bayesian/likelihood.py:595-596``): the ring maps (``_ring_maps_analytic`` through its C restatement,
 times mean(cd2i) sum(relint), FFT convolution, times the scale factor), the weighted least squares and
-``solve_profile`` (``oracle/profile.py``), the model's sub-rings with the new densities (the package's host
-``subrings_batch``, bit-equal to the reference's ``subrings``), then the MC model (or, with ``galmodtype``
-ANALYTIC in the payload, the ANALYTIC model ``_galmod_analytic`` through its C restatement).
+``solve_profile`` (``oracle/profile.py``), the model's sub-rings with the new densities (the reference's
+``subrings`` restated in ``oracle/host.py``), then the MC model (or, with ``galmodtype`` ANALYTIC in the payload,
+the ANALYTIC model ``_galmod_analytic`` through its C restatement). ``reference_payload`` builds a whole batch with
+the oracle alone (the reference arm of ``bench.py``, which loads no product library).
 One evaluation per process, as the reference's fork pool (``bbarolo/bayesian/sampling.py:184-193``), with the
 FFT on one worker thread; throughput = evaluations / wall time over all processes.
 """
@@ -80,15 +81,15 @@ def profile_dens(k, P=None):
 
 
 def model_table(k, x, P=None):
-    """The MC sub-ring table of member k with the ring densities x (nr)."""
-    from bbarolo2_gb300.galmod import model_rows, subrings_batch
+    """The MC sub-ring table of member k with the ring densities x (nr): the reference's ``subrings`` of its
+    CENTRED model rings (``oracle/host.py``)."""
+    from oracle import host
     P = P or _W
     pr = P["prof"]
-    rows = pr["rows"][k:k + 1].copy()
-    rows[0, pr["dens_row"]] = x[:pr["nr"]]
-    mrows, mr = model_rows(rows, pr["proto"], pr["mode"], pr["gsetup"].radsep)
-    sr, nv = subrings_batch(pr["gsetup"], mr, mrows)
-    return sr[0], nv[0]
+    row = pr["rows"][k].copy()
+    row[pr["dens_row"]] = x[:pr["nr"]]
+    st = pr["hsetup"]
+    return host.subrings(st, host.model_rings(host.rings_of_row(pr["proto"], row), pr["mode"], st.radsep))
 
 
 def evaluate(k):
@@ -138,7 +139,90 @@ def setup_payload(dm, sr, nv, boxes, seed, data, mask, maskmode, like=None, rows
                          nr=pr["nr"], nzq=1 if not np.any(ms[:, 6] > 0) else 1024,
                          mcd_relint=float(np.mean(st.cd2i)) * float(np.sum(st.relint)),
                          scalefactor=dm.scalefactor, rows=np.asarray(rows, float), proto=proto, mode=dm.ringmode,
-                         dens_row=RING_KEYS.index("dens"), gsetup=st)
+                         dens_row=RING_KEYS.index("dens"), hsetup=_host_setup(dm.cin))
+    return P
+
+
+def _host_setup(cube):
+    from oracle import host
+    return host.Setup(cube)
+
+
+# ---------------------------------------------------------------------------------------- the reference arm
+RING_KEYS = ("radii", "xpos", "ypos", "vsys", "vrot", "vdisp", "vrad", "vvert", "dvdz", "zcyl", "dens", "z0", "inc",
+             "phi", "z0thick", "fthick", "vdispthick")
+
+
+def ring_rows(rings):
+    return np.vstack([np.asarray(getattr(rings, k), float) for k in RING_KEYS])
+
+
+def reference_payload(cube, rings, rows, seed=1, noise=0.005, galmodtype="MC"):
+    """The worker payload of a batch of the 160x160x128 workload built by the oracle alone (the reference's host
+    set-up restated in ``oracle/host.py``, the mock from the oracle's MC model and the FFT convolution): what the
+    CPU reference arm evaluates, without the device library. rows (B, 17, nr) in RING_KEYS order."""
+    import math
+    from scipy import ndimage
+    from oracle import host
+    from oracle import oracle as O
+    O.lib()
+    st = host.Setup(cube)
+    kern = host.beam_kernel(cube)
+    h = cube.Head()
+    nx, ny, nz = cube.DimX(), cube.DimY(), cube.DimZ()
+    mr = host.model_rings(rings, "CENTRED", st.radsep)
+    sr0, nv0 = host.subrings(st, mr)
+    m = np.zeros((ny, nx, nz))
+    O.galmod_mc(m, sr0, 0, sr0.shape[1], seed, st.radsep, nv0, st.cdens, st.cmode, st.pixarea, st.cdelt[0],
+                st.cdelt[1], st.crota2, 0, 0, nx, ny, st.ltype, st.sig_instr, st.axtyp, st.velsys, st.lfreq0,
+                st.crval3, st.cdelt3, st.crpix3, st.relint, st.cd2i)
+    truth = fft_convolve(np.ascontiguousarray(m.transpose(2, 0, 1)), kern)
+    truth[truth < 1e-12] = 0.
+    rms = noise * float(truth.max())
+    g = np.random.default_rng(1)
+    nse = fft_convolve(g.normal(0., rms, truth.shape), kern)
+    nse *= rms / np.std(nse)
+    data = (truth + nse).astype(np.float32)
+    rad = abs(h.Bmaj() / h.Cdelt(1))
+    yy, xx = np.mgrid[-int(rad) - 1:int(rad) + 2, -int(rad) - 1:int(rad) + 2]
+    disk = (xx * xx + yy * yy) <= rad * rad
+    mask = ndimage.binary_dilation(truth > 3 * rms, structure=disk[None])
+    mask = ndimage.binary_dilation(mask, structure=np.ones((7, 1, 1), bool))
+    # the likelihood's total-intensity maps (bbarolo/bayesian/likelihood.py:180-221, density.py:80-83)
+    v = mask & np.isfinite(data) & (data != 0)
+    y = np.where(v, data, 0.).astype(np.float64).sum(axis=0)
+    cnt = v.sum(axis=0)
+    srms = rms * np.sqrt(cnt.astype(np.float64))
+    ok = cnt > 0
+    bmaj, bmin = abs(h.Bmaj()), abs(h.Bmin())
+    corr = math.pi * bmaj * bmin / (4. * math.log(2.)) / abs(h.Cdelt(0) * h.Cdelt(1))
+    members = []
+    for row in np.asarray(rows, float):
+        rk = host.rings_of_row(rings, row)
+        mk = host.model_rings(rk, "CENTRED", st.radsep)
+        srk, nvk = host.subrings(st, mk)
+        ext = host.exterior_ring(st, rk, bmaj * 3600.)
+        sre, _ = host.subrings(st, host.model_rings(ext, "CENTRED", st.radsep))
+        members.append((srk, nvk, host.box(cube, rk, final=True), np.concatenate([srk, sre], axis=1)))
+    wm = host.ring_weights(st, rings, "CENTRED")
+    we = host.ring_weights(st, host.exterior_ring(st, rings, bmaj * 3600.), "CENTRED")
+    widx = np.ascontiguousarray(np.concatenate([wm[0], np.where(we[0] >= 0, we[0] + rings.nr, -1)]), np.int64)
+    wval = np.ascontiguousarray(np.concatenate([wm[1], we[1]]))
+    ext0 = host.exterior_ring(st, rings, bmaj * 3600.)
+    ms = np.stack([mm[3] for mm in members])
+    P = dict(setup=dict(nz=nz, radsep=st.radsep, cdens=st.cdens, cmode=st.cmode, pixarea=st.pixarea,
+                        cdelt0=st.cdelt[0], cdelt1=st.cdelt[1], crota2=st.crota2, ltype=st.ltype,
+                        sig_instr=st.sig_instr, axtyp=st.axtyp, velsys=st.velsys, crval3=st.crval3,
+                        cdelt3=st.cdelt3, crpix3=st.crpix3, chwidth=st.chmin, zstep=host.zstep(cube, st)),
+             sr=[mm[0] for mm in members], nv=[mm[1] for mm in members], boxes=[mm[2] for mm in members],
+             seed=seed, lfreq0=st.lfreq0, relint=st.relint, cd2i=st.cd2i, kernel=kern, data=data, mask=mask,
+             maskmode=2, galmodtype=galmodtype.upper(), vedges=np.ascontiguousarray(st.vedges[None]),
+             prof=dict(maps_sr=ms, widx=widx, wval=wval, box=([0, 0], [nx, ny]), y=y, rms=srms, ok=ok,
+                       Rc=np.r_[np.asarray(rings.radii, float), float(ext0.radii[0])], smooth=0.3, corr=corr,
+                       floor=0.05, nr=rings.nr, nzq=1 if not np.any(ms[:, 6] > 0) else 1024,
+                       mcd_relint=float(np.mean(st.cd2i)) * float(np.sum(st.relint)), scalefactor=1.0,
+                       rows=np.asarray(rows, float), proto=rings, mode="CENTRED",
+                       dens_row=RING_KEYS.index("dens"), hsetup=st))
     return P
 
 
