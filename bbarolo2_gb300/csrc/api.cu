@@ -4,6 +4,7 @@
 // One context = one device, one CUDA stream, the constants of one cube (grid, beam kernel, data). Device
 // buffers grow with the largest batch seen and are reused. Errors are returned as status codes with a
 // message (bbgpu_last_error); nothing throws across the ABI.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdarg.h>
@@ -208,6 +209,19 @@ struct bbgpu_ctx {
                                   // result plus the difference (ring maps, MC model)
     int lean = 0;                 // the batch qualifies for the fast deposit kernels (one line, a linear channel
                                   // map, at most 128 samples per cloud)
+    // the beam convolution of the batch models: 0 float32 FMA (k_conv_resid), 1 bf16x3 or 2 tf32x3 on the tensor
+    // cores (k_conv_tc; the float32 kernel where a batch does not qualify)
+    int conv_variant = 0;
+    std::vector<double> h_kernel;         // the beam kernel (ky, kx) float64
+    void *d_bimg = nullptr;               // its B operand image for conv_variant
+    size_t d_bimg_cap = 0;
+    int bimg_variant = 0;
+    CUtensorMap *d_tmaps = nullptr;       // per member: TMA descriptor of its model
+    size_t d_tmaps_cap = 0;
+    std::vector<CUtensorMap> h_tmaps;
+    std::vector<long long> tmaps_key;     // (model, mstride, nz, boxes) of the descriptors on the device
+    int npart_used = 0;                   // partial pairs per member of the last convolution
+    int conv_used = 0;                    // variant of the last batch convolution
     long long launches = 0;
     long long h2d = 0, d2h = 0;
     cudaEvent_t ev[NTIMER + 1] = {};
@@ -479,6 +493,7 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
     cudaFree(ctx->d_sub); cudaFree(ctx->d_mem); cudaFree(ctx->d_pix); cudaFree(ctx->d_bucket);
     cudaFree(ctx->d_tcount); cudaFree(ctx->d_toff); cudaFree(ctx->d_tcur); cudaFree(ctx->d_model); cudaFree(ctx->d_scan);
     cudaFree(ctx->d_smooth); cudaFree(ctx->d_model64); cudaFree(ctx->d_partial); cudaFree(ctx->d_out2);
+    cudaFree(ctx->d_bimg); cudaFree(ctx->d_tmaps);
     cudaFree(ctx->d_err);
     for (void *q : {(void *)ctx->d_ppix, (void *)ctx->d_lc, (void *)ctx->d_ord, (void *)ctx->d_p0, (void *)ctx->d_ent,
                     (void *)ctx->d_pw, (void *)ctx->d_pwy, (void *)ctx->d_lv, (void *)ctx->d_near, (void *)ctx->d_psub,
@@ -562,6 +577,10 @@ extern "C" int bbgpu_set_option(bbgpu_ctx *ctx, int opt, int value) {
             ctx->share = value != 0;
             ctx->mc_dirty = true;
             ctx->an_dirty = true;
+            break;
+        case 4:
+            if (value < 0 || value > 2) return fail(ctx, BBGPU_ERR_ARG, "option 4: convolution variant 0, 1 or 2");
+            ctx->conv_variant = value;
             break;
         default: return fail(ctx, BBGPU_ERR_ARG, "unknown option %d", opt);
     }
@@ -695,6 +714,8 @@ extern "C" int bbgpu_set_kernel(bbgpu_ctx *ctx, const double *kernel, int ky, in
     ctx->ky = ky;
     ctx->kx = kx;
     ctx->kxw = kxw;
+    ctx->h_kernel.assign(kernel, kernel + (size_t)ky * kx);
+    ctx->bimg_variant = 0;
     ctx->kernel_set = true;
     return BBGPU_OK;
 }
@@ -798,7 +819,7 @@ static int batch_prepare_analytic(bbgpu_ctx *ctx, int nb, int nsub, const double
     ctx->lean = 0;
     ctx->ntile_total = 0;
     ctx->mstride = (long long)g.nx * g.ny * g.nz;
-    ctx->npart = conv_resid_npart(ctx->mem_host.data(), nb, g.nz);
+    ctx->npart = std::max(conv_resid_npart(ctx->mem_host.data(), nb, g.nz), conv_tc_npart(ctx->mem_host.data(), nb, g.nz));
     ctx->h2d = 0;
     // the azimuthal samples of the radii (uploaded when the radii change)
     std::string key((const char *)sr, sizeof(double) * nsub);
@@ -961,7 +982,7 @@ static int batch_prepare(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const
     ctx->ntile_total = toff;
     ctx->mc_dirty = true;
     ctx->mstride = (long long)g.nx * g.ny * g.nz;
-    ctx->npart = conv_resid_npart(ctx->mem_host.data(), nb, g.nz);
+    ctx->npart = std::max(conv_resid_npart(ctx->mem_host.data(), nb, g.nz), conv_tc_npart(ctx->mem_host.data(), nb, g.nz));
     size_t ncl = (size_t)nb * (E->host.ncloud ? E->host.ncloud : 1);
     if ((rc = dgrow(ctx, &ctx->d_sub, &ctx->d_sub_cap, (size_t)nb * (nsub ? nsub : 1)))) return rc;
     if ((rc = dgrow(ctx, &ctx->d_mem, &ctx->d_mem_cap, (size_t)nb))) return rc;
@@ -1268,6 +1289,58 @@ static int mc_lists(bbgpu_ctx *ctx, cudaStream_t s, bool tm) {
     return 0;
 }
 
+// The beam convolution and residual of the batch's models: on the tensor cores (ctx->conv_variant 1 or 2) when the
+// kernel, the channels and the tile table qualify, else the float32 kernel. Sets npart_used and conv_used.
+static int conv_batch(bbgpu_ctx *ctx, cudaStream_t s, bool conv, bool do_resid, TileSrc ts) {
+    const GridDev &g = ctx->g;
+    float *smoothed = ctx->keep_smoothed ? ctx->d_smooth : nullptr;
+    const int v = ctx->conv_variant;
+    const bool tc = conv && v && conv_tc_supported(v, ctx->ky, ctx->kx, g.nz) && (ctx->mstride % 4) == 0 &&
+                    (!ts.tsrc || ts.shx >= 3) && !ts.kout;
+    if (!tc) {
+        launch_conv_resid(s, g, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->d_model, ctx->mstride, g.nz,
+                          ctx->d_taps, ctx->ky, ctx->kx, ctx->kxw, smoothed, conv ? 1 : 0, do_resid ? 1 : 0,
+                          ctx->d_partial, ts);
+        CKL();
+        ctx->npart_used = conv_resid_npart(ctx->mem_host.data(), ctx->nb, g.nz);
+        ctx->conv_used = 0;
+        return 0;
+    }
+    int rc;
+    if (ctx->bimg_variant != v) {
+        std::vector<uint8_t> img;
+        conv_tc_image(v, ctx->h_kernel.data(), ctx->ky, ctx->kx, img);
+        if ((rc = dgrow(ctx, (uint8_t **)&ctx->d_bimg, &ctx->d_bimg_cap, img.size()))) return rc;
+        CK(cudaMemcpyAsync(ctx->d_bimg, img.data(), img.size(), cudaMemcpyHostToDevice, s));
+        CK(cudaStreamSynchronize(s));
+        ctx->bimg_variant = v;
+    }
+    // the members' TMA descriptors, rebuilt when the model buffer or a box changes
+    std::vector<long long> key{(long long)(uintptr_t)ctx->d_model, ctx->mstride, (long long)g.nz, (long long)ctx->nb};
+    for (int k = 0; k < ctx->nb; k++) {
+        key.push_back(ctx->mem_host[k].bx);
+        key.push_back(ctx->mem_host[k].by);
+        key.push_back((long long)(uintptr_t)ctx->mem_host[k].deff);
+    }
+    if (key != ctx->tmaps_key) {
+        if (!conv_tc_maps(ctx->mem_host.data(), ctx->nb, ctx->d_model, ctx->mstride, g.nz, g.nx, g.ny, ctx->h_tmaps))
+            return fail(ctx, BBGPU_ERR_CUDA, "cuTensorMapEncodeTiled refused a model descriptor");
+        if ((rc = dgrow(ctx, &ctx->d_tmaps, &ctx->d_tmaps_cap, 2 * (size_t)ctx->nb))) return rc;
+        CK(cudaMemcpyAsync(ctx->d_tmaps, ctx->h_tmaps.data(), sizeof(CUtensorMap) * 2 * ctx->nb,
+                           cudaMemcpyHostToDevice, s));
+        CK(cudaStreamSynchronize(s));
+        ctx->tmaps_key = key;
+    }
+    const int npart = conv_tc_npart(ctx->mem_host.data(), ctx->nb, g.nz);
+    CK(cudaMemsetAsync(ctx->d_partial, 0, sizeof(double) * 2 * (size_t)ctx->nb * npart, s));
+    launch_conv_tc(s, v, g, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->d_tmaps, ctx->d_bimg, ctx->mstride, g.nz,
+                   ctx->ky, ctx->kx, smoothed, 1, do_resid ? 1 : 0, ctx->d_partial, npart, ts, ctx->d_err);
+    CKL();
+    ctx->npart_used = npart;
+    ctx->conv_used = v;
+    return 0;
+}
+
 static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
     if (!ctx->uploaded) return fail(ctx, BBGPU_ERR_STATE, "run before upload");
     const GridDev &g = ctx->g;
@@ -1374,14 +1447,12 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
         TileSrc ts{nullptr, 0, 0, nullptr, 0};
         if (ctx->galmodtype == BBGPU_MC && ctx->mc_n2)
             ts = TileSrc{ctx->d_tsrc, ilog2(ctx->tx), ilog2(ctx->ty), nullptr, 0};
-        launch_conv_resid(s, g, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->d_model, ctx->mstride, g.nz,
-                          ctx->d_taps, ctx->ky, ctx->kx, ctx->kxw, ctx->keep_smoothed ? ctx->d_smooth : nullptr,
-                          conv ? 1 : 0, do_resid ? 1 : 0, ctx->d_partial, ts);
-        CKL();
+        int rc = conv_batch(ctx, s, conv, do_resid, ts);
+        if (rc) return rc;
     }
     if (tm) CK(cudaEventRecord(ctx->ev[12], s));
     if (do_resid) {
-        launch_reduce_partials(s, ctx->d_partial, ctx->npart, ctx->nb, ctx->d_out2);
+        launch_reduce_partials(s, ctx->d_partial, ctx->npart_used, ctx->nb, ctx->d_out2);
         CKL();
     }
     if (tm) {
@@ -1403,6 +1474,9 @@ static int check_err(bbgpu_ctx *ctx) {
     if (*ctx->h_err) {
         int e = *ctx->h_err;
         CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+        if (e & ERR_TC)
+            return fail(ctx, BBGPU_ERR_KERNEL,
+                        "the tensor-core convolution gave up waiting for one of its stages (bounded wait expired)");
         if (e & ERR_SHARE)
             return fail(ctx, BBGPU_ERR_KERNEL,
                         "a member computed as a difference from member 0's model has another fixed-point exponent "

@@ -1,8 +1,11 @@
 // Launch wrappers of the bbgpu kernels (defined in mc.cu, conv.cu, analytic.cu, resid.cu), called by api.cu.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <vector>
 
 #include "internal.h"
 
@@ -137,6 +140,22 @@ void launch_conv_table(cudaStream_t s, const GridDev &g, const MemberDev *mem, i
                        const float *model, long long mstride, int nz, const float *taps, int ky, int kx, int kxw,
                        float *smoothed, int do_conv, int do_resid, double *partial, int npart, TileSrc ts);
 void launch_reduce_partials(cudaStream_t s, const double *partial, int npart, int nb, double *out2);
+
+// ---- convolution + residual on the tensor cores (conv_tc.cu): variant 1 bf16x3, 2 tf32x3 (split products,
+// FP32 accumulation in TMEM). Kernels of at most 16 rows and 33 columns, nz a multiple of 4 (TMA rows of 16 bytes).
+#define ERR_TC 16                 // a bounded wait of the tensor-core convolution expired
+bool conv_tc_supported(int variant, int ky, int kx, int nz);
+// the B operand image (the banded Toeplitz rows of the flipped kernel, split hi / lo) of a kernel (ky, kx)
+void conv_tc_image(int variant, const double *kern, int ky, int kx, std::vector<uint8_t> &img);
+// TMA descriptors: maps[k] the model (by, bx, nz) float32 of member k at model + k mstride, maps[nb + k] its data
+// (the cube's deff, ny x nx x nz)
+bool conv_tc_maps(const MemberDev *mem_host, int nb, const float *model, long long mstride, int nz, int nx, int ny,
+                  std::vector<CUtensorMap> &maps);
+// partial pairs per member (16 x 16 pixel tiles x blocks of 128 channels x 4 channel groups); zeroed by the caller
+int conv_tc_npart(const MemberDev *mem_host, int nb, int nz);
+void launch_conv_tc(cudaStream_t s, int variant, const GridDev &g, const MemberDev *mem, const MemberDev *mem_host,
+                    int nb, const CUtensorMap *maps, const void *bimg, long long mstride, int nz, int ky, int kx,
+                    float *smoothed, int do_conv, int do_resid, double *partial, int npart, TileSrc ts, int *err);
 
 // ---- layouts and stand-alone residuals (resid.cu)
 void launch_prep_deff(cudaStream_t s, const float *data, const uint8_t *mask, const uint8_t *region, int maskmode,

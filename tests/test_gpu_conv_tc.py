@@ -1,0 +1,125 @@
+"""The beam convolution of the batch path in its three variants: float32 FMA (k_conv_resid) and the tensor-core
+kernels (k_conv_tc: tcgen05 MMAs with split products, bf16x3 and tf32x3, FP32 accumulation in TMEM), each
+compared per voxel with the FP64 oracle (the direct convolution of the same model, the reference's FFT to 1e-16),
+and their sums of squared residuals with the oracle pipeline's."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+# largest relative error of a smoothed voxel against the FP64 convolution of the same model, over the voxels above
+# FLOOR times the peak (below it the reference's own threshold of 1e-12 and float32 underflow dominate). The
+# smoothed cube is required within 1e-5 relative: float32 and tf32x3 meet it; bf16x3 is bounded by its split
+# (a = ah + al + ea, |ea| <= 2^-16 |a|, likewise the taps, and the dropped al bl): 1.6e-5 measured on these
+# cubes, the same figure as an exact float64 emulation of the split products, so it is tested at 2.5e-5 and
+# left out of the variants the autotuner may choose under the 1e-5 bound.
+NORTH_STAR = 1e-5
+REL_TOL = {0: NORTH_STAR, 1: 2.5e-5, 2: NORTH_STAR}
+FLOOR = 1e-6
+NAMES = {0: "f32", 1: "bf16x3", 2: "tf32x3"}
+
+
+def _setup(wl, nb, seed=0):
+    from bbarolo2_gb300 import configs, engine
+    from bbarolo2_gb300.galmod import ring_rows_batch
+    cube, rings = configs.WORKLOADS[wl](galmodtype="MC")
+    dm = engine.DiskModel(cube)
+    truth = dm.array(rings, seed=1)
+    g = np.random.default_rng(seed)
+    sigma = 0.01 * truth.max()
+    data = (truth + g.normal(0, sigma, truth.shape)).astype(np.float32)
+    mask = truth > 3 * sigma
+    L = engine.BatchLikelihood(dm, data, mask, maskmode=2, sigma=sigma)
+    rows = ring_rows_batch([rings] * nb)
+    rows[1:, 4] *= 1 + 0.05 * g.standard_normal((nb - 1, rings.nr))
+    rows[1:, 5] *= 1 + 0.2 * g.random((nb - 1, rings.nr))
+    return dm, L, rings, rows
+
+
+def _smoothed(ctx, L, sr, nv, descs, boxes, variant):
+    from bbarolo2_gb300 import _lib
+    ctx.set_option(4, variant)
+    ss, _ = L.run(sr, nv, descs)
+    nz = L.shape[0]
+    out, mods = [], []
+    for k, (blo, bhi) in enumerate(boxes):
+        by, bx = bhi[1] - blo[1], bhi[0] - blo[0]
+        s = np.zeros((by, bx, nz), np.float32)
+        m = np.zeros((by, bx, nz), np.float32)
+        ctx.check(ctx.L.bbgpu_eval_model(ctx.h, k, 1, _lib.ptr(s), by, bx, nz))
+        ctx.check(ctx.L.bbgpu_eval_model(ctx.h, k, 0, _lib.ptr(m), by, bx, nz))
+        out.append(s)
+        mods.append(m)
+    return ss, out, mods
+
+
+@pytest.mark.parametrize("wl,nb", [("classic64", 3), ("global160", 3), ("bayes256", 2)])
+def test_conv_variants_per_voxel_vs_fp64(gpu_lib, oracle_lib, wl, nb):
+    from bbarolo2_gb300 import _lib
+    dm, L, rings, rows = _setup(wl, nb)
+    ctx = dm.ctx
+    sr, nv, descs, boxes = L.prepare(rows, rings, seed=1)
+    ctx.set_option(_lib.OPT_KEEP_SMOOTHED, 1)
+    try:
+        res = {v: _smoothed(ctx, L, sr, nv, descs, boxes, v) for v in (0, 1, 2)}
+    finally:
+        ctx.set_option(_lib.OPT_KEEP_SMOOTHED, 0)
+        ctx.set_option(4, 0)
+    worst = {}
+    for k in range(nb):
+        model = res[0][2][k]
+        for v in (1, 2):                       # the same unsmoothed model in every run
+            np.testing.assert_array_equal(res[v][2][k], model)
+        ref = oracle_lib.conv_same(model.astype(np.float64).transpose(2, 0, 1), dm.cfield, dm.scalefactor)
+        ref = ref.transpose(1, 2, 0)
+        big = ref > FLOOR * ref.max()
+        for v in (0, 1, 2):
+            out = res[v][1][k].astype(np.float64)
+            rel = np.abs(out[big] - ref[big]) / ref[big]
+            worst[v] = max(worst.get(v, 0.0), float(rel.max()))
+            # below the floor: within the floor of the peak
+            assert np.abs(out[~big] - ref[~big]).max() <= 2 * FLOOR * ref.max()
+    print({NAMES[v]: f"{worst[v]:.2e}" for v in worst})
+    for v in (0, 1, 2):
+        assert worst[v] <= REL_TOL[v], (NAMES[v], worst[v])
+    # the sums of squares of the variants agree (the residual against the data, f64 accumulation)
+    for v in (1, 2):
+        np.testing.assert_allclose(res[v][0], res[0][0], rtol=1e-5)
+
+
+def test_conv_variants_deterministic_and_shared_batch(gpu_lib):
+    """A finite-difference batch (members computed as differences from member 0, tiles taken from its model and
+    its partial sums) gives the same sums with and without the sharing, on the tensor cores as with float32."""
+    from bbarolo2_gb300 import _lib
+    from bbarolo2_gb300.galmod import ring_rows_batch
+    dm, L, rings, _ = _setup("global160", 2)
+    base = ring_rows_batch([rings])[0]
+    nb = 9
+    rows = np.repeat(base[None], nb, axis=0)
+    for i in range(1, nb):
+        rows[i, 4 if i % 2 else 5, (3 * i) % rings.nr] += 2.0 if i % 2 else 0.5
+    ctx = dm.ctx
+    sr, nv, descs, boxes = L.prepare(rows, rings, seed=1)
+    out = {}
+    try:
+        for v in (0, 1, 2):
+            ctx.set_option(4, v)
+            for share in (1, 0):
+                ctx.set_option(_lib.OPT_SHARE, share)
+                a, _ = L.run(sr, nv, descs)
+                b, _ = L.run(sr, nv, descs)
+                np.testing.assert_array_equal(a, b)
+                out[v, share] = a
+            np.testing.assert_array_equal(out[v, 1], out[v, 0])
+    finally:
+        ctx.set_option(_lib.OPT_SHARE, 1)
+        ctx.set_option(4, 0)
+    for v in (1, 2):
+        np.testing.assert_allclose(out[v, 1], out[0, 1], rtol=1e-5)
+
+
+def test_conv_variant_option_checked(gpu_lib):
+    from bbarolo2_gb300 import _lib
+    ctx = _lib.Context(0)
+    assert ctx.L.bbgpu_set_option(ctx.h, 4, 3) == _lib.ERR_ARG
+    assert ctx.L.bbgpu_set_option(ctx.h, 4, 2) == _lib.OK
