@@ -109,6 +109,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, volatile
     const long long t0 = clock64();
     for (unsigned it = 0;; it++) {
         if (mbar_test(b, parity)) return true;
+        if (it >= 8) __nanosleep(32);               // (a waiting warp leaves the issue slots to the others)
         if ((it & 63) == 63) {
             if (*abort) return false;
             if (clock64() - t0 > (1LL << 31)) {
@@ -257,7 +258,9 @@ __device__ __forceinline__ bool next_run(unsigned skip, int nt, int &i, int &ta,
 template <int V, int KP>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant__ TcArgs a) {
     extern __shared__ uint8_t smraw[];
-    uint8_t *sm = (uint8_t *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
+    // (aligned by an offset on the shared pointer itself: a pointer rebuilt from an integer would lose its address
+    // space, and every access through it would be a generic load or store)
+    uint8_t *sm = smraw + ((1024u - (saddr(smraw) & 1023u)) & 1023u);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint8_t *fst = sm;                                       // NFS x fstage: input rows, float32 [px][128]
     uint8_t *ast = fst + NFS * a.fstage;                     // NAS x (hi, lo) operand stages
@@ -568,7 +571,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&freeb[v % TC_RING]);
                     const float *D = (const float *)(dst_ + (gd % NDS) * DBOX_BYTES) + ch;
-                    if (zok) {
+                    if (zok && !a.smoothed && a.do_resid && a.do_conv == 1 && !fr) {
+                        // the likelihood's case: threshold, scale and the sum of squares only
+                        const int nxv = min(TC_X, mbx - x0);
+                        float s2 = 0.0f;
+#pragma unroll
+                        for (int x = 0; x < TC_X; x++) {
+                            float m = acc[x];
+                            m = m < 1.0e-12f ? 0.0f : m * scale;
+                            const float d = D[x * TC_M];
+                            const float rr = d - m;
+                            s2 += (x < nxv && d == d) ? rr * rr : 0.0f;
+                        }
+                        ss += s2;
+                    } else if (zok) {
 #pragma unroll
                         for (int x = 0; x < TC_X; x++) {
                             const int xx = x0 + x;
