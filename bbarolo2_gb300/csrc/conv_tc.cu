@@ -19,14 +19,16 @@
 // ah bh + ah bl + al bh in FP32 accumulation (dropped al bl and the splits' remainders: ~2^-17 relative per
 // product). TF32X3: the same with tf32 halves (~2^-21). Both are compared per voxel with the float64 oracle.
 //
-// Pipeline (persistent CTAs, one per SM, 11 warps; each CTA walks its work items, a strip or a run of its tiles):
+// Pipeline (persistent CTAs, one per SM, 15 warps; each CTA walks its work items, a strip or a run of its tiles):
 // warp 0 issues TMA loads of each input row (8-pixel boxes of 128 channels, zero fill outside the box; with a tile
-// table each box from the member whose model holds that deposit tile) into float32 staging stages; warps 2-5 split
-// the staged row into the hi/lo operand stage (K-major canonical layout, no swizzle) and flag rows that are all
-// zero; warp 1 (one lane) issues the MMAs and commits their completion to the stage's barrier and to the completed
-// output row's barrier; warp 10 stages the data rows of the residual by TMA; warps 6-9 are the epilogue. Every wait
-// on an mbarrier is bounded (about one second): on expiry the kernel sets ERR_TC in the error flag, waits (bounded)
-// for its copies and MMAs in flight, frees its TMEM and returns.
+// table each box from the member whose model holds that deposit tile) into float32 staging stages; warps 2-9 split
+// the staged row into the hi/lo operand stage (K-major canonical layout, no swizzle; two warps per 32 channels, a
+// half row each) and flag rows that are all zero; warp 1 (one lane) issues the MMAs and commits their completion
+// to the stage's barrier and to the completed output row's barrier; warp 14 stages the data rows of the residual by
+// TMA; warps 10-13 are the epilogue (warp w reads TMEM lanes 32 (w mod 4) .. 32 (w mod 4) + 31). A role's time per
+// row is its instruction count times the latency of its one warp per scheduler: the split, the longest, has two.
+// Every wait on an mbarrier is bounded (about one second): on expiry the kernel sets ERR_TC in the error flag, waits
+// (bounded) for its copies and MMAs in flight, frees its TMEM and returns.
 
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -50,7 +52,7 @@ constexpr int TC_M = 128;          // channels of a CTA
 constexpr int NFS = 4;             // float32 staging stages of model rows
 constexpr int NAS = 2;             // operand stages
 constexpr int NDS = 4;             // float32 stages of data rows
-constexpr int TC_THREADS = 352;
+constexpr int TC_THREADS = 480;
 constexpr int TC_MAX_TILES = 16;   // 16-row tiles of a work item
 constexpr int BOX_PX = 8;          // pixels of a TMA box of the model
 constexpr int BOX_BYTES = BOX_PX * TC_M * 4;
@@ -273,11 +275,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
     int *misc = (int *)(fin + 1);
     volatile int *abort_flag = misc;                         // [0]
     volatile uint32_t *tmem_hold = (volatile uint32_t *)(misc + 1);
-    volatile int *rowflag = misc + 2;                        // NAS x 4
+    volatile int *rowflag = misc + 2;                        // NAS x 8 (per splitting warp)
 
     if (threadIdx.x == 0) {
-        for (int i = 0; i < NFS; i++) { mbar_init(&full_f[i], 1); mbar_init(&empty_f[i], 4); }
-        for (int i = 0; i < NAS; i++) { mbar_init(&full_a[i], 4); mbar_init(&empty_a[i], 1); }
+        for (int i = 0; i < NFS; i++) { mbar_init(&full_f[i], 1); mbar_init(&empty_f[i], 8); }
+        for (int i = 0; i < NAS; i++) { mbar_init(&full_a[i], 8); mbar_init(&empty_a[i], 1); }
         for (int i = 0; i < NDS; i++) { mbar_init(&full_d[i], 1); mbar_init(&empty_d[i], 4); }
         for (int i = 0; i < TC_RING; i++) { mbar_init(&ready[i], 1); mbar_init(&freeb[i], 4); }
         mbar_init(fin, 1);
@@ -298,7 +300,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
     __syncthreads();
     tc_fence_after();
     const uint32_t tbase = *tmem_hold;
-    if (warp >= 6 && warp < 10) {
+    if (warp >= 10 && warp < 14) {
         // zero accumulators: every MMA accumulates
         const uint32_t tl = tbase + ((uint32_t)((warp & 3) * 32) << 16);
         for (int c = 0; c < TC_COLS; c += 16) tmem_zero16(tl + c);
@@ -357,7 +359,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
                 const uint32_t q = gf - 1 - j;
                 mbar_wait(&full_f[q % NFS], (q / NFS) & 1, abort_flag, err);
             }
-    } else if (warp == 10) {
+    } else if (warp == 14) {
         // ---------------------------------------------------------------- TMA: data rows of the residual
         uint32_t gd = 0;
         bool ok = true;
@@ -423,7 +425,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
                         }
                         const int lo = max(0, r - ky + 1), hi = min(r, nout - 1);
                         const bool nzr =
-                            rowflag[sa * 4] | rowflag[sa * 4 + 1] | rowflag[sa * 4 + 2] | rowflag[sa * 4 + 3];
+                            rowflag[sa * 8] | rowflag[sa * 8 + 1] | rowflag[sa * 8 + 2] | rowflag[sa * 8 + 3] |
+                            rowflag[sa * 8 + 4] | rowflag[sa * 8 + 5] | rowflag[sa * 8 + 6] | rowflag[sa * 8 + 7];
                         if (nzr && lo <= hi) {
                             const uint32_t ahi = saddr(ast + sa * a.astage), alo = ahi + a.aop;
                             for (int o = lo; o <= hi;) {
@@ -457,9 +460,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
             mma_commit(fin);
             mbar_wait(fin, 0, abort_flag, err);
         }
-    } else if (warp < 6) {
-        // ---------------------------------------------------------------- operand split
-        const int cg = warp - 2, ch = cg * 32 + lane;
+    } else if (warp < 10) {
+        // ---------------------------------------------------------------- operand split (warps 2-9)
+        // two warps per group of 32 channels, each splitting half of the row's pixels
+        const int sw = warp - 2, cg = sw & 3, half = sw >> 2, ch = cg * 32 + lane;
         uint32_t gf = 0, ga = 0;
         bool ok = true;
         for (int idx = blockIdx.x; ok && idx < nitems; idx += gridDim.x) {
@@ -467,7 +471,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
             if (!it.valid) continue;
             const unsigned skip = skip_mask(a, it, lane, -1);
             const int mby = a.mem[it.k].by;
-            const int z = it.zb * TC_M + ch;
+            const bool zin = it.zb * TC_M + ch < a.nz;
+            const int wused = zin ? a.wused : 0;
             int i = 0, ta, tb;
             while (ok && next_run(skip, it.nt, i, ta, tb)) {
                 const int ylo = (it.t0 + ta) * TC_X;
@@ -481,38 +486,44 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
                     const float *F = (const float *)(fst + sf * a.fstage) + (size_t)a.dx * TC_M + ch;
                     uint8_t *Ah = ast + sa * a.astage + (ch >> 3) * a.sbo_a + (ch & 7) * 16;
                     uint8_t *Al = Ah + a.aop;
-                    bool any = false;
+                    uint32_t bits = 0;
                     if (V == 0) {
+                        constexpr int NC = KP / 16;                  // 8-pixel chunks of this warp's half
 #pragma unroll
-                        for (int kc = 0; kc < KP / 8; kc++) {
+                        for (int c = 0; c < NC; c++) {
+                            const int kc = half * NC + c;
                             float v[8];
 #pragma unroll
                             for (int e = 0; e < 8; e++) {
                                 const int kk = kc * 8 + e;
-                                v[e] = (kk < a.wused && z < a.nz) ? F[kk * TC_M] : 0.0f;
-                                any |= v[e] != 0.0f;
+                                v[e] = kk < wused ? F[kk * TC_M] : 0.0f;
+                                bits |= __float_as_uint(v[e]);
                             }
-                            uint4 h, l;
-                            float hv[8];
+                            uint32_t h[4], l[4];
 #pragma unroll
-                            for (int e = 0; e < 8; e++) hv[e] = __bfloat162float(__float2bfloat16_rn(v[e]));
-                            h.x = pack_bf16(hv[0], hv[1]); h.y = pack_bf16(hv[2], hv[3]);
-                            h.z = pack_bf16(hv[4], hv[5]); h.w = pack_bf16(hv[6], hv[7]);
-                            l.x = pack_bf16(v[0] - hv[0], v[1] - hv[1]); l.y = pack_bf16(v[2] - hv[2], v[3] - hv[3]);
-                            l.z = pack_bf16(v[4] - hv[4], v[5] - hv[5]); l.w = pack_bf16(v[6] - hv[6], v[7] - hv[7]);
-                            *(uint4 *)(Ah + kc * 128) = h;
-                            *(uint4 *)(Al + kc * 128) = l;
+                            for (int e = 0; e < 4; e++) {
+                                const __nv_bfloat162 hb = __float22bfloat162_rn(make_float2(v[2 * e], v[2 * e + 1]));
+                                const float2 hf = __bfloat1622float2(hb);
+                                const __nv_bfloat162 lb =
+                                    __float22bfloat162_rn(make_float2(v[2 * e] - hf.x, v[2 * e + 1] - hf.y));
+                                h[e] = *(const uint32_t *)&hb;
+                                l[e] = *(const uint32_t *)&lb;
+                            }
+                            *(uint4 *)(Ah + kc * 128) = make_uint4(h[0], h[1], h[2], h[3]);
+                            *(uint4 *)(Al + kc * 128) = make_uint4(l[0], l[1], l[2], l[3]);
                         }
                     } else {
+                        constexpr int NC = KP / 8;                   // 4-pixel chunks of this warp's half
 #pragma unroll
-                        for (int kc = 0; kc < KP / 4; kc++) {
+                        for (int c = 0; c < NC; c++) {
+                            const int kc = half * NC + c;
                             if (kc * 4 >= a.nks * 8) break;          // (beyond the MMAs' K: never read)
                             float v[4];
 #pragma unroll
                             for (int e = 0; e < 4; e++) {
                                 const int kk = kc * 4 + e;
-                                v[e] = (kk < a.wused && z < a.nz) ? F[kk * TC_M] : 0.0f;
-                                any |= v[e] != 0.0f;
+                                v[e] = kk < wused ? F[kk * TC_M] : 0.0f;
+                                bits |= __float_as_uint(v[e]);
                             }
                             float4 h, l;
                             h.x = tf32_rna(v[0]); h.y = tf32_rna(v[1]); h.z = tf32_rna(v[2]); h.w = tf32_rna(v[3]);
@@ -522,9 +533,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
                         }
                     }
                     fence_async_smem();
-                    const unsigned bal = __ballot_sync(0xffffffffu, any);
+                    const unsigned bal = __ballot_sync(0xffffffffu, (bits << 1) != 0);   // (any value but +-0)
                     if (lane == 0) {
-                        rowflag[sa * 4 + cg] = bal != 0;
+                        rowflag[sa * 8 + sw] = bal != 0;
                         mbar_arrive(&full_a[sa]);
                         mbar_arrive(&empty_f[sf]);
                     }
@@ -533,7 +544,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
             }
         }
     } else {
-        // ---------------------------------------------------------------- epilogue (warps 6-9)
+        // ---------------------------------------------------------------- epilogue (warps 10-13)
         const int eg = warp & 3, ch = eg * 32 + lane;
         const uint32_t tl = tbase + ((uint32_t)(eg * 32) << 16);
         const float scale = (float)a.g.scalefactor;
