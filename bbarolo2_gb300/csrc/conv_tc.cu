@@ -19,14 +19,15 @@
 // ah bh + ah bl + al bh in FP32 accumulation (dropped al bl and the splits' remainders: ~2^-17 relative per
 // product). TF32X3: the same with tf32 halves (~2^-21). Both are compared per voxel with the float64 oracle.
 //
-// Pipeline (persistent CTAs, one per SM, 15 warps; each CTA walks its work items, a strip or a run of its tiles):
+// Pipeline (persistent CTAs, one per SM, 19 warps; each CTA walks its work items, a strip or a run of its tiles):
 // warp 0 issues TMA loads of each input row (8-pixel boxes of 128 channels, zero fill outside the box; with a tile
 // table each box from the member whose model holds that deposit tile) into float32 staging stages; warps 2-9 split
 // the staged row into the hi/lo operand stage (K-major canonical layout, no swizzle; two warps per 32 channels, a
 // half row each) and flag rows that are all zero; warp 1 (one lane) issues the MMAs and commits their completion
-// to the stage's barrier and to the completed output row's barrier; warp 14 stages the data rows of the residual by
-// TMA; warps 10-13 are the epilogue (warp w reads TMEM lanes 32 (w mod 4) .. 32 (w mod 4) + 31). A role's time per
-// row is its instruction count times the latency of its one warp per scheduler: the split, the longest, has two.
+// to the stage's barrier and to the completed output row's barrier; warp 18 stages the data rows of the residual by
+// TMA; warps 10-17 are the epilogue (warp w reads TMEM lanes 32 (w mod 4) .. 32 (w mod 4) + 31, half of a row's
+// columns each). A role's time per row is its instruction count times the latency of its warps on each scheduler:
+// the split and the epilogue, the longest, have two warps per lane quarter.
 // Every wait on an mbarrier is bounded (about one second): on expiry the kernel sets ERR_TC in the error flag, waits
 // (bounded) for its copies and MMAs in flight, frees its TMEM and returns.
 
@@ -52,7 +53,9 @@ constexpr int TC_M = 128;          // channels of a CTA
 constexpr int NFS = 4;             // float32 staging stages of model rows
 constexpr int NAS = 2;             // operand stages
 constexpr int NDS = 4;             // float32 stages of data rows
-constexpr int TC_THREADS = 480;
+constexpr int TC_THREADS = 608;
+constexpr int EPW = 8;             // epilogue warps: two per TMEM lane quarter, 8 columns of a row each
+constexpr int EPC = TC_X / 2;
 constexpr int TC_MAX_TILES = 16;   // 16-row tiles of a work item
 constexpr int BOX_PX = 8;          // pixels of a TMA box of the model
 constexpr int BOX_BYTES = BOX_PX * TC_M * 4;
@@ -171,6 +174,22 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
     for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_zero8(uint32_t taddr) {
+    const uint32_t z = 0;
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(taddr), "r"(z)
+                 : "memory");
+}
+
 __device__ __forceinline__ void tmem_zero16(uint32_t taddr) {
     const uint32_t z = 0;
     asm volatile(
@@ -225,7 +244,7 @@ __device__ __forceinline__ Item item_of(const TcArgs &a, int idx) {
 
 // (warp-wide) bit i set: tile t0 + i of the item takes member 0's sums (a member computed as a difference from
 // member 0 whose tile's input lies wholly in member 0's deposit tiles); with eg >= 0 the lane also writes the
-// reduction's sentinel (-1) into that channel group's partial pair of the tile
+// reduction's sentinel (-1) into that epilogue warp's partial pair of the tile
 __device__ __forceinline__ unsigned skip_mask(const TcArgs &a, const Item &it, int lane, int eg) {
     bool sk = false;
     if (a.ts.tsrc && it.k != 0 && !a.smoothed && lane < it.nt) {
@@ -239,7 +258,7 @@ __device__ __forceinline__ unsigned skip_mask(const TcArgs &a, const Item &it, i
                 if (__ldg(&a.ts.tsrc[M.tile_off + yt * M.ntx + xt]) != 0) { sk = false; break; }
         if (sk && eg >= 0 && a.do_resid) {
             double *p = a.partial +
-                        2 * ((size_t)it.k * a.npart + ((size_t)(ty * it.ntx + it.sx) * a.nzb + it.zb) * 4 + eg);
+                        2 * ((size_t)it.k * a.npart + ((size_t)(ty * it.ntx + it.sx) * a.nzb + it.zb) * EPW + eg);
             p[0] = -1.0;
             p[1] = 0.0;
         }
@@ -275,13 +294,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
     int *misc = (int *)(fin + 1);
     volatile int *abort_flag = misc;                         // [0]
     volatile uint32_t *tmem_hold = (volatile uint32_t *)(misc + 1);
-    volatile int *rowflag = misc + 2;                        // NAS x 8 (per splitting warp)
+    volatile uint8_t *rowflag = (volatile uint8_t *)(misc + 2);   // NAS x 8 bytes (per splitting warp)
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < NFS; i++) { mbar_init(&full_f[i], 1); mbar_init(&empty_f[i], 8); }
         for (int i = 0; i < NAS; i++) { mbar_init(&full_a[i], 8); mbar_init(&empty_a[i], 1); }
-        for (int i = 0; i < NDS; i++) { mbar_init(&full_d[i], 1); mbar_init(&empty_d[i], 4); }
-        for (int i = 0; i < TC_RING; i++) { mbar_init(&ready[i], 1); mbar_init(&freeb[i], 4); }
+        for (int i = 0; i < NDS; i++) { mbar_init(&full_d[i], 1); mbar_init(&empty_d[i], EPW); }
+        for (int i = 0; i < TC_RING; i++) { mbar_init(&ready[i], 1); mbar_init(&freeb[i], EPW); }
         mbar_init(fin, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -300,10 +319,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
     __syncthreads();
     tc_fence_after();
     const uint32_t tbase = *tmem_hold;
-    if (warp >= 10 && warp < 14) {
+    if (warp >= 10 && warp < 10 + EPW) {
         // zero accumulators: every MMA accumulates
-        const uint32_t tl = tbase + ((uint32_t)((warp & 3) * 32) << 16);
-        for (int c = 0; c < TC_COLS; c += 16) tmem_zero16(tl + c);
+        const uint32_t tl = tbase + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(((warp - 10) >> 2) * EPC);
+        for (int c = 0; c < TC_COLS; c += TC_X) tmem_zero8(tl + c);
         tmem_wait_st();
         tc_fence_before();
     }
@@ -359,7 +378,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
                 const uint32_t q = gf - 1 - j;
                 mbar_wait(&full_f[q % NFS], (q / NFS) & 1, abort_flag, err);
             }
-    } else if (warp == 14) {
+    } else if (warp == 10 + EPW) {
         // ---------------------------------------------------------------- TMA: data rows of the residual
         uint32_t gd = 0;
         bool ok = true;
@@ -397,9 +416,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
         const uint32_t idesc0 = (1u << 4) | ((V == 0 ? 1u : 2u) << 7) | ((V == 0 ? 1u : 2u) << 10) |
                                 ((uint32_t)(TC_M >> 4) << 24);
         const int nks = a.nks;                               // K steps of 32 bytes
+        constexpr int KSMAX = V == 0 ? KP / 16 : KP / 8;
         uint32_t ga = 0, vbase = 0;
         bool ok = true;
-        const uint32_t bhi = saddr(bsm), blo = bhi + a.bop;
+        // the descriptors of the first operand stage and of B, advanced by adding address offsets (the descriptor's
+        // low field is the shared-memory address / 16; every address stays below 256 KB, so nothing carries out)
+        const uint64_t dA0 = sdesc(saddr(ast), 128, a.sbo_a), dB0 = sdesc(saddr(bsm), 128, a.sbo_b);
+        const uint64_t astg16 = a.astage >> 4, aop16 = a.aop >> 4, bop16 = a.bop >> 4, sbob16 = a.sbo_b >> 4;
         for (int idx = blockIdx.x; ok && idx < nitems; idx += gridDim.x) {
             const Item it = item_of(a, idx);
             if (!it.valid) continue;
@@ -424,24 +447,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
                             }
                         }
                         const int lo = max(0, r - ky + 1), hi = min(r, nout - 1);
-                        const bool nzr =
-                            rowflag[sa * 8] | rowflag[sa * 8 + 1] | rowflag[sa * 8 + 2] | rowflag[sa * 8 + 3] |
-                            rowflag[sa * 8 + 4] | rowflag[sa * 8 + 5] | rowflag[sa * 8 + 6] | rowflag[sa * 8 + 7];
+                        const bool nzr = *(volatile const uint64_t *)(rowflag + sa * 8) != 0;
                         if (nzr && lo <= hi) {
-                            const uint32_t ahi = saddr(ast + sa * a.astage), alo = ahi + a.aop;
+                            const uint64_t dA = dA0 + (uint64_t)sa * astg16;
                             for (int o = lo; o <= hi;) {
                                 const int slot = (int)((vbase + o) % TC_RING);
                                 const int n = min(min(hi - o + 1, TC_RING - slot), 256 / TC_X);
                                 const int jb = ky - 1 - (r - o);
                                 const uint32_t idesc = idesc0 | ((uint32_t)((TC_X * n) >> 3) << 17);
                                 const uint32_t dtm = tbase + (uint32_t)(slot * TC_X);
-                                const uint32_t boff = (uint32_t)(jb * 2) * a.sbo_b;
+                                const uint64_t dB = dB0 + (uint64_t)(jb * 2) * sbob16;
 #pragma unroll
                                 for (int p = 0; p < 3; p++) {
-                                    const uint32_t aa = p == 2 ? alo : ahi, bb = (p == 1 ? blo : bhi) + boff;
-                                    for (int ks = 0; ks < nks; ks++)
-                                        mma<V>(dtm, sdesc(aa + 256 * ks, 128, a.sbo_a),
-                                               sdesc(bb + 256 * ks, 128, a.sbo_b), idesc);
+                                    const uint64_t da = dA + (p == 2 ? aop16 : 0), db = dB + (p == 1 ? bop16 : 0);
+#pragma unroll
+                                    for (int ks = 0; ks < KSMAX; ks++)
+                                        if (ks < nks) mma<V>(dtm, da + 16 * ks, db + 16 * ks, idesc);
                                 }
                                 o += n;
                             }
@@ -544,23 +565,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
             }
         }
     } else {
-        // ---------------------------------------------------------------- epilogue (warps 10-13)
-        const int eg = warp & 3, ch = eg * 32 + lane;
-        const uint32_t tl = tbase + ((uint32_t)(eg * 32) << 16);
+        // ---------------------------------------------------------------- epilogue (warps 10-17)
+        // warp w: TMEM lanes (channels) 32 (w mod 4) + lane, columns ex0 .. ex0 + 7 of each output row
+        const int ep = warp - 10, eg = warp & 3, ch = eg * 32 + lane, ex0 = (ep >> 2) * EPC;
+        const uint32_t tl = tbase + ((uint32_t)(eg * 32) << 16) + (uint32_t)ex0;
         const float scale = (float)a.g.scalefactor;
         uint32_t vbase = 0, gd = 0;
         bool ok = true;
         for (int idx = blockIdx.x; ok && idx < nitems; idx += gridDim.x) {
             const Item it = item_of(a, idx);
             if (!it.valid) continue;
-            const unsigned skip = skip_mask(a, it, lane, eg);
+            const unsigned skip = skip_mask(a, it, lane, ep);
             const MemberDev &Mg = a.mem[it.k];
             const int mbx = Mg.bx, mby = Mg.by;
             const float sig2 = Mg.sigma2f, eps2 = Mg.eps2f;
             const bool fr = Mg.eps2 > 0.0;
             const int z = it.zb * TC_M + ch;
             const bool zok = z < a.nz;
-            const int x0 = it.sx * TC_X;
+            const int x0 = it.sx * TC_X + ex0;
             float ss = 0.0f, lg = 0.0f;
             int i = 0, ta, tb;
             while (ok && next_run(skip, it.nt, i, ta, tb)) {
@@ -573,21 +595,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
                     if (ok && a.do_resid) ok = mbar_wait(&full_d[gd % NDS], (gd / NDS) & 1, abort_flag, err);
                     if (!(ok = __all_sync(0xffffffffu, ok))) break;
                     tc_fence_after();
-                    float acc[TC_X];
+                    float acc[EPC];
                     const uint32_t col = (v % TC_RING) * TC_X;
-                    tmem_ld16(tl + col, acc);
-                    tmem_zero16(tl + col);
+                    tmem_ld8(tl + col, acc);
+                    tmem_zero8(tl + col);
                     tmem_wait_st();
                     tc_fence_before();
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&freeb[v % TC_RING]);
-                    const float *D = (const float *)(dst_ + (gd % NDS) * DBOX_BYTES) + ch;
+                    const float *D = (const float *)(dst_ + (gd % NDS) * DBOX_BYTES) + ex0 * TC_M + ch;
                     if (zok && !a.smoothed && a.do_resid && a.do_conv == 1 && !fr) {
                         // the likelihood's case: threshold, scale and the sum of squares only
-                        const int nxv = min(TC_X, mbx - x0);
+                        const int nxv = min(EPC, mbx - x0);
                         float s2 = 0.0f;
 #pragma unroll
-                        for (int x = 0; x < TC_X; x++) {
+                        for (int x = 0; x < EPC; x++) {
                             float m = acc[x];
                             m = m < 1.0e-12f ? 0.0f : m * scale;
                             const float d = D[x * TC_M];
@@ -597,7 +619,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
                         ss += s2;
                     } else if (zok) {
 #pragma unroll
-                        for (int x = 0; x < TC_X; x++) {
+                        for (int x = 0; x < EPC; x++) {
                             const int xx = x0 + x;
                             if (xx >= mbx) continue;
                             float m = acc[x];
@@ -628,7 +650,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
                     }
                     if (((y & (TC_X - 1)) == TC_X - 1) || oy == nout - 1) {
                         // the tile's sums of this warp's 32 channels, float64 in a fixed order (one partial pair
-                        // per tile, channel block and channel group: the reduction adds them in index order)
+                        // per tile, channel block and epilogue warp: the reduction adds them in index order)
                         double ds = (double)ss, dl = (double)lg;
 #pragma unroll
                         for (int o = 16; o > 0; o >>= 1) {
@@ -637,8 +659,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
                         }
                         if (lane == 0 && a.do_resid) {
                             double *p = a.partial + 2 * ((size_t)it.k * a.npart +
-                                                         ((size_t)((y >> 4) * it.ntx + it.sx) * a.nzb + it.zb) * 4 +
-                                                         eg);
+                                                         ((size_t)((y >> 4) * it.ntx + it.sx) * a.nzb + it.zb) * EPW +
+                                                         ep);
                             p[0] = ds;
                             p[1] = dl;
                         }
@@ -811,7 +833,7 @@ int conv_tc_npart(const MemberDev *mem_host, int nb, int nz) {
     int maxt = 0;
     for (int k = 0; k < nb; k++)
         maxt = max(maxt, ((mem_host[k].bx + TC_X - 1) / TC_X) * ((mem_host[k].by + TC_X - 1) / TC_X));
-    return maxt * ((nz + TC_M - 1) / TC_M) * 4;
+    return maxt * ((nz + TC_M - 1) / TC_M) * EPW;
 }
 
 // the convolution + residual of a batch on the tensor cores (partial sums as launch_conv_resid, npart =

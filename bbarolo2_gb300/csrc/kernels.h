@@ -151,7 +151,7 @@ void conv_tc_image(int variant, const double *kern, int ky, int kx, std::vector<
 // (the cube's deff, ny x nx x nz)
 bool conv_tc_maps(const MemberDev *mem_host, int nb, const float *model, long long mstride, int nz, int nx, int ny,
                   std::vector<CUtensorMap> &maps);
-// partial pairs per member (16 x 16 pixel tiles x blocks of 128 channels x 4 channel groups); zeroed by the caller
+// partial pairs per member (16 x 16 pixel tiles x blocks of 128 channels x 8 epilogue warps); zeroed by the caller
 int conv_tc_npart(const MemberDev *mem_host, int nb, int nz);
 void launch_conv_tc(cudaStream_t s, int variant, const GridDev &g, const MemberDev *mem, const MemberDev *mem_host,
                     int nb, const CUtensorMap *maps, const void *bimg, long long mstride, int nz, int ky, int kx,
