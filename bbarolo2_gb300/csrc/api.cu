@@ -14,6 +14,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <array>
 #include <string>
 #include <vector>
 
@@ -211,7 +212,11 @@ struct bbgpu_ctx {
                                   // map, at most 128 samples per cloud)
     // the beam convolution of the batch models: 0 float32 FMA (k_conv_resid), 1 bf16x3 or 2 tf32x3 on the tensor
     // cores (k_conv_tc; the float32 kernel where a batch does not qualify)
-    int conv_variant = 0;
+    int conv_variant = -1;                // -1: the autotuner's choice (below)
+    // the autotuner: per kernel shape and channels (ky, kx, nz), the variant it chose, timed on the first batch
+    // (float32 and tf32x3, the variants within 1e-5 per voxel of the float64 convolution), and its timings (ms)
+    std::vector<std::array<int, 4>> tuned;
+    float tune_ms[3] = {-1.f, -1.f, -1.f};
     std::vector<double> h_kernel;         // the beam kernel (ky, kx) float64
     void *d_bimg = nullptr;               // its B operand image for conv_variant
     size_t d_bimg_cap = 0;
@@ -579,11 +584,20 @@ extern "C" int bbgpu_set_option(bbgpu_ctx *ctx, int opt, int value) {
             ctx->an_dirty = true;
             break;
         case 4:
-            if (value < 0 || value > 2) return fail(ctx, BBGPU_ERR_ARG, "option 4: convolution variant 0, 1 or 2");
+            if (value < -1 || value > 2)
+                return fail(ctx, BBGPU_ERR_ARG, "option 4: convolution variant -1 (autotuned), 0, 1 or 2");
             ctx->conv_variant = value;
             break;
         default: return fail(ctx, BBGPU_ERR_ARG, "unknown option %d", opt);
     }
+    return BBGPU_OK;
+}
+
+extern "C" int bbgpu_conv_variant(const bbgpu_ctx *ctx, int *used, float *tune_ms) {
+    if (!ctx) return BBGPU_ERR_ARG;
+    if (used) *used = ctx->conv_used;
+    if (tune_ms)
+        for (int i = 0; i < 3; i++) tune_ms[i] = ctx->tune_ms[i];
     return BBGPU_OK;
 }
 
@@ -716,6 +730,7 @@ extern "C" int bbgpu_set_kernel(bbgpu_ctx *ctx, const double *kernel, int ky, in
     ctx->kxw = kxw;
     ctx->h_kernel.assign(kernel, kernel + (size_t)ky * kx);
     ctx->bimg_variant = 0;
+    ctx->tuned.clear();
     ctx->kernel_set = true;
     return BBGPU_OK;
 }
@@ -1291,12 +1306,76 @@ static int mc_lists(bbgpu_ctx *ctx, cudaStream_t s, bool tm) {
 
 // The beam convolution and residual of the batch's models: on the tensor cores (ctx->conv_variant 1 or 2) when the
 // kernel, the channels and the tile table qualify, else the float32 kernel. Sets npart_used and conv_used.
+static bool conv_tc_ok(const bbgpu_ctx *ctx, int v, const TileSrc &ts) {
+    return v && conv_tc_supported(v, ctx->ky, ctx->kx, ctx->g.nz) && (ctx->mstride % 4) == 0 &&
+           (!ts.tsrc || ts.shx >= 3) && !ts.kout;
+}
+
+static int conv_run(bbgpu_ctx *ctx, cudaStream_t s, int v, bool conv, bool do_resid, TileSrc ts);
+
+// The variant of the batch convolution: the option's, or (option -1) the autotuner's for this kernel and these
+// channels. The autotuner runs the batch's convolution with each candidate (float32; tf32x3 where the kernel and the
+// channels qualify) on the batch in hand, twice each, times the second run with events, and keeps the faster for the
+// context's lifetime: every later batch with the same kernel shape and channels gets the same arithmetic.
+static int conv_variant_of(bbgpu_ctx *ctx, cudaStream_t s, bool conv, bool do_resid, TileSrc ts, int &v) {
+    v = ctx->conv_variant;
+    if (v >= 0 || !conv) {
+        v = v < 0 ? 0 : v;
+        return 0;
+    }
+    for (auto &t : ctx->tuned)
+        if (t[0] == ctx->ky && t[1] == ctx->kx && t[2] == ctx->g.nz) {
+            v = t[3];
+            return 0;
+        }
+    int best = 0;
+    float bms = 1e30f;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    int rc = 0;
+    for (int cand : {0, 2}) {
+        if (cand && !conv_tc_ok(ctx, cand, ts)) continue;
+        float ms = 0.f;
+        for (int rep = 0; rep < 2 && !rc; rep++) {
+            cudaEventRecord(e0, s);
+            rc = conv_run(ctx, s, cand, conv, do_resid, ts);
+            cudaEventRecord(e1, s);
+        }
+        if (rc) break;
+        if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+            rc = fail(ctx, BBGPU_ERR_CUDA, "convolution autotuner: event timing failed");
+            break;
+        }
+        ctx->tune_ms[cand] = ms;
+        if (ms < bms) {
+            bms = ms;
+            best = cand;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    ctx->tuned.push_back({ctx->ky, ctx->kx, ctx->g.nz, best});
+    v = best;
+    return 0;
+}
+
+// The beam convolution and residual of the batch's models with the variant of conv_variant_of. Sets npart_used
+// and conv_used.
 static int conv_batch(bbgpu_ctx *ctx, cudaStream_t s, bool conv, bool do_resid, TileSrc ts) {
+    int v = 0;
+    int rc = conv_variant_of(ctx, s, conv, do_resid, ts, v);
+    if (rc) return rc;
+    return conv_run(ctx, s, v, conv, do_resid, ts);
+}
+
+// the convolution with variant v: on the tensor cores (1 bf16x3, 2 tf32x3) when the kernel, the channels and the tile
+// table qualify, else the float32 kernel
+static int conv_run(bbgpu_ctx *ctx, cudaStream_t s, int v, bool conv, bool do_resid, TileSrc ts) {
     const GridDev &g = ctx->g;
     float *smoothed = ctx->keep_smoothed ? ctx->d_smooth : nullptr;
-    const int v = ctx->conv_variant;
-    const bool tc = conv && v && conv_tc_supported(v, ctx->ky, ctx->kx, g.nz) && (ctx->mstride % 4) == 0 &&
-                    (!ts.tsrc || ts.shx >= 3) && !ts.kout;
+    const bool tc = conv && conv_tc_ok(ctx, v, ts);
     if (!tc) {
         launch_conv_resid(s, g, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->d_model, ctx->mstride, g.nz,
                           ctx->d_taps, ctx->ky, ctx->kx, ctx->kxw, smoothed, conv ? 1 : 0, do_resid ? 1 : 0,

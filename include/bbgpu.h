@@ -157,8 +157,17 @@ int bbgpu_sync(bbgpu_ctx *ctx);
 /* Options: 1 keep the smoothed models of a batch (for bbgpu_eval_model), 2 time the kernels of each run,
  * 3 compute the members of a batch that differ from the first member in a few sub-rings (the steps of a
  * finite-difference gradient) as the first member's ring maps, profile and MC model plus the difference (default
- * 1; the results are the same bit for bit, 0 computes every member from all its samples and clouds). */
+ * 1; the results are the same bit for bit, 0 computes every member from all its samples and clouds);
+ * 4 the beam convolution of the batch models: 0 float32 FMA, 1 bf16x3 or 2 tf32x3 on the tensor cores (split
+ * products, FP32 accumulation), -1 (default) the faster of float32 and tf32x3, timed on the first batch of each
+ * kernel shape and channel count and kept for the context's lifetime. float32 and tf32x3 keep every smoothed
+ * voxel within 1e-5 of the float64 convolution; bf16x3 within about 2e-5 (its split), so it is never chosen
+ * automatically. The ring maps of the flux normalisation always use float32. */
 int bbgpu_set_option(bbgpu_ctx *ctx, int option, int value);
+
+/* The variant of the last batch convolution (0 float32, 1 bf16x3, 2 tf32x3) and the autotuner's timings of a batch
+ * convolution in ms per variant (-1: not timed). No counterpart in the reference (its convolution is scipy's FFT). */
+int bbgpu_conv_variant(const bbgpu_ctx *ctx, int *used, float *tune_ms);
 
 /* ---- without allocation ------------------------------------------------------------------------------- */
 /* bbgpu_sumsq_residuals / bbgpu_residuals_fracerr for callers that may not allocate device memory (their own

@@ -64,7 +64,7 @@ def test_conv_variants_per_voxel_vs_fp64(gpu_lib, oracle_lib, wl, nb):
         res = {v: _smoothed(ctx, L, sr, nv, descs, boxes, v) for v in (0, 1, 2)}
     finally:
         ctx.set_option(_lib.OPT_KEEP_SMOOTHED, 0)
-        ctx.set_option(4, 0)
+        ctx.set_option(4, -1)
     worst = {}
     for k in range(nb):
         model = res[0][2][k]
@@ -113,7 +113,7 @@ def test_conv_variants_deterministic_and_shared_batch(gpu_lib):
             np.testing.assert_array_equal(out[v, 1], out[v, 0])
     finally:
         ctx.set_option(_lib.OPT_SHARE, 1)
-        ctx.set_option(4, 0)
+        ctx.set_option(4, -1)
     for v in (1, 2):
         np.testing.assert_allclose(out[v, 1], out[0, 1], rtol=1e-5)
 
@@ -122,4 +122,26 @@ def test_conv_variant_option_checked(gpu_lib):
     from bbarolo2_gb300 import _lib
     ctx = _lib.Context(0)
     assert ctx.L.bbgpu_set_option(ctx.h, 4, 3) == _lib.ERR_ARG
+    assert ctx.L.bbgpu_set_option(ctx.h, 4, -2) == _lib.ERR_ARG
     assert ctx.L.bbgpu_set_option(ctx.h, 4, 2) == _lib.OK
+    assert ctx.L.bbgpu_set_option(ctx.h, 4, -1) == _lib.OK
+
+
+def test_conv_autotuner_picks_a_variant_within_the_bound(gpu_lib):
+    """With the default option the first batch times float32 and tf32x3 and keeps the faster (never bf16x3, whose
+    split is above 1e-5 per voxel); later batches of the same kernel and channels use it and give the same sums."""
+    from bbarolo2_gb300 import _lib
+    dm, L, rings, rows = _setup("global160", 3)
+    ctx = dm.ctx
+    sr, nv, descs, boxes = L.prepare(rows, rings, seed=1)
+    a, _ = L.run(sr, nv, descs)
+    used, ms = ctx.conv_variant()
+    assert used in (_lib.CONV_F32, _lib.CONV_TF32X3), used
+    assert set(ms) == {"f32", "tf32x3"} and all(v > 0 for v in ms.values()), ms
+    b, _ = L.run(sr, nv, descs)
+    assert ctx.conv_variant()[0] == used
+    np.testing.assert_array_equal(a, b)
+    ctx.set_option(4, 0)
+    c, _ = L.run(sr, nv, descs)
+    ctx.set_option(4, -1)
+    np.testing.assert_allclose(a, c, rtol=1e-5)
