@@ -237,6 +237,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-analytic", action="store_true", help="skip the ANALYTIC GALMOD leg")
     ap.add_argument("--no-central", action="store_true", help="skip the 321-point central-difference batch")
+    ap.add_argument("--no-variants", action="store_true",
+                    help="skip the per-variant convolution times and errors")
     ap.add_argument("--no-random", action="store_true",
                     help="skip the batch of independent points and the gradient batch without shared ring maps")
     args = ap.parse_args()
@@ -325,11 +327,22 @@ def main():
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
             "traffic": measured_traffic(dom, B, members[dom]), "kernel": dom, "peak_source": src,
             "algorithmic_bytes": nbytes, "members": members[dom]}
+    used, tune = ctx.conv_variant()
     if dom == "conv_resid":
-        roof["f32_tflops"] = alg["conv_resid"][1] / (kt[dom] * 1e-3) / 1e12
+        # the convolution's useful arithmetic (2 x taps flop a voxel), and on the tensor cores its fraction of the
+        # dense tensor peak (bf16 measured; tf32 runs at half that rate)
+        useful = alg["conv_resid"][1] / (kt[dom] * 1e-3) / 1e12
+        roof["conv_variant"] = _lib.CONV_NAMES[used]
+        roof["useful_tflops"] = useful
+        if used:
+            tpk = bf16 if used == _lib.CONV_BF16X3 else bf16 / 2.
+            roof["tensor"] = {"achieved_useful_tflops": useful, "peak_tflops": tpk, "frac": useful / tpk,
+                              "peak": "bf16 dense (measured)" if used == 1 else "tf32 dense (half the measured bf16)"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 (f64 reduction; bit-exact int cloud indices)", "data": "synthetic",
+            "vs_baseline": None,
+            "dtype": f"f32 models, {_lib.CONV_NAMES[used]} beam convolution, f64 reductions; bit-exact int cloud indices",
+            "data": "synthetic",
             "config": {"workload": "global160: GLOBAL 3DFIT 160x160x128, 40 rings, MC GALMOD, 13x9 beam, batch of "
                                    f"{B} (base + 160 parameter steps)", "batch": B, "galmodtype": "MC",
                        "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (per-batch models 2 GB)",
@@ -343,7 +356,10 @@ def main():
                                           "computes every member in full)"}},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "kernel_ms": kt, "roofline": roof, "clocks": clocks,
+            "conv": {"variant": _lib.CONV_NAMES[used], "autotune_ms": tune},
             "logL_sample": [float(out[0]), float(out[1])]}
+    if not args.no_variants:
+        line["conv"]["variants"] = conv_variants_leg(ctx, L, rows, rings, sr, nv, descs)
     if not args.no_analytic:
         line["analytic"] = analytic_leg(ctx, L, rows, rings, sr, nv, descs, args, dist, world)
     if B == 161 and not args.no_central:
@@ -361,6 +377,55 @@ def main():
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def conv_variants_leg(ctx, L, rows, rings, sr, nv, descs):
+    """Each variant of the batch convolution (float32, bf16x3 and tf32x3 on the tensor cores): its device time on the
+    bench batch, and the largest relative error of a smoothed voxel (above 1e-6 of the peak) of two members against
+    the float64 FFT convolution of the same model (scipy, the reference's algorithm in float64)."""
+    from scipy.signal import fftconvolve
+    from bbarolo2_gb300 import _lib
+    dm = L.model
+    B = rows.shape[0]
+    ms = L._maps_sr                      # (the map tables of the whole batch: prepare() below replaces them)
+    assert ms.shape[0] == B
+    res = {}
+    try:
+        for v in (_lib.CONV_F32, _lib.CONV_BF16X3, _lib.CONV_TF32X3):
+            ctx.set_option(_lib.OPT_CONV, v)
+            ctx.check(ctx.L.bbgpu_eval_upload(ctx.h, _lib.MC, B, sr.shape[2], _lib.ptr(sr), _lib.ptr(nv),
+                                              _lib.ptr(descs)))
+            ctx.check(ctx.L.bbgpu_eval_upload_profile(ctx.h, ms.shape[2], _lib.ptr(ms), _lib.ptr(L._prof["widx"]),
+                                                      _lib.ptr(L._prof["wval"])))
+            ctx.set_option(_lib.OPT_TIMING, 1)
+            t = []
+            for _ in range(3):
+                ctx.check(ctx.L.bbgpu_eval_run(ctx.h))
+                t.append(ctx.run_times()["conv_resid"])
+            ctx.set_option(_lib.OPT_TIMING, 0)
+            ctx.set_option(_lib.OPT_KEEP_SMOOTHED, 1)
+            s2, n2, d2, b2 = L.prepare(rows[:2], rings, seed=1)
+            L.run(s2, n2, d2)
+            worst = 0.0
+            for k, (blo, bhi) in enumerate(b2):
+                by, bx, nz = bhi[1] - blo[1], bhi[0] - blo[0], L.shape[0]
+                sm = np.zeros((by, bx, nz), np.float32)
+                mo = np.zeros((by, bx, nz), np.float32)
+                ctx.check(ctx.L.bbgpu_eval_model(ctx.h, k, 1, _lib.ptr(sm), by, bx, nz))
+                ctx.check(ctx.L.bbgpu_eval_model(ctx.h, k, 0, _lib.ptr(mo), by, bx, nz))
+                ref = fftconvolve(mo.astype(np.float64).transpose(2, 0, 1), dm.cfield[None], mode="same",
+                                  axes=(1, 2)).transpose(1, 2, 0)
+                ref[ref < 1e-12] = 0.
+                ref *= dm.scalefactor
+                big = ref > 1e-6 * ref.max()
+                worst = max(worst, float((np.abs(sm[big] - ref[big]) / ref[big]).max()))
+            ctx.set_option(_lib.OPT_KEEP_SMOOTHED, 0)
+            res[_lib.CONV_NAMES[v]] = {"conv_ms": float(np.median(t)), "max_rel_err_vs_fp64": worst}
+    finally:
+        ctx.set_option(_lib.OPT_KEEP_SMOOTHED, 0)
+        ctx.set_option(_lib.OPT_CONV, _lib.CONV_AUTO)
+        L._maps_sr = ms                  # (the whole batch's tables, which the next legs upload)
+    return res
 
 
 def random_rows(rings, batch, seed=2):
