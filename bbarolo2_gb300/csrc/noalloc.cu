@@ -136,7 +136,7 @@ extern "C" int bbgpu_sumsq_residuals_noalloc(const double *model, const float *d
                                              double sigma2, double eps2, double *out2, void *stream) {
     if (!model || !data || !out2 || nz < 0 || ny < 0 || nx < 0) return BBGPU_ERR_ARG;
     if (maskmode < 0 || maskmode > 2 || (maskmode != 0 && !mask)) return BBGPU_ERR_ARG;
-    if (eps2 > 0 && !(sigma2 > 0)) return BBGPU_ERR_ARG;
+    if (!(eps2 >= 0) || (eps2 > 0 && !(sigma2 > 0))) return BBGPU_ERR_ARG;   // (a NaN eps2 fails the first test)
     const long long n = (long long)nz * ny * nx;
     const long long nblocks = (n + NOALLOC_VOXELS_PER_BLOCK - 1) / NOALLOC_VOXELS_PER_BLOCK;
     if (nblocks > NOALLOC_MAX_BLOCKS) return BBGPU_ERR_ARG;   // more voxels than the scratch holds sums for
@@ -144,9 +144,14 @@ extern "C" int bbgpu_sumsq_residuals_noalloc(const double *model, const float *d
     int rc = scratch_address(&scratch);
     if (rc != BBGPU_OK) return rc;
     cudaStream_t s = (cudaStream_t)stream;
-    if (nblocks > 0)
+    // an error left by earlier CUDA work of the caller is not this call's: report it without launching, and leave
+    // it for the caller to read
+    if (cudaPeekAtLastError() != cudaSuccess) return BBGPU_ERR_CUDA;
+    if (nblocks > 0) {
         k_sumsq_blocks<<<(unsigned)nblocks, NOALLOC_THREADS, 0, s>>>(model, data, mask, maskmode, region, n,
                                                                      (long long)ny * nx, sigma2, eps2, scratch);
+        if (cudaGetLastError() != cudaSuccess) return BBGPU_ERR_CUDA;
+    }
     k_sumsq_final<<<1, NOALLOC_THREADS, 0, s>>>(scratch, (int)nblocks, out2);
     if (cudaGetLastError() != cudaSuccess) return BBGPU_ERR_CUDA;
     return BBGPU_OK;

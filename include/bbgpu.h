@@ -177,8 +177,10 @@ int bbgpu_conv_variant(const bbgpu_ctx *ctx, int *used, float *tune_ms);
  * DEVICE pointers of the current device; eps2 = 0 gives the plain sum of squares. Kernels run on stream
  * (cudaStream_t, NULL: the default stream) and out2 is written there. The partial sums use a 64 KB scratch
  * array held by every GPU that loads the library; at most 16,777,216 voxels (4096 blocks of 4096) per call,
- * BBGPU_ERR_ARG beyond. The first call on a device looks the array's address up (cudaGetSymbolAddress): make
- * it before any stream capture. Calls whose kernels overlap on the GPU share the array and race. */
+ * BBGPU_ERR_ARG beyond (and for a negative or NaN eps2). The first call on a device looks the array's address up
+ * (cudaGetSymbolAddress) and keeps it: make it before any stream capture, and do not reset the device
+ * (cudaDeviceReset) between calls. A CUDA error pending from earlier work makes the call return BBGPU_ERR_CUDA
+ * without launching. Calls whose kernels overlap on the GPU share the array and race. */
 int bbgpu_sumsq_residuals_noalloc(const double *model, const float *data, const uint8_t *mask, int maskmode,
                                   const uint8_t *region, int nz, int ny, int nx, double sigma2, double eps2,
                                   double *out2, void *stream);

@@ -16,7 +16,12 @@ import os
 import sys
 import types
 
-REF_ROOT = os.environ.get("BBAROLO_REF", "/root/reference")
+def ref_root():
+    """The reference source tree: the directory named by the BBAROLO_REF environment variable (required)."""
+    root = os.environ.get("BBAROLO_REF")
+    if not root or not os.path.isdir(os.path.join(root, "bbarolo")):
+        raise RuntimeError("set BBAROLO_REF to the root of the reference source tree (the directory holding bbarolo/)")
+    return root
 
 
 def _stub_numba():
@@ -41,7 +46,7 @@ def _stub_numba():
 def load():
     """Returns a namespace with the reference modules (_rng, galmod, smooth, galfit, likelihood)."""
     _stub_numba()
-    pkg = os.path.join(REF_ROOT, "bbarolo")
+    pkg = os.path.join(ref_root(), "bbarolo")
     if "bbarolo" not in sys.modules:
         m = types.ModuleType("bbarolo")
         m.__path__ = [pkg]

@@ -1,6 +1,6 @@
 """Generates the golden fixtures of the model path by running the REFERENCE's own kernels.
 
-Run in a container that has the reference source tree (``BBAROLO_REF``, default ``/root/reference``):
+Run in a container that has the reference source tree, named by the ``BBAROLO_REF`` environment variable:
 
     python tests/golden/make_golden.py
 

@@ -75,3 +75,8 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(gpu_lib):
     rc = L.bbgpu_sumsq_residuals_noalloc(a.data_ptr(), b.data_ptr(), None, 0, None, 4097, 64, 64, 1.0, 0.0,
                                          out.data_ptr(), None)
     assert rc == _lib.ERR_ARG
+    # a negative or NaN fractional error is refused, as the allocating entry point refuses it
+    for eps2 in (-0.01, float("nan")):
+        rc = L.bbgpu_sumsq_residuals_noalloc(a.data_ptr(), b.data_ptr(), None, 0, None, 2, 2, 2, 1.0, eps2,
+                                             out.data_ptr(), None)
+        assert rc == _lib.ERR_ARG, eps2
