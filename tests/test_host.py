@@ -187,11 +187,12 @@ def test_batch_boxes_match_model_box():
 
 
 def test_count_ring_pixels_matches_reference_rule():
-    """The annulus pixel count of a ring (``_count_ring_pixels``) on a box crossing the cube edge."""
-    from bbarolo2_gb300.galfit import _count_ring_pixels
+    """The annulus pixel count of a ring (``_count_ring_pixels`` of bbarolo/galfit.py:199-216) on a box crossing
+    the cube edge."""
+    from bbarolo2_gb300.classic import ring_pixels
     m = np.zeros((30, 40), np.int32)
     m[5:20, 10:35] = 3
-    nt, ni = _count_ring_pixels(m, 2, 3, 39, 32, 20.5, 12.0, 30., 50., 4., 9.)
+    nt, ni = ring_pixels(m, (2, 3), (39, 32), 20.5, 12.0, 30., 50., 4., 9.)
     # the same count written out pixel by pixel
     import math
     F = math.pi / 180.
@@ -280,3 +281,35 @@ def test_oracle_host_setup_equals_package(wl):
     np.testing.assert_array_equal(nv, no)
     np.testing.assert_array_equal(BeamKernel.from_cube(cube).kernel, host.beam_kernel(cube))
     assert galmod.outer_edge(rings, "CENTRED") == host.outer_edge_centred(rings)
+
+
+def test_classic_simplex_on_a_quadratic():
+    """The simplex coroutine of the CLASSIC fit minimises a quadratic bowl (no bounds: each point evaluated as
+    given), converging within its tolerance and budget."""
+    from bbarolo2_gb300.classic import simplex
+    co = simplex([3.0, -2.0], [1.0, 1.0], 1e-10, 2000)
+    pt = next(co)
+    n = 0
+    try:
+        while True:
+            f = (pt[0] - 1.0) ** 2 + 2.0 * (pt[1] + 0.5) ** 2 + 3.0
+            n += 1
+            pt = co.send((f, np.array(pt)))
+    except StopIteration as e:
+        ok, fmin, xmin = e.value
+    assert ok and abs(fmin - 3.0) < 1e-8 and np.allclose(xmin, [1.0, -0.5], atol=1e-4), (ok, fmin, xmin, n)
+
+
+def test_classic_bounds_rules():
+    """Trial values outside the bounds: VROT and VDISP redrawn inside (one deviate each), INC and PA clipped within
+    their deltas of the initial value, the others reset to it."""
+    from bbarolo2_gb300.classic import Limits, into_bounds
+    draws = iter([0.25, 0.5])
+    vrot = Limits(0., 1000., "redraw", 50.)
+    assert into_bounds("vrot", 300., vrot, 120., lambda: next(draws)) == 170. - 0.25 * 50.
+    vd = Limits(1., 40., "redraw")
+    assert into_bounds("vdisp", 0.5, vd, 8., lambda: next(draws)) == 1. + 0.5 * 8.
+    assert into_bounds("inc", 80., Limits(40., 70., "clip", 5.), 60., None) == 65.
+    assert into_bounds("z0", -1., Limits(0., 1000., "reset"), 3., None) == 3.
+    assert into_bounds("dens", -1., Limits(0., np.inf, "reset"), 0.7, None) == 0.7
+    assert into_bounds("vrot", 130., vrot, 120., None) == 130.
