@@ -14,7 +14,7 @@ LIBPATH = os.path.join(HERE, "_build", "libbbgpu.so")
 
 OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_KERNEL = 0, -1, -2, -3, -4, -5
 MC, ANALYTIC = 0, 1
-OPT_KEEP_SMOOTHED, OPT_TIMING, OPT_SHARE, OPT_CONV = 1, 2, 3, 4
+OPT_KEEP_SMOOTHED, OPT_TIMING, OPT_SHARE, OPT_CONV, OPT_GRAPHS = 1, 2, 3, 4, 5
 CONV_AUTO, CONV_F32, CONV_BF16X3, CONV_TF32X3 = -1, 0, 1, 2
 CONV_NAMES = {0: "f32", 1: "bf16x3", 2: "tf32x3"}
 
@@ -26,7 +26,7 @@ SYMBOLS = ("bbgpu_ctx_create", "bbgpu_ctx_destroy", "bbgpu_last_error", "bbgpu_v
            "bbgpu_eval_batch", "bbgpu_eval_model", "bbgpu_sync", "bbgpu_set_option", "bbgpu_launch_count",
            "bbgpu_last_run_times", "bbgpu_kernel_name", "bbgpu_transfer_bytes", "bbgpu_shared_members",
            "bbgpu_sumsq_residuals_noalloc", "bbgpu_set_profile", "bbgpu_eval_upload_profile", "bbgpu_eval_profile", "bbgpu_solve_profile",
-           "bbgpu_subrings_rows", "bbgpu_conv_variant")
+           "bbgpu_subrings_rows", "bbgpu_conv_variant", "bbgpu_graph_stats")
 
 
 class Grid(C.Structure):
@@ -101,6 +101,7 @@ def load(path=None):
         "bbgpu_transfer_bytes": (i, [vp, vp, vp]),
         "bbgpu_shared_members": (i, [vp, vp, vp, vp, vp]),
         "bbgpu_conv_variant": (i, [vp, vp, vp]),
+        "bbgpu_graph_stats": (i, [vp, vp, vp]),
         "bbgpu_sumsq_residuals_noalloc": (i, [vp, vp, vp, i, vp, i, i, i, d, d, vp, vp]),
         "bbgpu_set_profile": (i, [vp, i, i, i, i, i, vp, vp, vp, vp, d, d, d, d]),
         "bbgpu_eval_upload_profile": (i, [vp, i, vp, vp, vp]),
@@ -171,6 +172,12 @@ class Context:
 
     def set_option(self, opt, value):
         self.check(self.L.bbgpu_set_option(self.h, int(opt), int(value)))
+
+    def graph_stats(self):
+        """(graph replays so far, kernels per replay of the current batch's graph, 0 without one)."""
+        a, b = np.zeros(1, np.int64), np.zeros(1, np.int64)
+        self.check(self.L.bbgpu_graph_stats(self.h, ptr(a), ptr(b)))
+        return int(a[0]), int(b[0])
 
     def conv_variant(self):
         """(variant of the last batch convolution, {variant: ms} of the autotuner's timings)."""

@@ -226,6 +226,11 @@ struct bbgpu_ctx {
     std::vector<CUtensorMap> h_tmaps;
     std::vector<long long> tmaps_key;     // (model, mstride, nz, boxes) of the descriptors on the device
     int npart_used = 0;                   // partial pairs per member of the last convolution
+    // CUDA graph of a batch run (option 5): captured on the second run of an unchanged batch, replayed after.
+    // gen counts the changes of what a run reads (uploads, options, reallocations, stand-alone calls).
+    bool use_graphs = true;
+    long long gen = 1, gen_ran = 0, graph_gen = 0, graph_fail_gen = 0, graph_launches = 0, graph_replays = 0;
+    cudaGraphExec_t gexec = nullptr;
     int conv_used = 0;                    // variant of the last batch convolution
     long long launches = 0;
     long long h2d = 0, d2h = 0;
@@ -260,6 +265,7 @@ static int fail(bbgpu_ctx *c, int code, const char *fmt, ...) {
 template <class T>
 static int dgrow(bbgpu_ctx *ctx, T **p, size_t *cap, size_t n) {
     if (n <= *cap && *p) return 0;
+    ctx->gen++;                       // (a captured batch run holds the old address)
     if (*p) cudaFree(*p);
     *p = nullptr;
     *cap = 0;
@@ -499,6 +505,7 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
     cudaFree(ctx->d_tcount); cudaFree(ctx->d_toff); cudaFree(ctx->d_tcur); cudaFree(ctx->d_model); cudaFree(ctx->d_scan);
     cudaFree(ctx->d_smooth); cudaFree(ctx->d_model64); cudaFree(ctx->d_partial); cudaFree(ctx->d_out2);
     cudaFree(ctx->d_bimg); cudaFree(ctx->d_tmaps);
+    if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
     cudaFree(ctx->d_err);
     for (void *q : {(void *)ctx->d_ppix, (void *)ctx->d_lc, (void *)ctx->d_ord, (void *)ctx->d_p0, (void *)ctx->d_ent,
                     (void *)ctx->d_pw, (void *)ctx->d_pwy, (void *)ctx->d_lv, (void *)ctx->d_near, (void *)ctx->d_psub,
@@ -575,6 +582,7 @@ extern "C" int bbgpu_transfer_bytes(const bbgpu_ctx *ctx, int64_t *h2d, int64_t 
 
 extern "C" int bbgpu_set_option(bbgpu_ctx *ctx, int opt, int value) {
     if (!ctx) return BBGPU_ERR_ARG;
+    ctx->gen++;
     switch (opt) {
         case 1: ctx->keep_smoothed = value != 0; break;
         case 2: ctx->timing = value != 0; break;
@@ -583,6 +591,7 @@ extern "C" int bbgpu_set_option(bbgpu_ctx *ctx, int opt, int value) {
             ctx->mc_dirty = true;
             ctx->an_dirty = true;
             break;
+        case 5: ctx->use_graphs = value != 0; break;
         case 4:
             if (value < -1 || value > 2)
                 return fail(ctx, BBGPU_ERR_ARG, "option 4: convolution variant -1 (autotuned), 0, 1 or 2");
@@ -604,6 +613,7 @@ extern "C" int bbgpu_conv_variant(const bbgpu_ctx *ctx, int *used, float *tune_m
 // ------------------------------------------------------------------------------------------- set-up
 extern "C" int bbgpu_set_grid(bbgpu_ctx *ctx, const bbgpu_grid *gr, const double *cd2i, const double *lfreq0,
                               const double *relint, const double *vedges) {
+    if (ctx) ctx->gen++;
     if (!ctx || !gr || !cd2i || !lfreq0 || !relint) return fail(ctx, BBGPU_ERR_ARG, "set_grid: null argument");
     if (gr->nx <= 0 || gr->ny <= 0 || gr->nz <= 0) return fail(ctx, BBGPU_ERR_ARG, "set_grid: empty cube");
     if (gr->nlines < 1 || gr->nlines > BBGPU_MAXL)
@@ -712,6 +722,7 @@ extern "C" int bbgpu_set_grid(bbgpu_ctx *ctx, const bbgpu_grid *gr, const double
 }
 
 extern "C" int bbgpu_set_kernel(bbgpu_ctx *ctx, const double *kernel, int ky, int kx) {
+    if (ctx) ctx->gen++;
     if (!ctx) return BBGPU_ERR_ARG;
     if (!kernel || ky < 1 || kx < 1 || !(ky & 1) || !(kx & 1) || ky > BBGPU_MAXK || kx > BBGPU_MAXK)
         return fail(ctx, BBGPU_ERR_ARG, "set_kernel: kernel sides must be odd, 1 to %d", BBGPU_MAXK);
@@ -736,6 +747,7 @@ extern "C" int bbgpu_set_kernel(bbgpu_ctx *ctx, const double *kernel, int ky, in
 }
 
 extern "C" int bbgpu_set_cube(bbgpu_ctx *ctx, const float *data, const uint8_t *mask, const uint8_t *region) {
+    if (ctx) ctx->gen++;
     if (!ctx) return BBGPU_ERR_ARG;
     if (!ctx->grid_set) return fail(ctx, BBGPU_ERR_STATE, "set_cube before set_grid");
     if (!data) return fail(ctx, BBGPU_ERR_ARG, "set_cube: null data");
@@ -1571,16 +1583,75 @@ static int check_err(bbgpu_ctx *ctx) {
 
 extern "C" int bbgpu_eval_upload(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const double *sr,
                                  const int64_t *nv, const bbgpu_eval_desc *descs) {
+    if (ctx) ctx->gen++;
     if (!ctx) return BBGPU_ERR_ARG;
     CK(cudaSetDevice(ctx->device));
     ctx->want64 = false;
     return batch_prepare(ctx, galmodtype, nb, nsub, sr, nv, descs, true);
 }
 
+// A batch run through a CUDA graph (option 5, on by default): the run after one that completed with the same
+// state (nothing uploaded, set or reallocated since: its host-side set-up is done) is captured, both streams with
+// their fork and join, and replayed by every later run of that state; the stage timers run without a graph. A
+// capture that fails leaves the run to the ordinary path.
+static int graph_run(bbgpu_ctx *ctx) {
+    if (ctx->gexec && ctx->graph_gen == ctx->gen) {
+        CK(cudaGraphLaunch(ctx->gexec, ctx->stream));
+        ctx->launches += ctx->graph_launches;
+        ctx->graph_replays++;
+        ctx->ran = true;
+        return 0;
+    }
+    if (ctx->gexec) {
+        cudaGraphExecDestroy(ctx->gexec);
+        ctx->gexec = nullptr;
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    const long long l0 = ctx->launches, g0 = ctx->gen;
+    if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    const int rc = batch_run(ctx, true);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+    const bool ok = !rc && e == cudaSuccess && graph && ctx->gen == g0 &&
+                    cudaGraphInstantiate(&ctx->gexec, graph, 0) == cudaSuccess;
+    if (graph) cudaGraphDestroy(graph);
+    if (!ok) {
+        cudaGetLastError();
+        if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+        ctx->gexec = nullptr;
+        ctx->launches = l0;
+        return -1;
+    }
+    ctx->graph_gen = ctx->gen;
+    ctx->graph_launches = ctx->launches - l0;
+    CK(cudaGraphLaunch(ctx->gexec, ctx->stream));
+    ctx->ran = true;
+    return 0;
+}
+
 extern "C" int bbgpu_eval_run(bbgpu_ctx *ctx) {
     if (!ctx) return BBGPU_ERR_ARG;
     CK(cudaSetDevice(ctx->device));
-    return batch_run(ctx, true);
+    if (ctx->use_graphs && !ctx->timing && ctx->uploaded && ctx->gen_ran == ctx->gen &&
+        ctx->graph_fail_gen != ctx->gen) {
+        const int rc = graph_run(ctx);
+        if (rc >= 0) return rc;
+        ctx->graph_fail_gen = ctx->gen;   // (the capture failed: this state runs without a graph)
+    }
+    const long long g0 = ctx->gen;
+    const int rc = batch_run(ctx, true);
+    if (!rc && ctx->gen == g0) ctx->gen_ran = g0;
+    return rc;
+}
+
+extern "C" int bbgpu_graph_stats(const bbgpu_ctx *ctx, int64_t *replays, int64_t *kernels) {
+    if (!ctx) return BBGPU_ERR_ARG;
+    if (replays) *replays = ctx->graph_replays;
+    if (kernels) *kernels = ctx->gexec && ctx->graph_gen == ctx->gen ? ctx->graph_launches : 0;
+    return BBGPU_OK;
 }
 
 extern "C" int bbgpu_eval_download(bbgpu_ctx *ctx, double *ss, double *lg) {
@@ -1600,6 +1671,7 @@ extern "C" int bbgpu_eval_download(bbgpu_ctx *ctx, double *ss, double *lg) {
 
 extern "C" int bbgpu_eval_batch(bbgpu_ctx *ctx, int galmodtype, int nb, int nsub, const double *sr, const int64_t *nv,
                                 const bbgpu_eval_desc *descs, double *ss, double *lg) {
+    if (ctx) ctx->gen++;
     int rc = bbgpu_eval_upload(ctx, galmodtype, nb, nsub, sr, nv, descs);
     if (rc) return rc;
     rc = bbgpu_eval_run(ctx);
@@ -1636,6 +1708,7 @@ extern "C" int bbgpu_eval_model(bbgpu_ctx *ctx, int k, int smoothed, float *out,
 // ------------------------------------------------------------------------------------------- reference kernels
 extern "C" int bbgpu_galmod_mc(bbgpu_ctx *ctx, double *out, const double *sr, int nsub, int ring_lo, int ring_hi,
                                uint64_t seed, const int64_t *nv, int blo0, int blo1, int bhi0, int bhi1) {
+    if (ctx) ctx->gen++;
     if (!ctx) return BBGPU_ERR_ARG;
     if (!out || !sr || !nv || ring_lo < 0 || ring_hi > nsub || ring_lo > ring_hi)
         return fail(ctx, BBGPU_ERR_ARG, "galmod_mc: invalid arguments");
@@ -1669,6 +1742,7 @@ extern "C" int bbgpu_galmod_mc(bbgpu_ctx *ctx, double *out, const double *sr, in
 
 extern "C" int bbgpu_convolve(bbgpu_ctx *ctx, const double *in, double *out, int nz, int ny, int nx, double scale,
                               int threshold) {
+    if (ctx) ctx->gen++;
     if (!ctx) return BBGPU_ERR_ARG;
     if (!in || !out || nz < 1 || ny < 1 || nx < 1) return fail(ctx, BBGPU_ERR_ARG, "convolve: invalid arguments");
     if (!ctx->kernel_set) return fail(ctx, BBGPU_ERR_STATE, "convolve before set_kernel");
@@ -1753,6 +1827,7 @@ static int sumsq_common(bbgpu_ctx *ctx, const double *model, const float *data, 
 
 extern "C" int bbgpu_sumsq_residuals(bbgpu_ctx *ctx, const double *model, const float *data, const uint8_t *mask,
                                      int maskmode, const uint8_t *region, int nz, int ny, int nx, double *out) {
+    if (ctx) ctx->gen++;
     double o2[2];
     int rc = sumsq_common(ctx, model, data, mask, maskmode, region, nz, ny, nx, 1.0, 0.0, o2);
     if (!rc && out) *out = o2[0];
@@ -1762,6 +1837,7 @@ extern "C" int bbgpu_sumsq_residuals(bbgpu_ctx *ctx, const double *model, const 
 extern "C" int bbgpu_residuals_fracerr(bbgpu_ctx *ctx, const double *model, const float *data, const uint8_t *mask,
                                        int maskmode, const uint8_t *region, int nz, int ny, int nx, double sigma2,
                                        double eps2, double *out2) {
+    if (ctx) ctx->gen++;
     if (ctx && !(sigma2 > 0)) return fail(ctx, BBGPU_ERR_ARG, "residuals_fracerr: sigma2 must be > 0");
     if (ctx && !(eps2 > 0)) return fail(ctx, BBGPU_ERR_ARG, "residuals_fracerr: eps2 must be > 0");
     return sumsq_common(ctx, model, data, mask, maskmode, region, nz, ny, nx, sigma2, eps2, out2);
@@ -1821,6 +1897,7 @@ static int an_upload(bbgpu_ctx *ctx, DevBufs &B, const std::vector<AnSub> &subs,
 
 extern "C" int bbgpu_galmod_analytic(bbgpu_ctx *ctx, double *out, const double *sr, int nsub, int ring_lo, int ring_hi,
                                      int nzq, int blo0, int blo1, int bhi0, int bhi1) {
+    if (ctx) ctx->gen++;
     if (!ctx) return BBGPU_ERR_ARG;
     if (!out || !sr || ring_lo < 0 || ring_hi > nsub || ring_lo > ring_hi || blo0 > bhi0 || blo1 > bhi1)
         return fail(ctx, BBGPU_ERR_ARG, "galmod_analytic: invalid arguments");
@@ -1877,6 +1954,7 @@ extern "C" int bbgpu_galmod_analytic(bbgpu_ctx *ctx, double *out, const double *
 extern "C" int bbgpu_ring_maps_analytic(bbgpu_ctx *ctx, double *out, int nr, const double *sr, int nsub,
                                         const int64_t *widx, const double *wval, int nzq, int blo0, int blo1, int bhi0,
                                         int bhi1) {
+    if (ctx) ctx->gen++;
     if (!ctx) return BBGPU_ERR_ARG;
     if (!out || !sr || !widx || !wval || nr < 0 || nsub < 0 || blo0 > bhi0 || blo1 > bhi1)
         return fail(ctx, BBGPU_ERR_ARG, "ring_maps_analytic: invalid arguments");
@@ -1921,6 +1999,7 @@ extern "C" int bbgpu_ring_maps_analytic(bbgpu_ctx *ctx, double *out, int nr, con
 
 extern "C" int bbgpu_conv_sparse(bbgpu_ctx *ctx, const double *model, double *out, int ny, int nx, int nz,
                                  const double *kernel, int ky, int kx, double scale) {
+    if (ctx) ctx->gen++;
     if (!ctx) return BBGPU_ERR_ARG;
     if (!model || !out || !kernel || ny < 0 || nx < 0 || nz < 0 || ky < 1 || kx < 1)
         return fail(ctx, BBGPU_ERR_ARG, "conv_sparse: invalid arguments");
@@ -1946,6 +2025,7 @@ extern "C" int bbgpu_norm(bbgpu_ctx *ctx, double *model, int bsy, int bsx, int n
                           double r1, double r2, double wpow, int side, int ftype, const double *chan_noise,
                           double data_noise, double bweight, int normtype, const double *pre, const int64_t *ilo,
                           const int64_t *ihi, int ky, const double *thr, int foot, double hmax, double *out) {
+    if (ctx) ctx->gen++;
     if (!ctx) return BBGPU_ERR_ARG;
     if (!model || !data || !mask || !chan_noise || !out || bsy < 0 || bsx < 0 || nz < 1 || blo0 < 0 || blo1 < 0 ||
         blo1 + bsy > dny || blo0 + bsx > dnx || (pre && (!ilo || !ihi || !thr || ky < 1)))
@@ -2081,6 +2161,7 @@ static int profile_consts(bbgpu_ctx *ctx, const double *radii, int n, double smo
 extern "C" int bbgpu_set_profile(bbgpu_ctx *ctx, int nr, int blo0, int blo1, int bhi0, int bhi1, const double *ymap,
                                  const double *rms, const uint8_t *ok, const double *radii, double smooth,
                                  double corr, double floor_, double mapscale) {
+    if (ctx) ctx->gen++;
     if (!ctx) return BBGPU_ERR_ARG;
     if (!ctx->grid_set) return fail(ctx, BBGPU_ERR_STATE, "set_profile before set_grid");
     const GridDev &g = ctx->g;
@@ -2157,6 +2238,7 @@ extern "C" int bbgpu_set_profile(bbgpu_ctx *ctx, int nr, int blo0, int blo1, int
 
 extern "C" int bbgpu_eval_upload_profile(bbgpu_ctx *ctx, int nsm, const double *sr_maps, const int64_t *widx,
                                          const double *wval) {
+    if (ctx) ctx->gen++;
     if (!ctx) return BBGPU_ERR_ARG;
     if (!ctx->prof_set) return fail(ctx, BBGPU_ERR_STATE, "eval_upload_profile before set_profile");
     if (!ctx->uploaded) return fail(ctx, BBGPU_ERR_STATE, "eval_upload_profile before eval_upload");
@@ -2395,6 +2477,7 @@ extern "C" int bbgpu_eval_profile(bbgpu_ctx *ctx, double *x, int *status) {
 
 extern "C" int bbgpu_solve_profile(bbgpu_ctx *ctx, const double *A, const double *b, int m, int n, const double *radii,
                                    double smooth, double corr, double floor_, double *x, int *status) {
+    if (ctx) ctx->gen++;
     if (!ctx) return BBGPU_ERR_ARG;
     if (!A || !b || !radii || !x || m < 1 || n < 1 || n > PROF_NMAX)
         return fail(ctx, BBGPU_ERR_ARG, "solve_profile: invalid arguments (1 to %d unknowns)", PROF_NMAX);

@@ -279,6 +279,7 @@ def main():
     ctx.check(ctx.L.bbgpu_sync(ctx.h))
     dt = time.perf_counter() - t0
     launches = ctx.launches - l0
+    graph_replays, graph_kernels = ctx.graph_stats()
     dt = max_over_ranks(dt, dist)
     if dist:
         dist.barrier()
@@ -357,6 +358,8 @@ def main():
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "kernel_ms": kt, "roofline": roof, "clocks": clocks,
             "conv": {"variant": _lib.CONV_NAMES[used], "autotune_ms": tune},
+            "graph": {"replays": graph_replays, "kernels_per_replay": graph_kernels,
+                      "note": "the timed batch runs replay one CUDA graph of the batch (two streams, fork and join)"},
             "logL_sample": [float(out[0]), float(out[1])]}
     if not args.no_variants:
         line["conv"]["variants"] = conv_variants_leg(ctx, L, rows, rings, sr, nv, descs)

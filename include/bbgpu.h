@@ -162,8 +162,15 @@ int bbgpu_sync(bbgpu_ctx *ctx);
  * products, FP32 accumulation), -1 (default) the faster of float32 and tf32x3, timed on the first batch of each
  * kernel shape and channel count and kept for the context's lifetime. float32 and tf32x3 keep every smoothed
  * voxel within 1e-5 of the float64 convolution; bf16x3 within about 2e-5 (its split), so it is never chosen
- * automatically. The ring maps of the flux normalisation always use float32. */
+ * automatically. The ring maps of the flux normalisation always use float32;
+ * 5 CUDA graphs (default 1): the second bbgpu_eval_run of an unchanged batch (nothing uploaded, set or
+ * reallocated since the first) is captured into a graph, both streams included, and later runs of that batch
+ * replay it; 0 launches every kernel each run. The stage timers (option 2) run without a graph. */
 int bbgpu_set_option(bbgpu_ctx *ctx, int option, int value);
+
+/* The graph of the current batch: replays so far in the context, kernels per replay (0: no graph for the current
+ * state). No counterpart in the reference. */
+int bbgpu_graph_stats(const bbgpu_ctx *ctx, int64_t *replays, int64_t *kernels);
 
 /* The variant of the last batch convolution (0 float32, 1 bf16x3, 2 tf32x3) and the autotuner's timings of a batch
  * convolution in ms per variant (-1: not timed). No counterpart in the reference (its convolution is scipy's FFT). */
