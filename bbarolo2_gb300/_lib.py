@@ -26,7 +26,9 @@ SYMBOLS = ("bbgpu_ctx_create", "bbgpu_ctx_destroy", "bbgpu_last_error", "bbgpu_v
            "bbgpu_eval_batch", "bbgpu_eval_model", "bbgpu_sync", "bbgpu_set_option", "bbgpu_launch_count",
            "bbgpu_last_run_times", "bbgpu_kernel_name", "bbgpu_transfer_bytes", "bbgpu_shared_members",
            "bbgpu_sumsq_residuals_noalloc", "bbgpu_set_profile", "bbgpu_eval_upload_profile", "bbgpu_eval_profile", "bbgpu_solve_profile",
-           "bbgpu_subrings_rows", "bbgpu_conv_variant", "bbgpu_graph_stats")
+           "bbgpu_subrings_rows", "bbgpu_conv_variant", "bbgpu_graph_stats", "bbgpu_mlp_create",
+           "bbgpu_mlp_destroy", "bbgpu_mlp_nparams", "bbgpu_mlp_get_params", "bbgpu_mlp_set_params",
+           "bbgpu_mlp_predict", "bbgpu_mlp_gradients", "bbgpu_mlp_train_step")
 
 
 class Grid(C.Structure):
@@ -102,6 +104,14 @@ def load(path=None):
         "bbgpu_shared_members": (i, [vp, vp, vp, vp, vp]),
         "bbgpu_conv_variant": (i, [vp, vp, vp]),
         "bbgpu_graph_stats": (i, [vp, vp, vp]),
+        "bbgpu_mlp_create": (i, [C.POINTER(vp), i, i, i, u64]),
+        "bbgpu_mlp_destroy": (i, [vp]),
+        "bbgpu_mlp_nparams": (C.c_longlong, [vp]),
+        "bbgpu_mlp_get_params": (i, [vp, vp]),
+        "bbgpu_mlp_set_params": (i, [vp, vp]),
+        "bbgpu_mlp_predict": (i, [vp, vp, i, vp]),
+        "bbgpu_mlp_gradients": (i, [vp, vp, vp, i, vp, vp]),
+        "bbgpu_mlp_train_step": (i, [vp, vp, vp, i, C.c_float, vp]),
         "bbgpu_sumsq_residuals_noalloc": (i, [vp, vp, vp, i, vp, i, i, i, d, d, vp, vp]),
         "bbgpu_set_profile": (i, [vp, i, i, i, i, i, vp, vp, vp, vp, d, d, d, d]),
         "bbgpu_eval_upload_profile": (i, [vp, i, vp, vp, vp]),

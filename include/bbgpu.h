@@ -176,6 +176,23 @@ int bbgpu_graph_stats(const bbgpu_ctx *ctx, int64_t *replays, int64_t *kernels);
  * convolution in ms per variant (-1: not timed). No counterpart in the reference (its convolution is scipy's FFT). */
 int bbgpu_conv_variant(const bbgpu_ctx *ctx, int *used, float *tune_ms);
 
+/* ---- the surrogate of the log-likelihood ------------------------------------------------------------------- */
+/* A multilayer perceptron d_in -> hidden -> hidden -> hidden -> 1 (GELU) trained online on the likelihood evaluations
+ * of a sampler, to screen its proposals. No counterpart in the reference (its nested sampler trains neural bounds in
+ * numba, bbarolo/bayesian/nautilus/mlp.py:18-118, and bounds/neural.py). BF16 weights and activations in the
+ * products, FP32 accumulation, FP32 master weights and Adam (beta 0.9, 0.999, eps 1e-8). Inputs x (n, d_in) and
+ * targets t (n) float32 host arrays; the loss is the mean squared error. Parameters (float32, flattened): W1
+ * (hidden, d_in), b1, W2 (hidden, hidden), b2, W3, b3, w4 (hidden), b4. */
+typedef struct bbgpu_mlp bbgpu_mlp;
+int bbgpu_mlp_create(bbgpu_mlp **out, int device, int d_in, int hidden, uint64_t seed);
+int bbgpu_mlp_destroy(bbgpu_mlp *m);
+long long bbgpu_mlp_nparams(const bbgpu_mlp *m);
+int bbgpu_mlp_get_params(const bbgpu_mlp *m, float *params);
+int bbgpu_mlp_set_params(bbgpu_mlp *m, const float *params);      /* (also resets Adam) */
+int bbgpu_mlp_predict(bbgpu_mlp *m, const float *x, int n, float *y);
+int bbgpu_mlp_gradients(bbgpu_mlp *m, const float *x, const float *t, int n, float *grads, float *loss);
+int bbgpu_mlp_train_step(bbgpu_mlp *m, const float *x, const float *t, int n, float lr, float *loss);
+
 /* ---- without allocation ------------------------------------------------------------------------------- */
 /* bbgpu_sumsq_residuals / bbgpu_residuals_fracerr for callers that may not allocate device memory (their own
  * memory pool, a stream being captured into a CUDA graph, a fixed footprint after warm-up). No counterpart in
