@@ -237,6 +237,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-analytic", action="store_true", help="skip the ANALYTIC GALMOD leg")
     ap.add_argument("--no-central", action="store_true", help="skip the 321-point central-difference batch")
+    ap.add_argument("--no-bayes", action="store_true",
+                    help="skip the 256x256x192 batch of 1024 points and the BAYESIAN fit")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the per-variant convolution times and errors")
     ap.add_argument("--no-random", action="store_true",
@@ -370,6 +372,9 @@ def main():
     if not args.no_random:
         line["random"] = batch_leg(ctx, L, rings, random_rows(rings, B), args, dist, world)
         line["unshared"] = batch_leg(ctx, L, rings, rows, args, dist, world, share=False)
+    if not args.no_bayes:
+        line["bayes256"] = bayes256_leg(args, dist, world)
+        line["bayes_fit"] = bayes_fit_leg()
     if rank == 0 and not args.no_cpu:
         vals, cores, n = cpu_leg(dm, L, rows, rings, data, mask)
         line["cpu_baseline"] = {"value": float(np.median(vals)), "unit": UNIT, "cores": cores, "kind": "port",
@@ -429,6 +434,96 @@ def conv_variants_leg(ctx, L, rows, rings, sr, nv, descs):
         ctx.set_option(_lib.OPT_CONV, _lib.CONV_AUTO)
         L._maps_sr = ms                  # (the whole batch's tables, which the next legs upload)
     return res
+
+
+def bayes256_leg(args, dist, world, nb=1024):
+    """BAYESIAN 3DFIT at 256x256x192 (20 rings; VROT and VDISP per ring, INC and PA global: 42 dimensions; priors
+    vrot 0-350 km/s, vdisp 1-40 km/s, inc 30-80, pa 0-360; truth drawn from them with seed 7; beam 4 pixels; noise 1%
+    of the peak; the ANALYTIC model, the reference's default for BAYESIAN): one batch of nb independent points about
+    the truth, as a nested sampler's live points late in a run, evaluated per launch (device-resident, the batch run
+    replayed as a CUDA graph) and end to end. DENS is fixed at the truth (no flux normalisation)."""
+    from bbarolo2_gb300 import _lib, bayesian, configs, engine
+    cube, rings = configs.bayes256(galmodtype="ANALYTIC")
+    dm = engine.DiskModel(cube, galmodtype="ANALYTIC")
+    truth = dm.array(rings, seed=1)
+    sigma = 0.01 * float(truth.max())
+    g = np.random.default_rng(7)
+    data = (truth + g.normal(0., sigma, truth.shape)).astype(np.float32)
+    L = engine.BatchLikelihood(dm, data, truth > 3 * sigma, maskmode=2, sigma=sigma)
+    prob = bayesian.Problem(rings, per_ring=("vrot", "vdisp"), global_=("inc", "phi"),
+                            priors={"vrot": (0., 350.), "vdisp": (1., 40.), "inc": (30., 80.), "phi": (0., 360.)})
+    t0 = np.clip(prob.unit(np.r_[rings.vrot, rings.vdisp, rings.inc[0], rings.phi[0]])[0], 0, 1)
+    ctx = dm.ctx
+    while True:
+        u = np.clip(t0 + 0.002 * g.standard_normal((nb, prob.ndim)), 0., 1.)
+        rows = prob.rows(u)
+        try:
+            sr, nv, descs, boxes = L.prepare(rows, rings, seed=1)
+            ctx.check(ctx.L.bbgpu_eval_upload(ctx.h, _lib.ANALYTIC, nb, sr.shape[2], _lib.ptr(sr), _lib.ptr(nv),
+                                              _lib.ptr(descs)))
+            ctx.check(ctx.L.bbgpu_eval_run(ctx.h))
+            break
+        except _lib.DeviceError:
+            if nb <= 128:
+                raise
+            nb //= 2                   # (device memory: halve the batch)
+    steps = max(2, args.steps // 4)
+    for _ in range(2):
+        ctx.check(ctx.L.bbgpu_eval_run(ctx.h))
+    ctx.check(ctx.L.bbgpu_sync(ctx.h))
+    t = time.perf_counter()
+    for _ in range(steps):
+        ctx.check(ctx.L.bbgpu_eval_run(ctx.h))
+    ctx.check(ctx.L.bbgpu_sync(ctx.h))
+    dt = max_over_ranks(time.perf_counter() - t, dist)
+    replays, kernels = ctx.graph_stats()
+    ctx.set_option(_lib.OPT_TIMING, 1)
+    ctx.check(ctx.L.bbgpu_eval_run(ctx.h))
+    kt = {k: round(v, 3) for k, v in ctx.run_times().items() if v > 0.01}
+    ctx.set_option(_lib.OPT_TIMING, 0)
+    L.evaluate(rows, rings, seed=1, galmodtype="ANALYTIC")
+    t = time.perf_counter()
+    for _ in range(steps):
+        L.evaluate(rows, rings, seed=1, galmodtype="ANALYTIC")
+    te = max_over_ranks(time.perf_counter() - t, dist)
+    return {"batch": nb, "ndim": prob.ndim, "value": throughput(nb, steps, world, dt), "unit": UNIT,
+            "ms_per_step": 1e3 * dt / steps, "e2e": throughput(nb, steps, world, te), "kernel_ms": kt,
+            "graph": {"replays": replays, "kernels_per_replay": kernels},
+            "config": "256x256x192, 20 rings, 42 dimensions, ANALYTIC, DENS fixed"}
+
+
+def bayes_fit_leg(seed=11):
+    """BAYESIAN fit time at dlogZ <= 0.1 (nested sampling, 100 live points, batches of 1024 proposals) on a reduced
+    problem: a 64x64x64 cube, four rings, VROT and VDISP per ring, INC and PA global (10 dimensions), the ANALYTIC
+    model; plain, then with the learned surrogate screening the proposals (same seed: the same proposals)."""
+    from bbarolo2_gb300 import bayesian, configs, engine
+    from bbarolo2_gb300.rings import Rings
+    cube, _ = configs.classic64(galmodtype="ANALYTIC")
+    r = np.array([20., 50., 80., 110.])
+    truth = Rings().setRings(radii=r, xpos=32., ypos=32., vsys=1000., vrot=150. * (1 - np.exp(-r / 40.)),
+                             vdisp=10., inc=55., phi=45., z0=0., dens=np.exp(-r / 60.))
+    dm = engine.DiskModel(cube, galmodtype="ANALYTIC")
+    model = dm.array(truth, seed=1)
+    sigma = 0.02 * float(model.max())
+    g = np.random.default_rng(7)
+    data = (model + dm.convolve_planes(g.normal(0., sigma, model.shape)) * 2.).astype(np.float32)
+    like = engine.BatchLikelihood(dm, data, model > 2 * sigma, maskmode=2, sigma=sigma)
+    prob = bayesian.Problem(truth, per_ring=("vrot", "vdisp"), global_=("inc", "phi"),
+                            priors={"vrot": (20., 200.), "vdisp": (2., 30.), "inc": (40., 70.), "phi": (30., 60.)})
+    kw = dict(n_live=100, n_batch=1024, dlogz=0.1, seed=seed, galmodtype="ANALYTIC")
+    out = {}
+    for name, sur in (("plain", False), ("screened", True)):
+        res = bayesian.fit(like, prob, surrogate=sur, **kw)
+        out[name] = {"wall_s": res["wall"], "logz": res["logz"], "logzerr": res["logzerr"], "n_like": res["n_like"],
+                     "n_proposed": res["n_proposed"], "iterations": res["iterations"]}
+        if sur:
+            out[name].update(n_screened=res["n_screened"], screen_batches=res["screen_batches"],
+                             surrogate_rmse=res.get("surrogate_rmse"))
+        out[name]["theta_median"] = [round(float(v), 4) for v in res["theta_median"]]
+    out["dlogz_screened_vs_plain"] = out["screened"]["logz"] - out["plain"]["logz"]
+    out["speedup"] = out["plain"]["wall_s"] / out["screened"]["wall_s"]
+    out["problem"] = "64x64x64, 4 rings, 10 dimensions, ANALYTIC, 100 live points, dlogZ <= 0.1"
+    return out
 
 
 def random_rows(rings, batch, seed=2):
