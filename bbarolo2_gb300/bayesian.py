@@ -47,7 +47,11 @@ class Problem:
 
     def rows(self, u):
         """The ring-value rows (n, 17, nr) of unit-cube points."""
-        th = self.theta(u)
+        return self.rows_theta(self.theta(u))
+
+    def rows_theta(self, theta):
+        """The ring-value rows (n, 17, nr) of parameter vectors."""
+        th = np.atleast_2d(np.asarray(theta, float))
         rows = np.repeat(self.base[None], len(th), axis=0)
         for j, (row, rings, _, _) in enumerate(self.cols):
             rows[:, row, rings] = th[:, j:j + 1]
@@ -72,6 +76,32 @@ class DeviceLogLike:
                                                       galmodtype=self.galmodtype)
         self.calls += len(u)
         return out
+
+    def of_theta(self, thetas):
+        """log L of parameter vectors (the batch log-likelihood of the GLOBAL fit)."""
+        th = np.atleast_2d(np.asarray(thetas, float))
+        out = np.empty(len(th))
+        for a in range(0, len(th), self.chunk):
+            rows = self.problem.rows_theta(th[a:a + self.chunk])
+            out[a:a + len(rows)] = self.like.evaluate(rows, self.problem.proto, seed=self.seed,
+                                                      galmodtype=self.galmodtype)
+        self.calls += len(th)
+        return out
+
+
+def global_fit(like, problem, theta0, galmodtype=None, step=1e-3, errors=True, options=None, nsamples=4000,
+               seed=None):
+    """METHOD GLOBAL: the maximum of log L within the priors from theta0 (``bbarolo2_gb300.optimize``), every
+    gradient and Hessian stencil one device batch. Returns the result of ``optimize.optimize`` with ``calls``."""
+    from .optimize import optimize
+    ll = DeviceLogLike(like, problem, galmodtype=galmodtype)
+    lo = np.array([c[2] for c in problem.cols])
+    hi = np.array([c[3] for c in problem.cols])
+    names = [RING_KEYS[c[0]] for c in problem.cols]
+    res = optimize(ll.of_theta, lo, hi, theta0, step=step, errors=errors, options=options, nsamples=nsamples,
+                   seed=seed, names=names)
+    res["calls"] = ll.calls
+    return res
 
 
 def fit(like, problem, n_live=400, n_batch=1024, dlogz=0.1, seed=0, surrogate=False, galmodtype=None,
