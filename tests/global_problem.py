@@ -1,21 +1,34 @@
 """The reduced GLOBAL problem of the fit-level parity tests, built from the oracle alone.
 
-A 64x64x64 cube (10" pixels, 5 km/s channels, 30" beam), four rings at 20-110", VROT and VDISP per ring with INC and PA
-global (10 free parameters, uniform priors), the ANALYTIC model of a thin disk (z0 = 0). The mock is the oracle's
+A 64x64x64 cube (10" pixels, 5 km/s channels, 30" beam), four rings at 20-110", the ANALYTIC model of a thin disk
+(z0 = 0), uniform priors. Two cases: "kin", VROT and VDISP per ring (8 free parameters, the geometry at the truth),
+and "geo", VROT and VDISP per ring with INC and PA global (10 free parameters). The mock is the oracle's
 ANALYTIC model of the truth, convolved in float64, plus white noise of 2% of its peak (seed 7); the likelihood mask is
 the convolved truth above twice the noise, mask mode 2 (Bayesian3DFIT's default).
 
 ``oracle_loglikes(P)`` is the reference's log L of a list of parameter vectors computed by the oracle
 (``bbarolo/bayesian/likelihood.py:567-619``: the model in its box, the "same" convolution, the residual of the box and
 the data outside it), the likelihood the reference's own GLOBAL fit is run on to make ``tests/golden/global.npz``.
+
+The likelihood is smooth in VROT and VDISP, but in INC and PA it is a staircase: the ANALYTIC model puts each
+azimuth sample in one pixel, so that a change of the geometry moves flux between pixels in steps (of up to several
+units of log L at this noise, over fractions of the Laplace sigma of PA). A fit of "geo" therefore ends wherever its
+path meets the staircase; ``STARTS`` gives the starts of the reference's fits that measure how far apart its own
+fits from nearby starts land.
 """
 
 import math
 
 import numpy as np
 
-FREE = (("vrot", 4, (20., 200.)), ("vdisp", 4, (2., 30.)), ("inc", 1, (40., 70.)), ("phi", 1, (30., 60.)))
-X0 = np.array([70., 100., 120., 140., 14., 8., 12., 9., 50., 40.])    # the start of the fits
+FREE = {"kin": (("vrot", 4, (20., 200.)), ("vdisp", 4, (2., 30.))),
+        "geo": (("vrot", 4, (20., 200.)), ("vdisp", 4, (2., 30.)), ("inc", 1, (40., 70.)), ("phi", 1, (30., 60.)))}
+X0 = {"kin": np.array([70., 100., 120., 140., 14., 8., 12., 9.]),             # the start of the fits
+      "geo": np.array([70., 100., 120., 140., 14., 8., 12., 9., 50., 40.])}
+# the reference's fits of "geo" from nearby starts (its own scatter on the staircase)
+STARTS = [X0["geo"] + d for d in (np.r_[[2., -2., 2., -2.], [1., -1., 1., -1.], 0.5, 0.5],
+                                 np.r_[[-2., 2., -2., 2.], [-1., 1., -1., 1.], -0.5, 0.5],
+                                 np.r_[[1., 1., 1., 1.], [0.5, 0.5, 0.5, 0.5], 0.5, -0.5])]
 
 
 def cube_and_truth():
@@ -28,9 +41,9 @@ def cube_and_truth():
     return cube, truth
 
 
-def bounds():
+def bounds(case):
     lo, hi, names = [], [], []
-    for name, n, (a, b) in FREE:
+    for name, n, (a, b) in FREE[case]:
         lo += [a] * n
         hi += [b] * n
         names += [name] * n
@@ -38,9 +51,9 @@ def bounds():
 
 
 class Problem:
-    """The cube, truth, mock and the oracle's set-up of the reduced GLOBAL problem."""
+    """The cube, truth, mock and the oracle's set-up of the reduced GLOBAL problem (case "kin" or "geo")."""
 
-    def __init__(self):
+    def __init__(self, case):
         from oracle import host
         from oracle import oracle as O
         O.lib()
@@ -58,7 +71,8 @@ class Problem:
         self.valid = valid
         self.d2 = np.where(valid, self.data.astype(np.float64) ** 2, 0.)
         self.nvox = int(valid.sum())
-        self.lo, self.hi, self.names = bounds()
+        self.case = case
+        self.lo, self.hi, self.names = bounds(case)
 
     def row(self, theta):
         """The ring-value row (17, nr) of a parameter vector (None: the truth)."""
@@ -67,11 +81,10 @@ class Problem:
         if theta is None:
             return row
         th = np.asarray(theta, float)
-        nr = self.truth.nr
-        row[RING_KEYS.index("vrot")] = th[:nr]
-        row[RING_KEYS.index("vdisp")] = th[nr:2 * nr]
-        row[RING_KEYS.index("inc")] = th[2 * nr]
-        row[RING_KEYS.index("phi")] = th[2 * nr + 1]
+        k = 0
+        for name, n, _ in FREE[self.case]:
+            row[RING_KEYS.index(name)] = th[k:k + n] if n > 1 else th[k]
+            k += n
         return row
 
     def model(self, row, box=False):

@@ -10,28 +10,26 @@ import global_problem as G
 from golden_io import load
 
 
-@pytest.fixture(scope="module")
-def problem(oracle_lib):
-    return G.Problem()
-
-
-def test_mock_matches_fixture(problem):
+def test_mock_matches_fixture(oracle_lib):
+    P = G.Problem("kin")
     ref = load("global.npz")
-    assert problem.nvox == int(ref["nvox"])
-    assert abs(problem.data.astype(np.float64).sum() - float(ref["data_sum"])) <= 1e-9 * abs(float(ref["data_sum"]))
+    assert P.nvox == int(ref["nvox"])
+    assert abs(P.data.astype(np.float64).sum() - float(ref["data_sum"])) <= 1e-9 * abs(float(ref["data_sum"]))
 
 
-def test_driver_reproduces_reference_fit(problem):
+@pytest.mark.parametrize("case", ["kin", "geo"])
+def test_driver_reproduces_reference_fit(oracle_lib, case):
     from bbarolo2_gb300.optimize import optimize
+    P = G.Problem(case)
     ref = load("global.npz")
-    res = optimize(problem.loglikes, problem.lo, problem.hi, G.X0, seed=1, nsamples=200, names=problem.names)
-    err = ref["errors"]
-    assert np.all(np.abs(res.x - ref["x"]) <= 1e-6 * err), (res.x, ref["x"])
+    res = optimize(P.loglikes, P.lo, P.hi, G.X0[case], seed=1, nsamples=200, names=P.names)
+    x, err, H = ref[f"{case}/x"], ref[f"{case}/errors"], ref[f"{case}/hessian"]
+    assert np.all(np.abs(res.x - x) <= 1e-6 * err), (res.x, x)
     np.testing.assert_allclose(res.errors, err, rtol=1e-6)
-    np.testing.assert_allclose(res.hessian, ref["hessian"], rtol=1e-6, atol=1e-9 * np.abs(ref["hessian"]).max())
-    assert res.nfev == int(ref["nfev"]) and res.nit == int(ref["nit"])
-    assert abs(res.logl - float(ref["logl"])) <= 1e-9 * abs(float(ref["logl"]))
-    assert res.message == str(ref["message"])
+    np.testing.assert_allclose(res.hessian, H, rtol=1e-6, atol=1e-9 * np.abs(H).max())
+    assert res.nfev == int(ref[f"{case}/nfev"]) and res.nit == int(ref[f"{case}/nit"])
+    assert abs(res.logl - float(ref[f"{case}/logl"])) <= 1e-9 * abs(float(ref[f"{case}/logl"]))
+    assert res.message == str(ref[f"{case}/message"])
 
 
 def test_driver_bounds_and_errors():
