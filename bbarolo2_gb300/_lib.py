@@ -28,7 +28,7 @@ SYMBOLS = ("bbgpu_ctx_create", "bbgpu_ctx_destroy", "bbgpu_last_error", "bbgpu_v
            "bbgpu_sumsq_residuals_noalloc", "bbgpu_set_profile", "bbgpu_eval_upload_profile", "bbgpu_eval_profile", "bbgpu_solve_profile",
            "bbgpu_subrings_rows", "bbgpu_conv_variant", "bbgpu_graph_stats", "bbgpu_mlp_create",
            "bbgpu_mlp_destroy", "bbgpu_mlp_nparams", "bbgpu_mlp_get_params", "bbgpu_mlp_set_params",
-           "bbgpu_mlp_predict", "bbgpu_mlp_gradients", "bbgpu_mlp_train_step")
+           "bbgpu_mlp_predict", "bbgpu_mlp_gradients", "bbgpu_mlp_train_step", "bbgpu_mlp_train")
 
 
 class Grid(C.Structure):
@@ -112,6 +112,7 @@ def load(path=None):
         "bbgpu_mlp_predict": (i, [vp, vp, i, vp]),
         "bbgpu_mlp_gradients": (i, [vp, vp, vp, i, vp, vp]),
         "bbgpu_mlp_train_step": (i, [vp, vp, vp, i, C.c_float, vp]),
+        "bbgpu_mlp_train": (i, [vp, vp, vp, C.c_longlong, i, i, C.c_float, C.c_uint64, vp]),
         "bbgpu_sumsq_residuals_noalloc": (i, [vp, vp, vp, i, vp, i, i, i, d, d, vp, vp]),
         "bbgpu_set_profile": (i, [vp, i, i, i, i, i, vp, vp, vp, vp, d, d, d, d]),
         "bbgpu_eval_upload_profile": (i, [vp, i, vp, vp, vp]),

@@ -15,17 +15,19 @@ from .rings import RING_KEYS
 
 class Problem:
     """The parameter space of a fit: per_ring (names of per-ring parameters), global_ (names of parameters shared by
-    the rings), priors {name: (lo, hi)}; proto: the rings (radii and the values of the fixed parameters)."""
+    the rings), priors {name: (lo, hi)}; proto: the rings (radii and the values of the fixed parameters); free_rings:
+    the rings whose per-ring parameters are free (default all; the others keep proto's values)."""
 
-    def __init__(self, proto, per_ring=("vrot", "vdisp"), global_=("inc", "phi"), priors=None):
+    def __init__(self, proto, per_ring=("vrot", "vdisp"), global_=("inc", "phi"), priors=None, free_rings=None):
         self.proto = proto
         self.per_ring, self.global_ = tuple(per_ring), tuple(global_)
         self.priors = dict(priors or {})
         nr = proto.nr
+        rings = range(nr) if free_rings is None else [int(r) for r in free_rings]
         self.cols = []                                       # (row of RING_KEYS, rings it sets, lo, hi)
         for name in self.per_ring:
             lo, hi = self.priors[name]
-            for r in range(nr):
+            for r in rings:
                 self.cols.append((RING_KEYS.index(name), [r], float(lo), float(hi)))
         for name in self.global_:
             lo, hi = self.priors[name]

@@ -58,4 +58,23 @@ def bayes256(galmodtype="ANALYTIC", iseed=1, seed=7):
     return cube, rings
 
 
+def bayes256_subproblem(free_rings=(2, 7, 12, 17), noise=0.02, seed=7):
+    """The BAYESIAN problem of the screen's benchmark: the ``bayes256`` cube and rings (ANALYTIC), the mock its model
+    plus white noise of `noise` of the peak, the mask the model above twice the noise; VROT and VDISP of `free_rings`
+    free (uniform priors: VROT within 40 km/s of the free rings' truths, VDISP 1-40 km/s), the other rings and the
+    geometry at the truth. Returns (BatchLikelihood, bayesian.Problem)."""
+    from . import bayesian, engine
+    cube, truth = bayes256(galmodtype="ANALYTIC")
+    dm = engine.DiskModel(cube, galmodtype="ANALYTIC")
+    model = dm.array(truth, seed=1)
+    sigma = noise * float(model.max())
+    g = np.random.default_rng(seed)
+    data = (model + g.normal(0., sigma, model.shape)).astype(np.float32)
+    like = engine.BatchLikelihood(dm, data, model > 2 * sigma, maskmode=2, sigma=sigma)
+    vr = np.asarray(truth.vrot, float)[list(free_rings)]
+    prob = bayesian.Problem(truth, per_ring=("vrot", "vdisp"), global_=(), free_rings=free_rings,
+                            priors={"vrot": (float(vr.min()) - 40., float(vr.max()) + 40.), "vdisp": (1., 40.)})
+    return like, prob
+
+
 WORKLOADS = {"classic64": classic64, "global160": global160, "bayes256": bayes256}

@@ -158,15 +158,25 @@ __global__ void k_out_back(int n, int H, const float *__restrict__ dy, const __n
     if (dz32) dz32[i] = d;
 }
 
-// column sums: out[j] = sum_b in[b][j] (+ the sum of v[b] a[b][j] products for the output weights when v given)
-__global__ void k_colsum(int n, int N, const float *__restrict__ in, const float *__restrict__ v,
-                         const __nv_bfloat16 *__restrict__ a, float *__restrict__ out) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= N) return;
+// column sums: out[j] = sum_b in[b][j] (or, with v given, sum_b v[b] a[b][j]: the output weights' gradient); a block
+// of 32 columns x 32 row groups, the groups' partial sums added in shared memory
+__global__ void __launch_bounds__(1024) k_colsum(int n, int N, const float *__restrict__ in,
+                                                 const float *__restrict__ v, const __nv_bfloat16 *__restrict__ a,
+                                                 float *__restrict__ out) {
+    __shared__ float part[32][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int j = blockIdx.x * 32 + tx;
     float s = 0.0f;
-    for (int b = 0; b < n; b++)
-        s += v ? v[b] * __bfloat162float(a[(size_t)b * N + j]) : in[(size_t)b * N + j];
-    out[j] = s;
+    if (j < N)
+        for (int b = ty; b < n; b += 32)
+            s += v ? v[b] * __bfloat162float(a[(size_t)b * N + j]) : in[(size_t)b * N + j];
+    part[ty][tx] = s;
+    __syncthreads();
+    if (ty == 0 && j < N) {
+        float t = 0.0f;
+        for (int k = 0; k < 32; k++) t += part[k][tx];
+        out[j] = t;
+    }
 }
 
 __global__ void k_sum(int n, const float *__restrict__ v, float *__restrict__ out) {
@@ -202,6 +212,21 @@ __global__ void k_to_bf16(long long n, const float *__restrict__ in, __nv_bfloat
     if (i < n) out[i] = __float2bfloat16_rn(in[i]);
 }
 
+// a minibatch of `rows` rows drawn with replacement from the n rows of a resident training set: row r of step
+// `step` is the set's row hash(seed, step, r) mod n (inputs to BF16, targets as they are)
+__global__ void k_gather_batch(int rows, int d, int n, unsigned long long seed, int step,
+                               const float *__restrict__ xs, const float *__restrict__ ts,
+                               __nv_bfloat16 *__restrict__ x16, float *__restrict__ t) {
+    const int r = blockIdx.x;
+    unsigned long long z = seed + 0x9E3779B97F4A7C15ull * ((unsigned long long)step * 0x100000001ull + r + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    const long long src = (long long)(z % (unsigned long long)n);
+    for (int k = threadIdx.x; k < d; k += blockDim.x) x16[(size_t)r * d + k] = __float2bfloat16_rn(xs[src * d + k]);
+    if (threadIdx.x == 0) t[r] = ts[src];
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------------------------------------- host side
@@ -216,6 +241,8 @@ struct bbgpu_mlp {
     float *xf = nullptr, *t = nullptr, *y = nullptr, *dy = nullptr, *loss = nullptr;
     __nv_bfloat16 *x16 = nullptr, *a[3] = {}, *dz[2] = {};
     float *z[3] = {}, *dz32[2] = {};
+    float *set_x = nullptr, *set_t = nullptr;   // the resident training set of bbgpu_mlp_train
+    long long set_cap = 0;
     cudaStream_t s = nullptr;
 };
 
@@ -275,7 +302,7 @@ void backward(bbgpu_mlp *m, int n) {
     const size_t nh = (size_t)n * H;
     k_out_back<<<(unsigned)((nh + 255) / 256), 256, 0, m->s>>>(n, H, m->dy, W + m->off[6], m->z[2], m->dz[0],
                                                                 m->dz32[0]);
-    k_colsum<<<(H + 127) / 128, 128, 0, m->s>>>(n, H, nullptr, m->dy, m->a[2], G + m->off[6]);
+    k_colsum<<<(H + 31) / 32, 1024, 0, m->s>>>(n, H, nullptr, m->dy, m->a[2], G + m->off[6]);
     k_sum<<<1, 256, 0, m->s>>>(n, m->dy, G + m->off[7]);
     int cur = 0;
     for (int l = 2; l >= 0; l--) {
@@ -284,7 +311,7 @@ void backward(bbgpu_mlp *m, int n) {
         // weight gradient: G[j][k] = sum_b dz[b][j] below[b][k]; bias gradient: column sums of dz
         gemm<__nv_bfloat16, __nv_bfloat16, EPI_F32>(m->s, H, kin, n, m->dz[cur], 1, H, below, kin, 1, nullptr,
                                                     nullptr, nullptr, G + m->off[2 * l]);
-        k_colsum<<<(H + 127) / 128, 128, 0, m->s>>>(n, H, m->dz32[cur], nullptr, nullptr, G + m->off[2 * l + 1]);
+        k_colsum<<<(H + 31) / 32, 1024, 0, m->s>>>(n, H, m->dz32[cur], nullptr, nullptr, G + m->off[2 * l + 1]);
         if (l > 0)   // the layer below: dz'[b][k] = (sum_j dz[b][j] W[j][k]) gelu'(z'[b][k])
             gemm<__nv_bfloat16, __nv_bfloat16, EPI_GELU_GRAD>(m->s, n, H, H, m->dz[cur], H, 1, W + m->off[2 * l], H,
                                                               1, nullptr, m->z[l - 1], m->dz[1 - cur],
@@ -368,6 +395,7 @@ extern "C" int bbgpu_mlp_destroy(bbgpu_mlp *m) {
     cudaFree(m->xf); cudaFree(m->t); cudaFree(m->y); cudaFree(m->dy); cudaFree(m->x16);
     for (int i = 0; i < 3; i++) { cudaFree(m->a[i]); cudaFree(m->z[i]); }
     for (int i = 0; i < 2; i++) { cudaFree(m->dz[i]); cudaFree(m->dz32[i]); }
+    cudaFree(m->set_x); cudaFree(m->set_t);
     if (m->s) cudaStreamDestroy(m->s);
     delete m;
     return BBGPU_OK;
@@ -420,12 +448,10 @@ extern "C" int bbgpu_mlp_gradients(bbgpu_mlp *m, const float *x, const float *t,
     return rc;
 }
 
-extern "C" int bbgpu_mlp_train_step(bbgpu_mlp *m, const float *x, const float *t, int n, float lr, float *loss) {
-    if (!m || !x || !t || n < 1 || !(lr > 0)) return BBGPU_ERR_ARG;
-    if (cudaSetDevice(m->device) != cudaSuccess) return BBGPU_ERR_CUDA;
-    int rc = load_x(m, x, n);
-    if (rc) return rc;
-    cudaMemcpyAsync(m->t, t, sizeof(float) * n, cudaMemcpyHostToDevice, m->s);
+namespace {
+
+// one Adam step on the rows already in x16 / t
+void adam_step(bbgpu_mlp *m, int n, float lr) {
     forward(m, n, m->t);
     backward(m, n);
     m->step++;
@@ -433,6 +459,48 @@ extern "C" int bbgpu_mlp_train_step(bbgpu_mlp *m, const float *x, const float *t
     k_adam<<<(unsigned)((m->np + 255) / 256), 256, 0, m->s>>>(m->np, m->w, m->m1, m->m2, m->g, m->w16, lr, b1, b2,
                                                               1.0f - powf(b1, (float)m->step),
                                                               1.0f - powf(b2, (float)m->step), 1e-8f);
+}
+
+}  // namespace
+
+extern "C" int bbgpu_mlp_train(bbgpu_mlp *m, const float *x, const float *t, long long n, int steps, int batch,
+                               float lr, uint64_t seed, float *loss) {
+    if (!m || !x || !t || n < 1 || n > 0x7fffffffLL || steps < 1 || batch < 1 || !(lr > 0)) return BBGPU_ERR_ARG;
+    if (cudaSetDevice(m->device) != cudaSuccess) return BBGPU_ERR_CUDA;
+    int rc = grow(m, batch);
+    if (rc) return rc;
+    if (n > m->set_cap) {
+        cudaFree(m->set_x);
+        cudaFree(m->set_t);
+        m->set_x = m->set_t = nullptr;
+        m->set_cap = 0;
+        if (cudaMalloc(&m->set_x, sizeof(float) * (size_t)n * m->d) != cudaSuccess ||
+            cudaMalloc(&m->set_t, sizeof(float) * (size_t)n) != cudaSuccess) {
+            cudaGetLastError();
+            return BBGPU_ERR_NOMEM;
+        }
+        m->set_cap = n;
+    }
+    cudaMemcpyAsync(m->set_x, x, sizeof(float) * (size_t)n * m->d, cudaMemcpyHostToDevice, m->s);
+    cudaMemcpyAsync(m->set_t, t, sizeof(float) * (size_t)n, cudaMemcpyHostToDevice, m->s);
+    for (int k = 0; k < steps; k++) {
+        k_gather_batch<<<batch, 64, 0, m->s>>>(batch, m->d, (int)n, seed, k, m->set_x, m->set_t, m->x16, m->t);
+        adam_step(m, batch, lr);
+    }
+    float ls = 0.0f;
+    cudaMemcpyAsync(&ls, m->loss, sizeof(float), cudaMemcpyDeviceToHost, m->s);
+    rc = finish(m);
+    if (loss) *loss = ls / (float)batch;
+    return rc;
+}
+
+extern "C" int bbgpu_mlp_train_step(bbgpu_mlp *m, const float *x, const float *t, int n, float lr, float *loss) {
+    if (!m || !x || !t || n < 1 || !(lr > 0)) return BBGPU_ERR_ARG;
+    if (cudaSetDevice(m->device) != cudaSuccess) return BBGPU_ERR_CUDA;
+    int rc = load_x(m, x, n);
+    if (rc) return rc;
+    cudaMemcpyAsync(m->t, t, sizeof(float) * n, cudaMemcpyHostToDevice, m->s);
+    adam_step(m, n, lr);
     float ls = 0.0f;
     cudaMemcpyAsync(&ls, m->loss, sizeof(float), cudaMemcpyDeviceToHost, m->s);
     rc = finish(m);

@@ -9,9 +9,14 @@ a proposal that beats the current worst point replaces it (a uniform draw within
 new threshold, is a uniform draw within the new region).
 
 Screen (``surrogate``): the proposals pass through the learned surrogate first, and only those it predicts above the
-threshold minus a margin reach the exact likelihood; the others count as rejected. The surrogate is retrained on the
-exact evaluations every n_live / 4 replacements, and the screen is used only while its error on the latest evaluations it was not
-trained on, near the threshold, stays below ``max_rmse`` (0.5 in log L): else every proposal is evaluated exactly.
+threshold they would meet, minus a margin, reach the exact likelihood; the others count as rejected. The threshold a
+proposal meets is the one after the replacements by the proposals before it in the batch: the pass is played on the
+predictions less the margin (``_screen``), which keeps that threshold at or below the exact pass's whenever the
+surrogate's error is within the margin, so that no proposal the exact pass would accept is turned away. The surrogate
+is retrained on the exact evaluations every n_live / 4 replacements once the live points' log L span less than
+``fit_range`` (40; before, the threshold moves by more than the surrogate's window between fits, and no fit passes the
+check below), and the screen is used only while its error on the latest evaluations it was not trained on, near the
+threshold, stays below ``max_rmse`` (0.5 in log L): else every proposal is evaluated exactly.
 The proposals are the same random draws with and without the screen, so a run with a screen that never turns away a
 point the exact likelihood would accept is the run without it, point for point.
 
@@ -55,7 +60,7 @@ class _Ellipsoid:
 
 
 def sample(loglike, ndim, n_live=400, n_batch=1024, dlogz=0.1, seed=0, enlarge=1.25, surrogate=None,
-           retrain_every=None, max_rmse=0.5, margin=None, max_batches=100000, verbose=False):
+           retrain_every=None, max_rmse=0.5, margin=None, fit_range=40.0, max_batches=100000, verbose=False):
     """Nested sampling of loglike (a function of an (n, ndim) array of unit-cube points -> n log-likelihoods) until
     the live points can add at most dlogz to log Z. Returns a dict: logz, logzerr, samples (unit cube), logl, logwt
     (log weights), n_like (exact evaluations), n_proposed, n_screened (proposals the screen turned away), iterations,
@@ -89,7 +94,7 @@ def sample(loglike, ndim, n_live=400, n_batch=1024, dlogz=0.1, seed=0, enlarge=1
         use = np.ones(len(cand), bool)
         if surrogate is not None and screen_ok:
             delta = margin if margin is not None else max(4.0 * surrogate.last_rmse, 0.5)
-            use = surrogate.predict(cand) > thr - delta
+            use = _screen(surrogate.predict(cand), logl, delta)
             n_screen += int((~use).sum())
             screen_batches += 1
         if use.any():
@@ -114,7 +119,7 @@ def sample(loglike, ndim, n_live=400, n_batch=1024, dlogz=0.1, seed=0, enlarge=1
             u[worst] = cand[c]
             logl[worst] = vals[c]
             it += 1
-        if surrogate is not None and it >= next_fit:
+        if surrogate is not None and it >= next_fit and float(logl.max() - logl.min()) < fit_range:
             screen_ok = _refit(surrogate, hist_u, hist_l, untrained_from, u, logl, max_rmse)
             untrained_from = len(hist_u)
             next_fit = it + retrain_every
@@ -134,6 +139,22 @@ def sample(loglike, ndim, n_live=400, n_batch=1024, dlogz=0.1, seed=0, enlarge=1
     return dict(logz=float(logz), logzerr=math.sqrt(max(h, 0.0) / n_live), samples=np.asarray(dead_u),
                 logl=np.asarray(dead_l), logwt=logwt, n_like=n_like, n_proposed=n_prop, n_screened=n_screen,
                 iterations=it, wall=time.perf_counter() - t0, screen_batches=screen_batches, information=h)
+
+
+def _screen(pred, live_l, delta):
+    """The proposals worth an exact evaluation: those predicted above the threshold of their turn in the pass, less
+    delta. The pass is played with the predictions less delta as the values of the replacing points, a lower bound of
+    their exact values when the surrogate's error is below delta, so the played threshold stays at or below the exact
+    one at every turn (the sorted live values of the play never exceed the exact ones)."""
+    play = np.array(live_l, float)
+    use = np.zeros(len(pred), bool)
+    for c, p in enumerate(np.asarray(pred, float)):
+        w = int(np.argmin(play))
+        if p > play[w] - delta:
+            use[c] = True
+            if p - delta > play[w]:
+                play[w] = p - delta
+    return use
 
 
 def _refit(sur, hist_u, hist_l, untrained_from, live_u, live_l, max_rmse):

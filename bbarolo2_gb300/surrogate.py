@@ -59,6 +59,17 @@ class MLP:
                                                  C.byref(loss)), "bbgpu_mlp_gradients")
         return g, float(loss.value)
 
+    def train(self, x, t, steps, batch, lr=1e-3, seed=0):
+        """`steps` Adam steps on minibatches of `batch` rows drawn on the device from the set (x, t); returns the
+        last minibatch's loss."""
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        loss = C.c_float(0)
+        self._check(self.L.bbgpu_mlp_train(self.h, _lib.ptr(x), _lib.ptr(t), len(x), int(steps), int(batch),
+                                           C.c_float(lr), int(seed) & (2 ** 64 - 1), C.byref(loss)),
+                    "bbgpu_mlp_train")
+        return float(loss.value)
+
     def train_step(self, x, t, lr=1e-3):
         x = np.ascontiguousarray(x, np.float32)
         t = np.ascontiguousarray(t, np.float32)
@@ -109,11 +120,8 @@ class Surrogate:
         self.ymu, self.ysd = float(center), float(scale)
         x = self._x(u)
         t = np.clip((np.asarray(logl, float) - self.ymu) / self.ysd, -1.0, 1.0).astype(np.float32)
-        n = len(x)
-        loss = np.nan
-        for _ in range(self.steps):
-            idx = self.rng.integers(0, n, min(self.batch, n))
-            loss = self.net.train_step(x[idx], t[idx], self.lr)
+        # the minibatches are drawn on the device: one call for all the steps
+        loss = self.net.train(x, t, self.steps, min(self.batch, len(x)), self.lr, int(self.rng.integers(2 ** 62)))
         self.trained = True
         return loss * self.ysd ** 2
 

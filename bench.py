@@ -493,23 +493,12 @@ def bayes256_leg(args, dist, world, nb=1024):
 
 
 def bayes_fit_leg(seed=11):
-    """BAYESIAN fit time at dlogZ <= 0.1 (nested sampling, 100 live points, batches of 1024 proposals) on a reduced
-    problem: a 64x64x64 cube, four rings, VROT and VDISP per ring, INC and PA global (10 dimensions), the ANALYTIC
-    model; plain, then with the learned surrogate screening the proposals (same seed: the same proposals)."""
-    from bbarolo2_gb300 import bayesian, configs, engine
-    from bbarolo2_gb300.rings import Rings
-    cube, _ = configs.classic64(galmodtype="ANALYTIC")
-    r = np.array([20., 50., 80., 110.])
-    truth = Rings().setRings(radii=r, xpos=32., ypos=32., vsys=1000., vrot=150. * (1 - np.exp(-r / 40.)),
-                             vdisp=10., inc=55., phi=45., z0=0., dens=np.exp(-r / 60.))
-    dm = engine.DiskModel(cube, galmodtype="ANALYTIC")
-    model = dm.array(truth, seed=1)
-    sigma = 0.02 * float(model.max())
-    g = np.random.default_rng(7)
-    data = (model + dm.convolve_planes(g.normal(0., sigma, model.shape)) * 2.).astype(np.float32)
-    like = engine.BatchLikelihood(dm, data, model > 2 * sigma, maskmode=2, sigma=sigma)
-    prob = bayesian.Problem(truth, per_ring=("vrot", "vdisp"), global_=("inc", "phi"),
-                            priors={"vrot": (20., 200.), "vdisp": (2., 30.), "inc": (40., 70.), "phi": (30., 60.)})
+    """BAYESIAN fit time at dlogZ <= 0.1 (nested sampling, 100 live points, batches of 1024 proposals) on the
+    256x256x192 cube of the BAYESIAN workload (20 rings, ANALYTIC) with VROT and VDISP of four rings free (8
+    dimensions; ``configs.bayes256_subproblem``): plain, then with the learned surrogate screening the proposals (same
+    seed: the same proposals)."""
+    from bbarolo2_gb300 import bayesian, configs
+    like, prob = configs.bayes256_subproblem()
     kw = dict(n_live=100, n_batch=1024, dlogz=0.1, seed=seed, galmodtype="ANALYTIC")
     out = {}
     for name, sur in (("plain", False), ("screened", True)):
@@ -520,9 +509,14 @@ def bayes_fit_leg(seed=11):
             out[name].update(n_screened=res["n_screened"], screen_batches=res["screen_batches"],
                              surrogate_rmse=res.get("surrogate_rmse"))
         out[name]["theta_median"] = [round(float(v), 4) for v in res["theta_median"]]
+        out[name]["theta_std"] = [round(float(v), 4) for v in res["theta_std"]]
+    sd = np.asarray(out["plain"]["theta_std"])
     out["dlogz_screened_vs_plain"] = out["screened"]["logz"] - out["plain"]["logz"]
+    out["max_median_shift_sigma"] = float(np.max(np.abs(np.asarray(out["screened"]["theta_median"]) -
+                                                      np.asarray(out["plain"]["theta_median"])) / sd))
     out["speedup"] = out["plain"]["wall_s"] / out["screened"]["wall_s"]
-    out["problem"] = "64x64x64, 4 rings, 10 dimensions, ANALYTIC, 100 live points, dlogZ <= 0.1"
+    out["calls_ratio"] = out["plain"]["n_like"] / out["screened"]["n_like"]
+    out["problem"] = "256x256x192, 20 rings, VROT+VDISP of 4 rings free (8 dimensions), ANALYTIC, 100 live points"
     return out
 
 

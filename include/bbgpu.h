@@ -192,6 +192,11 @@ int bbgpu_mlp_set_params(bbgpu_mlp *m, const float *params);      /* (also reset
 int bbgpu_mlp_predict(bbgpu_mlp *m, const float *x, int n, float *y);
 int bbgpu_mlp_gradients(bbgpu_mlp *m, const float *x, const float *t, int n, float *grads, float *loss);
 int bbgpu_mlp_train_step(bbgpu_mlp *m, const float *x, const float *t, int n, float lr, float *loss);
+/* `steps` Adam steps on minibatches of `batch` rows drawn with replacement (a hash of seed, step and row) from the
+ * training set x (n, d_in), t (n), which is copied to the device once: one call, one synchronisation. loss: the
+ * mean squared error of the last minibatch (before its step). n < 2^31. */
+int bbgpu_mlp_train(bbgpu_mlp *m, const float *x, const float *t, long long n, int steps, int batch, float lr,
+                    uint64_t seed, float *loss);
 
 /* ---- without allocation ------------------------------------------------------------------------------- */
 /* bbgpu_sumsq_residuals / bbgpu_residuals_fracerr for callers that may not allocate device memory (their own

@@ -107,6 +107,29 @@ def test_mlp_training_converges(gpu_lib):
     assert float(np.mean((y - t) ** 2)) < 0.05 * first, (first, float(np.mean((y - t) ** 2)))
 
 
+def test_mlp_train_on_device_minibatches(gpu_lib):
+    """bbgpu_mlp_train (the minibatches drawn on the device, one call): the same fit as the host loop, repeatable for a
+    seed, and a one-row minibatch of a one-row set is exactly train_step on that row."""
+    from bbarolo2_gb300.surrogate import MLP
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal((4096, D)).astype(np.float32)
+    w = rng.standard_normal(D) / np.sqrt(D)
+    t = (x @ w + 0.3 * (x[:, :5] ** 2).sum(1)).astype(np.float32)
+    t = (t - t.mean()) / t.std()
+    a, b = MLP(D, H, seed=2), MLP(D, H, seed=2)
+    la = a.train(x, t, 600, 512, 1e-3, seed=5)
+    lb = b.train(x, t, 600, 512, 1e-3, seed=5)
+    assert abs(la - lb) <= 1e-5 * abs(la)          # (the reported loss is summed with atomics; the weights are not)
+    np.testing.assert_array_equal(a.params(), b.params())
+    y = a.predict(x)
+    assert float(np.mean((y - t) ** 2)) < 0.05, float(np.mean((y - t) ** 2))
+    c, d = MLP(D, H, seed=3), MLP(D, H, seed=3)
+    c.train(x[:1], t[:1], 3, 1, 1e-3, seed=9)
+    for _ in range(3):
+        d.train_step(x[:1], t[:1], 1e-3)
+    np.testing.assert_array_equal(c.params(), d.params())
+
+
 def test_mlp_rejects_bad_arguments(gpu_lib):
     import ctypes as C
     from bbarolo2_gb300 import _lib

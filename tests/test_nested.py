@@ -33,3 +33,28 @@ def test_same_seed_same_run():
     a = nested.sample(f, 3, n_live=100, n_batch=256, seed=5)
     b = nested.sample(f, 3, n_live=100, n_batch=256, seed=5)
     assert a["logz"] == b["logz"] and a["n_like"] == b["n_like"]
+
+
+def test_screen_plays_the_rising_threshold():
+    """The screen keeps every proposal the exact pass would accept when the surrogate's error is within the margin,
+    and turns away those below the threshold the earlier proposals of the batch raise."""
+    from bbarolo2_gb300.nested import _screen
+    g = np.random.default_rng(3)
+    for trial in range(50):
+        live = g.normal(0., 3., 40)
+        exact = g.normal(0., 4., 300)
+        delta = 0.5
+        pred = exact + g.uniform(-0.49, 0.49, exact.size)
+        use = _screen(pred, live, delta)
+        # the exact pass
+        cur = live.copy()
+        for c, v in enumerate(exact):
+            w = int(np.argmin(cur))
+            if v > cur[w]:
+                assert use[c], (trial, c)
+                cur[w] = v
+        # a proposal far below the initial threshold is turned away
+        assert not _screen(np.array([live.min() - 10.]), live, delta)[0]
+    # the rising threshold: the same value offered twice after the live minimum rose past it is turned away once
+    live = np.array([0., 5., 5., 5.])
+    assert list(_screen(np.array([4., 1.]), live, 0.5)) == [True, False]
