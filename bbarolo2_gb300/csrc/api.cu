@@ -215,7 +215,7 @@ struct bbgpu_ctx {
     int conv_variant = -1;                // -1: the autotuner's choice (below)
     // the autotuner: per kernel shape and channels (ky, kx, nz), the variant it chose, timed on the first batch
     // (float32 and tf32x3, the variants within 1e-5 per voxel of the float64 convolution), and its timings (ms)
-    std::vector<std::array<int, 4>> tuned;
+    std::vector<std::array<int, 4>> tuned;      // (ky, kx, nz, variant)
     float tune_ms[3] = {-1.f, -1.f, -1.f};
     std::vector<double> h_kernel;         // the beam kernel (ky, kx) float64
     void *d_bimg = nullptr;               // its B operand image for conv_variant
@@ -726,16 +726,18 @@ extern "C" int bbgpu_set_kernel(bbgpu_ctx *ctx, const double *kernel, int ky, in
     if (!ctx) return BBGPU_ERR_ARG;
     if (!kernel || ky < 1 || kx < 1 || !(ky & 1) || !(kx & 1) || ky > BBGPU_MAXK || kx > BBGPU_MAXK)
         return fail(ctx, BBGPU_ERR_ARG, "set_kernel: kernel sides must be odd, 1 to %d", BBGPU_MAXK);
-    std::vector<float> taps((size_t)ky * 31);
+    // the shared-memory templates of k_conv_resid take widths up to 31 and tiles up to 220 KB; a wider kernel
+    // (kxw = 0) keeps all its taps and runs k_conv_wide
+    std::vector<float> taps((size_t)ky * std::max(kx, 31));
     int kxw = conv_taps(kernel, ky, kx, taps.data());
-    if (!kxw) return fail(ctx, BBGPU_ERR_ARG, "set_kernel: kernel width %d above 31", kx);
-    size_t smem = (size_t)(16 + ky - 1) * (16 + kxw - 1) * 32 * 4 + (size_t)ky * kxw * 4;
-    if (smem > 220 * 1024) return fail(ctx, BBGPU_ERR_ARG, "set_kernel: kernel %dx%d too large", ky, kx);
+    if (kxw && (size_t)(16 + ky - 1) * (16 + kxw - 1) * 32 * 4 + (size_t)ky * kxw * 4 > 220 * 1024) kxw = 0;
+    if (!kxw) conv_wide_taps(kernel, ky, kx, taps.data());
+    const size_t ntaps = (size_t)ky * (kxw ? kxw : kx);
     CK(cudaSetDevice(ctx->device));
     cudaFree(ctx->d_taps);
     ctx->d_taps = nullptr;
-    CK(cudaMalloc(&ctx->d_taps, (size_t)ky * kxw * sizeof(float)));
-    CK(cudaMemcpy(ctx->d_taps, taps.data(), (size_t)ky * kxw * sizeof(float), cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&ctx->d_taps, ntaps * sizeof(float)));
+    CK(cudaMemcpy(ctx->d_taps, taps.data(), ntaps * sizeof(float), cudaMemcpyHostToDevice));
     ctx->ky = ky;
     ctx->kx = kx;
     ctx->kxw = kxw;
@@ -1335,6 +1337,8 @@ static int conv_variant_of(bbgpu_ctx *ctx, cudaStream_t s, bool conv, bool do_re
         v = v < 0 ? 0 : v;
         return 0;
     }
+    // one choice per kernel shape and channel count, made on the first batch: a parameter vector then gets the
+    // same bits in a batch of any size or composition (a sampler's points, a gradient's stencil)
     for (auto &t : ctx->tuned)
         if (t[0] == ctx->ky && t[1] == ctx->kx && t[2] == ctx->g.nz) {
             v = t[3];

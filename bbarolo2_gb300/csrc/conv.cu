@@ -91,6 +91,11 @@ void launch_conv_resid(cudaStream_t s, const GridDev &g, const MemberDev *mem, c
     const int npart = maxt * nzb;
     if (!do_conv) kxw = 1;
     const bool z16 = conv_zb(nz) == 16;
+    if (kxw == 0) {            // a kernel wider than the templates: taps (ky, kx) in global memory
+        launch_conv_wide(s, g, mem, nb, maxt, nzb, z16, model, mstride, nz, taps, ky, kx, smoothed, do_conv, do_resid,
+                         partial, npart, ts);
+        return;
+    }
     if (ts.tsrc) {
         launch_conv_table(s, g, mem, nb, maxt, nzb, z16, model, mstride, nz, taps, ky, kx, kxw, smoothed, do_conv,
                           do_resid, partial, npart, ts);

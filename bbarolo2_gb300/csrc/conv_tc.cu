@@ -162,18 +162,6 @@ __device__ __forceinline__ void mma_commit(uint64_t *b) {
                  : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
-}
-
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v) {
     uint32_t r[8];
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
@@ -190,13 +178,6 @@ __device__ __forceinline__ void tmem_zero8(uint32_t taddr) {
                  : "memory");
 }
 
-__device__ __forceinline__ void tmem_zero16(uint32_t taddr) {
-    const uint32_t z = 0;
-    asm volatile(
-        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(taddr),
-        "r"(z)
-        : "memory");
-}
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 __device__ __forceinline__ void tma_load3(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, uint64_t *bar) {
@@ -205,12 +186,6 @@ __device__ __forceinline__ void tma_load3(uint32_t dst, const CUtensorMap *map, 
             dst),
         "l"((uint64_t)map), "r"(saddr(bar)), "r"(c0), "r"(c1), "r"(c2)
         : "memory");
-}
-
-__device__ __forceinline__ uint32_t pack_bf16(float lo_elem, float hi_elem) {
-    const uint32_t a = __bfloat16_as_ushort(__float2bfloat16_rn(lo_elem));
-    const uint32_t b = __bfloat16_as_ushort(__float2bfloat16_rn(hi_elem));
-    return a | (b << 16);
 }
 
 __device__ __forceinline__ float tf32_rna(float v) {

@@ -12,7 +12,7 @@
 #endif
 
 #define BBGPU_MAXL 4          // emission lines supported by the device path
-#define BBGPU_MAXK 63         // largest beam kernel side
+#define BBGPU_MAXK 511        // largest beam kernel side (the reference's FFT convolver: below 512)
 #define BBGPU_NSR 16          // rows of a sub-ring table
 
 // Per (member, sub-ring) parameters of the MC deposit. f64 fields reproduce the reference's arithmetic

@@ -140,6 +140,11 @@ void launch_conv_table(cudaStream_t s, const GridDev &g, const MemberDev *mem, i
                        const float *model, long long mstride, int nz, const float *taps, int ky, int kx, int kxw,
                        float *smoothed, int do_conv, int do_resid, double *partial, int npart, TileSrc ts);
 void launch_reduce_partials(cudaStream_t s, const double *partial, int npart, int nb, double *out2);
+// (conv_wide.cu: kernels wider than the templates, kxw = 0 in launch_conv_resid; the taps (ky, kx) flipped)
+void conv_wide_taps(const double *k, int ky, int kx, float *taps);
+void launch_conv_wide(cudaStream_t s, const GridDev &g, const MemberDev *mem, int nb, int maxt, int nzb, bool z16,
+                      const float *model, long long mstride, int nz, const float *taps, int ky, int kx,
+                      float *smoothed, int do_conv, int do_resid, double *partial, int npart, TileSrc ts);
 
 // ---- convolution + residual on the tensor cores (conv_tc.cu): variant 1 bf16x3, 2 tf32x3 (split products,
 // FP32 accumulation in TMEM). Kernels of at most 16 rows and 33 columns, nz a multiple of 4 (TMA rows of 16 bytes).

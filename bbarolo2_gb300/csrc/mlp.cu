@@ -33,9 +33,8 @@ __device__ __forceinline__ float gelu_grad(float z) {
     return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
 }
 
-// element (i, k) of a strided operand: p[i * si + k * sk], as BF16 from BF16 or FP32 storage
+// element (i, k) of a strided BF16 operand: p[i * si + k * sk]
 __device__ __forceinline__ __nv_bfloat16 elem(const __nv_bfloat16 *p, long long off) { return p[off]; }
-__device__ __forceinline__ __nv_bfloat16 elem(const float *p, long long off) { return __float2bfloat16_rn(p[off]); }
 
 // C (M x N) = A (M x K) B (K x N), A(m, t) = A[m sam + t sat], B(t, j) = B[t sbt + j sbj]. Epilogues:
 //  EPI_BIAS_GELU: z = C + bias[j] -> Z[m][j] (FP32), out[m][j] = gelu(z) (BF16)

@@ -76,7 +76,11 @@ int bbgpu_version(void);
 /* cd2i (nz), lfreq0 (nlines), relint (nlines), vedges (nlines, nz+1) velocity channel edges per line. */
 int bbgpu_set_grid(bbgpu_ctx *ctx, const bbgpu_grid *g, const double *cd2i, const double *lfreq0,
                    const double *relint, const double *vedges);
-/* Beam kernel (ky, kx) float64 (bbarolo/smooth.py:62-88); ky, kx odd, at most 63 x 63. */
+/* Beam kernel (ky, kx) float64 (bbarolo/smooth.py:62-88); ky, kx odd, at most 511 (the reference's FFT convolver
+ * takes sides below 512). The float32 convolution stages its input tile in shared memory for widths up to 31 with
+ * (16 + ky - 1) (16 + width - 1) 128 bytes within 220 KB (ky up to 23 at width 31) and reads wider kernels' inputs
+ * from global memory (k_conv_wide); the tensor-core variants take ky <= 32 and widths <= 33, and the f32 kernel
+ * runs when they cannot. */
 int bbgpu_set_kernel(bbgpu_ctx *ctx, const double *kernel, int ky, int kx);
 /* Cube data (nz, ny, nx) float32, mask (nz, ny, nx) uint8 or NULL, region (ny, nx) uint8 or NULL. */
 int bbgpu_set_cube(bbgpu_ctx *ctx, const float *data, const uint8_t *mask, const uint8_t *region);
@@ -200,14 +204,14 @@ int bbgpu_mlp_train(bbgpu_mlp *m, const float *x, const float *t, long long n, i
 
 /* ---- without allocation ------------------------------------------------------------------------------- */
 /* bbgpu_sumsq_residuals / bbgpu_residuals_fracerr for callers that may not allocate device memory (their own
- * memory pool, a stream being captured into a CUDA graph, a fixed footprint after warm-up). No counterpart in
+ * memory pool, a fixed footprint after warm-up). No counterpart in
  * the reference: it exists for such callers. Needs no context. model (nz, ny, nx) float64, data float32, mask
  * and region uint8 and out2 (double[2]: sum of squares or variance-weighted sum, sum of log-variances) are
  * DEVICE pointers of the current device; eps2 = 0 gives the plain sum of squares. Kernels run on stream
  * (cudaStream_t, NULL: the default stream) and out2 is written there. The partial sums use a 64 KB scratch
  * array held by every GPU that loads the library; at most 16,777,216 voxels (4096 blocks of 4096) per call,
  * BBGPU_ERR_ARG beyond (and for a negative or NaN eps2). The first call on a device looks the array's address up
- * (cudaGetSymbolAddress) and keeps it: make it before any stream capture, and do not reset the device
+ * (cudaGetSymbolAddress) and keeps it: do not reset the device
  * (cudaDeviceReset) between calls. A CUDA error pending from earlier work makes the call return BBGPU_ERR_CUDA
  * without launching. Calls whose kernels overlap on the GPU share the array and race. */
 int bbgpu_sumsq_residuals_noalloc(const double *model, const float *data, const uint8_t *mask, int maskmode,
