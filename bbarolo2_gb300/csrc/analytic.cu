@@ -314,7 +314,27 @@ __device__ __forceinline__ float phi_f32(float t, const float *__restrict__ tab)
     return fmaf(x - (float)k, t1 - t0, t0);
 }
 
-__global__ void __launch_bounds__(ANF_WPB * 32) k_an_model_fast(GridDev g, const AnSub *__restrict__ subs, int nsub,
+// The line of a float32-path sample: bbarolo/galmod.py:407 and :410 (_velgrid, _lround) in float-float (about 44
+// bits: the channel and the velocity relative to vref within ~1e-11 of the reference's float64 values); within 1e-6
+// of a channel boundary the reference's float64 operations decide the centre channel. Returns the centre channel
+// and the line-of-sight velocity v (float-float).
+__device__ __forceinline__ long long fast_line_centre(const AnSub &S, const GridDev &g, float4 cq,
+                                                      const double2 *__restrict__ cp, ff &v) {
+    const ff caz{cq.x, cq.y}, saz{cq.z, cq.w};
+    v = ff_add(ff_mul(ff{S.vroth, S.vrotl}, caz), ff_mul(ff{S.vradh, S.vradl}, saz));
+    v = ff_add(ff_mul(v, ff{S.sinch, S.sincl}), ff_mul(ff{S.vverth, S.vvertl}, ff{S.cinch, S.cincl}));
+    v = ff_add(ff{S.vsysh, S.vsysl}, v);
+    const ff chd = ff_add(ff_mul(v, ff{g.ia0h, g.ia0l}), ff{g.ib0h, g.ib0l});
+    int kci;
+    if (ff_round(chd, kci)) return kci;
+    const double2 c = *cp;
+    const double vplane = __dadd_rn(__dadd_rn(S.vsys, __dmul_rn(__dadd_rn(__dmul_rn(S.vrot, c.x),
+                                                                          __dmul_rn(S.vrad, c.y)), S.sinc)),
+                                    __dmul_rn(S.vvert, S.cinc));
+    return lround_ref(velgrid_exact(vplane, g, 0));
+}
+
+__global__ void __launch_bounds__(ANF_WPB * 32, 4) k_an_model_fast(GridDev g, const AnSub *__restrict__ subs, int nsub,
                                                                 const int *__restrict__ sbase,
                                                                 const int *__restrict__ ssub,
                                                                 const double2 *__restrict__ cs,
@@ -330,7 +350,7 @@ __global__ void __launch_bounds__(ANF_WPB * 32) k_an_model_fast(GridDev g, const
                                                                 const float *__restrict__ ptabf,
                                                                 const MemberDev *__restrict__ mem,
                                                                 unsigned long long *__restrict__ out64,
-                                                                long long mstride) {
+                                                                long long mstride, int skip_thin) {
     extern __shared__ float anf_smem[];                     // per warp: the CDF at the edges, the profile
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long gs = (long long)blockIdx.x * ANF_WPB + w;
@@ -340,7 +360,7 @@ __global__ void __launch_bounds__(ANF_WPB * 32) k_an_model_fast(GridDev g, const
     const long long s = sg.s;
     const int ir = ssub[s];
     const AnSub &S = subs[(size_t)sg.src * nsub + ir];
-    if (!S.active || !S.anfast) return;
+    if (!S.active || !S.anfast || (skip_thin && S.nzz == 1)) return;
     const float2 cf = csf[s];
     const bool rec = cf.x >= 0.0f;                          // (the sign of the float32 table is the float64 test's)
     if (S.wzero & (rec ? 1 : 2)) return;
@@ -353,26 +373,8 @@ __global__ void __launch_bounds__(ANF_WPB * 32) k_an_model_fast(GridDev g, const
     unsigned long long *o64 = out64 + (size_t)k * mstride;
     int k0 = 0, nk = -1;                                    // the line's channels (nk < 0: not computed yet)
     auto line = [&]() {
-        // bbarolo/galmod.py:407 and :410 (_velgrid, _lround) in float-float (about 44 bits: the channel and the
-        // velocity relative to vref within ~1e-11 of the reference's float64 values); within 1e-6 of a channel
-        // boundary the reference's float64 operations decide the centre channel
-        const float4 cq = csff[s];
-        const ff caz{cq.x, cq.y}, saz{cq.z, cq.w};
-        ff v = ff_add(ff_mul(ff{S.vroth, S.vrotl}, caz), ff_mul(ff{S.vradh, S.vradl}, saz));
-        v = ff_add(ff_mul(v, ff{S.sinch, S.sincl}), ff_mul(ff{S.vverth, S.vvertl}, ff{S.cinch, S.cincl}));
-        v = ff_add(ff{S.vsysh, S.vsysl}, v);
-        const ff chd = ff_add(ff_mul(v, ff{g.ia0h, g.ia0l}), ff{g.ib0h, g.ib0l});
-        int kci;
-        long long kc;
-        if (ff_round(chd, kci)) {
-            kc = kci;
-        } else {
-            const double2 c = cs[s];
-            const double vplane = __dadd_rn(__dadd_rn(S.vsys, __dmul_rn(__dadd_rn(__dmul_rn(S.vrot, c.x),
-                                                                                  __dmul_rn(S.vrad, c.y)), S.sinc)),
-                                            __dmul_rn(S.vvert, S.cinc));
-            kc = lround_ref(velgrid_exact(vplane, g, 0));
-        }
+        ff v;
+        const long long kc = fast_line_centre(S, g, csff[s], cs + s, v);
         long long a0 = kc - S.K, a1 = kc + S.K + 1;
         if (a0 < 0) a0 = 0;
         if (a1 > nz) a1 = nz;
@@ -449,6 +451,89 @@ __global__ void __launch_bounds__(ANF_WPB * 32) k_an_model_fast(GridDev g, const
             cg1 = __shfl_sync(FULL, g1, cnt - 1);
             cws = __shfl_sync(FULL, v, cnt - 1);
             open = true;
+        }
+    }
+}
+
+// The float32 path of the samples of thin sub-rings (one height, nzz = 1), 32 samples a warp: each lane sets up its
+// own sample (segment, pixel, box test, line centre, amplitude), then the warp deposits the samples in the box one
+// after another with its lanes over the channels. The same operations as k_an_model_fast on such a sample (one run
+// of one height: its weight is the height's), so the deposits are the same integers; the warp-uniform set-up that
+// k_an_model_fast repeats on 32 lanes for each sample is done once per lane here.
+__global__ void __launch_bounds__(ANF_WPB * 32, 4) k_an_model_thin(GridDev g, const AnSub *__restrict__ subs, int nsub,
+                                                                   const int *__restrict__ sbase,
+                                                                   const int *__restrict__ ssub,
+                                                                   const double2 *__restrict__ cs,
+                                                                   const float2 *__restrict__ csf,
+                                                                   const float4 *__restrict__ csff,
+                                                                   const long long *__restrict__ astart,
+                                                                   const int4 *__restrict__ aseg, int nseg,
+                                                                   long long ntot, const double *__restrict__ zq,
+                                                                   const float *__restrict__ zqf,
+                                                                   const float *__restrict__ wqf,
+                                                                   const float2 *__restrict__ vef,
+                                                                   const float *__restrict__ cd2if,
+                                                                   const float *__restrict__ ptabf,
+                                                                   const MemberDev *__restrict__ mem,
+                                                                   unsigned long long *__restrict__ out64,
+                                                                   long long mstride) {
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long gs = ((long long)blockIdx.x * ANF_WPB + w) * 32 + lane;
+    const int nz = g.nz;
+    bool ok = false;
+    int k0 = 0, nk = 0;
+    long long opix = 0;
+    float vrh = 0.0f, vrl = 0.0f, invf = 0.0f, amp = 0.0f, ws = 0.0f;
+    AnSeg sg;
+    if (an_seg(gs, astart, aseg, nseg, ntot, sbase, sg)) {
+        const long long s = sg.s;
+        const int ir = ssub[s];
+        const AnSub &S = subs[(size_t)sg.src * nsub + ir];
+        const float2 cf = csf[s];
+        const bool rec = cf.x >= 0.0f;
+        if (S.active && S.anfast && S.nzz == 1 && !(S.wzero & (rec ? 1 : 2))) {
+            const int kr = (int)(s - sbase[ir]) >= S.naz ? 1 : 0;
+            const PixF px = pix_setup(S, kr, cf, zqf + S.zq_off, 1);
+            int g0, g1;
+            sample_pixel(S, px, kr, cs + s, 1, 0.f, zq + S.zq_off, g.cdelt0, g.cdelt1, g0, g1);
+            const MemberDev &M = mem[sg.k];
+            if (g0 >= M.blo0 && g0 < M.bhi0 && g1 >= M.blo1 && g1 < M.bhi1) {
+                ff v;
+                const long long kc = fast_line_centre(S, g, csff[s], cs + s, v);
+                long long a0 = kc - S.K, a1 = kc + S.K + 1;
+                if (a0 < 0) a0 = 0;
+                if (a1 > nz) a1 = nz;
+                if (a1 > a0) {
+                    ok = true;
+                    k0 = (int)a0;
+                    nk = (int)(a1 - a0);
+                    const ff vr = ff_add(v, ff{-g.vrefh, -g.vrefl});
+                    vrh = vr.hi;
+                    vrl = vr.lo;
+                    invf = S.invf;
+                    amp = (float)sg.sign * ldexpf(S.af * (rec ? S.wrecf : S.wappf), M.fix_exp);
+                    ws = wqf[S.zq_off];
+                    opix = (long long)sg.k * mstride + ((long long)(g1 - M.blo1) * M.bx + (g0 - M.blo0)) * nz + k0;
+                }
+            }
+        }
+    }
+    unsigned todo = __ballot_sync(FULL, ok);
+    while (todo) {
+        const int e = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const int ek0 = __shfl_sync(FULL, k0, e), enk = __shfl_sync(FULL, nk, e);
+        const float evh = __shfl_sync(FULL, vrh, e), evl = __shfl_sync(FULL, vrl, e);
+        const float einv = __shfl_sync(FULL, invf, e), eamp = __shfl_sync(FULL, amp, e);
+        const float ews = __shfl_sync(FULL, ws, e);
+        const long long eop = __shfl_sync(FULL, opix, e);
+        for (int j = lane; j < enk; j += 32) {
+            const float2 ea = __ldg(vef + ek0 + j), eb = __ldg(vef + ek0 + j + 1);
+            const float ta = (__fsub_rn(ea.x, evh) + __fsub_rn(ea.y, evl)) * einv;
+            const float tb = (__fsub_rn(eb.x, evh) + __fsub_rn(eb.y, evl)) * einv;
+            const float p = fabsf(phi_f32(tb, ptabf) - phi_f32(ta, ptabf)) * __ldg(cd2if + ek0 + j) * eamp;
+            const long long q = f32_to_ll(p * ews);
+            if (q) atomicAdd(out64 + eop + j, (unsigned long long)q);
         }
     }
 }
@@ -536,16 +621,23 @@ void launch_an_model_fast(cudaStream_t s, const GridDev &g, const AnSub *subs, i
                           const int *ssub, const double *cs, const float *csf, const float *csff,
                           const long long *astart, const int *aseg, int nseg, long long ntot,
                           const double *zq, const float *zqf, const float *wqf, const float *vef, const float *cd2if,
-                          const float *ptabf, const MemberDev *mem, long long *out64, long long mstride) {
+                          const float *ptabf, const MemberDev *mem, long long *out64, long long mstride, int thin,
+                          int thick) {
     const long long nw = ntot;
     if (nw == 0 || nseg == 0) return;
+    if (thin)
+        k_an_model_thin<<<(unsigned)((nw + 32 * ANF_WPB - 1) / (32 * ANF_WPB)), ANF_WPB * 32, 0, s>>>(
+            g, subs, nsub, sbase, ssub, (const double2 *)cs, (const float2 *)csf, (const float4 *)csff, astart,
+            (const int4 *)aseg, nseg, ntot, zq, zqf, wqf, (const float2 *)vef, cd2if, ptabf, mem,
+            (unsigned long long *)out64, mstride);
+    if (!thick) return;
     const size_t smem = an_fast_smem_bytes(g.nz);
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(k_an_model_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_an_model_fast<<<(unsigned)((nw + ANF_WPB - 1) / ANF_WPB), ANF_WPB * 32, smem, s>>>(
         g, subs, nsub, sbase, ssub, (const double2 *)cs, (const float2 *)csf, (const float4 *)csff, astart,
         (const int4 *)aseg, nseg, ntot, zq, zqf, wqf,
-        (const float2 *)vef, cd2if, ptabf, mem, (unsigned long long *)out64, mstride);
+        (const float2 *)vef, cd2if, ptabf, mem, (unsigned long long *)out64, mstride, thin);
 }
 
 void launch_an_maps(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase, const int *ssub,

@@ -190,6 +190,7 @@ struct bbgpu_ctx {
     // ANALYTIC batches: sub-ring constants per member, the sample table of the model's sub-rings, their vertical
     // grids (host cache mirrored on the device) and the fixed-point models
     AnSub *h_asub = nullptr, *d_asub = nullptr;
+    int an_thin = 0, an_thick = 0, an_exact = 1;   // the ANALYTIC kernels the uploaded batch needs
     size_t h_asub_cap = 0, d_asub_cap = 0;
     int *d_asbase = nullptr, *d_assub = nullptr;
     size_t d_asbase_cap = 0, d_assub_cap = 0;
@@ -924,6 +925,17 @@ static int batch_prepare_analytic(bbgpu_ctx *ctx, int nb, int nsub, const double
     if (ctx->want64)
         if ((rc = dgrow(ctx, &ctx->d_model64, &ctx->d_model64_cap, (size_t)nb * ctx->mstride))) return rc;
     if ((rc = dgrow(ctx, &ctx->d_reuse, &ctx->d_reuse_cap, (size_t)nb * (nsub ? nsub : 1)))) return rc;
+    // which ANALYTIC kernels the batch needs: the float32 path of thin sub-rings (one height), of thick ones, the
+    // exact kernel for the others (a reused column is member 0's, whose flags count already)
+    ctx->an_thin = ctx->an_thick = ctx->an_exact = 0;
+    for (size_t i = 0; i < (size_t)nb * nsub; i++) {
+        if (ctx->h_reuse[i]) continue;
+        const AnSub &S = ctx->h_asub[i];
+        if (!S.active) continue;
+        if (!S.anfast) ctx->an_exact = 1;
+        else if (S.nzz == 1) ctx->an_thin = 1;
+        else ctx->an_thick = 1;
+    }
     CK(cudaMemcpyAsync(ctx->d_asub, ctx->h_asub, sizeof(AnSub) * (size_t)nb * nsub, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(ctx->d_mem, ctx->h_mem, sizeof(MemberDev) * (size_t)nb, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(ctx->d_reuse, ctx->h_reuse, (size_t)nb * nsub, cudaMemcpyHostToDevice, ctx->stream));
@@ -1476,12 +1488,14 @@ static int batch_run(bbgpu_ctx *ctx, bool do_resid) {
         launch_an_model_fast(s, g, ctx->d_asub, ctx->nsub, ctx->d_asbase, ctx->d_assub, ctx->d_acs, ctx->d_acsf,
                              (const float *)ctx->d_acsff, ctx->d_astart, ctx->d_aseg, ctx->an_nseg, ctx->an_ntot,
                              ctx->d_azq, ctx->d_azqf, ctx->d_awqf, (const float *)ctx->d_vef, ctx->d_cd2if,
-                             ctx->d_ptabf, ctx->d_mem, ctx->d_model_fx, ctx->mstride);
+                             ctx->d_ptabf, ctx->d_mem, ctx->d_model_fx, ctx->mstride, ctx->an_thin, ctx->an_thick);
         CKL();
-        launch_an_model(s, g, ctx->d_asub, ctx->nsub, ctx->d_asbase, ctx->d_assub, ctx->d_acs, ctx->d_astart,
-                        ctx->d_aseg, ctx->an_nseg, ctx->an_ntot, ctx->d_azq, ctx->d_awq, ctx->d_vedges, ctx->d_cd2i,
-                        ctx->d_ptab, ctx->d_mem, ctx->d_model_fx, ctx->mstride, 1);
-        CKL();
+        if (ctx->an_exact) {
+            launch_an_model(s, g, ctx->d_asub, ctx->nsub, ctx->d_asbase, ctx->d_assub, ctx->d_acs, ctx->d_astart,
+                            ctx->d_aseg, ctx->an_nseg, ctx->an_ntot, ctx->d_azq, ctx->d_awq, ctx->d_vedges,
+                            ctx->d_cd2i, ctx->d_ptab, ctx->d_mem, ctx->d_model_fx, ctx->mstride, 1);
+            CKL();
+        }
         launch_fix_to_model(s, ctx->d_model_fx, ctx->d_mem, ctx->nb, ctx->mstride, g.nz, ctx->d_model,
                             ctx->want64 ? ctx->d_model64 : nullptr, ctx->an_n2 ? ctx->d_mbase : nullptr);
         CKL();

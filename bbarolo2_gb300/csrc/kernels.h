@@ -203,7 +203,8 @@ void launch_an_model_fast(cudaStream_t s, const GridDev &g, const AnSub *subs, i
                           const int *ssub, const double *cs, const float *csf, const float *csff,
                           const long long *astart, const int *aseg, int nseg, long long ntot,
                           const double *zq, const float *zqf, const float *wqf, const float *vef, const float *cd2if,
-                          const float *ptabf, const MemberDev *mem, long long *out64, long long mstride);
+                          const float *ptabf, const MemberDev *mem, long long *out64, long long mstride, int thin,
+                          int thick);
 void launch_an_maps(cudaStream_t s, const GridDev &g, const AnSub *subs, int nsub, const int *sbase, const int *ssub,
                     const double *cs, long long nsamp, const double *zq, const double *wq, const long long *widx,
                     const double *wval, const MemberDev &M, long long *maps64);

@@ -239,6 +239,9 @@ def main():
     ap.add_argument("--no-central", action="store_true", help="skip the 321-point central-difference batch")
     ap.add_argument("--no-bayes", action="store_true",
                     help="skip the 256x256x192 batch of 1024 points and the BAYESIAN fit")
+    ap.add_argument("--bayes-nb", type=int, default=1024,
+                    help="points per launch of the 256x256x192 batch (the BAYESIAN workload: 1024)")
+    ap.add_argument("--no-bayes-fit", action="store_true", help="skip the BAYESIAN fit time (plain and screened)")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the per-variant convolution times and errors")
     ap.add_argument("--no-random", action="store_true",
@@ -373,8 +376,9 @@ def main():
         line["random"] = batch_leg(ctx, L, rings, random_rows(rings, B), args, dist, world)
         line["unshared"] = batch_leg(ctx, L, rings, rows, args, dist, world, share=False)
     if not args.no_bayes:
-        line["bayes256"] = bayes256_leg(args, dist, world)
-        line["bayes_fit"] = bayes_fit_leg()
+        line["bayes256"] = bayes256_leg(args, dist, world, nb=args.bayes_nb)
+        if not args.no_bayes_fit:
+            line["bayes_fit"] = bayes_fit_leg()
     if rank == 0 and not args.no_cpu:
         vals, cores, n = cpu_leg(dm, L, rows, rings, data, mask)
         line["cpu_baseline"] = {"value": float(np.median(vals)), "unit": UNIT, "cores": cores, "kind": "port",
