@@ -93,12 +93,14 @@ class MLP:
 class Surrogate:
     """log L(u) on the unit cube of a sampler, learned from its evaluations (u, log L).
 
-    ``fit(u, logl, center)`` trains on the pairs for ``steps`` Adam steps of minibatches; ``predict(u)`` returns
+    ``fit(u, logl, center)`` trains on the pairs for ``steps`` Adam steps of minibatches (``steps_warm`` after the
+    first fit); ``predict(u)`` returns
     log L (within the fitted window about the center); ``rmse(u, logl)`` the error on pairs it was not fitted on."""
 
-    def __init__(self, ndim, hidden=256, seed=0, device=0, lr=1e-3, steps=150, batch=1024):
+    def __init__(self, ndim, hidden=256, seed=0, device=0, lr=1e-3, steps=150, batch=1024, steps_warm=150):
         self.net = MLP(ndim, hidden, seed, device)
         self.lr, self.steps, self.batch = float(lr), int(steps), int(batch)
+        self.steps_warm = int(steps_warm)
         self.rng = np.random.default_rng(seed)
         self.mu = np.zeros(ndim)
         self.sd = np.ones(ndim)
@@ -120,8 +122,10 @@ class Surrogate:
         self.ymu, self.ysd = float(center), float(scale)
         x = self._x(u)
         t = np.clip((np.asarray(logl, float) - self.ymu) / self.ysd, -1.0, 1.0).astype(np.float32)
-        # the minibatches are drawn on the device: one call for all the steps
-        loss = self.net.train(x, t, self.steps, min(self.batch, len(x)), self.lr, int(self.rng.integers(2 ** 62)))
+        # the minibatches are drawn on the device: one call for all the steps (fewer once warm: the network starts
+        # from the last fit, whose window moved by a fraction of its width since)
+        steps = self.steps_warm if self.trained else self.steps
+        loss = self.net.train(x, t, steps, min(self.batch, len(x)), self.lr, int(self.rng.integers(2 ** 62)))
         self.trained = True
         return loss * self.ysd ** 2
 

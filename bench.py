@@ -142,8 +142,10 @@ def step_rows(rings, batch):
 
 
 # ncu summaries (profiles/) with the DRAM traffic of a kernel's launch at the default batch
+# (the convolution by variant: the float32 kernel and the tensor-core tf32x3 kernel are different launches)
 TRAFFIC = {"mc_deposit": "k_mc_deposit_px.global160_b161.dram.txt", "mc_replay": "mc_replay.global160_b161.dram.txt",
-           "conv_resid": "k_conv_resid.global160_b161.dram.txt"}
+           "conv_resid/f32": "k_conv_resid.global160_b161.dram.txt",
+           "conv_resid/tf32x3": "k_conv_tc.global160_b161.dram.txt"}
 
 
 def measured_traffic(kernel, batch, members=None):
@@ -330,10 +332,11 @@ def main():
     dom = max((k for k in members if k in kt and members[k]), key=kt.get)
     nbytes = alg[dom + "_bytes"](members[dom])
     achieved = nbytes / (kt[dom] * 1e-3) / 1e9
-    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": measured_traffic(dom, B, members[dom]), "kernel": dom, "peak_source": src,
-            "algorithmic_bytes": nbytes, "members": members[dom]}
     used, tune = ctx.conv_variant()
+    tkey = f"{dom}/{_lib.CONV_NAMES[used]}" if dom == "conv_resid" else dom
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": measured_traffic(tkey, B, members[dom]), "kernel": dom, "peak_source": src,
+            "algorithmic_bytes": nbytes, "members": members[dom]}
     if dom == "conv_resid":
         # the convolution's useful arithmetic (2 x taps flop a voxel), and on the tensor cores its fraction of the
         # dense tensor peak (bf16 measured; tf32 runs at half that rate)
