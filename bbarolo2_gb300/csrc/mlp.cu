@@ -16,6 +16,7 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "../../include/bbgpu.h"
@@ -25,6 +26,7 @@ namespace {
 constexpr int GT = 64;       // tile of m and of j
 constexpr int GK = 32;       // chunk of t
 constexpr int GPAD = 8;      // (padding of the shared-memory rows: no bank conflicts on the fragment loads)
+constexpr int KSPLIT = 8;    // K ranges of the weight-gradient products (K = the batch rows)
 
 enum Epi { EPI_BIAS_GELU = 0, EPI_GELU_GRAD = 1, EPI_F32 = 2 };
 
@@ -50,6 +52,11 @@ __global__ void __launch_bounds__(128) k_gemm(int M, int N, int K, const TA *__r
     __shared__ __align__(16) __nv_bfloat16 As[GT][GK + GPAD];
     __shared__ __align__(16) __nv_bfloat16 Bs[GT][GK + GPAD];   // [j][t]
     const int m0 = blockIdx.y * GT, j0 = blockIdx.x * GT;
+    // split K (EPI_F32 only): block z takes the K range [z kper, (z + 1) kper) and writes its partial product to
+    // F32 + z M N (summed in order by k_sum_splits)
+    const int kper = (K + gridDim.z - 1) / gridDim.z;
+    const int tb = blockIdx.z * kper, te = min(K, tb + kper);
+    if (EPI == EPI_F32) F32 += (size_t)blockIdx.z * M * N;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wm = (warp >> 1) * 32, wj = (warp & 1) * 32;
     const int g = lane >> 2, c = lane & 3;
@@ -60,14 +67,14 @@ __global__ void __launch_bounds__(128) k_gemm(int M, int N, int K, const TA *__r
         for (int b = 0; b < 4; b++)
 #pragma unroll
             for (int q = 0; q < 4; q++) acc[a][b][q] = 0.0f;
-    for (int t0 = 0; t0 < K; t0 += GK) {
+    for (int t0 = tb; t0 < te; t0 += GK) {
         for (int e = threadIdx.x; e < GT * GK; e += 128) {
             const int i = e / GK, t = e % GK;
             const int m = m0 + i, j = j0 + i, tt = t0 + t;
-            As[i][t] = (m < M && tt < K) ? elem(A, (long long)m * sam + (long long)tt * sat)
-                                         : __float2bfloat16_rn(0.0f);
-            Bs[i][t] = (j < N && tt < K) ? elem(B, (long long)tt * sbt + (long long)j * sbj)
-                                         : __float2bfloat16_rn(0.0f);
+            As[i][t] = (m < M && tt < te) ? elem(A, (long long)m * sam + (long long)tt * sat)
+                                          : __float2bfloat16_rn(0.0f);
+            Bs[i][t] = (j < N && tt < te) ? elem(B, (long long)tt * sbt + (long long)j * sbj)
+                                          : __float2bfloat16_rn(0.0f);
         }
         __syncthreads();
 #pragma unroll
@@ -178,6 +185,15 @@ __global__ void __launch_bounds__(1024) k_colsum(int n, int N, const float *__re
     }
 }
 
+// out[i] = sum over the splits z (in order) of part[z][i]
+__global__ void k_sum_splits(long long n, int nsplit, const float *__restrict__ part, float *__restrict__ out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float a = part[i];
+    for (int z = 1; z < nsplit; z++) a += part[(size_t)z * n + i];
+    out[i] = a;
+}
+
 __global__ void k_sum(int n, const float *__restrict__ v, float *__restrict__ out) {
     __shared__ float sh[256];
     float s = 0.0f;
@@ -241,6 +257,7 @@ struct bbgpu_mlp {
     __nv_bfloat16 *x16 = nullptr, *a[3] = {}, *dz[2] = {};
     float *z[3] = {}, *dz32[2] = {};
     float *set_x = nullptr, *set_t = nullptr;   // the resident training set of bbgpu_mlp_train
+    float *split = nullptr;                      // the partial weight gradients of a split-K product
     long long set_cap = 0;
     cudaStream_t s = nullptr;
 };
@@ -274,8 +291,8 @@ int grow(bbgpu_mlp *m, int n) {
 
 template <typename TA, typename TB, int EPI>
 void gemm(cudaStream_t s, int M, int N, int K, const TA *A, long long sam, long long sat, const TB *B, long long sbt,
-          long long sbj, const float *bias, float *Z, __nv_bfloat16 *out, float *F32) {
-    dim3 grid((N + GT - 1) / GT, (M + GT - 1) / GT);
+          long long sbj, const float *bias, float *Z, __nv_bfloat16 *out, float *F32, int nsplit = 1) {
+    dim3 grid((N + GT - 1) / GT, (M + GT - 1) / GT, nsplit);
     k_gemm<TA, TB, EPI><<<grid, 128, 0, s>>>(M, N, K, A, sam, sat, B, sbt, sbj, bias, Z, out, F32);
 }
 
@@ -308,8 +325,14 @@ void backward(bbgpu_mlp *m, int n) {
         const __nv_bfloat16 *below = l > 0 ? m->a[l - 1] : m->x16;
         const int kin = l > 0 ? H : d;
         // weight gradient: G[j][k] = sum_b dz[b][j] below[b][k]; bias gradient: column sums of dz
+        // (K = the batch rows: split in KSPLIT ranges, the partial products summed in order)
+        const int ns = std::max(1, std::min(KSPLIT, n / 128));
         gemm<__nv_bfloat16, __nv_bfloat16, EPI_F32>(m->s, H, kin, n, m->dz[cur], 1, H, below, kin, 1, nullptr,
-                                                    nullptr, nullptr, G + m->off[2 * l]);
+                                                    nullptr, nullptr, ns > 1 ? m->split : G + m->off[2 * l], ns);
+        if (ns > 1) {
+            const long long nn = (long long)H * kin;
+            k_sum_splits<<<(unsigned)((nn + 255) / 256), 256, 0, m->s>>>(nn, ns, m->split, G + m->off[2 * l]);
+        }
         k_colsum<<<(H + 31) / 32, 1024, 0, m->s>>>(n, H, m->dz32[cur], nullptr, nullptr, G + m->off[2 * l + 1]);
         if (l > 0)   // the layer below: dz'[b][k] = (sum_j dz[b][j] W[j][k]) gelu'(z'[b][k])
             gemm<__nv_bfloat16, __nv_bfloat16, EPI_GELU_GRAD>(m->s, n, H, H, m->dz[cur], H, 1, W + m->off[2 * l], H,
@@ -372,6 +395,7 @@ extern "C" int bbgpu_mlp_create(bbgpu_mlp **out, int device, int d_in, int hidde
               cudaMalloc(&m->m1, sizeof(float) * m->np) == cudaSuccess &&
               cudaMalloc(&m->m2, sizeof(float) * m->np) == cudaSuccess &&
               cudaMalloc(&m->w16, sizeof(__nv_bfloat16) * m->np) == cudaSuccess &&
+              cudaMalloc(&m->split, sizeof(float) * KSPLIT * (size_t)hidden * std::max(hidden, d_in)) == cudaSuccess &&
               cudaMalloc(&m->loss, sizeof(float)) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
@@ -394,7 +418,7 @@ extern "C" int bbgpu_mlp_destroy(bbgpu_mlp *m) {
     cudaFree(m->xf); cudaFree(m->t); cudaFree(m->y); cudaFree(m->dy); cudaFree(m->x16);
     for (int i = 0; i < 3; i++) { cudaFree(m->a[i]); cudaFree(m->z[i]); }
     for (int i = 0; i < 2; i++) { cudaFree(m->dz[i]); cudaFree(m->dz32[i]); }
-    cudaFree(m->set_x); cudaFree(m->set_t);
+    cudaFree(m->set_x); cudaFree(m->set_t); cudaFree(m->split);
     if (m->s) cudaStreamDestroy(m->s);
     delete m;
     return BBGPU_OK;
