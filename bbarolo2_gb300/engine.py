@@ -434,8 +434,34 @@ class BatchLikelihood:
     def evaluate(self, rows, proto, seed=None, galmodtype=None):
         """log L of each ring set (rows (B, 17, nr) in RING_KEYS order, radii and options as proto)."""
         sr, nv, descs, boxes = self.prepare(rows, proto, seed)
-        ss, lg = self.run(sr, nv, descs, galmodtype)
+        try:
+            ss, lg = self.run(sr, nv, descs, galmodtype)
+        except _lib.DeviceError as e:
+            if self._prof is None or "changed the MC cloud layout" not in str(e):
+                raise
+            return self._evaluate_split(rows, proto, seed, galmodtype)
         return self.finish(ss, lg, boxes)
+
+    def _evaluate_split(self, rows, proto, seed, galmodtype):
+        """A batch whose recomputed density profile changed the MC cloud layout of a member (a ring at zero, or
+        above the 10-clouds-per-pixel floor: the batch's layout, set up from the members' DENS, no longer holds).
+        Its halves are evaluated apart, down to single members; a single member whose layout changes is evaluated
+        with the profile's densities as its DENS and no profile, which is the reference's evaluation: its model is
+        built from the rings whose DENS the profile has set (``bbarolo/bayesian/density.py:13-25``,
+        ``bbarolo/bayesian/likelihood.py:595-596``), and so are its clouds."""
+        rows = np.asarray(rows, float)
+        if len(rows) > 1:
+            h = len(rows) // 2
+            return np.concatenate([self.evaluate(rows[:h], proto, seed, galmodtype),
+                                   self.evaluate(rows[h:], proto, seed, galmodtype)])
+        x, _ = self.last_profile()
+        own = rows.copy()
+        own[0, RING_KEYS.index("dens")] = x[0, :self._prof["nr"]]
+        prof, self._prof = self._prof, None
+        try:
+            return self.evaluate(own, proto, seed, galmodtype)
+        finally:
+            self._prof = prof
 
     def run(self, sr, nv, descs, galmodtype=None):
         dm = self.model

@@ -72,3 +72,21 @@ def test_global_fit_geo_as_good_as_reference(gpu_lib, oracle_lib):
           "at the reference's fits", np.round(ref_ll, 3), "likelihoods", res.nfev, "time", round(res.time, 3), "s")
     assert dev_ll >= min(ref_ll) - 1.0, (dev_ll, ref_ll)
     assert np.all(np.abs(dx) <= 4.0), dx
+
+
+def test_bayesian_posterior_matches_reference_laplace(gpu_lib, oracle_lib):
+    """BAYESIAN on the "kin" problem (a smooth, nearly Gaussian likelihood with uniform priors): the device sampler's
+    posterior medians within 0.1 sigma of the reference's GLOBAL best fit and its spreads within 10% of the
+    reference's Laplace errors (the posterior of a Gaussian likelihood under flat priors is centred on the maximum
+    with those widths; the sampler's Monte Carlo noise with 400 live points is a few hundredths of sigma)."""
+    from bbarolo2_gb300 import bayesian
+    P, like, prob = _device_fit("kin")
+    ref = load("global.npz")
+    res = bayesian.fit(like, prob, n_live=400, n_batch=1024, dlogz=0.1, seed=3, galmodtype="ANALYTIC")
+    err = ref["kin/errors"]
+    dm = (res["theta_median"] - ref["kin/x"]) / err
+    ds = res["theta_std"] / err
+    print("BAYESIAN kin: (median - x_ref) / sigma_ref", np.round(dm, 3), "std / sigma_ref", np.round(ds, 3),
+          "likelihoods", res["n_like"], "wall", round(res["wall"], 2), "s")
+    assert np.all(np.abs(dm) <= 0.1), dm
+    assert np.all(np.abs(ds - 1.0) <= 0.1), ds

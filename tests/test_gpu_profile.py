@@ -84,9 +84,9 @@ def test_ring_maps_fixture(gpu_lib):
         assert np.abs(K - ref).max() <= MAP_TOL * np.abs(ref).max(), mode
 
 
-def _batch_workload(B=5):
-    """A 64x64x64 MC fit with a sech2 layer: the mock, its likelihood and B ring sets (base + steps of INC, PA,
-    VROT: the geometry is free, so the profile changes with each member)."""
+def _batch_workload(B=5, bright=1.0):
+    """A 64x64x64 MC fit with a sech2 layer: the mock (its flux times `bright`), its likelihood and B ring sets
+    (base + steps of INC, PA, VROT: the geometry is free, so the profile changes with each member)."""
     from bbarolo2_gb300 import engine
     from bbarolo2_gb300.galmod import ring_rows_batch
     from golden.cases import cube64, rings64
@@ -97,7 +97,7 @@ def _batch_workload(B=5):
     truth = dm.array(rings, seed=1)
     rms = 0.01 * float(truth.max())
     g = np.random.default_rng(4)
-    data = (truth + dm.convolve_planes(g.normal(0., rms, truth.shape)) * 3.).astype(np.float32)
+    data = (bright * truth + dm.convolve_planes(g.normal(0., rms, truth.shape)) * 3.).astype(np.float32)
     mask = truth > 0.02 * truth.max()
     L = engine.BatchLikelihood(dm, data, mask, maskmode=2, sigma=rms)
     mom0, mrms, ok = L.data_maps()
@@ -190,3 +190,22 @@ def test_batch_profile_shared_members(gpu_lib, oracle_lib, galmodtype):
     ll2 = L.evaluate(rows[::-1].copy(), rings, seed=1, galmodtype=galmodtype)
     x2, _ = L.last_profile()
     np.testing.assert_array_equal(x2, x[::-1])
+
+
+def test_batch_profile_changes_mc_layout(gpu_lib, oracle_lib):
+    """Data three times brighter than the rings' DENS (8 clouds per pixel of ring area, under the floor of 10): the
+    deconvolved profile lifts the densities above the floor, so the members' cloud counts are not those of the
+    batch's layout. The batch falls back to evaluating each such member with the profile's densities as its DENS,
+    the reference's model: log L against the oracle pipeline, which builds each member's sub-rings from its profile."""
+    from oracle import cpu_baseline as CB
+    dm, L, rings, rows, data = _batch_workload(B=4, bright=3.0)
+    ll = L.evaluate(rows, rings, seed=1)
+    sr, nv, descs, boxes = L.prepare(rows, rings, seed=1)
+    P = CB.setup_payload(dm, sr, nv, boxes, 1, data, L.mask, L.maskmode, like=L, rows=rows, proto=rings)
+    CB._W.clear()
+    CB._W.update(P)
+    for k in range(len(rows)):
+        x = CB.profile_dens(k)
+        assert x[:rings.nr].max() * 10 > 10, x            # (above the floor: another layout)
+        ll_ref = L.finish(np.array([CB.evaluate(k)]), np.zeros(1), [boxes[k]])[0]
+        assert abs(ll[k] - ll_ref) <= SS_RTOL * abs(ll_ref), (k, ll[k], ll_ref)
