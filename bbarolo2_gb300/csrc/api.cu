@@ -223,6 +223,7 @@ struct bbgpu_ctx {
     size_t d_bimg_cap = 0;
     int bimg_variant = 0;
     CUtensorMap *d_tmaps = nullptr;       // per member: TMA descriptor of its model
+    int *d_tcq = nullptr;                 // the next work item of a tensor-core convolution launch
     size_t d_tmaps_cap = 0;
     std::vector<CUtensorMap> h_tmaps;
     std::vector<long long> tmaps_key;     // (model, mstride, nz, boxes) of the descriptors on the device
@@ -505,7 +506,7 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
     cudaFree(ctx->d_sub); cudaFree(ctx->d_mem); cudaFree(ctx->d_pix); cudaFree(ctx->d_bucket);
     cudaFree(ctx->d_tcount); cudaFree(ctx->d_toff); cudaFree(ctx->d_tcur); cudaFree(ctx->d_model); cudaFree(ctx->d_scan);
     cudaFree(ctx->d_smooth); cudaFree(ctx->d_model64); cudaFree(ctx->d_partial); cudaFree(ctx->d_out2);
-    cudaFree(ctx->d_bimg); cudaFree(ctx->d_tmaps);
+    cudaFree(ctx->d_bimg); cudaFree(ctx->d_tmaps); cudaFree(ctx->d_tcq);
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
     cudaFree(ctx->d_err);
     for (void *q : {(void *)ctx->d_ppix, (void *)ctx->d_lc, (void *)ctx->d_ord, (void *)ctx->d_p0, (void *)ctx->d_ent,
@@ -1439,9 +1440,11 @@ static int conv_run(bbgpu_ctx *ctx, cudaStream_t s, int v, bool conv, bool do_re
         ctx->tmaps_key = key;
     }
     const int npart = conv_tc_npart(ctx->mem_host.data(), ctx->nb, g.nz);
+    if (!ctx->d_tcq) CK(cudaMalloc(&ctx->d_tcq, sizeof(int)));
     CK(cudaMemsetAsync(ctx->d_partial, 0, sizeof(double) * 2 * (size_t)ctx->nb * npart, s));
     launch_conv_tc(s, v, g, ctx->d_mem, ctx->mem_host.data(), ctx->nb, ctx->d_tmaps, ctx->d_bimg, ctx->mstride, g.nz,
-                   ctx->ky, ctx->kx, smoothed, 1, do_resid ? 1 : 0, ctx->d_partial, npart, ts, ctx->d_err);
+                   ctx->ky, ctx->kx, smoothed, 1, do_resid ? 1 : 0, ctx->d_partial, npart, ts, ctx->d_err,
+                   ctx->d_tcq);
     CKL();
     ctx->npart_used = npart;
     ctx->conv_used = v;

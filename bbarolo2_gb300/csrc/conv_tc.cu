@@ -19,7 +19,8 @@
 // ah bh + ah bl + al bh in FP32 accumulation (dropped al bl and the splits' remainders: ~2^-17 relative per
 // product). TF32X3: the same with tf32 halves (~2^-21). Both are compared per voxel with the float64 oracle.
 //
-// Pipeline (persistent CTAs, one per SM, 19 warps; each CTA walks its work items, a strip or a run of its tiles):
+// Pipeline (persistent CTAs, one per SM, 19 warps; each CTA takes work items, a strip or a run of its tiles, from a
+// counter of the launch as it finishes the previous ones, so that the CTAs end together):
 // warp 0 issues TMA loads of each input row (8-pixel boxes of 128 channels, zero fill outside the box; with a tile
 // table each box from the member whose model holds that deposit tile) into float32 staging stages; warps 2-9 split
 // the staged row into the hi/lo operand stage (K-major canonical layout, no swizzle; two warps per 32 channels, a
@@ -60,6 +61,7 @@ constexpr int TC_MAX_TILES = 16;   // 16-row tiles of a work item
 constexpr int BOX_PX = 8;          // pixels of a TMA box of the model
 constexpr int BOX_BYTES = BOX_PX * TC_M * 4;
 constexpr int DBOX_BYTES = TC_X * TC_M * 4;   // a data row of the strip
+constexpr int ITQ = 8;             // slots of the ring that passes the CTA's work items to its warps
 
 struct TcArgs {
     GridDev g;
@@ -79,6 +81,7 @@ struct TcArgs {
     int npart;
     TileSrc ts;
     int *err;
+    int *queue;                    // the launch's next work item (zeroed before the launch)
     unsigned fstage, astage, aop, bop, sbo_a, sbo_b;   // layout (bytes)
 };
 
@@ -266,10 +269,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
     uint64_t *full_f = bars, *empty_f = full_f + NFS, *full_a = empty_f + NFS, *empty_a = full_a + NAS;
     uint64_t *full_d = empty_a + NAS, *empty_d = full_d + NDS;
     uint64_t *ready = empty_d + NDS, *freeb = ready + TC_RING, *fin = freeb + TC_RING;
-    int *misc = (int *)(fin + 1);
+    uint64_t *itq_full = fin + 1, *itq_empty = itq_full + ITQ;
+    int *misc = (int *)(itq_empty + ITQ);
     volatile int *abort_flag = misc;                         // [0]
     volatile uint32_t *tmem_hold = (volatile uint32_t *)(misc + 1);
     volatile uint8_t *rowflag = (volatile uint8_t *)(misc + 2);   // NAS x 8 bytes (per splitting warp)
+    volatile int *itq = misc + 8;                                 // ITQ work items
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < NFS; i++) { mbar_init(&full_f[i], 1); mbar_init(&empty_f[i], 8); }
@@ -277,6 +282,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
         for (int i = 0; i < NDS; i++) { mbar_init(&full_d[i], 1); mbar_init(&empty_d[i], EPW); }
         for (int i = 0; i < TC_RING; i++) { mbar_init(&ready[i], 1); mbar_init(&freeb[i], EPW); }
         mbar_init(fin, 1);
+        for (int i = 0; i < ITQ; i++) { mbar_init(&itq_full[i], 1); mbar_init(&itq_empty[i], TC_THREADS / 32 - 1); }
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -307,11 +313,40 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
     int *err = a.err;
     const int ky = a.ky, hy = a.hy;
     const int nitems = a.nitems;
+    // The CTA's work items, taken one at a time from the launch's counter (the CTAs that finish early take more:
+    // the items' costs differ, e.g. the tiles a member shares with member 0 are skipped): warp 0 takes item q and
+    // puts it in slot q mod ITQ of a ring, the other 18 warps read the slots in order (item -1: no more). Warp-uniform.
+    auto next_item = [&](uint32_t q, bool &ok) -> int {
+        int idx = -1;
+        if (lane == 0 && ok) {
+            const int sl = (int)(q % ITQ);
+            if (warp == 0) {
+                if (q >= ITQ) ok = mbar_wait(&itq_empty[sl], ((q / ITQ) - 1) & 1, abort_flag, err);
+                if (ok) {
+                    const int v = atomicAdd(a.queue, 1);
+                    idx = v < nitems ? v : -1;
+                    itq[sl] = idx;
+                    mbar_arrive(&itq_full[sl]);
+                }
+            } else {
+                ok = mbar_wait(&itq_full[sl], (q / ITQ) & 1, abort_flag, err);
+                if (ok) {
+                    idx = itq[sl];
+                    mbar_arrive(&itq_empty[sl]);
+                }
+            }
+        }
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        idx = __shfl_sync(0xffffffffu, idx, 0);
+        return ok ? idx : -1;
+    };
     if (warp == 0) {
         // ---------------------------------------------------------------- TMA: input rows of the model
         uint32_t gf = 0;
         bool ok = true;
-        for (int idx = blockIdx.x; ok && idx < nitems; idx += gridDim.x) {
+        for (uint32_t q = 0; ok; q++) {
+            const int idx = next_item(q, ok);
+            if (idx < 0) break;
             const Item it = item_of(a, idx);
             if (!it.valid) continue;
             const unsigned skip = skip_mask(a, it, lane, -1);
@@ -357,7 +392,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
         // ---------------------------------------------------------------- TMA: data rows of the residual
         uint32_t gd = 0;
         bool ok = true;
-        for (int idx = blockIdx.x; ok && idx < nitems; idx += gridDim.x) {
+        for (uint32_t q = 0; ok; q++) {
+            const int idx = next_item(q, ok);
+            if (idx < 0) break;
             const Item it = item_of(a, idx);
             if (!it.valid) continue;
             const unsigned skip = skip_mask(a, it, lane, -1);
@@ -398,7 +435,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
         // low field is the shared-memory address / 16; every address stays below 256 KB, so nothing carries out)
         const uint64_t dA0 = sdesc(saddr(ast), 128, a.sbo_a), dB0 = sdesc(saddr(bsm), 128, a.sbo_b);
         const uint64_t astg16 = a.astage >> 4, aop16 = a.aop >> 4, bop16 = a.bop >> 4, sbob16 = a.sbo_b >> 4;
-        for (int idx = blockIdx.x; ok && idx < nitems; idx += gridDim.x) {
+        for (uint32_t q = 0; ok; q++) {
+            const int idx = next_item(q, ok);
+            if (idx < 0) break;
             const Item it = item_of(a, idx);
             if (!it.valid) continue;
             const unsigned skip = skip_mask(a, it, lane, -1);
@@ -462,7 +501,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
         const int sw = warp - 2, cg = sw & 3, half = sw >> 2, ch = cg * 32 + lane;
         uint32_t gf = 0, ga = 0;
         bool ok = true;
-        for (int idx = blockIdx.x; ok && idx < nitems; idx += gridDim.x) {
+        for (uint32_t q = 0; ok; q++) {
+            const int idx = next_item(q, ok);
+            if (idx < 0) break;
             const Item it = item_of(a, idx);
             if (!it.valid) continue;
             const unsigned skip = skip_mask(a, it, lane, -1);
@@ -547,7 +588,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv_tc(const __grid_constant
         const float scale = (float)a.g.scalefactor;
         uint32_t vbase = 0, gd = 0;
         bool ok = true;
-        for (int idx = blockIdx.x; ok && idx < nitems; idx += gridDim.x) {
+        for (uint32_t q = 0; ok; q++) {
+            const int idx = next_item(q, ok);
+            if (idx < 0) break;
             const Item it = item_of(a, idx);
             if (!it.valid) continue;
             const unsigned skip = skip_mask(a, it, lane, ep);
@@ -726,7 +769,7 @@ TcLayout tc_layout(int variant, int ky, int kx) {
     L.fstage = (unsigned)L.nbox * BOX_BYTES;
     // K steps of 32 bytes that cover the used pixels (16 bf16 or 8 tf32 each)
     L.nks = variant == 1 ? (L.wused + 15) / 16 : (L.wused + 7) / 8;
-    const size_t bars = (2 * NFS + 2 * NAS + 2 * NDS + 2 * TC_RING + 1) * 8;
+    const size_t bars = (2 * NFS + 2 * NAS + 2 * NDS + 2 * TC_RING + 1 + 2 * ITQ) * 8;
     L.smem = 1024 + NFS * (size_t)L.fstage + NAS * (size_t)L.astage + ((L.bbytes + 127) & ~127u) +
              NDS * (size_t)DBOX_BYTES + bars + 32 * 4;
     return L;
@@ -815,7 +858,8 @@ int conv_tc_npart(const MemberDev *mem_host, int nb, int nz) {
 // conv_tc_npart; the caller zeroes them first). maps: device copies of conv_tc_maps; bimg: conv_tc_image.
 void launch_conv_tc(cudaStream_t s, int variant, const GridDev &g, const MemberDev *mem, const MemberDev *mem_host,
                     int nb, const CUtensorMap *maps, const void *bimg, long long mstride, int nz, int ky, int kx,
-                    float *smoothed, int do_conv, int do_resid, double *partial, int npart, TileSrc ts, int *err) {
+                    float *smoothed, int do_conv, int do_resid, double *partial, int npart, TileSrc ts, int *err,
+                    int *queue) {
     const TcLayout L = tc_layout(variant, ky, kx);
     int ntxg = 0, ntyg = 0;
     for (int k = 0; k < nb; k++) {
@@ -855,8 +899,10 @@ void launch_conv_tc(cudaStream_t s, int variant, const GridDev &g, const MemberD
     a.npart = npart;
     a.ts = ts;
     a.err = err;
+    a.queue = queue;
     a.fstage = L.fstage; a.astage = L.astage; a.aop = L.aop; a.bop = L.bop; a.sbo_a = L.sbo_a; a.sbo_b = L.sbo_b;
     dim3 grid(std::min(a.nitems, nsm));
+    cudaMemsetAsync(queue, 0, sizeof(int), s);
 #define TC_CASE(V, KP)                                                                                           \
     {                                                                                                            \
         static size_t configured = 0;                                                                            \

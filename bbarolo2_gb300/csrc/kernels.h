@@ -160,7 +160,8 @@ bool conv_tc_maps(const MemberDev *mem_host, int nb, const float *model, long lo
 int conv_tc_npart(const MemberDev *mem_host, int nb, int nz);
 void launch_conv_tc(cudaStream_t s, int variant, const GridDev &g, const MemberDev *mem, const MemberDev *mem_host,
                     int nb, const CUtensorMap *maps, const void *bimg, long long mstride, int nz, int ky, int kx,
-                    float *smoothed, int do_conv, int do_resid, double *partial, int npart, TileSrc ts, int *err);
+                    float *smoothed, int do_conv, int do_resid, double *partial, int npart, TileSrc ts, int *err,
+                    int *queue);
 
 // ---- layouts and stand-alone residuals (resid.cu)
 void launch_prep_deff(cudaStream_t s, const float *data, const uint8_t *mask, const uint8_t *region, int maskmode,
