@@ -199,12 +199,31 @@ __global__ void k_prof_gather(const double *__restrict__ xu, const int *__restri
 
 // ------------------------------------------------------------------------------------------- Gram matrix
 // CTA (tile of GRAM_TP used pixels, member k). Entry e < n(n+1)/2: G[i][j] (i <= j, row-major packed upper),
-// then h[i]. The tile is staged in shared memory as float64 (the maps and the maps times the pixel weights) with
-// the range of rings not zero at each pixel, so that each product is one float64 FMA over the band of rings that
-// overlap there; the entries outside the union of the tile's bands (the used pixels come in compact blocks, so
+// then h[i]. The tile is staged in shared memory with the range of rings not zero at each pixel, so that each entry
+// sums its products over the band of rings that overlap there. Float32 maps: the maps as they are, the maps times
+// the pixel weights and the weighted data in float-float (hi + lo, about 46 bits), each product of a float-float and
+// a float32 map and its sum carried in float-float with error-free transformations (float32 units, no float64
+// pipe), the tile's sum converted to float64 at the end; float64 maps: float64 FMAs; the entries outside the union of the tile's bands (the used pixels come in compact blocks, so
 // the union is narrow) are zero without a loop. Partial sums per tile, summed over the tiles in order by
 // k_prof_gram_reduce.
 // pix == nullptr: the pixels 0 .. npix_used - 1; wpix == nullptr: unit weights.
+// s = sh + sl += (xh + xl) b: the product by TwoProduct (the float32 product and its exact error) plus xl b, the
+// sum by TwoSum (operations rounded one by one: no contraction)
+__device__ __forceinline__ void ff_madd(float &sh, float &sl, float xh, float xl, float b) {
+    const float p = __fmul_rn(xh, b);
+    float e = __fmaf_rn(xh, b, -p);
+    e = __fmaf_rn(xl, b, e);
+    const float s = __fadd_rn(sh, p);
+    const float z = __fsub_rn(s, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, z)), __fsub_rn(p, z));
+    sh = s;
+    sl = __fadd_rn(sl, __fadd_rn(err, e));
+}
+
+__device__ __forceinline__ void out_entry(double *part, int k, int t, int nent, int e, double v) {
+    part[((size_t)k * gridDim.x + t) * nent + e] = v;
+}
+
 template <class T>
 __global__ void __launch_bounds__(256) k_prof_gram(const T *__restrict__ K, ProfBox box, const int *__restrict__ pix,
                                                    const double *__restrict__ wpix, const double *__restrict__ wy,
@@ -213,10 +232,14 @@ __global__ void __launch_bounds__(256) k_prof_gram(const T *__restrict__ K, Prof
                                                    double *__restrict__ part, KRows kr) {
     extern __shared__ double gsm[];
     const int n = box.nrp;
+    constexpr bool FF = sizeof(T) == 4;
     double *Kd = gsm;                                       // GRAM_TP x n maps
     double *Kw = Kd + GRAM_TP * n;                          // GRAM_TP x n maps x pixel weight
     double *wys = Kw + GRAM_TP * n;                         // GRAM_TP weighted data
-    int *lo = (int *)(wys + GRAM_TP), *hi = lo + GRAM_TP;   // rings not zero at the pixel: lo .. hi
+    float *Kf = (float *)gsm;                               // (FF: the maps; maps x weight, hi and lo; data, hi, lo)
+    float *Kwh = Kf + GRAM_TP * n, *Kwl = Kwh + GRAM_TP * n;
+    float *wyh = Kwl + GRAM_TP * n, *wyl = wyh + GRAM_TP;
+    int *lo = FF ? (int *)(wyl + GRAM_TP) : (int *)(wys + GRAM_TP), *hi = lo + GRAM_TP;   // rings not zero: lo .. hi
     __shared__ int srow[GRAM_TP];                           // the row whose K holds each pixel
     const int k = blockIdx.y, t = blockIdx.x;
     const int p0 = t * GRAM_TP;
@@ -259,11 +282,30 @@ __global__ void __launch_bounds__(256) k_prof_gram(const T *__restrict__ K, Prof
     for (int i = threadIdx.x; i < np * n; i += blockDim.x) {
         const int pp = i / n, r = i - pp * n;
         const long long q = pix ? pix[p0 + pp] : p0 + pp;
-        const double v = (double)K[((size_t)srow[pp] * box.npix + q) * n + r];
-        Kd[i] = v;
-        Kw[i] = v * (wpix ? wpix[p0 + pp] : 1.0);
+        const T kv = K[((size_t)srow[pp] * box.npix + q) * n + r];
+        const double w = wpix ? wpix[p0 + pp] : 1.0;
+        if constexpr (FF) {
+            // kv x w in float-float: kv x wh exactly (TwoProduct), plus kv x wl rounded
+            const float wh = (float)w, wl = (float)(w - (double)wh);
+            const float ph = __fmul_rn(kv, wh);
+            Kf[i] = kv;
+            Kwh[i] = ph;
+            Kwl[i] = __fadd_rn(__fmaf_rn(kv, wh, -ph), __fmul_rn(kv, wl));
+        } else {
+            Kd[i] = (double)kv;
+            Kw[i] = (double)kv * w;
+        }
     }
-    for (int i = threadIdx.x; i < np; i += blockDim.x) wys[i] = wy[p0 + i];
+    for (int i = threadIdx.x; i < np; i += blockDim.x) {
+        if constexpr (FF) {
+            const double y = wy[p0 + i];
+            const float yh = (float)y;
+            wyh[i] = yh;
+            wyl[i] = (float)(y - (double)yh);
+        } else {
+            wys[i] = wy[p0 + i];
+        }
+    }
     __syncthreads();
     __shared__ int band[2];                                 // the tile's rings: band[0] .. band[1]
     if (threadIdx.x == 0) { band[0] = n; band[1] = -1; }
@@ -271,7 +313,7 @@ __global__ void __launch_bounds__(256) k_prof_gram(const T *__restrict__ K, Prof
     for (int pp = threadIdx.x; pp < np; pp += blockDim.x) {
         int a = n, b = -1;
         for (int r = 0; r < n; r++)
-            if (Kd[pp * n + r] != 0.0) {
+            if (FF ? Kf[pp * n + r] != 0.0f : Kd[pp * n + r] != 0.0) {
                 a = min(a, r);
                 b = r;
             }
@@ -288,6 +330,21 @@ __global__ void __launch_bounds__(256) k_prof_gram(const T *__restrict__ K, Prof
     for (int e = threadIdx.x; e < nent; e += blockDim.x) {
         const int i = ent_i[e], j = ent_j[e];
         double acc = 0.0;
+        if constexpr (FF) {
+            float sh = 0.0f, sl = 0.0f;
+            if (j >= 0) {
+                if (i >= blo && j <= bhi)
+                    for (int pp = 0; pp < np; pp++)
+                        if (lo[pp] <= i && j <= hi[pp])
+                            ff_madd(sh, sl, Kwh[pp * n + i], Kwl[pp * n + i], Kf[pp * n + j]);
+            } else {
+                if (i >= blo && i <= bhi)
+                    for (int pp = 0; pp < np; pp++)
+                        if (lo[pp] <= i && i <= hi[pp]) ff_madd(sh, sl, wyh[pp], wyl[pp], Kf[pp * n + i]);
+            }
+            out_entry(part, k, t, nent, e, (double)sh + (double)sl);
+            continue;
+        }
         if (j >= 0) {
             if (i >= blo && j <= bhi)                       // (an entry outside the tile's rings sums to zero)
                 for (int pp = 0; pp < np; pp++)
@@ -818,7 +875,9 @@ static void prof_gram(cudaStream_t s, const T *K, const ProfBox &box, const int 
                       double *part, double *gh, KRows kr) {
     const int nt = prof_gram_tiles(npix_used);
     if (nb == 0 || nt == 0) return;
-    const size_t smem = (size_t)(2 * GRAM_TP * box.nrp + GRAM_TP) * sizeof(double) + 2 * GRAM_TP * sizeof(int);
+    const size_t smem = sizeof(T) == 4
+                            ? (size_t)(3 * GRAM_TP * box.nrp + 2 * GRAM_TP) * sizeof(float) + 2 * GRAM_TP * sizeof(int)
+                            : (size_t)(2 * GRAM_TP * box.nrp + GRAM_TP) * sizeof(double) + 2 * GRAM_TP * sizeof(int);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_prof_gram<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_prof_gram<T><<<dim3(nt, nb), 256, smem, s>>>(K, box, pix, wpix, wy, npix_used, ent_i, ent_j, nent, part, kr);
     k_prof_gram_reduce<<<dim3((nent + 127) / 128, nb), 128, 0, s>>>(part, nt, nent, gh, kr.ktab ? kr.gflag : nullptr);
