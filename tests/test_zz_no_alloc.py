@@ -1,7 +1,6 @@
 """The allocation-free residual entry point (bbgpu_sumsq_residuals_noalloc) against the allocating one.
 
-Callers that may not allocate device memory (their own pool, a stream being captured into a graph, a fixed
-footprint) pass device buffers; the entry point keeps its partial sums in a scratch array of the library. Two
+Callers that may not allocate device memory (their own pool, a fixed footprint) pass device buffers; the entry point keeps its partial sums in a scratch array of the library. Two
 calls in a row must give the sums of bbgpu_sumsq_residuals / bbgpu_residuals_fracerr (same voxels, float64;
 only the summation order differs). This file is collected last: it runs alone or after the other tests."""
 import numpy as np
@@ -80,3 +79,29 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(gpu_lib):
         rc = L.bbgpu_sumsq_residuals_noalloc(a.data_ptr(), b.data_ptr(), None, 0, None, 2, 2, 2, 1.0, eps2,
                                              out.data_ptr(), None)
         assert rc == _lib.ERR_ARG, eps2
+
+
+def test_noalloc_edge_sizes(gpu_lib):
+    """No voxels: the sums are zero (written by the final kernel alone); exactly as many voxels as the scratch array
+    holds sums for (4096 blocks of 4096): accepted, and equal to the allocating entry point."""
+    torch = pytest.importorskip("torch")
+    from bbarolo2_gb300 import _lib
+    L = _lib.load()
+    a = torch.zeros(8, dtype=torch.float64, device="cuda")
+    b = torch.zeros(8, dtype=torch.float32, device="cuda")
+    out = torch.full((2,), 7.0, dtype=torch.float64, device="cuda")
+    rc = L.bbgpu_sumsq_residuals_noalloc(a.data_ptr(), b.data_ptr(), None, 0, None, 0, 64, 64, 1.0, 0.0,
+                                         out.data_ptr(), None)
+    assert rc == _lib.OK
+    torch.cuda.synchronize()
+    assert out.cpu().numpy().tolist() == [0.0, 0.0]
+    nz, ny, nx = 1024, 128, 128                          # 16,777,216 voxels
+    g = torch.Generator(device="cuda").manual_seed(5)
+    model = torch.rand((nz, ny, nx), dtype=torch.float64, device="cuda", generator=g)
+    data = (model + 0.1 * torch.randn((nz, ny, nx), dtype=torch.float64, device="cuda", generator=g)).float()
+    rc = L.bbgpu_sumsq_residuals_noalloc(model.data_ptr(), data.data_ptr(), None, 0, None, nz, ny, nx, 1.0, 0.0,
+                                         out.data_ptr(), None)
+    assert rc == _lib.OK
+    torch.cuda.synchronize()
+    ref = float(((data.double() - model) ** 2).sum())
+    assert abs(float(out[0]) - ref) <= 1e-10 * ref, (float(out[0]), ref)
