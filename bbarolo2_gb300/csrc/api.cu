@@ -22,7 +22,8 @@
 #include "kernels.h"
 
 #define BBGPU_VERSION 1
-#define NLAYOUT 4
+#define NLAYOUT 64                          // cached MC layouts (the single-ring models of a CLASSIC stage have one each)
+#define LAYOUT_BUDGET (1ll << 31)           // device bytes the cached layouts may hold (least recently used evicted)
 #define NTIMER 13
 
 // the timed stages of a batch: the flux normalisation (ring maps, their beam convolution, the normal equations,
@@ -34,10 +35,16 @@ static const char *KNAMES[NTIMER] = {"prof_maps", "prof_conv",  "prof_gram",  "p
                                      "mc_deposit_delta", "mc_replay", "an_model", "conv_resid",
                                      "reduce_partials"};
 
+struct PoolBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+};
+
 struct LayoutEntry {
     LayoutHost host;
     LayoutDev dev;
     double zspan = 0.0;           // largest spread (max - min) of one cloud's normal deviates
+    long long bytes = 0;          // device bytes of the layout
     bool valid = false;
     long long last_use = 0;
 };
@@ -71,6 +78,7 @@ struct bbgpu_ctx {
     LayoutEntry layouts[NLAYOUT];
     long long use_clock = 0;
     LayoutEntry *cur = nullptr;
+    std::vector<PoolBuf> pool[8];       // the scratch buffers of the stand-alone calls (DevBufs), per call site
     // batch
     int nb = 0, nsub = 0, galmodtype = 0, tx = 8, ty = 8, ntile_total = 0, npart = 0;
     bool uploaded = false, ran = false;
@@ -407,16 +415,41 @@ static int get_layout(bbgpu_ctx *ctx, uint64_t seed, int nsub, const int *nc, co
         }
         if (!E.valid || E.last_use < victim->last_use) victim = &E;
     }
-    if (victim->valid) {
+    // room: the least recently used slot, and more while the cached layouts hold more than the budget
+    auto evict = [&](LayoutEntry &E) -> int {
         CK(cudaStreamSynchronize(ctx->stream));
-        layout_dev_free(victim->dev);
-        bbh_layout_free(&victim->host);
-        victim->valid = false;
+        layout_dev_free(E.dev);
+        bbh_layout_free(&E.host);
+        E.valid = false;
+        E.bytes = 0;
+        if (ctx->cur == &E) {          // (the uploaded MC batch used it: it must be uploaded again)
+            ctx->cur = nullptr;
+            ctx->uploaded = false;
+            ctx->gen++;
+        }
+        return 0;
+    };
+    if (victim->valid && evict(*victim)) return BBGPU_ERR_CUDA;
+    for (;;) {
+        long long total = 0;
+        LayoutEntry *lru = nullptr;
+        for (auto &E : ctx->layouts)
+            if (E.valid) {
+                total += E.bytes;
+                if (!lru || E.last_use < lru->last_use) lru = &E;
+            }
+        if (total <= LAYOUT_BUDGET || !lru) break;
+        if (evict(*lru)) return BBGPU_ERR_CUDA;
     }
     if (bbh_layout_build(&victim->host, seed, ctx->g.ltype, nsub, nc, nv, R0, ctx->g.radsep) != 0)
         return fail(ctx, BBGPU_ERR_NOMEM, "MC layout: too many clouds or host allocation failed");
     int rc = upload_layout(ctx, *victim);
     if (rc) return rc;
+    {
+        const LayoutHost &H = victim->host;
+        victim->bytes = (long long)H.ncloud * 56 + (long long)H.nsubcloud * 12 + (long long)H.nslow * 8 +
+                        (long long)H.nsub * 16;
+    }
     victim->valid = true;
     victim->last_use = ++ctx->use_clock;
     *out = victim;
@@ -507,6 +540,8 @@ extern "C" int bbgpu_ctx_destroy(bbgpu_ctx *ctx) {
     cudaFree(ctx->d_tcount); cudaFree(ctx->d_toff); cudaFree(ctx->d_tcur); cudaFree(ctx->d_model); cudaFree(ctx->d_scan);
     cudaFree(ctx->d_smooth); cudaFree(ctx->d_model64); cudaFree(ctx->d_partial); cudaFree(ctx->d_out2);
     cudaFree(ctx->d_bimg); cudaFree(ctx->d_tmaps); cudaFree(ctx->d_tcq);
+    for (auto &v : ctx->pool)
+        for (auto &b : v) cudaFree(b.p);
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
     cudaFree(ctx->d_err);
     for (void *q : {(void *)ctx->d_ppix, (void *)ctx->d_lc, (void *)ctx->d_ord, (void *)ctx->d_p0, (void *)ctx->d_ent,
@@ -1865,20 +1900,32 @@ extern "C" int bbgpu_residuals_fracerr(bbgpu_ctx *ctx, const double *model, cons
 }
 
 // A scoped set of device buffers freed at the end of a stand-alone entry point.
+// Scratch buffers of a stand-alone call: the i-th buffer of call site `tag` is kept in the context and reused by
+// the next call of that site (grown when too small), so that a call allocates nothing once warm (a cudaFree would
+// also wait for the whole device). The calls of a context run in order on its stream, so reuse is safe.
 struct DevBufs {
-    std::vector<void *> p;
-    ~DevBufs() {
-        for (void *q : p) cudaFree(q);
-    }
+    bbgpu_ctx *ctx;
+    int tag;
+    size_t i = 0;
+    DevBufs(bbgpu_ctx *c, int t) : ctx(c), tag(t) {}
     template <class T>
     bool get(T **out, size_t n) {
-        void *q = nullptr;
-        if (cudaMalloc(&q, n ? n : 1) != cudaSuccess) {
-            cudaGetLastError();
-            return false;
+        std::vector<PoolBuf> &v = ctx->pool[tag];
+        if (i == v.size()) v.push_back(PoolBuf{});
+        PoolBuf &b = v[i++];
+        const size_t need = n ? n : 1;
+        if (b.cap < need) {
+            if (b.p) cudaFree(b.p);
+            b.p = nullptr;
+            b.cap = 0;
+            const size_t want = need + need / 4;
+            if (cudaMalloc(&b.p, want) != cudaSuccess) {
+                cudaGetLastError();
+                return false;
+            }
+            b.cap = want;
         }
-        p.push_back(q);
-        *out = (T *)q;
+        *out = (T *)b.p;
         return true;
     }
 };
@@ -1939,7 +1986,7 @@ extern "C" int bbgpu_galmod_analytic(bbgpu_ctx *ctx, double *out, const double *
                               subs.data(), zc);
     const std::vector<double> &zq = zc.zq, &wq = zc.wq;
     if (e == -10000) return fail(ctx, BBGPU_ERR_ARG, "galmod_analytic: the total flux is not finite");
-    DevBufs B;
+    DevBufs B(ctx, 0);
     AnDev D;
     int rc = an_upload(ctx, B, subs, s2.data(), ns, zq, wq, D);
     if (rc) return rc;
@@ -1992,7 +2039,7 @@ extern "C" int bbgpu_ring_maps_analytic(bbgpu_ctx *ctx, double *out, int nr, con
                               subs.data(), zc);
     const std::vector<double> &zq = zc.zq, &wq = zc.wq;
     if (e == -10000) return fail(ctx, BBGPU_ERR_ARG, "ring_maps_analytic: the weights are not finite");
-    DevBufs B;
+    DevBufs B(ctx, 1);
     AnDev D;
     int rc = an_upload(ctx, B, subs, sr, nsub, zq, wq, D);
     if (rc) return rc;
@@ -2027,7 +2074,7 @@ extern "C" int bbgpu_conv_sparse(bbgpu_ctx *ctx, const double *model, double *ou
     CK(cudaSetDevice(ctx->device));
     const size_t n = (size_t)ny * nx * nz;
     if (n == 0) return BBGPU_OK;
-    DevBufs B;
+    DevBufs B(ctx, 2);
     double *dm = nullptr, *dout = nullptr, *dk = nullptr;
     if (!B.get(&dm, n * 8) || !B.get(&dout, n * 8) || !B.get(&dk, (size_t)ky * kx * 8))
         return fail(ctx, BBGPU_ERR_NOMEM, "conv_sparse: allocation failed");
@@ -2067,7 +2114,7 @@ extern "C" int bbgpu_norm(bbgpu_ctx *ctx, double *model, int bsy, int bsx, int n
             memcpy(&dbox[((size_t)y * bsx + x) * nz], data + src, sizeof(float) * nz);
             memcpy(&mbox[((size_t)y * bsx + x) * nz], mask + src, nz);
         }
-    DevBufs B;
+    DevBufs B(ctx, 3);
     double *dm = nullptr, *dw = nullptr, *dcn = nullptr, *dpre = nullptr, *dthr = nullptr, *dpart = nullptr,
            *dP = nullptr;
     float *dd = nullptr;
@@ -2517,7 +2564,7 @@ extern "C" int bbgpu_solve_profile(bbgpu_ctx *ctx, const double *A, const double
     ProfBox bx{};
     bx.nrp = n;
     bx.npix = m;
-    DevBufs B;
+    DevBufs B(ctx, 4);
     double *dA = nullptr, *db = nullptr, *dpart = nullptr, *dgh = nullptr, *dx = nullptr;
     int *dpp = nullptr, *dst = nullptr;
     const int nt = prof_gram_tiles(m);
