@@ -43,6 +43,22 @@ def free_parameters(free):
     return out
 
 
+def default_par(**kw):
+    """The 3DFIT parameters a CLASSIC fit reads, with the reference's defaults (``bbarolo/params.py``): FREE "VROT
+    VDISP", one stage, NORM AZIM, FTYPE 2, WFUNC 2, SIDE B, TOL 1e-3, and the GALMOD ones of the cube; keywords
+    override them."""
+    import types
+    par = types.SimpleNamespace(FREE="VROT VDISP", DELTAVROT=1000.0, MINVDISP=0.1, MAXVDISP=1000.0, DELTAINC=5.0,
+                                DELTAPHI=15.0, TOL=1e-3, FTYPE=2, WFUNC=2, SIDE="B", BWEIGHT=1.0, NORM="AZIM",
+                                NORMALCUBE=True, TWOSTAGE=False, flagERRORS=False, STARTRAD=0, DENSFLUX=True,
+                                CDENS=10, CMODE=1, ISEED=1, LTYPE=1, NV=-1, REDSHIFT=0.0, EMPTY=True,
+                                RESTWAVE=[-1.0], RESTFREQ=[-1.0], RELINT=[1.0], SM=True, RADMAXA=-1.0,
+                                RADMAXR=-1.0)
+    for k, v in kw.items():
+        setattr(par, k, v)
+    return par
+
+
 @dataclass
 class Limits:
     """The bounds of one free parameter for a stage: [lo, hi] from the initial rings, and how a trial value outside

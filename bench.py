@@ -244,6 +244,7 @@ def main():
     ap.add_argument("--bayes-nb", type=int, default=1024,
                     help="points per launch of the 256x256x192 batch (the BAYESIAN workload: 1024)")
     ap.add_argument("--no-bayes-fit", action="store_true", help="skip the BAYESIAN fit time (plain and screened)")
+    ap.add_argument("--no-classic", action="store_true", help="skip the CLASSIC fit of the 64x64x64 workload")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the per-variant convolution times and errors")
     ap.add_argument("--no-random", action="store_true",
@@ -378,6 +379,8 @@ def main():
     if not args.no_random:
         line["random"] = batch_leg(ctx, L, rings, random_rows(rings, B), args, dist, world)
         line["unshared"] = batch_leg(ctx, L, rings, rows, args, dist, world, share=False)
+    if not args.no_classic:
+        line["classic_fit"] = classic_leg()
     if not args.no_bayes:
         line["bayes256"] = bayes256_leg(args, dist, world, nb=args.bayes_nb)
         if not args.no_bayes_fit:
@@ -525,6 +528,35 @@ def bayes_fit_leg(seed=11):
     out["calls_ratio"] = out["plain"]["n_like"] / out["screened"]["n_like"]
     out["problem"] = "256x256x192, 20 rings, VROT+VDISP of 4 rings free (8 dimensions), ANALYTIC, 100 live points"
     return out
+
+
+def classic_leg():
+    """CLASSIC 3DFIT of the 64x64x64 workload (8 rings, VROT and VDISP free from 120 and 8 km/s, the reference's
+    defaults: NORM AZIM, FTYPE 2, WFUNC 2; noise 1% of the peak, seed 1; mask of the model above three times the
+    noise): the fit's wall time (the rings of the stage advanced together, each evaluation a single-ring model,
+    sparse convolution and normalisation on the device), its evaluations, and the fitted values against the truth."""
+    from bbarolo2_gb300 import classic, configs, engine
+    cube, rings = configs.classic64(galmodtype="MC")
+    dm = engine.DiskModel(cube)
+    truth = dm.array(rings, seed=1)
+    sigma = 0.01 * float(truth.max())
+    g = np.random.default_rng(1)
+    cube.array = (truth + g.normal(0., sigma, truth.shape)).astype(np.float32)
+    inr = rings.copy()
+    inr.vrot = np.full(inr.nr, 120.)
+    inr.vdisp = np.full(inr.nr, 8.)
+    fit = classic.ClassicFit(cube, inr, classic.default_par(), sigma, truth > 3 * sigma)
+    fit.run()                                  # (warm-up: device buffers and the rings' cloud layouts)
+    fit = classic.ClassicFit(cube, inr, classic.default_par(), sigma, truth > 3 * sigma)
+    t = time.perf_counter()
+    out, ok = fit.run()
+    wall = time.perf_counter() - t
+    n = sum(len(v) for v in fit.log.values())
+    return {"wall_s": wall, "evaluations": n, "ms_per_evaluation": 1e3 * wall / max(n, 1),
+            "rings_converged": int(sum(ok)), "rings": int(rings.nr),
+            "max_abs_err_vrot": float(np.max(np.abs(out.vrot - rings.vrot))),
+            "max_abs_err_vdisp": float(np.max(np.abs(out.vdisp - rings.vdisp))),
+            "problem": "64x64x64, 8 rings, VROT+VDISP free from 120/8 km/s, MC model, one stage"}
 
 
 def random_rows(rings, batch, seed=2):
