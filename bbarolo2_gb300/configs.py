@@ -58,6 +58,40 @@ def bayes256(galmodtype="ANALYTIC", iseed=1, seed=7):
     return cube, rings
 
 
+def galaxy_population(n, seed=11, nmax=320, zmax=256):
+    """n mock galaxies with the spread of the heterogeneous batch: cubes of nx = ny uniform in [32, nmax] pixels of
+    10" and nz uniform in [32, zmax] channels, 5-50 rings (at most one per two pixels) out to 0.4 of the cube, inclination 20-80 degrees, position
+    angle 0-360, flat rotation 50-300 km/s reached as (2/pi) arctan(r / (0.2 rmax)), dispersion 5-30 km/s, scale
+    height 0-0.2 rmax, circular beam of 2-6 pixels FWHM, noise 0.5-2% of the peak (ANALYTIC model); the channel
+    width makes the line span about 80% of the band. Returns a list of (cube, rings, noise fraction)."""
+    g = np.random.default_rng(seed)
+    out = []
+    for _ in range(int(n)):
+        nx = int(g.integers(32, nmax + 1))
+        nz = int(g.integers(32, zmax + 1))
+        nr = int(g.integers(5, 51))
+        nr = min(nr, int(0.4 * nx / 2))          # (rings at least two pixels apart: GALMOD's sub-ring spacing)
+        inc, pa = float(g.uniform(20., 80.)), float(g.uniform(0., 360.))
+        vflat, vdisp = float(g.uniform(50., 300.)), float(g.uniform(5., 30.))
+        pix = 10.
+        rmax = 0.4 * nx * pix
+        z0 = float(g.uniform(0., 0.2)) * rmax
+        fwhm = float(g.uniform(2., 6.)) * pix
+        noise = float(g.uniform(0.005, 0.02))
+        dv = 2. * (vflat * math.sin(math.radians(inc)) + 4. * vdisp) / (0.8 * nz)
+        par = Params(CDENS=10, ISEED=1, LTYPE=1, galmodtype="ANALYTIC")
+        cube = Cube.empty(nx, nx, nz, [-pix / 3600., pix / 3600., dv], beam=fwhm / 3600., par=par,
+                          crpix=[nx / 2. + 0.5, nx / 2. + 0.5, nz / 2. + 0.5], crval=[60., 0., 1000.],
+                          cunit=("deg", "deg", "km/s"))
+        r = (np.arange(nr) + 0.5) * (rmax / nr)
+        c = (nx - 1) / 2.
+        rings = Rings().setRings(radii=r, xpos=c, ypos=c, vsys=1000.,
+                                 vrot=vflat * (2 / math.pi) * np.arctan(r / (0.2 * rmax)), vdisp=vdisp, inc=inc,
+                                 phi=pa, z0=z0, dens=np.exp(-r / (0.5 * rmax)))
+        out.append((cube, rings, noise))
+    return out
+
+
 def bayes256_subproblem(free_rings=(2, 7, 12, 17), noise=0.02, seed=7):
     """The BAYESIAN problem of the screen's benchmark: the ``bayes256`` cube and rings (ANALYTIC), the mock its model
     plus white noise of `noise` of the peak, the mask the model above twice the noise; VROT and VDISP of `free_rings`

@@ -245,6 +245,7 @@ def main():
                     help="points per launch of the 256x256x192 batch (the BAYESIAN workload: 1024)")
     ap.add_argument("--no-bayes-fit", action="store_true", help="skip the BAYESIAN fit time (plain and screened)")
     ap.add_argument("--no-classic", action="store_true", help="skip the CLASSIC fit of the 64x64x64 workload")
+    ap.add_argument("--no-ragged", action="store_true", help="skip the heterogeneous batch of 128 galaxies")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the per-variant convolution times and errors")
     ap.add_argument("--no-random", action="store_true",
@@ -381,6 +382,8 @@ def main():
         line["unshared"] = batch_leg(ctx, L, rings, rows, args, dist, world, share=False)
     if not args.no_classic:
         line["classic_fit"] = classic_leg()
+    if not args.no_ragged:
+        line["ragged"] = ragged_leg(args, dist, world)
     if not args.no_bayes:
         line["bayes256"] = bayes256_leg(args, dist, world, nb=args.bayes_nb)
         if not args.no_bayes_fit:
@@ -557,6 +560,46 @@ def classic_leg():
             "max_abs_err_vrot": float(np.max(np.abs(out.vrot - rings.vrot))),
             "max_abs_err_vdisp": float(np.max(np.abs(out.vdisp - rings.vdisp))),
             "problem": "64x64x64, 8 rings, VROT+VDISP free from 120/8 km/s, MC model, one stage"}
+
+
+def ragged_leg(args, dist, world, ngal=128, nb=4):
+    """A heterogeneous batch (``ragged.GalaxyBatch``): ngal galaxies of the heterogeneous population (seed 11: cubes
+    of 32-320 pixels a side and 32-256 channels, 5-50 rings, every geometry, scale height and beam different; the
+    ANALYTIC model), nb ring sets about each galaxy's truth; every galaxy's batch queued on its own context and
+    stream before any result is read, graph replays once warm. Device rate (upload once, runs and result reads
+    timed) and end to end (ring tables, uploads, runs and reads timed)."""
+    from bbarolo2_gb300 import configs
+    from bbarolo2_gb300.galmod import ring_rows_batch
+    from bbarolo2_gb300.ragged import GalaxyBatch
+    pop = configs.galaxy_population(ngal, seed=11)
+    batch = GalaxyBatch.mock(pop, seed=3)
+    g = np.random.default_rng(5)
+    rows = []
+    for _, _, rings in batch.items:
+        r = ring_rows_batch([rings] * nb)
+        r[1:, 4] *= 1 + 0.02 * g.standard_normal((nb - 1, rings.nr))
+        r[1:, 5] *= 1 + 0.05 * g.random((nb - 1, rings.nr))
+        rows.append(r)
+    boxes = batch.upload(rows, seed=1)
+    for _ in range(3):
+        batch.run()
+        batch.download(boxes)
+    steps = max(2, args.steps // 2)
+    t = time.perf_counter()
+    for _ in range(steps):
+        batch.run()
+        batch.download(boxes)
+    dt = max_over_ranks(time.perf_counter() - t, dist)
+    t = time.perf_counter()
+    for _ in range(steps):
+        batch.evaluate(rows, seed=1)
+    te = max_over_ranks(time.perf_counter() - t, dist)
+    n = ngal * nb
+    vox = [c.DimX() * c.DimY() * c.DimZ() for c, _, _ in pop]
+    return {"galaxies": ngal, "per_galaxy": nb, "value": throughput(n, steps, world, dt), "unit": UNIT,
+            "ms_per_step": 1e3 * dt / steps, "e2e": throughput(n, steps, world, te),
+            "voxels_per_cube": {"min": int(min(vox)), "median": int(np.median(vox)), "max": int(max(vox))},
+            "note": "one context and stream per galaxy, all queued before the reads; not one launch"}
 
 
 def random_rows(rings, batch, seed=2):
