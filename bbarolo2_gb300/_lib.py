@@ -28,7 +28,10 @@ SYMBOLS = ("bbgpu_ctx_create", "bbgpu_ctx_destroy", "bbgpu_last_error", "bbgpu_v
            "bbgpu_sumsq_residuals_noalloc", "bbgpu_set_profile", "bbgpu_eval_upload_profile", "bbgpu_eval_profile", "bbgpu_solve_profile",
            "bbgpu_subrings_rows", "bbgpu_conv_variant", "bbgpu_graph_stats", "bbgpu_mlp_create",
            "bbgpu_mlp_destroy", "bbgpu_mlp_nparams", "bbgpu_mlp_get_params", "bbgpu_mlp_set_params",
-           "bbgpu_mlp_predict", "bbgpu_mlp_gradients", "bbgpu_mlp_train_step", "bbgpu_mlp_train")
+           "bbgpu_mlp_predict", "bbgpu_mlp_gradients", "bbgpu_mlp_train_step", "bbgpu_mlp_train",
+           "bbgpu_wind_create", "bbgpu_wind_destroy", "bbgpu_wind_last_error", "bbgpu_wind_launch_count",
+           "bbgpu_wind_set_cells", "bbgpu_wind_points", "bbgpu_wind_set_points", "bbgpu_wind_boxes",
+           "bbgpu_wind_columns", "bbgpu_wind_set_weights", "bbgpu_wind_normal", "bbgpu_wind_model")
 
 
 class Grid(C.Structure):
@@ -38,6 +41,17 @@ class Grid(C.Structure):
                 ("crota2", C.c_double), ("sig_instr", C.c_double), ("crval3", C.c_double),
                 ("cdelt3", C.c_double), ("crpix3", C.c_double), ("chwidth", C.c_double), ("zstep", C.c_double),
                 ("scalefactor", C.c_double)]
+
+
+class WindGrid(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("nlines", C.c_int), ("axtyp", C.c_int),
+                ("velsys", C.c_int), ("cdelt0", C.c_double), ("cdelt1", C.c_double), ("sig_instr", C.c_double),
+                ("chmin", C.c_double), ("crval3", C.c_double), ("cdelt3", C.c_double), ("crpix3", C.c_double)]
+
+
+class WindGeometry(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("x0", "y0", "vsys", "sinc", "cinc", "spa", "cpa", "th_in", "th_out",
+                                          "rmax")]
 
 
 class EvalDesc(C.Structure):
@@ -118,6 +132,18 @@ def load(path=None):
         "bbgpu_eval_upload_profile": (i, [vp, i, vp, vp, vp]),
         "bbgpu_eval_profile": (i, [vp, vp, vp]),
         "bbgpu_solve_profile": (i, [vp, vp, vp, i, i, vp, d, d, d, vp, vp]),
+        "bbgpu_wind_create": (i, [C.POINTER(vp), i, C.POINTER(WindGrid), vp, vp, vp, vp, i, i, vp, vp, i]),
+        "bbgpu_wind_destroy": (i, [vp]),
+        "bbgpu_wind_last_error": (C.c_char_p, [vp]),
+        "bbgpu_wind_launch_count": (i64, [vp]),
+        "bbgpu_wind_set_cells": (i, [vp, i, vp, vp, vp]),
+        "bbgpu_wind_points": (i, [vp, C.POINTER(WindGeometry), i, vp, vp, vp, vp] + [vp] * 8),
+        "bbgpu_wind_set_points": (i, [vp, vp, vp, vp, vp, vp]),
+        "bbgpu_wind_boxes": (i, [vp, vp, vp, vp, vp]),
+        "bbgpu_wind_columns": (i, [vp, vp, vp]),
+        "bbgpu_wind_set_weights": (i, [vp, vp, vp]),
+        "bbgpu_wind_normal": (i, [vp, d, vp, vp]),
+        "bbgpu_wind_model": (i, [vp, vp, vp]),
     }
     for name, (res, args) in proto.items():
         f = getattr(L, name)

@@ -13,6 +13,11 @@ rings of the stated shape. Choices not fixed by the problem statements are made 
   every sub-ring is the floor of 10 per pixel of ring area (``bbarolo/galmod.py:112-114``).
 * ``bayes256``   - 256x256 px x 192 channels, 4" pixels, 6 km/s channels, 20 rings at 8 + 16k", beam 4 px FWHM
   (16"), truth drawn from the priors (vrot U(0,350), vdisp U(1,40), inc U(30,80), pa U(0,360)) with seed 7.
+* ``wind_circinus`` - a WINDFIT problem with the shapes of the reference's Circinus example (MUSE [OIII]): 173x238
+  px of 0.2" x 41 channels of 75 km/s (on a velocity axis) from -1725 to +1275 km/s, 0.9" beam, SPECRES 0.85
+  channels; cells of 3.6" on the approaching cone (OPENANG 110, CONELEN 52": 3192 cells), quadrature for winds up to
+  1600 km/s (the prior's bound) and no intrinsic dispersion; the wind at VWIND 338 km/s, INC 71.6, PA 25, apex at
+  pixel (20, 40) (about half of the cone's quadrature points fall in the cube).
 """
 
 import math
@@ -112,3 +117,29 @@ def bayes256_subproblem(free_rings=(2, 7, 12, 17), noise=0.02, seed=7):
 
 
 WORKLOADS = {"classic64": classic64, "global160": global160, "bayes256": bayes256}
+
+
+def wind_circinus():
+    """The Circinus-shaped WINDFIT problem (module docstring): (WindModel with its quadrature, WindPars of the
+    wind)."""
+    from .wind import WindCells, WindModel, WindPars
+    par = Params(specres=0.85)
+    cube = Cube.empty(173, 238, 41, [-0.2 / 3600., 0.2 / 3600., 75.], beam=0.9 / 3600., par=par,
+                      crpix=[87., 120., 24.], crval=[213.29, -65.34, 0.], cunit=("deg", "deg", "km/s"))
+    wm = WindModel(cube, WindCells.resolved(52., 55., 3.6, cones=(-1,))).quadrature(vmax=1600., sigmin=0.)
+    p = WindPars([26.], 338., 0., xpos=20., ypos=40., inc=71.6, pa=25., openang=110., conelen=52.)
+    return wm, p
+
+
+def wind_data(wm, p, noise=0.05, seed=1):
+    """Mock data of the wind p: the model with the emissivity (r / 26")^-3.4 of the cells plus Gaussian noise of
+    noise times its peak; W = 1 / sigma^2 on the voxels where the model is above 1e-3 of its peak, 0 elsewhere (the
+    mask of the fit). Returns (W, W d)."""
+    c = wm.cells.cells
+    r = 0.5 * (c[:, 1] + c[:, 2])
+    model = wm.cube(p, amp=(r / 26.) ** -3.4)
+    peak = float(model.max())
+    sig = noise * peak
+    d = model + np.random.default_rng(seed).normal(0., sig, model.shape)
+    W = np.where(model > 1e-3 * peak, 1. / sig ** 2, 0.)
+    return W, W * d

@@ -246,6 +246,7 @@ def main():
     ap.add_argument("--no-bayes-fit", action="store_true", help="skip the BAYESIAN fit time (plain and screened)")
     ap.add_argument("--no-classic", action="store_true", help="skip the CLASSIC fit of the 64x64x64 workload")
     ap.add_argument("--no-ragged", action="store_true", help="skip the heterogeneous batch of 128 galaxies")
+    ap.add_argument("--no-wind", action="store_true", help="skip the WINDFIT normal equations (Circinus shapes)")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the per-variant convolution times and errors")
     ap.add_argument("--no-random", action="store_true",
@@ -384,6 +385,8 @@ def main():
         line["classic_fit"] = classic_leg()
     if not args.no_ragged:
         line["ragged"] = ragged_leg(args, dist, world)
+    if not args.no_wind:
+        line["wind"] = wind_leg(args, dist, world, cpu=rank == 0 and not args.no_cpu)
     if not args.no_bayes:
         line["bayes256"] = bayes256_leg(args, dist, world, nb=args.bayes_nb)
         if not args.no_bayes_fit:
@@ -600,6 +603,79 @@ def ragged_leg(args, dist, world, ngal=128, nb=4):
             "ms_per_step": 1e3 * dt / steps, "e2e": throughput(n, steps, world, te),
             "voxels_per_cube": {"min": int(min(vox)), "median": int(np.median(vox)), "max": int(max(vox))},
             "note": "one context and stream per galaxy, all queued before the reads; not one launch"}
+
+
+def wind_leg(args, dist, world, cpu=True):
+    """WINDFIT's per-likelihood column work on the Circinus-shaped problem (``configs.wind_circinus``: 3192 cells,
+    1.9 million quadrature points, 173x238x41 voxels): for one wind, the quadrature points, the columns (deposit and
+    beam convolution) and the normal equations G, b of the columns over the voxel lists pruned at 1e-3 (the default
+    of the reference's likelihood), G (3192 x 3192) and b read back. Each step a new wind (VWIND and INC moved, as a
+    fit moves them), through the public API (``WindModel.boxes``, ``Boxes.voxel_lists``, ``Boxes.normal``). The CPU
+    leg: the oracle (the reference's kernels restated in C, one thread) on one wind; parity: its G and b against
+    the device's."""
+    from bbarolo2_gb300 import configs
+    from bbarolo2_gb300.wind import WindPars
+    wm, p0 = configs.wind_circinus()
+    W, Wd = configs.wind_data(wm, p0)
+    rel = 1e-3
+
+    def wind(k):
+        return WindPars(p0.radii, p0.vwind + 3. * (k % 7), 0., xpos=p0.xpos, ypos=p0.ypos, inc=p0.inc + 0.05 * (k % 5),
+                        pa=p0.pa, openang=p0.openang, conelen=p0.conelen)
+
+    def one(k, stages=None):
+        t0 = time.perf_counter()
+        B = wm.boxes(wind(k))
+        t1 = time.perf_counter()
+        G, b = B.normal(Wd, W, B.voxel_lists(W, rel=rel))
+        if stages is not None:
+            stages[0] += t1 - t0
+            stages[1] += time.perf_counter() - t1
+        return B, G, b
+
+    for k in range(max(3, args.warmup)):
+        one(k)
+    steps = max(3, args.steps // 2)
+    stages = [0., 0.]
+    l0 = wm.launches()
+    t = time.perf_counter()
+    for k in range(steps):
+        B, G, b = one(k, stages)
+    dt = max_over_ranks(time.perf_counter() - t, dist)
+    launches = (wm.launches() - l0) // steps
+    out = {"workload": "wind_circinus: 173x238x41 voxels, 3192 cells (approaching cone), "
+                       f"{wm.cells.npoints} quadrature points, beam kernel {2 * wm.hy + 1}x{2 * wm.hx + 1}",
+           "metric": "wind likelihood column evaluations/s (points + columns + normal equations, G and b read)",
+           "value": throughput(1, steps, world, dt), "ms_per_evaluation": 1e3 * dt / steps,
+           "ms_columns": 1e3 * stages[0] / steps, "ms_normal": 1e3 * stages[1] / steps,
+           "column_values": int(B.total), "nonempty_columns": int(np.sum(np.diff(B.offs) > 0)),
+           "gpu_launches_per_evaluation": int(launches), "prune": rel,
+           "d2h_bytes_per_evaluation": int(G.nbytes + b.nbytes + B.boxes.nbytes)}
+    if cpu:
+        from oracle import oracle as O
+        p = wind(steps - 1)
+        su = wm.setup
+        inc, ang = math.radians(p.inc), math.radians(p.pa) + su.crota2
+        t = time.perf_counter()
+        pts = O.wind_points(wm.cells.cells, wm.cells.qn, wm.cells.qoff, p.radii, p.vwind, p.vdisp, p.vrot, p.xpos,
+                            p.ypos, p.vsys * 1000., math.sin(inc), math.cos(inc), math.sin(ang), math.cos(ang),
+                            wm.cdelt[0], wm.cdelt[1], math.radians(0.5 * p.openin), math.radians(0.5 * p.openang),
+                            p.conelen, su.sig_instr)
+        spec = dict(chmin=su._chmin, axtyp=su.axtyp, velsys=su.velsys, lfreq0=su.lfreq0, crval3=su.crval3,
+                    cdelt3=su.cdelt3, crpix3=su.crpix3)
+        nz, ny, nx = wm.shape
+        lim = np.array([0, nx, 0, ny, 0, nz])
+        buf, offs, boxes = O.wind_boxes(pts, pts["w"], lim, wm.shape, wm.kern, wm.kx, wm.ky, wm.separable, spec,
+                                        su._vedges_lines, su.relint, wm.cells.qoff)
+        Go, bo = O.wind_normal(buf, offs, boxes, Wd, W, lim, rel)
+        tc = time.perf_counter() - t
+        out["cpu_baseline"] = {"value": 1. / tc, "unit": "evaluations/s", "cores": 1, "kind": "port",
+                               "sample": "one wind: the oracle's points, columns and normal equations"}
+        out["max_rel_err_G"] = float(np.abs(G - Go).max() / np.abs(Go).max())
+        out["max_rel_err_b"] = float(np.abs(b - bo).max() / np.abs(bo).max())
+        out["boxes_equal"] = bool(np.array_equal(B.boxes, boxes))
+    wm.close()
+    return out
 
 
 def random_rows(rings, batch, seed=2):

@@ -17,6 +17,11 @@
  *   bbgpu_norm                <- _norm(model, data, mask, blo0, blo1, x0, y0, phi, inc, ...)      bbarolo/galfit.py:39-41
  *   bbgpu_eval_*              <- LikelihoodMixin._log_likelihood(theta) for a batch of theta:
  *                                DiskModel.array -> convolve -> _calculate_residuals             bbarolo/bayesian/likelihood.py:567-619
+ *   bbgpu_wind_points         <- _wind_points(cells, qn, qoff, radii, vw, vd, vr, ...)            bbarolo/windmodel.py:225-227
+ *   bbgpu_wind_boxes          <- WindModel.boxes(p, lim, pts, weight): _raw_boxes, _deposit_raw,
+ *                                _convolve_boxes                                                   bbarolo/windmodel.py:829-859
+ *   bbgpu_wind_normal         <- Boxes.voxel_lists(wm, lim, rel) + Boxes.normal(wd, wm, lists)    bbarolo/windmodel.py:672-687
+ *   bbgpu_wind_model          <- Boxes.model(amp, shape) (_scatter)                               bbarolo/windmodel.py:584-585, 657
  *
  * Layouts follow the reference: sub-ring tables sr (16, nsub) float64 in internal units (row order of
  * GalmodSetup.subrings, bbarolo/galmod.py:761-851); models (ny, nx, nz) float64 ("yxz"); cubes (nz, ny, nx).
@@ -201,6 +206,57 @@ int bbgpu_mlp_train_step(bbgpu_mlp *m, const float *x, const float *t, int n, fl
  * mean squared error of the last minibatch (before its step). n < 2^31. */
 int bbgpu_mlp_train(bbgpu_mlp *m, const float *x, const float *t, long long n, int steps, int batch, float lr,
                     uint64_t seed, float *loss);
+
+/* ---- bi-conical wind models (WINDFIT) ------------------------------------------------------------------ */
+/* The column engine of the wind models: a handle per cube (its spectral axis, lines and beam) and grid of cells
+ * (bbarolo/windmodel.py:89-210, 706-803). A column is the model of one cell for unit amplitude, a dense box
+ * (x0, x1, y0, y1, k0, k1) of the cube ([lo, hi), values in (channel, y, x) order from the column's offset). */
+typedef struct bbgpu_wind bbgpu_wind;
+typedef struct {
+    int nx, ny, nz;           /* cube dimensions */
+    int nlines;               /* emission lines (at most 4) */
+    int axtyp, velsys;        /* spectral axis, as bbgpu_grid */
+    double cdelt0, cdelt1;    /* arcsec per pixel with the sign of CDELT (WindModel.cdelt) */
+    double sig_instr;         /* instrumental dispersion (m/s) */
+    double chmin;             /* narrowest channel in velocity (m/s; GalmodSetup._chmin) */
+    double crval3, cdelt3, crpix3;
+} bbgpu_wind_grid;
+/* The geometry of one wind (WindModel.points, bbarolo/windmodel.py:808-827): centre (pixels), VSYS (m/s), sin and
+ * cos of INC and of PA + CROTA, the half opening angles OPENIN/2 and OPENANG/2 (radians) and CONELEN (arcsec). */
+typedef struct {
+    double x0, y0, vsys, sinc, cinc, spa, cpa, th_in, th_out, rmax;
+} bbgpu_wind_pars;
+/* lfreq0, relint (nlines); vedges (nlines, nz + 1): the velocity of the channel edges per line; kern (2hy+1,
+ * 2hx+1) the beam kernel, hx = hy = 0 for the bilinear deposit alone; separable: kx (2hx+1), ky (2hy+1). */
+int bbgpu_wind_create(bbgpu_wind **out, int device, const bbgpu_wind_grid *g, const double *lfreq0,
+                      const double *relint, const double *vedges, const double *kern, int hy, int hx, const double *kx,
+                      const double *ky, int separable);
+int bbgpu_wind_destroy(bbgpu_wind *w);
+const char *bbgpu_wind_last_error(const bbgpu_wind *w);
+int64_t bbgpu_wind_launch_count(const bbgpu_wind *w);
+/* The cells (ncell, 7: cone, r0, r1, theta0, theta1, phi0, phi1; arcsec and radians), their quadrature counts qn
+ * (ncell, 3) and point offsets qoff (ncell + 1) (WindCells.cells, qn, qoff). At most 16384 cells, 2^31 - 1 points. */
+int bbgpu_wind_set_cells(bbgpu_wind *w, int ncell, const double *cells, const int64_t *qn, const int64_t *qoff);
+/* The quadrature points of the wind p (radii, vwind, vdisp, vrot: nrad <= 256 shells, arcsec and km/s), kept on the
+ * device; the non-NULL outputs are filled (gx, gy, vel, sig, wt, r per point; vol, rbar per cell). */
+int bbgpu_wind_points(bbgpu_wind *w, const bbgpu_wind_pars *p, int nrad, const double *radii, const double *vwind,
+                      const double *vdisp, const double *vrot, double *gx, double *gy, double *vel, double *sig,
+                      double *wt, double *r, double *vol, double *rbar);
+/* Points given by the caller instead (gx, gy, vel, sig, weights; one per quadrature point). */
+int bbgpu_wind_set_points(bbgpu_wind *w, const double *gx, const double *gy, const double *vel, const double *sig,
+                          const double *wt);
+/* The columns of the current points within lim (6: x0, x1, y0, y1, k0, k1 of the cube), the points' weights times
+ * weight (one per point, or NULL); boxes (ncell, 6) and total (the number of column values) returned. */
+int bbgpu_wind_boxes(bbgpu_wind *w, const int64_t *lim, const double *weight, int64_t *boxes, int64_t *total);
+/* The column values (total) and their offsets (ncell + 1). */
+int bbgpu_wind_columns(bbgpu_wind *w, double *buf, int64_t *offs);
+/* The weights wm and the weighted data wd = wm * data (nz, ny, nx) of the normal equations, kept on the device. */
+int bbgpu_wind_set_weights(bbgpu_wind *w, const double *wm, const double *wd);
+/* G (ncell, ncell) = A'WA and b (ncell) = A'Wd over the voxel-list entries of the columns (value != 0, |value| >=
+ * rel x the peak of its column, wm != 0). */
+int bbgpu_wind_normal(bbgpu_wind *w, double rel, double *G, double *b);
+/* out (nz, ny, nx) = sum_k amp[k] column k. */
+int bbgpu_wind_model(bbgpu_wind *w, const double *amp, double *out);
 
 /* ---- without allocation ------------------------------------------------------------------------------- */
 /* bbgpu_sumsq_residuals / bbgpu_residuals_fracerr for callers that may not allocate device memory (their own

@@ -760,3 +760,309 @@ double ref_norm(double *model, int bsy, int bsx, int nz, const float *data, cons
     if (numPix_tot - numBlanks == 0) return INFINITY;
     return pow(1 + (double)numBlanks / (double)numPix_tot, bweight) * minfunc / (double)(numPix_tot - numBlanks);
 }
+
+/* ------------------------------------------------------------------ WindModel (bbarolo/windmodel.py:212-602)
+ * The columns of the bi-conical wind model of WINDFIT: quadrature points of the cells, their bilinear deposit in
+ * the raw box of each cell, the beam convolution of the boxes and the normal equations of the columns. Boxes are
+ * (x0, x1, y0, y1, k0, k1), [lo, hi), their values in (channel, y, x) order from the offset of the box. */
+
+/* bbarolo/windmodel.py:212-222: ys(xs) at r, linear, constant beyond the ends */
+static double wind_interp(double r, const double *xs, const double *ys, int n) {
+    if (n == 1 || r <= xs[0]) return ys[0];
+    if (r >= xs[n - 1]) return ys[n - 1];
+    int j = 0;
+    while (xs[j] < r) j++;                      /* numpy searchsorted, side='left' */
+    double t = (r - xs[j - 1]) / (xs[j] - xs[j - 1]);
+    return ys[j - 1] + t * (ys[j] - ys[j - 1]);
+}
+
+/* bbarolo/windmodel.py:225-288. cells: (ncell, 7) = cone, r0, r1, t0, t1, p0, p1; qn: (ncell, 3). */
+void ref_wind_points(const double *cells, const int64_t *qn, const int64_t *qoff, int ncell, const double *radii,
+                     const double *vw, const double *vd, const double *vr, int nrad, double x0, double y0,
+                     double vsys, double sinc, double cinc, double spa, double cpa, double cd0, double cd1,
+                     double th_in, double th_out, double rmax, double sig_instr, double *gx, double *gy, double *vel,
+                     double *sig, double *w, double *rr, double *vol, double *rbar) {
+    for (int k = 0; k < ncell; k++) {
+        const double *c = cells + (size_t)k * 7;
+        double cs = c[0], r0 = c[1];
+        double r1 = rmax < c[2] ? rmax : c[2];
+        double t0 = th_in > c[3] ? th_in : c[3];
+        double t1 = th_out < c[4] ? th_out : c[4];
+        double p0 = c[5], p1 = c[6];
+        int64_t nqr = qn[3 * k], nqt = qn[3 * k + 1], nqp = qn[3 * k + 2];
+        int64_t i0 = qoff[k], i1 = qoff[k + 1];
+        if (r1 <= r0 || t1 <= t0) {
+            for (int64_t i = i0; i < i1; i++) {
+                gx[i] = -1e9; gy[i] = -1e9; vel[i] = 0.; sig[i] = 1.; w[i] = 0.; rr[i] = r0;
+            }
+            vol[k] = 0.;
+            rbar[k] = r1 > r0 ? 0.5 * (r0 + r1) : r0;
+            continue;
+        }
+        double dr = (r1 - r0) / (double)nqr, dt = (t1 - t0) / (double)nqt, dp = (p1 - p0) / (double)nqp;
+        int64_t i = i0;
+        double wsum = 0.;
+        for (int64_t a = 0; a < nqr; a++) {
+            double r = r0 + ((double)a + 0.5) * dr;
+            double vrad = wind_interp(r, radii, vw, nrad) * 1000.;
+            double disp = wind_interp(r, radii, vd, nrad) * 1000.;
+            double vrot = wind_interp(r, radii, vr, nrad) * 1000.;
+            double s = sqrt(disp * disp + sig_instr * sig_instr);
+            for (int64_t b = 0; b < nqt; b++) {
+                double th = t0 + ((double)b + 0.5) * dt;
+                double st = sin(th), ct = cos(th);
+                for (int64_t q = 0; q < nqp; q++) {
+                    double ph = p0 + ((double)q + 0.5) * dp;
+                    double sp = sin(ph), cp = cos(ph);
+                    double R = r * st, z = cs * r * ct;
+                    double x = R * cp;
+                    double ys = R * sp * cinc - z * sinc;
+                    gx[i] = x0 + (x * spa - ys * cpa) / cd0;
+                    gy[i] = y0 + (x * cpa + ys * spa) / cd1;
+                    vel[i] = vsys + vrad * (cs * ct * cinc + st * sp * sinc) + vrot * cp * sinc;
+                    sig[i] = s;
+                    w[i] = r * r * st;
+                    rr[i] = r;
+                    wsum += w[i];
+                    i++;
+                }
+            }
+        }
+        double V = (pow(r1, 3.0) - pow(r0, 3.0)) / 3. * (cos(t0) - cos(t1)) * (p1 - p0);
+        vol[k] = V;
+        double f = wsum > 0 ? V / wsum : 0.;
+        double rs = 0.;
+        for (int64_t j = i0; j < i1; j++) {
+            w[j] *= f;
+            rs += w[j] * rr[j];
+        }
+        rbar[k] = V > 0 ? rs / V : 0.5 * (r0 + r1);
+    }
+}
+
+static inline int wind_point_ok(double w, double gx, double gy) {
+    return w > 0. && fabs(gx) < 1e8 && fabs(gy) < 1e8;
+}
+
+/* bbarolo/windmodel.py:291-319 */
+void ref_wind_raw_boxes(const int64_t *qoff, int ncell, const double *gx, const double *gy, const double *vel,
+                        const double *sig, const double *w, const int64_t *lim, double chmin, int axtyp, int velsys,
+                        int nlines, const double *lfreq0, double crval3, double cdelt3, double crpix3,
+                        int64_t *rboxes) {
+    for (int k = 0; k < ncell; k++) {
+        int64_t bx0 = 1 << 30, bx1 = -(1 << 30), by0 = 1 << 30, by1 = -(1 << 30), bk0 = 1 << 30, bk1 = -(1 << 30);
+        for (int64_t i = qoff[k]; i < qoff[k + 1]; i++) {
+            if (!wind_point_ok(w[i], gx[i], gy[i])) continue;
+            int64_t ix = (int64_t)floor(gx[i]), iy = (int64_t)floor(gy[i]);
+            if (ix < bx0) bx0 = ix;
+            if (ix + 2 > bx1) bx1 = ix + 2;
+            if (iy < by0) by0 = iy;
+            if (iy + 2 > by1) by1 = iy + 2;
+            int64_t K = (int64_t)(5.0 * sig[i] / chmin) + 2;
+            for (int nl = 0; nl < nlines; nl++) {
+                int64_t kc = lround_ref(velgrid(vel[i], axtyp, velsys, lfreq0[nl], crval3, cdelt3, crpix3));
+                if (kc - K < bk0) bk0 = kc - K;
+                if (kc + K + 1 > bk1) bk1 = kc + K + 1;
+            }
+        }
+        if (bx0 < lim[0]) bx0 = lim[0];
+        if (bx1 > lim[1]) bx1 = lim[1];
+        if (by0 < lim[2]) by0 = lim[2];
+        if (by1 > lim[3]) by1 = lim[3];
+        if (bk0 < lim[4]) bk0 = lim[4];
+        if (bk1 > lim[5]) bk1 = lim[5];
+        if (bx1 <= bx0 || by1 <= by0 || bk1 <= bk0) {
+            bx0 = bx1 = lim[0];
+            by0 = by1 = lim[2];
+            bk0 = bk1 = lim[4];
+        }
+        int64_t *o = rboxes + 6 * (size_t)k;
+        o[0] = bx0; o[1] = bx1; o[2] = by0; o[3] = by1; o[4] = bk0; o[5] = bk1;
+    }
+}
+
+/* bbarolo/windmodel.py:322-366. vedges: (nlines, nz + 1); cd2i: the channel factors (ones for the wind). */
+void ref_wind_deposit_raw(double *rbuf, const int64_t *roffs, const int64_t *rboxes, const int64_t *qoff, int ncell,
+                          const double *gx, const double *gy, const double *vel, const double *sig, const double *w,
+                          const double *vedges, const double *relint, const double *cd2i, double chmin, int axtyp,
+                          int velsys, int nlines, const double *lfreq0, double crval3, double cdelt3, double crpix3,
+                          int nz) {
+    if (!phi_ready) phi_table();
+    double *prof = malloc(sizeof(double) * (size_t)(nz > 0 ? nz : 1));
+    for (int k = 0; k < ncell; k++) {
+        const int64_t *B = rboxes + 6 * (size_t)k;
+        int64_t x0 = B[0], x1 = B[1], y0 = B[2], y1 = B[3], k0 = B[4], k1 = B[5];
+        if (x1 <= x0 || y1 <= y0 || k1 <= k0) continue;
+        int64_t bx = x1 - x0, by = y1 - y0, base = roffs[k];
+        for (int64_t i = qoff[k]; i < qoff[k + 1]; i++) {
+            if (!wind_point_ok(w[i], gx[i], gy[i])) continue;
+            int64_t ix = (int64_t)floor(gx[i]), iy = (int64_t)floor(gy[i]);
+            double fx = gx[i] - (double)ix, fy = gy[i] - (double)iy;
+            double s = sig[i];
+            if (s < 1e-6 * chmin) s = 1e-6 * chmin;
+            int64_t K = (int64_t)(5.0 * s / chmin) + 2;
+            for (int nl = 0; nl < nlines; nl++) {
+                int64_t kc = lround_ref(velgrid(vel[i], axtyp, velsys, lfreq0[nl], crval3, cdelt3, crpix3));
+                int64_t kk0;
+                int nk = line_profile(prof, vel[i], s, vedges + (size_t)nl * (nz + 1), cd2i, kc, K, nz, &kk0);
+                double amp = w[i] * relint[nl];
+                for (int j = 0; j < nk; j++) {
+                    int64_t kz = kk0 + j;
+                    if (kz < k0 || kz >= k1) continue;
+                    double pv = amp * prof[j];
+                    if (pv == 0.) continue;
+                    for (int dy = 0; dy < 2; dy++) {
+                        int64_t yy = iy + dy;
+                        if (yy < y0 || yy >= y1) continue;
+                        double wy = dy == 1 ? fy : 1. - fy;
+                        int64_t row = base + ((kz - k0) * by + (yy - y0)) * bx - x0;
+                        for (int dx = 0; dx < 2; dx++) {
+                            int64_t xx = ix + dx;
+                            if (xx < x0 || xx >= x1) continue;
+                            double wx = dx == 1 ? fx : 1. - fx;
+                            rbuf[row + xx] += pv * wx * wy;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    free(prof);
+}
+
+/* bbarolo/windmodel.py:369-423. kern: (2hy+1, 2hx+1); kx, ky: the 1D kernels when separable. buf accumulated. */
+void ref_wind_convolve_boxes(const double *rbuf, const int64_t *roffs, const int64_t *rboxes, int ncell,
+                             const double *kern, int hy, int hx, const double *kx, const double *ky, int separable,
+                             double *buf, const int64_t *offs, const int64_t *boxes) {
+    int kw = 2 * hx + 1;
+    for (int k = 0; k < ncell; k++) {
+        const int64_t *R = rboxes + 6 * (size_t)k, *B = boxes + 6 * (size_t)k;
+        int64_t rx0 = R[0], rx1 = R[1], ry0 = R[2], ry1 = R[3], rk0 = R[4], rk1 = R[5];
+        int64_t x0 = B[0], x1 = B[1], y0 = B[2], y1 = B[3], k0 = B[4], k1 = B[5];
+        if (rx1 <= rx0 || ry1 <= ry0 || rk1 <= rk0 || x1 <= x0 || y1 <= y0 || k1 <= k0) continue;
+        int64_t rbx = rx1 - rx0, rby = ry1 - ry0, bx = x1 - x0, by = y1 - y0;
+        int64_t za = rk0 > k0 ? rk0 : k0, zb = rk1 < k1 ? rk1 : k1;
+        if (separable) {
+            double *tmp = malloc(sizeof(double) * (size_t)(rby * bx));
+            for (int64_t kz = za; kz < zb; kz++) {
+                memset(tmp, 0, sizeof(double) * (size_t)(rby * bx));
+                for (int64_t y = ry0; y < ry1; y++) {
+                    const double *rrow = rbuf + roffs[k] + ((kz - rk0) * rby + (y - ry0)) * rbx - rx0;
+                    for (int64_t x = rx0; x < rx1; x++) {
+                        double v = rrow[x];
+                        if (v == 0.) continue;
+                        for (int jx = -hx; jx <= hx; jx++) {
+                            int64_t xx = x + jx;
+                            if (xx < x0 || xx >= x1) continue;
+                            tmp[(y - ry0) * bx + (xx - x0)] += v * kx[jx + hx];
+                        }
+                    }
+                }
+                for (int64_t y = ry0; y < ry1; y++)
+                    for (int jy = -hy; jy <= hy; jy++) {
+                        int64_t yy = y + jy;
+                        if (yy < y0 || yy >= y1) continue;
+                        double f = ky[jy + hy];
+                        double *row = buf + offs[k] + ((kz - k0) * by + (yy - y0)) * bx;
+                        for (int64_t xx = 0; xx < bx; xx++) row[xx] += f * tmp[(y - ry0) * bx + xx];
+                    }
+            }
+            free(tmp);
+        } else {
+            for (int64_t kz = za; kz < zb; kz++)
+                for (int64_t y = ry0; y < ry1; y++) {
+                    const double *rrow = rbuf + roffs[k] + ((kz - rk0) * rby + (y - ry0)) * rbx - rx0;
+                    for (int64_t x = rx0; x < rx1; x++) {
+                        double v = rrow[x];
+                        if (v == 0.) continue;
+                        for (int jy = -hy; jy <= hy; jy++) {
+                            int64_t yy = y + jy;
+                            if (yy < y0 || yy >= y1) continue;
+                            double *row = buf + offs[k] + ((kz - k0) * by + (yy - y0)) * bx - x0;
+                            for (int jx = -hx; jx <= hx; jx++) {
+                                int64_t xx = x + jx;
+                                if (xx < x0 || xx >= x1) continue;
+                                row[xx] += v * kern[(jy + hy) * kw + jx + hx];
+                            }
+                        }
+                    }
+                }
+        }
+    }
+}
+
+/* bbarolo/windmodel.py:477-554: the voxel lists of the columns within lim (entries v != 0, |v| >= rel * the peak of
+ * the column, wm != 0) and the normal equations from them: G[k, l] = sum(A_k A_l wm), b[k] = sum(A_k wd). wd, wm:
+ * (nz, ny, nx). G (ncell x ncell) and b are overwritten. */
+void ref_wind_normal(const double *buf, const int64_t *offs, const int64_t *boxes, int ncell, const double *wd,
+                     const double *wm, int ny, int nx, const int64_t *lim, double rel, double *G, double *b) {
+    int64_t lx = lim[1] - lim[0], ly = lim[3] - lim[2], nvox = lx * ly * (lim[5] - lim[4]);
+    int64_t *start = calloc((size_t)nvox + 1, sizeof(int64_t));
+    double *thr = malloc(sizeof(double) * (size_t)(ncell > 0 ? ncell : 1));
+    for (int k = 0; k < ncell; k++) {
+        double m = 0.;
+        for (int64_t j = offs[k]; j < offs[k + 1]; j++) if (fabs(buf[j]) > m) m = fabs(buf[j]);
+        thr[k] = rel * m;
+    }
+#define WIND_ENTRIES(BODY)                                                                                      \
+    for (int k = 0; k < ncell; k++) {                                                                           \
+        const int64_t *B = boxes + 6 * (size_t)k;                                                               \
+        int64_t x0 = B[0], x1 = B[1], y0 = B[2], y1 = B[3], k0 = B[4], k1 = B[5];                               \
+        if (x1 <= x0 || y1 <= y0 || k1 <= k0) continue;                                                         \
+        int64_t bx = x1 - x0, by = y1 - y0;                                                                     \
+        for (int64_t kz = k0; kz < k1; kz++)                                                                    \
+            for (int64_t y = y0; y < y1; y++) {                                                                 \
+                int64_t row = offs[k] + ((kz - k0) * by + (y - y0)) * bx - x0;                                  \
+                int64_t vrow = ((kz - lim[4]) * ly + (y - lim[2])) * lx - lim[0];                               \
+                for (int64_t x = x0; x < x1; x++) {                                                             \
+                    double v = buf[row + x];                                                                    \
+                    if (v != 0. && fabs(v) >= thr[k] && wm[((size_t)kz * ny + y) * nx + x] != 0.) { BODY }     \
+                }                                                                                               \
+            }                                                                                                   \
+    }
+    WIND_ENTRIES(start[vrow + x + 1]++;)
+    for (int64_t i = 0; i < nvox; i++) start[i + 1] += start[i];
+    int64_t ne = start[nvox];
+    int32_t *cell = malloc(sizeof(int32_t) * (size_t)(ne > 0 ? ne : 1));
+    double *val = malloc(sizeof(double) * (size_t)(ne > 0 ? ne : 1));
+    int64_t *fill = malloc(sizeof(int64_t) * (size_t)(nvox > 0 ? nvox : 1));
+    memcpy(fill, start, sizeof(int64_t) * (size_t)nvox);
+    WIND_ENTRIES({ int64_t j = fill[vrow + x]; cell[j] = k; val[j] = v; fill[vrow + x] = j + 1; })
+#undef WIND_ENTRIES
+    memset(G, 0, sizeof(double) * (size_t)ncell * ncell);
+    memset(b, 0, sizeof(double) * (size_t)ncell);
+    for (int64_t i = 0; i < nvox; i++) {
+        int64_t j0 = start[i], j1 = start[i + 1];
+        if (j1 == j0) continue;
+        int64_t x = lim[0] + i % lx, y = lim[2] + (i / lx) % ly, kz = lim[4] + i / (lx * ly);
+        double wv = wm[((size_t)kz * ny + y) * nx + x], d = wd[((size_t)kz * ny + y) * nx + x];
+        for (int64_t p = j0; p < j1; p++) {
+            int kp = cell[p];
+            double ap = val[p];
+            b[kp] += ap * d;
+            double wa = wv * ap;
+            for (int64_t q = p; q < j1; q++) G[(size_t)kp * ncell + cell[q]] += wa * val[q];
+        }
+    }
+    for (int k = 0; k < ncell; k++)
+        for (int l = k + 1; l < ncell; l++) G[(size_t)l * ncell + k] = G[(size_t)k * ncell + l];
+    free(start); free(thr); free(cell); free(val); free(fill);
+}
+
+/* bbarolo/windmodel.py:584-602: out (nz, ny, nx) += sum_k amp[k] A_k */
+void ref_wind_scatter(double *out, int ny, int nx, const double *buf, const int64_t *offs, const int64_t *boxes,
+                      int ncell, const double *amp) {
+    for (int k = 0; k < ncell; k++) {
+        double a = amp[k];
+        if (a == 0.) continue;
+        const int64_t *B = boxes + 6 * (size_t)k;
+        int64_t x0 = B[0], x1 = B[1], y0 = B[2], y1 = B[3], k0 = B[4], k1 = B[5];
+        if (x1 <= x0 || y1 <= y0 || k1 <= k0) continue;
+        int64_t bx = x1 - x0, by = y1 - y0;
+        for (int64_t kz = k0; kz < k1; kz++)
+            for (int64_t y = y0; y < y1; y++) {
+                int64_t row = offs[k] + ((kz - k0) * by + (y - y0)) * bx - x0;
+                for (int64_t x = x0; x < x1; x++) out[((size_t)kz * ny + y) * nx + x] += a * buf[row + x];
+            }
+    }
+}

@@ -210,3 +210,114 @@ def norm(model, data, mask, blo0, blo1, x0, y0, phi, inc, r1, r2, wpow, side, ft
                                 _i(int(side)), _i(int(ftype)), _ptr(cn), _d(data_noise), _d(bweight),
                                 _i(int(normtype)), _ptr(pre_), _ptr(ilo), _ptr(ihi), _i(ilo.size), _ptr(thr),
                                 _i(int(foot)), _d(hmax)))
+
+
+# ---------------------------------------------------------------------------------------------- wind models
+def _ai64(a):
+    return np.ascontiguousarray(a, dtype=np.int64)
+
+
+def wind_points(cells, qn, qoff, radii, vw, vd, vr, x0, y0, vsys, sinc, cinc, spa, cpa, cd0, cd1, th_in, th_out,
+                rmax, sig_instr):
+    """``bbarolo/windmodel.py:225-288``: a dict of gx, gy, vel, sig, w, r (per point) and vol, rbar (per cell)."""
+    cells, qn, qoff = _f64(cells), _ai64(qn), _ai64(qoff)
+    rs = [_f64(a) for a in (radii, vw, vd, vr)]
+    n, m = int(qoff[-1]), cells.shape[0]
+    out = {k: np.empty(n) for k in ("gx", "gy", "vel", "sig", "w", "r")}
+    out.update(vol=np.empty(m), rbar=np.empty(m))
+    lib().ref_wind_points(_ptr(cells), _ptr(qn), _ptr(qoff), _i(m), *[_ptr(a) for a in rs], _i(rs[0].size),
+                          *[_d(v) for v in (x0, y0, vsys, sinc, cinc, spa, cpa, cd0, cd1, th_in, th_out, rmax,
+                                            sig_instr)],
+                          *[_ptr(out[k]) for k in ("gx", "gy", "vel", "sig", "w", "r", "vol", "rbar")])
+    return out
+
+
+def _spec_args(chmin, axtyp, velsys, lfreq0, crval3, cdelt3, crpix3):
+    lf = _f64(lfreq0)
+    return lf, [_d(chmin), _i(int(axtyp)), _i(int(velsys)), _i(lf.size), _ptr(lf), _d(crval3), _d(cdelt3),
+                _d(crpix3)]
+
+
+def wind_raw_boxes(qoff, gx, gy, vel, sig, w, lim, chmin, axtyp, velsys, lfreq0, crval3, cdelt3, crpix3):
+    """``bbarolo/windmodel.py:291-319``: the raw boxes (ncell, 6) of the points within lim."""
+    qoff = _ai64(qoff)
+    pts = [_f64(a) for a in (gx, gy, vel, sig, w)]
+    lim = _ai64(lim)
+    out = np.empty((qoff.size - 1, 6), dtype=np.int64)
+    lf, spec = _spec_args(chmin, axtyp, velsys, lfreq0, crval3, cdelt3, crpix3)
+    lib().ref_wind_raw_boxes(_ptr(qoff), _i(qoff.size - 1), *[_ptr(a) for a in pts], _ptr(lim), *spec, _ptr(out))
+    return out
+
+
+def wind_deposit_raw(rbuf, roffs, rboxes, qoff, gx, gy, vel, sig, w, vedges, relint, cd2i, chmin, axtyp, velsys,
+                     lfreq0, crval3, cdelt3, crpix3, nz):
+    """``bbarolo/windmodel.py:322-366``: rbuf (float64) accumulated."""
+    assert rbuf.dtype == np.float64 and rbuf.flags.c_contiguous
+    roffs, rboxes, qoff = _ai64(roffs), _ai64(rboxes), _ai64(qoff)
+    pts = [_f64(a) for a in (gx, gy, vel, sig, w)]
+    ve, ri, cd = _f64(vedges), _f64(relint), _f64(cd2i)
+    lf, spec = _spec_args(chmin, axtyp, velsys, lfreq0, crval3, cdelt3, crpix3)
+    lib().ref_wind_deposit_raw(_ptr(rbuf), _ptr(roffs), _ptr(rboxes), _ptr(qoff), _i(qoff.size - 1),
+                               *[_ptr(a) for a in pts], _ptr(ve), _ptr(ri), _ptr(cd), *spec, _i(int(nz)))
+    return rbuf
+
+
+def wind_convolve_boxes(rbuf, roffs, rboxes, kern, kx, ky, separable, buf, offs, boxes):
+    """``bbarolo/windmodel.py:369-423``: buf (float64) accumulated."""
+    assert buf.dtype == np.float64 and buf.flags.c_contiguous
+    kern = _f64(kern)
+    hy, hx = kern.shape[0] // 2, kern.shape[1] // 2
+    lib().ref_wind_convolve_boxes(_ptr(_f64(rbuf)), _ptr(_ai64(roffs)), _ptr(_ai64(rboxes)), _i(len(roffs) - 1),
+                                  _ptr(kern), _i(hy), _i(hx), _ptr(_f64(kx)), _ptr(_f64(ky)), _i(int(bool(separable))),
+                                  _ptr(buf), _ptr(_ai64(offs)), _ptr(_ai64(boxes)))
+    return buf
+
+
+def wind_normal(buf, offs, boxes, wd, wm, lim, rel=0.):
+    """``bbarolo/windmodel.py:477-554`` (voxel lists, then the normal equations): (G, b)."""
+    wd, wm = _f64(wd), _f64(wm)
+    n = len(offs) - 1
+    G, b = np.empty((n, n)), np.empty(n)
+    lib().ref_wind_normal(_ptr(_f64(buf)), _ptr(_ai64(offs)), _ptr(_ai64(boxes)), _i(n), _ptr(wd), _ptr(wm),
+                          _i(wm.shape[1]), _i(wm.shape[2]), _ptr(_ai64(lim)), _d(rel), _ptr(G), _ptr(b))
+    return G, b
+
+
+def wind_scatter(shape, buf, offs, boxes, amp):
+    """``bbarolo/windmodel.py:584-602``: the model (nz, ny, nx) of the columns with amplitudes amp."""
+    out = np.zeros(shape)
+    lib().ref_wind_scatter(_ptr(out), _i(shape[1]), _i(shape[2]), _ptr(_f64(buf)), _ptr(_ai64(offs)),
+                           _ptr(_ai64(boxes)), _i(len(offs) - 1), _ptr(_f64(amp)))
+    return out
+
+
+def _offsets(boxes):
+    size = (boxes[:, 1] - boxes[:, 0]) * (boxes[:, 3] - boxes[:, 2]) * (boxes[:, 5] - boxes[:, 4])
+    return np.concatenate([[0], np.cumsum(np.maximum(size, 0))]).astype(np.int64)
+
+
+def wind_boxes(pts, w, lim, shape, kern, kx, ky, separable, spec, vedges, relint, qoff):
+    """The columns of the points (``WindModel.boxes``, ``bbarolo/windmodel.py:829-859``): the raw boxes within lim
+    grown by the beam, the bilinear deposit, then the boxes grown by the beam and clipped to lim and the convolution.
+    spec: dict of chmin, axtyp, velsys, lfreq0, crval3, cdelt3, crpix3. Returns (buf, offs, boxes)."""
+    lim = _ai64(lim)
+    hy, hx = kern.shape[0] // 2, kern.shape[1] // 2
+    rlim = lim + np.array([-hx, hx, -hy, hy, 0, 0])
+    sp = (spec["chmin"], spec["axtyp"], spec["velsys"], spec["lfreq0"], spec["crval3"], spec["cdelt3"],
+          spec["crpix3"])
+    rboxes = wind_raw_boxes(qoff, pts["gx"], pts["gy"], pts["vel"], pts["sig"], w, rlim, *sp)
+    roffs = _offsets(rboxes)
+    rbuf = np.zeros(int(roffs[-1]))
+    wind_deposit_raw(rbuf, roffs, rboxes, qoff, pts["gx"], pts["gy"], pts["vel"], pts["sig"], w, vedges, relint,
+                     np.ones(shape[0]), *sp, shape[0])
+    if hx == 0 and hy == 0:
+        return rbuf, roffs, np.clip(rboxes, np.repeat(lim[::2], 2), np.repeat(lim[1::2], 2))
+    boxes = rboxes + np.array([-hx, hx, -hy, hy, 0, 0])
+    boxes[:, 0:2] = np.clip(boxes[:, 0:2], lim[0], lim[1])
+    boxes[:, 2:4] = np.clip(boxes[:, 2:4], lim[2], lim[3])
+    empty = (rboxes[:, 1] <= rboxes[:, 0]) | (boxes[:, 1] <= boxes[:, 0]) | (boxes[:, 3] <= boxes[:, 2])
+    boxes[empty] = (lim[0], lim[0], lim[2], lim[2], lim[4], lim[4])
+    offs = _offsets(boxes)
+    buf = np.zeros(int(offs[-1]))
+    wind_convolve_boxes(rbuf, roffs, rboxes, kern, kx, ky, separable, buf, offs, boxes)
+    return buf, offs, boxes

@@ -1,0 +1,103 @@
+"""The wind models on the CPU: the oracle's restatement of ``bbarolo/windmodel.py`` against the reference's own
+kernels (``tests/golden/wind.npz``, made by ``tests/golden/make_wind.py``), and the package's host side of
+``bbarolo2_gb300.wind`` (cells, quadrature, beam kernel, host Boxes) against the same fixtures."""
+import numpy as np
+import pytest
+
+import wind_cases as WC
+from golden_io import cases
+
+NAMES = list(WC.CASES)
+
+
+def _case(name):
+    z, idx = cases("wind.npz")
+    return {k.split("/", 1)[1]: z[k] for k in z.files if k.startswith(name + "/")}, idx[name]
+
+
+def _oracle_points(O, a, m, name):
+    c = WC.CASES[name]
+    g = WC.geometry(c["pars"], m["crota2"])
+    from bbarolo2_gb300.wind import WindPars
+    P = WindPars(**c["pars"])
+    return O.wind_points(a["cells"], a["qn"], a["qoff"], P.radii, P.vwind, P.vdisp, P.vrot, P.xpos, P.ypos, g["vsys"],
+                         g["sinc"], g["cinc"], g["spa"], g["cpa"], m["cdelt0"], m["cdelt1"], g["th_in"], g["th_out"],
+                         g["rmax"], m["sig_instr"])
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_wind_points_match_reference(oracle_lib, name):
+    a, m = _case(name)
+    pts = _oracle_points(oracle_lib, a, m, name)
+    for k in ("gx", "gy", "vel", "sig", "w", "r"):
+        np.testing.assert_array_equal(pts[k], a["pts_" + k], err_msg=k)
+    np.testing.assert_array_equal(pts["vol"], a["vol"])
+    np.testing.assert_array_equal(pts["rbar"], a["rbar"])
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_wind_columns_match_reference(oracle_lib, name):
+    """Raw boxes, deposit, grown boxes and convolution of the reference's points: bit-equal to the reference."""
+    O = oracle_lib
+    a, m = _case(name)
+    pts = {k: a["pts_" + k] for k in ("gx", "gy", "vel", "sig", "w", "r")}
+    wt = WC.point_weight(name, pts["r"])
+    w = pts["w"] if wt is None else pts["w"] * wt
+    spec = dict(chmin=m["chmin"], axtyp=m["axtyp"], velsys=m["velsys"], lfreq0=a["lfreq0"], crval3=m["crval3"],
+                cdelt3=m["cdelt3"], crpix3=m["crpix3"])
+    buf, offs, boxes = O.wind_boxes(pts, w, a["lim"], tuple(m["shape"]), a["kern"], a["kx"], a["ky"],
+                                    bool(a["separable"]), spec, a["vedges"], a["relint"], a["qoff"])
+    np.testing.assert_array_equal(boxes, a["boxes"])
+    np.testing.assert_array_equal(offs, a["offs"])
+    np.testing.assert_array_equal(buf, a["buf"])
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_wind_normal_and_model_match_reference(oracle_lib, name):
+    O = oracle_lib
+    a, m = _case(name)
+    shape = tuple(m["shape"])
+    W, d, Wd = WC.weights(name, shape)
+    G, b = O.wind_normal(a["buf"], a["offs"], a["boxes"], Wd, W, a["lim"], m["rel"])
+    np.testing.assert_array_equal(G, a["G"])
+    np.testing.assert_array_equal(b, a["b"])
+    np.testing.assert_array_equal(O.wind_scatter(shape, a["buf"], a["offs"], a["boxes"], a["amp"]), a["model"])
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_host_cells_quadrature_and_beam_match_reference(name):
+    """The package's WindCells, quadrature and beam kernel (no device needed) equal the reference's."""
+    from bbarolo2_gb300 import wind
+    a, m = _case(name)
+    c = WC.CASES[name]
+    wm = wind.WindModel(WC.cube(**c["cube"]), WC.make_cells(wind, c["cells"]), smooth=c["smooth"])
+    wm.quadrature(*c["quad"])
+    np.testing.assert_array_equal(wm.cells.cells, a["cells"])
+    np.testing.assert_array_equal(wm.cells.qn, a["qn"])
+    np.testing.assert_array_equal(wm.cells.qoff, a["qoff"])
+    assert wm.cells.spacing == float(a["spacing"])
+    assert (wm.hx, wm.hy) == tuple(a["hxhy"]) and wm.separable == bool(a["separable"])
+    np.testing.assert_allclose(wm.kern, a["kern"], rtol=1e-13, atol=1e-17)
+    np.testing.assert_allclose(wm.kx, a["kx"], rtol=1e-13)
+    np.testing.assert_allclose(wm.ky, a["ky"], rtol=1e-13)
+    np.testing.assert_allclose(wm.psfq, a["psfq"], rtol=1e-13)
+    np.testing.assert_array_equal(wm.setup._vedges_lines, a["vedges"])
+    assert wm.cdelt == (m["cdelt0"], m["cdelt1"])
+
+
+@pytest.mark.parametrize("name", ["sep", "ell"])
+def test_host_boxes_normal_equals_dense(name):
+    """Host Boxes (the reference's values): G = A'WA and b = A'Wd of the dense columns when nothing is pruned, and
+    the pruned selection equal to the reference's lists."""
+    from bbarolo2_gb300 import wind
+    a, m = _case(name)
+    shape = tuple(m["shape"])
+    W, d, Wd = WC.weights(name, shape)
+    B = wind.Boxes(a["buf"].copy(), a["offs"], a["boxes"])
+    G, b = B.normal(Wd, W, B.voxel_lists(W, a["lim"], rel=m["rel"]))
+    np.testing.assert_allclose(G, a["G"], rtol=1e-12, atol=1e-12 * np.abs(a["G"]).max())
+    np.testing.assert_allclose(b, a["b"], rtol=1e-12, atol=1e-12 * np.abs(a["b"]).max())
+    if m["rel"] == 0:
+        A = B.dense(shape)
+        np.testing.assert_allclose(G, A.T @ (W.ravel()[:, None] * A), rtol=1e-12, atol=1e-12 * np.abs(G).max())
+    np.testing.assert_allclose(B.model(a["amp"], shape), a["model"], rtol=1e-12, atol=1e-15)
