@@ -142,7 +142,7 @@ def load(path=None):
         "bbgpu_wind_boxes": (i, [vp, vp, vp, vp, vp]),
         "bbgpu_wind_columns": (i, [vp, vp, vp]),
         "bbgpu_wind_set_weights": (i, [vp, vp, vp]),
-        "bbgpu_wind_normal": (i, [vp, d, vp, vp]),
+        "bbgpu_wind_normal": (i, [vp, vp, d, vp, vp]),
         "bbgpu_wind_model": (i, [vp, vp, vp]),
     }
     for name, (res, args) in proto.items():

@@ -15,10 +15,10 @@
 //   k_wind_conv_*    one thread per voxel of a box: the beam convolution of each raw box into its grown box, as
 //                    two 1D passes for a separable beam, else with the 2D kernel, each sum in the reference's order
 //                    (windmodel.py:369-423);
-//   k_wind_pairs     the pairs of cells whose boxes intersect (k <= l), appended to a list;
-//   k_wind_gram      one warp per pair: G[k, l] = sum over the intersection of W A_k A_l, and b[k] = sum of A_k Wd
-//                    on the diagonal pairs, over the entries of the voxel lists of the reference (A != 0,
-//                    |A| >= rel x the peak of the column, W != 0; windmodel.py:477-554).
+//   k_wind_lists     the voxel lists of the reference (windmodel.py:477-527): the entries (A != 0, |A| >= rel x
+//                    the peak of the column, W != 0) counted per voxel, offsets by a scan, then written;
+//   k_wind_lists_gram  one warp per voxel: b[k] += A_k Wd and G[k, l] += W A_k A_l over the pairs of its entries
+//                    (windmodel.py:530-554), float64 atomics.
 // Everything is float64, as the reference. The sums differ from the reference's sequential sums by rounding only
 // (the deposits' order is not fixed, and the reductions are trees).
 #include <cuda_runtime.h>
@@ -31,11 +31,13 @@
 
 #include "../../include/bbgpu.h"
 #include "internal.h"
+#include "kernels.h"
 
 #define WIND_PHI_N 6146
 #define WIND_MAXL 4
 #define WIND_MAXRAD 256
 #define WIND_MAXCELL 16384
+#define WIND_SMEM_VALS 26624          // the largest raw box deposited in shared memory (208 KB of 64-bit sums)
 #define W_C_MS 2.99792458e08
 #define FULLMASK 0xffffffffu
 
@@ -81,9 +83,9 @@ struct bbgpu_wind {
     // normal equations
     double *d_W = nullptr, *d_Wd = nullptr, *d_thr = nullptr, *d_G = nullptr, *d_b = nullptr, *d_out = nullptr;
     size_t cap_out = 0;
-    int2 *d_pairs = nullptr;
-    long long cap_pairs = 0;
-    int *d_npairs = nullptr;
+    int *d_cnt = nullptr, *d_start = nullptr, *d_cursor = nullptr, *d_scan = nullptr, *d_ecell = nullptr;
+    double *d_eval = nullptr;
+    size_t cap_cnt = 0, cap_start = 0, cap_cursor = 0, cap_scan = 0, cap_ecell = 0, cap_eval = 0;
     bool have_weights = false;
     int64_t launches = 0;
     std::string err;
@@ -291,27 +293,18 @@ __global__ void __launch_bounds__(256) k_wind_rawbox(const long long *__restrict
     for (int j = 0; j < 6; j++) rbox[6 * (size_t)k + j] = o[j];
 }
 
-// bbarolo/windmodel.py:322-366: one warp per point, lanes over the channels of its line window
-__global__ void __launch_bounds__(256) k_wind_deposit(const int *__restrict__ pcell, long long npts,
-                                                      const double *__restrict__ gx, const double *__restrict__ gy,
-                                                      const double *__restrict__ vel, const double *__restrict__ sig,
-                                                      const double *__restrict__ w, const double *__restrict__ wt,
-                                                      const long long *__restrict__ rbox,
-                                                      const long long *__restrict__ roffs,
-                                                      const double *__restrict__ vedges,
-                                                      const double *__restrict__ ptab, WindGridDev g,
-                                                      double *__restrict__ rbuf) {
-    const long long i = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (i >= npts) return;
-    const double wi = wpoint(w, wt, i), px = gx[i], py = gy[i];
-    if (!wpoint_ok(wi, px, py)) return;
-    const int k = pcell[i];
-    const long long *B = rbox + 6 * (size_t)k;
-    const long long x0 = B[0], x1 = B[1], y0 = B[2], y1 = B[3], k0 = B[4], k1 = B[5];
-    if (x1 <= x0 || y1 <= y0 || k1 <= k0) return;
-    const long long bx = x1 - x0, by = y1 - y0, base = roffs[k];
-    const long long ix = (long long)floor(px), iy = (long long)floor(py);
+// the deposits of point i (bbarolo/windmodel.py:335-366): the channel-integrated line of each line times the
+// bilinear weights, lanes over the channels of the line window; put(offset in the raw box, value)
+template <class Put>
+__device__ __forceinline__ void deposit_point(long long i, double wi, const double *__restrict__ gx,
+                                              const double *__restrict__ gy, const double *__restrict__ vel,
+                                              const double *__restrict__ sig, const long long *B,
+                                              const double *__restrict__ vedges, const double *__restrict__ ptab,
+                                              const WindGridDev &g, int lane, Put put) {
+    const int x0 = (int)B[0], x1 = (int)B[1], y0 = (int)B[2], y1 = (int)B[3], k0 = (int)B[4], k1 = (int)B[5];
+    const int bx = x1 - x0, by = y1 - y0;
+    const double px = gx[i], py = gy[i];
+    const int ix = (int)floor(px), iy = (int)floor(py);
     const double fx = __dsub_rn(px, (double)ix), fy = __dsub_rn(py, (double)iy);
     double s = sig[i];
     const double smin = __dmul_rn(1e-6, g.chmin);
@@ -322,232 +315,372 @@ __global__ void __launch_bounds__(256) k_wind_deposit(const int *__restrict__ pc
     for (int nl = 0; nl < g.nlines; nl++) {
         const long long kc = wround(wvelgrid(v, g, nl));
         long long a0 = kc - K, a1 = kc + K + 1;
-        if (a0 < 0) a0 = 0;
-        if (a1 > g.nz) a1 = g.nz;
+        if (a0 < k0) a0 = k0;                 // (the window clipped to the cube, then to the box)
+        if (a1 > k1) a1 = k1;
         if (a1 <= a0) continue;
         const double *ve = vedges + (size_t)nl * (g.nz + 1);
         const double amp = __dmul_rn(wi, g.relint[nl]);
-        for (long long kz = a0 + lane; kz < a1; kz += 32) {
-            if (kz < k0 || kz >= k1) continue;
+        for (int kz = (int)a0 + lane; kz < (int)a1; kz += 32) {
             const double f = __dsub_rn(wphi(__dmul_rn(__dsub_rn(ve[kz + 1], v), inv), ptab),
                                        wphi(__dmul_rn(__dsub_rn(ve[kz], v), inv), ptab));
             const double pv = __dmul_rn(amp, f >= 0 ? f : -f);
             if (pv == 0.) continue;
             for (int dy = 0; dy < 2; dy++) {
-                const long long yy = iy + dy;
+                const int yy = iy + dy;
                 if (yy < y0 || yy >= y1) continue;
                 const double wy = dy == 1 ? fy : __dsub_rn(1., fy);
-                const long long row = base + ((kz - k0) * by + (yy - y0)) * bx - x0;
+                const int row = ((kz - k0) * by + (yy - y0)) * bx - x0;
                 for (int dx = 0; dx < 2; dx++) {
-                    const long long xx = ix + dx;
+                    const int xx = ix + dx;
                     if (xx < x0 || xx >= x1) continue;
                     const double wx = dx == 1 ? fx : __dsub_rn(1., fx);
-                    atomicAdd(rbuf + row + xx, __dmul_rn(__dmul_rn(pv, wx), wy));
+                    put(row + xx, __dmul_rn(__dmul_rn(pv, wx), wy));
                 }
             }
         }
     }
 }
 
-// the box of flat index v: the largest k with offs[k] <= v (offs non-decreasing, v < offs[n])
-__device__ __forceinline__ int box_of(const long long *__restrict__ offs, int n, long long v) {
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (offs[mid] <= v) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
+__device__ __forceinline__ long long box_size(const long long *B) {
+    return (B[1] - B[0]) * (B[3] - B[2]) * (B[5] - B[4]);
 }
+
+// one CTA per cell whose raw box holds at most maxvals values: its points deposited in shared memory in 64-bit
+// fixed point (units of 2^(E-62), 2^E above the sum of the cell's weights times the lines' |relint|: no overflow;
+// exact sums, independent of their order), the box written once
+__global__ void __launch_bounds__(512) k_wind_deposit_cell(const long long *__restrict__ qoff,
+                                                           const double *__restrict__ gx,
+                                                           const double *__restrict__ gy,
+                                                           const double *__restrict__ vel,
+                                                           const double *__restrict__ sig,
+                                                           const double *__restrict__ w,
+                                                           const double *__restrict__ wt,
+                                                           const long long *__restrict__ rbox,
+                                                           const long long *__restrict__ roffs,
+                                                           const double *__restrict__ vedges,
+                                                           const double *__restrict__ ptab, WindGridDev g,
+                                                           long long maxvals, double *__restrict__ rbuf) {
+    extern __shared__ unsigned long long acc[];
+    __shared__ double red[16];
+    const int k = blockIdx.x;
+    const long long *B = rbox + 6 * (size_t)k;
+    if (B[1] <= B[0] || B[3] <= B[2] || B[5] <= B[4]) return;
+    const int size = (int)box_size(B);
+    if (size > maxvals) return;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int j = threadIdx.x; j < size; j += blockDim.x) acc[j] = 0ull;
+    const long long i0 = qoff[k], i1 = qoff[k + 1];
+    double sw = 0.;
+    for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const double wi = wpoint(w, wt, i);
+        if (wpoint_ok(wi, gx[i], gy[i])) sw += wi;
+    }
+    sw = warp_sum(sw);
+    if (lane == 0) red[wid] = sw;
+    __syncthreads();
+    sw = 0.;
+    for (int j = 0; j < nw; j++) sw += red[j];
+    double rs = 0.;
+    for (int nl = 0; nl < g.nlines; nl++) rs += fabs(g.relint[nl]);
+    int E = 0;
+    frexp(sw * rs * 1.0000001 + 1e-300, &E);
+    const double scale = ldexp(1.0, 62 - E), unit = ldexp(1.0, E - 62);
+    // a thread per point: its line window channel by channel (the CDF carried from one edge to the next, as the
+    // reference), the four bilinear weights times the fixed-point scale computed once per point
+    const int x0 = (int)B[0], x1 = (int)B[1], y0 = (int)B[2], y1 = (int)B[3], k0 = (int)B[4], k1 = (int)B[5];
+    const int bx = x1 - x0, by = y1 - y0;
+    const double smin = __dmul_rn(1e-6, g.chmin);
+    for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const double wi = wpoint(w, wt, i), px = gx[i], py = gy[i];
+        if (!wpoint_ok(wi, px, py)) continue;
+        const int ix = (int)floor(px), iy = (int)floor(py);
+        const double fx = __dsub_rn(px, (double)ix), fy = __dsub_rn(py, (double)iy);
+        const double wx[2] = {__dsub_rn(1., fx), fx}, wy[2] = {__dsub_rn(1., fy), fy};
+        double c4[4];
+        int o4[4];
+        int nc = 0;
+        for (int dy = 0; dy < 2; dy++)
+            for (int dx = 0; dx < 2; dx++) {
+                const int xx = ix + dx, yy = iy + dy;
+                if (xx < x0 || xx >= x1 || yy < y0 || yy >= y1) continue;
+                c4[nc] = wx[dx] * wy[dy] * scale;
+                o4[nc++] = (yy - y0) * bx + (xx - x0);
+            }
+        if (nc == 0) continue;
+        double sg = sig[i];
+        if (sg < smin) sg = smin;
+        const long long K = (long long)__ddiv_rn(__dmul_rn(5.0, sg), g.chmin) + 2;
+        const double inv = __ddiv_rn(1.0, sg);
+        const double v = vel[i];
+        for (int nl = 0; nl < g.nlines; nl++) {
+            const long long kc = wround(wvelgrid(v, g, nl));
+            long long a0 = kc - K, a1 = kc + K + 1;
+            if (a0 < k0) a0 = k0;
+            if (a1 > k1) a1 = k1;
+            if (a1 <= a0) continue;
+            const double *ve = vedges + (size_t)nl * (g.nz + 1);
+            const double amp = __dmul_rn(wi, g.relint[nl]);
+            double pp = wphi(__dmul_rn(__dsub_rn(ve[a0], v), inv), ptab);
+            for (int kz = (int)a0; kz < (int)a1; kz++) {
+                const double pn = wphi(__dmul_rn(__dsub_rn(ve[kz + 1], v), inv), ptab);
+                const double f = __dsub_rn(pn, pp);
+                pp = pn;
+                const double pv = __dmul_rn(amp, f >= 0 ? f : -f);
+                if (pv == 0.) continue;
+                unsigned long long *plane = acc + (size_t)(kz - k0) * by * bx;
+                for (int c = 0; c < nc; c++)
+                    atomicAdd(plane + o4[c], (unsigned long long)__double2ll_rn(pv * c4[c]));
+            }
+        }
+    }
+    __syncthreads();
+    double *out = rbuf + roffs[k];
+    for (int j = threadIdx.x; j < size; j += blockDim.x) out[j] = (double)(long long)acc[j] * unit;
+}
+
+// one warp per point of the cells whose raw box holds more than maxvals values: float64 atomics in global memory
+__global__ void __launch_bounds__(256) k_wind_deposit(const int *__restrict__ pcell, long long npts,
+                                                      const double *__restrict__ gx, const double *__restrict__ gy,
+                                                      const double *__restrict__ vel, const double *__restrict__ sig,
+                                                      const double *__restrict__ w, const double *__restrict__ wt,
+                                                      const long long *__restrict__ rbox,
+                                                      const long long *__restrict__ roffs,
+                                                      const double *__restrict__ vedges,
+                                                      const double *__restrict__ ptab, WindGridDev g,
+                                                      long long maxvals, double *__restrict__ rbuf) {
+    const long long i = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= npts) return;
+    const double wi = wpoint(w, wt, i);
+    if (!wpoint_ok(wi, gx[i], gy[i])) return;
+    const int k = pcell[i];
+    const long long *B = rbox + 6 * (size_t)k;
+    if (B[1] <= B[0] || B[3] <= B[2] || B[5] <= B[4] || box_size(B) <= maxvals) return;
+    double *base = rbuf + roffs[k];
+    deposit_point(i, wi, gx, gy, vel, sig, B, vedges, ptab, g, lane,
+                  [&](int o, double val) { atomicAdd(base + o, val); });
+}
+
+// The beam convolution of the raw boxes: one CTA row block per (box, blockIdx.y), a warp per output row, lanes
+// over its columns; each sum over the taps in the reference's order (raw columns, then raw rows, ascending), as
+// fused multiply-adds (the reference skips the zero values, which add nothing). These kernels are bound by the
+// float64 pipe (two fused multiply-adds per clock per SM on this GPU): no other float64 work per tap.
 
 // bbarolo/windmodel.py:380-393, the x pass of a separable beam: tmp (box k: raw channels x raw rows x grown columns)
 __global__ void __launch_bounds__(256) k_wind_conv_x(const double *__restrict__ rbuf, const long long *__restrict__ roffs,
                                                      const long long *__restrict__ rbox,
                                                      const long long *__restrict__ box,
-                                                     const long long *__restrict__ toffs, int ncell, long long ttot,
+                                                     const long long *__restrict__ toffs,
                                                      const double *__restrict__ kx, int hx, double *__restrict__ tmp) {
-    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= ttot) return;
-    const int k = box_of(toffs, ncell, v);
+    const int k = blockIdx.x;
+    if (toffs[k + 1] == toffs[k]) return;
     const long long *R = rbox + 6 * (size_t)k, *B = box + 6 * (size_t)k;
-    const long long rx0 = R[0], rx1 = R[1], rby = R[3] - R[2], rbx = rx1 - rx0;
-    const long long x0 = B[0], bx = B[1] - x0;
-    const long long loc = v - toffs[k];
-    const long long xx = x0 + loc % bx, y = (loc / bx) % rby, kz = loc / (bx * rby);
-    const double *row = rbuf + roffs[k] + (kz * rby + y) * rbx - rx0;
-    double acc = 0.;
-    const long long xa = std::max(rx0, xx - hx), xb = std::min(rx1 - 1, xx + hx);
-    for (long long x = xa; x <= xb; x++) {
-        const double a = row[x];
-        if (a != 0.) acc = __dadd_rn(acc, __dmul_rn(a, kx[xx - x + hx]));
+    const int rx0 = (int)R[0], rx1 = (int)R[1], rby = (int)(R[3] - R[2]), rbz = (int)(R[5] - R[4]);
+    const int rbx = rx1 - rx0, x0 = (int)B[0], bx = (int)(B[1] - B[0]);
+    const int lane = threadIdx.x & 31, nw = (blockDim.x >> 5) * gridDim.y;
+    const double *src = rbuf + roffs[k];
+    double *dst = tmp + toffs[k];
+    for (int row = (threadIdx.x >> 5) + (blockDim.x >> 5) * blockIdx.y; row < rbz * rby; row += nw) {
+        const double *a = src + (size_t)row * rbx - rx0;
+        double *o = dst + (size_t)row * bx;
+        for (int c = lane; c < bx; c += 32) {
+            const int xx = x0 + c;
+            const int xa = max(rx0, xx - hx), xb = min(rx1 - 1, xx + hx);
+            double acc = 0.;
+            for (int x = xa; x <= xb; x++) acc = fma(a[x], kx[xx - x + hx], acc);
+            o[c] = acc;
+        }
     }
-    tmp[v] = acc;
 }
 
 // bbarolo/windmodel.py:394-401, the y pass of a separable beam: buf (box k) from tmp
 __global__ void __launch_bounds__(256) k_wind_conv_y(const double *__restrict__ tmp, const long long *__restrict__ toffs,
                                                      const long long *__restrict__ rbox,
                                                      const long long *__restrict__ box,
-                                                     const long long *__restrict__ offs, int ncell, long long tot,
+                                                     const long long *__restrict__ offs,
                                                      const double *__restrict__ ky, int hy, double *__restrict__ buf) {
-    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= tot) return;
-    const int k = box_of(offs, ncell, v);
+    const int k = blockIdx.x;
+    if (offs[k + 1] == offs[k] || toffs[k + 1] == toffs[k]) return;
     const long long *R = rbox + 6 * (size_t)k, *B = box + 6 * (size_t)k;
-    const long long ry0 = R[2], ry1 = R[3], rby = ry1 - ry0;
-    const long long bx = B[1] - B[0], by = B[3] - B[2], y0 = B[2];
-    const long long loc = v - offs[k];
-    const long long xl = loc % bx, yy = y0 + (loc / bx) % by, kz = loc / (bx * by);
-    if (R[1] <= R[0] || rby <= 0 || R[5] <= R[4]) {
-        buf[v] = 0.;
-        return;
+    const int ry0 = (int)R[2], ry1 = (int)R[3], rby = ry1 - ry0;
+    const int bx = (int)(B[1] - B[0]), by = (int)(B[3] - B[2]), bz = (int)(B[5] - B[4]), y0 = (int)B[2];
+    const int lane = threadIdx.x & 31, nw = (blockDim.x >> 5) * gridDim.y;
+    const double *src = tmp + toffs[k];
+    double *dst = buf + offs[k];
+    for (int row = (threadIdx.x >> 5) + (blockDim.x >> 5) * blockIdx.y; row < bz * by; row += nw) {
+        const int kz = row / by, yy = y0 + (row - kz * by);
+        const int ya = max(ry0, yy - hy), yb = min(ry1 - 1, yy + hy);
+        const double *t = src + (size_t)kz * rby * bx;
+        double *o = dst + (size_t)row * bx;
+        for (int c = lane; c < bx; c += 32) {
+            double acc = 0.;
+            for (int y = ya; y <= yb; y++) acc = fma(ky[yy - y + hy], t[(size_t)(y - ry0) * bx + c], acc);
+            o[c] = acc;
+        }
     }
-    const double *col = tmp + toffs[k] + kz * rby * bx + xl;
-    double acc = 0.;
-    const long long ya = std::max(ry0, yy - hy), yb = std::min(ry1 - 1, yy + hy);
-    for (long long y = ya; y <= yb; y++) acc = __dadd_rn(acc, __dmul_rn(ky[yy - y + hy], col[(y - ry0) * bx]));
-    buf[v] = acc;
 }
 
 // bbarolo/windmodel.py:402-423: the 2D beam (not separable), kern (2hy+1, 2hx+1)
 __global__ void __launch_bounds__(256) k_wind_conv_2d(const double *__restrict__ rbuf, const long long *__restrict__ roffs,
                                                       const long long *__restrict__ rbox,
                                                       const long long *__restrict__ box,
-                                                      const long long *__restrict__ offs, int ncell, long long tot,
+                                                      const long long *__restrict__ offs,
                                                       const double *__restrict__ kern, int hy, int hx,
                                                       double *__restrict__ buf) {
-    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= tot) return;
-    const int k = box_of(offs, ncell, v);
+    const int k = blockIdx.x;
+    if (offs[k + 1] == offs[k]) return;
     const long long *R = rbox + 6 * (size_t)k, *B = box + 6 * (size_t)k;
-    const long long rx0 = R[0], rx1 = R[1], ry0 = R[2], ry1 = R[3], rbx = rx1 - rx0, rby = ry1 - ry0;
-    const long long bx = B[1] - B[0], by = B[3] - B[2];
-    const long long loc = v - offs[k];
-    const long long xx = B[0] + loc % bx, yy = B[2] + (loc / bx) % by, kz = loc / (bx * by);
-    if (rbx <= 0 || rby <= 0 || R[5] <= R[4]) {
-        buf[v] = 0.;
-        return;
-    }
-    const int kw = 2 * hx + 1;
-    const double *plane = rbuf + roffs[k] + kz * rby * rbx;
-    double acc = 0.;
-    const long long ya = std::max(ry0, yy - hy), yb = std::min(ry1 - 1, yy + hy);
-    const long long xa = std::max(rx0, xx - hx), xb = std::min(rx1 - 1, xx + hx);
-    for (long long y = ya; y <= yb; y++) {
-        const double *row = plane + (y - ry0) * rbx - rx0;
-        const double *kr = kern + (yy - y + hy) * kw + hx + xx;
-        for (long long x = xa; x <= xb; x++) {
-            const double a = row[x];
-            if (a != 0.) acc = __dadd_rn(acc, __dmul_rn(a, kr[-x]));
+    const int rx0 = (int)R[0], rx1 = (int)R[1], ry0 = (int)R[2], ry1 = (int)R[3];
+    const int rbx = rx1 - rx0, rby = ry1 - ry0;
+    if (rbx <= 0 || rby <= 0 || R[5] <= R[4]) return;
+    const int x0 = (int)B[0], bx = (int)(B[1] - B[0]), by = (int)(B[3] - B[2]), bz = (int)(B[5] - B[4]);
+    const int y0 = (int)B[2], kw = 2 * hx + 1;
+    const int lane = threadIdx.x & 31, nw = (blockDim.x >> 5) * gridDim.y;
+    const double *src = rbuf + roffs[k];
+    double *dst = buf + offs[k];
+    for (int row = (threadIdx.x >> 5) + (blockDim.x >> 5) * blockIdx.y; row < bz * by; row += nw) {
+        const int kz = row / by, yy = y0 + (row - kz * by);
+        const int ya = max(ry0, yy - hy), yb = min(ry1 - 1, yy + hy);
+        const double *plane = src + (size_t)kz * rby * rbx;
+        double *o = dst + (size_t)row * bx;
+        for (int c = lane; c < bx; c += 32) {
+            const int xx = x0 + c;
+            const int xa = max(rx0, xx - hx), xb = min(rx1 - 1, xx + hx);
+            double acc = 0.;
+            for (int y = ya; y <= yb; y++) {
+                const double *r = plane + (size_t)(y - ry0) * rbx - rx0;
+                const double *kr = kern + (yy - y + hy) * kw + hx + xx;
+                for (int x = xa; x <= xb; x++) acc = fma(r[x], kr[-x], acc);
+            }
+            o[c] = acc;
         }
     }
-    buf[v] = acc;
 }
 
 // rel x the peak |value| of each column (one CTA per column)
 __global__ void __launch_bounds__(256) k_wind_thr(const double *__restrict__ buf, const long long *__restrict__ offs,
                                                   double rel, double *__restrict__ thr) {
-    __shared__ double red[8];
+    __shared__ unsigned long long red[8];
     const int k = blockIdx.x;
-    double m = 0.;
-    for (long long j = offs[k] + threadIdx.x; j < offs[k + 1]; j += blockDim.x) m = fmax(m, fabs(buf[j]));
-    for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(FULLMASK, m, o));
+    // (the magnitudes compared as integers: the bit patterns of non-negative doubles order as their values)
+    unsigned long long m = 0;
+    for (long long j = offs[k] + threadIdx.x; j < offs[k + 1]; j += blockDim.x) {
+        const unsigned long long a = (unsigned long long)__double_as_longlong(buf[j]) & 0x7fffffffffffffffull;
+        if (a <= 0x7ff0000000000000ull) m = max(m, a);              // (NaN never raises the peak)
+    }
+    for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(FULLMASK, m, o));
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int i = 1; i < (int)(blockDim.x >> 5); i++) m = fmax(m, red[i]);
-        m = fmax(m, red[0]);
-        thr[k] = __dmul_rn(rel, m);
+        for (int i = 1; i < (int)(blockDim.x >> 5); i++) m = max(m, red[i]);
+        thr[k] = __dmul_rn(rel, __longlong_as_double((long long)m));
     }
 }
 
-__device__ __forceinline__ bool box_empty(const long long *B) {
-    return B[1] <= B[0] || B[3] <= B[2] || B[5] <= B[4];
-}
-
-// the pairs (k <= l) of non-empty boxes that intersect; row k of the pairs per blockIdx.y
-__global__ void __launch_bounds__(256) k_wind_pairs(const long long *__restrict__ box, int ncell, long long cap,
-                                                    int2 *__restrict__ pairs, int *__restrict__ npairs) {
-    const int k = blockIdx.y;
-    const long long *A = box + 6 * (size_t)k;
-    if (box_empty(A)) return;
-    for (int l = k + blockIdx.x * blockDim.x + threadIdx.x; l < ncell; l += gridDim.x * blockDim.x) {
-        const long long *B = box + 6 * (size_t)l;
-        if (box_empty(B)) continue;
-        if (std::max(A[0], B[0]) >= std::min(A[1], B[1]) || std::max(A[2], B[2]) >= std::min(A[3], B[3]) ||
-            std::max(A[4], B[4]) >= std::min(A[5], B[5]))
-            continue;
-        const int j = atomicAdd(npairs, 1);
-        if (j < cap) pairs[j] = make_int2(k, l);
-    }
-}
-
-// one warp per pair: G[k, l] = G[l, k] = sum W A_k A_l over the entries of both; b[k] on the diagonal pairs
-__global__ void __launch_bounds__(256) k_wind_gram(const double *__restrict__ buf, const long long *__restrict__ offs,
-                                                   const long long *__restrict__ box, const double *__restrict__ thr,
-                                                   const int2 *__restrict__ pairs, const int *__restrict__ npairs,
-                                                   long long cap, int ncell, int ny, int nx,
-                                                   const double *__restrict__ W, const double *__restrict__ Wd,
-                                                   double *__restrict__ G, double *__restrict__ b) {
-    const int lane = threadIdx.x & 31;
-    const long long np = std::min((long long)*npairs, cap);
-    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long p = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < np; p += nw) {
-        const int2 kl = pairs[p];
-        const long long *A = box + 6 * (size_t)kl.x, *B = box + 6 * (size_t)kl.y;
-        const long long xa = std::max(A[0], B[0]), xb = std::min(A[1], B[1]);
-        const long long ya = std::max(A[2], B[2]), yb = std::min(A[3], B[3]);
-        const long long za = std::max(A[4], B[4]), zb = std::min(A[5], B[5]);
-        const long long lx = xb - xa, ly = yb - ya, n = lx * ly * (zb - za);
-        const long long abx = A[1] - A[0], aby = A[3] - A[2], bbx = B[1] - B[0], bby = B[3] - B[2];
-        const double *ba = buf + offs[kl.x], *bb = buf + offs[kl.y];
-        const double ta = thr[kl.x], tb = thr[kl.y];
-        const bool diag = kl.x == kl.y;
-        double s = 0., sb = 0.;
-        for (long long v = lane; v < n; v += 32) {
-            const long long x = xa + v % lx, y = ya + (v / lx) % ly, z = za + v / (lx * ly);
-            const size_t cv = ((size_t)z * ny + y) * nx + x;
-            const double wv = W[cv];
-            if (wv == 0.) continue;
-            const double a = ba[((z - A[4]) * aby + (y - A[2])) * abx + (x - A[0])];
-            if (a == 0. || !(fabs(a) >= ta)) continue;
-            if (diag) {
-                s = __dadd_rn(s, __dmul_rn(__dmul_rn(wv, a), a));
-                sb = __dadd_rn(sb, __dmul_rn(a, Wd[cv]));
-                continue;
+// The voxel lists of the columns within lim (bbarolo/windmodel.py:477-527): an entry per column value that is
+// != 0, at least thr[k] in magnitude and on a voxel with W != 0. pass 0 counts the entries of each voxel of lim;
+// pass 1 writes them (cell, value) from the voxels' cursors. One CTA per column, a warp per row of its box.
+__global__ void __launch_bounds__(256) k_wind_lists(int pass, const double *__restrict__ buf,
+                                                    const long long *__restrict__ offs,
+                                                    const long long *__restrict__ box,
+                                                    const double *__restrict__ thr, const double *__restrict__ W,
+                                                    int ny, int nx, WindLim lim, int *__restrict__ cnt,
+                                                    int *__restrict__ cursor, int *__restrict__ ecell,
+                                                    double *__restrict__ eval) {
+    const int k = blockIdx.x;
+    const long long *B = box + 6 * (size_t)k;
+    const int bx = (int)(B[1] - B[0]), by = (int)(B[3] - B[2]), bz = (int)(B[5] - B[4]);
+    if (bx <= 0 || by <= 0 || bz <= 0) return;
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int lx = (int)(lim.x1 - lim.x0), ly = (int)(lim.y1 - lim.y0);
+    // (the tests as integers on the bit patterns: |v| >= t for t >= 0, v != 0 and W != 0, off the float64 pipe)
+    const unsigned long long t = (unsigned long long)__double_as_longlong(thr[k]);
+    const double *col = buf + offs[k];
+    for (int row = threadIdx.x >> 5; row < by * bz; row += nw) {
+        const int zr = row / by, yr = row - zr * by;
+        const int z = (int)B[4] + zr, y = (int)B[2] + yr;
+        const double *a = col + (size_t)row * bx;
+        const double *wr = W + ((size_t)z * ny + y) * nx + B[0];
+        const int vrow = ((z - (int)lim.k0) * ly + (y - (int)lim.y0)) * lx + (int)(B[0] - lim.x0);
+        for (int x = lane; x < bx; x += 32) {
+            const double v = a[x];
+            const unsigned long long av = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+            const unsigned long long aw = (unsigned long long)__double_as_longlong(wr[x]) & 0x7fffffffffffffffull;
+            if (av == 0 || av < t || av > 0x7ff0000000000000ull || aw == 0) continue;
+            if (pass == 0) {
+                atomicAdd(cnt + vrow + x, 1);
+            } else {
+                const int j = atomicAdd(cursor + vrow + x, 1);
+                ecell[j] = k;
+                eval[j] = v;
             }
-            const double c = bb[((z - B[4]) * bby + (y - B[2])) * bbx + (x - B[0])];
-            if (c == 0. || !(fabs(c) >= tb)) continue;
-            s = __dadd_rn(s, __dmul_rn(__dmul_rn(wv, a), c));
-        }
-        s = warp_sum(s);
-        if (lane == 0) {
-            G[(size_t)kl.x * ncell + kl.y] = s;
-            G[(size_t)kl.y * ncell + kl.x] = s;
-        }
-        if (diag) {
-            sb = warp_sum(sb);
-            if (lane == 0) b[kl.x] = sb;
         }
     }
 }
 
-// bbarolo/windmodel.py:584-602: out (nz, ny, nx) += amp[k] A_k
+// bbarolo/windmodel.py:530-554: one warp per voxel of lim: b[k] += A_k Wd over its entries and, for every pair of
+// its entries (k <= l), G[k, l] += (W A_k) A_l (float64 atomics; G is made symmetric afterwards)
+__global__ void __launch_bounds__(256) k_wind_lists_gram(const int *__restrict__ cnt, const int *__restrict__ start,
+                                                         const int *__restrict__ ecell,
+                                                         const double *__restrict__ eval, int nvox,
+                                                         const double *__restrict__ W, const double *__restrict__ Wd,
+                                                         int ny, int nx, WindLim lim, int ncell,
+                                                         double *__restrict__ G, double *__restrict__ b) {
+    const long long wv = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (wv >= nvox) return;
+    const int i = (int)wv;
+    const int n = cnt[i];
+    if (n == 0) return;
+    const int lx = (int)(lim.x1 - lim.x0), ly = (int)(lim.y1 - lim.y0);
+    const int x = (int)lim.x0 + i % lx, t = i / lx;
+    const int y = (int)lim.y0 + t % ly, z = (int)lim.k0 + t / ly;
+    const size_t cv = ((size_t)z * ny + y) * nx + x;
+    const double w = W[cv], d = Wd[cv];
+    const int j0 = start[i];
+    for (int p = lane; p < n; p += 32) atomicAdd(b + ecell[j0 + p], __dmul_rn(eval[j0 + p], d));
+    for (int p = 0; p < n; p++) {
+        const int kp = ecell[j0 + p];
+        const double ap = eval[j0 + p];
+        for (int q = p + lane; q < n; q += 32) {
+            const int kq = ecell[j0 + q];
+            const double aq = eval[j0 + q];
+            // (the reference's order: the weight times the value of the lower cell, times the other)
+            if (kp <= kq) atomicAdd(G + (size_t)kp * ncell + kq, __dmul_rn(__dmul_rn(w, ap), aq));
+            else atomicAdd(G + (size_t)kq * ncell + kp, __dmul_rn(__dmul_rn(w, aq), ap));
+        }
+    }
+}
+
+// G[l, k] = G[k, l] for l > k
+__global__ void __launch_bounds__(256) k_wind_sym(double *__restrict__ G, int n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)n * n) return;
+    const int r = (int)(i / n), c = (int)(i - (long long)r * n);
+    if (r > c) G[i] = G[(size_t)c * n + r];
+}
+
+// bbarolo/windmodel.py:584-602: out (nz, ny, nx) += amp[k] A_k (one CTA row block per column, float64 atomics)
 __global__ void __launch_bounds__(256) k_wind_scatter(const double *__restrict__ buf, const long long *__restrict__ offs,
-                                                      const long long *__restrict__ box, int ncell, long long tot,
+                                                      const long long *__restrict__ box,
                                                       const double *__restrict__ amp, int ny, int nx,
                                                       double *__restrict__ out) {
-    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= tot) return;
-    const int k = box_of(offs, ncell, v);
+    const int k = blockIdx.x;
     const double a = amp[k];
-    if (a == 0.) return;
+    if (a == 0. || offs[k + 1] == offs[k]) return;
     const long long *B = box + 6 * (size_t)k;
-    const long long bx = B[1] - B[0], by = B[3] - B[2];
-    const long long loc = v - offs[k];
-    const long long x = B[0] + loc % bx, y = B[2] + (loc / bx) % by, z = B[4] + loc / (bx * by);
-    const double val = buf[v];
-    if (val != 0.) atomicAdd(out + ((size_t)z * ny + y) * nx + x, __dmul_rn(a, val));
+    const int bx = (int)(B[1] - B[0]), by = (int)(B[3] - B[2]), bz = (int)(B[5] - B[4]);
+    const int lane = threadIdx.x & 31, nw = (blockDim.x >> 5) * gridDim.y;
+    const double *src = buf + offs[k];
+    for (int row = (threadIdx.x >> 5) + (blockDim.x >> 5) * blockIdx.y; row < bz * by; row += nw) {
+        const int zr = row / by, z = (int)B[4] + zr, y = (int)B[2] + (row - zr * by);
+        double *o = out + ((size_t)z * ny + y) * nx + B[0];
+        const double *r = src + (size_t)row * bx;
+        for (int c = lane; c < bx; c += 32) {
+            const double v = r[c];
+            if (v != 0.) atomicAdd(o + c, __dmul_rn(a, v));
+        }
+    }
 }
 
 unsigned grid_of(long long n, int per) {
@@ -593,7 +726,8 @@ extern "C" int bbgpu_wind_create(bbgpu_wind **out, int device, const bbgpu_wind_
     if (!out || !g || !lfreq0 || !relint || !vedges || !kern) return BBGPU_ERR_ARG;
     *out = nullptr;
     if (g->nx < 1 || g->ny < 1 || g->nz < 1 || g->nlines < 1 || g->nlines > WIND_MAXL || hx < 0 || hy < 0 ||
-        hx > 255 || hy > 255 || !(g->chmin > 0) || g->cdelt0 == 0 || g->cdelt1 == 0 || g->cdelt3 == 0)
+        hx > 255 || hy > 255 || !(g->chmin > 0) || g->cdelt0 == 0 || g->cdelt1 == 0 || g->cdelt3 == 0 ||
+        (long long)g->nx * g->ny * g->nz >= (1LL << 31))
         return BBGPU_ERR_ARG;
     if (separable && (!kx || !ky)) return BBGPU_ERR_ARG;
     if (cudaSetDevice(device) != cudaSuccess) return BBGPU_ERR_CUDA;
@@ -619,8 +753,7 @@ extern "C" int bbgpu_wind_create(bbgpu_wind **out, int device, const bbgpu_wind_
               cudaMalloc(&w->d_ky, sizeof(double) * (2 * hy + 1)) == cudaSuccess &&
               cudaMalloc(&w->d_vedges, sizeof(double) * ne) == cudaSuccess &&
               cudaMalloc(&w->d_ptab, sizeof(double) * WIND_PHI_N) == cudaSuccess &&
-              cudaMalloc(&w->d_rad, sizeof(double) * 4 * WIND_MAXRAD) == cudaSuccess &&
-              cudaMalloc(&w->d_npairs, sizeof(int)) == cudaSuccess;
+              cudaMalloc(&w->d_rad, sizeof(double) * 4 * WIND_MAXRAD) == cudaSuccess;
     ok = ok && cudaMemcpy(w->d_kern, kern, sizeof(double) * nk, cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(w->d_vedges, vedges, sizeof(double) * ne, cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(w->d_ptab, ptab.data(), sizeof(double) * WIND_PHI_N, cudaMemcpyHostToDevice) == cudaSuccess;
@@ -632,6 +765,12 @@ extern "C" int bbgpu_wind_create(bbgpu_wind **out, int device, const bbgpu_wind_
         bbgpu_wind_destroy(w);
         return BBGPU_ERR_NOMEM;
     }
+    if (cudaFuncSetAttribute(k_wind_deposit_cell, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(sizeof(unsigned long long) * WIND_SMEM_VALS)) != cudaSuccess) {
+        cudaGetLastError();
+        bbgpu_wind_destroy(w);
+        return BBGPU_ERR_CUDA;
+    }
     *out = w;
     return BBGPU_OK;
 }
@@ -639,14 +778,12 @@ extern "C" int bbgpu_wind_create(bbgpu_wind **out, int device, const bbgpu_wind_
 static void free_cells(bbgpu_wind *w) {
     void *ps[] = {w->d_cells, w->d_qn, w->d_qoff, w->d_pcell, w->d_gx, w->d_gy, w->d_vel, w->d_sig, w->d_w,
                   w->d_rr, w->d_vol, w->d_rbar, w->d_weight, w->d_rbox, w->d_box, w->d_roffs, w->d_offs,
-                  w->d_toffs, w->d_thr, w->d_G, w->d_b, w->d_pairs};
+                  w->d_toffs, w->d_thr, w->d_G, w->d_b};
     for (void *p : ps) cudaFree(p);
     w->d_cells = nullptr; w->d_qn = nullptr; w->d_qoff = nullptr; w->d_pcell = nullptr;
     w->d_gx = w->d_gy = w->d_vel = w->d_sig = w->d_w = w->d_rr = w->d_vol = w->d_rbar = w->d_weight = nullptr;
     w->d_rbox = w->d_box = w->d_roffs = w->d_offs = w->d_toffs = nullptr;
     w->d_thr = w->d_G = w->d_b = nullptr;
-    w->d_pairs = nullptr;
-    w->cap_pairs = 0;
     w->ncell = 0;
     w->npts = 0;
     w->have_points = w->have_boxes = false;
@@ -657,8 +794,8 @@ extern "C" int bbgpu_wind_destroy(bbgpu_wind *w) {
     cudaSetDevice(w->device);
     if (w->s) cudaStreamSynchronize(w->s);
     free_cells(w);
-    void *ps[] = {w->d_kern, w->d_kx, w->d_ky, w->d_vedges, w->d_ptab, w->d_rad, w->d_npairs, w->d_rbuf,
-                  w->d_buf, w->d_tmp, w->d_W, w->d_Wd, w->d_out};
+    void *ps[] = {w->d_kern, w->d_kx, w->d_ky, w->d_vedges, w->d_ptab, w->d_rad, w->d_rbuf, w->d_buf, w->d_tmp,
+                  w->d_W, w->d_Wd, w->d_out, w->d_cnt, w->d_start, w->d_cursor, w->d_scan, w->d_ecell, w->d_eval};
     for (void *p : ps) cudaFree(p);
     if (w->s) cudaStreamDestroy(w->s);
     delete w;
@@ -712,8 +849,6 @@ extern "C" int bbgpu_wind_set_cells(bbgpu_wind *w, int ncell, const double *cell
          cudaMalloc(&w->d_roffs, sizeof(long long) * (ncell + 1)) == cudaSuccess &&
          cudaMalloc(&w->d_offs, sizeof(long long) * (ncell + 1)) == cudaSuccess &&
          cudaMalloc(&w->d_toffs, sizeof(long long) * (ncell + 1)) == cudaSuccess;
-    w->cap_pairs = (long long)ncell * (ncell + 1) / 2;
-    ok = ok && cudaMalloc(&w->d_pairs, sizeof(int2) * (size_t)w->cap_pairs) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
         free_cells(w);
@@ -879,27 +1014,43 @@ extern "C" int bbgpu_wind_boxes(bbgpu_wind *w, const int64_t *lim, const double 
                                                 cudaMemcpyHostToDevice, w->s), "up");
     if (!rc) rc = cuda_check(w, cudaMemcpyAsync(w->d_toffs, w->h_toffs.data(), sizeof(long long) * (n + 1),
                                                 cudaMemcpyHostToDevice, w->s), "up");
-    if (!rc && rtot) rc = cuda_check(w, cudaMemsetAsync(w->d_rbuf, 0, sizeof(double) * rtot, w->s), "memset");
     if (rc) return rc;
-    if (rtot)
-        k_wind_deposit<<<grid_of(w->npts * 32, 256), 256, 0, w->s>>>(w->d_pcell, w->npts, w->d_gx, w->d_gy, w->d_vel,
-                                                                     w->d_sig, w->d_w, wt, w->d_rbox, w->d_roffs,
-                                                                     w->d_vedges, w->d_ptab, w->g, w->d_rbuf);
-    if (conv && tot) {
-        if (w->separable) {
-            if (ttot)
-                k_wind_conv_x<<<grid_of(ttot, 256), 256, 0, w->s>>>(w->d_rbuf, w->d_roffs, w->d_rbox, w->d_box,
-                                                                    w->d_toffs, n, ttot, w->d_kx, hx, w->d_tmp);
-            k_wind_conv_y<<<grid_of(tot, 256), 256, 0, w->s>>>(w->d_tmp, w->d_toffs, w->d_rbox, w->d_box, w->d_offs,
-                                                               n, tot, w->d_ky, hy, w->d_buf);
-            w->launches += 2;
-        } else {
-            k_wind_conv_2d<<<grid_of(tot, 256), 256, 0, w->s>>>(w->d_rbuf, w->d_roffs, w->d_rbox, w->d_box,
-                                                                w->d_offs, n, tot, w->d_kern, hy, hx, w->d_buf);
+    if (rtot) {
+        // cells whose raw box fits in shared memory: one CTA each; the others: float64 atomics in global memory
+        long long big = 0;
+        for (int k = 0; k < n; k++) big = std::max(big, w->h_roffs[k + 1] - w->h_roffs[k]);
+        const long long maxvals = std::min(big, (long long)WIND_SMEM_VALS);
+        if (maxvals > 0) {
+            k_wind_deposit_cell<<<n, 512, sizeof(unsigned long long) * maxvals, w->s>>>(
+                w->d_qoff, w->d_gx, w->d_gy, w->d_vel, w->d_sig, w->d_w, wt, w->d_rbox, w->d_roffs, w->d_vedges,
+                w->d_ptab, w->g, maxvals, w->d_rbuf);
+            w->launches++;
+        }
+        if (big > maxvals) {
+            rc = cuda_check(w, cudaMemsetAsync(w->d_rbuf, 0, sizeof(double) * rtot, w->s), "memset");
+            if (rc) return rc;
+            k_wind_deposit<<<grid_of(w->npts * 32, 256), 256, 0, w->s>>>(w->d_pcell, w->npts, w->d_gx, w->d_gy,
+                                                                         w->d_vel, w->d_sig, w->d_w, wt, w->d_rbox,
+                                                                         w->d_roffs, w->d_vedges, w->d_ptab, w->g,
+                                                                         maxvals, w->d_rbuf);
             w->launches++;
         }
     }
-    w->launches += rtot ? 1 : 0;
+    if (conv && tot) {
+        const dim3 cg((unsigned)n, 4);
+        if (w->separable) {
+            if (ttot)
+                k_wind_conv_x<<<cg, 256, 0, w->s>>>(w->d_rbuf, w->d_roffs, w->d_rbox, w->d_box, w->d_toffs,
+                                                    w->d_kx, hx, w->d_tmp);
+            k_wind_conv_y<<<cg, 256, 0, w->s>>>(w->d_tmp, w->d_toffs, w->d_rbox, w->d_box, w->d_offs, w->d_ky, hy,
+                                                w->d_buf);
+            w->launches += 2;
+        } else {
+            k_wind_conv_2d<<<cg, 256, 0, w->s>>>(w->d_rbuf, w->d_roffs, w->d_rbox, w->d_box, w->d_offs, w->d_kern,
+                                                 hy, hx, w->d_buf);
+            w->launches++;
+        }
+    }
     rc = cuda_check(w, cudaGetLastError(), "wind deposit/convolution");
     if (rc) return rc;
     w->total = tot;
@@ -946,41 +1097,61 @@ extern "C" int bbgpu_wind_set_weights(bbgpu_wind *w, const double *wm, const dou
     return rc;
 }
 
-extern "C" int bbgpu_wind_normal(bbgpu_wind *w, double rel, double *G, double *b) {
+extern "C" int bbgpu_wind_normal(bbgpu_wind *w, const int64_t *lim, double rel, double *G, double *b) {
     if (!w || !(rel >= 0.)) return BBGPU_ERR_ARG;
     if (!w->have_boxes) return fail(w, BBGPU_ERR_STATE, "no columns (bbgpu_wind_boxes)");
     if (!w->have_weights) return fail(w, BBGPU_ERR_STATE, "no weights (bbgpu_wind_set_weights)");
     cudaSetDevice(w->device);
     const int n = w->ncell;
+    const int64_t cube[6] = {0, w->g.nx, 0, w->g.ny, 0, w->g.nz};
+    if (!lim) lim = cube;
+    if (lim[0] < 0 || lim[2] < 0 || lim[4] < 0 || lim[1] > w->g.nx || lim[3] > w->g.ny || lim[5] > w->g.nz ||
+        lim[0] > lim[1] || lim[2] > lim[3] || lim[4] > lim[5])
+        return fail(w, BBGPU_ERR_ARG, "lim must lie within the cube");
+    for (int k = 0; k < n; k++) {
+        const long long *B = w->h_box.data() + 6 * (size_t)k;
+        if (B[1] <= B[0] || B[3] <= B[2] || B[5] <= B[4]) continue;
+        if (B[0] < lim[0] || B[1] > lim[1] || B[2] < lim[2] || B[3] > lim[3] || B[4] < lim[4] || B[5] > lim[5])
+            return fail(w, BBGPU_ERR_ARG, "the columns reach outside lim");
+    }
+    const WindLim L{lim[0], lim[1], lim[2], lim[3], lim[4], lim[5]};
+    const long long nvox = (lim[1] - lim[0]) * (lim[3] - lim[2]) * (lim[5] - lim[4]);
+    if (w->total >= (1LL << 31)) return fail(w, BBGPU_ERR_ARG, "more than 2^31 column values");
     const double *buf = columns_ptr(w);
-    int rc = cuda_check(w, cudaMemsetAsync(w->d_G, 0, sizeof(double) * n * (size_t)n, w->s), "memset G");
+    int rc = grow(w, &w->d_cnt, w->cap_cnt, (size_t)nvox + 1);
+    if (!rc) rc = grow(w, &w->d_start, w->cap_start, (size_t)nvox + 1);
+    if (!rc) rc = grow(w, &w->d_cursor, w->cap_cursor, (size_t)nvox + 1);
+    if (!rc) rc = grow(w, &w->d_scan, w->cap_scan, (size_t)(nvox + 1023) / 1024 + 1);
+    if (!rc) rc = grow(w, &w->d_ecell, w->cap_ecell, (size_t)w->total + 1);
+    if (!rc) rc = grow(w, &w->d_eval, w->cap_eval, (size_t)w->total + 1);
+    if (rc) return rc;
+    rc = cuda_check(w, cudaMemsetAsync(w->d_G, 0, sizeof(double) * n * (size_t)n, w->s), "memset G");
     if (!rc) rc = cuda_check(w, cudaMemsetAsync(w->d_b, 0, sizeof(double) * n, w->s), "memset b");
-    if (!rc) rc = cuda_check(w, cudaMemsetAsync(w->d_npairs, 0, sizeof(int), w->s), "memset pairs");
+    if (!rc) rc = cuda_check(w, cudaMemsetAsync(w->d_cnt, 0, sizeof(int) * (size_t)nvox, w->s), "memset counts");
     if (!rc && rel == 0.) rc = cuda_check(w, cudaMemsetAsync(w->d_thr, 0, sizeof(double) * n, w->s), "memset thr");
     if (rc) return rc;
-    if (rel > 0. && w->total) {
-        k_wind_thr<<<n, 256, 0, w->s>>>(buf, w->d_offs, rel, w->d_thr);
-        w->launches++;
+    if (w->total && nvox) {
+        if (rel > 0.) {
+            k_wind_thr<<<n, 256, 0, w->s>>>(buf, w->d_offs, rel, w->d_thr);
+            w->launches++;
+        }
+        k_wind_lists<<<n, 256, 0, w->s>>>(0, buf, w->d_offs, w->d_box, w->d_thr, w->d_W, w->g.ny, w->g.nx, L,
+                                          w->d_cnt, nullptr, nullptr, nullptr);
+        launch_scan_tiles(w->s, w->d_cnt, w->d_start, w->d_cursor, (int)nvox, w->d_scan);
+        k_wind_lists<<<n, 256, 0, w->s>>>(1, buf, w->d_offs, w->d_box, w->d_thr, w->d_W, w->g.ny, w->g.nx, L,
+                                          nullptr, w->d_cursor, w->d_ecell, w->d_eval);
+        k_wind_lists_gram<<<grid_of(nvox * 32, 256), 256, 0, w->s>>>(w->d_cnt, w->d_start, w->d_ecell, w->d_eval,
+                                                                      (int)nvox, w->d_W, w->d_Wd, w->g.ny, w->g.nx,
+                                                                      L, n, w->d_G, w->d_b);
+        k_wind_sym<<<grid_of((long long)n * n, 256), 256, 0, w->s>>>(w->d_G, n);
+        w->launches += 7;
     }
-    if (w->total) {
-        const dim3 pg((unsigned)std::min(64, (n + 255) / 256), (unsigned)n);
-        k_wind_pairs<<<pg, 256, 0, w->s>>>(w->d_box, n, w->cap_pairs, w->d_pairs, w->d_npairs);
-        int dev_sms = 152;
-        cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, w->device);
-        k_wind_gram<<<dev_sms * 8, 256, 0, w->s>>>(buf, w->d_offs, w->d_box, w->d_thr, w->d_pairs, w->d_npairs,
-                                                   w->cap_pairs, n, w->g.ny, w->g.nx, w->d_W, w->d_Wd, w->d_G,
-                                                   w->d_b);
-        w->launches += 2;
-    }
-    rc = cuda_check(w, cudaGetLastError(), "k_wind_gram");
-    int np = 0;
-    if (!rc) rc = cuda_check(w, cudaMemcpyAsync(&np, w->d_npairs, sizeof(int), cudaMemcpyDeviceToHost, w->s), "np");
+    rc = cuda_check(w, cudaGetLastError(), "wind normal equations");
     if (!rc && G) rc = cuda_check(w, cudaMemcpyAsync(G, w->d_G, sizeof(double) * n * (size_t)n,
                                                      cudaMemcpyDeviceToHost, w->s), "G download");
     if (!rc && b) rc = cuda_check(w, cudaMemcpyAsync(b, w->d_b, sizeof(double) * n, cudaMemcpyDeviceToHost, w->s),
                                   "b download");
     if (!rc) rc = cuda_check(w, cudaStreamSynchronize(w->s), "normal equations");
-    if (!rc && np > w->cap_pairs) rc = fail(w, BBGPU_ERR_KERNEL, "pair list overflow");
     return rc;
 }
 
@@ -996,8 +1167,8 @@ extern "C" int bbgpu_wind_model(bbgpu_wind *w, const double *amp, double *out) {
     if (!rc) rc = cuda_check(w, cudaMemsetAsync(w->d_out, 0, sizeof(double) * nv, w->s), "memset");
     if (rc) return rc;
     if (w->total) {
-        k_wind_scatter<<<grid_of(w->total, 256), 256, 0, w->s>>>(columns_ptr(w), w->d_offs, w->d_box, w->ncell,
-                                                                  w->total, d_amp, w->g.ny, w->g.nx, w->d_out);
+        k_wind_scatter<<<dim3((unsigned)w->ncell, 4), 256, 0, w->s>>>(columns_ptr(w), w->d_offs, w->d_box, d_amp,
+                                                                       w->g.ny, w->g.nx, w->d_out);
         w->launches++;
     }
     rc = cuda_check(w, cudaGetLastError(), "k_wind_scatter");

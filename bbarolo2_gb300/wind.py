@@ -367,8 +367,8 @@ class DeviceBoxes(Boxes):
         if self._gen != self._wm._gen_boxes and self._buf is not None:
             return super().normal(wd, wm, lists)
         self._live("normal equations")
-        rel = 0. if lists is None else float(lists[1])
-        return self._wm._normal(wd, wm, rel)
+        lim, rel = (self.lim(), 0.) if lists is None else lists
+        return self._wm._normal(wd, wm, lim, float(rel))
 
     def model(self, amp, shape):
         if tuple(shape) != self._wm.shape:
@@ -573,7 +573,7 @@ class WindModel:
         self._gen_boxes += 1
         return DeviceBoxes(self, boxes, total.value, self._gen_boxes)
 
-    def _normal(self, wd, wm, rel):
+    def _normal(self, wd, wm, lim, rel):
         key = (id(wm), id(wd))
         if self._wkey != key:
             W = np.ascontiguousarray(wm, dtype=np.float64)
@@ -584,7 +584,8 @@ class WindModel:
             self._wkey, self._wref = key, (wm, wd)
         n = self.cells.ncell
         G, b = np.empty((n, n)), np.empty(n)
-        self._call("bbgpu_wind_normal", float(rel), _lib.ptr(G), _lib.ptr(b))
+        lim = np.ascontiguousarray(lim, dtype=np.int64)
+        self._call("bbgpu_wind_normal", _lib.ptr(lim), float(rel), _lib.ptr(G), _lib.ptr(b))
         return G, b
 
     def cube(self, p, amp=None, weight=None, lim=None):

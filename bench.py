@@ -247,6 +247,8 @@ def main():
     ap.add_argument("--no-classic", action="store_true", help="skip the CLASSIC fit of the 64x64x64 workload")
     ap.add_argument("--no-ragged", action="store_true", help="skip the heterogeneous batch of 128 galaxies")
     ap.add_argument("--no-wind", action="store_true", help="skip the WINDFIT normal equations (Circinus shapes)")
+    ap.add_argument("--wind-only", action="store_true",
+                    help="run the WINDFIT leg alone and print its line (for profiling it)")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the per-variant convolution times and errors")
     ap.add_argument("--no-random", action="store_true",
@@ -261,6 +263,11 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
+    if args.wind_only:
+        out = wind_leg(args, dist, world, cpu=rank == 0 and not args.no_cpu)
+        if rank == 0:
+            print(json.dumps({"wind": out}))
+        return 0
     if args.impl == "reference":
         if rank != 0:
             return 0

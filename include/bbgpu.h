@@ -252,9 +252,9 @@ int bbgpu_wind_boxes(bbgpu_wind *w, const int64_t *lim, const double *weight, in
 int bbgpu_wind_columns(bbgpu_wind *w, double *buf, int64_t *offs);
 /* The weights wm and the weighted data wd = wm * data (nz, ny, nx) of the normal equations, kept on the device. */
 int bbgpu_wind_set_weights(bbgpu_wind *w, const double *wm, const double *wd);
-/* G (ncell, ncell) = A'WA and b (ncell) = A'Wd over the voxel-list entries of the columns (value != 0, |value| >=
- * rel x the peak of its column, wm != 0). */
-int bbgpu_wind_normal(bbgpu_wind *w, double rel, double *G, double *b);
+/* G (ncell, ncell) = A'WA and b (ncell) = A'Wd over the voxel lists of the columns within lim (6 integers, NULL:
+ * the cube; the columns must lie inside it): the values != 0, |value| >= rel x the peak of their column, wm != 0. */
+int bbgpu_wind_normal(bbgpu_wind *w, const int64_t *lim, double rel, double *G, double *b);
 /* out (nz, ny, nx) = sum_k amp[k] column k. */
 int bbgpu_wind_model(bbgpu_wind *w, const double *amp, double *out);
 
