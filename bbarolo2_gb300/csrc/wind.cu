@@ -61,7 +61,8 @@ struct bbgpu_wind {
     cudaStream_t s = nullptr;
     WindGridDev g{};
     int hx = 0, hy = 0, separable = 1;
-    double *d_kern = nullptr, *d_kx = nullptr, *d_ky = nullptr, *d_vedges = nullptr, *d_ptab = nullptr;
+    double *d_vedges = nullptr, *d_ptab = nullptr;
+    float2 *d_kern = nullptr, *d_kx = nullptr, *d_ky = nullptr;     // the beam taps as float-float (hi, lo)
     // cells and their quadrature
     int ncell = 0;
     long long npts = 0;
@@ -76,8 +77,10 @@ struct bbgpu_wind {
     // boxes of the last bbgpu_wind_boxes
     long long *d_rbox = nullptr, *d_box = nullptr, *d_roffs = nullptr, *d_offs = nullptr, *d_toffs = nullptr;
     std::vector<long long> h_rbox, h_box, h_offs, h_roffs, h_toffs;
-    double *d_rbuf = nullptr, *d_buf = nullptr, *d_tmp = nullptr;
-    size_t cap_rbuf = 0, cap_buf = 0, cap_tmp = 0;
+    double *d_rbuf = nullptr, *d_buf = nullptr;
+    float2 *d_rff = nullptr, *d_tmp = nullptr;      // raw boxes scaled to [0, 1) and the x pass, float-float
+    int *d_bexp = nullptr;                          // the power of two of each raw box
+    size_t cap_rbuf = 0, cap_buf = 0, cap_tmp = 0, cap_rff = 0;
     long long total = 0;
     bool have_boxes = false;
     // normal equations
@@ -462,70 +465,121 @@ __global__ void __launch_bounds__(256) k_wind_deposit(const int *__restrict__ pc
 }
 
 // The beam convolution of the raw boxes: one CTA row block per (box, blockIdx.y), a warp per output row, lanes
-// over its columns; each sum over the taps in the reference's order (raw columns, then raw rows, ascending), as
-// fused multiply-adds (the reference skips the zero values, which add nothing). These kernels are bound by the
-// float64 pipe (two fused multiply-adds per clock per SM on this GPU): no other float64 work per tap.
+// over its columns; each sum over the taps in the reference's order (raw columns, then raw rows, ascending). The
+// float64 pipe of this GPU does two fused multiply-adds per clock per SM, so the sums run in float-float on the
+// float32 pipes (an unevaluated sum hi + lo of two float32: products with their exact rounding error from an FMA,
+// sums by an error-free two-sum, the low parts accumulated apart; relative error ~1e-14 of the box's peak) on the
+// values of each raw box scaled by a power of two into [0, 1) (k_wind_to_ff), and the result converted back to
+// float64 and unscaled.
+
+// a += x * k in float-float (x, k: hi, lo); the low-order terms of the product and the rounding error of the sum
+// are gathered in al
+__device__ __forceinline__ void ff_fma(float &ah, float &al, float2 x, float2 k) {
+    const float p = __fmul_rn(x.x, k.x);
+    const float e = fmaf(x.x, k.x, -p);
+    const float c = fmaf(x.x, k.y, fmaf(x.y, k.x, e));
+    const float s = __fadd_rn(ah, p);
+    const float bb = __fsub_rn(s, ah);
+    const float err = __fadd_rn(__fsub_rn(ah, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    ah = s;
+    al = __fadd_rn(al, __fadd_rn(err, c));
+}
+
+__device__ __forceinline__ float2 ff_norm(float ah, float al) {
+    const float h = __fadd_rn(ah, al);
+    return make_float2(h, __fsub_rn(al, __fsub_rn(h, ah)));
+}
+
+// one CTA per raw box: its values times 2^-E (2^E above the box's largest magnitude) as float-float, and E
+__global__ void __launch_bounds__(256) k_wind_to_ff(const double *__restrict__ rbuf, const long long *__restrict__ roffs,
+                                                    float2 *__restrict__ rff, int *__restrict__ bexp) {
+    __shared__ unsigned long long red[8];
+    const int k = blockIdx.x;
+    const long long j0 = roffs[k], j1 = roffs[k + 1];
+    if (j1 == j0) return;
+    unsigned long long m = 0;
+    for (long long j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+        const unsigned long long a = (unsigned long long)__double_as_longlong(rbuf[j]) & 0x7fffffffffffffffull;
+        if (a < 0x7ff0000000000000ull) m = max(m, a);
+    }
+    for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(FULLMASK, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) m = max(m, red[i]);
+    int E = 0;
+    if (m) frexp(__longlong_as_double((long long)m), &E);
+    const double sc = ldexp(1.0, -E);
+    for (long long j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+        const double v = __dmul_rn(rbuf[j], sc);
+        const float h = __double2float_rn(v);
+        rff[j] = make_float2(h, __double2float_rn(__dsub_rn(v, (double)h)));
+    }
+    if (threadIdx.x == 0) bexp[k] = E;
+}
 
 // bbarolo/windmodel.py:380-393, the x pass of a separable beam: tmp (box k: raw channels x raw rows x grown columns)
-__global__ void __launch_bounds__(256) k_wind_conv_x(const double *__restrict__ rbuf, const long long *__restrict__ roffs,
+__global__ void __launch_bounds__(256) k_wind_conv_x(const float2 *__restrict__ rff, const long long *__restrict__ roffs,
                                                      const long long *__restrict__ rbox,
                                                      const long long *__restrict__ box,
                                                      const long long *__restrict__ toffs,
-                                                     const double *__restrict__ kx, int hx, double *__restrict__ tmp) {
+                                                     const float2 *__restrict__ kx, int hx, float2 *__restrict__ tmp) {
     const int k = blockIdx.x;
     if (toffs[k + 1] == toffs[k]) return;
     const long long *R = rbox + 6 * (size_t)k, *B = box + 6 * (size_t)k;
     const int rx0 = (int)R[0], rx1 = (int)R[1], rby = (int)(R[3] - R[2]), rbz = (int)(R[5] - R[4]);
     const int rbx = rx1 - rx0, x0 = (int)B[0], bx = (int)(B[1] - B[0]);
     const int lane = threadIdx.x & 31, nw = (blockDim.x >> 5) * gridDim.y;
-    const double *src = rbuf + roffs[k];
-    double *dst = tmp + toffs[k];
+    const float2 *src = rff + roffs[k];
+    float2 *dst = tmp + toffs[k];
     for (int row = (threadIdx.x >> 5) + (blockDim.x >> 5) * blockIdx.y; row < rbz * rby; row += nw) {
-        const double *a = src + (size_t)row * rbx - rx0;
-        double *o = dst + (size_t)row * bx;
+        const float2 *a = src + (size_t)row * rbx - rx0;
+        float2 *o = dst + (size_t)row * bx;
         for (int c = lane; c < bx; c += 32) {
             const int xx = x0 + c;
             const int xa = max(rx0, xx - hx), xb = min(rx1 - 1, xx + hx);
-            double acc = 0.;
-            for (int x = xa; x <= xb; x++) acc = fma(a[x], kx[xx - x + hx], acc);
-            o[c] = acc;
+            float ah = 0.f, al = 0.f;
+            for (int x = xa; x <= xb; x++) ff_fma(ah, al, a[x], kx[xx - x + hx]);
+            o[c] = ff_norm(ah, al);
         }
     }
 }
 
-// bbarolo/windmodel.py:394-401, the y pass of a separable beam: buf (box k) from tmp
-__global__ void __launch_bounds__(256) k_wind_conv_y(const double *__restrict__ tmp, const long long *__restrict__ toffs,
+// bbarolo/windmodel.py:394-401, the y pass of a separable beam: buf (box k, float64) from tmp
+__global__ void __launch_bounds__(256) k_wind_conv_y(const float2 *__restrict__ tmp, const long long *__restrict__ toffs,
                                                      const long long *__restrict__ rbox,
                                                      const long long *__restrict__ box,
                                                      const long long *__restrict__ offs,
-                                                     const double *__restrict__ ky, int hy, double *__restrict__ buf) {
+                                                     const int *__restrict__ bexp, const float2 *__restrict__ ky,
+                                                     int hy, double *__restrict__ buf) {
     const int k = blockIdx.x;
     if (offs[k + 1] == offs[k] || toffs[k + 1] == toffs[k]) return;
     const long long *R = rbox + 6 * (size_t)k, *B = box + 6 * (size_t)k;
     const int ry0 = (int)R[2], ry1 = (int)R[3], rby = ry1 - ry0;
     const int bx = (int)(B[1] - B[0]), by = (int)(B[3] - B[2]), bz = (int)(B[5] - B[4]), y0 = (int)B[2];
     const int lane = threadIdx.x & 31, nw = (blockDim.x >> 5) * gridDim.y;
-    const double *src = tmp + toffs[k];
+    const double sc = ldexp(1.0, bexp[k]);
+    const float2 *src = tmp + toffs[k];
     double *dst = buf + offs[k];
     for (int row = (threadIdx.x >> 5) + (blockDim.x >> 5) * blockIdx.y; row < bz * by; row += nw) {
         const int kz = row / by, yy = y0 + (row - kz * by);
         const int ya = max(ry0, yy - hy), yb = min(ry1 - 1, yy + hy);
-        const double *t = src + (size_t)kz * rby * bx;
+        const float2 *t = src + (size_t)kz * rby * bx;
         double *o = dst + (size_t)row * bx;
         for (int c = lane; c < bx; c += 32) {
-            double acc = 0.;
-            for (int y = ya; y <= yb; y++) acc = fma(ky[yy - y + hy], t[(size_t)(y - ry0) * bx + c], acc);
-            o[c] = acc;
+            float ah = 0.f, al = 0.f;
+            for (int y = ya; y <= yb; y++) ff_fma(ah, al, t[(size_t)(y - ry0) * bx + c], ky[yy - y + hy]);
+            o[c] = __dmul_rn(__dadd_rn((double)ah, (double)al), sc);
         }
     }
 }
 
 // bbarolo/windmodel.py:402-423: the 2D beam (not separable), kern (2hy+1, 2hx+1)
-__global__ void __launch_bounds__(256) k_wind_conv_2d(const double *__restrict__ rbuf, const long long *__restrict__ roffs,
+__global__ void __launch_bounds__(256) k_wind_conv_2d(const float2 *__restrict__ rff, const long long *__restrict__ roffs,
                                                       const long long *__restrict__ rbox,
                                                       const long long *__restrict__ box,
                                                       const long long *__restrict__ offs,
-                                                      const double *__restrict__ kern, int hy, int hx,
+                                                      const int *__restrict__ bexp,
+                                                      const float2 *__restrict__ kern, int hy, int hx,
                                                       double *__restrict__ buf) {
     const int k = blockIdx.x;
     if (offs[k + 1] == offs[k]) return;
@@ -536,23 +590,24 @@ __global__ void __launch_bounds__(256) k_wind_conv_2d(const double *__restrict__
     const int x0 = (int)B[0], bx = (int)(B[1] - B[0]), by = (int)(B[3] - B[2]), bz = (int)(B[5] - B[4]);
     const int y0 = (int)B[2], kw = 2 * hx + 1;
     const int lane = threadIdx.x & 31, nw = (blockDim.x >> 5) * gridDim.y;
-    const double *src = rbuf + roffs[k];
+    const double sc = ldexp(1.0, bexp[k]);
+    const float2 *src = rff + roffs[k];
     double *dst = buf + offs[k];
     for (int row = (threadIdx.x >> 5) + (blockDim.x >> 5) * blockIdx.y; row < bz * by; row += nw) {
         const int kz = row / by, yy = y0 + (row - kz * by);
         const int ya = max(ry0, yy - hy), yb = min(ry1 - 1, yy + hy);
-        const double *plane = src + (size_t)kz * rby * rbx;
+        const float2 *plane = src + (size_t)kz * rby * rbx;
         double *o = dst + (size_t)row * bx;
         for (int c = lane; c < bx; c += 32) {
             const int xx = x0 + c;
             const int xa = max(rx0, xx - hx), xb = min(rx1 - 1, xx + hx);
-            double acc = 0.;
+            float ah = 0.f, al = 0.f;
             for (int y = ya; y <= yb; y++) {
-                const double *r = plane + (size_t)(y - ry0) * rbx - rx0;
-                const double *kr = kern + (yy - y + hy) * kw + hx + xx;
-                for (int x = xa; x <= xb; x++) acc = fma(r[x], kr[-x], acc);
+                const float2 *r = plane + (size_t)(y - ry0) * rbx - rx0;
+                const float2 *kr = kern + (yy - y + hy) * kw + hx + xx;
+                for (int x = xa; x <= xb; x++) ff_fma(ah, al, r[x], kr[-x]);
             }
-            o[c] = acc;
+            o[c] = __dmul_rn(__dadd_rn((double)ah, (double)al), sc);
         }
     }
 }
@@ -748,18 +803,29 @@ extern "C" int bbgpu_wind_create(bbgpu_wind **out, int device, const bbgpu_wind_
     wind_phi_table(ptab);
     const size_t nk = (size_t)(2 * hy + 1) * (2 * hx + 1), ne = (size_t)g->nlines * (g->nz + 1);
     bool ok = cudaStreamCreateWithFlags(&w->s, cudaStreamNonBlocking) == cudaSuccess &&
-              cudaMalloc(&w->d_kern, sizeof(double) * nk) == cudaSuccess &&
-              cudaMalloc(&w->d_kx, sizeof(double) * (2 * hx + 1)) == cudaSuccess &&
-              cudaMalloc(&w->d_ky, sizeof(double) * (2 * hy + 1)) == cudaSuccess &&
+              cudaMalloc(&w->d_kern, sizeof(float2) * nk) == cudaSuccess &&
+              cudaMalloc(&w->d_kx, sizeof(float2) * (2 * hx + 1)) == cudaSuccess &&
+              cudaMalloc(&w->d_ky, sizeof(float2) * (2 * hy + 1)) == cudaSuccess &&
               cudaMalloc(&w->d_vedges, sizeof(double) * ne) == cudaSuccess &&
               cudaMalloc(&w->d_ptab, sizeof(double) * WIND_PHI_N) == cudaSuccess &&
               cudaMalloc(&w->d_rad, sizeof(double) * 4 * WIND_MAXRAD) == cudaSuccess;
-    ok = ok && cudaMemcpy(w->d_kern, kern, sizeof(double) * nk, cudaMemcpyHostToDevice) == cudaSuccess &&
+    auto split = [](const double *v, size_t n) {
+        std::vector<float2> o(n);
+        for (size_t i = 0; i < n; i++) {
+            const float h = (float)v[i];
+            o[i] = make_float2(h, (float)(v[i] - (double)h));
+        }
+        return o;
+    };
+    const std::vector<float2> k2 = split(kern, nk);
+    const std::vector<float2> kx2 = separable ? split(kx, 2 * hx + 1) : std::vector<float2>(2 * hx + 1);
+    const std::vector<float2> ky2 = separable ? split(ky, 2 * hy + 1) : std::vector<float2>(2 * hy + 1);
+    ok = ok && cudaMemcpy(w->d_kern, k2.data(), sizeof(float2) * nk, cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(w->d_vedges, vedges, sizeof(double) * ne, cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(w->d_ptab, ptab.data(), sizeof(double) * WIND_PHI_N, cudaMemcpyHostToDevice) == cudaSuccess;
     if (ok && separable)
-        ok = cudaMemcpy(w->d_kx, kx, sizeof(double) * (2 * hx + 1), cudaMemcpyHostToDevice) == cudaSuccess &&
-             cudaMemcpy(w->d_ky, ky, sizeof(double) * (2 * hy + 1), cudaMemcpyHostToDevice) == cudaSuccess;
+        ok = cudaMemcpy(w->d_kx, kx2.data(), sizeof(float2) * (2 * hx + 1), cudaMemcpyHostToDevice) == cudaSuccess &&
+             cudaMemcpy(w->d_ky, ky2.data(), sizeof(float2) * (2 * hy + 1), cudaMemcpyHostToDevice) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
         bbgpu_wind_destroy(w);
@@ -778,12 +844,13 @@ extern "C" int bbgpu_wind_create(bbgpu_wind **out, int device, const bbgpu_wind_
 static void free_cells(bbgpu_wind *w) {
     void *ps[] = {w->d_cells, w->d_qn, w->d_qoff, w->d_pcell, w->d_gx, w->d_gy, w->d_vel, w->d_sig, w->d_w,
                   w->d_rr, w->d_vol, w->d_rbar, w->d_weight, w->d_rbox, w->d_box, w->d_roffs, w->d_offs,
-                  w->d_toffs, w->d_thr, w->d_G, w->d_b};
+                  w->d_toffs, w->d_thr, w->d_G, w->d_b, w->d_bexp};
     for (void *p : ps) cudaFree(p);
     w->d_cells = nullptr; w->d_qn = nullptr; w->d_qoff = nullptr; w->d_pcell = nullptr;
     w->d_gx = w->d_gy = w->d_vel = w->d_sig = w->d_w = w->d_rr = w->d_vol = w->d_rbar = w->d_weight = nullptr;
     w->d_rbox = w->d_box = w->d_roffs = w->d_offs = w->d_toffs = nullptr;
     w->d_thr = w->d_G = w->d_b = nullptr;
+    w->d_bexp = nullptr;
     w->ncell = 0;
     w->npts = 0;
     w->have_points = w->have_boxes = false;
@@ -795,6 +862,7 @@ extern "C" int bbgpu_wind_destroy(bbgpu_wind *w) {
     if (w->s) cudaStreamSynchronize(w->s);
     free_cells(w);
     void *ps[] = {w->d_kern, w->d_kx, w->d_ky, w->d_vedges, w->d_ptab, w->d_rad, w->d_rbuf, w->d_buf, w->d_tmp,
+                  w->d_rff,
                   w->d_W, w->d_Wd, w->d_out, w->d_cnt, w->d_start, w->d_cursor, w->d_scan, w->d_ecell, w->d_eval};
     for (void *p : ps) cudaFree(p);
     if (w->s) cudaStreamDestroy(w->s);
@@ -842,6 +910,7 @@ extern "C" int bbgpu_wind_set_cells(bbgpu_wind *w, int ncell, const double *cell
     ok = ok && cudaMalloc(&w->d_vol, sizeof(double) * ncell) == cudaSuccess &&
          cudaMalloc(&w->d_rbar, sizeof(double) * ncell) == cudaSuccess &&
          cudaMalloc(&w->d_thr, sizeof(double) * ncell) == cudaSuccess &&
+         cudaMalloc(&w->d_bexp, sizeof(int) * ncell) == cudaSuccess &&
          cudaMalloc(&w->d_b, sizeof(double) * ncell) == cudaSuccess &&
          cudaMalloc(&w->d_G, sizeof(double) * ncell * (size_t)ncell) == cudaSuccess;
     ok = ok && cudaMalloc(&w->d_rbox, sizeof(long long) * 6 * ncell) == cudaSuccess &&
@@ -1006,6 +1075,7 @@ extern "C" int bbgpu_wind_boxes(bbgpu_wind *w, const int64_t *lim, const double 
     rc = grow(w, &w->d_rbuf, w->cap_rbuf, (size_t)rtot);
     if (!rc && conv) rc = grow(w, &w->d_buf, w->cap_buf, (size_t)tot);
     if (!rc && conv && w->separable) rc = grow(w, &w->d_tmp, w->cap_tmp, (size_t)ttot);
+    if (!rc && conv) rc = grow(w, &w->d_rff, w->cap_rff, (size_t)rtot);
     if (rc) return rc;
     rc = cuda_check(w, cudaMemcpyAsync(w->d_box, B, sizeof(long long) * 6 * n, cudaMemcpyHostToDevice, w->s), "up");
     if (!rc) rc = cuda_check(w, cudaMemcpyAsync(w->d_roffs, w->h_roffs.data(), sizeof(long long) * (n + 1),
@@ -1038,17 +1108,18 @@ extern "C" int bbgpu_wind_boxes(bbgpu_wind *w, const int64_t *lim, const double 
     }
     if (conv && tot) {
         const dim3 cg((unsigned)n, 4);
+        k_wind_to_ff<<<n, 256, 0, w->s>>>(w->d_rbuf, w->d_roffs, w->d_rff, w->d_bexp);
         if (w->separable) {
             if (ttot)
-                k_wind_conv_x<<<cg, 256, 0, w->s>>>(w->d_rbuf, w->d_roffs, w->d_rbox, w->d_box, w->d_toffs,
+                k_wind_conv_x<<<cg, 256, 0, w->s>>>(w->d_rff, w->d_roffs, w->d_rbox, w->d_box, w->d_toffs,
                                                     w->d_kx, hx, w->d_tmp);
-            k_wind_conv_y<<<cg, 256, 0, w->s>>>(w->d_tmp, w->d_toffs, w->d_rbox, w->d_box, w->d_offs, w->d_ky, hy,
-                                                w->d_buf);
-            w->launches += 2;
+            k_wind_conv_y<<<cg, 256, 0, w->s>>>(w->d_tmp, w->d_toffs, w->d_rbox, w->d_box, w->d_offs, w->d_bexp,
+                                                w->d_ky, hy, w->d_buf);
+            w->launches += 3;
         } else {
-            k_wind_conv_2d<<<cg, 256, 0, w->s>>>(w->d_rbuf, w->d_roffs, w->d_rbox, w->d_box, w->d_offs, w->d_kern,
-                                                 hy, hx, w->d_buf);
-            w->launches++;
+            k_wind_conv_2d<<<cg, 256, 0, w->s>>>(w->d_rff, w->d_roffs, w->d_rbox, w->d_box, w->d_offs, w->d_bexp,
+                                                 w->d_kern, hy, hx, w->d_buf);
+            w->launches += 2;
         }
     }
     rc = cuda_check(w, cudaGetLastError(), "wind deposit/convolution");
