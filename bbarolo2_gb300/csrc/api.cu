@@ -1963,6 +1963,78 @@ static int an_upload(bbgpu_ctx *ctx, DevBufs &B, const std::vector<AnSub> &subs,
     return 0;
 }
 
+extern "C" int bbgpu_galmod_wind(bbgpu_ctx *ctx, double *out, const double *sr, int nsub, int ring_lo, int ring_hi,
+                                 uint64_t seed, double sep, const int64_t *nv, int blo0, int blo1, int bhi0, int bhi1) {
+    if (!ctx) return BBGPU_ERR_ARG;
+    if (!out || !sr || !nv || ring_lo < 0 || ring_hi > nsub || ring_lo > ring_hi || !(sep > 0))
+        return fail(ctx, BBGPU_ERR_ARG, "galmod_wind: invalid arguments");
+    if (!ctx->grid_set) return fail(ctx, BBGPU_ERR_STATE, "galmod_wind: no grid (bbgpu_set_grid)");
+    CK(cudaSetDevice(ctx->device));
+    const int by = bhi1 - blo1, bx = bhi0 - blo0;
+    if (by <= 0 || bx <= 0 || ring_hi == ring_lo) return BBGPU_OK;
+    WindClouds W;
+    const int e = bbh_wind_clouds(&W, seed, sr, nsub, ring_lo, ring_hi, sep, nv, &ctx->g);
+    if (e) return fail(ctx, BBGPU_ERR_ARG, "galmod_wind: cloud or velocity-sample counts out of range");
+    const long long ncl = (long long)W.shell.size();
+    const size_t n = (size_t)by * bx * ctx->g.nz;
+    if (ncl == 0) return BBGPU_OK;
+    // fixed-point unit: 2^E above the total flux of the deposits
+    double rs = 0., cmax = 0.;
+    for (int l = 0; l < ctx->g.nlines; l++) rs += fabs(ctx->g.relint[l]);
+    for (double c : ctx->h_cd2i) cmax = std::max(cmax, fabs(c));
+    const double bound = W.total * rs * cmax;
+    if (!(bound > 0) || !std::isfinite(bound)) return BBGPU_OK;
+    int E = 0;
+    frexp(bound * 1.0000001, &E);
+    const double scale = ldexp(1.0, 62 - E), unit = ldexp(1.0, E - 62);
+    WindShell *d_sh = nullptr;
+    int *d_shell = nullptr;
+    double *d_geo = nullptr, *d_nrm = nullptr;
+    long long *d_nb = nullptr;
+    unsigned long long *d_acc = nullptr;
+    auto release = [&]() {
+        cudaFree(d_sh); cudaFree(d_shell); cudaFree(d_geo); cudaFree(d_nrm); cudaFree(d_nb); cudaFree(d_acc);
+    };
+    bool ok = cudaMalloc(&d_sh, sizeof(WindShell) * W.shells.size()) == cudaSuccess &&
+              cudaMalloc(&d_shell, sizeof(int) * ncl) == cudaSuccess &&
+              cudaMalloc(&d_geo, sizeof(double) * W.geo.size()) == cudaSuccess &&
+              cudaMalloc(&d_nrm, sizeof(double) * std::max<size_t>(W.normals.size(), 1)) == cudaSuccess &&
+              cudaMalloc(&d_nb, sizeof(long long) * ncl) == cudaSuccess &&
+              cudaMalloc(&d_acc, sizeof(unsigned long long) * n) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        release();
+        return fail(ctx, BBGPU_ERR_NOMEM, "galmod_wind: device allocation failed");
+    }
+    cudaStream_t s = ctx->stream;
+    ok = cudaMemcpyAsync(d_sh, W.shells.data(), sizeof(WindShell) * W.shells.size(), cudaMemcpyHostToDevice, s) ==
+             cudaSuccess &&
+         cudaMemcpyAsync(d_shell, W.shell.data(), sizeof(int) * ncl, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+         cudaMemcpyAsync(d_geo, W.geo.data(), sizeof(double) * W.geo.size(), cudaMemcpyHostToDevice, s) == cudaSuccess &&
+         (W.normals.empty() || cudaMemcpyAsync(d_nrm, W.normals.data(), sizeof(double) * W.normals.size(),
+                                               cudaMemcpyHostToDevice, s) == cudaSuccess) &&
+         cudaMemcpyAsync(d_nb, W.nbase.data(), sizeof(long long) * ncl, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+         cudaMemsetAsync(d_acc, 0, sizeof(unsigned long long) * n, s) == cudaSuccess;
+    if (ok) {
+        launch_wind_mc(s, d_sh, d_shell, d_geo, d_nb, d_nrm, ncl, ctx->g, ctx->d_cd2i, blo0, blo1, bhi0, bhi1, scale,
+                       d_acc);
+        ctx->launches++;
+        ok = cudaGetLastError() == cudaSuccess;
+    }
+    std::vector<unsigned long long> acc;
+    if (ok) {
+        acc.resize(n);
+        ok = cudaMemcpyAsync(acc.data(), d_acc, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost, s) ==
+                 cudaSuccess &&
+             cudaStreamSynchronize(s) == cudaSuccess;
+    }
+    release();
+    if (!ok) return fail(ctx, BBGPU_ERR_CUDA, "galmod_wind: CUDA failure");
+    for (size_t i = 0; i < n; i++)
+        if (acc[i]) out[i] += (double)(long long)acc[i] * unit;
+    return BBGPU_OK;
+}
+
 extern "C" int bbgpu_galmod_analytic(bbgpu_ctx *ctx, double *out, const double *sr, int nsub, int ring_lo, int ring_hi,
                                      int nzq, int blo0, int blo1, int bhi0, int bhi1) {
     if (ctx) ctx->gen++;

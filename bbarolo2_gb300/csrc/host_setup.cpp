@@ -177,6 +177,55 @@ uint64_t bbh_layout_key(uint64_t seed, int ltype, int nsub, const int *nc, const
     return h;
 }
 
+// Parses the stream of _galmod_wind (bbarolo/galmod.py:546-590): per shell its cloud count and constants (each
+// in the reference's float64 operation order, with the C library's sin and cos), per cloud the three uniforms
+// made into its radius, azimuth (cos, sin) and polar angle (sin, cos), and its velocity deviates.
+int bbh_wind_clouds(WindClouds *W, uint64_t seed, const double *sr, int nsub, int lo, int hi, double sep,
+                    const int64_t *nv, const GridDev *g) {
+    if (!W || !sr || !nv || lo < 0 || hi > nsub || lo > hi) return -1;
+    *W = WindClouds();
+    Stream st(seed);
+    auto SRV = [&](int row, int ir) { return sr[(size_t)row * nsub + ir]; };
+    for (int ir = lo; ir < hi; ir++) {
+        const double rtmp = SRV(0, ir);
+        const int64_t nc = lround_ref(g->cdens * pow(SRV(4, ir), (double)g->cmode) * 2 * M_PI * rtmp * sep /
+                                      g->pixarea);
+        if (nc == 0) continue;
+        if (nc < 0 || nc > (1LL << 31) || nv[ir] < 1 || nv[ir] > (1 << 20)) return -2;
+        WindShell s{};
+        s.vrot = SRV(1, ir);
+        s.vsph = SRV(2, ir);
+        const double opentmp = SRV(7, ir) / 2.;
+        s.vdisp = sqrt(SRV(3, ir) * SRV(3, ir) + g->sig_instr * g->sig_instr);
+        s.vsys = SRV(10, ir);
+        s.sinc = sin(SRV(5, ir));
+        s.cinc = cos(SRV(5, ir));
+        const double pa = SRV(6, ir);
+        s.spa = sin(pa) * cos(g->crota2) + cos(pa) * sin(g->crota2);
+        s.cpa = cos(pa) * cos(g->crota2) - sin(pa) * sin(g->crota2);
+        s.xpos = SRV(8, ir);
+        s.ypos = SRV(9, ir);
+        s.nvr = (int)nv[ir];
+        s.fluxsc = SRV(4, ir) * 2 * M_PI * rtmp * sep / (double)(nc * nv[ir]);
+        const int si = (int)W->shells.size();
+        W->shells.push_back(s);
+        const double r_in2 = pow(rtmp - 0.5 * sep, 2.0);
+        for (int64_t ic = 0; ic < nc; ic++) {
+            const double rad = sqrt(r_in2 + 2 * sep * rtmp * fabs(2.0 * st.uniform() - 1.0));
+            const double az = 2 * M_PI * fabs(2.0 * st.uniform() - 1.0);
+            double ph = opentmp * fabs(2.0 * st.uniform() - 1.0);
+            if (ic % 2 == 0) ph = M_PI - ph;
+            W->shell.push_back(si);
+            const double geo[5] = {rad, cos(az), sin(az), sin(ph), cos(ph)};
+            W->geo.insert(W->geo.end(), geo, geo + 5);
+            W->nbase.push_back((long long)W->normals.size());
+            for (int iv = 0; iv < s.nvr; iv++) W->normals.push_back(st.normal());
+        }
+        W->total += (double)nc * s.nvr * fabs(s.fluxsc);
+    }
+    return 0;
+}
+
 // Parses the stream of _galmod_mc (bbarolo/galmod.py:100-144) for clouds counts nc and velocity samples nv
 // per sub-ring: the draws are the same whatever the ring velocities, geometry and box, so each cloud's
 // radius, azimuth, layer deviate and the first word of each of its normals are recorded once.

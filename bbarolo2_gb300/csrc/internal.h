@@ -92,8 +92,29 @@ struct LayoutHost {
 };
 
 #ifdef __cplusplus
+// GALWIND WTYPE 1 (bbarolo/galmod.py:539-590): the constants of a shell with clouds, and the clouds of a stream
+struct WindShell {
+    double fluxsc, vdisp, vsys, vsph, vrot, sinc, cinc, spa, cpa, xpos, ypos;
+    int nvr, pad;
+};
+
+#ifdef __cplusplus
+struct WindClouds {
+    std::vector<WindShell> shells;
+    std::vector<int> shell;             // per cloud: its shell (index into shells)
+    std::vector<double> geo;            // per cloud: rad, cos az, sin az, sin ph, cos ph
+    std::vector<long long> nbase;       // per cloud: its first velocity deviate in normals
+    std::vector<double> normals;        // the velocity deviates of the clouds, in stream order
+    double total = 0.;                  // sum over the clouds of nvr x fluxsc
+};
+#endif
+
 extern "C++" {
 // host_setup.cpp
+// the stream of _galmod_wind for the shells [lo, hi) of sr (11, nsub): per cloud its radius, azimuth, polar angle
+// and velocity deviates (all drawn, as the reference, also for clouds outside any box); 0 or a negative error
+int bbh_wind_clouds(WindClouds *W, uint64_t seed, const double *sr, int nsub, int lo, int hi, double sep,
+                    const int64_t *nv, const GridDev *g);
 void bbh_zig_tables(int64_t *kn, double *wn, double *fn);
 void bbh_phi_table(double *tab);      // 6146 entries
 int bbh_layout_build(LayoutHost *L, uint64_t seed, int ltype, int nsub, const int *nc, const int *nv,

@@ -275,3 +275,9 @@ void launch_an_dens(cudaStream_t s, const GridDev &g, AnSub *sub, int nsub, Memb
 void launch_fill_submc(cudaStream_t s, SubMC *sub, int nsub, int nb, const signed char *reused, const MemberDev *mem,
                        int nlines);
 void launch_fill_copy(cudaStream_t s, void *base, size_t elt_bytes, int nsub, int nb, const signed char *reused);
+
+// GALWIND WTYPE 1 (galwind.cu): one thread per cloud; acc (by, bx, nz) of 64-bit fixed-point sums (units 1/scale)
+void launch_wind_mc(cudaStream_t st, const WindShell *shells, const int *shell, const double *geo,
+                    const long long *nbase, const double *normals, long long ncloud, const GridDev &g,
+                    const double *cd2i, int blo0, int blo1, int bhi0, int bhi1, double scale,
+                    unsigned long long *acc);

@@ -108,6 +108,18 @@ class DiskModel:
                                                   _lib.ptr(nv), int(blo[0]), int(blo[1]), int(bhi[0]), int(bhi[1])))
         return out
 
+    def galmod_wind(self, out, sr, ring_lo, ring_hi, seed, sep, nv, blo, bhi):
+        """``_galmod_wind`` on the device (GALWIND WTYPE 1, ``bbarolo/galmod.py:539-590``): sr (11, nsub) of the
+        shells, out (by, bx, nz) float64 accumulated; the cloud density, CMODE and the lines are this model's."""
+        sr = np.ascontiguousarray(sr, np.float64)
+        nv = np.ascontiguousarray(nv, np.int64)
+        assert out.dtype == np.float64 and out.flags.c_contiguous
+        self.ctx.check(self.ctx.L.bbgpu_galmod_wind(self.ctx.h, _lib.ptr(out), _lib.ptr(sr), sr.shape[1],
+                                                    int(ring_lo), int(ring_hi), int(seed) & 0xFFFFFFFFFFFFFFFF,
+                                                    float(sep), _lib.ptr(nv), int(blo[0]), int(blo[1]), int(bhi[0]),
+                                                    int(bhi[1])))
+        return out
+
     def build(self, rings, blo=(0, 0), bhi=None, seed=None, galmodtype=None, layout="zyx"):
         """The non-convolved model of rings (used as nodes) in [blo, bhi) (``GalmodSetup.build``)."""
         st = self.setup

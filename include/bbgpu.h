@@ -17,6 +17,7 @@
  *   bbgpu_norm                <- _norm(model, data, mask, blo0, blo1, x0, y0, phi, inc, ...)      bbarolo/galfit.py:39-41
  *   bbgpu_eval_*              <- LikelihoodMixin._log_likelihood(theta) for a batch of theta:
  *                                DiskModel.array -> convolve -> _calculate_residuals             bbarolo/bayesian/likelihood.py:567-619
+ *   bbgpu_galmod_wind         <- _galmod_wind(out, sr, ring_lo, ring_hi, seed, sep, nv, ...)      bbarolo/galmod.py:539-542
  *   bbgpu_wind_points         <- _wind_points(cells, qn, qoff, radii, vw, vd, vr, ...)            bbarolo/windmodel.py:225-227
  *   bbgpu_wind_boxes          <- WindModel.boxes(p, lim, pts, weight): _raw_boxes, _deposit_raw,
  *                                _convolve_boxes                                                   bbarolo/windmodel.py:829-859
@@ -94,6 +95,12 @@ int bbgpu_set_cube(bbgpu_ctx *ctx, const float *data, const uint8_t *mask, const
 /* out (bhi1-blo1, bhi0-blo0, nz) float64 is ACCUMULATED (out +=), as the reference kernels. */
 int bbgpu_galmod_mc(bbgpu_ctx *ctx, double *out, const double *sr, int nsub, int ring_lo, int ring_hi,
                     uint64_t seed, const int64_t *nv, int blo0, int blo1, int bhi0, int bhi1);
+/* GALWIND WTYPE 1: the clouds of spherical shells. sr (11, nsub): radius, vrot, vsph, vdisp, dens, inc, pa,
+ * openang, xpos, ypos, vsys (internal units); sep: the shells' thickness (arcmin); the grid's cdens, cmode,
+ * pixarea, cdelt, crota2, sig_instr, spectral axis, lines and cd2i are those of bbgpu_set_grid. out (bhi1-blo1,
+ * bhi0-blo0, nz) float64 is ACCUMULATED. */
+int bbgpu_galmod_wind(bbgpu_ctx *ctx, double *out, const double *sr, int nsub, int ring_lo, int ring_hi,
+                      uint64_t seed, double sep, const int64_t *nv, int blo0, int blo1, int bhi0, int bhi1);
 int bbgpu_galmod_analytic(bbgpu_ctx *ctx, double *out, const double *sr, int nsub, int ring_lo, int ring_hi,
                           int nzq, int blo0, int blo1, int bhi0, int bhi1);
 /* out (nr, bhi1-blo1, bhi0-blo0) float64 accumulated; widx (nsub, 2) int64 (-1: none), wval (nsub, 2). */

@@ -1066,3 +1066,60 @@ void ref_wind_scatter(double *out, int ny, int nx, const double *buf, const int6
             }
     }
 }
+
+/* ------------------------------------------------------------------ _galmod_wind (bbarolo/galmod.py:539-590)
+ * GALWIND WTYPE 1: Monte-Carlo clouds on spherical shells of a bi-cone. out: (ny, nx, nz) float64, accumulated.
+ * sr: (11, nsub): radius, vrot, vsph, vdisp, dens, inc, pa, openang, xpos, ypos, vsys (internal units). */
+void ref_galmod_wind(double *out, int ny, int nx, int nz, const double *sr, int nsub, int ring_lo, int ring_hi,
+                     uint64_t seed, double sep, const int64_t *nv, double cdens, int cmode, double pixarea,
+                     double cdelt0, double cdelt1, double crota2, int64_t blo0, int64_t blo1, int64_t bhi0,
+                     int64_t bhi1, double sig_instr, int axtyp, int velsys, int nlines, const double *lfreq0,
+                     double crval3, double cdelt3, double crpix3, const double *relint, const double *cd2i) {
+    (void)ny;
+    uint64_t st[2];
+    ref_rng_init(seed, st);
+    for (int ir = ring_lo; ir < ring_hi; ir++) {
+        double rtmp = SR(0, ir);
+        int64_t nc = lround_ref(cdens * pow(SR(4, ir), (double)cmode) * 2 * M_PI * rtmp * sep / pixarea);
+        if (nc == 0) continue;
+        double vrottmp = SR(1, ir), vsphtmp = SR(2, ir);
+        double opentmp = SR(7, ir) / 2.;
+        double vdisptmp = sqrt(SR(3, ir) * SR(3, ir) + sig_instr * sig_instr);
+        double vsystmp = SR(10, ir);
+        double sinc = sin(SR(5, ir)), cinc = cos(SR(5, ir));
+        double pa = SR(6, ir);
+        double spa = sin(pa) * cos(crota2) + cos(pa) * sin(crota2);
+        double cpa = cos(pa) * cos(crota2) - sin(pa) * sin(crota2);
+        int64_t nvr = nv[ir];
+        double fluxsc = SR(4, ir) * 2 * M_PI * rtmp * sep / (double)(nc * nvr);
+        double r_in2 = pow(rtmp - 0.5 * sep, 2.0);           /* (the reference's float ** 2) */
+        for (int64_t ic = 0; ic < nc; ic++) {
+            double rad = sqrt(r_in2 + 2 * sep * rtmp * fabs(2.0 * ref_rng_uniform(st) - 1.0));
+            double az = 2 * M_PI * fabs(2.0 * ref_rng_uniform(st) - 1.0);
+            double saz = sin(az), caz = cos(az);
+            double ph = opentmp * fabs(2.0 * ref_rng_uniform(st) - 1.0);
+            if (ic % 2 == 0) ph = M_PI - ph;
+            double sphi = sin(ph), cphi = cos(ph);
+            double R = rad * sphi, z = rad * cphi;
+            double x = R * caz;
+            double y = R * saz * cinc - z * sinc;
+            int64_t g0 = lround_ref(SR(8, ir) + (x * spa - y * cpa) / cdelt0);
+            int64_t g1 = lround_ref(SR(9, ir) + (x * cpa + y * spa) / cdelt1);
+            if (g0 < blo0 || g0 >= bhi0 || g1 < blo1 || g1 >= bhi1) {
+                for (int64_t iv = 0; iv < nvr; iv++) ref_rng_normal(st);
+                continue;
+            }
+            int64_t px = g0 - blo0, py = g1 - blo1;
+            double vs = vsystmp + vsphtmp * (cphi * cinc + sphi * saz * sinc) + vrottmp * caz * sinc;
+            double *o = out + ((size_t)py * nx + (size_t)px) * nz;
+            for (int64_t iv = 0; iv < nvr; iv++) {
+                double v = vs + ref_rng_normal(st) * vdisptmp;
+                for (int nl = 0; nl < nlines; nl++) {
+                    int64_t isubs = lround_ref(velgrid(v, axtyp, velsys, lfreq0[nl], crval3, cdelt3, crpix3));
+                    if (isubs < 0 || isubs >= nz) continue;
+                    o[isubs] += relint[nl] * fluxsc * cd2i[isubs];
+                }
+            }
+        }
+    }
+}

@@ -321,3 +321,19 @@ def wind_boxes(pts, w, lim, shape, kern, kx, ky, separable, spec, vedges, relint
     buf = np.zeros(int(offs[-1]))
     wind_convolve_boxes(rbuf, roffs, rboxes, kern, kx, ky, separable, buf, offs, boxes)
     return buf, offs, boxes
+
+
+def galmod_wind(out, sr, ring_lo, ring_hi, seed, sep, nv, cdens, cmode, pixarea, cdelt0, cdelt1, crota2, blo0,
+                blo1, bhi0, bhi1, sig_instr, axtyp, velsys, lfreq0, crval3, cdelt3, crpix3, relint, cd2i):
+    """``bbarolo/galmod.py:539-590`` with the same arguments; out (ny, nx, nz) float64 is accumulated."""
+    assert out.dtype == np.float64 and out.flags.c_contiguous
+    sr = _f64(sr)
+    nv = np.ascontiguousarray(nv, np.int64)
+    lf, ri, cd = _f64(lfreq0), _f64(relint), _f64(cd2i)
+    ny, nx, nz = out.shape
+    lib().ref_galmod_wind(_ptr(out), _i(ny), _i(nx), _i(nz), _ptr(sr), _i(sr.shape[1]), _i(ring_lo), _i(ring_hi),
+                          _u64(int(seed)), _d(sep), _ptr(nv), _d(cdens), _i(int(cmode)), _d(pixarea), _d(cdelt0),
+                          _d(cdelt1), _d(crota2), _i64(blo0), _i64(blo1), _i64(bhi0), _i64(bhi1), _d(sig_instr),
+                          _i(int(axtyp)), _i(int(velsys)), _i(lf.size), _ptr(lf), _d(crval3), _d(cdelt3), _d(crpix3),
+                          _ptr(ri), _ptr(cd))
+    return out

@@ -6,7 +6,8 @@ Run in a container that has the reference source tree, named by the ``BBAROLO_RE
 
 ``bbarolo/windmodel.py`` is imported with a stub numba (``_refimport.py``), so its kernels run as plain Python:
 ``WindCells`` (cells and quadrature), ``WindModel._set_psf`` (the beam kernel), ``_wind_points``, ``_raw_boxes``,
-``_deposit_raw``, ``_convolve_boxes``, ``_voxel_lists``, ``_normal_lists`` and ``_scatter``. The glue of
+``_deposit_raw``, ``_convolve_boxes``, ``_voxel_lists``, ``_normal_lists`` and ``_scatter``; for GALWIND WTYPE 1
+``bbarolo/galwind.py``'s ``GalWind._shells`` and ``bbarolo/galmod.py``'s ``_galmod_wind``. The glue of
 ``WindModel.boxes`` (``bbarolo/windmodel.py:829-859``) is repeated here around them. The cubes, the spectral
 constants (``GalmodSetup``) and the cases come from the package and ``tests/wind_cases.py``.
 """
@@ -107,10 +108,58 @@ def run_case(name):
     return out, meta
 
 
+def run_galwind(name):
+    """GALWIND WTYPE 1: the reference's GalWind._shells (on a stand-in of the GalWind object) and _galmod_wind over
+    the chunks of shells (the loop of GalWind._spherical, bbarolo/galwind.py:301-331)."""
+    for mod, attrs in (("bbarolo.moments", ("MomentMap",)), ("bbarolo.pvslice", ("PositionVelocity",)),
+                       ("bbarolo.plotscripts", ("run_scripts", "F"))):
+        if mod not in sys.modules:                       # (plotting modules: not needed by the model)
+            m = types.ModuleType(mod)
+            for a in attrs:
+                setattr(m, a, None)
+            sys.modules[mod] = m
+    GW = importlib.import_module("bbarolo.galwind")
+    from bbarolo2_gb300.galwind import GalWindPars, wind_setup
+    c = WC.GW_CASES[name]
+    cube = WC.cube(**c["cube"])
+    p = c["par"]
+    su = wind_setup(cube, GalWindPars(**p))
+    fake = types.SimpleNamespace(par=types.SimpleNamespace(**WC.gw_reference_par(p)),
+                                 _center=lambda: (p["xpos"], p["ypos"]))
+    sr, nv, sep = GW.GalWind._shells(fake, su)
+    nz, ny, nx = cube.DimZ(), cube.DimY(), cube.DimX()
+    (b0, b1), (e0, e1) = c["box"] if c["box"] is not None else ((0, 0), (nx, ny))
+    out = np.zeros((e1 - b1, e0 - b0, nz))
+    nsh = sr.shape[1]
+    chunks = [ch for ch in np.array_split(np.arange(nsh), max(1, min(c["threads"], nsh))) if len(ch)]
+    seed = int(p["iseed"]) & 0xFFFFFFFF
+    for t, ch in enumerate(chunks):
+        buf = np.zeros_like(out)
+        ns.galmod._galmod_wind(buf, sr, int(ch[0]), int(ch[-1]) + 1, (seed + 7919 * t) & 0xFFFFFFFF, sep, nv,
+                               su.cdens, 1, su.pixarea, su.cdelt[0], su.cdelt[1], su.crota2, b0, b1, e0, e1,
+                               su.sig_instr, su.axtyp, su.velsys, su.lfreq0, su.crval3, su.cdelt3, su.crpix3,
+                               su.relint, su.cd2i)
+        out += buf
+    idx = np.flatnonzero(out)
+    arrays = dict(sr=sr, nv=nv, idx=idx, val=out.ravel()[idx], cd2i=su.cd2i, lfreq0=su.lfreq0, relint=su.relint,
+                  chunks=np.array([[int(ch[0]), int(ch[-1]) + 1] for ch in chunks]))
+    meta = dict(sep=sep, cdens=su.cdens, pixarea=su.pixarea, cdelt0=su.cdelt[0], cdelt1=su.cdelt[1],
+                crota2=su.crota2, sig_instr=su.sig_instr, axtyp=int(su.axtyp), velsys=int(su.velsys),
+                crval3=su.crval3, cdelt3=su.cdelt3, crpix3=su.crpix3, seed=seed, box=[[b0, b1], [e0, e1]],
+                shape=list(out.shape))
+    print(f"  {name}: {nsh} shells, {len(chunks)} chunks, {idx.size} voxels with clouds")
+    return arrays, meta
+
+
 def main():
     arrays, index = {}, {}
     for name in WC.CASES:
         out, meta = run_case(name)
+        for k, v in out.items():
+            arrays[f"{name}/{k}"] = np.asarray(v)
+        index[name] = meta
+    for name in WC.GW_CASES:
+        out, meta = run_galwind(name)
         for k, v in out.items():
             arrays[f"{name}/{k}"] = np.asarray(v)
         index[name] = meta

@@ -101,3 +101,40 @@ def test_host_boxes_normal_equals_dense(name):
         A = B.dense(shape)
         np.testing.assert_allclose(G, A.T @ (W.ravel()[:, None] * A), rtol=1e-12, atol=1e-12 * np.abs(G).max())
     np.testing.assert_allclose(B.model(a["amp"], shape), a["model"], rtol=1e-12, atol=1e-15)
+
+
+# ---------------------------------------------------------------------------------------------- GALWIND WTYPE 1
+GW_NAMES = list(WC.GW_CASES)
+
+
+@pytest.mark.parametrize("name", GW_NAMES)
+def test_host_wind_shells_match_reference(name):
+    """The package's shells of a GALWIND WTYPE 1 model equal the reference's GalWind._shells."""
+    from bbarolo2_gb300.galwind import GalWindPars, wind_setup, wind_shells
+    a, m = _case(name)
+    c = WC.GW_CASES[name]
+    par = GalWindPars(**c["par"])
+    sr, nv, sep = wind_shells(par, wind_setup(WC.cube(**c["cube"]), par))
+    np.testing.assert_array_equal(sr, a["sr"])
+    np.testing.assert_array_equal(nv, a["nv"])
+    assert sep == m["sep"]
+
+
+def gw_oracle(O, a, m, ring_lo, ring_hi, seed, out):
+    (b0, b1), (e0, e1) = m["box"]
+    return O.galmod_wind(out, a["sr"], ring_lo, ring_hi, seed, m["sep"], a["nv"], m["cdens"], 1, m["pixarea"],
+                         m["cdelt0"], m["cdelt1"], m["crota2"], b0, b1, e0, e1, m["sig_instr"], m["axtyp"], m["velsys"],
+                         a["lfreq0"], m["crval3"], m["cdelt3"], m["crpix3"], a["relint"], a["cd2i"])
+
+
+@pytest.mark.parametrize("name", GW_NAMES)
+def test_oracle_galmod_wind_matches_reference(oracle_lib, name):
+    """The oracle's _galmod_wind over the chunks of shells, summed in chunk order: bit-equal to the reference's."""
+    a, m = _case(name)
+    out = np.zeros(m["shape"])
+    for t, (lo, hi) in enumerate(a["chunks"]):
+        buf = gw_oracle(oracle_lib, a, m, int(lo), int(hi), (m["seed"] + 7919 * t) & 0xFFFFFFFF, np.zeros(m["shape"]))
+        out += buf
+    idx = np.flatnonzero(out)
+    np.testing.assert_array_equal(idx, a["idx"])
+    np.testing.assert_array_equal(out.ravel()[idx], a["val"])

@@ -76,3 +76,30 @@ def geometry(p, crota2):
     return dict(vsys=p.get("vsys", 0.) * 1000., sinc=math.sin(inc), cinc=math.cos(inc), spa=math.sin(ang),
                 cpa=math.cos(ang), th_in=math.radians(0.5 * p.get("openin", 0.)),
                 th_out=math.radians(0.5 * p["openang"]), rmax=p["conelen"])
+
+
+# GALWIND WTYPE 1 (the Monte-Carlo shells): cube kwargs, the GalWindPars, threads (chunks of shells, one stream each)
+# and the box of the kernel call (None: the cube)
+GW_CASES = {
+    "gw_velo": dict(cube=dict(nx=24, nz=20),
+                    par=dict(xpos=11.5, ypos=11.5, vsys=0., inc=60., phi=45., conelen=140., nlayers=10, vwind=150.,
+                             vdisp=10., dens=10., openang=60., cdens=50., nv=10, iseed=3),
+                    threads=3, box=None),
+    "gw_radii_freq": dict(cube=dict(nx=20, nz=16, pix=8., beam=None, freq=True, crota=15.),
+                          par=dict(xpos=9.7, ypos=10.2, vsys=20., inc=70., phi=-30., conelen=120.,
+                                   radii=[10., 40., 80., 120.], vrot=20., vwind=[100., 150., 200., 180.],
+                                   vdisp=[0., 0., 8., 12.], dens=[5., 3., 2., 1.], openang=[40., 50., 60., 70.],
+                                   cdens=20., nv=-1, iseed=7),
+                          threads=2, box=((3, 2), (17, 19))),
+}
+
+
+def gw_reference_par(p):
+    """The parameters of a GW case as the reference's parameter file gives them (strings for the per-radius
+    values, RADII "-1" when not given)."""
+    def text(v):
+        return " ".join(str(float(x)) for x in np.atleast_1d(v))
+    return dict(PHI=p["phi"], INC=p["inc"], VSYS=p["vsys"], CONELEN=p["conelen"], NLAYERS=p.get("nlayers", 25),
+                RADII="-1" if p.get("radii") is None else text(p["radii"]), VROT=text(p.get("vrot", 0.)),
+                VWIND=text(p["vwind"]), VDISP=text(p["vdisp"]), DENS=text(p["dens"]), OPENANG=text(p["openang"]),
+                NV=p["nv"], CDENS=p["cdens"], ISEED=p["iseed"])
