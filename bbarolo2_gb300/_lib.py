@@ -29,7 +29,7 @@ SYMBOLS = ("bbgpu_ctx_create", "bbgpu_ctx_destroy", "bbgpu_last_error", "bbgpu_v
            "bbgpu_subrings_rows", "bbgpu_conv_variant", "bbgpu_graph_stats", "bbgpu_mlp_create",
            "bbgpu_mlp_destroy", "bbgpu_mlp_nparams", "bbgpu_mlp_get_params", "bbgpu_mlp_set_params",
            "bbgpu_mlp_predict", "bbgpu_mlp_gradients", "bbgpu_mlp_train_step", "bbgpu_mlp_train",
-           "bbgpu_galmod_wind", "bbgpu_wind_create", "bbgpu_wind_destroy", "bbgpu_wind_last_error", "bbgpu_wind_launch_count",
+           "bbgpu_galmod_wind", "bbgpu_galwind_spherical", "bbgpu_wind_create", "bbgpu_wind_destroy", "bbgpu_wind_last_error", "bbgpu_wind_launch_count",
            "bbgpu_wind_set_cells", "bbgpu_wind_points", "bbgpu_wind_set_points", "bbgpu_wind_boxes",
            "bbgpu_wind_columns", "bbgpu_wind_set_weights", "bbgpu_wind_normal", "bbgpu_wind_model")
 
@@ -133,6 +133,7 @@ def load(path=None):
         "bbgpu_eval_profile": (i, [vp, vp, vp]),
         "bbgpu_solve_profile": (i, [vp, vp, vp, i, i, vp, d, d, d, vp, vp]),
         "bbgpu_galmod_wind": (i, [vp, vp, vp, i, i, i, u64, d, vp, i, i, i, i]),
+        "bbgpu_galwind_spherical": (i, [vp, vp, vp, i, i, vp, vp, vp, d, vp, i, i, i, i, i]),
         "bbgpu_wind_create": (i, [C.POINTER(vp), i, C.POINTER(WindGrid), vp, vp, vp, vp, i, i, vp, vp, i]),
         "bbgpu_wind_destroy": (i, [vp]),
         "bbgpu_wind_last_error": (C.c_char_p, [vp]),

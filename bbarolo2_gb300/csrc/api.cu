@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <array>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/bbgpu.h"
@@ -1963,26 +1964,29 @@ static int an_upload(bbgpu_ctx *ctx, DevBufs &B, const std::vector<AnSub> &subs,
     return 0;
 }
 
-extern "C" int bbgpu_galmod_wind(bbgpu_ctx *ctx, double *out, const double *sr, int nsub, int ring_lo, int ring_hi,
-                                 uint64_t seed, double sep, const int64_t *nv, int blo0, int blo1, int bhi0, int bhi1) {
-    if (!ctx) return BBGPU_ERR_ARG;
-    if (!out || !sr || !nv || ring_lo < 0 || ring_hi > nsub || ring_lo > ring_hi || !(sep > 0))
-        return fail(ctx, BBGPU_ERR_ARG, "galmod_wind: invalid arguments");
-    if (!ctx->grid_set) return fail(ctx, BBGPU_ERR_STATE, "galmod_wind: no grid (bbgpu_set_grid)");
-    CK(cudaSetDevice(ctx->device));
+// The clouds of one or more chunks of shells (each parsed from its own stream) placed and deposited in one pass:
+// the fixed-point sums are exact, so the chunks' deposits add in any order; out += the sum of the chunks.
+static int wind_mc_run(bbgpu_ctx *ctx, double *out, std::vector<WindClouds> &chunks, int blo0, int blo1, int bhi0,
+                       int bhi1) {
     const int by = bhi1 - blo1, bx = bhi0 - blo0;
-    if (by <= 0 || bx <= 0 || ring_hi == ring_lo) return BBGPU_OK;
-    WindClouds W;
-    const int e = bbh_wind_clouds(&W, seed, sr, nsub, ring_lo, ring_hi, sep, nv, &ctx->g);
-    if (e) return fail(ctx, BBGPU_ERR_ARG, "galmod_wind: cloud or velocity-sample counts out of range");
-    const long long ncl = (long long)W.shell.size();
     const size_t n = (size_t)by * bx * ctx->g.nz;
+    // the chunks' arrays go to the device at their offsets (shell indices and deviate offsets shifted)
+    size_t nsh = 0, ncl = 0, nnrm = 0;
+    double total = 0.;
+    for (WindClouds &c : chunks) {
+        for (int &v : c.shell) v += (int)nsh;
+        for (long long &v : c.nbase) v += (long long)nnrm;
+        nsh += c.shells.size();
+        ncl += c.shell.size();
+        nnrm += c.normals.size();
+        total += c.total;
+    }
     if (ncl == 0) return BBGPU_OK;
     // fixed-point unit: 2^E above the total flux of the deposits
     double rs = 0., cmax = 0.;
     for (int l = 0; l < ctx->g.nlines; l++) rs += fabs(ctx->g.relint[l]);
     for (double c : ctx->h_cd2i) cmax = std::max(cmax, fabs(c));
-    const double bound = W.total * rs * cmax;
+    const double bound = total * rs * cmax;
     if (!(bound > 0) || !std::isfinite(bound)) return BBGPU_OK;
     int E = 0;
     frexp(bound * 1.0000001, &E);
@@ -1995,10 +1999,10 @@ extern "C" int bbgpu_galmod_wind(bbgpu_ctx *ctx, double *out, const double *sr, 
     auto release = [&]() {
         cudaFree(d_sh); cudaFree(d_shell); cudaFree(d_geo); cudaFree(d_nrm); cudaFree(d_nb); cudaFree(d_acc);
     };
-    bool ok = cudaMalloc(&d_sh, sizeof(WindShell) * W.shells.size()) == cudaSuccess &&
+    bool ok = cudaMalloc(&d_sh, sizeof(WindShell) * nsh) == cudaSuccess &&
               cudaMalloc(&d_shell, sizeof(int) * ncl) == cudaSuccess &&
-              cudaMalloc(&d_geo, sizeof(double) * W.geo.size()) == cudaSuccess &&
-              cudaMalloc(&d_nrm, sizeof(double) * std::max<size_t>(W.normals.size(), 1)) == cudaSuccess &&
+              cudaMalloc(&d_geo, sizeof(double) * 5 * ncl) == cudaSuccess &&
+              cudaMalloc(&d_nrm, sizeof(double) * std::max<size_t>(nnrm, 1)) == cudaSuccess &&
               cudaMalloc(&d_nb, sizeof(long long) * ncl) == cudaSuccess &&
               cudaMalloc(&d_acc, sizeof(unsigned long long) * n) == cudaSuccess;
     if (!ok) {
@@ -2007,17 +2011,24 @@ extern "C" int bbgpu_galmod_wind(bbgpu_ctx *ctx, double *out, const double *sr, 
         return fail(ctx, BBGPU_ERR_NOMEM, "galmod_wind: device allocation failed");
     }
     cudaStream_t s = ctx->stream;
-    ok = cudaMemcpyAsync(d_sh, W.shells.data(), sizeof(WindShell) * W.shells.size(), cudaMemcpyHostToDevice, s) ==
-             cudaSuccess &&
-         cudaMemcpyAsync(d_shell, W.shell.data(), sizeof(int) * ncl, cudaMemcpyHostToDevice, s) == cudaSuccess &&
-         cudaMemcpyAsync(d_geo, W.geo.data(), sizeof(double) * W.geo.size(), cudaMemcpyHostToDevice, s) == cudaSuccess &&
-         (W.normals.empty() || cudaMemcpyAsync(d_nrm, W.normals.data(), sizeof(double) * W.normals.size(),
-                                               cudaMemcpyHostToDevice, s) == cudaSuccess) &&
-         cudaMemcpyAsync(d_nb, W.nbase.data(), sizeof(long long) * ncl, cudaMemcpyHostToDevice, s) == cudaSuccess &&
-         cudaMemsetAsync(d_acc, 0, sizeof(unsigned long long) * n, s) == cudaSuccess;
+    ok = cudaMemsetAsync(d_acc, 0, sizeof(unsigned long long) * n, s) == cudaSuccess;
+    size_t o_sh = 0, o_cl = 0, o_n = 0;
+    for (const WindClouds &c : chunks) {
+        auto up = [&](void *dst, const void *src, size_t bytes) {
+            return !bytes || cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s) == cudaSuccess;
+        };
+        ok = ok && up(d_sh + o_sh, c.shells.data(), sizeof(WindShell) * c.shells.size()) &&
+             up(d_shell + o_cl, c.shell.data(), sizeof(int) * c.shell.size()) &&
+             up(d_geo + 5 * o_cl, c.geo.data(), sizeof(double) * c.geo.size()) &&
+             up(d_nb + o_cl, c.nbase.data(), sizeof(long long) * c.nbase.size()) &&
+             up(d_nrm + o_n, c.normals.data(), sizeof(double) * c.normals.size());
+        o_sh += c.shells.size();
+        o_cl += c.shell.size();
+        o_n += c.normals.size();
+    }
     if (ok) {
-        launch_wind_mc(s, d_sh, d_shell, d_geo, d_nb, d_nrm, ncl, ctx->g, ctx->d_cd2i, blo0, blo1, bhi0, bhi1, scale,
-                       d_acc);
+        launch_wind_mc(s, d_sh, d_shell, d_geo, d_nb, d_nrm, (long long)ncl, ctx->g, ctx->d_cd2i, blo0, blo1, bhi0,
+                       bhi1, scale, d_acc);
         ctx->launches++;
         ok = cudaGetLastError() == cudaSuccess;
     }
@@ -2033,6 +2044,55 @@ extern "C" int bbgpu_galmod_wind(bbgpu_ctx *ctx, double *out, const double *sr, 
     for (size_t i = 0; i < n; i++)
         if (acc[i]) out[i] += (double)(long long)acc[i] * unit;
     return BBGPU_OK;
+}
+
+static int wind_args(bbgpu_ctx *ctx, const double *out, const double *sr, const int64_t *nv, double sep) {
+    if (!out || !sr || !nv || !(sep > 0)) return fail(ctx, BBGPU_ERR_ARG, "galmod_wind: invalid arguments");
+    if (!ctx->grid_set) return fail(ctx, BBGPU_ERR_STATE, "galmod_wind: no grid (bbgpu_set_grid)");
+    return BBGPU_OK;
+}
+
+extern "C" int bbgpu_galmod_wind(bbgpu_ctx *ctx, double *out, const double *sr, int nsub, int ring_lo, int ring_hi,
+                                 uint64_t seed, double sep, const int64_t *nv, int blo0, int blo1, int bhi0, int bhi1) {
+    if (!ctx) return BBGPU_ERR_ARG;
+    int rc = wind_args(ctx, out, sr, nv, sep);
+    if (rc) return rc;
+    if (ring_lo < 0 || ring_hi > nsub || ring_lo > ring_hi) return fail(ctx, BBGPU_ERR_ARG, "galmod_wind: shells");
+    CK(cudaSetDevice(ctx->device));
+    if (bhi1 <= blo1 || bhi0 <= blo0 || ring_hi == ring_lo) return BBGPU_OK;
+    std::vector<WindClouds> W(1);
+    if (bbh_wind_clouds(&W[0], seed, sr, nsub, ring_lo, ring_hi, sep, nv, &ctx->g))
+        return fail(ctx, BBGPU_ERR_ARG, "galmod_wind: cloud or velocity-sample counts out of range");
+    return wind_mc_run(ctx, out, W, blo0, blo1, bhi0, bhi1);
+}
+
+extern "C" int bbgpu_galwind_spherical(bbgpu_ctx *ctx, double *out, const double *sr, int nsub, int nchunks,
+                                       const int *chunk_lo, const int *chunk_hi, const uint64_t *seeds, double sep,
+                                       const int64_t *nv, int blo0, int blo1, int bhi0, int bhi1, int threads) {
+    if (!ctx) return BBGPU_ERR_ARG;
+    int rc = wind_args(ctx, out, sr, nv, sep);
+    if (rc) return rc;
+    if (nchunks < 0 || (nchunks && (!chunk_lo || !chunk_hi || !seeds)))
+        return fail(ctx, BBGPU_ERR_ARG, "galwind_spherical: chunks");
+    for (int c = 0; c < nchunks; c++)
+        if (chunk_lo[c] < 0 || chunk_hi[c] > nsub || chunk_lo[c] > chunk_hi[c])
+            return fail(ctx, BBGPU_ERR_ARG, "galwind_spherical: a chunk outside the shells");
+    CK(cudaSetDevice(ctx->device));
+    if (bhi1 <= blo1 || bhi0 <= blo0 || nchunks == 0) return BBGPU_OK;
+    // the chunks' streams parsed on host threads (each chunk its own stream), then one device pass
+    std::vector<WindClouds> W(nchunks);
+    std::vector<int> err(nchunks, 0);
+    const int nt = std::max(1, std::min(threads, nchunks));
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; t++)
+        pool.emplace_back([&, t]() {
+            for (int c = t; c < nchunks; c += nt)
+                err[c] = bbh_wind_clouds(&W[c], seeds[c], sr, nsub, chunk_lo[c], chunk_hi[c], sep, nv, &ctx->g);
+        });
+    for (std::thread &th : pool) th.join();
+    for (int e : err)
+        if (e) return fail(ctx, BBGPU_ERR_ARG, "galwind_spherical: cloud or velocity-sample counts out of range");
+    return wind_mc_run(ctx, out, W, blo0, blo1, bhi0, bhi1);
 }
 
 extern "C" int bbgpu_galmod_analytic(bbgpu_ctx *ctx, double *out, const double *sr, int nsub, int ring_lo, int ring_hi,

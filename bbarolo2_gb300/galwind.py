@@ -102,18 +102,29 @@ class GalWindMC:
         self.cube, self.par, self.threads = cube, par, int(threads)
         self.dm = DiskModel(cube, par=wind_gmpar(cube, par), densflux=False, smooth=False, device=device)
         self.setup = self.dm.setup
-        self.sr, self.nv, self.sep = wind_shells(par, self.setup)
+        sr, nv, self.sep = wind_shells(par, self.setup)
+        self.sr, self.nv = np.ascontiguousarray(sr, np.float64), np.ascontiguousarray(nv, np.int64)
 
     def chunks(self):
         ns = self.sr.shape[1]
         n = max(1, min(self.threads, ns))
         return [c for c in np.array_split(np.arange(ns), n) if len(c)]
 
-    def model(self):
+    def model(self, host_threads=None):
+        """The model cube (nz, ny, nx): the chunks' streams parsed on host_threads threads (default: as many as
+        the chunks, at most the host's cores), every cloud deposited in one device pass."""
+        import os
+        from . import _lib
         c = self.cube
         out = np.zeros((c.DimY(), c.DimX(), c.DimZ()))
         seed = int(self.par.ISEED) & 0xFFFFFFFF
-        for t, ch in enumerate(self.chunks()):
-            self.dm.galmod_wind(out, self.sr, int(ch[0]), int(ch[-1]) + 1, (seed + 7919 * t) & 0xFFFFFFFF,
-                                self.sep, self.nv, (0, 0), (c.DimX(), c.DimY()))
+        ch = self.chunks()
+        lo = np.array([int(x[0]) for x in ch], dtype=np.int32)
+        hi = np.array([int(x[-1]) + 1 for x in ch], dtype=np.int32)
+        seeds = np.array([(seed + 7919 * t) & 0xFFFFFFFF for t in range(len(ch))], dtype=np.uint64)
+        nt = host_threads or min(len(ch), os.cpu_count() or 1)
+        ctx = self.dm.ctx
+        ctx.check(ctx.L.bbgpu_galwind_spherical(ctx.h, _lib.ptr(out), _lib.ptr(self.sr), self.sr.shape[1], len(ch),
+                                                _lib.ptr(lo), _lib.ptr(hi), _lib.ptr(seeds), float(self.sep),
+                                                _lib.ptr(self.nv), 0, 0, c.DimX(), c.DimY(), int(nt)))
         return np.ascontiguousarray(out.transpose(2, 0, 1))

@@ -247,8 +247,9 @@ def main():
     ap.add_argument("--no-classic", action="store_true", help="skip the CLASSIC fit of the 64x64x64 workload")
     ap.add_argument("--no-ragged", action="store_true", help="skip the heterogeneous batch of 128 galaxies")
     ap.add_argument("--no-wind", action="store_true", help="skip the WINDFIT normal equations (Circinus shapes)")
+    ap.add_argument("--no-galwind", action="store_true", help="skip the GALWIND WTYPE 1 model")
     ap.add_argument("--wind-only", action="store_true",
-                    help="run the WINDFIT leg alone and print its line (for profiling it)")
+                    help="run the WINDFIT and GALWIND legs alone and print their line (for profiling them)")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the per-variant convolution times and errors")
     ap.add_argument("--no-random", action="store_true",
@@ -264,9 +265,11 @@ def main():
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
     if args.wind_only:
-        out = wind_leg(args, dist, world, cpu=rank == 0 and not args.no_cpu)
+        out = {"wind": wind_leg(args, dist, world, cpu=rank == 0 and not args.no_cpu)}
+        if not args.no_galwind:
+            out["galwind"] = galwind_leg(args, dist, world, cpu=rank == 0 and not args.no_cpu)
         if rank == 0:
-            print(json.dumps({"wind": out}))
+            print(json.dumps(out))
         return 0
     if args.impl == "reference":
         if rank != 0:
@@ -394,6 +397,8 @@ def main():
         line["ragged"] = ragged_leg(args, dist, world)
     if not args.no_wind:
         line["wind"] = wind_leg(args, dist, world, cpu=rank == 0 and not args.no_cpu)
+    if not args.no_galwind:
+        line["galwind"] = galwind_leg(args, dist, world, cpu=rank == 0 and not args.no_cpu)
     if not args.no_bayes:
         line["bayes256"] = bayes256_leg(args, dist, world, nb=args.bayes_nb)
         if not args.no_bayes_fit:
@@ -682,6 +687,51 @@ def wind_leg(args, dist, world, cpu=True):
         out["max_rel_err_b"] = float(np.abs(b - bo).max() / np.abs(bo).max())
         out["boxes_equal"] = bool(np.array_equal(B.boxes, boxes))
     wm.close()
+    return out
+
+
+def galwind_leg(args, dist, world, cpu=True):
+    """GALWIND WTYPE 1 (the Monte-Carlo shells of a bi-cone, ``galwind.GalWindMC``) on a 128x128x64 cube of 4"
+    pixels and 10 km/s channels: CONELEN 240" (80 shells 3" apart), OPENANG 60, VWIND 300, VDISP 20 km/s, DENS 10,
+    CDENS 20, NV 20, INC 60, PHI 45, 16 chunks of shells (THREADS 16): the model's wall time through the public API
+    (streams parsed on host threads, clouds placed and deposited on the device, the cube read back). The CPU leg: the
+    oracle (the reference's _galmod_wind restated in C, one thread) over the same chunks; parity: the two models."""
+    from bbarolo2_gb300.cube import Cube, Params
+    from bbarolo2_gb300.galwind import GalWindMC, GalWindPars
+    cube = Cube.empty(128, 128, 64, [-4. / 3600., 4. / 3600., 10.], par=Params(), crpix=[64.5, 64.5, 32.5],
+                      crval=[60., 0., 0.], cunit=("deg", "deg", "km/s"))
+    par = GalWindPars(xpos=63.5, ypos=63.5, vsys=0., inc=60., phi=45., conelen=240., nlayers=30, vwind=300.,
+                      vdisp=20., dens=10., openang=60., cdens=20., nv=20, iseed=3)
+    gw = GalWindMC(cube, par, threads=16)
+    for _ in range(max(2, args.warmup)):
+        mod = gw.model()
+    steps = max(3, args.steps // 4)
+    t = time.perf_counter()
+    for _ in range(steps):
+        mod = gw.model()
+    dt = max_over_ranks(time.perf_counter() - t, dist)
+    st = gw.setup
+    nc = np.rint(st.cdens * gw.sr[4] * 2 * math.pi * gw.sr[0] * gw.sep / st.pixarea)
+    out = {"workload": "galwind_shells: 128x128x64 voxels, %d shells, %d clouds, %d velocity samples, 16 chunks"
+                       % (gw.sr.shape[1], int(nc.sum()), int((nc * gw.nv).sum())),
+           "metric": "GALWIND WTYPE 1 models/s (streams parsed, clouds deposited, cube read back)",
+           "value": throughput(1, steps, world, dt), "ms_per_model": 1e3 * dt / steps}
+    if cpu:
+        from oracle import oracle as O
+        ref = np.zeros((cube.DimY(), cube.DimX(), cube.DimZ()))
+        seed = int(par.ISEED) & 0xFFFFFFFF
+        t = time.perf_counter()
+        for k, ch in enumerate(gw.chunks()):
+            ref += O.galmod_wind(np.zeros_like(ref), gw.sr, int(ch[0]), int(ch[-1]) + 1,
+                                 (seed + 7919 * k) & 0xFFFFFFFF, gw.sep, gw.nv, st.cdens, 1, st.pixarea, st.cdelt[0],
+                                 st.cdelt[1], st.crota2, 0, 0, cube.DimX(), cube.DimY(), st.sig_instr, st.axtyp,
+                                 st.velsys, st.lfreq0, st.crval3, st.cdelt3, st.crpix3, st.relint, st.cd2i)
+        tc = time.perf_counter() - t
+        ref = ref.transpose(2, 0, 1)
+        out["cpu_baseline"] = {"value": 1. / tc, "unit": "models/s", "cores": 1, "kind": "port",
+                               "sample": "one model: the oracle's _galmod_wind over the 16 chunks"}
+        out["same_voxels"] = bool(np.array_equal(mod != 0, ref != 0))
+        out["max_rel_err"] = float(np.max(np.abs(mod - ref) / np.maximum(np.abs(ref), 1e-300)))
     return out
 
 

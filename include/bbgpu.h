@@ -18,6 +18,7 @@
  *   bbgpu_eval_*              <- LikelihoodMixin._log_likelihood(theta) for a batch of theta:
  *                                DiskModel.array -> convolve -> _calculate_residuals             bbarolo/bayesian/likelihood.py:567-619
  *   bbgpu_galmod_wind         <- _galmod_wind(out, sr, ring_lo, ring_hi, seed, sep, nv, ...)      bbarolo/galmod.py:539-542
+ *   bbgpu_galwind_spherical   <- GalWind._spherical(out): the chunks of shells and their seeds    bbarolo/galwind.py:301-331
  *   bbgpu_wind_points         <- _wind_points(cells, qn, qoff, radii, vw, vd, vr, ...)            bbarolo/windmodel.py:225-227
  *   bbgpu_wind_boxes          <- WindModel.boxes(p, lim, pts, weight): _raw_boxes, _deposit_raw,
  *                                _convolve_boxes                                                   bbarolo/windmodel.py:829-859
@@ -101,6 +102,12 @@ int bbgpu_galmod_mc(bbgpu_ctx *ctx, double *out, const double *sr, int nsub, int
  * bhi0-blo0, nz) float64 is ACCUMULATED. */
 int bbgpu_galmod_wind(bbgpu_ctx *ctx, double *out, const double *sr, int nsub, int ring_lo, int ring_hi,
                       uint64_t seed, double sep, const int64_t *nv, int blo0, int blo1, int bhi0, int bhi1);
+/* GalWind._spherical (bbarolo/galwind.py:301-331): the chunks [chunk_lo[c], chunk_hi[c]) of the shells, each with
+ * its own stream seeds[c], their streams parsed on up to `threads` host threads, all clouds deposited in one pass;
+ * out += the sum of the chunks' models (the fixed-point sums are exact: the same as adding them one by one). */
+int bbgpu_galwind_spherical(bbgpu_ctx *ctx, double *out, const double *sr, int nsub, int nchunks,
+                            const int *chunk_lo, const int *chunk_hi, const uint64_t *seeds, double sep,
+                            const int64_t *nv, int blo0, int blo1, int bhi0, int bhi1, int threads);
 int bbgpu_galmod_analytic(bbgpu_ctx *ctx, double *out, const double *sr, int nsub, int ring_lo, int ring_hi,
                           int nzq, int blo0, int blo1, int bhi0, int bhi1);
 /* out (nr, bhi1-blo1, bhi0-blo0) float64 accumulated; widx (nsub, 2) int64 (-1: none), wval (nsub, 2). */
