@@ -70,6 +70,7 @@ struct bbgpu_wind {
     int4 *d_qn = nullptr;
     long long *d_qoff = nullptr;
     int *d_pcell = nullptr;
+    int tabmax = 0;                     // the largest per-cell sample table of k_wind_points_cell (doubles)
     // points of the last bbgpu_wind_points / bbgpu_wind_set_points
     double *d_gx = nullptr, *d_gy = nullptr, *d_vel = nullptr, *d_sig = nullptr, *d_w = nullptr, *d_rr = nullptr;
     double *d_vol = nullptr, *d_rbar = nullptr, *d_weight = nullptr, *d_rad = nullptr;
@@ -196,6 +197,67 @@ __global__ void __launch_bounds__(256) k_wind_points(const double *__restrict__ 
     sig[i] = s;
     w[i] = __dmul_rn(__dmul_rn(r, r), st);
     rr[i] = r;
+}
+
+// The same points with one CTA per cell: the values that depend on the radial, polar or azimuthal sample alone
+// (radius, velocities and dispersion; sin and cos of theta; sin and cos of phi) computed once per sample into shared
+// memory, then combined per point with the same operations as k_wind_points (bit-identical results).
+__global__ void __launch_bounds__(256) k_wind_points_cell(const double *__restrict__ cells, const int4 *__restrict__ qn,
+                                                          const long long *__restrict__ qoff, WindParsDev p,
+                                                          const double *__restrict__ rad, WindGridDev g,
+                                                          double *__restrict__ gx, double *__restrict__ gy,
+                                                          double *__restrict__ vel, double *__restrict__ sig,
+                                                          double *__restrict__ w, double *__restrict__ rr) {
+    extern __shared__ double tab[];
+    const int k = blockIdx.x;
+    const double *c = cells + 7 * (size_t)k;
+    const long long i0 = qoff[k], i1 = qoff[k + 1];
+    double r0, r1, t0, t1;
+    if (!wclip(c, p, r0, r1, t0, t1)) {
+        for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+            gx[i] = -1e9; gy[i] = -1e9; vel[i] = 0.; sig[i] = 1.; w[i] = 0.; rr[i] = r0;
+        }
+        return;
+    }
+    const int4 q = qn[k];
+    double *tr = tab, *tvr = tab + q.x, *tds = tab + 2 * q.x, *tvo = tab + 3 * q.x, *tst = tab + 4 * q.x;
+    double *tct = tst + q.y, *tsp = tct + q.y, *tcp = tsp + q.z;
+    const double cs = c[0], p0 = c[5], p1 = c[6];
+    const double dr = __ddiv_rn(__dsub_rn(r1, r0), (double)q.x);
+    const double dt = __ddiv_rn(__dsub_rn(t1, t0), (double)q.y);
+    const double dp = __ddiv_rn(__dsub_rn(p1, p0), (double)q.z);
+    const int n = p.nrad;
+    for (int a = threadIdx.x; a < q.x; a += blockDim.x) {
+        const double r = __dadd_rn(r0, __dmul_rn(__dadd_rn((double)a, 0.5), dr));
+        tr[a] = r;
+        tvr[a] = __dmul_rn(winterp(r, rad, rad + n, n), 1000.);
+        const double disp = __dmul_rn(winterp(r, rad, rad + 2 * n, n), 1000.);
+        tvo[a] = __dmul_rn(winterp(r, rad, rad + 3 * n, n), 1000.);
+        tds[a] = __dsqrt_rn(__dadd_rn(__dmul_rn(disp, disp), __dmul_rn(g.sig_instr, g.sig_instr)));
+    }
+    for (int b = threadIdx.x; b < q.y; b += blockDim.x)
+        sincos(__dadd_rn(t0, __dmul_rn(__dadd_rn((double)b, 0.5), dt)), tst + b, tct + b);
+    for (int cc = threadIdx.x; cc < q.z; cc += blockDim.x)
+        sincos(__dadd_rn(p0, __dmul_rn(__dadd_rn((double)cc, 0.5), dp)), tsp + cc, tcp + cc);
+    __syncthreads();
+    const int tp = q.y * q.z;
+    for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const int j = (int)(i - i0);
+        const int a = j / tp, rem = j - a * tp;
+        const int b = rem / q.z, cc = rem - b * q.z;
+        const double r = tr[a], st = tst[b], ct = tct[b], sp = tsp[cc], cp = tcp[cc];
+        const double R = __dmul_rn(r, st);
+        const double z = __dmul_rn(__dmul_rn(cs, r), ct);
+        const double x = __dmul_rn(R, cp);
+        const double ys = __dsub_rn(__dmul_rn(__dmul_rn(R, sp), p.cinc), __dmul_rn(z, p.sinc));
+        gx[i] = __dadd_rn(p.x0, __ddiv_rn(__dsub_rn(__dmul_rn(x, p.spa), __dmul_rn(ys, p.cpa)), g.cd0));
+        gy[i] = __dadd_rn(p.y0, __ddiv_rn(__dadd_rn(__dmul_rn(x, p.cpa), __dmul_rn(ys, p.spa)), g.cd1));
+        const double geo = __dadd_rn(__dmul_rn(__dmul_rn(cs, ct), p.cinc), __dmul_rn(__dmul_rn(st, sp), p.sinc));
+        vel[i] = __dadd_rn(__dadd_rn(p.vsys, __dmul_rn(tvr[a], geo)), __dmul_rn(__dmul_rn(tvo[a], cp), p.sinc));
+        sig[i] = tds[a];
+        w[i] = __dmul_rn(__dmul_rn(r, r), st);
+        rr[i] = r;
+    }
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -832,7 +894,9 @@ extern "C" int bbgpu_wind_create(bbgpu_wind **out, int device, const bbgpu_wind_
         return BBGPU_ERR_NOMEM;
     }
     if (cudaFuncSetAttribute(k_wind_deposit_cell, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)(sizeof(unsigned long long) * WIND_SMEM_VALS)) != cudaSuccess) {
+                             (int)(sizeof(unsigned long long) * WIND_SMEM_VALS)) != cudaSuccess ||
+        cudaFuncSetAttribute(k_wind_points_cell, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(sizeof(double) * WIND_SMEM_VALS)) != cudaSuccess) {
         cudaGetLastError();
         bbgpu_wind_destroy(w);
         return BBGPU_ERR_CUDA;
@@ -933,6 +997,8 @@ extern "C" int bbgpu_wind_set_cells(bbgpu_wind *w, int ncell, const double *cell
     }
     w->ncell = ncell;
     w->npts = np;
+    w->tabmax = 0;
+    for (int k = 0; k < ncell; k++) w->tabmax = std::max(w->tabmax, 5 * q[k].x + 2 * q[k].y + 2 * q[k].z);
     w->h_rbox.assign(6 * (size_t)ncell, 0);
     w->h_box.assign(6 * (size_t)ncell, 0);
     w->h_offs.assign(ncell + 1, 0);
@@ -974,9 +1040,13 @@ extern "C" int bbgpu_wind_points(bbgpu_wind *w, const bbgpu_wind_pars *p, int nr
                                            w->s), "radii upload");
     if (rc) return rc;
     WindParsDev d{p->x0, p->y0, p->vsys, p->sinc, p->cinc, p->spa, p->cpa, p->th_in, p->th_out, p->rmax, nrad};
-    k_wind_points<<<grid_of(w->npts, 256), 256, 0, w->s>>>(w->d_cells, w->d_qn, w->d_qoff, w->d_pcell, w->npts, d,
-                                                            w->d_rad, w->g, w->d_gx, w->d_gy, w->d_vel, w->d_sig,
-                                                            w->d_w, w->d_rr);
+    if (w->tabmax <= WIND_SMEM_VALS)        // (the sample tables fit in shared memory: one CTA per cell)
+        k_wind_points_cell<<<w->ncell, 256, sizeof(double) * w->tabmax, w->s>>>(
+            w->d_cells, w->d_qn, w->d_qoff, d, w->d_rad, w->g, w->d_gx, w->d_gy, w->d_vel, w->d_sig, w->d_w, w->d_rr);
+    else
+        k_wind_points<<<grid_of(w->npts, 256), 256, 0, w->s>>>(w->d_cells, w->d_qn, w->d_qoff, w->d_pcell, w->npts,
+                                                                d, w->d_rad, w->g, w->d_gx, w->d_gy, w->d_vel,
+                                                                w->d_sig, w->d_w, w->d_rr);
     k_wind_cells<<<grid_of((long long)w->ncell * 32, 256), 256, 0, w->s>>>(w->d_cells, w->d_qoff, w->ncell, d, w->d_w,
                                                                           w->d_rr, w->d_vol, w->d_rbar);
     w->launches += 2;

@@ -138,3 +138,29 @@ def test_oracle_galmod_wind_matches_reference(oracle_lib, name):
     idx = np.flatnonzero(out)
     np.testing.assert_array_equal(idx, a["idx"])
     np.testing.assert_array_equal(out.ravel()[idx], a["val"])
+
+
+def test_host_wind_parameter_checks():
+    """The reference's refusals: opening angles out of order, a non-positive CONELEN, shells too close, bad cells."""
+    from bbarolo2_gb300.galmod import BBaroloError
+    from bbarolo2_gb300.galwind import GalWindPars, wind_setup, wind_shells
+    from bbarolo2_gb300.wind import WindCells, WindPars
+    with pytest.raises(BBaroloError):
+        WindPars([50.], 100., 10., openang=30., openin=40.).check()
+    with pytest.raises(BBaroloError):
+        WindPars([50.], 100., 10., conelen=-1.).check()
+    with pytest.raises(BBaroloError):
+        WindPars([50., 40.], 100., 10.)
+    with pytest.raises(BBaroloError):
+        WindPars([10., 50.], [100., 200., 300.], 10.)
+    for bad in (dict(redges=[0.]), dict(redges=[10., 5.]), dict(redges=[0., 10.], ntheta=0),
+                dict(redges=[0., 10.], thmax=95.), dict(redges=[0., 10.], cones=(2,))):
+        with pytest.raises(BBaroloError):
+            WindCells(**bad)
+    c = WC.GW_CASES["gw_velo"]
+    par = GalWindPars(**dict(c["par"], radii=[10., 10.5, 40.]))
+    with pytest.raises(BBaroloError):
+        wind_shells(par, wind_setup(WC.cube(**c["cube"]), par))
+    par = GalWindPars(**dict(c["par"], vdisp=-1.))
+    with pytest.raises(BBaroloError):
+        wind_shells(par, wind_setup(WC.cube(**c["cube"]), par))
