@@ -1971,14 +1971,16 @@ static int wind_mc_run(bbgpu_ctx *ctx, double *out, std::vector<WindClouds> &chu
     const int by = bhi1 - blo1, bx = bhi0 - blo0;
     const size_t n = (size_t)by * bx * ctx->g.nz;
     // the chunks' arrays go to the device at their offsets (shell indices and deviate offsets shifted)
-    size_t nsh = 0, ncl = 0, nnrm = 0;
+    size_t nsh = 0, ncl = 0, nhz = 0, nsl = 0;
     double total = 0.;
     for (WindClouds &c : chunks) {
         for (int &v : c.shell) v += (int)nsh;
-        for (long long &v : c.nbase) v += (long long)nnrm;
+        for (long long &v : c.nbase) v += (long long)nhz;
+        for (long long &v : c.sbase) v += (long long)nsl;
         nsh += c.shells.size();
         ncl += c.shell.size();
-        nnrm += c.normals.size();
+        nhz += c.hz.size();
+        nsl += c.slow.size();
         total += c.total;
     }
     if (ncl == 0) return BBGPU_OK;
@@ -1992,18 +1994,21 @@ static int wind_mc_run(bbgpu_ctx *ctx, double *out, std::vector<WindClouds> &chu
     frexp(bound * 1.0000001, &E);
     const double scale = ldexp(1.0, 62 - E), unit = ldexp(1.0, E - 62);
     WindShell *d_sh = nullptr;
-    int *d_shell = nullptr;
-    double *d_geo = nullptr, *d_nrm = nullptr;
-    long long *d_nb = nullptr;
+    int *d_shell = nullptr, *d_hz = nullptr;
+    double *d_geo = nullptr, *d_slow = nullptr;
+    long long *d_nb = nullptr, *d_sb = nullptr;
     unsigned long long *d_acc = nullptr;
     auto release = [&]() {
-        cudaFree(d_sh); cudaFree(d_shell); cudaFree(d_geo); cudaFree(d_nrm); cudaFree(d_nb); cudaFree(d_acc);
+        cudaFree(d_sh); cudaFree(d_shell); cudaFree(d_hz); cudaFree(d_geo); cudaFree(d_slow); cudaFree(d_nb);
+        cudaFree(d_sb); cudaFree(d_acc);
     };
     bool ok = cudaMalloc(&d_sh, sizeof(WindShell) * nsh) == cudaSuccess &&
               cudaMalloc(&d_shell, sizeof(int) * ncl) == cudaSuccess &&
               cudaMalloc(&d_geo, sizeof(double) * 5 * ncl) == cudaSuccess &&
-              cudaMalloc(&d_nrm, sizeof(double) * std::max<size_t>(nnrm, 1)) == cudaSuccess &&
+              cudaMalloc(&d_hz, sizeof(int) * std::max<size_t>(nhz, 1)) == cudaSuccess &&
+              cudaMalloc(&d_slow, sizeof(double) * std::max<size_t>(nsl, 1)) == cudaSuccess &&
               cudaMalloc(&d_nb, sizeof(long long) * ncl) == cudaSuccess &&
+              cudaMalloc(&d_sb, sizeof(long long) * ncl) == cudaSuccess &&
               cudaMalloc(&d_acc, sizeof(unsigned long long) * n) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
@@ -2012,7 +2017,7 @@ static int wind_mc_run(bbgpu_ctx *ctx, double *out, std::vector<WindClouds> &chu
     }
     cudaStream_t s = ctx->stream;
     ok = cudaMemsetAsync(d_acc, 0, sizeof(unsigned long long) * n, s) == cudaSuccess;
-    size_t o_sh = 0, o_cl = 0, o_n = 0;
+    size_t o_sh = 0, o_cl = 0, o_hz = 0, o_sl = 0;
     for (const WindClouds &c : chunks) {
         auto up = [&](void *dst, const void *src, size_t bytes) {
             return !bytes || cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s) == cudaSuccess;
@@ -2021,14 +2026,17 @@ static int wind_mc_run(bbgpu_ctx *ctx, double *out, std::vector<WindClouds> &chu
              up(d_shell + o_cl, c.shell.data(), sizeof(int) * c.shell.size()) &&
              up(d_geo + 5 * o_cl, c.geo.data(), sizeof(double) * c.geo.size()) &&
              up(d_nb + o_cl, c.nbase.data(), sizeof(long long) * c.nbase.size()) &&
-             up(d_nrm + o_n, c.normals.data(), sizeof(double) * c.normals.size());
+             up(d_sb + o_cl, c.sbase.data(), sizeof(long long) * c.sbase.size()) &&
+             up(d_hz + o_hz, c.hz.data(), sizeof(int) * c.hz.size()) &&
+             up(d_slow + o_sl, c.slow.data(), sizeof(double) * c.slow.size());
         o_sh += c.shells.size();
         o_cl += c.shell.size();
-        o_n += c.normals.size();
+        o_hz += c.hz.size();
+        o_sl += c.slow.size();
     }
     if (ok) {
-        launch_wind_mc(s, d_sh, d_shell, d_geo, d_nb, d_nrm, (long long)ncl, ctx->g, ctx->d_cd2i, blo0, blo1, bhi0,
-                       bhi1, scale, d_acc);
+        launch_wind_mc(s, d_sh, d_shell, d_geo, d_nb, d_sb, d_hz, d_slow, ctx->d_zig, (long long)ncl, ctx->g,
+                       ctx->d_cd2i, blo0, blo1, bhi0, bhi1, scale, d_acc);
         ctx->launches++;
         ok = cudaGetLastError() == cudaSuccess;
     }

@@ -179,19 +179,36 @@ uint64_t bbh_layout_key(uint64_t seed, int ltype, int nsub, const int *nc, const
 
 // Parses the stream of _galmod_wind (bbarolo/galmod.py:546-590): per shell its cloud count and constants (each
 // in the reference's float64 operation order, with the C library's sin and cos), per cloud the three uniforms
-// made into its radius, azimuth (cos, sin) and polar angle (sin, cos), and its velocity deviates.
+// made into its radius, azimuth (cos, sin) and polar angle (sin, cos), and its velocity deviates (the first word of
+// each, and the values of the rare ones that took the ziggurat's slow path).
 int bbh_wind_clouds(WindClouds *W, uint64_t seed, const double *sr, int nsub, int lo, int hi, double sep,
                     const int64_t *nv, const GridDev *g) {
     if (!W || !sr || !nv || lo < 0 || hi > nsub || lo > hi) return -1;
     *W = WindClouds();
     Stream st(seed);
     auto SRV = [&](int row, int ir) { return sr[(size_t)row * nsub + ir]; };
+    auto count = [&](int ir) {
+        return lround_ref(g->cdens * pow(SRV(4, ir), (double)g->cmode) * 2 * M_PI * SRV(0, ir) * sep / g->pixarea);
+    };
+    // (the arrays sized first: the clouds and deviates of every shell)
+    size_t ncl = 0, nnrm = 0;
+    for (int ir = lo; ir < hi; ir++) {
+        const int64_t nc = count(ir);
+        if (nc < 0 || nc > (1LL << 31) || nv[ir] < 1 || nv[ir] > (1 << 20)) return -2;
+        ncl += (size_t)nc;
+        nnrm += (size_t)nc * (size_t)nv[ir];
+    }
+    W->shell.resize(ncl);
+    W->geo.resize(5 * ncl);
+    W->nbase.resize(ncl);
+    W->sbase.resize(ncl);
+    W->hz.resize(nnrm);
+    W->slow.reserve(nnrm / 50 + 16);
+    size_t icl = 0, inr = 0;
     for (int ir = lo; ir < hi; ir++) {
         const double rtmp = SRV(0, ir);
-        const int64_t nc = lround_ref(g->cdens * pow(SRV(4, ir), (double)g->cmode) * 2 * M_PI * rtmp * sep /
-                                      g->pixarea);
+        const int64_t nc = count(ir);
         if (nc == 0) continue;
-        if (nc < 0 || nc > (1LL << 31) || nv[ir] < 1 || nv[ir] > (1 << 20)) return -2;
         WindShell s{};
         s.vrot = SRV(1, ir);
         s.vsph = SRV(2, ir);
@@ -210,16 +227,29 @@ int bbh_wind_clouds(WindClouds *W, uint64_t seed, const double *sr, int nsub, in
         const int si = (int)W->shells.size();
         W->shells.push_back(s);
         const double r_in2 = pow(rtmp - 0.5 * sep, 2.0);
-        for (int64_t ic = 0; ic < nc; ic++) {
+        int *shp = W->shell.data();
+        double *geo = W->geo.data();
+        int32_t *hz = W->hz.data();
+        long long *nb = W->nbase.data(), *sb = W->sbase.data();
+        for (int64_t ic = 0; ic < nc; ic++, icl++) {
             const double rad = sqrt(r_in2 + 2 * sep * rtmp * fabs(2.0 * st.uniform() - 1.0));
             const double az = 2 * M_PI * fabs(2.0 * st.uniform() - 1.0);
             double ph = opentmp * fabs(2.0 * st.uniform() - 1.0);
             if (ic % 2 == 0) ph = M_PI - ph;
-            W->shell.push_back(si);
-            const double geo[5] = {rad, cos(az), sin(az), sin(ph), cos(ph)};
-            W->geo.insert(W->geo.end(), geo, geo + 5);
-            W->nbase.push_back((long long)W->normals.size());
-            for (int iv = 0; iv < s.nvr; iv++) W->normals.push_back(st.normal());
+            shp[icl] = si;
+            double *gc = geo + 5 * icl;
+            gc[0] = rad;
+            gc[1] = cos(az);
+            gc[2] = sin(az);
+            gc[3] = sin(ph);
+            gc[4] = cos(ph);
+            nb[icl] = (long long)inr;
+            sb[icl] = (long long)W->slow.size();
+            for (int iv = 0; iv < s.nvr; iv++) {
+                bool slow;
+                const double v = st.normal(hz + inr++, &slow);
+                if (slow) W->slow.push_back(v);
+            }
         }
         W->total += (double)nc * s.nvr * fabs(s.fluxsc);
     }

@@ -103,8 +103,10 @@ struct WindClouds {
     std::vector<WindShell> shells;
     std::vector<int> shell;             // per cloud: its shell (index into shells)
     std::vector<double> geo;            // per cloud: rad, cos az, sin az, sin ph, cos ph
-    std::vector<long long> nbase;       // per cloud: its first velocity deviate in normals
-    std::vector<double> normals;        // the velocity deviates of the clouds, in stream order
+    std::vector<long long> nbase;       // per cloud: its first velocity deviate in hz
+    std::vector<long long> sbase;       // per cloud: its first deviate in slow
+    std::vector<int32_t> hz;            // the velocity deviates in stream order: the first word of each ziggurat
+    std::vector<double> slow;           // the values of the deviates that left the ziggurat's one-word path
     double total = 0.;                  // sum over the clouds of nvr x fluxsc
 };
 #endif

@@ -278,6 +278,6 @@ void launch_fill_copy(cudaStream_t s, void *base, size_t elt_bytes, int nsub, in
 
 // GALWIND WTYPE 1 (galwind.cu): one thread per cloud; acc (by, bx, nz) of 64-bit fixed-point sums (units 1/scale)
 void launch_wind_mc(cudaStream_t st, const WindShell *shells, const int *shell, const double *geo,
-                    const long long *nbase, const double *normals, long long ncloud, const GridDev &g,
-                    const double *cd2i, int blo0, int blo1, int bhi0, int bhi1, double scale,
-                    unsigned long long *acc);
+                    const long long *nbase, const long long *sbase, const int *hz, const double *slow,
+                    const ZigDev *zig, long long ncloud, const GridDev &g, const double *cd2i, int blo0, int blo1,
+                    int bhi0, int bhi1, double scale, unsigned long long *acc);
