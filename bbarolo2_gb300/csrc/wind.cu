@@ -1160,6 +1160,10 @@ extern "C" int bbgpu_wind_boxes(bbgpu_wind *w, const int64_t *lim, const double 
         long long big = 0;
         for (int k = 0; k < n; k++) big = std::max(big, w->h_roffs[k + 1] - w->h_roffs[k]);
         const long long maxvals = std::min(big, (long long)WIND_SMEM_VALS);
+        if (big > maxvals) {        // (the global path accumulates: its boxes start at zero; the others are written)
+            rc = cuda_check(w, cudaMemsetAsync(w->d_rbuf, 0, sizeof(double) * rtot, w->s), "memset");
+            if (rc) return rc;
+        }
         if (maxvals > 0) {
             k_wind_deposit_cell<<<n, 512, sizeof(unsigned long long) * maxvals, w->s>>>(
                 w->d_qoff, w->d_gx, w->d_gy, w->d_vel, w->d_sig, w->d_w, wt, w->d_rbox, w->d_roffs, w->d_vedges,
@@ -1167,8 +1171,6 @@ extern "C" int bbgpu_wind_boxes(bbgpu_wind *w, const int64_t *lim, const double 
             w->launches++;
         }
         if (big > maxvals) {
-            rc = cuda_check(w, cudaMemsetAsync(w->d_rbuf, 0, sizeof(double) * rtot, w->s), "memset");
-            if (rc) return rc;
             k_wind_deposit<<<grid_of(w->npts * 32, 256), 256, 0, w->s>>>(w->d_pcell, w->npts, w->d_gx, w->d_gy,
                                                                          w->d_vel, w->d_sig, w->d_w, wt, w->d_rbox,
                                                                          w->d_roffs, w->d_vedges, w->d_ptab, w->g,

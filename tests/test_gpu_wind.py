@@ -133,3 +133,35 @@ def test_wind_large_vs_oracle(gpu_lib, oracle_lib, size):
     print(f"{wm.cells.ncell} cells, {wm.cells.npoints} points, {B.total} column values")
     _close(G, Go, 1e-11, "G")
     _close(b, bo, 1e-11, "b")
+
+
+def test_wind_cells_with_large_raw_boxes(gpu_lib, oracle_lib):
+    """Cells whose raw boxes exceed the shared-memory deposit (more than 26,624 values: float64 atomics in global
+    memory) beside small ones, on one cube: the columns and normal equations against the oracle."""
+    import math
+    from bbarolo2_gb300 import wind
+    cube = WC.cube(96, 60, beam=(30.,))
+    wm = wind.WindModel(cube, wind.WindCells([0., 30., 60., 450.], 1, 1, thmax=50.)).quadrature(250., 10.)
+    P = wind.WindPars([100.], 220., 10., vrot=30., xpos=47.5, ypos=48.2, inc=55., pa=20., openang=90., conelen=430.)
+    pts = wm.points(P)
+    B = wm.boxes(P, pts=pts)
+    su = wm.setup
+    hx, hy = wm.hx, wm.hy
+    lim = np.array([0, 96, 0, 96, 0, 60])
+    rb = oracle_lib.wind_raw_boxes(wm.cells.qoff, pts["gx"], pts["gy"], pts["vel"], pts["sig"], pts["w"],
+                                   lim + np.array([-hx, hx, -hy, hy, 0, 0]), su._chmin, su.axtyp, su.velsys,
+                                   su.lfreq0, su.crval3, su.cdelt3, su.crpix3)
+    size = (rb[:, 1] - rb[:, 0]) * (rb[:, 3] - rb[:, 2]) * (rb[:, 5] - rb[:, 4])
+    assert size.max() > 26624 and np.any((size > 0) & (size < 26624)), size
+    spec = dict(chmin=su._chmin, axtyp=su.axtyp, velsys=su.velsys, lfreq0=su.lfreq0, crval3=su.crval3,
+                cdelt3=su.cdelt3, crpix3=su.crpix3)
+    buf, offs, boxes = oracle_lib.wind_boxes(pts, pts["w"], lim, wm.shape, wm.kern, wm.kx, wm.ky, wm.separable, spec,
+                                             su._vedges_lines, su.relint, wm.cells.qoff)
+    np.testing.assert_array_equal(B.boxes, boxes)
+    _close(B.buf, buf, what="columns")
+    W, d, Wd = WC.weights("sep", wm.shape)
+    G, b = B.normal(Wd, W)
+    Go, bo = oracle_lib.wind_normal(B.buf, B.offs, B.boxes, Wd, W, B.lim(), 0.)
+    _close(G, Go, 1e-11, "G")
+    _close(b, bo, 1e-11, "b")
+    assert math.isfinite(float(G.sum()))
