@@ -1055,8 +1055,7 @@ extern "C" int bbgpu_wind_points(bbgpu_wind *w, const bbgpu_wind_pars *p, int nr
     // the rad upload reads a host vector that goes out of scope: wait for it before returning
     rc = cuda_check(w, cudaStreamSynchronize(w->s), "points");
     if (rc) return rc;
-    w->have_points = true;
-    w->have_boxes = false;
+    w->have_points = true;               // (the columns of the last bbgpu_wind_boxes stay valid)
     if (gx || gy || vel || sig || wt || r || vol || rbar) return download_points(w, gx, gy, vel, sig, wt, r, vol, rbar);
     return BBGPU_OK;
 }
@@ -1075,8 +1074,7 @@ extern "C" int bbgpu_wind_set_points(bbgpu_wind *w, const double *gx, const doub
     }
     int rc = cuda_check(w, cudaStreamSynchronize(w->s), "points upload");
     if (rc) return rc;
-    w->have_points = true;
-    w->have_boxes = false;
+    w->have_points = true;               // (the columns of the last bbgpu_wind_boxes stay valid)
     return BBGPU_OK;
 }
 
@@ -1088,6 +1086,7 @@ extern "C" int bbgpu_wind_boxes(bbgpu_wind *w, const int64_t *lim, const double 
         lim[1] > w->g.nx || lim[3] > w->g.ny || lim[5] > w->g.nz)
         return fail(w, BBGPU_ERR_ARG, "lim must lie within the cube");
     cudaSetDevice(w->device);
+    w->have_boxes = false;                  // (until these columns are complete)
     const int n = w->ncell, hx = w->hx, hy = w->hy;
     int rc;
     const double *wt = nullptr;

@@ -165,3 +165,19 @@ def test_wind_cells_with_large_raw_boxes(gpu_lib, oracle_lib):
     _close(G, Go, 1e-11, "G")
     _close(b, bo, 1e-11, "b")
     assert math.isfinite(float(G.sum()))
+
+
+def test_wind_columns_survive_a_points_call(gpu_lib):
+    """The columns of a boxes() call stay usable after the points of another wind are computed."""
+    wm, P = _model("sep")
+    B = wm.boxes(P)
+    m1 = B.model(np.ones(B.n), wm.shape)
+    wm.points(WindParsShift(P))
+    # (the model's sums of overlapping columns are float64 atomics: equal to rounding)
+    np.testing.assert_allclose(B.model(np.ones(B.n), wm.shape), m1, rtol=1e-13, atol=1e-15 * np.abs(m1).max())
+
+
+def WindParsShift(P):
+    q = P.copy()
+    q.inc += 5.
+    return q
