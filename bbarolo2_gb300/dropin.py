@@ -14,10 +14,16 @@ here                   reference                                           side 
 ``sumsq_residuals``    ``bbarolo/bayesian/likelihood.py:22``                returns the sum of squares
 ``residuals_fracerr``  ``bbarolo/bayesian/likelihood.py:48``                returns (sum r^2 / v, sum log(v / s^2))
 ``FFTConvolver_call``  ``bbarolo/smooth.py:145`` ``FFTConvolver.__call__``  the "same" convolution of the planes
+``galmod_wind``        ``bbarolo/galmod.py:539`` ``_galmod_wind``           out (by, bx, nz) += the wind's clouds
 =====================  ==================================================  ==========================================
 
+and the classes of the wind models (``bbarolo/windmodel.py``: ``WindModel``, ``WindCells``, ``WindPars``,
+``Boxes``) by those of ``bbarolo2_gb300.wind``, in ``bbarolo.windmodel`` and in ``bbarolo.bayesian.wind`` (which
+imports them by name), so that WINDFIT's likelihood builds its columns and normal equations on the device.
+
 ``install()`` binds them in place of the reference's functions in its modules (``bbarolo.galmod``,
-``bbarolo.galfit``, ``bbarolo.bayesian.likelihood``, ``bbarolo.smooth``), so that ``GalmodSetup._build``,
+``bbarolo.galfit``, ``bbarolo.bayesian.likelihood``, ``bbarolo.smooth``, ``bbarolo.galwind``, which imports
+``_galmod_wind`` by name), so that ``GalmodSetup._build``,
 ``DiskModel.array/convolve/ring_maps``, ``Galfit._norm_value`` and ``LikelihoodMixin._calculate_residuals`` take
 the device path unchanged; ``uninstall()`` restores them. The device contexts are cached by the scalars of the grid
 each call passes (one context per distinct grid, one per host thread).
@@ -122,6 +128,22 @@ def ring_maps_analytic(out, sr, widx, wval, radsep, pixarea, cdelt0, cdelt1, cro
     return out
 
 
+def galmod_wind(out, sr, ring_lo, ring_hi, seed, sep, nv, cdens, cmode, pixarea, cdelt0, cdelt1, crota2, blo0, blo1,
+                bhi0, bhi1, sig_instr, axtyp, velsys, lfreq0, crval3, cdelt3, crpix3, relint, cd2i):
+    """``_galmod_wind`` on the device (GALWIND WTYPE 1): out (bhi1 - blo1, bhi0 - blo0, nz) += the clouds of the
+    shells [ring_lo, ring_hi) of sr (11, nsub)."""
+    _out64(out)
+    nz = out.shape[2]
+    c = _grid_ctx(bhi0, bhi1, nz, sep, cdens, cmode, pixarea, cdelt0, cdelt1, crota2, 1, sig_instr, axtyp, velsys,
+                  lfreq0, crval3, cdelt3, crpix3, relint, cd2i)
+    sr = np.ascontiguousarray(sr, np.float64)
+    nv = np.ascontiguousarray(nv, np.int64)
+    c.check(c.L.bbgpu_galmod_wind(c.h, _lib.ptr(out), _lib.ptr(sr), sr.shape[1], int(ring_lo), int(ring_hi),
+                                  int(seed) & 0xFFFFFFFFFFFFFFFF, float(sep), _lib.ptr(nv), int(blo0), int(blo1),
+                                  int(bhi0), int(bhi1)))
+    return out
+
+
 def _plain_ctx():
     d = _ctxs()
     c = d.get("plain")
@@ -203,7 +225,17 @@ SEAMS = (("bbarolo.galmod", "_galmod_mc", galmod_mc),
          ("bbarolo.galmod", "_conv_sparse", conv_sparse),
          ("bbarolo.galfit", "_norm", norm),
          ("bbarolo.bayesian.likelihood", "_sumsq_residuals", sumsq_residuals),
-         ("bbarolo.bayesian.likelihood", "_residuals_fracerr", residuals_fracerr))
+         ("bbarolo.bayesian.likelihood", "_residuals_fracerr", residuals_fracerr),
+         ("bbarolo.galmod", "_galmod_wind", galmod_wind),
+         ("bbarolo.galwind", "_galmod_wind", galmod_wind))
+
+
+def _wind_classes():
+    from . import wind
+    return {"WindModel": wind.WindModel, "WindCells": wind.WindCells, "WindPars": wind.WindPars, "Boxes": wind.Boxes}
+
+
+WIND_MODULES = ("bbarolo.windmodel", "bbarolo.bayesian.wind")
 
 _saved = {}
 
@@ -226,6 +258,15 @@ def install(modules=None):
         _saved.setdefault(("bbarolo.smooth", "FFTConvolver.__call__"), cls.__call__)
         cls.__call__ = FFTConvolver_call
         done.append(("bbarolo.smooth", "FFTConvolver.__call__"))
+    for mname in WIND_MODULES:
+        m = mods.get(mname)
+        if m is None:
+            continue
+        for attr, cls in _wind_classes().items():
+            if hasattr(m, attr):
+                _saved.setdefault((mname, attr), getattr(m, attr))
+                setattr(m, attr, cls)
+                done.append((mname, attr))
     return done
 
 

@@ -22,9 +22,13 @@ def _fake_modules():
         def __call__(self, data, workers=None):
             return "reference"
     mods = {}
-    for name, attrs in (("bbarolo.galmod", ("_galmod_mc", "_galmod_analytic", "_ring_maps_analytic", "_conv_sparse")),
+    for name, attrs in (("bbarolo.galmod", ("_galmod_mc", "_galmod_analytic", "_ring_maps_analytic", "_conv_sparse",
+                                            "_galmod_wind")),
                         ("bbarolo.galfit", ("_norm",)),
-                        ("bbarolo.bayesian.likelihood", ("_sumsq_residuals", "_residuals_fracerr"))):
+                        ("bbarolo.bayesian.likelihood", ("_sumsq_residuals", "_residuals_fracerr")),
+                        ("bbarolo.galwind", ("_galmod_wind",)),
+                        ("bbarolo.windmodel", ("WindModel", "WindCells", "WindPars", "Boxes")),
+                        ("bbarolo.bayesian.wind", ("WindModel", "WindCells", "WindPars", "Boxes"))):
         m = types.ModuleType(name)
         for a in attrs:
             setattr(m, a, f)
@@ -39,14 +43,19 @@ def test_install_and_uninstall_swap_the_seams():
     from bbarolo2_gb300 import dropin
     mods, f, call = _fake_modules()
     done = dropin.install(mods)
-    assert len(done) == len(dropin.SEAMS) + 1
+    assert len(done) == len(dropin.SEAMS) + 1 + 8
     for mname, attr, fn in dropin.SEAMS:
         assert getattr(mods[mname], attr) is fn
     assert mods["bbarolo.smooth"].FFTConvolver.__call__ is dropin.FFTConvolver_call
+    from bbarolo2_gb300 import wind
+    for mname in dropin.WIND_MODULES:
+        assert mods[mname].WindModel is wind.WindModel and mods[mname].Boxes is wind.Boxes
     dropin.uninstall(mods)
     for mname, attr, fn in dropin.SEAMS:
         assert getattr(mods[mname], attr) is f
     assert mods["bbarolo.smooth"].FFTConvolver.__call__ is call
+    for mname in dropin.WIND_MODULES:
+        assert mods[mname].WindModel is f
 
 
 def test_install_skips_missing_modules():
@@ -87,6 +96,21 @@ def test_dropin_kernels_with_reference_arguments(gpu_lib):
     z = G.load("classic.npz")
     assert np.array_equal(dropin.conv_sparse(z["conv_sparse/model"], z["conv_sparse/kernel"], 2.5),
                           z["conv_sparse/out_scaled"])
+    # _galmod_wind with the reference's arguments (the chunks of a GALWIND fixture, summed in chunk order)
+    z, idx = G.cases("wind.npz")
+    for nm in ("gw_velo", "gw_radii_freq"):
+        m = idx[nm]
+        (b0, b1), (e0, e1) = m["box"]
+        out = np.zeros(m["shape"])
+        for t, (lo, hi) in enumerate(z[nm + "/chunks"]):
+            buf = dropin.galmod_wind(np.zeros(m["shape"]), z[nm + "/sr"], int(lo), int(hi),
+                                     (m["seed"] + 7919 * t) & 0xFFFFFFFF, m["sep"], z[nm + "/nv"], m["cdens"], 1,
+                                     m["pixarea"], m["cdelt0"], m["cdelt1"], m["crota2"], b0, b1, e0, e1,
+                                     m["sig_instr"], m["axtyp"], m["velsys"], z[nm + "/lfreq0"], m["crval3"],
+                                     m["cdelt3"], m["crpix3"], z[nm + "/relint"], z[nm + "/cd2i"])
+            out += buf
+        ref = G.dense(z[nm + "/idx"], z[nm + "/val"], m["shape"])
+        np.testing.assert_allclose(out, ref, rtol=1e-12, atol=0)
 
 
 @pytest.mark.gpu
