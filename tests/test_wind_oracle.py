@@ -164,3 +164,16 @@ def test_host_wind_parameter_checks():
     par = GalWindPars(**dict(c["par"], vdisp=-1.))
     with pytest.raises(BBaroloError):
         wind_shells(par, wind_setup(WC.cube(**c["cube"]), par))
+
+
+def test_circinus_workload_shapes():
+    """The bench's WINDFIT problem has the shapes of the reference's Circinus example (docs/examples/circinus.md:
+    3192 cells of 3.6 arcsec on the approaching cone of OPENANG 110 and CONELEN 52 arcsec, 173 x 238 x 41 voxels,
+    0.9 arcsec beam), with the quadrature capped at MAX_POINTS."""
+    from bbarolo2_gb300 import configs, wind
+    wm, p = configs.wind_circinus()
+    assert wm.cells.ncell == 3192
+    assert wm.shape == (41, 238, 173)
+    assert 0 < wm.cells.npoints <= wind.MAX_POINTS
+    assert set(wm.cells.cells[:, 0]) == {-1.0}
+    assert wm.separable and wm.hx == wm.hy
